@@ -1,0 +1,164 @@
+/* lvbgs.h -- C-ABI of the GB300 (sm_103a) SuBSENSE background subtractor.
+ *
+ * This is the boundary a C++ IBackgroundSubtractor_<lv::CUDA> specialisation (or any FFI)
+ * binds to. It replaces the missing CUDA implementation slot of the reference,
+ * modules/video/include/litiv/video/BackgroundSubtractionUtils.hpp:136-138
+ * ("IBackgroundSubtractor_<lv::CUDA> will not compile here, missing impl") and
+ * BackgroundSubtractorLBSP.hpp:77-80 (static_assert(eImpl!=lv::CUDA,"Missing impl")).
+ *
+ * Conventions: plain pointers and sizes; every call returns an lvbgs_status; the last
+ * error message of a handle is available through lvbgs_last_error(). The caller owns all
+ * image and mask buffers; a handle owns its model state, which stays resident in device
+ * memory between frames. A handle is single-writer (like a reference instance, which is
+ * not thread-safe); different handles may be driven from different host threads.
+ * Images are 8-bit, 1 or 3 interleaved channels (BGR order is irrelevant to the method),
+ * rows `stride` bytes apart. Masks are 8-bit, width*height bytes, 0 or 255.
+ * Image and mask pointers may be host (pageable or pinned) or device memory; the library
+ * detects which with cudaPointerGetAttributes.
+ */
+#ifndef LVBGS_H
+#define LVBGS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    LVBGS_OK = 0,
+    LVBGS_BAD_ARG = 1,         /* null pointer, bad parameter value (lvAssert_ in the reference) */
+    LVBGS_BAD_SIZE = 2,        /* size mismatch with the initialization frame */
+    LVBGS_BAD_TYPE = 3,        /* unsupported channel count / type */
+    LVBGS_NOT_INITIALIZED = 4, /* apply() before initialize() */
+    LVBGS_OOM = 5,             /* device allocation failed */
+    LVBGS_DEVICE_TIMEOUT = 6,  /* a bounded device-side wait gave up (kernel returned an error status) */
+    LVBGS_DEVICE_ERROR = 7,    /* CUDA runtime error, or no usable sm_103 device */
+    LVBGS_UNSUPPORTED = 8      /* configuration outside what this implementation covers */
+} lvbgs_status;
+
+typedef enum { LVBGS_ALGO_SUBSENSE = 0, LVBGS_ALGO_PAWCS = 1 } lvbgs_algo;
+
+typedef struct lvbgs_ctx* lvbgs_handle;
+
+/* Constructor parameters of BackgroundSubtractorSuBSENSE_ (BackgroundSubtractorSuBSENSE.hpp:52-57,
+ * defaults :22-31) and of IBackgroundSubtractorLBSP_ (BackgroundSubtractorLBSP.hpp:46-55, defaults
+ * :23-28), plus the seed of the counter-based generator that replaces rand(). */
+typedef struct {
+    size_t desc_dist_threshold_offset;   /* 3 */
+    size_t min_color_dist_threshold;     /* 30 */
+    size_t bg_samples;                   /* 50 (this implementation supports 1..64) */
+    size_t required_bg_samples;          /* 2 */
+    size_t samples_for_moving_avgs;      /* 100 */
+    float rel_lbsp_threshold;            /* 0.333f */
+    size_t lbsp_threshold_offset;        /* 0 */
+    int default_median_blur_kernel_size; /* 9 */
+    uint64_t seed;                       /* generator key; streams with different seeds draw independently */
+    int device_id;                       /* CUDA device (IParallelAlgo_<CUDA>(bInitUseCUDA, nDeviceID), algo.hpp:82-129) */
+} lvbgs_params;
+
+/* one stream's frame in a batched call */
+typedef struct {
+    const uint8_t* image; /* width*height*channels bytes, rows `stride` bytes apart (0 = dense) */
+    size_t stride;
+    uint8_t* fgmask;      /* output, width*height bytes, may be NULL */
+    double learning_rate; /* apply()'s learningRateOverride: <=0 uses the internal T(x) (default 0) */
+} lvbgs_frame;
+
+/* fills the reference defaults (BackgroundSubtractorSuBSENSE.hpp:22-31) */
+lvbgs_status lvbgs_default_params(lvbgs_algo algo, lvbgs_params* out);
+
+/* BackgroundSubtractorSuBSENSE_ constructor (BackgroundSubtractorSuBSENSE.cpp:62-78): checks the
+ * parameters (required samples <= samples, one positive threshold, non-negative LBSP threshold)
+ * and selects the CUDA device (lv::cuda::init, utils/src/cuda.cpp:18-75). */
+lvbgs_status lvbgs_create(lvbgs_algo algo, const lvbgs_params* params, lvbgs_handle* out);
+lvbgs_status lvbgs_destroy(lvbgs_handle h);
+
+/* IIBackgroundSubtractor::initialize(img, roi) (BackgroundSubtractionUtils.hpp:29-31,
+ * BackgroundSubtractorSuBSENSE.cpp:107-186). roi is NULL (whole frame) or width*height bytes of
+ * 0/255 values. Allocates the device model and builds it from the frame (refreshModel(1.0)). */
+lvbgs_status lvbgs_initialize(lvbgs_handle h, const uint8_t* image, int width, int height, int channels,
+                              size_t stride, const uint8_t* roi);
+
+/* IIBackgroundSubtractor::apply(img, fgmask, learningRateOverride) (BackgroundSubtractorSuBSENSE.cpp:188-612).
+ * Enqueues the frame step on `cuda_stream` (a cudaStream_t, NULL = the per-handle stream) and
+ * waits for it; fgmask receives the post-processed foreground mask. */
+lvbgs_status lvbgs_apply(lvbgs_handle h, const uint8_t* image, size_t stride, uint8_t* fgmask,
+                         double learning_rate, void* cuda_stream);
+
+/* Batched frame step: one persistent launch processes one frame of each of the n streams
+ * (handles on the same device, all initialized). Results are identical to n separate
+ * lvbgs_apply calls. Enqueued on cuda_stream; lvbgs_batch_wait() waits and reports device errors.
+ * Host buffers referenced by `frames` must stay valid until the wait returns. */
+lvbgs_status lvbgs_batch_apply(const lvbgs_handle* handles, const lvbgs_frame* frames, int n, void* cuda_stream);
+lvbgs_status lvbgs_batch_wait(const lvbgs_handle* handles, int n, void* cuda_stream);
+
+/* getBackgroundImage (BackgroundSubtractorSuBSENSE.cpp:614-630): width*height*channels bytes */
+lvbgs_status lvbgs_get_background(lvbgs_handle h, uint8_t* out);
+/* getBackgroundDescriptorsImage (BackgroundSubtractorSuBSENSE.cpp:632-649): width*height*channels uint16 */
+lvbgs_status lvbgs_get_background_descriptors(lvbgs_handle h, uint16_t* out);
+/* refreshModel(fSamplesRefreshFrac, bForceFGUpdate) (BackgroundSubtractorSuBSENSE.cpp:80-105) */
+lvbgs_status lvbgs_refresh_model(lvbgs_handle h, float fraction, int force_fg_update);
+/* setAutomaticModelReset (BackgroundSubtractionUtils.cpp:24-26) */
+lvbgs_status lvbgs_set_automatic_model_reset(lvbgs_handle h, int enabled);
+/* getDefaultLearningRate (BackgroundSubtractorSuBSENSE.hpp:69): always 0 */
+double lvbgs_get_default_learning_rate(lvbgs_handle h);
+/* getROICopy (BackgroundSubtractionUtils.cpp:50-52): the validated ROI, width*height bytes */
+lvbgs_status lvbgs_get_roi(lvbgs_handle h, uint8_t* out);
+
+/* sizes of an initialized handle */
+lvbgs_status lvbgs_get_size(lvbgs_handle h, int* width, int* height, int* channels);
+/* device bytes of the model state of a width x height x channels SuBSENSE stream (admission control) */
+size_t lvbgs_state_bytes(lvbgs_algo algo, int width, int height, int channels, size_t bg_samples);
+
+/* Moves a stream's whole device state to `host_buffer` (lvbgs_state_bytes() bytes, pinned memory
+ * recommended) and frees the device model; lvbgs_restore() uploads it again. The model evolves
+ * bit-identically across a spill/restore pair. */
+lvbgs_status lvbgs_spill(lvbgs_handle h, void* host_buffer, size_t bytes);
+lvbgs_status lvbgs_restore(lvbgs_handle h, const void* host_buffer, size_t bytes);
+
+/* LBSP::compute2 dense descriptor extraction on the device (modules/features2d/src/LBSP.cpp:102-152,
+ * LBSP.hpp:70-77). abs_threshold >= 0 selects LBSP(size_t) (absolute threshold), otherwise
+ * LBSP(rel_threshold, offset). desc: width*height*channels uint16; the 2-pixel border is left as is. */
+lvbgs_status lvbgs_lbsp_compute2(const uint8_t* image, int width, int height, int channels, long abs_threshold,
+                                 float rel_threshold, size_t offset, uint16_t* desc, int device_id);
+
+/* last error message of a handle (or of the library when h is NULL) */
+const char* lvbgs_last_error(lvbgs_handle h);
+
+/* ---- inspection (parity tests and tools): model state in the reference's layout ----
+ * `which` takes the map ids below; the layout is the reference's: one full-frame map per
+ * quantity, interleaved channels, and N sample images for the sample maps. */
+enum {
+    LVBGS_MAP_R = 0, LVBGS_MAP_V, LVBGS_MAP_T, LVBGS_MAP_DLAST, LVBGS_MAP_DMIN_LT, LVBGS_MAP_DMIN_ST,
+    LVBGS_MAP_RAW_LT, LVBGS_MAP_RAW_ST, LVBGS_MAP_FIN_LT, LVBGS_MAP_FIN_ST, /* float [H*W] */
+    LVBGS_MAP_UNSTABLE, LVBGS_MAP_BLINKS, LVBGS_MAP_LAST_RAW_FG, LVBGS_MAP_LAST_FG,
+    LVBGS_MAP_LAST_FG_DIL_INV, LVBGS_MAP_LAST_RAW_BLINK, LVBGS_MAP_ROI,     /* uint8 [H*W] */
+    LVBGS_MAP_LAST_COLOR,                                                    /* uint8 [H*W*C] */
+    LVBGS_MAP_LAST_DESC,                                                     /* uint16 [H*W*C] */
+    LVBGS_MAP_SAMPLE_COLOR,                                                  /* uint8 [N][H*W*C] */
+    LVBGS_MAP_SAMPLE_DESC,                                                   /* uint16 [N][H*W*C] */
+    LVBGS_MAP_DS_LT, LVBGS_MAP_DS_ST,                                        /* float [H/8*W/8*C] */
+    LVBGS_MAP_LUT,                                                           /* uint8 [256] */
+    LVBGS_MAP_COUNT
+};
+lvbgs_status lvbgs_debug_map_bytes(lvbgs_handle h, int which, size_t* bytes);
+lvbgs_status lvbgs_debug_get_map(lvbgs_handle h, int which, void* out, size_t bytes);
+
+/* frame-level scalars of a stream */
+typedef struct {
+    uint64_t frame_idx, frames_since_last_reset, model_reset_cooldown;
+    int32_t auto_model_reset_enabled, learning_rate_scaling_enabled, use_3x3_spread, median_blur_kernel_size;
+    float lr_lower_cap, lr_upper_cap, last_nonzero_desc_ratio;
+    uint64_t nonzero_desc_count, tot_color_diff;
+    uint64_t n_relevant_px, orig_roi_px;
+    uint64_t stat_samples_evaluated, stat_sample_writes; /* cumulative, for the algorithmic-byte count */
+    uint64_t stat_repair_rounds, stat_repair_rematched;  /* cumulative raster-order repair work */
+} lvbgs_scalars;
+lvbgs_status lvbgs_get_scalars(lvbgs_handle h, lvbgs_scalars* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LVBGS_H */

@@ -1,0 +1,8 @@
+"""GB300 (sm_103a) SuBSENSE background subtraction with LITIV's interface.
+
+The compute path is the in-tree CUDA library ``_build/liblvbgs.so`` (C-ABI in include/lvbgs.h);
+this package is its host-side mirror of the reference's BackgroundSubtractorSuBSENSE interface.
+"""
+from .bgs import BackgroundSubtractorSuBSENSE, LvException, batch_apply, lbsp_compute2  # noqa: F401
+from .synth import SyntheticStream  # noqa: F401
+from . import _lib  # noqa: F401

@@ -1,0 +1,109 @@
+"""ctypes binding of ``liblvbgs.so`` (the C-ABI declared in include/lvbgs.h and lvbgs_synth.h).
+
+The library is the only compute path: there is no CPU fallback. Loading fails loudly when the
+in-tree build is missing (build it with ``python -m litiv_gb300.build`` or
+``__graft_entry__.build()``).
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liblvbgs.so")
+
+# lvbgs_status
+OK, BAD_ARG, BAD_SIZE, BAD_TYPE, NOT_INITIALIZED, OOM, DEVICE_TIMEOUT, DEVICE_ERROR, UNSUPPORTED = range(9)
+STATUS_NAMES = ["OK", "BAD_ARG", "BAD_SIZE", "BAD_TYPE", "NOT_INITIALIZED", "OOM", "DEVICE_TIMEOUT",
+                "DEVICE_ERROR", "UNSUPPORTED"]
+ALGO_SUBSENSE, ALGO_PAWCS = 0, 1
+
+# map ids (LVBGS_MAP_*)
+MAP_NAMES = ["R", "V", "T", "DLAST", "DMIN_LT", "DMIN_ST", "RAW_LT", "RAW_ST", "FIN_LT", "FIN_ST",
+             "UNSTABLE", "BLINKS", "LAST_RAW_FG", "LAST_FG", "LAST_FG_DIL_INV", "LAST_RAW_BLINK", "ROI",
+             "LAST_COLOR", "LAST_DESC", "SAMPLE_COLOR", "SAMPLE_DESC", "DS_LT", "DS_ST", "LUT"]
+MAP_IDS = {n: i for i, n in enumerate(MAP_NAMES)}
+
+
+class LvbgsParams(C.Structure):
+    _fields_ = [("desc_dist_threshold_offset", C.c_size_t), ("min_color_dist_threshold", C.c_size_t),
+                ("bg_samples", C.c_size_t), ("required_bg_samples", C.c_size_t),
+                ("samples_for_moving_avgs", C.c_size_t), ("rel_lbsp_threshold", C.c_float),
+                ("lbsp_threshold_offset", C.c_size_t), ("default_median_blur_kernel_size", C.c_int),
+                ("seed", C.c_uint64), ("device_id", C.c_int)]
+
+
+class LvbgsFrame(C.Structure):
+    _fields_ = [("image", C.c_void_p), ("stride", C.c_size_t), ("fgmask", C.c_void_p),
+                ("learning_rate", C.c_double)]
+
+
+class LvbgsScalars(C.Structure):
+    _fields_ = [("frame_idx", C.c_uint64), ("frames_since_last_reset", C.c_uint64),
+                ("model_reset_cooldown", C.c_uint64), ("auto_model_reset_enabled", C.c_int32),
+                ("learning_rate_scaling_enabled", C.c_int32), ("use_3x3_spread", C.c_int32),
+                ("median_blur_kernel_size", C.c_int32), ("lr_lower_cap", C.c_float), ("lr_upper_cap", C.c_float),
+                ("last_nonzero_desc_ratio", C.c_float), ("nonzero_desc_count", C.c_uint64),
+                ("tot_color_diff", C.c_uint64), ("n_relevant_px", C.c_uint64), ("orig_roi_px", C.c_uint64),
+                ("stat_samples_evaluated", C.c_uint64), ("stat_sample_writes", C.c_uint64),
+                ("stat_repair_rounds", C.c_uint64), ("stat_repair_rematched", C.c_uint64)]
+
+
+class SynthConfig(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("channels", C.c_int), ("seed", C.c_uint64),
+                ("noise_sigma_milli", C.c_int), ("n_shapes", C.c_int), ("shape_min", C.c_int),
+                ("shape_max", C.c_int), ("speed_min_q8", C.c_int), ("speed_max_q8", C.c_int),
+                ("ellipses_only", C.c_int), ("ripple", C.c_int), ("drift", C.c_int), ("n_stopping", C.c_int),
+                ("n_frames", C.c_int)]
+
+
+# exported symbol -> (restype, argtypes)
+SIGNATURES = {
+    "lvbgs_default_params": (C.c_int, [C.c_int, C.POINTER(LvbgsParams)]),
+    "lvbgs_create": (C.c_int, [C.c_int, C.POINTER(LvbgsParams), C.POINTER(C.c_void_p)]),
+    "lvbgs_destroy": (C.c_int, [C.c_void_p]),
+    "lvbgs_initialize": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_size_t, C.c_void_p]),
+    "lvbgs_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_double, C.c_void_p]),
+    "lvbgs_batch_apply": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(LvbgsFrame), C.c_int, C.c_void_p]),
+    "lvbgs_batch_wait": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_void_p]),
+    "lvbgs_get_background": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lvbgs_get_background_descriptors": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lvbgs_refresh_model": (C.c_int, [C.c_void_p, C.c_float, C.c_int]),
+    "lvbgs_set_automatic_model_reset": (C.c_int, [C.c_void_p, C.c_int]),
+    "lvbgs_get_default_learning_rate": (C.c_double, [C.c_void_p]),
+    "lvbgs_get_roi": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lvbgs_get_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "lvbgs_state_bytes": (C.c_size_t, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_size_t]),
+    "lvbgs_spill": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "lvbgs_restore": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "lvbgs_lbsp_compute2": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_long, C.c_float, C.c_size_t,
+                                      C.c_void_p, C.c_int]),
+    "lvbgs_last_error": (C.c_char_p, [C.c_void_p]),
+    "lvbgs_debug_map_bytes": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]),
+    "lvbgs_debug_get_map": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]),
+    "lvbgs_get_scalars": (C.c_int, [C.c_void_p, C.POINTER(LvbgsScalars)]),
+    "lvsynth_preset": (C.c_int, [C.c_int, C.c_int, C.c_uint64, C.POINTER(SynthConfig)]),
+    "lvsynth_create": (C.c_int, [C.POINTER(SynthConfig), C.POINTER(C.c_void_p)]),
+    "lvsynth_destroy": (None, [C.c_void_p]),
+    "lvsynth_render": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "lvsynth_render_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+}
+
+_lib = None
+
+
+class LibraryMissing(ImportError):
+    pass
+
+
+def lib():
+    """Returns the loaded library; raises LibraryMissing when it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise LibraryMissing("liblvbgs.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib

@@ -1,0 +1,857 @@
+// C-ABI of the SuBSENSE CUDA path (include/lvbgs.h): handle management, parameter and input
+// validation (the reference's lvAssert_ checks), device allocation of the model, staging of
+// host/device frames, and the cooperative launch of the tick kernel for one or many streams.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/lvbgs.h"
+#include "lvbgs_internal.h"
+
+namespace lvbgs {
+extern "C" __global__ void lvbgs_subsense_tick(TickParams P, unsigned long long dsTotal, const unsigned long long* dsBase);
+extern "C" __global__ void lvbgs_init_maps(StreamDev S, const uint8_t* img, float tLo);
+extern "C" __global__ void lvbgs_refresh(StreamDev S, uint32_t frame, int start, int nref, int force, int lastBuf);
+extern "C" __global__ void lvbgs_background(StreamDev S, uint8_t* outCol, uint16_t* outDesc);
+extern "C" __global__ void lvbgs_unpack_samples(StreamDev S, uint8_t* col, uint16_t* desc);
+extern "C" __global__ void lvbgs_pack_samples(StreamDev S, const uint8_t* col, const uint16_t* desc);
+extern "C" __global__ void lvbgs_lbsp_dense(const uint8_t* img, int W, int H, int C, int absThr, float rel,
+                                            unsigned int off, uint16_t* desc);
+}  // namespace lvbgs
+
+using namespace lvbgs;
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_err;
+
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// work area of one launch: counters, barrier, repair lists, stream descriptor table
+struct Workspace {
+    TickWork* work = nullptr;
+    StreamDev* d_streams = nullptr;
+    unsigned long long* d_dsBase = nullptr;
+    unsigned long long* lists = nullptr;  // 4 lists of `cap` entries
+    size_t cap = 0;
+    int nStreamsCap = 0;
+    std::vector<StreamDev> h_streams;
+    std::vector<unsigned long long> h_dsBase;
+    void release() {
+        cudaFree(work);
+        cudaFree(d_streams);
+        cudaFree(d_dsBase);
+        cudaFree(lists);
+        *this = Workspace();
+    }
+    cudaError_t ensure(size_t px, int nStreams) {
+        cudaError_t e = cudaSuccess;
+        if (!work && (e = cudaMalloc(&work, sizeof(TickWork))) != cudaSuccess) return e;
+        if (nStreams > nStreamsCap) {
+            cudaFree(d_streams);
+            cudaFree(d_dsBase);
+            d_streams = nullptr;
+            d_dsBase = nullptr;
+            const int n = std::max(nStreams, 8);
+            if ((e = cudaMalloc(&d_streams, sizeof(StreamDev) * n)) != cudaSuccess) return e;
+            if ((e = cudaMalloc(&d_dsBase, sizeof(unsigned long long) * (n + 1))) != cudaSuccess) return e;
+            nStreamsCap = n;
+        }
+        if (px > cap) {
+            cudaFree(lists);
+            lists = nullptr;
+            if ((e = cudaMalloc(&lists, sizeof(unsigned long long) * px * 4)) != cudaSuccess) {
+                cap = 0;
+                return e;
+            }
+            cap = px;
+        }
+        return e;
+    }
+};
+
+}  // namespace
+
+struct lvbgs_ctx {
+    lvbgs_algo algo;
+    lvbgs_params prm;
+    int device = 0;
+    std::string err;
+    bool initialized = false;
+    bool spilled = false;
+    int W = 0, H = 0, C = 0;
+    size_t npx = 0;
+    std::vector<uint8_t> roi;
+    size_t n_rel = 0, orig_roi = 0;
+    // device memory: one block, persistent state first (the spill image), then scratch
+    uint8_t* dmem = nullptr;
+    size_t persistBytes = 0, totalBytes = 0;
+    StreamDev sd{};  // host copy of the descriptor (device pointers)
+    uint8_t* d_frame = nullptr;
+    uint8_t* d_mask = nullptr;
+    cudaStream_t stream = nullptr;
+    Workspace ws;       // single-stream launches
+    Workspace batchWs;  // batched launches led by this handle
+};
+
+namespace {
+
+lvbgs_status fail(lvbgs_handle h, lvbgs_status st, const std::string& msg) {
+    if (h) h->err = msg;
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_err = msg;
+    return st;
+}
+lvbgs_status cuda_fail(lvbgs_handle h, cudaError_t e, const char* what) {
+    const lvbgs_status st = (e == cudaErrorMemoryAllocation) ? LVBGS_OOM : LVBGS_DEVICE_ERROR;
+    return fail(h, st, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define LV_CUDA(h, call, what)                          \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) return cuda_fail(h, e_, what); \
+    } while (0)
+
+bool is_device_ptr(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// layout of one stream's device block
+struct Layout {
+    size_t off[32];
+    size_t persist, total;
+};
+enum {
+    L_CTL = 0, L_FM, L_UNST, L_LASTCOL, L_LASTDESC, L_SD, L_SC, L_ROI, L_BLINKS, L_LASTRAWFG, L_LASTFG, L_DILINV,
+    L_LASTRAWBLINK, L_KCTR, L_DSLT, L_DSST,
+    // scratch (not spilled)
+    L_STAMPD, L_STAMPR, L_PREFLOOD, L_COMBINED, L_LABEL, L_INTENT, L_FRAME, L_MASK, L_COUNT
+};
+Layout make_layout(int W, int H, int C, size_t N) {
+    const size_t npx = (size_t)W * H;
+    const size_t nds = (size_t)(W / 8) * (H / 8) * C;
+    size_t sz[L_COUNT];
+    sz[L_CTL] = sizeof(StreamCtl);
+    sz[L_FM] = 2 * kNumFloatMaps * npx * 4;
+    sz[L_UNST] = 2 * npx;
+    sz[L_LASTCOL] = 2 * npx * C;
+    sz[L_LASTDESC] = 2 * npx * C * 2;
+    sz[L_SD] = N * npx * (C == 3 ? 8 : 2);
+    sz[L_SC] = N * npx;
+    sz[L_ROI] = sz[L_BLINKS] = sz[L_LASTRAWFG] = sz[L_LASTFG] = sz[L_DILINV] = sz[L_LASTRAWBLINK] = npx;
+    sz[L_KCTR] = npx * 2;
+    sz[L_DSLT] = sz[L_DSST] = std::max<size_t>(nds, 1) * 4;
+    sz[L_STAMPD] = sz[L_STAMPR] = npx * 4;
+    sz[L_PREFLOOD] = sz[L_COMBINED] = npx;
+    sz[L_LABEL] = sz[L_INTENT] = npx * 4;
+    sz[L_FRAME] = npx * C;
+    sz[L_MASK] = npx;
+    Layout L;
+    size_t o = 0;
+    for (int i = 0; i < L_COUNT; ++i) {
+        if (i == L_STAMPD) L.persist = o;
+        L.off[i] = o;
+        o += align256(sz[i]);
+    }
+    L.total = o;
+    return L;
+}
+
+void fill_pointers(lvbgs_ctx* h, const Layout& L) {
+    StreamDev& S = h->sd;
+    uint8_t* b = h->dmem;
+    S.ctl = (StreamCtl*)(b + L.off[L_CTL]);
+    S.fm = (float*)(b + L.off[L_FM]);
+    S.unst = b + L.off[L_UNST];
+    S.lastCol = b + L.off[L_LASTCOL];
+    S.lastDesc = (uint16_t*)(b + L.off[L_LASTDESC]);
+    S.sD = b + L.off[L_SD];
+    S.sC = b + L.off[L_SC];
+    S.roi = b + L.off[L_ROI];
+    S.blinks = b + L.off[L_BLINKS];
+    S.lastRawFG = b + L.off[L_LASTRAWFG];
+    S.lastFG = b + L.off[L_LASTFG];
+    S.dilInv = b + L.off[L_DILINV];
+    S.lastRawBlink = b + L.off[L_LASTRAWBLINK];
+    S.kctr = (uint16_t*)(b + L.off[L_KCTR]);
+    S.dsLT = (float*)(b + L.off[L_DSLT]);
+    S.dsST = (float*)(b + L.off[L_DSST]);
+    S.stampD = (uint32_t*)(b + L.off[L_STAMPD]);
+    S.stampR = (uint32_t*)(b + L.off[L_STAMPR]);
+    S.preflood = b + L.off[L_PREFLOOD];
+    S.combined = b + L.off[L_COMBINED];
+    S.label = (int*)(b + L.off[L_LABEL]);
+    S.intent = (uint32_t*)(b + L.off[L_INTENT]);
+    h->d_frame = b + L.off[L_FRAME];
+    h->d_mask = b + L.off[L_MASK];
+}
+
+void fill_geometry(lvbgs_ctx* h) {
+    StreamDev& S = h->sd;
+    S.W = h->W;
+    S.H = h->H;
+    S.C = h->C;
+    S.npx = (int)h->npx;
+    S.tilesX = (h->W + kTileW - 1) / kTileW;
+    S.tilesY = (h->H + kTileH - 1) / kTileH;
+    S.nTiles = S.tilesX * S.tilesY;
+    S.tileBase = 0;
+    S.dsW = h->W / 8;
+    S.dsH = h->H / 8;
+    S.dsSX = S.dsW > 0 ? h->W / S.dsW : 1;
+    S.dsSY = S.dsH > 0 ? h->H / S.dsH : 1;
+    S.N = (int)h->prm.bg_samples;
+    S.nreq = (int)h->prm.required_bg_samples;
+    S.minColor = (int)h->prm.min_color_dist_threshold;
+    S.descOff = (int)h->prm.desc_dist_threshold_offset;
+    S.stabColorOff = (int)(h->prm.min_color_dist_threshold / 5);
+    S.nmv = (int)h->prm.samples_for_moving_avgs;
+    S.relThr = h->prm.rel_lbsp_threshold;
+    S.lbspOff = (unsigned)h->prm.lbsp_threshold_offset;
+    S.seed = h->prm.seed;
+}
+
+int g_coop_blocks_per_sm = -1, g_sm_count = 0;
+std::mutex g_occ_mu;
+cudaError_t coop_grid(int* maxBlocks) {
+    std::lock_guard<std::mutex> lk(g_occ_mu);
+    if (g_coop_blocks_per_sm < 0) {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_coop_blocks_per_sm, lvbgs_subsense_tick, kThreads, 0)) !=
+            cudaSuccess)
+            return e;
+    }
+    *maxBlocks = g_coop_blocks_per_sm * g_sm_count;
+    return cudaSuccess;
+}
+
+// enqueue one tick over n streams described in ws.h_streams (tileBase etc. filled here)
+lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t st) {
+    int totalTiles = 0;
+    size_t totalPx = 0;
+    unsigned long long ds = 0;
+    ws.h_dsBase.resize(n + 1);
+    for (int i = 0; i < n; ++i) {
+        StreamDev& S = ws.h_streams[i];
+        S.tileBase = totalTiles;
+        totalTiles += S.nTiles;
+        totalPx += (size_t)S.npx;
+        ws.h_dsBase[i] = ds;
+        // only streams with the frame-level analysis enabled down-sample (flag mirrored on the host)
+        if (S.lrScaling) ds += (unsigned long long)S.dsW * S.dsH;
+    }
+    ws.h_dsBase[n] = ds;
+    LV_CUDA(errh, ws.ensure(totalPx, n), "workspace allocation");
+    LV_CUDA(errh, cudaMemcpyAsync(ws.d_streams, ws.h_streams.data(), sizeof(StreamDev) * n, cudaMemcpyHostToDevice, st),
+            "descriptor upload");
+    LV_CUDA(errh, cudaMemcpyAsync(ws.d_dsBase, ws.h_dsBase.data(), sizeof(unsigned long long) * (n + 1),
+                                  cudaMemcpyHostToDevice, st),
+            "descriptor upload");
+    LV_CUDA(errh, cudaMemsetAsync(ws.work, 0, sizeof(TickWork), st), "work reset");
+    int maxBlocks = 0;
+    LV_CUDA(errh, coop_grid(&maxBlocks), "occupancy query");
+    if (maxBlocks <= 0) return fail(errh, LVBGS_DEVICE_ERROR, "tick kernel cannot be resident on this device");
+    const int grid = std::max(1, std::min(maxBlocks, totalTiles));
+    TickParams P;
+    P.streams = ws.d_streams;
+    P.nStreams = n;
+    P.totalTiles = totalTiles;
+    P.work = ws.work;
+    P.dlist[0] = ws.lists;
+    P.dlist[1] = ws.lists + ws.cap;
+    P.rlist[0] = ws.lists + 2 * ws.cap;
+    P.rlist[1] = ws.lists + 3 * ws.cap;
+    P.listCap = (unsigned)std::min<size_t>(ws.cap, 0xffffffffu);
+    const unsigned long long* dsb = ws.d_dsBase;
+    void* args[] = {&P, &ds, &dsb};
+    LV_CUDA(errh,
+            cudaLaunchCooperativeKernel((const void*)lvbgs_subsense_tick, dim3(grid), dim3(kThreads), args, 0, st),
+            "tick kernel launch");
+    return LVBGS_OK;
+}
+
+lvbgs_status read_work_status(lvbgs_handle errh, Workspace& ws) {
+    TickWork w;
+    LV_CUDA(errh, cudaMemcpy(&w, ws.work, sizeof(TickWork), cudaMemcpyDeviceToHost), "status read-back");
+    if (w.err & ERR_BARRIER_TIMEOUT) return fail(errh, LVBGS_DEVICE_TIMEOUT, "grid barrier wait timed out");
+    if (w.err & ERR_REPAIR_LIMIT) return fail(errh, LVBGS_DEVICE_ERROR, "raster-order repair did not converge");
+    if (w.err & ERR_UF_LIMIT) return fail(errh, LVBGS_DEVICE_ERROR, "hole-filling union-find exceeded its bound");
+    if (w.err & ERR_RING) return fail(errh, LVBGS_DEVICE_ERROR, "closed mask is not zero at pixel (0,0)");
+    return LVBGS_OK;
+}
+
+// stages a frame for the kernel: returns the device pointer the kernel reads
+lvbgs_status stage_frame(lvbgs_handle h, const uint8_t* img, size_t stride, cudaStream_t st, const uint8_t** out) {
+    const size_t row = (size_t)h->W * h->C;
+    if (stride == 0) stride = row;
+    if (stride < row) return fail(h, LVBGS_BAD_ARG, "image stride is smaller than width*channels");
+    const bool dev = is_device_ptr(img);
+    if (dev && stride == row) {
+        *out = img;
+        return LVBGS_OK;
+    }
+    LV_CUDA(h,
+            cudaMemcpy2DAsync(h->d_frame, row, img, stride, row, h->H, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                              st),
+            "frame upload");
+    *out = h->d_frame;
+    return LVBGS_OK;
+}
+
+void set_lr(StreamDev& S, double lr) {
+    // nLearningRate of the BG branch (:277 / :421)
+    if (std::isinf(lr)) {
+        S.lrMode = 1;
+        S.lrFixed = ~0ull;
+    } else if (lr > 0) {
+        S.lrMode = 1;
+        S.lrFixed = (unsigned long long)std::ceil(lr);
+    } else {
+        S.lrMode = 0;
+        S.lrFixed = 0;
+    }
+}
+
+lvbgs_status check_ready(lvbgs_handle h) {
+    if (!h) return fail(nullptr, LVBGS_BAD_ARG, "null handle");
+    if (!h->initialized) return fail(h, LVBGS_NOT_INITIALIZED, "algo & model must be initialized first");
+    if (h->spilled) return fail(h, LVBGS_NOT_INITIALIZED, "stream state is spilled to host memory; restore it first");
+    if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, LVBGS_DEVICE_ERROR, "cannot select the CUDA device");
+    return LVBGS_OK;
+}
+
+// box max over a (2r+1)^2 window clipped to the image
+void host_dilate(const std::vector<uint8_t>& src, std::vector<uint8_t>& dst, int W, int H, int r) {
+    std::vector<uint8_t> tmp(src.size());
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            uint8_t v = 0;
+            for (int d = -r; d <= r; ++d)
+                if (x + d >= 0 && x + d < W) v = std::max(v, src[(size_t)y * W + x + d]);
+            tmp[(size_t)y * W + x] = v;
+        }
+    dst.assign(src.size(), 0);
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            uint8_t v = 0;
+            for (int d = -r; d <= r; ++d)
+                if (y + d >= 0 && y + d < H) v = std::max(v, tmp[(size_t)(y + d) * W + x]);
+            dst[(size_t)y * W + x] = v;
+        }
+}
+
+uint8_t sat_round_u8(float v) {
+    const long r = std::lrint(v);
+    return (uint8_t)(r < 0 ? 0 : r > 255 ? 255 : r);
+}
+
+}  // namespace
+
+extern "C" {
+
+lvbgs_status lvbgs_default_params(lvbgs_algo algo, lvbgs_params* out) {
+    if (!out) return fail(nullptr, LVBGS_BAD_ARG, "null output");
+    if (algo != LVBGS_ALGO_SUBSENSE) return fail(nullptr, LVBGS_UNSUPPORTED, "only SuBSENSE is implemented on the GPU");
+    out->desc_dist_threshold_offset = 3;
+    out->min_color_dist_threshold = 30;
+    out->bg_samples = 50;
+    out->required_bg_samples = 2;
+    out->samples_for_moving_avgs = 100;
+    out->rel_lbsp_threshold = 0.333f;
+    out->lbsp_threshold_offset = 0;
+    out->default_median_blur_kernel_size = 9;
+    out->seed = 0;
+    out->device_id = 0;
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_create(lvbgs_algo algo, const lvbgs_params* p, lvbgs_handle* out) {
+    if (!out) return fail(nullptr, LVBGS_BAD_ARG, "null output handle");
+    *out = nullptr;
+    if (algo != LVBGS_ALGO_SUBSENSE) return fail(nullptr, LVBGS_UNSUPPORTED, "only SuBSENSE is implemented on the GPU");
+    lvbgs_params prm;
+    if (p) prm = *p;
+    else lvbgs_default_params(algo, &prm);
+    // BackgroundSubtractorSuBSENSE.cpp:76-77, BackgroundSubtractorLBSP.hpp:53
+    if (prm.bg_samples == 0 || prm.required_bg_samples > prm.bg_samples)
+        return fail(nullptr, LVBGS_BAD_ARG, "algo cannot require more sample matches than sample count in model");
+    if (prm.min_color_dist_threshold == 0 && prm.desc_dist_threshold_offset == 0)
+        return fail(nullptr, LVBGS_BAD_ARG, "distance thresholds must be positive values");
+    if (!(prm.rel_lbsp_threshold >= 0)) return fail(nullptr, LVBGS_BAD_ARG, "relative threshold for LBSP features must be non-negative");
+    if (prm.bg_samples > (size_t)kMaxSamples)
+        return fail(nullptr, LVBGS_UNSUPPORTED, "this implementation supports at most 64 model samples");
+    if (prm.samples_for_moving_avgs < 4 || prm.min_color_dist_threshold > 100000 || prm.desc_dist_threshold_offset > 100000)
+        return fail(nullptr, LVBGS_UNSUPPORTED, "parameter outside the supported range");
+    if (prm.default_median_blur_kernel_size < 1 || prm.default_median_blur_kernel_size > 31 ||
+        (prm.default_median_blur_kernel_size % 2) == 0)
+        return fail(nullptr, LVBGS_BAD_ARG, "median blur kernel size must be odd, between 1 and 31");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= prm.device_id || prm.device_id < 0) {
+        cudaGetLastError();
+        return fail(nullptr, LVBGS_DEVICE_ERROR, "no CUDA device with the requested id");
+    }
+    if (cudaSetDevice(prm.device_id) != cudaSuccess) return fail(nullptr, LVBGS_DEVICE_ERROR, "cannot select the CUDA device");
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, (const void*)lvbgs_subsense_tick) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(nullptr, LVBGS_DEVICE_ERROR, "the library's sm_103a kernels cannot run on this device");
+    }
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, prm.device_id);
+    if (!coop) return fail(nullptr, LVBGS_DEVICE_ERROR, "device does not support cooperative launches");
+    lvbgs_ctx* h = new lvbgs_ctx();
+    h->algo = algo;
+    h->prm = prm;
+    h->device = prm.device_id;
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return fail(nullptr, LVBGS_DEVICE_ERROR, "stream creation failed");
+    }
+    *out = h;
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_destroy(lvbgs_handle h) {
+    if (!h) return LVBGS_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaFree(h->dmem);
+    h->ws.release();
+    h->batchWs.release();
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_initialize(lvbgs_handle h, const uint8_t* img, int W, int H, int C, size_t stride, const uint8_t* roi) {
+    if (!h) return fail(nullptr, LVBGS_BAD_ARG, "null handle");
+    if (!img || W <= 0 || H <= 0) return fail(h, LVBGS_BAD_ARG, "provided image for initialization must be non-empty");
+    if (C == 4) return fail(h, LVBGS_UNSUPPORTED, "8UC4 frames are not handled by SuBSENSE's apply() (1 or 3 channels)");
+    if (C != 1 && C != 3) return fail(h, LVBGS_BAD_TYPE, "image must be of type 8UC1 or 8UC3");
+    if ((size_t)W * H >= (1ull << 31)) return fail(h, LVBGS_UNSUPPORTED, "frame too large");
+    if (cudaSetDevice(h->device) != cudaSuccess) return fail(h, LVBGS_DEVICE_ERROR, "cannot select the CUDA device");
+    const size_t npx = (size_t)W * H;
+    const size_t row = (size_t)W * C;
+    if (stride == 0) stride = row;
+    if (stride < row) return fail(h, LVBGS_BAD_ARG, "image stride is smaller than width*channels");
+    // ROI handling (BackgroundSubtractionUtils.cpp:83-101, validateROI :28-36)
+    std::vector<uint8_t> newroi(npx, 255);
+    if (roi) {
+        const bool devRoi = is_device_ptr(roi);
+        std::vector<uint8_t> r(npx);
+        if (devRoi) LV_CUDA(h, cudaMemcpy(r.data(), roi, npx, cudaMemcpyDeviceToHost), "roi download");
+        else std::memcpy(r.data(), roi, npx);
+        for (size_t i = 0; i < npx; ++i)
+            if (r[i] != 0 && r[i] != 255) return fail(h, LVBGS_BAD_ARG, "provided ROI mat values must be 0 or 255 only");
+        std::vector<uint8_t> d;
+        host_dilate(r, d, W, H, kBorder);
+        for (size_t i = 0; i < npx; ++i) newroi[i] = (uint8_t)(r[i] | (d[i] / 2));
+    }
+    size_t orig = 0;
+    for (size_t i = 0; i < npx; ++i) orig += newroi[i] != 0;
+    if (orig == 0) return fail(h, LVBGS_BAD_ARG, "provided ROI mat contains no useful pixels");
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x)
+            if (x < kBorder || y < kBorder || x >= W - kBorder || y >= H - kBorder) newroi[(size_t)y * W + x] = 0;
+    size_t fin = 0;
+    for (size_t i = 0; i < npx; ++i) fin += newroi[i] != 0;
+    if (fin == 0)
+        return fail(h, LVBGS_BAD_ARG, "provided ROI mat contains no useful pixels away from borders (descriptors will hit image bounds)");
+    // resolution-dependent parameters (BackgroundSubtractorSuBSENSE.cpp:112-128)
+    StreamCtl ctl;
+    std::memset(&ctl, 0, sizeof(ctl));
+    const int area = W * H;
+    if (orig >= npx / 2 && (int)npx >= 320 * 240) {
+        ctl.lr_scaling = 1;
+        ctl.auto_reset = 1;
+        ctl.use3x3 = !(area > 320 * 240 * 2);
+        int raw = (int)std::floor((float)area / (320 * 240) + 0.5f) + h->prm.default_median_blur_kernel_size;
+        raw = std::min(raw, 14);
+        ctl.median_k = (raw % 2) ? raw : raw - 1;
+        ctl.t_lo = 2.0f;
+        ctl.t_hi = 256.0f;
+        const int dsW = W / 8, dsH = H / 8;
+        if (dsW <= 0 || dsH <= 0 || W % dsW != 0 || H % dsH != 0)
+            return fail(h, LVBGS_UNSUPPORTED,
+                        "frame-level analysis needs an integral 1/8 down-sampling (INTER_AREA fast path): width and height must be multiples of width/8 and height/8");
+    } else {
+        ctl.lr_scaling = 0;
+        ctl.auto_reset = 0;
+        ctl.use3x3 = 1;
+        ctl.median_k = h->prm.default_median_blur_kernel_size;
+        ctl.t_lo = 4.0f;
+        ctl.t_hi = 512.0f;
+    }
+    const float rel = h->prm.rel_lbsp_threshold;
+    for (int t = 0; t <= 255; ++t)
+        ctl.lut[t] = C == 1 ? sat_round_u8(((float)t * rel + (float)h->prm.lbsp_threshold_offset) / 3)
+                            : sat_round_u8((float)t * rel + (float)h->prm.lbsp_threshold_offset);
+    ctl.n_rel = fin;
+    ctl.orig_roi = orig;
+    ctl.stamp_base = 1;
+    // (re)allocate the device model
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaFree(h->dmem);
+    h->dmem = nullptr;
+    h->initialized = false;
+    h->spilled = false;
+    const Layout L = make_layout(W, H, C, h->prm.bg_samples);
+    LV_CUDA(h, cudaMalloc(&h->dmem, L.total), "model allocation");
+    h->persistBytes = L.persist;
+    h->totalBytes = L.total;
+    h->W = W;
+    h->H = H;
+    h->C = C;
+    h->npx = npx;
+    h->roi = newroi;
+    h->n_rel = fin;
+    h->orig_roi = orig;
+    fill_pointers(h, L);
+    fill_geometry(h);
+    h->sd.lrScaling = ctl.lr_scaling;
+    cudaStream_t st = h->stream;
+    LV_CUDA(h, cudaMemsetAsync(h->dmem, 0, L.total, st), "model reset");
+    LV_CUDA(h, cudaMemcpyAsync(h->sd.ctl, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, st), "control upload");
+    LV_CUDA(h, cudaMemcpyAsync(h->sd.roi, h->roi.data(), npx, cudaMemcpyHostToDevice, st), "roi upload");
+    const uint8_t* dimg = nullptr;
+    lvbgs_status s = stage_frame(h, img, stride, st, &dimg);
+    if (s != LVBGS_OK) return s;
+    lvbgs_init_maps<<<1024, 256, 0, st>>>(h->sd, dimg, ctl.t_lo);
+    LV_CUDA(h, cudaGetLastError(), "init kernel launch");
+    // refreshModel(1.0f) at frame 0 (BackgroundSubtractorSuBSENSE.cpp:184)
+    lvbgs_refresh<<<1024, 256, 0, st>>>(h->sd, 0u, 0, (int)h->prm.bg_samples, 0, 0);
+    LV_CUDA(h, cudaGetLastError(), "refresh kernel launch");
+    LV_CUDA(h, h->ws.ensure(npx, 1), "workspace allocation");
+    LV_CUDA(h, cudaStreamSynchronize(st), "initialization");
+    h->initialized = true;
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_apply(lvbgs_handle h, const uint8_t* img, size_t stride, uint8_t* mask, double lr, void* cuda_stream) {
+    lvbgs_status s = check_ready(h);
+    if (s != LVBGS_OK) return s;
+    if (!img) return fail(h, LVBGS_BAD_ARG, "null input image");
+    cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : h->stream;
+    const uint8_t* dimg = nullptr;
+    if ((s = stage_frame(h, img, stride, st, &dimg)) != LVBGS_OK) return s;
+    const bool devMask = mask && is_device_ptr(mask);
+    h->ws.h_streams.assign(1, h->sd);
+    StreamDev& S = h->ws.h_streams[0];
+    S.frame = dimg;
+    S.maskOut = devMask ? mask : h->d_mask;
+    set_lr(S, lr);
+    if ((s = launch_tick(h, h->ws, 1, st)) != LVBGS_OK) return s;
+    if (mask && !devMask) LV_CUDA(h, cudaMemcpyAsync(mask, h->d_mask, h->npx, cudaMemcpyDeviceToHost, st), "mask download");
+    LV_CUDA(h, cudaStreamSynchronize(st), "frame step");
+    return read_work_status(h, h->ws);
+}
+
+lvbgs_status lvbgs_batch_apply(const lvbgs_handle* hs, const lvbgs_frame* frames, int n, void* cuda_stream) {
+    if (!hs || !frames || n <= 0) return fail(nullptr, LVBGS_BAD_ARG, "empty batch");
+    lvbgs_handle lead = hs[0];
+    for (int i = 0; i < n; ++i) {
+        lvbgs_status s = check_ready(hs[i]);
+        if (s != LVBGS_OK) return s;
+        if (hs[i]->device != lead->device) return fail(lead, LVBGS_BAD_ARG, "batched handles must share one device");
+        if (!frames[i].image) return fail(hs[i], LVBGS_BAD_ARG, "null input image");
+        for (int j = 0; j < i; ++j)
+            if (hs[j] == hs[i]) return fail(lead, LVBGS_BAD_ARG, "a handle appears twice in the batch");
+    }
+    cudaSetDevice(lead->device);
+    cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : lead->stream;
+    Workspace& ws = lead->batchWs;
+    ws.h_streams.resize(n);
+    for (int i = 0; i < n; ++i) {
+        lvbgs_handle h = hs[i];
+        const uint8_t* dimg = nullptr;
+        lvbgs_status s = stage_frame(h, frames[i].image, frames[i].stride, st, &dimg);
+        if (s != LVBGS_OK) return s;
+        ws.h_streams[i] = h->sd;
+        StreamDev& S = ws.h_streams[i];
+        S.frame = dimg;
+        const bool devMask = frames[i].fgmask && is_device_ptr(frames[i].fgmask);
+        S.maskOut = devMask ? frames[i].fgmask : h->d_mask;
+        set_lr(S, frames[i].learning_rate);
+    }
+    lvbgs_status s = launch_tick(lead, ws, n, st);
+    if (s != LVBGS_OK) return s;
+    for (int i = 0; i < n; ++i)
+        if (frames[i].fgmask && !is_device_ptr(frames[i].fgmask))
+            LV_CUDA(lead, cudaMemcpyAsync(frames[i].fgmask, hs[i]->d_mask, hs[i]->npx, cudaMemcpyDeviceToHost, st),
+                    "mask download");
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_batch_wait(const lvbgs_handle* hs, int n, void* cuda_stream) {
+    if (!hs || n <= 0) return fail(nullptr, LVBGS_BAD_ARG, "empty batch");
+    lvbgs_handle lead = hs[0];
+    cudaSetDevice(lead->device);
+    cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : lead->stream;
+    LV_CUDA(lead, cudaStreamSynchronize(st), "batched frame step");
+    return read_work_status(lead, lead->batchWs);
+}
+
+lvbgs_status lvbgs_get_background(lvbgs_handle h, uint8_t* out) {
+    lvbgs_status s = check_ready(h);
+    if (s != LVBGS_OK) return s;
+    if (!out) return fail(h, LVBGS_BAD_ARG, "null output");
+    const bool dev = is_device_ptr(out);
+    uint8_t* d = dev ? out : h->d_frame;
+    lvbgs_background<<<512, 256, 0, h->stream>>>(h->sd, d, nullptr);
+    LV_CUDA(h, cudaGetLastError(), "background kernel");
+    if (!dev) LV_CUDA(h, cudaMemcpyAsync(out, d, h->npx * h->C, cudaMemcpyDeviceToHost, h->stream), "download");
+    LV_CUDA(h, cudaStreamSynchronize(h->stream), "background image");
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_get_background_descriptors(lvbgs_handle h, uint16_t* out) {
+    lvbgs_status s = check_ready(h);
+    if (s != LVBGS_OK) return s;
+    if (!out) return fail(h, LVBGS_BAD_ARG, "null output");
+    uint16_t* d = nullptr;
+    LV_CUDA(h, cudaMallocAsync((void**)&d, h->npx * h->C * 2, h->stream), "temporary allocation");
+    lvbgs_background<<<512, 256, 0, h->stream>>>(h->sd, nullptr, d);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, h->npx * h->C * 2, cudaMemcpyDefault, h->stream);
+    cudaFreeAsync(d, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "background descriptors");
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_refresh_model(lvbgs_handle h, float frac, int force) {
+    lvbgs_status s = check_ready(h);
+    if (s != LVBGS_OK) return s;
+    if (!(frac > 0.0f && frac <= 1.0f)) return fail(h, LVBGS_BAD_ARG, "model refresh must be given as a non-null fraction");
+    StreamCtl ctl;
+    LV_CUDA(h, cudaMemcpy(&ctl, h->sd.ctl, sizeof(ctl), cudaMemcpyDeviceToHost), "control read");
+    const size_t N = h->prm.bg_samples;
+    const size_t nref = frac < 1.0f ? (size_t)(frac * (float)N) : N;
+    size_t start = 0;
+    if (frac < 1.0f) {
+        // frame-level draw (sentinel pixel) of nRefreshSampleStartPos (:86)
+        const uint32_t k = ctl.ksent++;
+        uint32_t c[4] = {k >> 2, kSentinelPx, (uint32_t)ctl.frame_idx, 0u};
+        philox4x32_10(c, (uint32_t)h->prm.seed, (uint32_t)(h->prm.seed >> 32));
+        start = (size_t)(c[k & 3u] & 0x7fffffffu) % N;
+        LV_CUDA(h, cudaMemcpy(&h->sd.ctl->ksent, &ctl.ksent, sizeof(ctl.ksent), cudaMemcpyHostToDevice), "control write");
+    }
+    lvbgs_refresh<<<1024, 256, 0, h->stream>>>(h->sd, (uint32_t)ctl.frame_idx, (int)start, (int)nref, force ? 1 : 0,
+                                               (int)(ctl.frame_idx & 1ull));
+    LV_CUDA(h, cudaGetLastError(), "refresh kernel");
+    LV_CUDA(h, cudaStreamSynchronize(h->stream), "refresh");
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_set_automatic_model_reset(lvbgs_handle h, int enabled) {
+    lvbgs_status s = check_ready(h);
+    if (s != LVBGS_OK) return s;
+    const int v = enabled ? 1 : 0;
+    LV_CUDA(h, cudaMemcpy(&h->sd.ctl->auto_reset, &v, sizeof(v), cudaMemcpyHostToDevice), "control write");
+    return LVBGS_OK;
+}
+
+double lvbgs_get_default_learning_rate(lvbgs_handle) { return 0.0; }
+
+lvbgs_status lvbgs_get_roi(lvbgs_handle h, uint8_t* out) {
+    if (!h || !out) return fail(h, LVBGS_BAD_ARG, "null argument");
+    if (!h->initialized) return fail(h, LVBGS_NOT_INITIALIZED, "algo must be initialized first");
+    std::memcpy(out, h->roi.data(), h->npx);
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_get_size(lvbgs_handle h, int* w, int* hh, int* c) {
+    if (!h) return fail(nullptr, LVBGS_BAD_ARG, "null handle");
+    if (!h->initialized) return fail(h, LVBGS_NOT_INITIALIZED, "algo must be initialized first");
+    if (w) *w = h->W;
+    if (hh) *hh = h->H;
+    if (c) *c = h->C;
+    return LVBGS_OK;
+}
+
+size_t lvbgs_state_bytes(lvbgs_algo algo, int W, int H, int C, size_t N) {
+    if (algo != LVBGS_ALGO_SUBSENSE || W <= 0 || H <= 0 || (C != 1 && C != 3)) return 0;
+    return make_layout(W, H, C, N ? N : 50).persist;
+}
+
+lvbgs_status lvbgs_spill(lvbgs_handle h, void* host, size_t bytes) {
+    lvbgs_status s = check_ready(h);
+    if (s != LVBGS_OK) return s;
+    if (!host || bytes < h->persistBytes) return fail(h, LVBGS_BAD_ARG, "spill buffer is smaller than lvbgs_state_bytes()");
+    LV_CUDA(h, cudaStreamSynchronize(h->stream), "spill");
+    LV_CUDA(h, cudaMemcpy(host, h->dmem, h->persistBytes, cudaMemcpyDeviceToHost), "spill copy");
+    cudaFree(h->dmem);
+    h->dmem = nullptr;
+    h->ws.release();
+    h->batchWs.release();
+    h->spilled = true;
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_restore(lvbgs_handle h, const void* host, size_t bytes) {
+    if (!h || !host) return fail(h, LVBGS_BAD_ARG, "null argument");
+    if (!h->initialized || !h->spilled) return fail(h, LVBGS_NOT_INITIALIZED, "stream is not spilled");
+    if (bytes < h->persistBytes) return fail(h, LVBGS_BAD_ARG, "restore buffer is smaller than lvbgs_state_bytes()");
+    cudaSetDevice(h->device);
+    const Layout L = make_layout(h->W, h->H, h->C, h->prm.bg_samples);
+    LV_CUDA(h, cudaMalloc(&h->dmem, L.total), "model allocation");
+    LV_CUDA(h, cudaMemcpy(h->dmem, host, h->persistBytes, cudaMemcpyHostToDevice), "restore copy");
+    LV_CUDA(h, cudaMemset(h->dmem + h->persistBytes, 0, L.total - h->persistBytes), "scratch reset");
+    fill_pointers(h, L);
+    // repair stamps restart from zero, so the stamp generation restarts above them
+    const unsigned int one = 1;
+    LV_CUDA(h, cudaMemcpy(&h->sd.ctl->stamp_base, &one, sizeof(one), cudaMemcpyHostToDevice), "control write");
+    LV_CUDA(h, h->ws.ensure(h->npx, 1), "workspace allocation");
+    h->spilled = false;
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_lbsp_compute2(const uint8_t* img, int W, int H, int C, long absThr, float rel, size_t off,
+                                 uint16_t* desc, int device_id) {
+    if (!img || !desc || W <= 0 || H <= 0) return fail(nullptr, LVBGS_BAD_ARG, "input image must be non-empty");
+    if (C != 1 && C != 3) return fail(nullptr, LVBGS_BAD_TYPE, "input image must be of type 8UC1/8UC3");
+    if (absThr < 0 && !(rel >= 0)) return fail(nullptr, LVBGS_BAD_ARG, "relative LBSP threshold must be non-negative");
+    if (cudaSetDevice(device_id) != cudaSuccess) return fail(nullptr, LVBGS_DEVICE_ERROR, "cannot select the CUDA device");
+    const size_t n = (size_t)W * H * C;
+    uint8_t* di = nullptr;
+    uint16_t* dd = nullptr;
+    LV_CUDA(nullptr, cudaMalloc(&di, n), "allocation");
+    cudaError_t e = cudaMalloc(&dd, n * 2);
+    if (e == cudaSuccess) e = cudaMemcpy(di, img, n, cudaMemcpyDefault);
+    if (e == cudaSuccess) e = cudaMemcpy(dd, desc, n * 2, cudaMemcpyDefault);  // border keeps the caller's content
+    if (e == cudaSuccess) {
+        const int thr = absThr < 0 ? -1 : (int)std::min<long>(absThr, 255);
+        lvbgs_lbsp_dense<<<256, 256>>>(di, W, H, C, thr, rel, (unsigned)off, dd);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(desc, dd, n * 2, cudaMemcpyDefault);
+    cudaFree(di);
+    cudaFree(dd);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "LBSP extraction");
+    return LVBGS_OK;
+}
+
+const char* lvbgs_last_error(lvbgs_handle h) {
+    if (h) return h->err.c_str();
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    static thread_local std::string copy;
+    copy = g_err;
+    return copy.c_str();
+}
+
+lvbgs_status lvbgs_debug_map_bytes(lvbgs_handle h, int which, size_t* bytes) {
+    if (!h || !bytes) return fail(h, LVBGS_BAD_ARG, "null argument");
+    if (!h->initialized) return fail(h, LVBGS_NOT_INITIALIZED, "algo must be initialized first");
+    const size_t npx = h->npx, C = (size_t)h->C, N = h->prm.bg_samples;
+    const size_t nds = (size_t)h->sd.dsW * h->sd.dsH * C;
+    if (which >= LVBGS_MAP_R && which <= LVBGS_MAP_FIN_ST) *bytes = npx * 4;
+    else if (which >= LVBGS_MAP_UNSTABLE && which <= LVBGS_MAP_ROI) *bytes = npx;
+    else if (which == LVBGS_MAP_LAST_COLOR) *bytes = npx * C;
+    else if (which == LVBGS_MAP_LAST_DESC) *bytes = npx * C * 2;
+    else if (which == LVBGS_MAP_SAMPLE_COLOR) *bytes = N * npx * C;
+    else if (which == LVBGS_MAP_SAMPLE_DESC) *bytes = N * npx * C * 2;
+    else if (which == LVBGS_MAP_DS_LT || which == LVBGS_MAP_DS_ST) *bytes = nds * 4;
+    else if (which == LVBGS_MAP_LUT) *bytes = 256;
+    else return fail(h, LVBGS_BAD_ARG, "unknown map id");
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_debug_get_map(lvbgs_handle h, int which, void* out, size_t bytes) {
+    lvbgs_status s = check_ready(h);
+    if (s != LVBGS_OK) return s;
+    size_t need = 0;
+    if ((s = lvbgs_debug_map_bytes(h, which, &need)) != LVBGS_OK) return s;
+    if (!out || bytes < need) return fail(h, LVBGS_BAD_ARG, "output buffer too small");
+    LV_CUDA(h, cudaStreamSynchronize(h->stream), "sync");
+    StreamCtl ctl;
+    LV_CUDA(h, cudaMemcpy(&ctl, h->sd.ctl, sizeof(ctl), cudaMemcpyDeviceToHost), "control read");
+    const int cur = (int)(ctl.frame_idx & 1ull);
+    const size_t npx = h->npx, C = (size_t)h->C, N = h->prm.bg_samples;
+    const StreamDev& S = h->sd;
+    const void* src = nullptr;
+    if (which >= LVBGS_MAP_R && which <= LVBGS_MAP_FIN_ST)
+        src = S.fm + (size_t)cur * kNumFloatMaps * npx + (size_t)(which - LVBGS_MAP_R) * npx;
+    else if (which == LVBGS_MAP_UNSTABLE) src = S.unst + (size_t)cur * npx;
+    else if (which == LVBGS_MAP_BLINKS) src = S.blinks;
+    else if (which == LVBGS_MAP_LAST_RAW_FG) src = S.lastRawFG;
+    else if (which == LVBGS_MAP_LAST_FG) src = S.lastFG;
+    else if (which == LVBGS_MAP_LAST_FG_DIL_INV) src = S.dilInv;
+    else if (which == LVBGS_MAP_LAST_RAW_BLINK) src = S.lastRawBlink;
+    else if (which == LVBGS_MAP_ROI) src = S.roi;
+    else if (which == LVBGS_MAP_LAST_COLOR) src = S.lastCol + (size_t)cur * npx * C;
+    else if (which == LVBGS_MAP_LAST_DESC) src = S.lastDesc + (size_t)cur * npx * C;
+    else if (which == LVBGS_MAP_DS_LT) src = S.dsLT;
+    else if (which == LVBGS_MAP_DS_ST) src = S.dsST;
+    else if (which == LVBGS_MAP_LUT) {
+        std::memcpy(out, ctl.lut, 256);
+        return LVBGS_OK;
+    }
+    if (src) {
+        LV_CUDA(h, cudaMemcpy(out, src, need, cudaMemcpyDeviceToHost), "map download");
+        return LVBGS_OK;
+    }
+    // sample images: unpack the planes into the reference's N images
+    uint8_t* dcol = nullptr;
+    uint16_t* ddesc = nullptr;
+    LV_CUDA(h, cudaMalloc(&dcol, N * npx * C), "temporary allocation");
+    cudaError_t e = cudaMalloc(&ddesc, N * npx * C * 2);
+    if (e == cudaSuccess) {
+        lvbgs_unpack_samples<<<1024, 256>>>(h->sd, dcol, ddesc);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        if (which == LVBGS_MAP_SAMPLE_COLOR) e = cudaMemcpy(out, dcol, need, cudaMemcpyDeviceToHost);
+        else e = cudaMemcpy(out, ddesc, need, cudaMemcpyDeviceToHost);
+    }
+    cudaFree(dcol);
+    cudaFree(ddesc);
+    if (e != cudaSuccess) return cuda_fail(h, e, "sample download");
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_get_scalars(lvbgs_handle h, lvbgs_scalars* out) {
+    lvbgs_status s = check_ready(h);
+    if (s != LVBGS_OK) return s;
+    if (!out) return fail(h, LVBGS_BAD_ARG, "null output");
+    LV_CUDA(h, cudaStreamSynchronize(h->stream), "sync");
+    StreamCtl c;
+    LV_CUDA(h, cudaMemcpy(&c, h->sd.ctl, sizeof(c), cudaMemcpyDeviceToHost), "control read");
+    std::memset(out, 0, sizeof(*out));
+    out->frame_idx = c.frame_idx;
+    out->frames_since_last_reset = c.frames_since_reset;
+    out->model_reset_cooldown = c.cooldown;
+    out->auto_model_reset_enabled = c.auto_reset;
+    out->learning_rate_scaling_enabled = c.lr_scaling;
+    out->use_3x3_spread = c.use3x3;
+    out->median_blur_kernel_size = c.median_k;
+    out->lr_lower_cap = c.t_lo;
+    out->lr_upper_cap = c.t_hi;
+    out->last_nonzero_desc_ratio = c.last_nz_ratio;
+    out->nonzero_desc_count = c.last_nz;
+    out->tot_color_diff = c.last_colordiff;
+    out->n_relevant_px = c.n_rel;
+    out->orig_roi_px = c.orig_roi;
+    out->stat_samples_evaluated = c.st_samples;
+    out->stat_sample_writes = c.st_writes;
+    out->stat_repair_rounds = c.st_rounds;
+    out->stat_repair_rematched = c.st_rematched;
+    return LVBGS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,1392 @@
+// SuBSENSE frame step for sm_103a: one cooperative persistent kernel per tick processes one
+// frame of every stream in the batch (a per-stream descriptor table, tiles drawn from a device
+// work queue), separated into phases by a bounded grid barrier.
+//
+// Exactness of the reference's sequential raster scan (BackgroundSubtractorSuBSENSE.cpp:201-481):
+// a pixel p reads two things another pixel writes during the same frame -- its own samples, which
+// an earlier pixel's neighbour update may have overwritten (:296-299/:442-448), and the D_last /
+// raw-segmentation-ST values of its randomly chosen neighbour q, which are this frame's values when
+// q precedes p (:292-293/:438-439). Random draws are keyed by (stream, frame, pixel, draw index),
+// so they do not depend on the scan order. The kernel therefore
+//   A  evaluates every pixel against the frame-start model and records an "intent" (decision,
+//      samples evaluated, own/neighbour sample writes, neighbour-update state),
+//   B  resolves the ghost test of each neighbour update against the values the scan would see,
+//      and marks every pixel whose evaluated samples were overwritten by an earlier pixel,
+//   M/R repairs: re-evaluates marked pixels with the overwritten samples (M) and re-resolves the
+//      ghost tests that read a pixel whose decision changed (R), marking the pixels whose incoming
+//      writes changed, until nothing changes (the dependencies follow raster order, so this is a
+//      fixed point reached in at most the length of the longest dependency chain),
+//   F  commits every sample write in raster order (last writer wins) and starts post-processing.
+// Post-processing, frame-level statistics and the automatic model reset follow in the same launch.
+#include <cuda_runtime.h>
+
+#include "lvbgs_internal.h"
+
+namespace lvbgs {
+
+// LBSP 16-bit double-cross pattern (LBSP.hpp:297-298)
+__constant__ int c_lbsp_dx[16] = {-2, 2, 0, 0, -2, 2, 2, -2, 0, -1, 0, 1, -1, 1, 1, -1};
+__constant__ int c_lbsp_dy[16] = {0, 0, -2, 2, 2, -2, 2, -2, 1, 0, -1, 0, -1, 1, -1, 1};
+// 7x7 Gaussian sampling weights (opencv.hpp:915-923) and 3x3 / 5x5 neighbour tables (opencv.hpp:945-964)
+__constant__ int c_pat7[49] = {2, 4, 6, 7, 6, 4, 2,     4, 8, 12, 14, 12, 8, 4, 6, 12, 21, 25, 21, 12, 6, 7, 14, 25, 28,
+                               25, 14, 7, 6, 12, 21, 25, 21, 12, 6, 4, 8, 12, 14, 12, 8, 4, 2, 4, 6, 7, 6, 4, 2};
+__constant__ int c_nb3[8][2] = {{-1, 1}, {0, 1}, {1, 1}, {-1, 0}, {1, 0}, {-1, -1}, {0, -1}, {1, -1}};
+__constant__ int c_nb5[24][2] = {{-2, 2}, {-1, 2}, {0, 2},   {1, 2},   {2, 2},   {-2, 1},  {-1, 1}, {0, 1},
+                                 {1, 1},  {2, 1},  {-2, 0},  {-1, 0},  {1, 0},   {2, 0},   {-2, -1}, {-1, -1},
+                                 {0, -1}, {1, -1}, {2, -1},  {-2, -2}, {-1, -2}, {0, -2},  {1, -2}, {2, -2}};
+
+constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
+constexpr int kMaxRepairIters = 4096;
+constexpr int kUFLimit = 1 << 22;
+
+// ------------------------------------------------------------------------------------------
+// small helpers
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ unsigned int ld_volatile(const unsigned int* p) { return *(const volatile unsigned int*)p; }
+
+// Grid-wide barrier for a cooperative launch (all CTAs co-resident). The wait is bounded: after
+// kBarrierTimeoutNs the CTA records ERR_BARRIER_TIMEOUT and every CTA leaves at its next check.
+__device__ bool grid_sync(TickWork* w) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int gen = ld_volatile(&w->bar_gen);
+        __threadfence();
+        const unsigned int arrived = atomicAdd(&w->bar_count, 1u) + 1u;
+        int ok = 1;
+        if (arrived == gridDim.x) {
+            atomicExch(&w->bar_count, 0u);
+            __threadfence();
+            atomicAdd(&w->bar_gen, 1u);
+        } else {
+            const unsigned long long t0 = gtimer();
+            while (ld_volatile(&w->bar_gen) == gen) {
+                if (ld_volatile(&w->err) != 0u) {
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(40);
+                if (gtimer() - t0 > kBarrierTimeoutNs) {
+                    atomicOr(&w->err, ERR_BARRIER_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        s_ok = ok && (ld_volatile(&w->err) == 0u);
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+__device__ __forceinline__ int find_stream_by_tile(const TickParams& P, int t) {
+    int lo = 0, hi = P.nStreams - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (P.streams[mid].tileBase <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// dynamic tile queue: returns the next tile index of phase `ph` (or >= totalTiles when done)
+__device__ __forceinline__ int next_tile(const TickParams& P, int ph) {
+    __shared__ int s_t;
+    __syncthreads();
+    if (threadIdx.x == 0) s_t = (int)atomicAdd(&P.work->phase_ctr[ph], 1u);
+    __syncthreads();
+    return s_t;
+}
+
+struct DrawState {
+    uint32_t blk;
+    uint32_t v[4];
+};
+__device__ __forceinline__ uint32_t draw_k(unsigned long long seed, uint32_t frame, uint32_t px, uint32_t k,
+                                           DrawState& ds) {
+    const uint32_t blk = k >> 2;
+    if (blk != ds.blk) {
+        uint32_t c[4] = {blk, px, frame, 0u};
+        philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+        ds.v[0] = c[0];
+        ds.v[1] = c[1];
+        ds.v[2] = c[2];
+        ds.v[3] = c[3];
+        ds.blk = blk;
+    }
+    return ds.v[k & 3u] & 0x7fffffffu;
+}
+// a % m for a 31-bit draw and a size_t modulus (m >= 2^32 leaves a unchanged)
+__device__ __forceinline__ unsigned long long mod_draw(uint32_t a, unsigned long long m) {
+    return m > 0xffffffffull ? (unsigned long long)a : (unsigned long long)(a % (uint32_t)m);
+}
+
+// LBSP::computeDescriptor_threshold (LBSP.hpp:193-202) on 16 packed taps: bit n = |tap_n - ref| > thr
+__device__ __forceinline__ uint32_t lbsp_thr(const uint32_t v[4], uint32_t ref, uint32_t thr) {
+    const uint32_t r4 = ref * 0x01010101u, t4 = thr * 0x01010101u;
+    uint32_t d = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t m = __vcmpgtu4(__vabsdiffu4(v[j], r4), t4);
+        d |= (((m & 0x80808080u) * 0x00204081u) >> 28) << (4 * j);
+    }
+    return d;
+}
+
+__device__ __forceinline__ void clamp_xy(int& x, int& y, int W, int H) {
+    if (x < kBorder) x = kBorder;
+    else if (x >= W - kBorder) x = W - kBorder - 1;
+    if (y < kBorder) y = kBorder;
+    else if (y >= H - kBorder) y = H - kBorder - 1;
+}
+
+__device__ __forceinline__ float fmin_std(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float fmax_std(float a, float b) { return (a < b) ? b : a; }
+
+struct FrameK {
+    float fLT, fST, t_lo, t_hi;
+    uint32_t frame;  // frame index of this tick (m_nFrameIdx after ++)
+    int cur, nxt;
+    int cooldown;  // m_nModelResetCooldown != 0
+    int use3x3;
+};
+__device__ __forceinline__ FrameK frame_consts(const StreamDev& S) {
+    const StreamCtl* ctl = S.ctl;
+    FrameK F;
+    const unsigned long long f = ctl->frame_idx + 1ull;
+    const unsigned long long nlt = (unsigned long long)S.nmv, nst = (unsigned long long)(S.nmv / 4);
+    F.fLT = 1.0f / (float)(f < nlt ? f : nlt);
+    F.fST = 1.0f / (float)(f < nst ? f : nst);
+    F.frame = (uint32_t)f;
+    F.cur = (int)(ctl->frame_idx & 1ull);
+    F.nxt = F.cur ^ 1;
+    F.cooldown = ctl->cooldown != 0ull;
+    F.t_lo = ctl->t_lo;
+    F.t_hi = ctl->t_hi;
+    F.use3x3 = ctl->use3x3;
+    return F;
+}
+
+// one override of a sample read: an earlier pixel's neighbour update of this pixel
+struct Ovr {
+    int s;
+    uint32_t col;      // packed colour bytes
+    uint64_t desc;     // packed descriptors
+};
+
+// ------------------------------------------------------------------------------------------
+// per-pixel evaluation: one iteration of the reference's raster loop for pixel p, against the
+// frame-start samples (optionally overridden). Writes the pixel's next-frame maps and returns
+// its intent word. (1ch: BackgroundSubtractorSuBSENSE.cpp:201-330, 3ch: :333-481)
+// ------------------------------------------------------------------------------------------
+template <int C, bool OVR>
+__device__ uint32_t eval_pixel(const StreamDev& S, const FrameK& F, const uint8_t* __restrict__ lut, int x, int y,
+                               int p, const uint32_t (&vals)[C][4], const uint32_t (&curr)[C],
+                               const uint32_t (&intra)[C], const Ovr* ov, int nov, uint64_t ovmask, int& nz,
+                               int& e_out) {
+    const int npx = S.npx;
+    const float* fc = S.fm + (size_t)F.cur * kNumFloatMaps * npx;
+    float* fn = S.fm + (size_t)F.nxt * kNumFloatMaps * npx;
+    float R = fc[FM_R * npx + p];
+    float V = fc[FM_V * npx + p];
+    float T = fc[FM_T * npx + p];
+    const float DL = fc[FM_DLAST * npx + p];
+    float DmLT = fc[FM_DMIN_LT * npx + p];
+    float DmST = fc[FM_DMIN_ST * npx + p];
+    float RwLT = fc[FM_RAW_LT * npx + p];
+    float RwST = fc[FM_RAW_ST * npx + p];
+    const float FnLT = fc[FM_FIN_LT * npx + p];
+    const float FnST = fc[FM_FIN_ST * npx + p];
+    const uint32_t uOld = S.unst[(size_t)F.cur * npx + p];
+    const uint32_t lastFG = S.lastFG[p];
+    const uint32_t blink = S.blinks[p];
+
+    // thresholds from R(x) and the previous unstable flag
+    const uint32_t colThr =
+        (uint32_t)__float2ull_rz(R * (float)S.minColor - (float)((uint32_t)(uOld == 0u) * (uint32_t)S.stabColorOff));
+    const unsigned long long descThr = (1ull << (unsigned)__float2ull_rz(floorf(R + 0.5f))) +
+                                       (unsigned long long)S.descOff + (unsigned long long)uOld * S.descOff;
+    const uint32_t uNew =
+        (R > 3.000f || (RwLT - FnLT) > 0.100f || (RwST - FnST) > 0.100f) ? 1u : 0u;
+
+    const int N = S.N, nreq = S.nreq;
+    int nGood = 0, s = 0;
+    uint32_t minDesc = C == 1 ? 16u : 48u, minSum = C == 1 ? 255u : 765u;
+    if (C == 1) {
+        const uint32_t cthr = colThr / 2u;
+        const uint16_t* sD = (const uint16_t*)S.sD;
+        while (nGood < nreq && s < N) {
+            uint32_t bgc, bgd;
+            if (OVR && ((ovmask >> s) & 1ull)) {
+                int k = nov - 1;
+                while (ov[k].s != s) --k;
+                bgc = ov[k].col & 0xffu;
+                bgd = (uint32_t)(ov[k].desc & 0xffffu);
+            } else {
+                bgc = S.sC[(size_t)s * npx + p];
+                bgd = sD[(size_t)s * npx + p];
+            }
+            const uint32_t colDist = (uint32_t)abs((int)curr[0] - (int)bgc);
+            if (colDist <= cthr) {
+                const uint32_t intraD = __popc(intra[0] ^ bgd);
+                const uint32_t interD = __popc(lbsp_thr(vals[0], bgc, lut[bgc]) ^ bgd);
+                const uint32_t descDist = (intraD + interD) / 2u;
+                if ((unsigned long long)descDist <= descThr) {
+                    uint32_t sumDist = (descDist / 4u) * 15u + colDist;
+                    if (sumDist > 255u) sumDist = 255u;
+                    if (sumDist <= cthr) {
+                        if (minDesc > descDist) minDesc = descDist;
+                        if (minSum > sumDist) minSum = sumDist;
+                        ++nGood;
+                    }
+                }
+            }
+            ++s;
+        }
+    } else {
+        const uint32_t totColThr = colThr * 3u, scThr = totColThr / 2u;
+        const unsigned long long totDescThr = descThr * 3ull;
+        const uint64_t* sD = (const uint64_t*)S.sD;
+        while (nGood < nreq && s < N) {
+            uint64_t d;
+            uint32_t c2 = 0;
+            bool ovr = false;
+            if (OVR && ((ovmask >> s) & 1ull)) {
+                int k = nov - 1;
+                while (ov[k].s != s) --k;
+                d = ov[k].desc | ((uint64_t)(ov[k].col & 0xffffu) << 48);
+                c2 = (ov[k].col >> 16) & 0xffu;
+                ovr = true;
+            } else {
+                d = sD[(size_t)s * npx + p];
+            }
+            uint32_t totDesc = 0, totSum = 0;
+            bool ok = true;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                uint32_t bgc;
+                if (c == 0) bgc = (uint32_t)(d >> 48) & 0xffu;
+                else if (c == 1) bgc = (uint32_t)(d >> 56) & 0xffu;
+                else bgc = ovr ? c2 : (uint32_t)S.sC[(size_t)s * npx + p];
+                const uint32_t bgd = (uint32_t)(d >> (16 * c)) & 0xffffu;
+                const uint32_t colDist = (uint32_t)abs((int)curr[c] - (int)bgc);
+                if (colDist > scThr) {
+                    ok = false;
+                    break;
+                }
+                const uint32_t intraD = __popc(intra[c] ^ bgd);
+                const uint32_t interD = __popc(lbsp_thr(vals[c], bgc, lut[bgc]) ^ bgd);
+                const uint32_t descDist = (intraD + interD) / 2u;
+                uint32_t sumDist = (descDist / 2u) * 15u + colDist;
+                if (sumDist > 255u) sumDist = 255u;
+                if (sumDist > scThr) {
+                    ok = false;
+                    break;
+                }
+                totDesc += descDist;
+                totSum += sumDist;
+            }
+            if (ok && !((unsigned long long)totDesc > totDescThr || totSum > totColThr)) {
+                if (minDesc > totDesc) minDesc = totDesc;
+                if (minSum > totSum) minSum = totSum;
+                ++nGood;
+            }
+            ++s;
+        }
+    }
+    e_out = s;
+
+    // D_last (:254-255 / :396-397): depends on the pixel alone
+    const uint8_t* lc = S.lastCol + (size_t)F.cur * npx * C + (size_t)p * C;
+    const uint16_t* ld = S.lastDesc + (size_t)F.cur * npx * C + (size_t)p * C;
+    uint32_t l1 = 0, hd = 0;
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        l1 += (uint32_t)abs((int)lc[c] - (int)curr[c]);
+        hd += __popc((uint32_t)ld[c] ^ intra[c]);
+    }
+    const float colMax = C == 1 ? 255.0f : 765.0f, descMax = C == 1 ? 16.0f : 48.0f;
+    const float normLast = ((float)l1 / colMax + (float)hd / descMax) / 2;
+    const float DLn = DL * (1.0f - F.fST) + normLast * F.fST;
+
+    uint32_t intent = kInValid | ((uint32_t)s << kInEShift);
+    DrawState ds;
+    ds.blk = 0xffffffffu;
+    const uint32_t seedFrame = F.frame;
+    const bool fg = nGood < nreq;
+    if (fg) {
+        const float md = ((float)minSum / colMax + (float)minDesc / descMax) / 2 + (float)(nreq - nGood) / (float)nreq;
+        const float nmd = fmin_std(1.0f, md);
+        DmLT = DmLT * (1.0f - F.fLT) + nmd * F.fLT;
+        DmST = DmST * (1.0f - F.fST) + nmd * F.fST;
+        RwLT = RwLT * (1.0f - F.fLT) + F.fLT;
+        RwST = RwST * (1.0f - F.fST) + F.fST;
+        intent |= kInFG;
+        if (F.cooldown && (draw_k(S.seed, seedFrame, (uint32_t)p, 0u, ds) % 2u) == 0u) {
+            const uint32_t so = draw_k(S.seed, seedFrame, (uint32_t)p, 1u, ds) % (uint32_t)N;
+            intent |= kInOwn | (so << kInSOwnShift);
+        }
+    } else {
+        const float nmd = ((float)minSum / colMax + (float)minDesc / descMax) / 2;
+        DmLT = DmLT * (1.0f - F.fLT) + nmd * F.fLT;
+        DmST = DmST * (1.0f - F.fST) + nmd * F.fST;
+        RwLT = RwLT * (1.0f - F.fLT);
+        RwST = RwST * (1.0f - F.fST);
+        const unsigned long long nLR = S.lrMode ? S.lrFixed : (unsigned long long)__float2ull_rz(ceilf(T));
+        uint32_t k = 0;
+        if (mod_draw(draw_k(S.seed, seedFrame, (uint32_t)p, k++, ds), nLR) == 0ull) {
+            const uint32_t so = draw_k(S.seed, seedFrame, (uint32_t)p, k++, ds) % (uint32_t)N;
+            intent |= kInOwn | (so << kInSOwnShift);
+        }
+        const bool use3 = F.use3x3 && !uNew;
+        const uint32_t rn = draw_k(S.seed, seedFrame, (uint32_t)p, k++, ds);
+        int nx, ny;
+        if (use3) {
+            const int r = (int)(rn % 8u);
+            nx = x + c_nb3[r][0];
+            ny = y + c_nb3[r][1];
+        } else {
+            const int r = (int)(rn % 24u);
+            nx = x + c_nb5[r][0];
+            ny = y + c_nb5[r][1];
+        }
+        clamp_xy(nx, ny, S.W, S.H);
+        const uint32_t code = (uint32_t)((ny - y + 2) * 5 + (nx - x + 2));
+        const uint32_t nrand = draw_k(S.seed, seedFrame, (uint32_t)p, k++, ds);
+        const unsigned long long X = use3 ? nLR : (nLR / 2ull + 1ull);
+        uint32_t st;
+        if (mod_draw(nrand, X) == 0ull) st = NB_WRITE;
+        else if (mod_draw(nrand, (unsigned long long)__float2ull_rz(F.t_lo)) == 0ull) st = NB_PENDING;
+        else st = NB_NO;
+        const uint32_t snb = draw_k(S.seed, seedFrame, (uint32_t)p, k, ds) % (uint32_t)N;
+        intent |= (code << kInCodeShift) | (st << kInNStShift) | (snb << kInSNbShift);
+    }
+
+    // feedback: T (:302-311), v (:312-318), R (:319-325)
+    const float mn = fmin_std(DmLT, DmST), mx = fmax_std(DmLT, DmST);
+    if (lastFG || (mn < 0.100f && fg)) {
+        if (T < F.t_hi) T += 0.5000f / (mx * V);
+    } else if (T > F.t_lo) {
+        T -= 0.2500f * V / mx;
+    }
+    if (T < F.t_lo) T = F.t_lo;
+    else if (T > F.t_hi) T = F.t_hi;
+    if (mx > 0.100f && blink) {
+        V += 1.000f;
+    } else if (V > 0.100f) {
+        V -= lastFG ? 0.100f / 4 : uNew ? 0.100f / 2 : 0.100f;
+        if (V < 0.100f) V = 0.100f;
+    }
+    // R < pow(1+2*min, 2) is evaluated in double by the reference; x*x of a float is exact in
+    // double, so compare exactly with the two-product split hi + lo of x*x
+    const float rx = 1.0f + mn * 2;
+    const float hi = rx * rx;
+    const float lo = fmaf(rx, rx, -hi);
+    if (R < hi || (R == hi && lo > 0.0f)) {
+        R += 0.01f * (V - 0.100f);
+    } else {
+        R -= 0.01f / V;
+        if (R < 1.0f) R = 1.0f;
+    }
+    uint32_t pc = 0;
+#pragma unroll
+    for (int c = 0; c < C; ++c) pc += __popc(intra[c]);
+    nz = pc >= (C == 1 ? 2u : 4u) ? 1 : 0;
+
+    fn[FM_R * npx + p] = R;
+    fn[FM_V * npx + p] = V;
+    fn[FM_T * npx + p] = T;
+    __stcg(&fn[FM_DLAST * npx + p], DLn);
+    fn[FM_DMIN_LT * npx + p] = DmLT;
+    fn[FM_DMIN_ST * npx + p] = DmST;
+    fn[FM_RAW_LT * npx + p] = RwLT;
+    __stcg(&fn[FM_RAW_ST * npx + p], RwST);
+    S.unst[(size_t)F.nxt * npx + p] = (uint8_t)uNew;
+    uint8_t* lcn = S.lastCol + (size_t)F.nxt * npx * C + (size_t)p * C;
+    uint16_t* ldn = S.lastDesc + (size_t)F.nxt * npx * C + (size_t)p * C;
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        lcn[c] = (uint8_t)curr[c];
+        __stcg(&ldn[c], (uint16_t)intra[c]);
+    }
+    return intent;
+}
+
+// gathers the 16 LBSP taps of channel c at (x, y) from a byte image (tile or frame)
+template <int C>
+__device__ __forceinline__ void gather_taps(const uint8_t* base, int rowStride, int c, uint32_t (&v)[4]) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        uint32_t w = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int n = j * 4 + i;
+            w |= (uint32_t)base[c_lbsp_dy[n] * rowStride + c_lbsp_dx[n] * C + c] << (8 * i);
+        }
+        v[j] = w;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// phase A: evaluate every pixel of a tile against the frame-start model
+// ------------------------------------------------------------------------------------------
+template <int C>
+__device__ void phaseA_tile(const TickParams& P, const StreamDev& S, int lt, uint8_t* smem) {
+    const int tx = lt % S.tilesX, ty = lt / S.tilesX;
+    const int x0 = tx * kTileW, y0 = ty * kTileH;
+    constexpr int RW = (kTileW + 2 * kBorder) * C;  // tile row bytes incl. halo
+    constexpr int RH = kTileH + 2 * kBorder;
+    uint8_t* tile = smem;
+    uint8_t* lut = smem + RW * RH;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = S.ctl->lut[i];
+    for (int i = threadIdx.x; i < RW * RH; i += blockDim.x) {
+        const int r = i / RW, cb = i % RW;
+        const int gy = y0 - kBorder + r, gx = x0 - kBorder + cb / C;
+        tile[i] = (gy >= 0 && gy < S.H && gx >= 0 && gx < S.W) ? __ldg(S.frame + ((size_t)gy * S.W + gx) * C + cb % C) : 0;
+    }
+    __syncthreads();
+    const FrameK F = frame_consts(S);
+    const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
+    const int x = x0 + lx, y = y0 + ly;
+    int nz = 0, e = 0;
+    if (x < S.W && y < S.H) {
+        const int p = y * S.W + x;
+        uint32_t intent = 0;
+        if (S.roi[p]) {
+            const uint8_t* base = tile + (ly + kBorder) * RW + (lx + kBorder) * C;
+            uint32_t vals[C][4], curr[C], intra[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                gather_taps<C>(base, RW, c, vals[c]);
+                curr[c] = base[c];
+                intra[c] = lbsp_thr(vals[c], curr[c], lut[curr[c]]);
+            }
+            intent = eval_pixel<C, false>(S, F, lut, x, y, p, vals, curr, intra, nullptr, 0, 0ull, nz, e);
+        }
+        __stcg(&S.intent[p], intent);
+    }
+    // per-tile reductions of the non-zero descriptor count and of the samples evaluated
+    for (int o = 16; o > 0; o >>= 1) {
+        nz += __shfl_xor_sync(0xffffffffu, nz, o);
+        e += __shfl_xor_sync(0xffffffffu, e, o);
+    }
+    if ((threadIdx.x & 31) == 0 && (nz || e)) {
+        if (nz) atomicAdd(&S.ctl->nz_acc, (unsigned long long)nz);
+        if (e) atomicAdd(&S.ctl->st_samples, (unsigned long long)e);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// list helpers for the repair loop
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ void push_item(unsigned long long* list, unsigned int* count, unsigned int cap,
+                                          uint32_t* stamps, uint32_t stamp, int si, int p, TickWork* w) {
+    if (atomicExch(&stamps[p], stamp) == stamp) return;
+    const unsigned int i = atomicAdd(count, 1u);
+    if (i < cap) list[i] = ((unsigned long long)si << 40) | (unsigned long long)(unsigned)p;
+    else atomicOr(&w->err, ERR_REPAIR_LIMIT);
+}
+
+// target pixel of a neighbour code relative to (x, y)
+__device__ __forceinline__ int code_target(int code, int x, int y, int W) {
+    const int dy = code / 5 - 2, dx = code % 5 - 2;
+    return (y + dy) * W + (x + dx);
+}
+
+// ghost test of pixel p's neighbour update (:292-295 / :438-441), reading the target's values as
+// the raster scan would: this frame's value when the target precedes (or is) p, else the previous
+// frame's
+__device__ __forceinline__ uint32_t resolve_ghost(const StreamDev& S, const FrameK& F, int p, int q) {
+    const int npx = S.npx;
+    const int buf = (q <= p) ? F.nxt : F.cur;
+    const float* fb = S.fm + (size_t)buf * kNumFloatMaps * npx;
+    const float qD = __ldcg(&fb[FM_DLAST * npx + q]);
+    const float qR = __ldcg(&fb[FM_RAW_ST * npx + q]);
+    return (qR > 0.995f && qD < 0.010f) ? NB_GHOST_WRITE : NB_GHOST_NO;
+}
+
+__device__ __forceinline__ uint32_t set_nst(uint32_t w, uint32_t st) {
+    return (w & ~(7u << kInNStShift)) | (st << kInNStShift);
+}
+
+// phase B: resolve pending ghost tests with the phase-A values; mark the pixels whose evaluated
+// samples an earlier pixel overwrites (initial repair frontier)
+__device__ void phaseB_tile(const TickParams& P, int si, const StreamDev& S, int lt) {
+    const int tx = lt % S.tilesX, ty = lt / S.tilesX;
+    const int x = tx * kTileW + threadIdx.x % kTileW, y = ty * kTileH + threadIdx.x / kTileW;
+    if (x >= S.W || y >= S.H) return;
+    const int p = y * S.W + x;
+    uint32_t w = __ldcg(&S.intent[p]);
+    if (!(w & kInValid)) return;
+    const FrameK F = frame_consts(S);
+    if (in_nst(w) == NB_PENDING) {
+        const int q = code_target((int)in_code(w), x, y, S.W);
+        w = set_nst(w, resolve_ghost(S, F, p, q));
+        __stcg(&S.intent[p], w);
+    }
+    if (in_nb_writes(w)) {
+        const int q = code_target((int)in_code(w), x, y, S.W);
+        if (q > p) {
+            const uint32_t wq = __ldcg(&S.intent[q]);
+            if ((wq & kInValid) && in_snb(w) < in_e(wq))
+                push_item(P.dlist[0], &P.work->dcount[0], P.listCap, S.stampD, S.ctl->stamp_base + 1u, si, q, P.work);
+        }
+    }
+}
+
+// frame down-sampling for the frame-level analysis (:568-584): one output pixel per thread
+__device__ void ds_item(const StreamDev& S, int i) {
+    const int C = S.C;
+    const int dx = i % S.dsW, dy = i / S.dsW;
+    const FrameK F = frame_consts(S);
+    const float scale = 1.f / (float)(S.dsSX * S.dsSY);
+    uint32_t dmax = 0;
+    for (int c = 0; c < C; ++c) {
+        int sum = 0;
+        for (int yy = 0; yy < S.dsSY; ++yy) {
+            const uint8_t* row = S.frame + ((size_t)(dy * S.dsSY + yy) * S.W + (size_t)dx * S.dsSX) * C + c;
+            for (int xx = 0; xx < S.dsSX; ++xx) sum += __ldg(row + xx * C);
+        }
+        int v = __float2int_rn((float)sum * scale);
+        v = v < 0 ? 0 : v > 255 ? 255 : v;
+        const size_t k = (size_t)i * C + c;
+        // accumulateWeighted: dst = src*a + dst*(1-a)
+        const float aL = F.fLT, bL = 1.0f - aL, aS = F.fST, bS = 1.0f - aS;
+        const float lt = (float)v * aL + S.dsLT[k] * bL;
+        const float st = (float)v * aS + S.dsST[k] * bS;
+        S.dsLT[k] = lt;
+        S.dsST[k] = st;
+        const uint32_t d = (uint32_t)__float2ull_rz(fabsf(st - lt));
+        if (C == 1) dmax = d / 2u;
+        else dmax = c == 0 ? d : (d > dmax ? d : dmax);
+    }
+    // reference order: max(d0, max(d1, d2)) -- identical to the running max for integers
+    if (dmax) atomicAdd(&S.ctl->colordiff_acc, (unsigned long long)dmax);
+}
+
+// ------------------------------------------------------------------------------------------
+// repair loop bodies
+// ------------------------------------------------------------------------------------------
+template <int C>
+__device__ void rematch_item(const TickParams& P, int si, const StreamDev& S, int q, uint32_t stampNext,
+                             int iterParity) {
+    const int W = S.W, x = q % W, y = q / W;
+    const FrameK F = frame_consts(S);
+    const uint32_t wOld = __ldcg(&S.intent[q]);
+    if (!(wOld & kInValid)) return;
+    // overrides: earlier pixels of the 5x5 window whose neighbour update targets q, raster order
+    Ovr ov[12];
+    int nov = 0;
+    uint64_t mask = 0;
+    for (int dy = -2; dy <= 0; ++dy)
+        for (int dx = -2; dx <= 2; ++dx) {
+            if (dy == 0 && dx >= 0) break;
+            const int px = x + dx, py = y + dy;
+            if (px < 0 || px >= W || py < 0) continue;
+            const int p = py * W + px;
+            const uint32_t w = __ldcg(&S.intent[p]);
+            if (!in_nb_writes(w) || (int)in_code(w) != (-dy + 2) * 5 + (-dx + 2)) continue;
+            const int sn = (int)in_snb(w);
+            uint32_t col = 0;
+            uint64_t desc = 0;
+            const uint16_t* ldn = S.lastDesc + (size_t)F.nxt * S.npx * C + (size_t)p * C;
+            for (int c = 0; c < C; ++c) {
+                col |= (uint32_t)__ldg(S.frame + (size_t)p * C + c) << (8 * c);
+                desc |= (uint64_t)__ldcg(&ldn[c]) << (16 * c);
+            }
+            int k = 0;
+            while (k < nov && ov[k].s != sn) ++k;
+            if (k == nov) ++nov;
+            ov[k].s = sn;
+            ov[k].col = col;
+            ov[k].desc = desc;
+            mask |= 1ull << sn;
+        }
+    // order matters only within one sample index (last writer wins); entries with distinct s are
+    // independent, and an overwritten entry keeps its slot but takes the latest writer's values
+    uint32_t vals[C][4], curr[C], intra[C];
+    const uint8_t* base = S.frame + (size_t)q * C;
+    for (int c = 0; c < C; ++c) {
+        for (int j = 0; j < 4; ++j) {
+            uint32_t wv = 0;
+            for (int i = 0; i < 4; ++i) {
+                const int n = j * 4 + i;
+                wv |= (uint32_t)__ldg(base + (c_lbsp_dy[n] * W + c_lbsp_dx[n]) * C + c) << (8 * i);
+            }
+            vals[c][j] = wv;
+        }
+        curr[c] = __ldg(base + c);
+        intra[c] = lbsp_thr(vals[c], curr[c], S.ctl->lut[curr[c]]);
+    }
+    atomicAdd(&S.ctl->st_rematched, 1ull);
+    int nz = 0, e = 0;
+    uint32_t wNew = eval_pixel<C, true>(S, F, S.ctl->lut, x, y, q, vals, curr, intra, ov, nov, mask, nz, e);
+    const bool decChanged = ((wNew ^ wOld) & kInFG) != 0u;
+    if (!decChanged) {
+        // same decision: same draws, same updates; keep the resolved neighbour state
+        wNew = (wOld & ~(127u << kInEShift)) | ((uint32_t)e << kInEShift);
+        __stcg(&S.intent[q], wNew);
+        return;
+    }
+    __stcg(&S.intent[q], wNew);
+    unsigned int* dcnt = &P.work->dcount[iterParity ^ 1];
+    unsigned long long* dl = P.dlist[iterParity ^ 1];
+    // the write that disappeared or appeared changes what its (later) target reads
+    if (in_nb_writes(wOld)) {
+        const int t = code_target((int)in_code(wOld), x, y, W);
+        if (t > q) push_item(dl, dcnt, P.listCap, S.stampD, stampNext, si, t, P.work);
+    }
+    if (in_nb_writes(wNew)) {
+        const int t = code_target((int)in_code(wNew), x, y, W);
+        if (t > q) push_item(dl, dcnt, P.listCap, S.stampD, stampNext, si, t, P.work);
+    }
+    // the raw-segmentation value of q changed: re-resolve ghost tests that read it (q itself and
+    // later pixels of its 5x5 window), and q's own new pending test
+    unsigned long long* rl = P.rlist[iterParity];
+    unsigned int* rcnt = &P.work->rcount[iterParity];
+    const uint32_t rstamp = stampNext;  // separate stamp array: one generation per iteration
+    for (int dy = 0; dy <= 2; ++dy)
+        for (int dx = -2; dx <= 2; ++dx) {
+            if (dy == 0 && dx < 0) continue;
+            const int px = x + dx, py = y + dy;
+            if (px < 0 || px >= W || py >= S.H) continue;
+            const int p = py * W + px;
+            const uint32_t w = (p == q) ? wNew : __ldcg(&S.intent[p]);
+            if (in_ghost(w) && code_target((int)in_code(w), px, py, W) == q)
+                push_item(rl, rcnt, P.listCap, S.stampR, rstamp, si, p, P.work);
+        }
+    if (in_nst(wNew) == NB_PENDING) push_item(rl, rcnt, P.listCap, S.stampR, rstamp, si, q, P.work);
+}
+
+__device__ void reresolve_item(const TickParams& P, int si, const StreamDev& S, int p, uint32_t stampNext,
+                               int iterParity) {
+    const int W = S.W, x = p % W, y = p / W;
+    const uint32_t w = __ldcg(&S.intent[p]);
+    if (!in_ghost(w)) return;
+    const FrameK F = frame_consts(S);
+    const int q = code_target((int)in_code(w), x, y, W);
+    const uint32_t st = resolve_ghost(S, F, p, q);
+    const uint32_t old = in_nst(w);
+    if (st == old) return;
+    __stcg(&S.intent[p], set_nst(w, st));
+    // readers during the last re-match pass saw PENDING as "no write"
+    const bool wroteBefore = old == NB_GHOST_WRITE, writesNow = st == NB_GHOST_WRITE;
+    if (wroteBefore != writesNow && q > p)
+        push_item(P.dlist[iterParity ^ 1], &P.work->dcount[iterParity ^ 1], P.listCap, S.stampD, stampNext, si, q,
+                  P.work);
+}
+
+// ------------------------------------------------------------------------------------------
+// phase F: commit the sample writes of the frame in raster order, the draw counters, the blink
+// maps and the 3x3 closing (:536-540); initializes the union-find labels of the hole filling
+// ------------------------------------------------------------------------------------------
+template <int C>
+__device__ void phaseF_tile(const TickParams& P, const StreamDev& S, int lt, uint8_t* smem) {
+    const int tx = lt % S.tilesX, ty = lt / S.tilesX;
+    const int x0 = tx * kTileW, y0 = ty * kTileH;
+    constexpr int IW = kTileW + 4, IH = kTileH + 4;  // intents with a 2-pixel halo
+    uint32_t* it = (uint32_t*)smem;
+    uint8_t* dil = smem + IW * IH * 4;  // (kTileW+2) x (kTileH+2) dilated raw mask
+    const int W = S.W, H = S.H, npx = S.npx;
+    for (int i = threadIdx.x; i < IW * IH; i += blockDim.x) {
+        const int gy = y0 - 2 + i / IW, gx = x0 - 2 + i % IW;
+        it[i] = (gy >= 0 && gy < H && gx >= 0 && gx < W) ? __ldcg(&S.intent[gy * W + gx]) : 0u;
+    }
+    __syncthreads();
+    // 3x3 dilation of the raw mask (out-of-frame pixels never win)
+    for (int i = threadIdx.x; i < (kTileW + 2) * (kTileH + 2); i += blockDim.x) {
+        const int ry = i / (kTileW + 2), rx = i % (kTileW + 2);
+        uint32_t v = 0;
+        for (int dy = 0; dy < 3; ++dy)
+            for (int dx = 0; dx < 3; ++dx) v |= it[(ry + dy) * IW + rx + dx] & kInFG;
+        dil[i] = v ? 255 : 0;
+    }
+    __syncthreads();
+    const FrameK F = frame_consts(S);
+    const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
+    const int x = x0 + lx, y = y0 + ly;
+    int nw = 0;
+    if (x < W && y < H) {
+        const int q = y * W + x;
+        // raster-ordered commit of every write targeting q (own write before own neighbour write)
+        for (int dy = -2; dy <= 2; ++dy)
+            for (int dx = -2; dx <= 2; ++dx) {
+                const uint32_t w = it[(ly + 2 + dy) * IW + lx + 2 + dx];
+                if (!(w & kInValid)) continue;
+                const int px = x + dx, py = y + dy;
+                const int p = py * W + px;
+                for (int pass = 0; pass < 2; ++pass) {
+                    int s;
+                    if (pass == 0) {
+                        if (dx != 0 || dy != 0 || !(w & kInOwn)) continue;
+                        s = (int)in_sown(w);
+                    } else {
+                        if (!in_nb_writes(w) || (int)in_code(w) != (-dy + 2) * 5 + (-dx + 2)) continue;
+                        s = (int)in_snb(w);
+                    }
+                    const uint16_t* ldn = S.lastDesc + (size_t)F.nxt * npx * C + (size_t)p * C;
+                    if (C == 3) {
+                        const uint64_t d = (uint64_t)__ldcg(&ldn[0]) | ((uint64_t)__ldcg(&ldn[1]) << 16) |
+                                           ((uint64_t)__ldcg(&ldn[2]) << 32) |
+                                           ((uint64_t)__ldg(S.frame + (size_t)p * 3) << 48) |
+                                           ((uint64_t)__ldg(S.frame + (size_t)p * 3 + 1) << 56);
+                        ((uint64_t*)S.sD)[(size_t)s * npx + q] = d;
+                        S.sC[(size_t)s * npx + q] = __ldg(S.frame + (size_t)p * 3 + 2);
+                    } else {
+                        ((uint16_t*)S.sD)[(size_t)s * npx + q] = __ldcg(&ldn[0]);
+                        S.sC[(size_t)s * npx + q] = __ldg(S.frame + p);
+                    }
+                    ++nw;
+                }
+            }
+        const uint32_t wq = it[(ly + 2) * IW + lx + 2];
+        uint16_t kend = 0;
+        if (wq & kInValid) {
+            if (wq & kInFG) kend = F.cooldown ? (uint16_t)(1 + ((wq & kInOwn) ? 1 : 0)) : 0;
+            else kend = (uint16_t)(1 + ((wq & kInOwn) ? 1 : 0) + 2 + (in_nb_writes(wq) ? 1 : 0));
+        }
+        S.kctr[q] = kend;
+        // blinks (:536-539)
+        const uint8_t raw = (wq & kInFG) ? 255 : 0;
+        const uint8_t cb = raw ^ S.lastRawFG[q];
+        S.blinks[q] = cb | S.lastRawBlink[q];
+        S.lastRawBlink[q] = cb;
+        S.lastRawFG[q] = raw;
+        // closing: erosion of the dilated mask (out-of-frame pixels never win)
+        uint8_t v = 255;
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int gx = x + dx, gy = y + dy;
+                if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+                v &= dil[(ly + 1 + dy) * (kTileW + 2) + lx + 1 + dx];
+            }
+        __stcg(&S.preflood[q], v);
+    }
+    for (int o = 16; o > 0; o >>= 1) nw += __shfl_xor_sync(0xffffffffu, nw, o);
+    if ((threadIdx.x & 31) == 0 && nw) atomicAdd(&S.ctl->st_writes, (unsigned long long)nw);
+}
+
+// ------------------------------------------------------------------------------------------
+// hole filling: cv::floodFill from (0,0) on the closed mask, rebuilt as border-seeded union-find.
+// The closed mask is 0 on the 2-pixel frame border (no ROI pixel lies there), so the component of
+// 0-pixels that contains pixel 0 is exactly the flood-filled region; with minimum-index roots its
+// root is 0, and holes are the 0-pixels whose root is not 0.
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ int uf_find(int* L, int a, TickWork* w) {
+    int n, it = 0;
+    while ((n = __ldcg(&L[a])) != a) {
+        a = n;
+        if (++it > kUFLimit) {
+            atomicOr(&w->err, ERR_UF_LIMIT);
+            break;
+        }
+    }
+    return a;
+}
+__device__ void uf_union(int* L, int a, int b, TickWork* w) {
+    for (int it = 0; it < kUFLimit; ++it) {
+        a = uf_find(L, a, w);
+        b = uf_find(L, b, w);
+        if (a == b) return;
+        if (a < b) {
+            const int old = atomicMin(&L[b], a);
+            if (old == b) return;
+            b = old;
+        } else {
+            const int old = atomicMin(&L[a], b);
+            if (old == a) return;
+            a = old;
+        }
+    }
+    atomicOr(&w->err, ERR_UF_LIMIT);
+}
+
+// P2a: tile-local union-find in shared memory, written as global labels (local roots)
+__device__ void phaseP2a_tile(const TickParams& P, const StreamDev& S, int lt, uint8_t* smem) {
+    const int tx = lt % S.tilesX, ty = lt / S.tilesX;
+    const int x0 = tx * kTileW, y0 = ty * kTileH;
+    volatile int* lab = (volatile int*)smem;
+    uint8_t* zero = smem + kThreads * 4;
+    const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
+    const int x = x0 + lx, y = y0 + ly;
+    const bool in = x < S.W && y < S.H;
+    const int q = y * S.W + x;
+    const bool z = in && __ldcg(&S.preflood[q]) == 0;
+    zero[threadIdx.x] = z;
+    lab[threadIdx.x] = z ? (int)threadIdx.x : -1;
+    __syncthreads();
+    for (int dir = 0; dir < 2; ++dir) {
+        const int nb = dir == 0 ? (lx + 1 < kTileW ? (int)threadIdx.x + 1 : -1) : (ly + 1 < kTileH ? (int)threadIdx.x + kTileW : -1);
+        if (z && nb >= 0 && zero[nb]) {
+            int a = threadIdx.x, b = nb;
+            for (int it = 0; it < 4096; ++it) {
+                while (lab[a] != a) a = lab[a];
+                while (lab[b] != b) b = lab[b];
+                if (a == b) break;
+                if (a < b) {
+                    const int old = atomicMin((int*)&lab[b], a);
+                    if (old == b) break;
+                    b = old;
+                } else {
+                    const int old = atomicMin((int*)&lab[a], b);
+                    if (old == a) break;
+                    a = old;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (in) {
+        int label = -1;
+        if (z) {
+            int a = threadIdx.x;
+            while (lab[a] != a) a = lab[a];
+            label = (y0 + a / kTileW) * S.W + x0 + a % kTileW;
+        }
+        __stcg(&S.label[q], label);
+    }
+}
+
+// P2b: unions across the right and bottom tile edges
+__device__ void phaseP2b_tile(const TickParams& P, const StreamDev& S, int lt) {
+    const int tx = lt % S.tilesX, ty = lt / S.tilesX;
+    const int x0 = tx * kTileW, y0 = ty * kTileH;
+    const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
+    const int x = x0 + lx, y = y0 + ly;
+    if (x >= S.W || y >= S.H) return;
+    const int q = y * S.W + x;
+    if (__ldcg(&S.preflood[q]) != 0) return;
+    if (lx == kTileW - 1 && x + 1 < S.W && __ldcg(&S.preflood[q + 1]) == 0) uf_union(S.label, q, q + 1, P.work);
+    if (ly == kTileH - 1 && y + 1 < S.H && __ldcg(&S.preflood[q + S.W]) == 0) uf_union(S.label, q, q + S.W, P.work);
+}
+
+// P2c + P3: holes, 3-fold erosion of the closed mask, and mask |= holes | eroded (:541-546)
+__device__ void phaseP2c_tile(const TickParams& P, const StreamDev& S, int lt, uint8_t* smem) {
+    const int tx = lt % S.tilesX, ty = lt / S.tilesX;
+    const int x0 = tx * kTileW, y0 = ty * kTileH;
+    constexpr int HW = kTileW + 6, HH = kTileH + 6;
+    uint8_t* pf = smem;
+    uint8_t* rowmin = smem + HW * HH;
+    const int W = S.W, H = S.H;
+    for (int i = threadIdx.x; i < HW * HH; i += blockDim.x) {
+        const int gy = y0 - 3 + i / HW, gx = x0 - 3 + i % HW;
+        pf[i] = (gy >= 0 && gy < H && gx >= 0 && gx < W) ? __ldcg(&S.preflood[gy * W + gx]) : 255;  // never wins
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kTileW * HH; i += blockDim.x) {
+        const int ry = i / kTileW, rx = i % kTileW;
+        uint8_t v = 255;
+        for (int d = 0; d < 7; ++d) v = min(v, pf[ry * HW + rx + d]);
+        rowmin[i] = v;
+    }
+    __syncthreads();
+    const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
+    const int x = x0 + lx, y = y0 + ly;
+    if (x >= W || y >= H) return;
+    const int q = y * W + x;
+    uint8_t er = 255;
+    for (int d = 0; d < 7; ++d) er = min(er, rowmin[(ly + d) * kTileW + lx]);
+    uint8_t hole = 0;
+    if (pf[(ly + 3) * HW + lx + 3] == 0) {
+        const int root = uf_find(S.label, __ldcg(&S.label[q]), P.work);
+        hole = root != 0 ? 255 : 0;
+    }
+    const uint8_t raw = (__ldcg(&S.intent[q]) & kInFG) ? 255 : 0;
+    __stcg(&S.combined[q], (uint8_t)(raw | hole | er));
+    if (q == 0 && pf[3 * HW + 3] != 0) atomicOr(&P.work->err, ERR_RING);
+}
+
+// P4: median blur (binary majority, replicate border) -> final mask; final-segmentation EMAs
+// via addWeighted (:547, :552-554)
+__device__ void phaseP4_tile(const TickParams& P, const StreamDev& S, int lt, uint8_t* smem) {
+    const int tx = lt % S.tilesX, ty = lt / S.tilesX;
+    const int x0 = tx * kTileW, y0 = ty * kTileH;
+    const int k = S.ctl->median_k, r = k / 2;
+    const int HW = kTileW + 2 * r, HH = kTileH + 2 * r;
+    uint8_t* cm = smem;
+    uint8_t* colcnt = smem + HW * HH;
+    const int W = S.W, H = S.H, npx = S.npx;
+    for (int i = threadIdx.x; i < HW * HH; i += blockDim.x) {
+        int gy = y0 - r + i / HW, gx = x0 - r + i % HW;
+        gy = gy < 0 ? 0 : gy >= H ? H - 1 : gy;
+        gx = gx < 0 ? 0 : gx >= W ? W - 1 : gx;
+        cm[i] = __ldcg(&S.combined[gy * W + gx]) ? 1 : 0;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kTileH * HW; i += blockDim.x) {
+        const int ry = i / HW, rx = i % HW;
+        int c = 0;
+        for (int d = 0; d < k; ++d) c += cm[(ry + d) * HW + rx];
+        colcnt[i] = (uint8_t)c;
+    }
+    __syncthreads();
+    const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
+    const int x = x0 + lx, y = y0 + ly;
+    if (x >= W || y >= H) return;
+    const int q = y * W + x;
+    int cnt = 0;
+    for (int d = 0; d < k; ++d) cnt += colcnt[ly * HW + lx + d];
+    const uint8_t fgv = (2 * cnt > k * k) ? 255 : 0;
+    __stcg(&S.lastFG[q], fgv);
+    if (S.maskOut) S.maskOut[q] = fgv;
+    const FrameK F = frame_consts(S);
+    const float* fc = S.fm + (size_t)F.cur * kNumFloatMaps * npx;
+    float* fn = S.fm + (size_t)F.nxt * kNumFloatMaps * npx;
+    const float aL = 1.0f - F.fLT, bL = (float)((1.0 / 255) * (double)F.fLT);
+    const float aS = 1.0f - F.fST, bS = (float)((1.0 / 255) * (double)F.fST);
+    const float m = (float)fgv;
+    fn[FM_FIN_LT * npx + q] = (fc[FM_FIN_LT * npx + q] * aL + m * bL) + 0.0f;
+    fn[FM_FIN_ST * npx + q] = (fc[FM_FIN_ST * npx + q] * aS + m * bS) + 0.0f;
+}
+
+// P5: 3-fold dilation of the final mask and blink masking with the previous and the new inverted
+// dilated masks (:548-551)
+__device__ void phaseP5_tile(const TickParams& P, const StreamDev& S, int lt, uint8_t* smem) {
+    const int tx = lt % S.tilesX, ty = lt / S.tilesX;
+    const int x0 = tx * kTileW, y0 = ty * kTileH;
+    constexpr int HW = kTileW + 6, HH = kTileH + 6;
+    uint8_t* fgm = smem;
+    uint8_t* rowmax = smem + HW * HH;
+    const int W = S.W, H = S.H;
+    for (int i = threadIdx.x; i < HW * HH; i += blockDim.x) {
+        const int gy = y0 - 3 + i / HW, gx = x0 - 3 + i % HW;
+        fgm[i] = (gy >= 0 && gy < H && gx >= 0 && gx < W) ? __ldcg(&S.lastFG[gy * W + gx]) : 0;  // never wins
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kTileW * HH; i += blockDim.x) {
+        const int ry = i / kTileW, rx = i % kTileW;
+        uint8_t v = 0;
+        for (int d = 0; d < 7; ++d) v = max(v, fgm[ry * HW + rx + d]);
+        rowmax[i] = v;
+    }
+    __syncthreads();
+    const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
+    const int x = x0 + lx, y = y0 + ly;
+    if (x >= W || y >= H) return;
+    const int q = y * W + x;
+    uint8_t dv = 0;
+    for (int d = 0; d < 7; ++d) dv = max(dv, rowmax[(ly + d) * kTileW + lx]);
+    const uint8_t inv = (uint8_t)~dv;
+    S.blinks[q] = (uint8_t)(S.blinks[q] & S.dilInv[q] & inv);
+    S.dilInv[q] = inv;
+}
+
+// frame-level epilogue of one stream (:555-611): LBSP threshold LUT adaptation, camera-motion
+// analysis, automatic model reset decision and learning-rate caps
+__device__ void stream_epilogue(const TickParams& P, const StreamDev& S) {
+    StreamCtl* ctl = S.ctl;
+    const float relThr = S.relThr;
+    const unsigned int lbspOff = S.lbspOff;
+    const unsigned long long nz = ctl->nz_acc;
+    ctl->last_nz = nz;
+    ctl->nz_acc = 0;
+    const float ratio = __ull2float_rn(nz) / __ull2float_rn(ctl->n_rel);
+    const float last = ctl->last_nz_ratio;
+    if (ratio < 0.100f && last < 0.100f) {
+        for (int t = 0; t <= 255; ++t) {
+            const float v = ceilf((float)t * relThr / 4) + (float)lbspOff;
+            const int lim = v > 255.0f ? 255 : (int)v;
+            if ((int)ctl->lut[t] > lim) --ctl->lut[t];
+        }
+    } else if (ratio > 0.500f && last > 0.500f) {
+        int lim = __float2int_rn((float)lbspOff + 255 * relThr);
+        lim = lim < 0 ? 0 : lim > 255 ? 255 : lim;
+        for (int t = 0; t <= 255; ++t)
+            if ((int)ctl->lut[t] < lim) ++ctl->lut[t];
+    }
+    ctl->last_nz_ratio = ratio;
+    ctl->refresh_pending = 0;
+    ctl->ksent = 0;
+    ctl->last_colordiff = 0;
+    if (ctl->lr_scaling) {
+        const unsigned long long tot = ctl->colordiff_acc;
+        ctl->last_colordiff = tot;
+        ctl->colordiff_acc = 0;
+        const float cr = __ull2float_rn(tot) / (float)(S.dsW * S.dsH);
+        const unsigned long long thr = (unsigned long long)(S.minColor / 2);
+        if (ctl->auto_reset) {
+            if (ctl->frames_since_reset > 1000ull) {
+                ctl->auto_reset = 0;
+            } else if (cr >= (float)thr && ctl->cooldown == 0ull) {
+                ctl->frames_since_reset = 0;
+                ctl->refresh_pending = 1;
+                ctl->cooldown = (unsigned long long)(S.nmv / 4);
+            } else {
+                ++ctl->frames_since_reset;
+            }
+        } else if (cr >= (float)(thr * 2ull)) {
+            ctl->frames_since_reset = 0;
+            ctl->auto_reset = 1;
+        }
+        if (cr >= (float)(thr / 2ull)) {
+            const int sh = ((int)(cr / 2)) & 31;
+            const int lo = 2 >> sh, hi = 256 >> sh;
+            ctl->t_lo = (float)(lo > 1 ? lo : 1);
+            ctl->t_hi = (float)(hi > 1 ? hi : 1);
+        } else {
+            ctl->t_lo = 2.0f;
+            ctl->t_hi = 256.0f;
+        }
+        if (ctl->cooldown > 0ull) --ctl->cooldown;
+    }
+}
+
+// refreshModel (:80-105) of one pixel; lastBuf holds the latest colour/descriptor frame
+template <int C>
+__device__ void refresh_pixel(const StreamDev& S, int p, uint32_t frame, int start, int nref, int force, int lastBuf) {
+    if (!S.roi[p]) return;
+    if (!force && S.lastFG[p]) return;
+    const int W = S.W, H = S.H, npx = S.npx, N = S.N;
+    const int x0 = p % W, y0 = p / W;
+    uint32_t k = S.kctr[p];
+    DrawState ds;
+    ds.blk = 0xffffffffu;
+    const uint8_t* lc = S.lastCol + (size_t)lastBuf * npx * C;
+    const uint16_t* ldd = S.lastDesc + (size_t)lastBuf * npx * C;
+    for (int s = start; s < start + nref; ++s) {
+        int r = 1 + (int)(draw_k(S.seed, frame, (uint32_t)p, k++, ds) % 512u);
+        int sx = 0, sy = 0;
+        for (int i = 0; i < 49; ++i) {
+            r -= c_pat7[i];
+            if (r <= 0) {
+                sy = i / 7;
+                sx = i % 7;
+                break;
+            }
+        }
+        sx += x0 - 3;
+        sy += y0 - 3;
+        clamp_xy(sx, sy, W, H);
+        const int sp = sy * W + sx;
+        if (!force && S.lastFG[sp]) continue;
+        const int rs = s % N;
+        if (C == 3) {
+            const uint64_t d = (uint64_t)ldd[(size_t)sp * 3] | ((uint64_t)ldd[(size_t)sp * 3 + 1] << 16) |
+                               ((uint64_t)ldd[(size_t)sp * 3 + 2] << 32) | ((uint64_t)lc[(size_t)sp * 3] << 48) |
+                               ((uint64_t)lc[(size_t)sp * 3 + 1] << 56);
+            ((uint64_t*)S.sD)[(size_t)rs * npx + p] = d;
+            S.sC[(size_t)rs * npx + p] = lc[(size_t)sp * 3 + 2];
+        } else {
+            ((uint16_t*)S.sD)[(size_t)rs * npx + p] = ldd[sp];
+            S.sC[(size_t)rs * npx + p] = lc[sp];
+        }
+    }
+    S.kctr[p] = (uint16_t)k;
+}
+
+// ------------------------------------------------------------------------------------------
+// the tick kernel
+// ------------------------------------------------------------------------------------------
+extern "C" __global__ void __launch_bounds__(kThreads, 2)
+    lvbgs_subsense_tick(TickParams P, unsigned long long dsTotal, const unsigned long long* dsBase) {
+    __shared__ __align__(16) uint8_t smem[8192];
+    TickWork* w = P.work;
+    // ---- A: evaluate all pixels ----
+    for (int t = next_tile(P, 0); t < P.totalTiles; t = next_tile(P, 0)) {
+        const int si = find_stream_by_tile(P, t);
+        const StreamDev& S = P.streams[si];
+        if (S.C == 3) phaseA_tile<3>(P, S, t - S.tileBase, smem);
+        else phaseA_tile<1>(P, S, t - S.tileBase, smem);
+    }
+    if (!grid_sync(w)) return;
+    // ---- B: resolve ghost tests, initial repair frontier; frame down-sampling ----
+    for (int t = next_tile(P, 1); t < P.totalTiles; t = next_tile(P, 1)) {
+        const int si = find_stream_by_tile(P, t);
+        phaseB_tile(P, si, P.streams[si], t - P.streams[si].tileBase);
+    }
+    {
+        const unsigned long long nth = (unsigned long long)gridDim.x * blockDim.x;
+        for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < dsTotal; i += nth) {
+            int lo = 0, hi = P.nStreams - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (dsBase[mid] <= i) lo = mid;
+                else hi = mid - 1;
+            }
+            ds_item(P.streams[lo], (int)(i - dsBase[lo]));
+        }
+    }
+    if (!grid_sync(w)) return;
+    // ---- M/R: repair to the raster-order fixed point ----
+    int iter = 0;
+    for (;;) {
+        const int par = iter & 1;
+        const unsigned int n = ld_volatile(&w->dcount[par]);
+        if (n == 0u) break;
+        if (iter >= kMaxRepairIters) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&w->err, ERR_REPAIR_LIMIT);
+            return;
+        }
+        const unsigned int nItems = n < P.listCap ? n : P.listCap;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            w->rcount[par ^ 1] = 0u;
+            w->rematched += nItems;
+        }
+        const unsigned int nth = gridDim.x * blockDim.x;
+        for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < nItems; i += nth) {
+            const unsigned long long item = __ldcg(&P.dlist[par][i]);
+            const int si = (int)(item >> 40), q = (int)(item & 0xffffffffffull);
+            const StreamDev& S = P.streams[si];
+            const uint32_t stampNext = S.ctl->stamp_base + (uint32_t)iter + 2u;
+            if (S.C == 3) rematch_item<3>(P, si, S, q, stampNext, par);
+            else rematch_item<1>(P, si, S, q, stampNext, par);
+        }
+        if (!grid_sync(w)) return;
+        const unsigned int nr0 = ld_volatile(&w->rcount[par]);
+        const unsigned int nr = nr0 < P.listCap ? nr0 : P.listCap;
+        if (blockIdx.x == 0 && threadIdx.x == 0) w->dcount[par] = 0u;
+        for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < nr; i += nth) {
+            const unsigned long long item = __ldcg(&P.rlist[par][i]);
+            const int si = (int)(item >> 40), p = (int)(item & 0xffffffffffull);
+            const StreamDev& S = P.streams[si];
+            reresolve_item(P, si, S, p, S.ctl->stamp_base + (uint32_t)iter + 2u, par);
+        }
+        if (!grid_sync(w)) return;
+        ++iter;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) w->iters = (unsigned)iter;
+    // ---- F: commit sample writes, blinks, closing ----
+    for (int t = next_tile(P, 2); t < P.totalTiles; t = next_tile(P, 2)) {
+        const int si = find_stream_by_tile(P, t);
+        const StreamDev& S = P.streams[si];
+        if (S.C == 3) phaseF_tile<3>(P, S, t - S.tileBase, smem);
+        else phaseF_tile<1>(P, S, t - S.tileBase, smem);
+    }
+    if (!grid_sync(w)) return;
+    for (int t = next_tile(P, 3); t < P.totalTiles; t = next_tile(P, 3)) {
+        const int si = find_stream_by_tile(P, t);
+        phaseP2a_tile(P, P.streams[si], t - P.streams[si].tileBase, smem);
+    }
+    if (!grid_sync(w)) return;
+    for (int t = next_tile(P, 4); t < P.totalTiles; t = next_tile(P, 4)) {
+        const int si = find_stream_by_tile(P, t);
+        phaseP2b_tile(P, P.streams[si], t - P.streams[si].tileBase);
+    }
+    if (!grid_sync(w)) return;
+    for (int t = next_tile(P, 5); t < P.totalTiles; t = next_tile(P, 5)) {
+        const int si = find_stream_by_tile(P, t);
+        phaseP2c_tile(P, P.streams[si], t - P.streams[si].tileBase, smem);
+    }
+    if (!grid_sync(w)) return;
+    for (int t = next_tile(P, 6); t < P.totalTiles; t = next_tile(P, 6)) {
+        const int si = find_stream_by_tile(P, t);
+        phaseP4_tile(P, P.streams[si], t - P.streams[si].tileBase, smem);
+    }
+    if (!grid_sync(w)) return;
+    // epilogue of each stream runs beside P5 (it reads nothing P5 writes)
+    if (blockIdx.x == gridDim.x - 1)
+        for (int si = threadIdx.x; si < P.nStreams; si += blockDim.x) {
+            const StreamDev& S = P.streams[si];
+            stream_epilogue(P, S);
+            if (S.ctl->refresh_pending) {
+                // nRefreshSampleStartPos = rand() % N with the frame-level (sentinel) counter
+                DrawState ds;
+                ds.blk = 0xffffffffu;
+                const uint32_t f = (uint32_t)(S.ctl->frame_idx + 1ull);
+                S.ctl->refresh_start = draw_k(S.seed, f, kSentinelPx, 0u, ds) % (uint32_t)S.N;
+                S.ctl->ksent = 1;
+            }
+        }
+    for (int t = next_tile(P, 7); t < P.totalTiles; t = next_tile(P, 7)) {
+        const int si = find_stream_by_tile(P, t);
+        phaseP5_tile(P, P.streams[si], t - P.streams[si].tileBase, smem);
+    }
+    if (!grid_sync(w)) return;
+    // ---- automatic model reset: refreshModel(0.1) and T(x) := 1 (:588-593) ----
+    for (int t = next_tile(P, 8); t < P.totalTiles; t = next_tile(P, 8)) {
+        const int si = find_stream_by_tile(P, t);
+        const StreamDev& S = P.streams[si];
+        if (!S.ctl->refresh_pending) continue;
+        const int lt = t - S.tileBase;
+        const int x = (lt % S.tilesX) * kTileW + threadIdx.x % kTileW;
+        const int y = (lt / S.tilesX) * kTileH + threadIdx.x / kTileW;
+        if (x >= S.W || y >= S.H) continue;
+        const int p = y * S.W + x;
+        const uint32_t f = (uint32_t)(S.ctl->frame_idx + 1ull);
+        const int nxt = (int)((S.ctl->frame_idx + 1ull) & 1ull);
+        const int nref = (int)(0.1f * (float)S.N);
+        if (S.C == 3) refresh_pixel<3>(S, p, f, (int)S.ctl->refresh_start, nref, 0, nxt);
+        else refresh_pixel<1>(S, p, f, (int)S.ctl->refresh_start, nref, 0, nxt);
+        S.fm[(size_t)0 * kNumFloatMaps * S.npx + FM_T * S.npx + p] = 1.0f;
+        S.fm[(size_t)1 * kNumFloatMaps * S.npx + FM_T * S.npx + p] = 1.0f;
+    }
+    // ---- the last CTA to finish closes the frame: frame index (parity) and repair stamps ----
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned int done = atomicAdd(&w->done_ctas, 1u) + 1u;
+        if (done == gridDim.x) {
+            __threadfence();
+            const unsigned int its = ld_volatile(&w->iters);
+            for (int si = 0; si < P.nStreams; ++si) {
+                StreamCtl* ctl = P.streams[si].ctl;
+                ctl->frame_idx += 1ull;
+                ctl->st_rounds += its;
+                ctl->stamp_base += (uint32_t)its + 4u;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// initialization, manual refresh, background images, LBSP extraction
+// ------------------------------------------------------------------------------------------
+// BackgroundSubtractorLBSP.cpp:21-65 + BackgroundSubtractorSuBSENSE.cpp:129-182 (map initial values)
+extern "C" __global__ void lvbgs_init_maps(StreamDev S, const uint8_t* img, float tLo) {
+    const int npx = S.npx;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npx; p += gridDim.x * blockDim.x) {
+        const int C = S.C, x = p % S.W, y = p / S.W;
+        for (int b = 0; b < 2; ++b) {
+            float* f = S.fm + (size_t)b * kNumFloatMaps * npx;
+            for (int m = 0; m < kNumFloatMaps; ++m) f[m * npx + p] = 0.0f;
+            f[FM_T * npx + p] = tLo;
+            f[FM_R * npx + p] = 1.0f;
+            f[FM_V * npx + p] = 10.0f;
+            S.unst[(size_t)b * npx + p] = 0;
+        }
+        const bool in = S.roi[p] != 0;
+        const bool desc = in && x > kBorder && y > kBorder && x < S.W - kBorder && y < S.H - kBorder;
+        for (int c = 0; c < C; ++c) {
+            const uint8_t v = in ? img[(size_t)p * C + c] : 0;
+            uint16_t d = 0;
+            if (desc) {
+                uint32_t vals[4];
+                const uint8_t* base = img + (size_t)p * C;
+                for (int j = 0; j < 4; ++j) {
+                    uint32_t wv = 0;
+                    for (int i = 0; i < 4; ++i) {
+                        const int n = j * 4 + i;
+                        wv |= (uint32_t)base[(c_lbsp_dy[n] * S.W + c_lbsp_dx[n]) * C + c] << (8 * i);
+                    }
+                    vals[j] = wv;
+                }
+                d = (uint16_t)lbsp_thr(vals, v, S.ctl->lut[v]);
+            }
+            for (int b = 0; b < 2; ++b) {
+                S.lastCol[(size_t)b * npx * C + (size_t)p * C + c] = v;
+                S.lastDesc[(size_t)b * npx * C + (size_t)p * C + c] = d;
+            }
+        }
+        S.blinks[p] = 0;
+        S.lastRawFG[p] = 0;
+        S.lastFG[p] = 0;
+        S.dilInv[p] = 0;
+        S.lastRawBlink[p] = 0;
+        S.kctr[p] = 0;
+        S.stampD[p] = 0;
+        S.stampR[p] = 0;
+    }
+}
+
+// refreshModel(frac, force) outside a frame step (initialize(), or a user call)
+extern "C" __global__ void lvbgs_refresh(StreamDev S, uint32_t frame, int start, int nref, int force, int lastBuf) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < S.npx; p += gridDim.x * blockDim.x) {
+        if (S.C == 3) refresh_pixel<3>(S, p, frame, start, nref, force, lastBuf);
+        else refresh_pixel<1>(S, p, frame, start, nref, force, lastBuf);
+    }
+}
+
+// getBackgroundImage / getBackgroundDescriptorsImage (:614-649): float mean in sample order
+extern "C" __global__ void lvbgs_background(StreamDev S, uint8_t* outCol, uint16_t* outDesc) {
+    const int npx = S.npx, C = S.C, N = S.N;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npx; p += gridDim.x * blockDim.x) {
+        for (int c = 0; c < C; ++c) {
+            float acc = 0.0f, accd = 0.0f;
+            for (int s = 0; s < N; ++s) {
+                uint32_t col, d;
+                if (C == 3) {
+                    const uint64_t v = ((const uint64_t*)S.sD)[(size_t)s * npx + p];
+                    col = c == 2 ? S.sC[(size_t)s * npx + p] : (uint32_t)(v >> (48 + 8 * c)) & 0xffu;
+                    d = (uint32_t)(v >> (16 * c)) & 0xffffu;
+                } else {
+                    col = S.sC[(size_t)s * npx + p];
+                    d = ((const uint16_t*)S.sD)[(size_t)s * npx + p];
+                }
+                acc += ((float)col) / (float)N;
+                accd += ((float)d) / (float)N;
+            }
+            if (outCol) {
+                int r = __float2int_rn(acc);
+                outCol[(size_t)p * C + c] = (uint8_t)(r < 0 ? 0 : r > 255 ? 255 : r);
+            }
+            if (outDesc) {
+                int r = __float2int_rn(accd);
+                outDesc[(size_t)p * C + c] = (uint16_t)(r < 0 ? 0 : r > 65535 ? 65535 : r);
+            }
+        }
+    }
+}
+
+// sample planes -> the reference's N sample images (inspection)
+extern "C" __global__ void lvbgs_unpack_samples(StreamDev S, uint8_t* col, uint16_t* desc) {
+    const size_t total = (size_t)S.N * S.npx;
+    const int C = S.C;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        if (C == 3) {
+            const uint64_t v = ((const uint64_t*)S.sD)[i];
+            for (int c = 0; c < 3; ++c) {
+                col[i * 3 + c] = c == 2 ? S.sC[i] : (uint8_t)(v >> (48 + 8 * c));
+                desc[i * 3 + c] = (uint16_t)(v >> (16 * c));
+            }
+        } else {
+            col[i] = S.sC[i];
+            desc[i] = ((const uint16_t*)S.sD)[i];
+        }
+    }
+}
+
+// the reference's N sample images -> sample planes (state restore)
+extern "C" __global__ void lvbgs_pack_samples(StreamDev S, const uint8_t* col, const uint16_t* desc) {
+    const size_t total = (size_t)S.N * S.npx;
+    const int C = S.C;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        if (C == 3) {
+            ((uint64_t*)S.sD)[i] = (uint64_t)desc[i * 3] | ((uint64_t)desc[i * 3 + 1] << 16) |
+                                   ((uint64_t)desc[i * 3 + 2] << 32) | ((uint64_t)col[i * 3] << 48) |
+                                   ((uint64_t)col[i * 3 + 1] << 56);
+            S.sC[i] = col[i * 3 + 2];
+        } else {
+            ((uint16_t*)S.sD)[i] = desc[i];
+            S.sC[i] = col[i];
+        }
+    }
+}
+
+// LBSP::compute2 (LBSP.cpp:102-152): dense extraction, absolute (thr >= 0) or relative threshold
+extern "C" __global__ void lvbgs_lbsp_dense(const uint8_t* img, int W, int H, int C, int absThr, float rel,
+                                            unsigned int off, uint16_t* desc) {
+    const int total = W * H;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x) {
+        const int x = p % W, y = p / W;
+        if (x < kBorder || y < kBorder || x >= W - kBorder || y >= H - kBorder) continue;
+        for (int c = 0; c < C; ++c) {
+            const uint8_t* base = img + (size_t)p * C;
+            uint32_t vals[4];
+            for (int j = 0; j < 4; ++j) {
+                uint32_t wv = 0;
+                for (int i = 0; i < 4; ++i) {
+                    const int n = j * 4 + i;
+                    wv |= (uint32_t)base[(c_lbsp_dy[n] * W + c_lbsp_dx[n]) * C + c] << (8 * i);
+                }
+                vals[j] = wv;
+            }
+            const uint32_t ref = base[c];
+            uint32_t thr;
+            if (absThr >= 0) {
+                thr = absThr > 255 ? 255u : (uint32_t)absThr;
+            } else {
+                int r = __float2int_rn((float)ref * rel + (float)off);
+                thr = (uint32_t)(r < 0 ? 0 : r > 255 ? 255 : r);
+            }
+            desc[(size_t)p * C + c] = (uint16_t)lbsp_thr(vals, ref, thr);
+        }
+    }
+}
+
+}  // namespace lvbgs

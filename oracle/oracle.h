@@ -1,0 +1,112 @@
+/* ORACLE (test infrastructure only; never linked into the product library).
+ *
+ * CPU restatement of the reference's SuBSENSE per-pixel background subtraction
+ * (plstcharles/litiv, modules/video/src/BackgroundSubtractorSuBSENSE.cpp) and of
+ * the LBSP descriptor (modules/features2d/include/litiv/features2d/LBSP.hpp).
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it,
+ * always as the checker.
+ *
+ * Parity pins: the LBSP descriptor is pinned by the reference's golden vector
+ * (modules/features2d/test/data/test_lbsp.bin, see tests/golden/). The rest of
+ * the path has no golden vectors in the reference and the reference itself
+ * cannot be built here (it needs OpenCV, which is absent), so the SuBSENSE
+ * model state, masks and the OpenCV image operations it calls are "parity
+ * unpinned" against the real reference; each function cites the reference
+ * lines it restates and states the OpenCV definition it uses.
+ */
+#ifndef LV_ORACLE_H
+#define LV_ORACLE_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct osub osub_t;
+
+typedef struct {
+    size_t desc_dist_threshold_offset;   /* BGSSUBSENSE_DEFAULT_DESC_DIST_THRESHOLD_OFFSET = 3 */
+    size_t min_color_dist_threshold;     /* = 30 */
+    size_t bg_samples;                   /* = 50 */
+    size_t required_bg_samples;          /* = 2 */
+    size_t samples_for_moving_avgs;      /* = 100 */
+    float rel_lbsp_threshold;            /* = 0.333f */
+    size_t lbsp_threshold_offset;        /* = 0 */
+    int default_median_blur_kernel_size; /* = 9 */
+    uint64_t seed;                       /* key of the counter-based generator */
+} osub_params;
+
+/* scalars of the frame-level state, for parity checks */
+typedef struct {
+    uint64_t frame_idx, frames_since_last_reset, model_reset_cooldown;
+    int32_t auto_model_reset_enabled, learning_rate_scaling_enabled, use_3x3_spread, median_blur_kernel_size;
+    float lr_lower_cap, lr_upper_cap, last_nonzero_desc_ratio;
+    uint64_t nonzero_desc_count, tot_color_diff;
+    uint64_t n_relevant_px, orig_roi_px;
+    uint64_t stat_samples_evaluated, stat_sample_writes;  /* for the algorithmic-byte count */
+} osub_scalars;
+
+enum {
+    OSUB_MAP_R = 0, OSUB_MAP_V, OSUB_MAP_T, OSUB_MAP_DLAST, OSUB_MAP_DMIN_LT, OSUB_MAP_DMIN_ST,
+    OSUB_MAP_RAW_LT, OSUB_MAP_RAW_ST, OSUB_MAP_FIN_LT, OSUB_MAP_FIN_ST,           /* float [H*W]   */
+    OSUB_MAP_UNSTABLE, OSUB_MAP_BLINKS, OSUB_MAP_LAST_RAW_FG, OSUB_MAP_LAST_FG,
+    OSUB_MAP_LAST_FG_DIL_INV, OSUB_MAP_LAST_RAW_BLINK, OSUB_MAP_ROI,             /* uint8 [H*W]   */
+    OSUB_MAP_LAST_COLOR,                                                           /* uint8 [H*W*C] */
+    OSUB_MAP_LAST_DESC,                                                            /* uint16 [H*W*C] */
+    OSUB_MAP_SAMPLE_COLOR,                                                         /* uint8 [N][H*W*C] */
+    OSUB_MAP_SAMPLE_DESC,                                                          /* uint16 [N][H*W*C] */
+    OSUB_MAP_DS_LT, OSUB_MAP_DS_ST,                                                /* float [H/8*W/8*C] */
+    OSUB_MAP_LUT,                                                                  /* uint8 [256] */
+    OSUB_MAP_COUNT
+};
+
+/* error codes (0 = ok) */
+#define OSUB_OK 0
+#define OSUB_EBADARG 1
+#define OSUB_ENOTINIT 2
+#define OSUB_EUNSUPPORTED 3
+
+void osub_default_params(osub_params* p);
+osub_t* osub_create(const osub_params* p);
+void osub_destroy(osub_t* o);
+/* BackgroundSubtractorSuBSENSE::initialize (BackgroundSubtractorSuBSENSE.cpp:107-186); roi may be NULL */
+int osub_initialize(osub_t* o, const uint8_t* img, int width, int height, int channels, const uint8_t* roi);
+/* BackgroundSubtractorSuBSENSE::apply (BackgroundSubtractorSuBSENSE.cpp:188-612) */
+int osub_apply(osub_t* o, const uint8_t* img, uint8_t* fgmask, double learning_rate_override);
+/* BackgroundSubtractorSuBSENSE::refreshModel (BackgroundSubtractorSuBSENSE.cpp:80-105) */
+int osub_refresh_model(osub_t* o, float frac, int force_fg);
+int osub_get_background(const osub_t* o, uint8_t* out);               /* :614-630 */
+int osub_get_background_descriptors(const osub_t* o, uint16_t* out);  /* :632-649 */
+void osub_set_automatic_model_reset(osub_t* o, int enabled);          /* BackgroundSubtractionUtils.cpp:24-26 */
+const void* osub_map(const osub_t* o, int which, size_t* nbytes);
+void osub_get_scalars(const osub_t* o, osub_scalars* s);
+
+/* LBSP::compute2 dense extraction (modules/features2d/src/LBSP.cpp:102-152).
+ * abs_threshold >= 0 selects the absolute-threshold variant, otherwise the relative
+ * one (rel_threshold, abs offset). Border pixels (2 px) are left untouched. */
+void olbsp_compute2(const uint8_t* img, int width, int height, int channels,
+                    long abs_threshold, float rel_threshold, size_t offset, uint16_t* desc);
+
+/* sampling helpers with border 2 (getSamplePosition_7x7_std2, getNeighborPosition_3x3/_5x5), for
+ * the property tests of utils/test/opencv.cpp:390-429 */
+void osample_pos_7x7(int rnd, int x0, int y0, int width, int height, int* sx, int* sy);
+void oneighbor_pos(int rnd, int use3x3, int x0, int y0, int width, int height, int* nx, int* ny);
+
+/* raw generator access, for the known-answer test */
+void ophilox_block(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+/* CPU baseline: runs n independent SuBSENSE instances (one per stream) over their
+ * frame sequences with a pool of n_threads workers (one instance per worker at a
+ * time, like lv::WorkerPool in apps/changedet/src/main.cpp:148-154).
+ * frames[i] holds n_frames[i] frames of widths[i]*heights[i]*channels[i] bytes;
+ * the first frame initializes, the others are applied. Returns the wall time in
+ * seconds of the whole run; masks may be NULL. */
+double orun_streams(int n_streams, const uint8_t* const* frames, const int* n_frames,
+                    const int* widths, const int* heights, const int* channels,
+                    const uint64_t* seeds, int n_threads, uint8_t* const* last_masks);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

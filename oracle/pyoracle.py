@@ -1,0 +1,185 @@
+"""ORACLE (test infrastructure only): ctypes wrapper of oracle/_build/liboracle.so.
+
+Loaded only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, as the checker.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+MAP_NAMES = ["R", "V", "T", "DLAST", "DMIN_LT", "DMIN_ST", "RAW_LT", "RAW_ST", "FIN_LT", "FIN_ST",
+             "UNSTABLE", "BLINKS", "LAST_RAW_FG", "LAST_FG", "LAST_FG_DIL_INV", "LAST_RAW_BLINK", "ROI",
+             "LAST_COLOR", "LAST_DESC", "SAMPLE_COLOR", "SAMPLE_DESC", "DS_LT", "DS_ST", "LUT"]
+
+
+class OParams(C.Structure):
+    _fields_ = [("desc_dist_threshold_offset", C.c_size_t), ("min_color_dist_threshold", C.c_size_t),
+                ("bg_samples", C.c_size_t), ("required_bg_samples", C.c_size_t),
+                ("samples_for_moving_avgs", C.c_size_t), ("rel_lbsp_threshold", C.c_float),
+                ("lbsp_threshold_offset", C.c_size_t), ("default_median_blur_kernel_size", C.c_int),
+                ("seed", C.c_uint64)]
+
+
+class OScalars(C.Structure):
+    _fields_ = [("frame_idx", C.c_uint64), ("frames_since_last_reset", C.c_uint64),
+                ("model_reset_cooldown", C.c_uint64), ("auto_model_reset_enabled", C.c_int32),
+                ("learning_rate_scaling_enabled", C.c_int32), ("use_3x3_spread", C.c_int32),
+                ("median_blur_kernel_size", C.c_int32), ("lr_lower_cap", C.c_float), ("lr_upper_cap", C.c_float),
+                ("last_nonzero_desc_ratio", C.c_float), ("nonzero_desc_count", C.c_uint64),
+                ("tot_color_diff", C.c_uint64), ("n_relevant_px", C.c_uint64), ("orig_roi_px", C.c_uint64),
+                ("stat_samples_evaluated", C.c_uint64), ("stat_sample_writes", C.c_uint64)]
+
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.osub_create.restype = C.c_void_p
+        L.osub_create.argtypes = [C.POINTER(OParams)]
+        L.osub_destroy.argtypes = [C.c_void_p]
+        L.osub_initialize.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        L.osub_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
+        L.osub_refresh_model.argtypes = [C.c_void_p, C.c_float, C.c_int]
+        L.osub_get_background.argtypes = [C.c_void_p, C.c_void_p]
+        L.osub_get_background_descriptors.argtypes = [C.c_void_p, C.c_void_p]
+        L.osub_set_automatic_model_reset.argtypes = [C.c_void_p, C.c_int]
+        L.osub_map.restype = C.c_void_p
+        L.osub_map.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]
+        L.osub_get_scalars.argtypes = [C.c_void_p, C.POINTER(OScalars)]
+        L.olbsp_compute2.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_long, C.c_float, C.c_size_t,
+                                     C.c_void_p]
+        L.osample_pos_7x7.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                      C.POINTER(C.c_int)]
+        L.oneighbor_pos.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                    C.POINTER(C.c_int)]
+        L.ophilox_block.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.orun_streams.restype = C.c_double
+        L.orun_streams.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_uint64), C.c_int,
+                                   C.POINTER(C.c_void_p)]
+        _lib = L
+    return _lib
+
+
+class OracleSuBSENSE:
+    """Sequential CPU SuBSENSE (the checker)."""
+
+    def __init__(self, seed=0, **params):
+        p = OParams()
+        lib().osub_default_params(C.byref(p))
+        p.seed = seed
+        for k, v in params.items():
+            setattr(p, k, v)
+        self.params = p
+        self._o = lib().osub_create(C.byref(p))
+        if not self._o:
+            raise ValueError("invalid oracle parameters")
+        self.shape = None
+
+    def close(self):
+        if self._o:
+            lib().osub_destroy(self._o)
+            self._o = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def initialize(self, img, roi=None):
+        img = np.ascontiguousarray(img, np.uint8)
+        H, W = img.shape[:2]
+        Cc = img.shape[2] if img.ndim == 3 else 1
+        r = None if roi is None else np.ascontiguousarray(roi, np.uint8)
+        st = lib().osub_initialize(self._o, img.ctypes.data_as(C.c_void_p), W, H, Cc,
+                                   r.ctypes.data_as(C.c_void_p) if r is not None else None)
+        if st != 0:
+            raise ValueError("oracle initialize failed (%d)" % st)
+        self.shape = (H, W, Cc)
+
+    def apply(self, img, lr=0.0):
+        img = np.ascontiguousarray(img, np.uint8)
+        H, W, _ = self.shape
+        mask = np.empty((H, W), np.uint8)
+        st = lib().osub_apply(self._o, img.ctypes.data_as(C.c_void_p), mask.ctypes.data_as(C.c_void_p), float(lr))
+        if st != 0:
+            raise ValueError("oracle apply failed (%d)" % st)
+        return mask
+
+    def refresh_model(self, frac, force=False):
+        return lib().osub_refresh_model(self._o, float(frac), 1 if force else 0)
+
+    def set_automatic_model_reset(self, v):
+        lib().osub_set_automatic_model_reset(self._o, 1 if v else 0)
+
+    def background(self):
+        H, W, Cc = self.shape
+        out = np.empty((H, W, Cc) if Cc > 1 else (H, W), np.uint8)
+        lib().osub_get_background(self._o, out.ctypes.data_as(C.c_void_p))
+        return out
+
+    def background_descriptors(self):
+        H, W, Cc = self.shape
+        out = np.empty((H, W, Cc) if Cc > 1 else (H, W), np.uint16)
+        lib().osub_get_background_descriptors(self._o, out.ctypes.data_as(C.c_void_p))
+        return out
+
+    def state_map(self, name):
+        n = C.c_size_t()
+        ptr = lib().osub_map(self._o, MAP_NAMES.index(name), C.byref(n))
+        raw = np.ctypeslib.as_array((C.c_uint8 * n.value).from_address(ptr)).copy()
+        H, W, Cc = self.shape
+        from litiv_gb300.bgs import map_view  # layout helper only (pure numpy)
+        return map_view(name, raw, W, H, Cc, self.params.bg_samples)
+
+    def scalars(self):
+        s = OScalars()
+        lib().osub_get_scalars(self._o, C.byref(s))
+        return {f: getattr(s, f) for f, _ in OScalars._fields_}
+
+
+def lbsp_compute2(img, abs_threshold=None, rel_threshold=0.333, offset=0, out=None):
+    img = np.ascontiguousarray(img, np.uint8)
+    H, W = img.shape[:2]
+    Cc = img.shape[2] if img.ndim == 3 else 1
+    if out is None:
+        out = np.zeros(img.shape, np.uint16)
+    thr = -1 if abs_threshold is None else int(abs_threshold)
+    lib().olbsp_compute2(img.ctypes.data_as(C.c_void_p), W, H, Cc, thr, float(rel_threshold), int(offset),
+                         out.ctypes.data_as(C.c_void_p))
+    return out
+
+
+def philox(ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib().ophilox_block(c, k, o)
+    return list(o)
+
+
+def run_streams(frames_list, seeds, n_threads):
+    """CPU baseline: frames_list[i] is a uint8 array [F, H, W(, C)]; returns wall seconds."""
+    n = len(frames_list)
+    arrs = [np.ascontiguousarray(f) for f in frames_list]
+    ptrs = (C.c_void_p * n)(*[a.ctypes.data for a in arrs])
+    nf = (C.c_int * n)(*[a.shape[0] for a in arrs])
+    ws = (C.c_int * n)(*[a.shape[2] for a in arrs])
+    hs = (C.c_int * n)(*[a.shape[1] for a in arrs])
+    cs = (C.c_int * n)(*[(a.shape[3] if a.ndim == 4 else 1) for a in arrs])
+    sd = (C.c_uint64 * n)(*seeds)
+    return lib().orun_streams(n, ptrs, nf, ws, hs, cs, sd, int(n_threads), None)
