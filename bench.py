@@ -1,0 +1,348 @@
+"""Benchmark: SuBSENSE Mpix/s on the 64-stream mixed-resolution workload, batched vs plain.
+
+A step is one frame tick of all 64 streams (16x320x240, 24x640x480, 16x1280x720, 8x1920x1080;
+48 BGR + 16 grayscale; 39,936,000 pixels) processed by one persistent launch of the SuBSENSE tick
+kernel. ``value`` is measured with the frames already resident in HBM; ``e2e`` goes through the
+C-ABI (lvbgs_batch_apply) with pinned host frames and host masks, so the host->device frame copies
+and device->host mask copies are inside the timed region. The plain form (one stream per launch,
+64 launches per tick) is measured on the same frames. Inputs and model state (~24 GB) are far
+larger than the 129 MB L2, so no flush is needed between steps.
+
+``--impl reference`` times the CPU restatement of the reference (oracle/) on the host cores over a
+bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SuBSENSE Mpix/s: batched 64-stream vs plain 1-stream on GB300; p99 frame ms"
+WORKLOAD = ("subsense-mix64: 16x320x240 + 24x640x480 + 16x1280x720 + 8x1920x1080, 48 BGR + 16 gray, "
+            "default parameters, synthetic seeded scenes")
+# CPU sample: 4 streams of each resolution class
+CPU_SAMPLE_STREAMS = [0, 1, 2, 3, 16, 17, 18, 19, 40, 41, 42, 43, 56, 57, 58, 59]
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) != len(self.FIELDS):
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(px_by_c, samples, writes):
+    """Algorithmic HBM bytes of one tick (per ROI pixel: frame c + mask 1 + 10 FP32 maps r+w 80 +
+    last colour/descriptor r+w 6c + u8 maps r+w 12, plus 3c bytes per evaluated sample and per
+    sample write)."""
+    total = 0
+    for c, (npx, s, w) in px_by_c.items():
+        total += npx * (c + 1 + 80 + 6 * c + 12) + 3 * c * (s + w)
+    return total
+
+
+def cpu_baseline(n_frames=6, threads=None):
+    """The oracle on the host cores: one instance per core across streams (lv::WorkerPool model)."""
+    from litiv_gb300 import SyntheticStream
+    from oracle import pyoracle
+    import numpy as np
+    threads = threads or os.cpu_count() or 1
+    frames, seeds, px = [], [], 0
+    for i in CPU_SAMPLE_STREAMS:
+        s = SyntheticStream(3, index=i, seed=1)
+        frames.append(np.stack([s.render(t) for t in range(n_frames)]))
+        seeds.append(1000 + i)
+        px += s.cfg.width * s.cfg.height * (n_frames - 1)
+    wall = pyoracle.run_streams(frames, seeds, threads)
+    return {"value": px / wall / 1e6, "unit": "Mpix/s", "cores": threads, "kind": "port",
+            "sample": "%d streams of the mix (4 per resolution), %d applied frames each, %.1f Mpix in %.1f s" % (
+                len(frames), n_frames - 1, px / 1e6, wall)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(n_frames=3)
+    t0 = time.time()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(n_frames=3))
+    el = time.time() - t0
+    v = sum(x["value"] for x in vals) / len(vals)
+    cb = dict(vals[-1])
+    cb["value"] = v
+    out = {"metric": METRIC, "impl": "reference", "value": v, "unit": "Mpix/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/f32",
+           "data": "synthetic", "config": {"workload": WORKLOAD, "sample": cb["sample"]},
+           "cpu_baseline": cb, "e2e": {"value": v, "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--streams", type=int, default=64, help="streams of the mix (debug: fewer)")
+    ap.add_argument("--plain-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    from litiv_gb300 import BackgroundSubtractorSuBSENSE, SyntheticStream
+    from litiv_gb300 import _lib as L
+    import ctypes as C
+
+    lib = L.lib()
+    n = args.streams
+    ticks = 1 + args.warmup + args.steps
+    synth = [SyntheticStream(3, index=i, seed=1) for i in range(n)]
+    dev_frames = []  # per stream: uint8 tensor [ticks, H, W, C]
+    for s in synth:
+        shp = (ticks,) + s.shape
+        buf = torch.empty(shp, dtype=torch.uint8, device="cuda")
+        for t in range(ticks):
+            s.render_device(t, buf[t].data_ptr(), None, torch.cuda.current_stream().cuda_stream)
+        dev_frames.append(buf)
+    torch.cuda.synchronize()
+    px_step = sum(s.cfg.width * s.cfg.height for s in synth)
+    stream = torch.cuda.current_stream()
+    sptr = C.c_void_p(stream.cuda_stream)
+
+    def make_subtractors(seed_base):
+        subs = []
+        for i, s in enumerate(synth):
+            b = BackgroundSubtractorSuBSENSE(seed=seed_base + i, device_id=local)
+            b.initialize(dev_frames[i][0])
+            subs.append(b)
+        return subs
+
+    def frames_struct(subs, t, masks, host=None):
+        fr = (L.LvbgsFrame * len(subs))()
+        for i in range(len(subs)):
+            fr[i].image = host[i][t].ctypes.data if host is not None else dev_frames[i][t].data_ptr()
+            fr[i].stride = 0
+            fr[i].fgmask = masks[i]
+            fr[i].learning_rate = 0.0
+        return fr
+
+    def check(st, h):
+        if st != L.OK:
+            raise RuntimeError("lvbgs error %d: %s" % (st, lib.lvbgs_last_error(h)))
+
+    # ---- batched form, device-resident frames ----
+    subs = make_subtractors(1000)
+    hs = (C.c_void_p * n)(*[b.handle for b in subs])
+    dmasks = [torch.empty((s.cfg.height, s.cfg.width), dtype=torch.uint8, device="cuda") for s in synth]
+    mptrs = [m.data_ptr() for m in dmasks]
+    frs = [frames_struct(subs, t, mptrs) for t in range(ticks)]
+    for t in range(1, 1 + args.warmup):
+        check(lib.lvbgs_batch_apply(hs, frs[t], n, sptr), hs[0])
+    check(lib.lvbgs_batch_wait(hs, n, sptr), hs[0])
+    sc0 = [b.scalars() for b in subs]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    with ClockSampler(local) as clk:
+        evs[0].record(stream)
+        for k in range(args.steps):
+            t = 1 + args.warmup + k
+            check(lib.lvbgs_batch_apply(hs, frs[t], n, sptr), hs[0])
+            evs[k + 1].record(stream)
+        check(lib.lvbgs_batch_wait(hs, n, sptr), hs[0])
+        torch.cuda.synchronize()
+    tick_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    total_ms = evs[0].elapsed_time(evs[-1])
+    if world > 1:
+        tt = torch.tensor([total_ms], dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(tt[0])
+    sc1 = [b.scalars() for b in subs]
+    value = px_step * args.steps * world / (total_ms / 1e3) / 1e6
+    px_by_c = {}
+    for s, a, b in zip(synth, sc0, sc1):
+        c = s.cfg.channels
+        e = px_by_c.setdefault(c, [0, 0, 0])
+        e[0] += (b["frame_idx"] - a["frame_idx"]) * b["n_relevant_px"]
+        e[1] += b["stat_samples_evaluated"] - a["stat_samples_evaluated"]
+        e[2] += b["stat_sample_writes"] - a["stat_sample_writes"]
+    alg_bytes_step = algorithmic_bytes({c: tuple(v) for c, v in px_by_c.items()}, 0, 0) / args.steps
+    ms_step = total_ms / args.steps
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg_bytes_step / (ms_step / 1e3) / 1e9
+    tick_sorted = sorted(tick_ms)
+    p50 = tick_sorted[len(tick_sorted) // 2]
+    p99 = tick_sorted[min(len(tick_sorted) - 1, int(round(0.99 * (len(tick_sorted) - 1))))]
+    rounds = sum(b["stat_repair_rounds"] - a["stat_repair_rounds"] for a, b in zip(sc0[:1], sc1[:1])) / args.steps
+    remat = sum(b["stat_repair_rematched"] - a["stat_repair_rematched"] for a, b in zip(sc0, sc1)) / args.steps
+
+    # ---- e2e through the C-ABI: pinned host frames in, host masks out ----
+    e2e = None
+    if not args.no_e2e:
+        e2e_steps = min(args.steps, 10)
+        host = []
+        for i in range(n):
+            hb = torch.empty(dev_frames[i].shape, dtype=torch.uint8, pin_memory=True)
+            hb.copy_(dev_frames[i])
+            host.append(hb.numpy())
+        hmasks = [torch.empty((s.cfg.height, s.cfg.width), dtype=torch.uint8, pin_memory=True) for s in synth]
+        hm = [m.data_ptr() for m in hmasks]
+        subs_e = make_subtractors(5000)
+        hse = (C.c_void_p * n)(*[b.handle for b in subs_e])
+        fre = [frames_struct(subs_e, t, hm, host=host) for t in range(ticks)]
+        for t in range(1, 1 + args.warmup):
+            check(lib.lvbgs_batch_apply(hse, fre[t], n, sptr), hse[0])
+        check(lib.lvbgs_batch_wait(hse, n, sptr), hse[0])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(e2e_steps):
+            t = 1 + args.warmup + k
+            check(lib.lvbgs_batch_apply(hse, fre[t], n, sptr), hse[0])
+            check(lib.lvbgs_batch_wait(hse, n, sptr), hse[0])  # masks are on the host after the wait
+        el = time.perf_counter() - t0
+        h2d = sum(int(np.prod(s.shape)) for s in synth)
+        e2e = {"value": px_step * e2e_steps / el / 1e6, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": px_step, "ms_per_step": el / e2e_steps * 1e3,
+               "note": "pinned host frames -> lvbgs_batch_apply -> host masks, wall clock incl. the waits"}
+        for b in subs_e:
+            b.close()
+
+    # ---- plain form: one stream per launch ----
+    plain = None
+    if args.plain_steps > 0:
+        subs_p = make_subtractors(1000)
+        for t in range(1, 1 + args.warmup):
+            for i, b in enumerate(subs_p):
+                one = (C.c_void_p * 1)(b.handle)
+                check(lib.lvbgs_batch_apply(one, C.byref(frs[t][i]), 1, sptr), b.handle)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ps = min(args.plain_steps, args.steps)
+        e0.record(stream)
+        for k in range(ps):
+            t = 1 + args.warmup + k
+            for i, b in enumerate(subs_p):
+                one = (C.c_void_p * 1)(b.handle)
+                check(lib.lvbgs_batch_apply(one, C.byref(frs[t][i]), 1, sptr), b.handle)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        for b in subs_p:
+            one = (C.c_void_p * 1)(b.handle)
+            check(lib.lvbgs_batch_wait(one, 1, sptr), b.handle)
+        pm = e0.elapsed_time(e1)
+        plain = {"value": px_step * ps / (pm / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_step": pm / ps,
+                 "launches_per_step": n}
+        for b in subs_p:
+            b.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline()
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8/f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "streams": n, "px_per_step": px_step,
+                       "l2": "inputs and model state (GBs) exceed L2; no flush",
+                       "parallelism": "one persistent cooperative launch per tick over all streams"},
+            "frames_per_s": n * args.steps * world / (total_ms / 1e3),
+            "p50_frame_ms": p50, "p99_frame_ms": p99,
+            "plain": plain,
+            "batched_vs_plain": (value / world / plain["value"]) if plain else None,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "note": "algorithmic bytes per tick / tick time; peak = measured copy bandwidth"},
+            "repair": {"rounds_per_tick": rounds, "rematched_px_per_tick": remat},
+            "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(out))
+    for b in subs:
+        b.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

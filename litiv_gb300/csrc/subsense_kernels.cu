@@ -471,15 +471,10 @@ __device__ void phaseA_tile(const TickParams& P, const StreamDev& S, int lt, uin
         }
         __stcg(&S.intent[p], intent);
     }
-    // per-tile reductions of the non-zero descriptor count and of the samples evaluated
-    for (int o = 16; o > 0; o >>= 1) {
-        nz += __shfl_xor_sync(0xffffffffu, nz, o);
-        e += __shfl_xor_sync(0xffffffffu, e, o);
-    }
-    if ((threadIdx.x & 31) == 0 && (nz || e)) {
-        if (nz) atomicAdd(&S.ctl->nz_acc, (unsigned long long)nz);
-        if (e) atomicAdd(&S.ctl->st_samples, (unsigned long long)e);
-    }
+    // per-warp reduction of the non-zero descriptor count (final: the descriptor does not depend
+    // on the repair)
+    for (int o = 16; o > 0; o >>= 1) nz += __shfl_xor_sync(0xffffffffu, nz, o);
+    if ((threadIdx.x & 31) == 0 && nz) atomicAdd(&S.ctl->nz_acc, (unsigned long long)nz);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -711,7 +706,7 @@ __device__ void phaseF_tile(const TickParams& P, const StreamDev& S, int lt, uin
     const FrameK F = frame_consts(S);
     const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
     const int x = x0 + lx, y = y0 + ly;
-    int nw = 0;
+    int nw = 0, ne = 0;
     if (x < W && y < H) {
         const int q = y * W + x;
         // raster-ordered commit of every write targeting q (own write before own neighbour write)
@@ -747,6 +742,7 @@ __device__ void phaseF_tile(const TickParams& P, const StreamDev& S, int lt, uin
             }
         const uint32_t wq = it[(ly + 2) * IW + lx + 2];
         uint16_t kend = 0;
+        ne = (int)in_e(wq);
         if (wq & kInValid) {
             if (wq & kInFG) kend = F.cooldown ? (uint16_t)(1 + ((wq & kInOwn) ? 1 : 0)) : 0;
             else kend = (uint16_t)(1 + ((wq & kInOwn) ? 1 : 0) + 2 + (in_nb_writes(wq) ? 1 : 0));
@@ -768,8 +764,14 @@ __device__ void phaseF_tile(const TickParams& P, const StreamDev& S, int lt, uin
             }
         __stcg(&S.preflood[q], v);
     }
-    for (int o = 16; o > 0; o >>= 1) nw += __shfl_xor_sync(0xffffffffu, nw, o);
-    if ((threadIdx.x & 31) == 0 && nw) atomicAdd(&S.ctl->st_writes, (unsigned long long)nw);
+    for (int o = 16; o > 0; o >>= 1) {
+        nw += __shfl_xor_sync(0xffffffffu, nw, o);
+        ne += __shfl_xor_sync(0xffffffffu, ne, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (nw) atomicAdd(&S.ctl->st_writes, (unsigned long long)nw);
+        if (ne) atomicAdd(&S.ctl->st_samples, (unsigned long long)ne);
+    }
 }
 
 // ------------------------------------------------------------------------------------------

@@ -1,0 +1,176 @@
+"""GPU parity tests: the CUDA path (through the C-ABI) against the oracle, bit-exact.
+
+Integer state, masks and descriptors must be identical; the FP32 feedback maps must be identical
+too (tolerance 0 ulp), since both sides use the reference's operation order without fused
+multiply-adds. Every frame compares every model map; the first mismatch is reported.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from litiv_gb300 import BackgroundSubtractorSuBSENSE, LvException, SyntheticStream, batch_apply, lbsp_compute2
+from oracle import pyoracle
+from tests.helpers import compare_state
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+MAX_ULP = 0  # FP32 tolerance of the feedback maps
+
+
+def run_pair(frames, seed=5, lrs=None, roi=None, check_every=1, with_samples=True, **params):
+    gpu = BackgroundSubtractorSuBSENSE(seed=seed, **params)
+    ora = pyoracle.OracleSuBSENSE(seed=seed, **{_oname(k): v for k, v in params.items()})
+    gpu.initialize(frames[0], roi)
+    ora.initialize(frames[0], roi)
+    bad = compare_state(gpu, ora, with_samples=with_samples)
+    assert not bad, "after initialize: " + "; ".join(bad)
+    for t, f in enumerate(frames[1:], start=1):
+        lr = 0.0 if lrs is None else lrs[t]
+        mg = gpu.apply(f, learningRateOverride=lr)
+        mo = ora.apply(f, lr)
+        assert np.array_equal(mg, mo), "frame %d: mask differs at %d px" % (t, int((mg != mo).sum()))
+        if t % check_every == 0 or t == len(frames) - 1:
+            bad = compare_state(gpu, ora, with_samples=with_samples)
+            assert not bad, "frame %d: %s" % (t, "; ".join(bad))
+    return gpu, ora
+
+
+def _oname(k):
+    return {"nDescDistThresholdOffset": "desc_dist_threshold_offset",
+            "nMinColorDistThreshold": "min_color_dist_threshold", "nBGSamples": "bg_samples",
+            "nRequiredBGSamples": "required_bg_samples", "nSamplesForMovingAvgs": "samples_for_moving_avgs",
+            "fRelLBSPThreshold": "rel_lbsp_threshold"}[k]
+
+
+def frames_of(stream, n, t0=0):
+    return [stream.render(t) for t in range(t0, t0 + n)]
+
+
+def test_lbsp_golden_vector_on_gpu():
+    img = np.load(os.path.join(GOLDEN, "lbsp_input_65x65_bgr.npy"))
+    gold = np.load(os.path.join(GOLDEN, "lbsp_abs20_65x65_u16c3.npy"))
+    desc = lbsp_compute2(img, abs_threshold=20)
+    np.testing.assert_array_equal(desc[2:-2, 2:-2], gold[2:-2, 2:-2])
+
+
+@pytest.mark.parametrize("channels", [1, 3])
+def test_lbsp_relative_matches_oracle(channels):
+    rng = np.random.default_rng(1)
+    img = rng.integers(0, 256, (53, 67, channels) if channels == 3 else (53, 67), dtype=np.uint8)
+    g = lbsp_compute2(img, rel_threshold=0.333, offset=2)
+    o = pyoracle.lbsp_compute2(img, rel_threshold=0.333, offset=2)
+    np.testing.assert_array_equal(g[2:-2, 2:-2], o[2:-2, 2:-2])
+
+
+def test_subsense_small_frame_bitexact():
+    """Small frame (frame-level analysis off, T caps x2, 9x9 median): every map, every frame."""
+    s = SyntheticStream(0, seed=3, width=48, height=40, shape_min=6, shape_max=14)
+    run_pair(frames_of(s, 25), seed=9)
+
+
+def test_subsense_config0_bitexact():
+    """320x240 BGR (config 0 shape): masks and all model state bit-exact over 60 frames."""
+    s = SyntheticStream(0, seed=1)
+    run_pair(frames_of(s, 61), seed=1, check_every=5)
+
+
+def test_subsense_gray_bitexact():
+    s = SyntheticStream(0, seed=8, channels=1)
+    run_pair(frames_of(s, 31), seed=2, check_every=5)
+
+
+def test_subsense_learning_rate_override_bitexact():
+    """lr=1 for the first frames (the changedet app's schedule, apps/changedet/src/main.cpp:390):
+    every background pixel updates itself and a neighbour, the densest raster-order dependencies."""
+    s = SyntheticStream(0, seed=4, width=96, height=72, shape_min=10, shape_max=24)
+    frames = frames_of(s, 31)
+    lrs = [1.0 if t <= 20 else 0.0 for t in range(len(frames))]
+    run_pair(frames, seed=4, lrs=lrs)
+
+
+def test_subsense_roi_bitexact():
+    s = SyntheticStream(0, seed=6)
+    roi = np.zeros((240, 320), np.uint8)
+    roi[30:210, 50:270] = 255
+    roi[100:140, 120:200] = 0
+    run_pair(frames_of(s, 21), seed=6, roi=roi, check_every=4)
+
+
+def test_subsense_auto_model_reset_bitexact():
+    """A sudden global intensity jump triggers the frame-level reset: refreshModel(0.1), T := 1."""
+    s = SyntheticStream(0, seed=12)
+    frames = frames_of(s, 48)
+    # +150 from frame 30 (before frame 25 the long- and short-term averages share one factor, so a
+    # change there cannot separate them); the reset fires at frame 43
+    for t in range(30, 48):
+        frames[t] = np.clip(frames[t].astype(np.int16) + 150, 0, 255).astype(np.uint8)
+    gpu, ora = run_pair(frames, seed=12, check_every=1)
+    assert ora.scalars()["model_reset_cooldown"] > 0  # the reset happened
+    assert gpu.scalars()["lr_lower_cap"] == 1.0
+
+
+def test_batched_streams_match_individual_runs():
+    """Three streams of different sizes / channel counts in one persistent launch per tick."""
+    streams = [SyntheticStream(0, seed=21), SyntheticStream(0, seed=22, channels=1, width=160, height=120),
+               SyntheticStream(0, seed=23, width=64, height=48, shape_min=8, shape_max=16)]
+    frames = [frames_of(s, 16) for s in streams]
+    gpus = [BackgroundSubtractorSuBSENSE(seed=100 + i) for i in range(3)]
+    oras = [pyoracle.OracleSuBSENSE(seed=100 + i) for i in range(3)]
+    for g, o, f in zip(gpus, oras, frames):
+        g.initialize(f[0])
+        o.initialize(f[0])
+    for t in range(1, 16):
+        masks = batch_apply(gpus, [f[t] for f in frames])
+        for i in range(3):
+            mo = oras[i].apply(frames[i][t])
+            assert np.array_equal(masks[i], mo), "stream %d frame %d" % (i, t)
+    for g, o in zip(gpus, oras):
+        assert not compare_state(g, o)
+
+
+def test_background_images_and_manual_refresh():
+    s = SyntheticStream(0, seed=31)
+    frames = frames_of(s, 12)
+    gpu, ora = run_pair(frames, seed=31, check_every=100)
+    np.testing.assert_array_equal(gpu.getBackgroundImage(), ora.background())
+    np.testing.assert_array_equal(gpu.getBackgroundDescriptorsImage(), ora.background_descriptors())
+    gpu.refreshModel(0.3)
+    ora.refresh_model(0.3)
+    gpu.refreshModel(1.0, True)
+    ora.refresh_model(1.0, True)
+    assert not compare_state(gpu, ora)
+    f = s.render(12)
+    assert np.array_equal(gpu.apply(f), ora.apply(f))
+    assert not compare_state(gpu, ora)
+
+
+def test_spill_restore_is_transparent():
+    s = SyntheticStream(0, seed=41, width=128, height=96)
+    frames = frames_of(s, 14)
+    a = BackgroundSubtractorSuBSENSE(seed=3)
+    b = BackgroundSubtractorSuBSENSE(seed=3)
+    a.initialize(frames[0])
+    b.initialize(frames[0])
+    for t in range(1, 14):
+        if t == 7:
+            buf = bytearray(a.state_bytes())
+            a.spill(buf)
+            with pytest.raises(LvException):
+                a.apply(frames[t])
+            a.restore(buf)
+        assert np.array_equal(a.apply(frames[t]), b.apply(frames[t]))
+
+
+def test_api_errors():
+    g = BackgroundSubtractorSuBSENSE()
+    with pytest.raises(LvException):
+        g.apply(np.zeros((20, 20, 3), np.uint8))
+    with pytest.raises(LvException):
+        g.initialize(np.zeros((20, 20, 3), np.uint8), np.full((20, 20), 3, np.uint8))
+    g.initialize(np.zeros((20, 20, 3), np.uint8))
+    with pytest.raises(LvException):
+        g.apply(np.zeros((21, 20, 3), np.uint8))
+    with pytest.raises(LvException):
+        g.refreshModel(0.0)
+    assert g.getDefaultLearningRate() == 0.0
