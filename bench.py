@@ -147,7 +147,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--streams", type=int, default=64, help="streams of the mix (debug: fewer)")
+    ap.add_argument("--streams", type=int, default=64, help="number of streams of the mix (profiling: fewer)")
+    ap.add_argument("--first", type=int, default=0, help="index of the first stream of the mix (profiling)")
     ap.add_argument("--plain-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -169,7 +170,7 @@ def main():
     lib = L.lib()
     n = args.streams
     ticks = 1 + args.warmup + args.steps
-    synth = [SyntheticStream(3, index=i, seed=1) for i in range(n)]
+    synth = [SyntheticStream(3, index=args.first + i, seed=1) for i in range(n)]
     dev_frames = []  # per stream: uint8 tensor [ticks, H, W, C]
     for s in synth:
         shp = (ticks,) + s.shape
@@ -179,8 +180,12 @@ def main():
         dev_frames.append(buf)
     torch.cuda.synchronize()
     px_step = sum(s.cfg.width * s.cfg.height for s in synth)
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library launches on it and the CUDA events are recorded on it (a NULL
+    # stream pointer would mean "the handle's own stream" to the C-ABI)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sptr = C.c_void_p(stream.cuda_stream)
+    assert stream.cuda_stream != 0
 
     def make_subtractors(seed_base):
         subs = []
@@ -252,6 +257,9 @@ def main():
     tick_sorted = sorted(tick_ms)
     p50 = tick_sorted[len(tick_sorted) // 2]
     p99 = tick_sorted[min(len(tick_sorted) - 1, int(round(0.99 * (len(tick_sorted) - 1))))]
+    prof = (C.c_double * 40)()
+    nprof = lib.lvbgs_debug_tick_profile(hs[0], 1, prof, 40)
+    phase_ms = [round(prof[i], 4) for i in range(nprof)]
     rounds = sum(b["stat_repair_rounds"] - a["stat_repair_rounds"] for a, b in zip(sc0[:1], sc1[:1])) / args.steps
     remat = sum(b["stat_repair_rematched"] - a["stat_repair_rematched"] for a, b in zip(sc0, sc1)) / args.steps
 
@@ -333,6 +341,7 @@ def main():
                          "frac": achieved / peak, "traffic": None,
                          "note": "algorithmic bytes per tick / tick time; peak = measured copy bandwidth"},
             "repair": {"rounds_per_tick": rounds, "rematched_px_per_tick": remat},
+            "phase_ms_last_tick": phase_ms,
             "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": args.steps,
             "clocks": clk.summary(),
         }

@@ -158,6 +158,11 @@ typedef struct {
 } lvbgs_scalars;
 lvbgs_status lvbgs_get_scalars(lvbgs_handle h, lvbgs_scalars* out);
 
+/* durations (ms) of the phases of the last frame step launched by h (batched != 0: the last batched
+ * step it led), in order: evaluation, ghost resolution, 2 per repair round, commit/closing,
+ * 3 hole-filling passes, median, dilation/blinks, model reset. Returns the number written. */
+int lvbgs_debug_tick_profile(lvbgs_handle h, int batched, double* out_ms, int max_n);
+
 #ifdef __cplusplus
 }
 #endif

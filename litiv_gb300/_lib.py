@@ -8,7 +8,8 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "liblvbgs.so")
+# LVBGS_LIB selects another build of the same library (e.g. to compare two builds side by side)
+LIB_PATH = os.environ.get("LVBGS_LIB") or os.path.join(HERE, "_build", "liblvbgs.so")
 
 # lvbgs_status
 OK, BAD_ARG, BAD_SIZE, BAD_TYPE, NOT_INITIALIZED, OOM, DEVICE_TIMEOUT, DEVICE_ERROR, UNSUPPORTED = range(9)
@@ -80,6 +81,7 @@ SIGNATURES = {
     "lvbgs_debug_map_bytes": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]),
     "lvbgs_debug_get_map": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]),
     "lvbgs_get_scalars": (C.c_int, [C.c_void_p, C.POINTER(LvbgsScalars)]),
+    "lvbgs_debug_tick_profile": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int]),
     "lvsynth_preset": (C.c_int, [C.c_int, C.c_int, C.c_uint64, C.POINTER(SynthConfig)]),
     "lvsynth_create": (C.c_int, [C.POINTER(SynthConfig), C.POINTER(C.c_void_p)]),
     "lvsynth_destroy": (None, [C.c_void_p]),

@@ -15,12 +15,25 @@
 #include "lvbgs_internal.h"
 
 namespace lvbgs {
-extern "C" __global__ void lvbgs_subsense_tick(TickParams P, unsigned long long dsTotal, const unsigned long long* dsBase);
+extern "C" __global__ void lvbgs_k_eval(TickParams P);
+extern "C" __global__ void lvbgs_k_resolve(TickParams P, unsigned long long dsTotal, const unsigned long long* dsBase);
+extern "C" __global__ void lvbgs_k_repair(TickParams P);
+extern "C" __global__ void lvbgs_k_commit(TickParams P);
+extern "C" __global__ void lvbgs_k_runs(TickParams P);
+extern "C" __global__ void lvbgs_k_vunion(TickParams P);
+extern "C" __global__ void lvbgs_k_holes(TickParams P);
+extern "C" __global__ void lvbgs_k_combine(TickParams P);
+extern "C" __global__ void lvbgs_k_median(TickParams P);
+extern "C" __global__ void lvbgs_k_epilogue(TickParams P);
+extern "C" __global__ void lvbgs_k_dilate(TickParams P);
+extern "C" __global__ void lvbgs_k_reset(TickParams P);
+extern "C" __global__ void lvbgs_k_close(TickParams P);
 extern "C" __global__ void lvbgs_init_maps(StreamDev S, const uint8_t* img, float tLo);
 extern "C" __global__ void lvbgs_refresh(StreamDev S, uint32_t frame, int start, int nref, int force, int lastBuf);
 extern "C" __global__ void lvbgs_background(StreamDev S, uint8_t* outCol, uint16_t* outDesc);
 extern "C" __global__ void lvbgs_unpack_samples(StreamDev S, uint8_t* col, uint16_t* desc);
 extern "C" __global__ void lvbgs_pack_samples(StreamDev S, const uint8_t* col, const uint16_t* desc);
+extern "C" __global__ void lvbgs_init_tables();
 extern "C" __global__ void lvbgs_lbsp_dense(const uint8_t* img, int W, int H, int C, int absThr, float rel,
                                             unsigned int off, uint16_t* desc);
 }  // namespace lvbgs
@@ -233,7 +246,7 @@ cudaError_t coop_grid(int* maxBlocks) {
         cudaError_t e = cudaGetDevice(&dev);
         if (e != cudaSuccess) return e;
         if ((e = cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_coop_blocks_per_sm, lvbgs_subsense_tick, kThreads, 0)) !=
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_coop_blocks_per_sm, lvbgs_k_repair, kThreads, 0)) !=
             cudaSuccess)
             return e;
     }
@@ -243,17 +256,19 @@ cudaError_t coop_grid(int* maxBlocks) {
 
 // enqueue one tick over n streams described in ws.h_streams (tileBase etc. filled here)
 lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t st) {
-    int totalTiles = 0;
+    int totalTiles = 0, totalRows = 0;
     size_t totalPx = 0;
     unsigned long long ds = 0;
     ws.h_dsBase.resize(n + 1);
     for (int i = 0; i < n; ++i) {
         StreamDev& S = ws.h_streams[i];
         S.tileBase = totalTiles;
+        S.rowBase = totalRows;
         totalTiles += S.nTiles;
+        totalRows += S.H;
         totalPx += (size_t)S.npx;
         ws.h_dsBase[i] = ds;
-        // only streams with the frame-level analysis enabled down-sample (flag mirrored on the host)
+        // only streams with the frame-level analysis enabled down-sample
         if (S.lrScaling) ds += (unsigned long long)S.dsW * S.dsH;
     }
     ws.h_dsBase[n] = ds;
@@ -266,12 +281,12 @@ lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t s
     LV_CUDA(errh, cudaMemsetAsync(ws.work, 0, sizeof(TickWork), st), "work reset");
     int maxBlocks = 0;
     LV_CUDA(errh, coop_grid(&maxBlocks), "occupancy query");
-    if (maxBlocks <= 0) return fail(errh, LVBGS_DEVICE_ERROR, "tick kernel cannot be resident on this device");
-    const int grid = std::max(1, std::min(maxBlocks, totalTiles));
+    if (maxBlocks <= 0) return fail(errh, LVBGS_DEVICE_ERROR, "repair kernel cannot be resident on this device");
     TickParams P;
     P.streams = ws.d_streams;
     P.nStreams = n;
     P.totalTiles = totalTiles;
+    P.totalRows = totalRows;
     P.work = ws.work;
     P.dlist[0] = ws.lists;
     P.dlist[1] = ws.lists + ws.cap;
@@ -279,10 +294,28 @@ lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t s
     P.rlist[1] = ws.lists + 3 * ws.cap;
     P.listCap = (unsigned)std::min<size_t>(ws.cap, 0xffffffffu);
     const unsigned long long* dsb = ws.d_dsBase;
-    void* args[] = {&P, &ds, &dsb};
-    LV_CUDA(errh,
-            cudaLaunchCooperativeKernel((const void*)lvbgs_subsense_tick, dim3(grid), dim3(kThreads), args, 0, st),
-            "tick kernel launch");
+    const dim3 blk(kThreads);
+    const int rowBlocks = (totalRows + 7) / 8;
+    const int dsBlocks = (int)((ds + kThreads - 1) / kThreads);
+    lvbgs_k_eval<<<totalTiles, blk, 0, st>>>(P);
+    lvbgs_k_resolve<<<totalTiles + dsBlocks, blk, 0, st>>>(P, ds, dsb);
+    {
+        const int grid = std::max(1, std::min(maxBlocks, std::max(1, totalTiles)));
+        void* args[] = {&P};
+        LV_CUDA(errh, cudaLaunchCooperativeKernel((const void*)lvbgs_k_repair, dim3(grid), blk, args, 0, st),
+                "repair kernel launch");
+    }
+    lvbgs_k_commit<<<totalTiles, blk, 0, st>>>(P);
+    lvbgs_k_runs<<<rowBlocks, blk, 0, st>>>(P);
+    lvbgs_k_vunion<<<rowBlocks, blk, 0, st>>>(P);
+    lvbgs_k_holes<<<rowBlocks, blk, 0, st>>>(P);
+    lvbgs_k_combine<<<totalTiles, blk, 0, st>>>(P);
+    lvbgs_k_median<<<totalTiles, blk, 0, st>>>(P);
+    lvbgs_k_epilogue<<<1, 128, 0, st>>>(P);
+    lvbgs_k_dilate<<<totalTiles, blk, 0, st>>>(P);
+    lvbgs_k_reset<<<std::max(1, std::min(totalTiles, g_sm_count * 8)), blk, 0, st>>>(P);
+    lvbgs_k_close<<<1, 128, 0, st>>>(P);
+    LV_CUDA(errh, cudaGetLastError(), "frame step launch");
     return LVBGS_OK;
 }
 
@@ -408,13 +441,27 @@ lvbgs_status lvbgs_create(lvbgs_algo algo, const lvbgs_params* p, lvbgs_handle* 
     }
     if (cudaSetDevice(prm.device_id) != cudaSuccess) return fail(nullptr, LVBGS_DEVICE_ERROR, "cannot select the CUDA device");
     cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, (const void*)lvbgs_subsense_tick) != cudaSuccess) {
+    if (cudaFuncGetAttributes(&fa, (const void*)lvbgs_k_eval) != cudaSuccess) {
         cudaGetLastError();
         return fail(nullptr, LVBGS_DEVICE_ERROR, "the library's sm_103a kernels cannot run on this device");
     }
     int coop = 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, prm.device_id);
     if (!coop) return fail(nullptr, LVBGS_DEVICE_ERROR, "device does not support cooperative launches");
+    {
+        // exact division tables, once per device
+        static std::mutex mu;
+        static std::vector<int> done;
+        std::lock_guard<std::mutex> lk(mu);
+        if (std::find(done.begin(), done.end(), prm.device_id) == done.end()) {
+            lvbgs_init_tables<<<1, 256>>>();
+            if (cudaDeviceSynchronize() != cudaSuccess) {
+                cudaGetLastError();
+                return fail(nullptr, LVBGS_DEVICE_ERROR, "table initialization failed");
+            }
+            done.push_back(prm.device_id);
+        }
+    }
     lvbgs_ctx* h = new lvbgs_ctx();
     h->algo = algo;
     h->prm = prm;
@@ -505,6 +552,7 @@ lvbgs_status lvbgs_initialize(lvbgs_handle h, const uint8_t* img, int W, int H, 
     ctl.n_rel = fin;
     ctl.orig_roi = orig;
     ctl.stamp_base = 1;
+    frame_factors(1ull, (int)h->prm.samples_for_moving_avgs, &ctl.fLT, &ctl.fST, &ctl.bLT, &ctl.bST);
     // (re)allocate the device model
     if (h->stream) cudaStreamSynchronize(h->stream);
     cudaFree(h->dmem);
@@ -823,6 +871,18 @@ lvbgs_status lvbgs_debug_get_map(lvbgs_handle h, int which, void* out, size_t by
     cudaFree(ddesc);
     if (e != cudaSuccess) return cuda_fail(h, e, "sample download");
     return LVBGS_OK;
+}
+
+int lvbgs_debug_tick_profile(lvbgs_handle h, int batched, double* out_ms, int max_n) {
+    if (!h || !out_ms || max_n <= 0) return 0;
+    Workspace& ws = batched ? h->batchWs : h->ws;
+    if (!ws.work) return 0;
+    TickWork w;
+    if (cudaMemcpy(&w, ws.work, sizeof(TickWork), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+    const int n = (int)std::min<unsigned>(w.nts, 40u);
+    int k = 0;
+    for (int i = 1; i < n && k < max_n; ++i) out_ms[k++] = (double)(w.ts[i] - w.ts[i - 1]) * 1e-6;
+    return k;
 }
 
 lvbgs_status lvbgs_get_scalars(lvbgs_handle h, lvbgs_scalars* out) {

@@ -66,6 +66,17 @@ LV_HD void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
     c[3] = x3;
 }
 
+// rolling-average factors of frame f (BackgroundSubtractorSuBSENSE.cpp:198-199): 1/min(f, N_mv) and
+// 1/min(f, N_mv/4), and the addWeighted mask weights (1.0/255)*factor of the final-segmentation
+// averages (:553-554); computed once per frame instead of per pixel
+LV_HD void frame_factors(unsigned long long f, int nmv, float* fLT, float* fST, float* bLT, float* bST) {
+    const unsigned long long nlt = (unsigned long long)nmv, nst = (unsigned long long)(nmv / 4);
+    *fLT = 1.0f / (float)(f < nlt ? f : nlt);
+    *fST = 1.0f / (float)(f < nst ? f : nst);
+    *bLT = (float)((1.0 / 255) * (double)*fLT);
+    *bST = (float)((1.0 / 255) * (double)*fST);
+}
+
 // ---- per-pixel "intent" word: outcome of the pixel's evaluation in the current frame ----
 // bit 0 valid (ROI pixel evaluated this frame), bit 1 foreground, bits 2-8 samples evaluated,
 // bit 9 own-sample write, bits 10-15 own sample index, bits 16-20 neighbour code (dy+2)*5+(dx+2)
@@ -99,6 +110,7 @@ struct StreamCtl {
     unsigned long long frames_since_reset, cooldown;
     int auto_reset, lr_scaling, use3x3, median_k;
     float t_lo, t_hi, last_nz_ratio, pad0;
+    float fLT, fST, bLT, bST;  // rolling-average factors of the next frame and their addWeighted weights
     unsigned long long nz_acc, colordiff_acc;    // accumulators of the frame in flight
     unsigned long long last_nz, last_colordiff;  // values of the last completed frame
     unsigned long long st_samples, st_writes, st_rounds, st_rematched;
@@ -112,6 +124,7 @@ struct StreamCtl {
 struct StreamDev {
     int W, H, C, npx;
     int tilesX, tilesY, tileBase, nTiles;
+    int rowBase, pad0;  // first row of this stream in the batch's row index space
     int dsW, dsH, dsSX, dsSY;
     int N, nreq, minColor, descOff, stabColorOff, nmv;
     float relThr;
@@ -148,6 +161,8 @@ struct TickWork {
     unsigned int dcount[2], rcount[2];
     unsigned int done_ctas, iters;
     unsigned long long rematched;
+    unsigned long long ts[40];  // %globaltimer after each grid barrier (CTA 0), for the phase profile
+    unsigned int nts, anyReset;  // anyReset: some stream refreshes its model this frame
 };
 
 // error codes reported in TickWork::err
@@ -157,6 +172,7 @@ struct TickParams {
     StreamDev* streams;
     int nStreams;
     int totalTiles;
+    int totalRows;
     TickWork* work;
     unsigned long long* dlist[2];  // (stream << 40) | pixel
     unsigned long long* rlist[2];

@@ -82,6 +82,7 @@ __device__ bool grid_sync(TickWork* w) {
         s_ok = ok && (ld_volatile(&w->err) == 0u);
     }
     __syncthreads();
+    if (blockIdx.x == 0 && threadIdx.x == 0 && w->nts < 40u) w->ts[w->nts++] = gtimer();
     return s_ok != 0;
 }
 
@@ -93,15 +94,6 @@ __device__ __forceinline__ int find_stream_by_tile(const TickParams& P, int t) {
         else hi = mid - 1;
     }
     return lo;
-}
-
-// dynamic tile queue: returns the next tile index of phase `ph` (or >= totalTiles when done)
-__device__ __forceinline__ int next_tile(const TickParams& P, int ph) {
-    __shared__ int s_t;
-    __syncthreads();
-    if (threadIdx.x == 0) s_t = (int)atomicAdd(&P.work->phase_ctr[ph], 1u);
-    __syncthreads();
-    return s_t;
 }
 
 struct DrawState {
@@ -156,13 +148,22 @@ struct FrameK {
     int cooldown;  // m_nModelResetCooldown != 0
     int use3x3;
 };
+// exact quotients i/765, i/255, i/48 and i/16 (IEEE division on the device, done once): the
+// normalized distances of :254/:258/:272 and :396/:400/:416 divide small integers by constants
+__device__ float g_div_col3[766], g_div_col1[256], g_div_desc3[49], g_div_desc1[17];
+extern "C" __global__ void lvbgs_init_tables() {
+    for (int i = threadIdx.x; i < 766; i += blockDim.x) g_div_col3[i] = (float)i / 765.0f;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) g_div_col1[i] = (float)i / 255.0f;
+    for (int i = threadIdx.x; i < 49; i += blockDim.x) g_div_desc3[i] = (float)i / 48.0f;
+    for (int i = threadIdx.x; i < 17; i += blockDim.x) g_div_desc1[i] = (float)i / 16.0f;
+}
+
 __device__ __forceinline__ FrameK frame_consts(const StreamDev& S) {
     const StreamCtl* ctl = S.ctl;
     FrameK F;
     const unsigned long long f = ctl->frame_idx + 1ull;
-    const unsigned long long nlt = (unsigned long long)S.nmv, nst = (unsigned long long)(S.nmv / 4);
-    F.fLT = 1.0f / (float)(f < nlt ? f : nlt);
-    F.fST = 1.0f / (float)(f < nst ? f : nst);
+    F.fLT = ctl->fLT;
+    F.fST = ctl->fST;
     F.frame = (uint32_t)f;
     F.cur = (int)(ctl->frame_idx & 1ull);
     F.nxt = F.cur ^ 1;
@@ -185,27 +186,63 @@ struct Ovr {
 // frame-start samples (optionally overridden). Writes the pixel's next-frame maps and returns
 // its intent word. (1ch: BackgroundSubtractorSuBSENSE.cpp:201-330, 3ch: :333-481)
 // ------------------------------------------------------------------------------------------
+// per-pixel inputs of one evaluation, loaded up front so that all of them are in flight together
+template <int C>
+struct PixIn {
+    float R, V, T, DL, DmLT, DmST, RwLT, RwST, FnLT, FnST;
+    uint32_t uOld, lastFG, blink;
+    uint32_t lc[C], ld[C];
+    uint64_t d0, d1;  // samples 0 and 1 (descriptor plane word)
+    uint32_t c0, c1;  // samples 0 and 1 (colour byte plane)
+};
+template <int C>
+__device__ __forceinline__ void load_pix(const StreamDev& S, const FrameK& F, int p, PixIn<C>& in) {
+    const int npx = S.npx;
+    const float* fc = S.fm + (size_t)F.cur * kNumFloatMaps * npx;
+    in.R = fc[FM_R * npx + p];
+    in.V = fc[FM_V * npx + p];
+    in.T = fc[FM_T * npx + p];
+    in.DL = fc[FM_DLAST * npx + p];
+    in.DmLT = fc[FM_DMIN_LT * npx + p];
+    in.DmST = fc[FM_DMIN_ST * npx + p];
+    in.RwLT = fc[FM_RAW_LT * npx + p];
+    in.RwST = fc[FM_RAW_ST * npx + p];
+    in.FnLT = fc[FM_FIN_LT * npx + p];
+    in.FnST = fc[FM_FIN_ST * npx + p];
+    in.uOld = S.unst[(size_t)F.cur * npx + p];
+    in.lastFG = S.lastFG[p];
+    in.blink = S.blinks[p];
+    const uint8_t* lc = S.lastCol + (size_t)F.cur * npx * C + (size_t)p * C;
+    const uint16_t* ld = S.lastDesc + (size_t)F.cur * npx * C + (size_t)p * C;
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        in.lc[c] = lc[c];
+        in.ld[c] = ld[c];
+    }
+    in.d0 = in.d1 = 0;
+    in.c0 = in.c1 = 0;
+    if (S.N > 0) {
+        in.d0 = C == 3 ? ((const uint64_t*)S.sD)[p] : (uint64_t)((const uint16_t*)S.sD)[p];
+        in.c0 = S.sC[p];
+    }
+    if (S.N > 1) {
+        in.d1 = C == 3 ? ((const uint64_t*)S.sD)[(size_t)npx + p] : (uint64_t)((const uint16_t*)S.sD)[(size_t)npx + p];
+        in.c1 = S.sC[(size_t)npx + p];
+    }
+}
+
 template <int C, bool OVR>
 __device__ uint32_t eval_pixel(const StreamDev& S, const FrameK& F, const uint8_t* __restrict__ lut, int x, int y,
-                               int p, const uint32_t (&vals)[C][4], const uint32_t (&curr)[C],
+                               int p, const PixIn<C>& in, const uint32_t (&vals)[C][4], const uint32_t (&curr)[C],
                                const uint32_t (&intra)[C], const Ovr* ov, int nov, uint64_t ovmask, int& nz,
                                int& e_out) {
     const int npx = S.npx;
-    const float* fc = S.fm + (size_t)F.cur * kNumFloatMaps * npx;
     float* fn = S.fm + (size_t)F.nxt * kNumFloatMaps * npx;
-    float R = fc[FM_R * npx + p];
-    float V = fc[FM_V * npx + p];
-    float T = fc[FM_T * npx + p];
-    const float DL = fc[FM_DLAST * npx + p];
-    float DmLT = fc[FM_DMIN_LT * npx + p];
-    float DmST = fc[FM_DMIN_ST * npx + p];
-    float RwLT = fc[FM_RAW_LT * npx + p];
-    float RwST = fc[FM_RAW_ST * npx + p];
-    const float FnLT = fc[FM_FIN_LT * npx + p];
-    const float FnST = fc[FM_FIN_ST * npx + p];
-    const uint32_t uOld = S.unst[(size_t)F.cur * npx + p];
-    const uint32_t lastFG = S.lastFG[p];
-    const uint32_t blink = S.blinks[p];
+    float R = in.R, V = in.V, T = in.T;
+    const float DL = in.DL;
+    float DmLT = in.DmLT, DmST = in.DmST, RwLT = in.RwLT, RwST = in.RwST;
+    const float FnLT = in.FnLT, FnST = in.FnST;
+    const uint32_t uOld = in.uOld, lastFG = in.lastFG, blink = in.blink;
 
     // thresholds from R(x) and the previous unstable flag
     const uint32_t colThr =
@@ -218,19 +255,26 @@ __device__ uint32_t eval_pixel(const StreamDev& S, const FrameK& F, const uint8_
     const int N = S.N, nreq = S.nreq;
     int nGood = 0, s = 0;
     uint32_t minDesc = C == 1 ? 16u : 48u, minSum = C == 1 ? 255u : 765u;
+    // Samples 0 and 1 arrive with the feedback maps; the loop then requests sample s+2 while it
+    // evaluates sample s (a rotating pair). The kernel is latency-bound, so the up-to-two wasted
+    // sample reads of an early exit are cheaper than waiting on a load.
     if (C == 1) {
         const uint32_t cthr = colThr / 2u;
         const uint16_t* sD = (const uint16_t*)S.sD;
+        uint32_t dA = (uint32_t)in.d0, dB = (uint32_t)in.d1, cA = in.c0, cB = in.c1;
         while (nGood < nreq && s < N) {
-            uint32_t bgc, bgd;
+            uint32_t bgc = cA, bgd = dA;
+            dA = dB;
+            cA = cB;
+            if (s + 2 < N) {
+                dB = sD[(size_t)(s + 2) * npx + p];
+                cB = S.sC[(size_t)(s + 2) * npx + p];
+            }
             if (OVR && ((ovmask >> s) & 1ull)) {
                 int k = nov - 1;
                 while (ov[k].s != s) --k;
                 bgc = ov[k].col & 0xffu;
                 bgd = (uint32_t)(ov[k].desc & 0xffffu);
-            } else {
-                bgc = S.sC[(size_t)s * npx + p];
-                bgd = sD[(size_t)s * npx + p];
             }
             const uint32_t colDist = (uint32_t)abs((int)curr[0] - (int)bgc);
             if (colDist <= cthr) {
@@ -253,27 +297,28 @@ __device__ uint32_t eval_pixel(const StreamDev& S, const FrameK& F, const uint8_
         const uint32_t totColThr = colThr * 3u, scThr = totColThr / 2u;
         const unsigned long long totDescThr = descThr * 3ull;
         const uint64_t* sD = (const uint64_t*)S.sD;
+        uint64_t dA = in.d0, dB = in.d1;
+        uint32_t cA = in.c0, cB = in.c1;
         while (nGood < nreq && s < N) {
-            uint64_t d;
-            uint32_t c2 = 0;
-            bool ovr = false;
+            uint64_t d = dA;
+            uint32_t c2 = cA;
+            dA = dB;
+            cA = cB;
+            if (s + 2 < N) {
+                dB = sD[(size_t)(s + 2) * npx + p];
+                cB = S.sC[(size_t)(s + 2) * npx + p];
+            }
             if (OVR && ((ovmask >> s) & 1ull)) {
                 int k = nov - 1;
                 while (ov[k].s != s) --k;
                 d = ov[k].desc | ((uint64_t)(ov[k].col & 0xffffu) << 48);
                 c2 = (ov[k].col >> 16) & 0xffu;
-                ovr = true;
-            } else {
-                d = sD[(size_t)s * npx + p];
             }
             uint32_t totDesc = 0, totSum = 0;
             bool ok = true;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                uint32_t bgc;
-                if (c == 0) bgc = (uint32_t)(d >> 48) & 0xffu;
-                else if (c == 1) bgc = (uint32_t)(d >> 56) & 0xffu;
-                else bgc = ovr ? c2 : (uint32_t)S.sC[(size_t)s * npx + p];
+                const uint32_t bgc = c == 0 ? (uint32_t)(d >> 48) & 0xffu : c == 1 ? (uint32_t)(d >> 56) & 0xffu : c2;
                 const uint32_t bgd = (uint32_t)(d >> (16 * c)) & 0xffffu;
                 const uint32_t colDist = (uint32_t)abs((int)curr[c] - (int)bgc);
                 if (colDist > scThr) {
@@ -303,16 +348,15 @@ __device__ uint32_t eval_pixel(const StreamDev& S, const FrameK& F, const uint8_
     e_out = s;
 
     // D_last (:254-255 / :396-397): depends on the pixel alone
-    const uint8_t* lc = S.lastCol + (size_t)F.cur * npx * C + (size_t)p * C;
-    const uint16_t* ld = S.lastDesc + (size_t)F.cur * npx * C + (size_t)p * C;
     uint32_t l1 = 0, hd = 0;
 #pragma unroll
     for (int c = 0; c < C; ++c) {
-        l1 += (uint32_t)abs((int)lc[c] - (int)curr[c]);
-        hd += __popc((uint32_t)ld[c] ^ intra[c]);
+        l1 += (uint32_t)abs((int)in.lc[c] - (int)curr[c]);
+        hd += __popc(in.ld[c] ^ intra[c]);
     }
-    const float colMax = C == 1 ? 255.0f : 765.0f, descMax = C == 1 ? 16.0f : 48.0f;
-    const float normLast = ((float)l1 / colMax + (float)hd / descMax) / 2;
+    const float* divCol = C == 1 ? g_div_col1 : g_div_col3;    // i / 255 or i / 765
+    const float* divDesc = C == 1 ? g_div_desc1 : g_div_desc3;  // i / 16 or i / 48
+    const float normLast = (__ldg(&divCol[l1]) + __ldg(&divDesc[hd])) / 2;
     const float DLn = DL * (1.0f - F.fST) + normLast * F.fST;
 
     uint32_t intent = kInValid | ((uint32_t)s << kInEShift);
@@ -321,7 +365,7 @@ __device__ uint32_t eval_pixel(const StreamDev& S, const FrameK& F, const uint8_
     const uint32_t seedFrame = F.frame;
     const bool fg = nGood < nreq;
     if (fg) {
-        const float md = ((float)minSum / colMax + (float)minDesc / descMax) / 2 + (float)(nreq - nGood) / (float)nreq;
+        const float md = (__ldg(&divCol[minSum]) + __ldg(&divDesc[minDesc])) / 2 + (float)(nreq - nGood) / (float)nreq;
         const float nmd = fmin_std(1.0f, md);
         DmLT = DmLT * (1.0f - F.fLT) + nmd * F.fLT;
         DmST = DmST * (1.0f - F.fST) + nmd * F.fST;
@@ -333,7 +377,7 @@ __device__ uint32_t eval_pixel(const StreamDev& S, const FrameK& F, const uint8_
             intent |= kInOwn | (so << kInSOwnShift);
         }
     } else {
-        const float nmd = ((float)minSum / colMax + (float)minDesc / descMax) / 2;
+        const float nmd = (__ldg(&divCol[minSum]) + __ldg(&divDesc[minDesc])) / 2;
         DmLT = DmLT * (1.0f - F.fLT) + nmd * F.fLT;
         DmST = DmST * (1.0f - F.fST) + nmd * F.fST;
         RwLT = RwLT * (1.0f - F.fLT);
@@ -440,26 +484,53 @@ template <int C>
 __device__ void phaseA_tile(const TickParams& P, const StreamDev& S, int lt, uint8_t* smem) {
     const int tx = lt % S.tilesX, ty = lt / S.tilesX;
     const int x0 = tx * kTileW, y0 = ty * kTileH;
-    constexpr int RW = (kTileW + 2 * kBorder) * C;  // tile row bytes incl. halo
+    // The tile holds rows y0-2 .. y0+9 of the frame; row r of the tile starts at frame byte
+    // (x0-2)*C - 2, which is 4-byte aligned for C in {1,3} and x0 a multiple of 32, so it is filled
+    // with aligned 32-bit loads when the frame rows are 4-byte aligned.
+    constexpr int NWORDS = ((kTileW + 2 * kBorder) * C + 2 + 3) / 4;  // words per tile row
+    constexpr int RW = NWORDS * 4;                                     // tile row stride (bytes)
     constexpr int RH = kTileH + 2 * kBorder;
-    uint8_t* tile = smem;
-    uint8_t* lut = smem + RW * RH;
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = S.ctl->lut[i];
-    for (int i = threadIdx.x; i < RW * RH; i += blockDim.x) {
-        const int r = i / RW, cb = i % RW;
-        const int gy = y0 - kBorder + r, gx = x0 - kBorder + cb / C;
-        tile[i] = (gy >= 0 && gy < S.H && gx >= 0 && gx < S.W) ? __ldg(S.frame + ((size_t)gy * S.W + gx) * C + cb % C) : 0;
-    }
-    __syncthreads();
     const FrameK F = frame_consts(S);
     const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
     const int x = x0 + lx, y = y0 + ly;
+    const bool inFrame = x < S.W && y < S.H;
+    const int p = y * S.W + x;
+    const bool active = inFrame && S.roi[p] != 0;
+    // per-pixel loads first: they overlap the tile load below
+    PixIn<C> in;
+    if (active) load_pix<C>(S, F, p, in);
+    uint8_t* tile = smem;
+    uint8_t* lut = smem + RW * RH;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = S.ctl->lut[i];
+    const long rowBytes = (long)S.W * C;
+    const long b0 = (long)(x0 - kBorder) * C - 2;  // frame byte of tile column 0
+#ifdef LV_AB_BYTE_TILE
+    const bool wordPath = false;
+#else
+    const bool wordPath = (rowBytes & 3) == 0 && (((uintptr_t)S.frame) & 3) == 0;
+#endif
+    for (int i = threadIdx.x; i < NWORDS * RH; i += blockDim.x) {
+        const int r = i / NWORDS, wi = i % NWORDS;
+        const int gy = y0 - kBorder + r;
+        const long b = b0 + 4 * wi;
+        uint32_t v = 0;
+        if (gy >= 0 && gy < S.H) {
+            const uint8_t* row = S.frame + (size_t)gy * rowBytes;
+            if (wordPath && b >= 0 && b + 4 <= rowBytes) {
+                v = __ldg((const uint32_t*)(row + b));
+            } else {
+                for (int k = 0; k < 4; ++k)
+                    if (b + k >= 0 && b + k < rowBytes) v |= (uint32_t)__ldg(row + b + k) << (8 * k);
+            }
+        }
+        *(uint32_t*)(tile + r * RW + 4 * wi) = v;
+    }
+    __syncthreads();
     int nz = 0, e = 0;
-    if (x < S.W && y < S.H) {
-        const int p = y * S.W + x;
+    if (inFrame) {
         uint32_t intent = 0;
-        if (S.roi[p]) {
-            const uint8_t* base = tile + (ly + kBorder) * RW + (lx + kBorder) * C;
+        if (active) {
+            const uint8_t* base = tile + (ly + kBorder) * RW + (lx + kBorder) * C + 2;
             uint32_t vals[C][4], curr[C], intra[C];
 #pragma unroll
             for (int c = 0; c < C; ++c) {
@@ -467,7 +538,7 @@ __device__ void phaseA_tile(const TickParams& P, const StreamDev& S, int lt, uin
                 curr[c] = base[c];
                 intra[c] = lbsp_thr(vals[c], curr[c], lut[curr[c]]);
             }
-            intent = eval_pixel<C, false>(S, F, lut, x, y, p, vals, curr, intra, nullptr, 0, 0ull, nz, e);
+            intent = eval_pixel<C, false>(S, F, lut, x, y, p, in, vals, curr, intra, nullptr, 0, 0ull, nz, e);
         }
         __stcg(&S.intent[p], intent);
     }
@@ -621,7 +692,9 @@ __device__ void rematch_item(const TickParams& P, int si, const StreamDev& S, in
     }
     atomicAdd(&S.ctl->st_rematched, 1ull);
     int nz = 0, e = 0;
-    uint32_t wNew = eval_pixel<C, true>(S, F, S.ctl->lut, x, y, q, vals, curr, intra, ov, nov, mask, nz, e);
+    PixIn<C> in;
+    load_pix<C>(S, F, q, in);
+    uint32_t wNew = eval_pixel<C, true>(S, F, S.ctl->lut, x, y, q, in, vals, curr, intra, ov, nov, mask, nz, e);
     const bool decChanged = ((wNew ^ wOld) & kInFG) != 0u;
     if (!decChanged) {
         // same decision: same draws, same updates; keep the resolved neighbour state
@@ -689,6 +762,10 @@ __device__ void phaseF_tile(const TickParams& P, const StreamDev& S, int lt, uin
     uint32_t* it = (uint32_t*)smem;
     uint8_t* dil = smem + IW * IH * 4;  // (kTileW+2) x (kTileH+2) dilated raw mask
     const int W = S.W, H = S.H, npx = S.npx;
+    const int lx0 = threadIdx.x % kTileW, ly0 = threadIdx.x / kTileW;
+    const bool inF = x0 + lx0 < W && y0 + ly0 < H;
+    const int q0 = (y0 + ly0) * W + x0 + lx0;
+    const uint8_t lastRaw = inF ? S.lastRawFG[q0] : 0, lastRawBlink = inF ? S.lastRawBlink[q0] : 0;
     for (int i = threadIdx.x; i < IW * IH; i += blockDim.x) {
         const int gy = y0 - 2 + i / IW, gx = x0 - 2 + i % IW;
         it[i] = (gy >= 0 && gy < H && gx >= 0 && gx < W) ? __ldcg(&S.intent[gy * W + gx]) : 0u;
@@ -709,37 +786,32 @@ __device__ void phaseF_tile(const TickParams& P, const StreamDev& S, int lt, uin
     int nw = 0, ne = 0;
     if (x < W && y < H) {
         const int q = y * W + x;
-        // raster-ordered commit of every write targeting q (own write before own neighbour write)
-        for (int dy = -2; dy <= 2; ++dy)
-            for (int dx = -2; dx <= 2; ++dx) {
-                const uint32_t w = it[(ly + 2 + dy) * IW + lx + 2 + dx];
-                if (!(w & kInValid)) continue;
-                const int px = x + dx, py = y + dy;
-                const int p = py * W + px;
-                for (int pass = 0; pass < 2; ++pass) {
-                    int s;
-                    if (pass == 0) {
-                        if (dx != 0 || dy != 0 || !(w & kInOwn)) continue;
-                        s = (int)in_sown(w);
-                    } else {
-                        if (!in_nb_writes(w) || (int)in_code(w) != (-dy + 2) * 5 + (-dx + 2)) continue;
-                        s = (int)in_snb(w);
-                    }
-                    const uint16_t* ldn = S.lastDesc + (size_t)F.nxt * npx * C + (size_t)p * C;
-                    if (C == 3) {
-                        const uint64_t d = (uint64_t)__ldcg(&ldn[0]) | ((uint64_t)__ldcg(&ldn[1]) << 16) |
-                                           ((uint64_t)__ldcg(&ldn[2]) << 32) |
-                                           ((uint64_t)__ldg(S.frame + (size_t)p * 3) << 48) |
-                                           ((uint64_t)__ldg(S.frame + (size_t)p * 3 + 1) << 56);
-                        ((uint64_t*)S.sD)[(size_t)s * npx + q] = d;
-                        S.sC[(size_t)s * npx + q] = __ldg(S.frame + (size_t)p * 3 + 2);
-                    } else {
-                        ((uint16_t*)S.sD)[(size_t)s * npx + q] = __ldcg(&ldn[0]);
-                        S.sC[(size_t)s * npx + q] = __ldg(S.frame + p);
-                    }
-                    ++nw;
-                }
+        // raster-ordered commit of every write targeting q (own write before own neighbour write).
+        // A writer at window slot k = (dy+2)*5 + (dx+2) targets q iff it is valid, its neighbour
+        // state is WRITE or GHOST_WRITE (state & 5 == 1) and its code is 24 - k.
+        constexpr uint32_t kNbMask = kInValid | (31u << kInCodeShift) | (5u << kInNStShift);
+        auto commit_write = [&](int p, int s) {
+            const uint16_t* ldn = S.lastDesc + (size_t)F.nxt * npx * C + (size_t)p * C;
+            if (C == 3) {
+                const uint64_t d = (uint64_t)__ldcg(&ldn[0]) | ((uint64_t)__ldcg(&ldn[1]) << 16) |
+                                   ((uint64_t)__ldcg(&ldn[2]) << 32) | ((uint64_t)__ldg(S.frame + (size_t)p * 3) << 48) |
+                                   ((uint64_t)__ldg(S.frame + (size_t)p * 3 + 1) << 56);
+                ((uint64_t*)S.sD)[(size_t)s * npx + q] = d;
+                S.sC[(size_t)s * npx + q] = __ldg(S.frame + (size_t)p * 3 + 2);
+            } else {
+                ((uint16_t*)S.sD)[(size_t)s * npx + q] = __ldcg(&ldn[0]);
+                S.sC[(size_t)s * npx + q] = __ldg(S.frame + p);
             }
+            ++nw;
+        };
+#pragma unroll
+        for (int k = 0; k < 25; ++k) {
+            const int dy = k / 5 - 2, dx = k % 5 - 2;
+            const uint32_t w = it[(ly + 2 + dy) * IW + lx + 2 + dx];
+            if (k == 12 && (w & kInValid) && (w & kInOwn)) commit_write(q, (int)in_sown(w));
+            if ((w & kNbMask) == (kInValid | ((uint32_t)(24 - k) << kInCodeShift) | (1u << kInNStShift)))
+                commit_write((y + dy) * W + (x + dx), (int)in_snb(w));
+        }
         const uint32_t wq = it[(ly + 2) * IW + lx + 2];
         uint16_t kend = 0;
         ne = (int)in_e(wq);
@@ -750,8 +822,8 @@ __device__ void phaseF_tile(const TickParams& P, const StreamDev& S, int lt, uin
         S.kctr[q] = kend;
         // blinks (:536-539)
         const uint8_t raw = (wq & kInFG) ? 255 : 0;
-        const uint8_t cb = raw ^ S.lastRawFG[q];
-        S.blinks[q] = cb | S.lastRawBlink[q];
+        const uint8_t cb = raw ^ lastRaw;
+        S.blinks[q] = cb | lastRawBlink;
         S.lastRawBlink[q] = cb;
         S.lastRawFG[q] = raw;
         // closing: erosion of the dilated mask (out-of-frame pixels never win)
@@ -775,10 +847,12 @@ __device__ void phaseF_tile(const TickParams& P, const StreamDev& S, int lt, uin
 }
 
 // ------------------------------------------------------------------------------------------
-// hole filling: cv::floodFill from (0,0) on the closed mask, rebuilt as border-seeded union-find.
-// The closed mask is 0 on the 2-pixel frame border (no ROI pixel lies there), so the component of
-// 0-pixels that contains pixel 0 is exactly the flood-filled region; with minimum-index roots its
-// root is 0, and holes are the 0-pixels whose root is not 0.
+// hole filling: cv::floodFill(closed, (0,0), 255) + bitwise_not (:541-543), rebuilt as union-find
+// over the runs of 0-pixels of each row. The closed mask is 0 on the 2-pixel frame border (no ROI
+// pixel lies there, and a 3x3 closing cannot reach it), so the flood-filled region is the
+// 4-connected component of 0-pixels that contains that border ring. Every row's first and last
+// run touch the ring and link straight to root 0; interior runs are united with the runs they
+// overlap in the row above. Holes are the 0-pixels whose run's root is not 0.
 // ------------------------------------------------------------------------------------------
 __device__ __forceinline__ int uf_find(int* L, int a, TickWork* w) {
     int n, it = 0;
@@ -809,67 +883,114 @@ __device__ void uf_union(int* L, int a, int b, TickWork* w) {
     atomicOr(&w->err, ERR_UF_LIMIT);
 }
 
-// P2a: tile-local union-find in shared memory, written as global labels (local roots)
-__device__ void phaseP2a_tile(const TickParams& P, const StreamDev& S, int lt, uint8_t* smem) {
-    const int tx = lt % S.tilesX, ty = lt / S.tilesX;
-    const int x0 = tx * kTileW, y0 = ty * kTileH;
-    volatile int* lab = (volatile int*)smem;
-    uint8_t* zero = smem + kThreads * 4;
-    const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
-    const int x = x0 + lx, y = y0 + ly;
-    const bool in = x < S.W && y < S.H;
-    const int q = y * S.W + x;
-    const bool z = in && __ldcg(&S.preflood[q]) == 0;
-    zero[threadIdx.x] = z;
-    lab[threadIdx.x] = z ? (int)threadIdx.x : -1;
-    __syncthreads();
-    for (int dir = 0; dir < 2; ++dir) {
-        const int nb = dir == 0 ? (lx + 1 < kTileW ? (int)threadIdx.x + 1 : -1) : (ly + 1 < kTileH ? (int)threadIdx.x + kTileW : -1);
-        if (z && nb >= 0 && zero[nb]) {
-            int a = threadIdx.x, b = nb;
-            for (int it = 0; it < 4096; ++it) {
-                while (lab[a] != a) a = lab[a];
-                while (lab[b] != b) b = lab[b];
-                if (a == b) break;
-                if (a < b) {
-                    const int old = atomicMin((int*)&lab[b], a);
-                    if (old == b) break;
-                    b = old;
-                } else {
-                    const int old = atomicMin((int*)&lab[a], b);
-                    if (old == a) break;
-                    a = old;
-                }
-            }
-        }
-        __syncthreads();
+// run start (x of the first pixel of the run of set bits) for each lane of a 32-pixel chunk
+struct RunTracker {
+    uint32_t carry;   // bit 31 of the previous chunk
+    int prevStart;    // start of the run that reached the end of the previous chunk
+    __device__ __forceinline__ void reset() {
+        carry = 0;
+        prevStart = -1;
     }
-    if (in) {
-        int label = -1;
-        if (z) {
-            int a = threadIdx.x;
-            while (lab[a] != a) a = lab[a];
-            label = (y0 + a / kTileW) * S.W + x0 + a % kTileW;
+    // returns the run start of this lane (undefined when its bit is 0) and advances
+    __device__ __forceinline__ int step(uint32_t ball, int x0, int lane) {
+        const uint32_t starts = ball & ~((ball << 1) | carry);
+        const uint32_t upto = starts & (0xffffffffu >> (31 - lane));
+        const int rs = upto ? x0 + 31 - __clz(upto) : prevStart;
+        const int rs31 = __shfl_sync(0xffffffffu, rs, 31);
+        if (ball >> 31) prevStart = rs31;
+        carry = ball >> 31;
+        return rs;
+    }
+};
+
+__device__ __forceinline__ int find_stream_by_row(const TickParams& P, int r) {
+    int lo = 0, hi = P.nStreams - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (P.streams[mid].rowBase <= r) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// runs pass: initializes the label of each run start (0 for runs touching the border ring)
+extern "C" __global__ void __launch_bounds__(256) lvbgs_k_runs(TickParams P) {
+    const int gr = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x & 31;
+    if (gr >= P.totalRows) return;
+    const StreamDev& S = P.streams[find_stream_by_row(P, gr)];
+    const int y = gr - S.rowBase, W = S.W, H = S.H;
+    const uint8_t* row = S.preflood + (size_t)y * W;
+    RunTracker rt;
+    rt.reset();
+    int last = -1;
+    bool ringOk = true;
+    for (int x0 = 0; x0 < W; x0 += 32) {
+        const int x = x0 + lane;
+        const bool z = x < W && __ldcg(&row[x]) == 0;
+        if (x < W && (x < 2 || x >= W - 2 || y < 2 || y >= H - 2) && !z) ringOk = false;
+        const uint32_t ball = __ballot_sync(0xffffffffu, z);
+        const uint32_t starts = ball & ~((ball << 1) | rt.carry);
+        const int rs = rt.step(ball, x0, lane);
+        if ((starts >> lane) & 1u) {
+            const int idx = y * W + x;
+            S.label[idx] = (x == 0 || y == 0 || y == H - 1) ? 0 : idx;
         }
-        __stcg(&S.label[q], label);
+        if (z) last = rs;
+    }
+    // the last run of the row reaches x = W-1, on the ring (held by the lane that read x = W-1)
+    const int lastRun = __shfl_sync(0xffffffffu, last, (W - 1) & 31);
+    if (lane == 0 && lastRun >= 0) S.label[y * W + lastRun] = 0;
+    if (__any_sync(0xffffffffu, !ringOk) && lane == 0) atomicOr(&P.work->err, ERR_RING);
+}
+
+// vertical pass: unites each run with the runs it overlaps in the row above
+extern "C" __global__ void __launch_bounds__(256) lvbgs_k_vunion(TickParams P) {
+    const int gr = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x & 31;
+    if (gr >= P.totalRows) return;
+    const StreamDev& S = P.streams[find_stream_by_row(P, gr)];
+    const int y = gr - S.rowBase, W = S.W;
+    if (y == 0) return;
+    const uint8_t* row = S.preflood + (size_t)y * W;
+    const uint8_t* up = row - W;
+    RunTracker rc, ru;
+    rc.reset();
+    ru.reset();
+    uint32_t ovCarry = 0;
+    for (int x0 = 0; x0 < W; x0 += 32) {
+        const int x = x0 + lane;
+        const bool zc = x < W && __ldcg(&row[x]) == 0;
+        const bool zu = x < W && __ldcg(&up[x]) == 0;
+        const uint32_t bc = __ballot_sync(0xffffffffu, zc), bu = __ballot_sync(0xffffffffu, zu);
+        const int rsc = rc.step(bc, x0, lane), rsu = ru.step(bu, x0, lane);
+        const uint32_t ov = bc & bu;
+        const uint32_t segStarts = ov & ~((ov << 1) | ovCarry);
+        ovCarry = ov >> 31;
+        if ((segStarts >> lane) & 1u) uf_union(S.label, y * W + rsc, (y - 1) * W + rsu, P.work);
     }
 }
 
-// P2b: unions across the right and bottom tile edges
-__device__ void phaseP2b_tile(const TickParams& P, const StreamDev& S, int lt) {
-    const int tx = lt % S.tilesX, ty = lt / S.tilesX;
-    const int x0 = tx * kTileW, y0 = ty * kTileH;
-    const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
-    const int x = x0 + lx, y = y0 + ly;
-    if (x >= S.W || y >= S.H) return;
-    const int q = y * S.W + x;
-    if (__ldcg(&S.preflood[q]) != 0) return;
-    if (lx == kTileW - 1 && x + 1 < S.W && __ldcg(&S.preflood[q + 1]) == 0) uf_union(S.label, q, q + 1, P.work);
-    if (ly == kTileH - 1 && y + 1 < S.H && __ldcg(&S.preflood[q + S.W]) == 0) uf_union(S.label, q, q + S.W, P.work);
+// holes pass: combined := 255 at the 0-pixels whose run is not connected to the ring, else 0
+extern "C" __global__ void __launch_bounds__(256) lvbgs_k_holes(TickParams P) {
+    const int gr = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x & 31;
+    if (gr >= P.totalRows) return;
+    const StreamDev& S = P.streams[find_stream_by_row(P, gr)];
+    const int y = gr - S.rowBase, W = S.W;
+    const uint8_t* row = S.preflood + (size_t)y * W;
+    RunTracker rt;
+    rt.reset();
+    for (int x0 = 0; x0 < W; x0 += 32) {
+        const int x = x0 + lane;
+        const bool z = x < W && __ldcg(&row[x]) == 0;
+        const uint32_t ball = __ballot_sync(0xffffffffu, z);
+        const int rs = rt.step(ball, x0, lane);
+        uint8_t hole = 0;
+        if (z) hole = uf_find(S.label, y * W + rs, P.work) != 0 ? 255 : 0;
+        if (x < W) S.combined[(size_t)y * W + x] = hole;
+    }
 }
 
-// P2c + P3: holes, 3-fold erosion of the closed mask, and mask |= holes | eroded (:541-546)
-__device__ void phaseP2c_tile(const TickParams& P, const StreamDev& S, int lt, uint8_t* smem) {
+// 3-fold erosion of the closed mask and mask |= holes | eroded (:544-546)
+__device__ void phaseP3_tile(const TickParams& P, const StreamDev& S, int lt, uint8_t* smem) {
     const int tx = lt % S.tilesX, ty = lt / S.tilesX;
     const int x0 = tx * kTileW, y0 = ty * kTileH;
     constexpr int HW = kTileW + 6, HH = kTileH + 6;
@@ -894,14 +1015,9 @@ __device__ void phaseP2c_tile(const TickParams& P, const StreamDev& S, int lt, u
     const int q = y * W + x;
     uint8_t er = 255;
     for (int d = 0; d < 7; ++d) er = min(er, rowmin[(ly + d) * kTileW + lx]);
-    uint8_t hole = 0;
-    if (pf[(ly + 3) * HW + lx + 3] == 0) {
-        const int root = uf_find(S.label, __ldcg(&S.label[q]), P.work);
-        hole = root != 0 ? 255 : 0;
-    }
+    const uint8_t hole = __ldcg(&S.combined[q]);
     const uint8_t raw = (__ldcg(&S.intent[q]) & kInFG) ? 255 : 0;
     __stcg(&S.combined[q], (uint8_t)(raw | hole | er));
-    if (q == 0 && pf[3 * HW + 3] != 0) atomicOr(&P.work->err, ERR_RING);
 }
 
 // P4: median blur (binary majority, replicate border) -> final mask; final-segmentation EMAs
@@ -914,6 +1030,12 @@ __device__ void phaseP4_tile(const TickParams& P, const StreamDev& S, int lt, ui
     uint8_t* cm = smem;
     uint8_t* colcnt = smem + HW * HH;
     const int W = S.W, H = S.H, npx = S.npx;
+    const FrameK F = frame_consts(S);
+    const int qx = x0 + (int)threadIdx.x % kTileW, qy = y0 + (int)threadIdx.x / kTileW;
+    const bool qin = qx < W && qy < H;
+    const int qq = qy * W + qx;
+    const float* fcur = S.fm + (size_t)F.cur * kNumFloatMaps * npx;
+    const float finLT = qin ? fcur[FM_FIN_LT * npx + qq] : 0.0f, finST = qin ? fcur[FM_FIN_ST * npx + qq] : 0.0f;
     for (int i = threadIdx.x; i < HW * HH; i += blockDim.x) {
         int gy = y0 - r + i / HW, gx = x0 - r + i % HW;
         gy = gy < 0 ? 0 : gy >= H ? H - 1 : gy;
@@ -937,14 +1059,12 @@ __device__ void phaseP4_tile(const TickParams& P, const StreamDev& S, int lt, ui
     const uint8_t fgv = (2 * cnt > k * k) ? 255 : 0;
     __stcg(&S.lastFG[q], fgv);
     if (S.maskOut) S.maskOut[q] = fgv;
-    const FrameK F = frame_consts(S);
-    const float* fc = S.fm + (size_t)F.cur * kNumFloatMaps * npx;
     float* fn = S.fm + (size_t)F.nxt * kNumFloatMaps * npx;
-    const float aL = 1.0f - F.fLT, bL = (float)((1.0 / 255) * (double)F.fLT);
-    const float aS = 1.0f - F.fST, bS = (float)((1.0 / 255) * (double)F.fST);
+    const float aL = 1.0f - F.fLT, bL = S.ctl->bLT;
+    const float aS = 1.0f - F.fST, bS = S.ctl->bST;
     const float m = (float)fgv;
-    fn[FM_FIN_LT * npx + q] = (fc[FM_FIN_LT * npx + q] * aL + m * bL) + 0.0f;
-    fn[FM_FIN_ST * npx + q] = (fc[FM_FIN_ST * npx + q] * aS + m * bS) + 0.0f;
+    fn[FM_FIN_LT * npx + q] = (finLT * aL + m * bL) + 0.0f;
+    fn[FM_FIN_ST * npx + q] = (finST * aS + m * bS) + 0.0f;
 }
 
 // P5: 3-fold dilation of the final mask and blink masking with the previous and the new inverted
@@ -956,6 +1076,9 @@ __device__ void phaseP5_tile(const TickParams& P, const StreamDev& S, int lt, ui
     uint8_t* fgm = smem;
     uint8_t* rowmax = smem + HW * HH;
     const int W = S.W, H = S.H;
+    const int qx = x0 + (int)threadIdx.x % kTileW, qy = y0 + (int)threadIdx.x / kTileW;
+    const bool qin = qx < W && qy < H;
+    const uint8_t bl0 = qin ? S.blinks[qy * W + qx] : 0, di0 = qin ? S.dilInv[qy * W + qx] : 0;
     for (int i = threadIdx.x; i < HW * HH; i += blockDim.x) {
         const int gy = y0 - 3 + i / HW, gx = x0 - 3 + i % HW;
         fgm[i] = (gy >= 0 && gy < H && gx >= 0 && gx < W) ? __ldcg(&S.lastFG[gy * W + gx]) : 0;  // never wins
@@ -975,7 +1098,7 @@ __device__ void phaseP5_tile(const TickParams& P, const StreamDev& S, int lt, ui
     uint8_t dv = 0;
     for (int d = 0; d < 7; ++d) dv = max(dv, rowmax[(ly + d) * kTileW + lx]);
     const uint8_t inv = (uint8_t)~dv;
-    S.blinks[q] = (uint8_t)(S.blinks[q] & S.dilInv[q] & inv);
+    S.blinks[q] = (uint8_t)(bl0 & di0 & inv);
     S.dilInv[q] = inv;
 }
 
@@ -1083,39 +1206,45 @@ __device__ void refresh_pixel(const StreamDev& S, int p, uint32_t frame, int sta
 }
 
 // ------------------------------------------------------------------------------------------
-// the tick kernel
+// the frame step: one kernel per phase, launched back to back (and captured in a CUDA graph) over
+// all streams of the batch; the repair loop is a cooperative kernel with grid barriers
 // ------------------------------------------------------------------------------------------
-extern "C" __global__ void __launch_bounds__(kThreads, 2)
-    lvbgs_subsense_tick(TickParams P, unsigned long long dsTotal, const unsigned long long* dsBase) {
-    __shared__ __align__(16) uint8_t smem[8192];
-    TickWork* w = P.work;
-    // ---- A: evaluate all pixels ----
-    for (int t = next_tile(P, 0); t < P.totalTiles; t = next_tile(P, 0)) {
-        const int si = find_stream_by_tile(P, t);
-        const StreamDev& S = P.streams[si];
-        if (S.C == 3) phaseA_tile<3>(P, S, t - S.tileBase, smem);
-        else phaseA_tile<1>(P, S, t - S.tileBase, smem);
-    }
-    if (!grid_sync(w)) return;
-    // ---- B: resolve ghost tests, initial repair frontier; frame down-sampling ----
-    for (int t = next_tile(P, 1); t < P.totalTiles; t = next_tile(P, 1)) {
+#define LV_TILE_KERNEL_PROLOGUE                                              \
+    const int t = blockIdx.x;                                               \
+    if (t >= P.totalTiles) return;                                          \
+    const int si = find_stream_by_tile(P, t);                               \
+    const StreamDev& S = P.streams[si];                                     \
+    const int lt = t - S.tileBase;
+
+extern "C" __global__ void __launch_bounds__(kThreads, 3) lvbgs_k_eval(TickParams P) {
+    __shared__ __align__(16) uint8_t smem[((((kTileW + 4) * 3 + 2 + 3) / 4) * 4) * (kTileH + 4) + 256];
+    LV_TILE_KERNEL_PROLOGUE
+    if (S.C == 3) phaseA_tile<3>(P, S, lt, smem);
+    else phaseA_tile<1>(P, S, lt, smem);
+}
+
+extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_resolve(TickParams P, unsigned long long dsTotal,
+                                                                       const unsigned long long* dsBase) {
+    if ((int)blockIdx.x < P.totalTiles) {
+        const int t = blockIdx.x;
         const int si = find_stream_by_tile(P, t);
         phaseB_tile(P, si, P.streams[si], t - P.streams[si].tileBase);
+        return;
     }
-    {
-        const unsigned long long nth = (unsigned long long)gridDim.x * blockDim.x;
-        for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < dsTotal; i += nth) {
-            int lo = 0, hi = P.nStreams - 1;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (dsBase[mid] <= i) lo = mid;
-                else hi = mid - 1;
-            }
-            ds_item(P.streams[lo], (int)(i - dsBase[lo]));
-        }
+    const unsigned long long i = (unsigned long long)(blockIdx.x - P.totalTiles) * blockDim.x + threadIdx.x;
+    if (i >= dsTotal) return;
+    int lo = 0, hi = P.nStreams - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (dsBase[mid] <= i) lo = mid;
+        else hi = mid - 1;
     }
-    if (!grid_sync(w)) return;
-    // ---- M/R: repair to the raster-order fixed point ----
+    ds_item(P.streams[lo], (int)(i - dsBase[lo]));
+}
+
+// repair to the raster-order fixed point (cooperative launch: all CTAs resident)
+extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_repair(TickParams P) {
+    TickWork* w = P.work;
     int iter = 0;
     for (;;) {
         const int par = iter & 1;
@@ -1153,55 +1282,55 @@ extern "C" __global__ void __launch_bounds__(kThreads, 2)
         ++iter;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) w->iters = (unsigned)iter;
-    // ---- F: commit sample writes, blinks, closing ----
-    for (int t = next_tile(P, 2); t < P.totalTiles; t = next_tile(P, 2)) {
-        const int si = find_stream_by_tile(P, t);
+}
+
+extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_commit(TickParams P) {
+    __shared__ __align__(16) uint8_t smem[(kTileW + 4) * (kTileH + 4) * 4 + (kTileW + 2) * (kTileH + 2)];
+    LV_TILE_KERNEL_PROLOGUE
+    if (S.C == 3) phaseF_tile<3>(P, S, lt, smem);
+    else phaseF_tile<1>(P, S, lt, smem);
+}
+
+extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_combine(TickParams P) {
+    __shared__ __align__(16) uint8_t smem[(kTileW + 6) * (kTileH + 6) + kTileW * (kTileH + 6)];
+    LV_TILE_KERNEL_PROLOGUE
+    phaseP3_tile(P, S, lt, smem);
+}
+
+extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_median(TickParams P) {
+    __shared__ __align__(16) uint8_t smem[(kTileW + 30) * (kTileH + 30) + kTileH * (kTileW + 30)];
+    LV_TILE_KERNEL_PROLOGUE
+    phaseP4_tile(P, S, lt, smem);
+}
+
+// frame-level epilogue of every stream (one thread per stream)
+extern "C" __global__ void lvbgs_k_epilogue(TickParams P) {
+    for (int si = blockIdx.x * blockDim.x + threadIdx.x; si < P.nStreams; si += gridDim.x * blockDim.x) {
         const StreamDev& S = P.streams[si];
-        if (S.C == 3) phaseF_tile<3>(P, S, t - S.tileBase, smem);
-        else phaseF_tile<1>(P, S, t - S.tileBase, smem);
-    }
-    if (!grid_sync(w)) return;
-    for (int t = next_tile(P, 3); t < P.totalTiles; t = next_tile(P, 3)) {
-        const int si = find_stream_by_tile(P, t);
-        phaseP2a_tile(P, P.streams[si], t - P.streams[si].tileBase, smem);
-    }
-    if (!grid_sync(w)) return;
-    for (int t = next_tile(P, 4); t < P.totalTiles; t = next_tile(P, 4)) {
-        const int si = find_stream_by_tile(P, t);
-        phaseP2b_tile(P, P.streams[si], t - P.streams[si].tileBase);
-    }
-    if (!grid_sync(w)) return;
-    for (int t = next_tile(P, 5); t < P.totalTiles; t = next_tile(P, 5)) {
-        const int si = find_stream_by_tile(P, t);
-        phaseP2c_tile(P, P.streams[si], t - P.streams[si].tileBase, smem);
-    }
-    if (!grid_sync(w)) return;
-    for (int t = next_tile(P, 6); t < P.totalTiles; t = next_tile(P, 6)) {
-        const int si = find_stream_by_tile(P, t);
-        phaseP4_tile(P, P.streams[si], t - P.streams[si].tileBase, smem);
-    }
-    if (!grid_sync(w)) return;
-    // epilogue of each stream runs beside P5 (it reads nothing P5 writes)
-    if (blockIdx.x == gridDim.x - 1)
-        for (int si = threadIdx.x; si < P.nStreams; si += blockDim.x) {
-            const StreamDev& S = P.streams[si];
-            stream_epilogue(P, S);
-            if (S.ctl->refresh_pending) {
-                // nRefreshSampleStartPos = rand() % N with the frame-level (sentinel) counter
-                DrawState ds;
-                ds.blk = 0xffffffffu;
-                const uint32_t f = (uint32_t)(S.ctl->frame_idx + 1ull);
-                S.ctl->refresh_start = draw_k(S.seed, f, kSentinelPx, 0u, ds) % (uint32_t)S.N;
-                S.ctl->ksent = 1;
-            }
+        stream_epilogue(P, S);
+        if (S.ctl->refresh_pending) {
+            // nRefreshSampleStartPos = rand() % N, drawn with the frame-level (sentinel) counter (:86)
+            DrawState ds;
+            ds.blk = 0xffffffffu;
+            const uint32_t f = (uint32_t)(S.ctl->frame_idx + 1ull);
+            S.ctl->refresh_start = draw_k(S.seed, f, kSentinelPx, 0u, ds) % (uint32_t)S.N;
+            S.ctl->ksent = 1;
+            atomicExch(&P.work->anyReset, 1u);
         }
-    for (int t = next_tile(P, 7); t < P.totalTiles; t = next_tile(P, 7)) {
-        const int si = find_stream_by_tile(P, t);
-        phaseP5_tile(P, P.streams[si], t - P.streams[si].tileBase, smem);
     }
-    if (!grid_sync(w)) return;
-    // ---- automatic model reset: refreshModel(0.1) and T(x) := 1 (:588-593) ----
-    for (int t = next_tile(P, 8); t < P.totalTiles; t = next_tile(P, 8)) {
+}
+
+extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_dilate(TickParams P) {
+    __shared__ __align__(16) uint8_t smem[(kTileW + 6) * (kTileH + 6) + kTileW * (kTileH + 6)];
+    LV_TILE_KERNEL_PROLOGUE
+    phaseP5_tile(P, S, lt, smem);
+}
+
+// automatic model reset: refreshModel(0.1) and T(x) := 1 everywhere (:588-593); a small grid
+// strides over the tiles of the streams that reset this frame
+extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_reset(TickParams P) {
+    if (ld_volatile(&P.work->anyReset) == 0u) return;
+    for (int t = blockIdx.x; t < P.totalTiles; t += gridDim.x) {
         const int si = find_stream_by_tile(P, t);
         const StreamDev& S = P.streams[si];
         if (!S.ctl->refresh_pending) continue;
@@ -1218,21 +1347,17 @@ extern "C" __global__ void __launch_bounds__(kThreads, 2)
         S.fm[(size_t)0 * kNumFloatMaps * S.npx + FM_T * S.npx + p] = 1.0f;
         S.fm[(size_t)1 * kNumFloatMaps * S.npx + FM_T * S.npx + p] = 1.0f;
     }
-    // ---- the last CTA to finish closes the frame: frame index (parity) and repair stamps ----
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const unsigned int done = atomicAdd(&w->done_ctas, 1u) + 1u;
-        if (done == gridDim.x) {
-            __threadfence();
-            const unsigned int its = ld_volatile(&w->iters);
-            for (int si = 0; si < P.nStreams; ++si) {
-                StreamCtl* ctl = P.streams[si].ctl;
-                ctl->frame_idx += 1ull;
-                ctl->st_rounds += its;
-                ctl->stamp_base += (uint32_t)its + 4u;
-            }
-        }
+}
+
+// closes the frame of every stream: frame index (and so the buffer parity), repair statistics
+extern "C" __global__ void lvbgs_k_close(TickParams P) {
+    const unsigned int its = P.work->iters;
+    for (int si = blockIdx.x * blockDim.x + threadIdx.x; si < P.nStreams; si += gridDim.x * blockDim.x) {
+        StreamCtl* ctl = P.streams[si].ctl;
+        ctl->frame_idx += 1ull;
+        ctl->st_rounds += its;
+        ctl->stamp_base += its + 4u;
+        frame_factors(ctl->frame_idx + 1ull, P.streams[si].nmv, &ctl->fLT, &ctl->fST, &ctl->bLT, &ctl->bST);
     }
 }
 
