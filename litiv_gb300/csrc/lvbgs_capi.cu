@@ -235,6 +235,7 @@ void fill_geometry(lvbgs_ctx* h) {
     S.relThr = h->prm.rel_lbsp_threshold;
     S.lbspOff = (unsigned)h->prm.lbsp_threshold_offset;
     S.seed = h->prm.seed;
+    S.nMagic = ((1ull << 40) + S.N - 1) / (unsigned long long)S.N;
 }
 
 int g_coop_blocks_per_sm = -1, g_sm_count = 0;

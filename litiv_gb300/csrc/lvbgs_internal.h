@@ -130,6 +130,7 @@ struct StreamDev {
     float relThr;
     unsigned int lbspOff;
     unsigned long long seed;
+    unsigned long long nMagic;  // ceil(2^40 / N): fast exact draw % N
     // per-launch inputs
     const uint8_t* frame;  // dense device frame
     uint8_t* maskOut;      // device output mask (may be null)

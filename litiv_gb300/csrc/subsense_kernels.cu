@@ -116,7 +116,16 @@ __device__ __forceinline__ uint32_t draw_k(unsigned long long seed, uint32_t fra
 }
 // a % m for a 31-bit draw and a size_t modulus (m >= 2^32 leaves a unchanged)
 __device__ __forceinline__ unsigned long long mod_draw(uint32_t a, unsigned long long m) {
-    return m > 0xffffffffull ? (unsigned long long)a : (unsigned long long)(a % (uint32_t)m);
+    if (m > 0xffffffffull) return (unsigned long long)a;
+    const uint32_t m32 = (uint32_t)m;
+    if ((m32 & (m32 - 1u)) == 0u) return (unsigned long long)(a & (m32 - 1u));  // powers of two (T = 2, 4, ...)
+    return (unsigned long long)(a % m32);
+}
+// a % N for a 31-bit draw with the stream's multiplier M = ceil(2^40 / N): for N <= 64 the
+// quotient error a*(M - 2^40/N)/2^40 < 2^-9 < 1/N, so floor(a*M / 2^40) is the exact quotient
+__device__ __forceinline__ uint32_t mod_n(uint32_t a, const StreamDev& S) {
+    const uint32_t q = (uint32_t)(((unsigned long long)a * S.nMagic) >> 40);
+    return a - q * (uint32_t)S.N;
 }
 
 // LBSP::computeDescriptor_threshold (LBSP.hpp:193-202) on 16 packed taps: bit n = |tap_n - ref| > thr
@@ -373,7 +382,7 @@ __device__ uint32_t eval_pixel(const StreamDev& S, const FrameK& F, const uint8_
         RwST = RwST * (1.0f - F.fST) + F.fST;
         intent |= kInFG;
         if (F.cooldown && (draw_k(S.seed, seedFrame, (uint32_t)p, 0u, ds) % 2u) == 0u) {
-            const uint32_t so = draw_k(S.seed, seedFrame, (uint32_t)p, 1u, ds) % (uint32_t)N;
+            const uint32_t so = mod_n(draw_k(S.seed, seedFrame, (uint32_t)p, 1u, ds), S);
             intent |= kInOwn | (so << kInSOwnShift);
         }
     } else {
@@ -385,7 +394,7 @@ __device__ uint32_t eval_pixel(const StreamDev& S, const FrameK& F, const uint8_
         const unsigned long long nLR = S.lrMode ? S.lrFixed : (unsigned long long)__float2ull_rz(ceilf(T));
         uint32_t k = 0;
         if (mod_draw(draw_k(S.seed, seedFrame, (uint32_t)p, k++, ds), nLR) == 0ull) {
-            const uint32_t so = draw_k(S.seed, seedFrame, (uint32_t)p, k++, ds) % (uint32_t)N;
+            const uint32_t so = mod_n(draw_k(S.seed, seedFrame, (uint32_t)p, k++, ds), S);
             intent |= kInOwn | (so << kInSOwnShift);
         }
         const bool use3 = F.use3x3 && !uNew;
@@ -408,7 +417,7 @@ __device__ uint32_t eval_pixel(const StreamDev& S, const FrameK& F, const uint8_
         if (mod_draw(nrand, X) == 0ull) st = NB_WRITE;
         else if (mod_draw(nrand, (unsigned long long)__float2ull_rz(F.t_lo)) == 0ull) st = NB_PENDING;
         else st = NB_NO;
-        const uint32_t snb = draw_k(S.seed, seedFrame, (uint32_t)p, k, ds) % (uint32_t)N;
+        const uint32_t snb = mod_n(draw_k(S.seed, seedFrame, (uint32_t)p, k, ds), S);
         intent |= (code << kInCodeShift) | (st << kInNStShift) | (snb << kInSNbShift);
     }
 
@@ -551,6 +560,25 @@ __device__ void phaseA_tile(const TickParams& P, const StreamDev& S, int lt, uin
 // ------------------------------------------------------------------------------------------
 // list helpers for the repair loop
 // ------------------------------------------------------------------------------------------
+// warp-aggregated push: every lane of the warp calls it (want = whether this lane pushes); one
+// counter atomic per warp instead of one per item
+__device__ __forceinline__ void push_item_warp(bool want, unsigned long long* list, unsigned int* count,
+                                               unsigned int cap, uint32_t* stamps, uint32_t stamp, int si, int p,
+                                               TickWork* w) {
+    const bool ok = want && atomicExch(&stamps[p], stamp) != stamp;
+    const unsigned int m = __ballot_sync(0xffffffffu, ok);
+    if (!m) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    unsigned int base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned int)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (ok) {
+        const unsigned int i = base + (unsigned int)__popc(m & ((1u << lane) - 1u));
+        if (i < cap) list[i] = ((unsigned long long)si << 40) | (unsigned long long)(unsigned)p;
+        else atomicOr(&w->err, ERR_REPAIR_LIMIT);
+    }
+}
+
 __device__ __forceinline__ void push_item(unsigned long long* list, unsigned int* count, unsigned int cap,
                                           uint32_t* stamps, uint32_t stamp, int si, int p, TickWork* w) {
     if (atomicExch(&stamps[p], stamp) == stamp) return;
@@ -586,24 +614,27 @@ __device__ __forceinline__ uint32_t set_nst(uint32_t w, uint32_t st) {
 __device__ void phaseB_tile(const TickParams& P, int si, const StreamDev& S, int lt) {
     const int tx = lt % S.tilesX, ty = lt / S.tilesX;
     const int x = tx * kTileW + threadIdx.x % kTileW, y = ty * kTileH + threadIdx.x / kTileW;
-    if (x >= S.W || y >= S.H) return;
+    const bool in = x < S.W && y < S.H;
     const int p = y * S.W + x;
-    uint32_t w = __ldcg(&S.intent[p]);
-    if (!(w & kInValid)) return;
-    const FrameK F = frame_consts(S);
-    if (in_nst(w) == NB_PENDING) {
-        const int q = code_target((int)in_code(w), x, y, S.W);
-        w = set_nst(w, resolve_ghost(S, F, p, q));
-        __stcg(&S.intent[p], w);
-    }
-    if (in_nb_writes(w)) {
-        const int q = code_target((int)in_code(w), x, y, S.W);
-        if (q > p) {
-            const uint32_t wq = __ldcg(&S.intent[q]);
-            if ((wq & kInValid) && in_snb(w) < in_e(wq))
-                push_item(P.dlist[0], &P.work->dcount[0], P.listCap, S.stampD, S.ctl->stamp_base + 1u, si, q, P.work);
+    uint32_t w = in ? __ldcg(&S.intent[p]) : 0u;
+    bool want = false;
+    int q = 0;
+    if (w & kInValid) {
+        if (in_nst(w) == NB_PENDING) {
+            const FrameK F = frame_consts(S);
+            w = set_nst(w, resolve_ghost(S, F, p, code_target((int)in_code(w), x, y, S.W)));
+            __stcg(&S.intent[p], w);
+        }
+        if (in_nb_writes(w)) {
+            q = code_target((int)in_code(w), x, y, S.W);
+            if (q > p) {
+                const uint32_t wq = __ldcg(&S.intent[q]);
+                want = (wq & kInValid) && in_snb(w) < in_e(wq);
+            }
         }
     }
+    // all lanes of the warp reach the aggregated push
+    push_item_warp(want, P.dlist[0], &P.work->dcount[0], P.listCap, S.stampD, S.ctl->stamp_base + 1u, si, q, P.work);
 }
 
 // frame down-sampling for the frame-level analysis (:568-584): one output pixel per thread
