@@ -1,8 +1,8 @@
 """Benchmark: SuBSENSE Mpix/s on the 64-stream mixed-resolution workload, batched vs plain.
 
 A step is one frame tick of all 64 streams (16x320x240, 24x640x480, 16x1280x720, 8x1920x1080;
-48 BGR + 16 grayscale; 39,936,000 pixels) processed by one persistent launch of the SuBSENSE tick
-kernel. ``value`` is measured with the frames already resident in HBM; ``e2e`` goes through the
+48 BGR + 16 grayscale; 39,936,000 pixels) processed by one batched frame step (13 kernel launches,
+each over all streams). ``value`` is measured with the frames already resident in HBM; ``e2e`` goes through the
 C-ABI (lvbgs_batch_apply) with pinned host frames and host masks, so the host->device frame copies
 and device->host mask copies are inside the timed region. The plain form (one stream per launch,
 64 launches per tick) is measured on the same frames. Inputs and model state (~24 GB) are far
@@ -90,13 +90,26 @@ class ClockSampler:
         return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def algorithmic_bytes(px_by_c, samples, writes):
-    """Algorithmic HBM bytes of one tick (per ROI pixel: frame c + mask 1 + 10 FP32 maps r+w 80 +
-    last colour/descriptor r+w 6c + u8 maps r+w 12, plus 3c bytes per evaluated sample and per
-    sample write)."""
+KERNELS = ["eval", "resolve", "repair", "commit", "runs", "vunion", "holes", "combine", "median", "epilogue",
+           "dilate", "reset", "close"]
+
+
+def algorithmic_bytes(px_by_c):
+    """Algorithmic HBM bytes of the whole path (per ROI pixel: frame c + mask 1 + 10 FP32 maps r+w 80 +
+    last colour/descriptor r+w 6c + u8 maps r+w 12, plus 3c bytes per evaluated sample and per sample
+    write)."""
     total = 0
     for c, (npx, s, w) in px_by_c.items():
         total += npx * (c + 1 + 80 + 6 * c + 12) + 3 * c * (s + w)
+    return total
+
+
+def eval_algorithmic_bytes(px_by_c):
+    """Algorithmic bytes of the evaluation kernel alone (per ROI pixel: frame c + 8 FP32 maps r+w 64 +
+    2 FP32 maps read 8 + last colour/descriptor r+w 6c + u8 maps 5, plus 3c bytes per evaluated sample)."""
+    total = 0
+    for c, (npx, s, w) in px_by_c.items():
+        total += npx * (c + 64 + 8 + 6 * c + 5) + 3 * c * s
     return total
 
 
@@ -218,6 +231,7 @@ def main():
         check(lib.lvbgs_batch_apply(hs, frs[t], n, sptr), hs[0])
     check(lib.lvbgs_batch_wait(hs, n, sptr), hs[0])
     sc0 = [b.scalars() for b in subs]
+    check(lib.lvbgs_debug_set_timing(hs[0], 1, args.steps), hs[0])
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -245,7 +259,8 @@ def main():
         e[0] += (b["frame_idx"] - a["frame_idx"]) * b["n_relevant_px"]
         e[1] += b["stat_samples_evaluated"] - a["stat_samples_evaluated"]
         e[2] += b["stat_sample_writes"] - a["stat_sample_writes"]
-    alg_bytes_step = algorithmic_bytes({c: tuple(v) for c, v in px_by_c.items()}, 0, 0) / args.steps
+    alg_bytes_step = algorithmic_bytes({c: tuple(v) for c, v in px_by_c.items()}) / args.steps
+    eval_bytes_step = eval_algorithmic_bytes({c: tuple(v) for c, v in px_by_c.items()}) / args.steps
     ms_step = total_ms / args.steps
     peaks = {}
     try:
@@ -257,9 +272,12 @@ def main():
     tick_sorted = sorted(tick_ms)
     p50 = tick_sorted[len(tick_sorted) // 2]
     p99 = tick_sorted[min(len(tick_sorted) - 1, int(round(0.99 * (len(tick_sorted) - 1))))]
-    prof = (C.c_double * 40)()
-    nprof = lib.lvbgs_debug_tick_profile(hs[0], 1, prof, 40)
-    phase_ms = [round(prof[i], 4) for i in range(nprof)]
+    prof = (C.c_double * 16)()
+    nprof = lib.lvbgs_debug_tick_profile(hs[0], 1, prof, 16)
+    kernel_ms = {KERNELS[i]: round(prof[i], 4) for i in range(nprof)}
+    lib.lvbgs_debug_set_timing(hs[0], 1, 0)
+    eval_ms = kernel_ms.get("eval") or float("nan")
+    eval_achieved = eval_bytes_step / (eval_ms / 1e3) / 1e9
     rounds = sum(b["stat_repair_rounds"] - a["stat_repair_rounds"] for a, b in zip(sc0[:1], sc1[:1])) / args.steps
     remat = sum(b["stat_repair_rematched"] - a["stat_repair_rematched"] for a, b in zip(sc0, sc1)) / args.steps
 
@@ -332,17 +350,20 @@ def main():
             "vs_baseline": None, "dtype": "u8/f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "streams": n, "px_per_step": px_step,
                        "l2": "inputs and model state (GBs) exceed L2; no flush",
-                       "parallelism": "one persistent cooperative launch per tick over all streams"},
+                       "parallelism": "one batched frame step per tick: 13 kernel launches, each over all 64 streams"},
             "frames_per_s": n * args.steps * world / (total_ms / 1e3),
             "p50_frame_ms": p50, "p99_frame_ms": p99,
             "plain": plain,
             "batched_vs_plain": (value / world / plain["value"]) if plain else None,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "note": "algorithmic bytes per tick / tick time; peak = measured copy bandwidth"},
+            "roofline": {"bound": "hbm", "kernel": "lvbgs_k_eval", "achieved": eval_achieved, "peak": peak,
+                         "unit": "GB/s", "frac": eval_achieved / peak, "traffic": None,
+                         "note": "algorithmic bytes of the evaluation kernel per launch / its average CUDA-event "
+                                 "duration in the timed region; peak = measured copy bandwidth (of measured)"},
+            "path_roofline": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                              "note": "algorithmic bytes of the whole frame step / tick time"},
             "repair": {"rounds_per_tick": rounds, "rematched_px_per_tick": remat},
-            "phase_ms_last_tick": phase_ms,
-            "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": args.steps,
+            "kernel_ms": kernel_ms,
+            "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": 13 * args.steps,
             "clocks": clk.summary(),
         }
         print(json.dumps(out))

@@ -158,9 +158,13 @@ typedef struct {
 } lvbgs_scalars;
 lvbgs_status lvbgs_get_scalars(lvbgs_handle h, lvbgs_scalars* out);
 
-/* durations (ms) of the phases of the last frame step launched by h (batched != 0: the last batched
- * step it led), in order: evaluation, ghost resolution, 2 per repair round, commit/closing,
- * 3 hole-filling passes, median, dilation/blinks, model reset. Returns the number written. */
+/* Per-kernel timing of frame steps (inspection): lvbgs_debug_set_timing(h, batched, n) records CUDA
+ * events around each kernel of the next n steps launched by h (batched != 0: the batched steps it
+ * leads; 0 disables); lvbgs_debug_tick_profile() waits for them and returns the average duration in
+ * ms of each kernel, in launch order: evaluation, ghost resolution, repair, commit/closing, row runs,
+ * vertical unions, holes, erosion/combination, median, frame-level epilogue, dilation/blinks,
+ * automatic model reset, frame close. Returns the number of values written. */
+lvbgs_status lvbgs_debug_set_timing(lvbgs_handle h, int batched, int n_ticks);
 int lvbgs_debug_tick_profile(lvbgs_handle h, int batched, double* out_ms, int max_n);
 
 #ifdef __cplusplus

@@ -57,7 +57,16 @@ struct Workspace {
     int nStreamsCap = 0;
     std::vector<StreamDev> h_streams;
     std::vector<unsigned long long> h_dsBase;
+    // optional per-kernel timing: a ring of kTimedKernels+1 events per tick
+    std::vector<cudaEvent_t> tev;
+    int tevTicks = 0, tevNext = 0, tevRecorded = 0;
+    void free_events() {
+        for (cudaEvent_t e : tev) cudaEventDestroy(e);
+        tev.clear();
+        tevTicks = tevNext = tevRecorded = 0;
+    }
     void release() {
+        free_events();
         cudaFree(work);
         cudaFree(d_streams);
         cudaFree(d_dsBase);
@@ -238,6 +247,7 @@ void fill_geometry(lvbgs_ctx* h) {
     S.nMagic = ((1ull << 40) + S.N - 1) / (unsigned long long)S.N;
 }
 
+constexpr int kTimedKernels = 13;  // kernels of one frame step, in launch order
 int g_coop_blocks_per_sm = -1, g_sm_count = 0;
 std::mutex g_occ_mu;
 cudaError_t coop_grid(int* maxBlocks) {
@@ -298,24 +308,47 @@ lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t s
     const dim3 blk(kThreads);
     const int rowBlocks = (totalRows + 7) / 8;
     const int dsBlocks = (int)((ds + kThreads - 1) / kThreads);
+    cudaEvent_t* tev = nullptr;
+    if (ws.tevTicks > 0) {
+        tev = &ws.tev[(size_t)ws.tevNext * (kTimedKernels + 1)];
+        ws.tevNext = (ws.tevNext + 1) % ws.tevTicks;
+        ws.tevRecorded = std::min(ws.tevRecorded + 1, ws.tevTicks);
+    }
+#define LV_TMARK(i) \
+    if (tev) cudaEventRecord(tev[i], st)
+    LV_TMARK(0);
     lvbgs_k_eval<<<totalTiles, blk, 0, st>>>(P);
+    LV_TMARK(1);
     lvbgs_k_resolve<<<totalTiles + dsBlocks, blk, 0, st>>>(P, ds, dsb);
+    LV_TMARK(2);
     {
         const int grid = std::max(1, std::min(maxBlocks, std::max(1, totalTiles)));
         void* args[] = {&P};
         LV_CUDA(errh, cudaLaunchCooperativeKernel((const void*)lvbgs_k_repair, dim3(grid), blk, args, 0, st),
                 "repair kernel launch");
     }
+    LV_TMARK(3);
     lvbgs_k_commit<<<totalTiles, blk, 0, st>>>(P);
+    LV_TMARK(4);
     lvbgs_k_runs<<<rowBlocks, blk, 0, st>>>(P);
+    LV_TMARK(5);
     lvbgs_k_vunion<<<rowBlocks, blk, 0, st>>>(P);
+    LV_TMARK(6);
     lvbgs_k_holes<<<rowBlocks, blk, 0, st>>>(P);
+    LV_TMARK(7);
     lvbgs_k_combine<<<totalTiles, blk, 0, st>>>(P);
+    LV_TMARK(8);
     lvbgs_k_median<<<totalTiles, blk, 0, st>>>(P);
+    LV_TMARK(9);
     lvbgs_k_epilogue<<<1, 128, 0, st>>>(P);
+    LV_TMARK(10);
     lvbgs_k_dilate<<<totalTiles, blk, 0, st>>>(P);
+    LV_TMARK(11);
     lvbgs_k_reset<<<std::max(1, std::min(totalTiles, g_sm_count * 8)), blk, 0, st>>>(P);
+    LV_TMARK(12);
     lvbgs_k_close<<<1, 128, 0, st>>>(P);
+    LV_TMARK(13);
+#undef LV_TMARK
     LV_CUDA(errh, cudaGetLastError(), "frame step launch");
     return LVBGS_OK;
 }
@@ -874,16 +907,38 @@ lvbgs_status lvbgs_debug_get_map(lvbgs_handle h, int which, void* out, size_t by
     return LVBGS_OK;
 }
 
+lvbgs_status lvbgs_debug_set_timing(lvbgs_handle h, int batched, int n_ticks) {
+    if (!h || n_ticks < 0) return fail(h, LVBGS_BAD_ARG, "bad argument");
+    cudaSetDevice(h->device);
+    Workspace& ws = batched ? h->batchWs : h->ws;
+    ws.free_events();
+    if (n_ticks == 0) return LVBGS_OK;
+    ws.tev.resize((size_t)n_ticks * (kTimedKernels + 1));
+    for (cudaEvent_t& e : ws.tev) LV_CUDA(h, cudaEventCreate(&e), "event creation");
+    ws.tevTicks = n_ticks;
+    return LVBGS_OK;
+}
+
 int lvbgs_debug_tick_profile(lvbgs_handle h, int batched, double* out_ms, int max_n) {
     if (!h || !out_ms || max_n <= 0) return 0;
+    cudaSetDevice(h->device);
     Workspace& ws = batched ? h->batchWs : h->ws;
-    if (!ws.work) return 0;
-    TickWork w;
-    if (cudaMemcpy(&w, ws.work, sizeof(TickWork), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
-    const int n = (int)std::min<unsigned>(w.nts, 40u);
-    int k = 0;
-    for (int i = 1; i < n && k < max_n; ++i) out_ms[k++] = (double)(w.ts[i] - w.ts[i - 1]) * 1e-6;
-    return k;
+    if (ws.tevRecorded == 0) return 0;
+    const int n = std::min(max_n, kTimedKernels);
+    for (int k = 0; k < n; ++k) out_ms[k] = 0.0;
+    for (int t = 0; t < ws.tevRecorded; ++t) {
+        cudaEvent_t* ev = &ws.tev[(size_t)t * (kTimedKernels + 1)];
+        if (cudaEventSynchronize(ev[kTimedKernels]) != cudaSuccess) return 0;
+        for (int k = 0; k < n; ++k) {
+            float ms = 0.0f;
+            if (cudaEventElapsedTime(&ms, ev[k], ev[k + 1]) != cudaSuccess) return 0;
+            out_ms[k] += ms;
+        }
+    }
+    for (int k = 0; k < n; ++k) out_ms[k] /= ws.tevRecorded;
+    ws.tevRecorded = 0;
+    ws.tevNext = 0;
+    return n;
 }
 
 lvbgs_status lvbgs_get_scalars(lvbgs_handle h, lvbgs_scalars* out) {
