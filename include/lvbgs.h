@@ -124,6 +124,19 @@ lvbgs_status lvbgs_restore(lvbgs_handle h, const void* host_buffer, size_t bytes
 lvbgs_status lvbgs_lbsp_compute2(const uint8_t* image, int width, int height, int channels, long abs_threshold,
                                  float rel_threshold, size_t offset, uint16_t* desc, int device_id);
 
+/* Same computation as lvbgs_lbsp_compute2, for callers that must not allocate device memory
+ * (a real-time thread with a no-allocation rule, a process held to a fixed GPU memory budget).
+ * No counterpart in the reference. It allocates nothing: the image and descriptors are staged in
+ * one device array reserved when the library is loaded (24 MiB on every GPU that loads it, kept
+ * until the process exits), so width*height*channels may not exceed 8,388,608 (LVBGS_BAD_SIZE
+ * otherwise). The first call on a device looks the array up on that device; make that first call
+ * before any stream capture. All calls share the one array: calls that overlap on the GPU (from
+ * several host threads, or on streams that run concurrently) race and must be serialised by the
+ * caller. The call returns after its work on cuda_stream (NULL: the default stream) completed. */
+lvbgs_status lvbgs_lbsp_compute2_noalloc(const uint8_t* image, int width, int height, int channels,
+                                         long abs_threshold, float rel_threshold, size_t offset, uint16_t* desc,
+                                         int device_id, void* cuda_stream);
+
 /* last error message of a handle (or of the library when h is NULL) */
 const char* lvbgs_last_error(lvbgs_handle h);
 

@@ -77,6 +77,8 @@ SIGNATURES = {
     "lvbgs_restore": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "lvbgs_lbsp_compute2": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_long, C.c_float, C.c_size_t,
                                       C.c_void_p, C.c_int]),
+    "lvbgs_lbsp_compute2_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_long, C.c_float,
+                                              C.c_size_t, C.c_void_p, C.c_int, C.c_void_p]),
     "lvbgs_last_error": (C.c_char_p, [C.c_void_p]),
     "lvbgs_debug_map_bytes": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]),
     "lvbgs_debug_get_map": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]),

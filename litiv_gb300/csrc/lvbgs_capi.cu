@@ -430,6 +430,9 @@ uint8_t sat_round_u8(float v) {
 
 }  // namespace
 
+// library-level error message (lvbgs_last_error(NULL)) for entry points defined in other files
+lvbgs_status lvbgs::report_error(lvbgs_status st, const char* msg) { return fail(nullptr, st, msg); }
+
 extern "C" {
 
 lvbgs_status lvbgs_default_params(lvbgs_algo algo, lvbgs_params* out) {

@@ -22,7 +22,12 @@
 #define LV_HD inline
 #endif
 
+#include "../../include/lvbgs.h"
+
 namespace lvbgs {
+
+// sets the library-level error message returned by lvbgs_last_error(NULL); returns st
+lvbgs_status report_error(lvbgs_status st, const char* msg);
 
 constexpr int kTileW = 32;  // one warp per tile row: coalesced 32-pixel rows
 constexpr int kTileH = 8;
