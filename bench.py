@@ -23,6 +23,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "SuBSENSE Mpix/s: batched 64-stream vs plain 1-stream on GB300; p99 frame ms"
+# DRAM bytes (read + write) of one evaluation-kernel launch per pixel, from an ncu capture of
+# dram__bytes_read.sum + dram__bytes_write.sum on six streams of the mix (indices 52-57: four
+# 1280x720, one of them gray, and two 1920x1080; 7,833,600 px): 1,047,309,312 + 335,310,592 bytes.
+# roofline.traffic scales it to the launch by pixels.
+EVAL_DRAM_BYTES_PER_PX = (1047309312 + 335310592) / 7833600
 WORKLOAD = ("subsense-mix64: 16x320x240 + 24x640x480 + 16x1280x720 + 8x1920x1080, 48 BGR + 16 gray, "
             "default parameters, synthetic seeded scenes")
 # CPU sample: 4 streams of each resolution class
@@ -131,6 +136,23 @@ def cpu_baseline(n_frames=6, threads=None):
                 len(frames), n_frames - 1, px / 1e6, wall)}
 
 
+def serving_run(seconds):
+    """The serving workload (Poisson arrivals of 4 streams/s up to 256 live, lives U[10, 60] s, 30 fps,
+    320x240/640x480/1280x720/1920x1080 with p = .3/.3/.3/.1, a quarter single-channel), started from its
+    stationary population, through the native serving loop with pinned host frames and masks."""
+    from litiv_gb300 import serving
+    r = serving.simulate(duration_s=seconds, warmup_s=3.0, render_threads=8, seed=1)
+    keep = ["window_s", "frames", "mpix_per_s", "frames_per_s", "offered_mpix_per_s", "p50_ms", "p90_ms", "p99_ms",
+            "max_ms", "admit_wait_p50_ms", "admit_wait_p99_ms", "mean_live", "mean_resident", "mean_tick_streams",
+            "gpu_busy_frac", "ticks", "arrivals", "admitted", "rejected", "dropped", "spills", "restores",
+            "late_frames", "peak_live", "peak_device_bytes", "status"]
+    out = {k: r[k] for k in keep}
+    out["workload"] = ("Poisson arrivals 4/s (max 256 live), lives U[10,60] s, 30 fps, 320x240/640x480/1280x720/"
+                       "1920x1080 at .3/.3/.3/.1, 1/4 single-channel; stationary start; latency = submit -> "
+                       "mask in pinned host memory")
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -165,6 +187,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--serving-seconds", type=float, default=20.0,
+                    help="measured span of the serving workload run (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -340,6 +364,10 @@ def main():
         for b in subs_p:
             b.close()
 
+    serve = None
+    if rank == 0 and args.serving_seconds > 0:
+        serve = serving_run(args.serving_seconds)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline()
@@ -356,7 +384,9 @@ def main():
             "plain": plain,
             "batched_vs_plain": (value / world / plain["value"]) if plain else None,
             "roofline": {"bound": "hbm", "kernel": "lvbgs_k_eval", "achieved": eval_achieved, "peak": peak,
-                         "unit": "GB/s", "frac": eval_achieved / peak, "traffic": None,
+                         "unit": "GB/s", "frac": eval_achieved / peak,
+                         "traffic": EVAL_DRAM_BYTES_PER_PX * px_step, "traffic_per_px": EVAL_DRAM_BYTES_PER_PX,
+                         "algorithmic_per_px": eval_bytes_step / px_step,
                          "note": "algorithmic bytes of the evaluation kernel per launch / its average CUDA-event "
                                  "duration in the timed region; peak = measured copy bandwidth (of measured)"},
             "path_roofline": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -364,6 +394,7 @@ def main():
             "repair": {"rounds_per_tick": rounds, "rematched_px_per_tick": remat},
             "kernel_ms": kernel_ms,
             "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": 13 * args.steps,
+            "serving": serve,
             "clocks": clk.summary(),
         }
         print(json.dumps(out))

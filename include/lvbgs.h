@@ -35,7 +35,8 @@ typedef enum {
     LVBGS_OOM = 5,             /* device allocation failed */
     LVBGS_DEVICE_TIMEOUT = 6,  /* a bounded device-side wait gave up (kernel returned an error status) */
     LVBGS_DEVICE_ERROR = 7,    /* CUDA runtime error, or no usable sm_103 device */
-    LVBGS_UNSUPPORTED = 8      /* configuration outside what this implementation covers */
+    LVBGS_UNSUPPORTED = 8,     /* configuration outside what this implementation covers */
+    LVBGS_BUSY = 9             /* serving: a queue or capacity limit refused the request (retry later) */
 } lvbgs_status;
 
 typedef enum { LVBGS_ALGO_SUBSENSE = 0, LVBGS_ALGO_PAWCS = 1 } lvbgs_algo;
@@ -94,6 +95,26 @@ lvbgs_status lvbgs_apply(lvbgs_handle h, const uint8_t* image, size_t stride, ui
 lvbgs_status lvbgs_batch_apply(const lvbgs_handle* handles, const lvbgs_frame* frames, int n, void* cuda_stream);
 lvbgs_status lvbgs_batch_wait(const lvbgs_handle* handles, int n, void* cuda_stream);
 
+/* Batch contexts (serving; no reference counterpart). A context owns the work area of batched
+ * frame steps (descriptor tables, repair lists, status), so that a scheduler can batch any subset
+ * of streams per tick and keep up to LVBGS_BATCH_MAX_INFLIGHT ticks in flight on one CUDA stream.
+ * The frames and masks of a tick in flight should be in pinned host memory (or device memory),
+ * so that enqueueing the next tick does not wait for it; a stream may be in at most one tick in
+ * flight. Results are identical to lvbgs_apply. */
+#define LVBGS_BATCH_MAX_INFLIGHT 4
+typedef struct lvbgs_batch_ctx* lvbgs_batch;
+/* reserve_px / reserve_streams size the work area (it grows on demand while no tick is in flight) */
+lvbgs_status lvbgs_batch_create(int device_id, size_t reserve_px, int reserve_streams, lvbgs_batch* out);
+lvbgs_status lvbgs_batch_destroy(lvbgs_batch b);
+lvbgs_status lvbgs_batch_reserve(lvbgs_batch b, size_t px, int n_streams);
+/* enqueues one tick over n streams on cuda_stream (required, non-NULL); *ticket names it */
+lvbgs_status lvbgs_batch_submit(lvbgs_batch b, const lvbgs_handle* handles, const lvbgs_frame* frames, int n,
+                                void* cuda_stream, uint64_t* ticket);
+/* 1: the tick has completed, 0: not yet, -1: unknown ticket or device error */
+int lvbgs_batch_query(lvbgs_batch b, uint64_t ticket);
+/* waits for the tick (oldest first) and returns its status, device-side error flags included */
+lvbgs_status lvbgs_batch_complete(lvbgs_batch b, uint64_t ticket);
+
 /* getBackgroundImage (BackgroundSubtractorSuBSENSE.cpp:614-630): width*height*channels bytes */
 lvbgs_status lvbgs_get_background(lvbgs_handle h, uint8_t* out);
 /* getBackgroundDescriptorsImage (BackgroundSubtractorSuBSENSE.cpp:632-649): width*height*channels uint16 */
@@ -111,6 +132,8 @@ lvbgs_status lvbgs_get_roi(lvbgs_handle h, uint8_t* out);
 lvbgs_status lvbgs_get_size(lvbgs_handle h, int* width, int* height, int* channels);
 /* device bytes of the model state of a width x height x channels SuBSENSE stream (admission control) */
 size_t lvbgs_state_bytes(lvbgs_algo algo, int width, int height, int channels, size_t bg_samples);
+/* all device bytes an initialized, resident handle holds (model, scratch and its own workspace) */
+size_t lvbgs_device_bytes(lvbgs_algo algo, int width, int height, int channels, size_t bg_samples);
 
 /* Moves a stream's whole device state to `host_buffer` (lvbgs_state_bytes() bytes, pinned memory
  * recommended) and frees the device model; lvbgs_restore() uploads it again. The model evolves

@@ -45,7 +45,9 @@ typedef struct lvsynth_scene* lvsynth_handle;
 /* Benchmark presets: config 0 (320x240 BGR, 200 frames), 1 (1920x1080 BGR, 500 frames, ripple,
  * drift, 8 ellipses, two stopping), 3 (stream `index` of the 64-stream mix: 16x320x240,
  * 24x640x480, 16x1280x720, 8x1920x1080; every fourth stream single-channel; noise sigma U[2,6];
- * 2-10 shapes; 300 frames). base_seed selects the sequence. */
+ * 2-10 shapes; 300 frames), 4 (a serving stream: index = 2 * resolution class {320x240, 640x480,
+ * 1280x720, 1920x1080} + 1 for single-channel, content as in the 64-stream mix). base_seed
+ * selects the sequence. */
 lvbgs_status lvsynth_preset(int config, int index, uint64_t base_seed, lvsynth_config* out);
 lvbgs_status lvsynth_create(const lvsynth_config* cfg, lvsynth_handle* out);
 void lvsynth_destroy(lvsynth_handle h);

@@ -1,4 +1,5 @@
-"""ctypes binding of ``liblvbgs.so`` (the C-ABI declared in include/lvbgs.h and lvbgs_synth.h).
+"""ctypes binding of ``liblvbgs.so`` (the C-ABI declared in include/lvbgs.h, lvbgs_synth.h and
+lvserve.h).
 
 The library is the only compute path: there is no CPU fallback. Loading fails loudly when the
 in-tree build is missing (build it with ``python -m litiv_gb300.build`` or
@@ -12,9 +13,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("LVBGS_LIB") or os.path.join(HERE, "_build", "liblvbgs.so")
 
 # lvbgs_status
-OK, BAD_ARG, BAD_SIZE, BAD_TYPE, NOT_INITIALIZED, OOM, DEVICE_TIMEOUT, DEVICE_ERROR, UNSUPPORTED = range(9)
+OK, BAD_ARG, BAD_SIZE, BAD_TYPE, NOT_INITIALIZED, OOM, DEVICE_TIMEOUT, DEVICE_ERROR, UNSUPPORTED, BUSY = range(10)
 STATUS_NAMES = ["OK", "BAD_ARG", "BAD_SIZE", "BAD_TYPE", "NOT_INITIALIZED", "OOM", "DEVICE_TIMEOUT",
-                "DEVICE_ERROR", "UNSUPPORTED"]
+                "DEVICE_ERROR", "UNSUPPORTED", "BUSY"]
 ALGO_SUBSENSE, ALGO_PAWCS = 0, 1
 
 # map ids (LVBGS_MAP_*)
@@ -56,6 +57,44 @@ class SynthConfig(C.Structure):
                 ("n_frames", C.c_int)]
 
 
+class ServeConfig(C.Structure):
+    _fields_ = [("device_id", C.c_int), ("hbm_budget_bytes", C.c_size_t), ("host_spill_budget_bytes", C.c_size_t),
+                ("max_live", C.c_int), ("max_queue", C.c_int), ("idle_spill_ms", C.c_double),
+                ("max_inflight", C.c_int)]
+
+
+class ServeResult(C.Structure):
+    _fields_ = [("stream_id", C.c_int), ("tag", C.c_uint64), ("status", C.c_int), ("latency_ms", C.c_double)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("frames_done", C.c_uint64), ("px_done", C.c_uint64), ("ticks", C.c_uint64),
+                ("admitted", C.c_uint64), ("rejected", C.c_uint64), ("busy_refusals", C.c_uint64),
+                ("spills", C.c_uint64), ("restores", C.c_uint64), ("closed", C.c_uint64), ("live", C.c_int),
+                ("waiting", C.c_int), ("resident", C.c_int), ("spilled", C.c_int),
+                ("device_bytes_in_use", C.c_size_t), ("peak_device_bytes", C.c_size_t),
+                ("mean_tick_streams", C.c_double), ("busy_ms", C.c_double)]
+
+
+class SimConfig(C.Structure):
+    _fields_ = [("duration_s", C.c_double), ("warmup_s", C.c_double), ("arrival_rate", C.c_double),
+                ("life_min_s", C.c_double), ("life_max_s", C.c_double), ("fps", C.c_double),
+                ("res_prob", C.c_double * 4), ("gray_prob", C.c_double), ("prefill", C.c_int),
+                ("pool_frames", C.c_int), ("render_threads", C.c_int), ("seed", C.c_uint64)]
+
+
+class SimResult(C.Structure):
+    _fields_ = [("window_s", C.c_double), ("frames", C.c_uint64), ("mpix_per_s", C.c_double),
+                ("frames_per_s", C.c_double), ("offered_mpix_per_s", C.c_double), ("p50_ms", C.c_double),
+                ("p90_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double),
+                ("admit_wait_p50_ms", C.c_double), ("admit_wait_p99_ms", C.c_double), ("mean_live", C.c_double),
+                ("mean_resident", C.c_double), ("mean_tick_streams", C.c_double), ("gpu_busy_frac", C.c_double),
+                ("ticks", C.c_uint64), ("arrivals", C.c_uint64), ("admitted", C.c_uint64),
+                ("rejected", C.c_uint64), ("dropped", C.c_uint64), ("spills", C.c_uint64),
+                ("restores", C.c_uint64), ("late_frames", C.c_uint64), ("peak_live", C.c_int),
+                ("peak_device_bytes", C.c_size_t), ("status", C.c_int)]
+
+
 # exported symbol -> (restype, argtypes)
 SIGNATURES = {
     "lvbgs_default_params": (C.c_int, [C.c_int, C.POINTER(LvbgsParams)]),
@@ -85,6 +124,32 @@ SIGNATURES = {
     "lvbgs_get_scalars": (C.c_int, [C.c_void_p, C.POINTER(LvbgsScalars)]),
     "lvbgs_debug_tick_profile": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int]),
     "lvbgs_debug_set_timing": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "lvbgs_device_bytes": (C.c_size_t, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_size_t]),
+    "lvbgs_batch_create": (C.c_int, [C.c_int, C.c_size_t, C.c_int, C.POINTER(C.c_void_p)]),
+    "lvbgs_batch_destroy": (C.c_int, [C.c_void_p]),
+    "lvbgs_batch_reserve": (C.c_int, [C.c_void_p, C.c_size_t, C.c_int]),
+    "lvbgs_batch_submit": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(LvbgsFrame), C.c_int, C.c_void_p,
+                                     C.POINTER(C.c_uint64)]),
+    "lvbgs_batch_query": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "lvbgs_batch_complete": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "lvserve_default_config": (C.c_int, [C.POINTER(ServeConfig)]),
+    "lvserve_create": (C.c_int, [C.POINTER(ServeConfig), C.POINTER(C.c_void_p)]),
+    "lvserve_destroy": (C.c_int, [C.c_void_p]),
+    "lvserve_open": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(LvbgsParams), C.c_void_p, C.c_int, C.c_int, C.c_int,
+                               C.c_size_t, C.c_void_p, C.POINTER(C.c_int)]),
+    "lvserve_submit": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p, C.c_double, C.c_uint64]),
+    "lvserve_close": (C.c_int, [C.c_void_p, C.c_int]),
+    "lvserve_poll": (C.c_int, [C.c_void_p, C.POINTER(ServeResult), C.c_int, C.c_int]),
+    "lvserve_drain": (C.c_int, [C.c_void_p, C.c_int]),
+    "lvserve_get_stats": (C.c_int, [C.c_void_p, C.POINTER(ServeStats)]),
+    "lvserve_latency_quantile": (C.c_double, [C.c_void_p, C.c_double]),
+    "lvserve_reset_stats": (C.c_int, [C.c_void_p]),
+    "lvserve_stream_state": (C.c_int, [C.c_void_p, C.c_int]),
+    "lvserve_last_error": (C.c_char_p, [C.c_void_p]),
+    "lvserve_plan_room": (C.c_int, [C.c_size_t, C.c_size_t, C.c_size_t, C.POINTER(C.c_size_t),
+                                    C.POINTER(C.c_double), C.c_int, C.c_double, C.POINTER(C.c_int)]),
+    "lvserve_default_sim_config": (C.c_int, [C.POINTER(SimConfig)]),
+    "lvserve_simulate": (C.c_int, [C.POINTER(ServeConfig), C.POINTER(SimConfig), C.POINTER(SimResult)]),
     "lvsynth_preset": (C.c_int, [C.c_int, C.c_int, C.c_uint64, C.POINTER(SynthConfig)]),
     "lvsynth_create": (C.c_int, [C.POINTER(SynthConfig), C.POINTER(C.c_void_p)]),
     "lvsynth_destroy": (None, [C.c_void_p]),

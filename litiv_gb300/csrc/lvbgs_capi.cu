@@ -265,28 +265,29 @@ cudaError_t coop_grid(int* maxBlocks) {
     return cudaSuccess;
 }
 
-// enqueue one tick over n streams described in ws.h_streams (tileBase etc. filled here)
-lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t st) {
+// enqueue one tick over the n streams described in hS (tileBase etc. filled here); hDs holds n+1
+// entries. Both are host arrays the descriptor uploads read from (pinned for ticks in flight).
+lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t st, StreamDev* hS,
+                         unsigned long long* hDs) {
     int totalTiles = 0, totalRows = 0;
     size_t totalPx = 0;
     unsigned long long ds = 0;
-    ws.h_dsBase.resize(n + 1);
     for (int i = 0; i < n; ++i) {
-        StreamDev& S = ws.h_streams[i];
+        StreamDev& S = hS[i];
         S.tileBase = totalTiles;
         S.rowBase = totalRows;
         totalTiles += S.nTiles;
         totalRows += S.H;
         totalPx += (size_t)S.npx;
-        ws.h_dsBase[i] = ds;
+        hDs[i] = ds;
         // only streams with the frame-level analysis enabled down-sample
         if (S.lrScaling) ds += (unsigned long long)S.dsW * S.dsH;
     }
-    ws.h_dsBase[n] = ds;
+    hDs[n] = ds;
     LV_CUDA(errh, ws.ensure(totalPx, n), "workspace allocation");
-    LV_CUDA(errh, cudaMemcpyAsync(ws.d_streams, ws.h_streams.data(), sizeof(StreamDev) * n, cudaMemcpyHostToDevice, st),
+    LV_CUDA(errh, cudaMemcpyAsync(ws.d_streams, hS, sizeof(StreamDev) * n, cudaMemcpyHostToDevice, st),
             "descriptor upload");
-    LV_CUDA(errh, cudaMemcpyAsync(ws.d_dsBase, ws.h_dsBase.data(), sizeof(unsigned long long) * (n + 1),
+    LV_CUDA(errh, cudaMemcpyAsync(ws.d_dsBase, hDs, sizeof(unsigned long long) * (n + 1),
                                   cudaMemcpyHostToDevice, st),
             "descriptor upload");
     LV_CUDA(errh, cudaMemsetAsync(ws.work, 0, sizeof(TickWork), st), "work reset");
@@ -352,15 +353,23 @@ lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t s
     LV_CUDA(errh, cudaGetLastError(), "frame step launch");
     return LVBGS_OK;
 }
+lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t st) {
+    ws.h_dsBase.resize(n + 1);
+    return launch_tick(errh, ws, n, st, ws.h_streams.data(), ws.h_dsBase.data());
+}
 
-lvbgs_status read_work_status(lvbgs_handle errh, Workspace& ws) {
-    TickWork w;
-    LV_CUDA(errh, cudaMemcpy(&w, ws.work, sizeof(TickWork), cudaMemcpyDeviceToHost), "status read-back");
+// the device-side error flags of a tick as a status
+lvbgs_status status_from_work(lvbgs_handle errh, const TickWork& w) {
     if (w.err & ERR_BARRIER_TIMEOUT) return fail(errh, LVBGS_DEVICE_TIMEOUT, "grid barrier wait timed out");
     if (w.err & ERR_REPAIR_LIMIT) return fail(errh, LVBGS_DEVICE_ERROR, "raster-order repair did not converge");
     if (w.err & ERR_UF_LIMIT) return fail(errh, LVBGS_DEVICE_ERROR, "hole-filling union-find exceeded its bound");
     if (w.err & ERR_RING) return fail(errh, LVBGS_DEVICE_ERROR, "closed mask is not zero at pixel (0,0)");
     return LVBGS_OK;
+}
+lvbgs_status read_work_status(lvbgs_handle errh, Workspace& ws) {
+    TickWork w;
+    LV_CUDA(errh, cudaMemcpy(&w, ws.work, sizeof(TickWork), cudaMemcpyDeviceToHost), "status read-back");
+    return status_from_work(errh, w);
 }
 
 // stages a frame for the kernel: returns the device pointer the kernel reads
@@ -647,7 +656,9 @@ lvbgs_status lvbgs_apply(lvbgs_handle h, const uint8_t* img, size_t stride, uint
     return read_work_status(h, h->ws);
 }
 
-lvbgs_status lvbgs_batch_apply(const lvbgs_handle* hs, const lvbgs_frame* frames, int n, void* cuda_stream) {
+namespace {
+// checks a batch (initialized handles on one device, each at most once)
+lvbgs_status check_batch(const lvbgs_handle* hs, const lvbgs_frame* frames, int n) {
     if (!hs || !frames || n <= 0) return fail(nullptr, LVBGS_BAD_ARG, "empty batch");
     lvbgs_handle lead = hs[0];
     for (int i = 0; i < n; ++i) {
@@ -658,29 +669,45 @@ lvbgs_status lvbgs_batch_apply(const lvbgs_handle* hs, const lvbgs_frame* frames
         for (int j = 0; j < i; ++j)
             if (hs[j] == hs[i]) return fail(lead, LVBGS_BAD_ARG, "a handle appears twice in the batch");
     }
-    cudaSetDevice(lead->device);
-    cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : lead->stream;
-    Workspace& ws = lead->batchWs;
-    ws.h_streams.resize(n);
+    return LVBGS_OK;
+}
+// stages the frames and fills the n stream descriptors of one batched tick
+lvbgs_status prepare_batch(const lvbgs_handle* hs, const lvbgs_frame* frames, int n, cudaStream_t st, StreamDev* out) {
     for (int i = 0; i < n; ++i) {
         lvbgs_handle h = hs[i];
         const uint8_t* dimg = nullptr;
         lvbgs_status s = stage_frame(h, frames[i].image, frames[i].stride, st, &dimg);
         if (s != LVBGS_OK) return s;
-        ws.h_streams[i] = h->sd;
-        StreamDev& S = ws.h_streams[i];
+        out[i] = h->sd;
+        StreamDev& S = out[i];
         S.frame = dimg;
         const bool devMask = frames[i].fgmask && is_device_ptr(frames[i].fgmask);
         S.maskOut = devMask ? frames[i].fgmask : h->d_mask;
         set_lr(S, frames[i].learning_rate);
     }
-    lvbgs_status s = launch_tick(lead, ws, n, st);
-    if (s != LVBGS_OK) return s;
+    return LVBGS_OK;
+}
+// enqueues the copies of the masks that go to host memory
+lvbgs_status download_masks(const lvbgs_handle* hs, const lvbgs_frame* frames, int n, cudaStream_t st) {
     for (int i = 0; i < n; ++i)
         if (frames[i].fgmask && !is_device_ptr(frames[i].fgmask))
-            LV_CUDA(lead, cudaMemcpyAsync(frames[i].fgmask, hs[i]->d_mask, hs[i]->npx, cudaMemcpyDeviceToHost, st),
+            LV_CUDA(hs[0], cudaMemcpyAsync(frames[i].fgmask, hs[i]->d_mask, hs[i]->npx, cudaMemcpyDeviceToHost, st),
                     "mask download");
     return LVBGS_OK;
+}
+}  // namespace
+
+lvbgs_status lvbgs_batch_apply(const lvbgs_handle* hs, const lvbgs_frame* frames, int n, void* cuda_stream) {
+    lvbgs_status s = check_batch(hs, frames, n);
+    if (s != LVBGS_OK) return s;
+    lvbgs_handle lead = hs[0];
+    cudaSetDevice(lead->device);
+    cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : lead->stream;
+    Workspace& ws = lead->batchWs;
+    ws.h_streams.resize(n);
+    if ((s = prepare_batch(hs, frames, n, st, ws.h_streams.data())) != LVBGS_OK) return s;
+    if ((s = launch_tick(lead, ws, n, st)) != LVBGS_OK) return s;
+    return download_masks(hs, frames, n, st);
 }
 
 lvbgs_status lvbgs_batch_wait(const lvbgs_handle* hs, int n, void* cuda_stream) {
@@ -690,6 +717,143 @@ lvbgs_status lvbgs_batch_wait(const lvbgs_handle* hs, int n, void* cuda_stream) 
     cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : lead->stream;
     LV_CUDA(lead, cudaStreamSynchronize(st), "batched frame step");
     return read_work_status(lead, lead->batchWs);
+}
+
+// ---- batch contexts: a work area owned apart from the streams, with ticks kept in flight ----
+struct lvbgs_batch_ctx {
+    int device = 0;
+    Workspace ws;
+    cudaStream_t stream = nullptr;  // the stream of the ticks in flight
+    struct Slot {
+        StreamDev* hS = nullptr;             // pinned descriptor table of the tick
+        unsigned long long* hDs = nullptr;   // pinned down-sampling offsets
+        TickWork* hWork = nullptr;           // pinned copy of the tick's status
+        int cap = 0;
+        cudaEvent_t done = nullptr;
+        uint64_t ticket = 0;
+        bool busy = false;
+    } slots[LVBGS_BATCH_MAX_INFLIGHT];
+    uint64_t next = 1;
+    int inflight = 0;
+};
+
+namespace {
+void free_slot(lvbgs_batch_ctx::Slot& sl) {
+    cudaFreeHost(sl.hS);
+    cudaFreeHost(sl.hDs);
+    sl.hS = nullptr;
+    sl.hDs = nullptr;
+    sl.cap = 0;
+}
+cudaError_t grow_slot(lvbgs_batch_ctx::Slot& sl, int n) {
+    if (n <= sl.cap) return cudaSuccess;
+    free_slot(sl);
+    const int cap = std::max(n + n / 2, 16);
+    cudaError_t e = cudaHostAlloc((void**)&sl.hS, sizeof(StreamDev) * cap, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaHostAlloc((void**)&sl.hDs, sizeof(unsigned long long) * (cap + 1), cudaHostAllocDefault);
+    if (e == cudaSuccess) sl.cap = cap;
+    return e;
+}
+}  // namespace
+
+lvbgs_status lvbgs_batch_create(int device_id, size_t reserve_px, int reserve_streams, lvbgs_batch* out) {
+    if (!out) return fail(nullptr, LVBGS_BAD_ARG, "null output");
+    *out = nullptr;
+    if (reserve_streams < 0) return fail(nullptr, LVBGS_BAD_ARG, "negative stream reservation");
+    if (cudaSetDevice(device_id) != cudaSuccess) return fail(nullptr, LVBGS_DEVICE_ERROR, "cannot select the CUDA device");
+    lvbgs_batch b = new lvbgs_batch_ctx();
+    b->device = device_id;
+    cudaError_t e = b->ws.ensure(std::max<size_t>(reserve_px, 1), std::max(reserve_streams, 1));
+    for (auto& sl : b->slots) {
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaHostAlloc((void**)&sl.hWork, sizeof(TickWork), cudaHostAllocDefault);
+        if (e == cudaSuccess) e = grow_slot(sl, std::max(reserve_streams, 1));
+    }
+    if (e != cudaSuccess) {
+        lvbgs_batch_destroy(b);
+        return cuda_fail(nullptr, e, "batch context allocation");
+    }
+    *out = b;
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_batch_destroy(lvbgs_batch b) {
+    if (!b) return LVBGS_OK;
+    cudaSetDevice(b->device);
+    for (auto& sl : b->slots)
+        if (sl.busy && sl.done) cudaEventSynchronize(sl.done);
+    for (auto& sl : b->slots) {
+        free_slot(sl);
+        cudaFreeHost(sl.hWork);
+        if (sl.done) cudaEventDestroy(sl.done);
+    }
+    b->ws.release();
+    delete b;
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_batch_reserve(lvbgs_batch b, size_t px, int n_streams) {
+    if (!b || n_streams < 0) return fail(nullptr, LVBGS_BAD_ARG, "bad argument");
+    cudaSetDevice(b->device);
+    if (b->inflight > 0 && (px > b->ws.cap || n_streams > b->ws.nStreamsCap))
+        return fail(nullptr, LVBGS_BAD_ARG, "cannot grow a batch context with ticks in flight");
+    LV_CUDA(nullptr, b->ws.ensure(std::max<size_t>(px, 1), std::max(n_streams, 1)), "batch workspace allocation");
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_batch_submit(lvbgs_batch b, const lvbgs_handle* hs, const lvbgs_frame* frames, int n,
+                                void* cuda_stream, uint64_t* ticket) {
+    if (!b || !ticket) return fail(nullptr, LVBGS_BAD_ARG, "null argument");
+    lvbgs_status s = check_batch(hs, frames, n);
+    if (s != LVBGS_OK) return s;
+    lvbgs_handle lead = hs[0];
+    if (lead->device != b->device) return fail(lead, LVBGS_BAD_ARG, "batch context and handles are on different devices");
+    cudaSetDevice(b->device);
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    if (!st) return fail(lead, LVBGS_BAD_ARG, "batched ticks of a context need an explicit CUDA stream");
+    if (b->inflight > 0 && st != b->stream)
+        return fail(lead, LVBGS_BAD_ARG, "ticks in flight on one batch context must share one CUDA stream");
+    lvbgs_batch_ctx::Slot& sl = b->slots[b->next % LVBGS_BATCH_MAX_INFLIGHT];
+    if (sl.busy) return fail(lead, LVBGS_BAD_ARG, "too many ticks in flight: complete the oldest first");
+    size_t px = 0;
+    for (int i = 0; i < n; ++i) px += hs[i]->npx;
+    if (b->inflight > 0 && (px > b->ws.cap || n > b->ws.nStreamsCap))
+        return fail(lead, LVBGS_BAD_ARG, "batch exceeds the context's reservation while ticks are in flight");
+    LV_CUDA(lead, grow_slot(sl, n), "descriptor table allocation");
+    if ((s = prepare_batch(hs, frames, n, st, sl.hS)) != LVBGS_OK) return s;
+    if ((s = launch_tick(lead, b->ws, n, st, sl.hS, sl.hDs)) != LVBGS_OK) return s;
+    if ((s = download_masks(hs, frames, n, st)) != LVBGS_OK) return s;
+    LV_CUDA(lead, cudaMemcpyAsync(sl.hWork, b->ws.work, sizeof(TickWork), cudaMemcpyDeviceToHost, st), "status copy");
+    LV_CUDA(lead, cudaEventRecord(sl.done, st), "completion event");
+    sl.ticket = b->next++;
+    sl.busy = true;
+    b->stream = st;
+    ++b->inflight;
+    *ticket = sl.ticket;
+    return LVBGS_OK;
+}
+
+int lvbgs_batch_query(lvbgs_batch b, uint64_t ticket) {
+    if (!b) return -1;
+    lvbgs_batch_ctx::Slot& sl = b->slots[ticket % LVBGS_BATCH_MAX_INFLIGHT];
+    if (!sl.busy || sl.ticket != ticket) return -1;
+    cudaSetDevice(b->device);
+    const cudaError_t e = cudaEventQuery(sl.done);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) return 0;
+    return -1;
+}
+
+lvbgs_status lvbgs_batch_complete(lvbgs_batch b, uint64_t ticket) {
+    if (!b) return fail(nullptr, LVBGS_BAD_ARG, "null batch context");
+    lvbgs_batch_ctx::Slot& sl = b->slots[ticket % LVBGS_BATCH_MAX_INFLIGHT];
+    if (!sl.busy || sl.ticket != ticket) return fail(nullptr, LVBGS_BAD_ARG, "unknown or already completed tick");
+    cudaSetDevice(b->device);
+    const cudaError_t e = cudaEventSynchronize(sl.done);
+    sl.busy = false;
+    --b->inflight;
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "batched frame step");
+    return status_from_work(nullptr, *sl.hWork);
 }
 
 lvbgs_status lvbgs_get_background(lvbgs_handle h, uint8_t* out) {
@@ -773,6 +937,15 @@ lvbgs_status lvbgs_get_size(lvbgs_handle h, int* w, int* hh, int* c) {
 size_t lvbgs_state_bytes(lvbgs_algo algo, int W, int H, int C, size_t N) {
     if (algo != LVBGS_ALGO_SUBSENSE || W <= 0 || H <= 0 || (C != 1 && C != 3)) return 0;
     return make_layout(W, H, C, N ? N : 50).persist;
+}
+
+size_t lvbgs_device_bytes(lvbgs_algo algo, int W, int H, int C, size_t N) {
+    if (algo != LVBGS_ALGO_SUBSENSE || W <= 0 || H <= 0 || (C != 1 && C != 3)) return 0;
+    // model and scratch block, plus the handle's own workspace (status, one descriptor table,
+    // four repair lists of one entry per pixel)
+    const size_t npx = (size_t)W * H;
+    return make_layout(W, H, C, N ? N : 50).total + sizeof(TickWork) + 8 * sizeof(StreamDev) +
+           9 * sizeof(unsigned long long) + 4 * sizeof(unsigned long long) * npx;
 }
 
 lvbgs_status lvbgs_spill(lvbgs_handle h, void* host, size_t bytes) {

@@ -226,6 +226,16 @@ lvbgs_status lvsynth_preset(int config, int index, uint64_t base, lvsynth_config
         const int sigma = rnd_range(seed, 1, 0, 2000, 6000);
         const int ns = rnd_range(seed, 2, 0, 2, 10);
         *o = lvsynth_config{W, H, C, seed, sigma, ns, 20, 60, 256, 768, 0, 0, 0, 0, 300};
+    } else if (config == 4) {
+        // serving streams: index = 2 * resolution class (320x240, 640x480, 1280x720, 1920x1080)
+        // + (1 for single-channel); content as in the 64-stream mix, one sequence per base seed
+        if (index < 0 || index >= 8) return LVBGS_BAD_ARG;
+        static const int kW[4] = {320, 640, 1280, 1920}, kH[4] = {240, 480, 720, 1080};
+        const int W = kW[index / 2], H = kH[index / 2], C = (index & 1) ? 1 : 3;
+        const uint64_t seed = base * 1000003ull + 64u + (uint64_t)index;
+        const int sigma = rnd_range(seed, 1, 0, 2000, 6000);
+        const int ns = rnd_range(seed, 2, 0, 2, 10);
+        *o = lvsynth_config{W, H, C, seed, sigma, ns, 20, 60, 256, 768, 0, 0, 0, 0, 1800};
     } else {
         return LVBGS_UNSUPPORTED;
     }

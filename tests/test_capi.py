@@ -17,7 +17,7 @@ def declared_functions():
     for path in glob.glob(os.path.join(INCLUDE, "*.h")):
         src = open(path).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b((?:lvbgs|lvsynth)_\w+)\s*\(", src, flags=re.M):
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b((?:lvbgs|lvsynth|lvserve)_\w+)\s*\(", src, flags=re.M):
             names.add(m.group(1))
     return names
 
