@@ -38,14 +38,22 @@ typedef struct {
     int drift;                   /* 1: +-15 global illumination drift over 250 frames */
     int n_stopping;              /* the first n shapes stop for 100 frames */
     int n_frames;                /* nominal sequence length */
+    int thermal;                 /* 1: thermal-like scene (see below); shape sizes are blob radii and speeds
+                                    are the random-walk step range in whole pixels */
 } lvsynth_config;
+
+/* Thermal-like scene (config 2): a smooth diagonal gradient 80..140 plus low-frequency value noise
+ * of amplitude 10 (random values on a 64-pixel grid, bilinear), warm blobs of intensity 180..240
+ * with a Gaussian falloff (sigma = radius/2, cut at two radii), each on a random walk of 1..5 pixels
+ * per frame in one of eight directions (reflected at the borders); ground truth = within one radius. */
 
 typedef struct lvsynth_scene* lvsynth_handle;
 
 /* Benchmark presets: config 0 (320x240 BGR, 200 frames), 1 (1920x1080 BGR, 500 frames, ripple,
  * drift, 8 ellipses, two stopping), 3 (stream `index` of the 64-stream mix: 16x320x240,
  * 24x640x480, 16x1280x720, 8x1920x1080; every fourth stream single-channel; noise sigma U[2,6];
- * 2-10 shapes; 300 frames), 4 (a serving stream: index = 2 * resolution class {320x240, 640x480,
+ * 2-10 shapes; 300 frames), 2 (640x480 single-channel thermal-like scene, six blobs of radius 10-40,
+ * noise sigma 2, 300 frames), 4 (a serving stream: index = 2 * resolution class {320x240, 640x480,
  * 1280x720, 1920x1080} + 1 for single-channel, content as in the 64-stream mix). base_seed
  * selects the sequence. */
 lvbgs_status lvsynth_preset(int config, int index, uint64_t base_seed, lvsynth_config* out);

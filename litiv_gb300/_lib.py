@@ -54,7 +54,7 @@ class SynthConfig(C.Structure):
                 ("noise_sigma_milli", C.c_int), ("n_shapes", C.c_int), ("shape_min", C.c_int),
                 ("shape_max", C.c_int), ("speed_min_q8", C.c_int), ("speed_max_q8", C.c_int),
                 ("ellipses_only", C.c_int), ("ripple", C.c_int), ("drift", C.c_int), ("n_stopping", C.c_int),
-                ("n_frames", C.c_int)]
+                ("n_frames", C.c_int), ("thermal", C.c_int)]
 
 
 class ServeConfig(C.Structure):

@@ -23,9 +23,11 @@ struct Shape {
     int ellipse;
     uint32_t col;  // packed channel values
 };
+constexpr int kFalloffN = 1024;  // falloff table over u = 256 * d^2 / r^2 in [0, 4)
 struct FrameParams {
     int W, H, C;
     int nShapes;
+    int thermal;  // shapes are blobs: (x, y) centre, w radius, col intensity
     Shape shapes[LVSYNTH_MAX_SHAPES];
     int drift;
     int rippleOn, rx0, ry0;
@@ -54,18 +56,30 @@ LV_HD int reflect_pos(long long p, long long range) {
 }
 
 // one pixel of frame t (host and device)
-LV_HD void render_px(const FrameParams& F, const uint8_t* tex, const int8_t* rippleTab, int x, int y, uint8_t* out,
-                     uint8_t* gt) {
+LV_HD void render_px(const FrameParams& F, const uint8_t* tex, const int8_t* rippleTab, const uint16_t* falloff, int x,
+                     int y, uint8_t* out, uint8_t* gt) {
     const int C = F.C;
     int v[3];
     const size_t p = (size_t)y * F.W + x;
     for (int c = 0; c < C; ++c) v[c] = tex[p * C + c] + F.drift;
+    int inside = 0;
+    if (F.thermal) {
+        // warm blobs with a Gaussian falloff: v += (I - v) * f(d^2 / r^2), f in 1/256
+        for (int i = 0; i < F.nShapes; ++i) {
+            const Shape& s = F.shapes[i];
+            const long long dx = x - s.x, dy = y - s.y, r2 = (long long)s.w * s.w;
+            const long long d2 = dx * dx + dy * dy;
+            if (d2 >= 4 * r2) continue;
+            const int f = falloff[(int)(d2 * 256 / r2)];
+            for (int c = 0; c < C; ++c) v[c] += (int)(((long long)((int)s.col - v[c]) * f) / 256);
+            if (d2 < r2) inside = 1;
+        }
+    }
     if (F.rippleOn && x >= F.rx0 && x < F.rx0 + kRippleW && y >= F.ry0 && y < F.ry0 + kRippleH) {
         const int r = rippleTab[(int)((11u * (uint32_t)x + 37u * F.t) % (uint32_t)kRipplePeriod)];
         for (int c = 0; c < C; ++c) v[c] += r;
     }
-    int inside = 0;
-    for (int i = 0; i < F.nShapes; ++i) {
+    for (int i = 0; i < (F.thermal ? 0 : F.nShapes); ++i) {
         const Shape& s = F.shapes[i];
         const int dx = x - s.x, dy = y - s.y;
         if (dx < 0 || dy < 0 || dx >= s.w || dy >= s.h) continue;
@@ -94,10 +108,11 @@ LV_HD void render_px(const FrameParams& F, const uint8_t* tex, const int8_t* rip
     if (gt) gt[p] = inside ? 255 : 0;
 }
 
-__global__ void render_kernel(FrameParams F, const uint8_t* tex, const int8_t* rippleTab, uint8_t* out, uint8_t* gt) {
+__global__ void render_kernel(FrameParams F, const uint8_t* tex, const int8_t* rippleTab, const uint16_t* falloff,
+                              uint8_t* out, uint8_t* gt) {
     const int total = F.W * F.H;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x)
-        render_px(F, tex, rippleTab, p % F.W, p / F.W, out, gt);
+        render_px(F, tex, rippleTab, falloff, p % F.W, p / F.W, out, gt);
 }
 
 }  // namespace
@@ -113,11 +128,36 @@ struct lvsynth_scene {
         long long x0, y0, vx, vy;  // 1/256 px
         int tstop;
     } shapes[LVSYNTH_MAX_SHAPES];
+    uint16_t falloff[kFalloffN];
     uint8_t* d_tex = nullptr;
     int8_t* d_ripple = nullptr;
+    uint16_t* d_falloff = nullptr;
 };
 
 namespace {
+
+// thermal background: diagonal gradient 80..140 plus value noise of amplitude 10 on a 64-px grid
+void build_thermal_texture(lvsynth_scene* s) {
+    const int W = s->cfg.width, H = s->cfg.height, C = s->cfg.channels;
+    const uint64_t seed = s->cfg.seed;
+    const int G = 64, gw = W / G + 2, gh = H / G + 2;
+    std::vector<int> grid((size_t)gw * gh);
+    for (int j = 0; j < gh; ++j)
+        for (int i = 0; i < gw; ++i) grid[(size_t)j * gw + i] = rnd_range(seed, 0x7E0u + (uint32_t)j, (uint32_t)i, -10, 10);
+    s->tex.resize((size_t)W * H * C);
+    const long long span = (long long)(W + H - 2 > 0 ? W + H - 2 : 1);
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const int gx = x / G, gy = y / G, fx = x % G, fy = y % G;
+            const long long a = grid[(size_t)gy * gw + gx], b = grid[(size_t)gy * gw + gx + 1];
+            const long long c = grid[(size_t)(gy + 1) * gw + gx], d = grid[(size_t)(gy + 1) * gw + gx + 1];
+            const long long top = a * (G - fx) + b * fx, bot = c * (G - fx) + d * fx;
+            const long long vn = top * (G - fy) + bot * fy;  // value noise x 64*64
+            const long long grad = 80 * 4096 + 60 * 4096 * (long long)(x + y) / span;
+            const long long v = (grad + vn + (vn >= 0 ? 2048 : -2048)) / 4096;
+            for (int ch = 0; ch < C; ++ch) s->tex[((size_t)y * W + x) * C + ch] = (uint8_t)std::min<long long>(std::max<long long>(v, 0), 255);
+        }
+}
 
 void build_texture(lvsynth_scene* s) {
     const int W = s->cfg.width, H = s->cfg.height, C = s->cfg.channels;
@@ -188,6 +228,43 @@ FrameParams frame_params(const lvsynth_scene* s, int t) {
     F.rx0 = s->rx0;
     F.ry0 = s->ry0;
     F.nShapes = c.n_shapes;
+    F.thermal = c.thermal;
+    if (c.thermal) {
+        // random walks: step k of blob i is one of eight directions times a length in [speed_min, speed_max]
+        static const int dirs[8][2] = {{1, 0}, {1, 1}, {0, 1}, {-1, 1}, {-1, 0}, {-1, -1}, {0, -1}, {1, -1}};
+        for (int i = 0; i < c.n_shapes; ++i) {
+            const auto& si = s->shapes[i];
+            long long px = si.x0, py = si.y0;
+            const int r = si.w;
+            for (int k = 0; k < t; ++k) {
+                const uint32_t rr = rnd32(c.seed, 0xB10Bu + (uint32_t)i, (uint32_t)k, 0x57u, 0);
+                const int dir = (int)(rr & 7u);
+                const int len = c.speed_min_q8 + (int)((rr >> 3) % (uint32_t)(c.speed_max_q8 - c.speed_min_q8 + 1));
+                px += dirs[dir][0] * len;
+                py += dirs[dir][1] * len;
+                // reflect into [r, W-1-r] x [r, H-1-r]
+                const long long lx = r, hx = c.width - 1 - r, ly = r, hy = c.height - 1 - r;
+                if (hx > lx) {
+                    while (px < lx || px > hx) px = px < lx ? 2 * lx - px : 2 * hx - px;
+                } else {
+                    px = c.width / 2;
+                }
+                if (hy > ly) {
+                    while (py < ly || py > hy) py = py < ly ? 2 * ly - py : 2 * hy - py;
+                } else {
+                    py = c.height / 2;
+                }
+            }
+            Shape& o = F.shapes[i];
+            o.x = (int)px;
+            o.y = (int)py;
+            o.w = r;
+            o.h = r;
+            o.ellipse = 1;
+            o.col = si.col;
+        }
+        return F;
+    }
     for (int i = 0; i < c.n_shapes; ++i) {
         const auto& si = s->shapes[i];
         long long te = t;
@@ -226,6 +303,10 @@ lvbgs_status lvsynth_preset(int config, int index, uint64_t base, lvsynth_config
         const int sigma = rnd_range(seed, 1, 0, 2000, 6000);
         const int ns = rnd_range(seed, 2, 0, 2, 10);
         *o = lvsynth_config{W, H, C, seed, sigma, ns, 20, 60, 256, 768, 0, 0, 0, 0, 300};
+    } else if (config == 2) {
+        // thermal-like 640x480 gray: six warm blobs (radius 10-40), random walks of 1-5 px per frame
+        if (index != 0) return LVBGS_BAD_ARG;
+        *o = lvsynth_config{640, 480, 1, base * 1000003ull + 2u, 2000, 6, 10, 40, 1, 5, 1, 0, 0, 0, 300, 1};
     } else if (config == 4) {
         // serving streams: index = 2 * resolution class (320x240, 640x480, 1280x720, 1920x1080)
         // + (1 for single-channel); content as in the 64-stream mix, one sequence per base seed
@@ -251,7 +332,17 @@ lvbgs_status lvsynth_create(const lvsynth_config* cfg, lvsynth_handle* out) {
         return LVBGS_BAD_ARG;
     lvsynth_scene* s = new lvsynth_scene();
     s->cfg = *cfg;
-    build_texture(s);
+    if (cfg->thermal) {
+        if (cfg->speed_min_q8 < 0 || cfg->speed_max_q8 < cfg->speed_min_q8) {
+            delete s;
+            return LVBGS_BAD_ARG;
+        }
+        build_thermal_texture(s);
+    } else {
+        build_texture(s);
+    }
+    // falloff exp(-2 u) (sigma = radius/2) in 1/256 over u = d^2/r^2 in [0, 4)
+    for (int i = 0; i < kFalloffN; ++i) s->falloff[i] = (uint16_t)std::lround(256.0 * std::exp(-2.0 * i / 256.0));
     for (int i = 0; i < kRipplePeriod; ++i) s->ripple[i] = (int8_t)std::lround(20.0 * std::sin(2.0 * M_PI * i / kRipplePeriod));
     const uint64_t seed = cfg->seed;
     s->rx0 = cfg->width > kRippleW ? rnd_range(seed, 10, 0, 0, cfg->width - kRippleW) : 0;
@@ -272,6 +363,14 @@ lvbgs_status lvsynth_create(const lvsynth_config* cfg, lvsynth_handle* out) {
         sh.vx = (rnd32(seed, a, 9, 0, 2) & 1u) ? vx : -vx;
         sh.vy = (rnd32(seed, a, 9, 0, 3) & 1u) ? vy : -vy;
         sh.tstop = i < cfg->n_stopping ? 50 + 150 * i : -1;
+        if (cfg->thermal) {
+            // blob: w = radius, col = intensity 180..240, (x0, y0) = centre in whole pixels
+            const int r = rnd_range(seed, a, 1, cfg->shape_min, cfg->shape_max);
+            sh.w = sh.h = r;
+            sh.col = (uint32_t)rnd_range(seed, a, 4, 180, 240);
+            sh.x0 = rnd_range(seed, a, 5, std::min(r, cfg->width - 1), std::max(r, cfg->width - 1 - r));
+            sh.y0 = rnd_range(seed, a, 6, std::min(r, cfg->height - 1), std::max(r, cfg->height - 1 - r));
+        }
     }
     *out = s;
     return LVBGS_OK;
@@ -281,6 +380,7 @@ void lvsynth_destroy(lvsynth_handle h) {
     if (!h) return;
     cudaFree(h->d_tex);
     cudaFree(h->d_ripple);
+    cudaFree(h->d_falloff);
     delete h;
 }
 
@@ -294,7 +394,7 @@ lvbgs_status lvsynth_render(lvsynth_handle h, int t, uint8_t* frame, uint8_t* gt
         out = scratch.data();
     }
     for (int y = 0; y < F.H; ++y)
-        for (int x = 0; x < F.W; ++x) render_px(F, h->tex.data(), h->ripple, x, y, out, gt);
+        for (int x = 0; x < F.W; ++x) render_px(F, h->tex.data(), h->ripple, h->falloff, x, y, out, gt);
     return LVBGS_OK;
 }
 
@@ -306,9 +406,12 @@ lvbgs_status lvsynth_render_device(lvsynth_handle h, int t, uint8_t* frame, uint
         if (cudaMemcpy(h->d_tex, h->tex.data(), h->tex.size(), cudaMemcpyHostToDevice) != cudaSuccess) return LVBGS_DEVICE_ERROR;
         if (cudaMemcpy(h->d_ripple, h->ripple, sizeof(h->ripple), cudaMemcpyHostToDevice) != cudaSuccess)
             return LVBGS_DEVICE_ERROR;
+        if (cudaMalloc(&h->d_falloff, sizeof(h->falloff)) != cudaSuccess) return LVBGS_OOM;
+        if (cudaMemcpy(h->d_falloff, h->falloff, sizeof(h->falloff), cudaMemcpyHostToDevice) != cudaSuccess)
+            return LVBGS_DEVICE_ERROR;
     }
     const FrameParams F = frame_params(h, t);
-    render_kernel<<<512, 256, 0, (cudaStream_t)stream>>>(F, h->d_tex, h->d_ripple, frame, gt);
+    render_kernel<<<512, 256, 0, (cudaStream_t)stream>>>(F, h->d_tex, h->d_ripple, h->d_falloff, frame, gt);
     return cudaGetLastError() == cudaSuccess ? LVBGS_OK : LVBGS_DEVICE_ERROR;
 }
 

@@ -96,6 +96,60 @@ void oneighbor_pos(int rnd, int use3x3, int x0, int y0, int width, int height, i
 /* raw generator access, for the known-answer test */
 void ophilox_block(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
+/* ---- PAWCS (modules/video/src/BackgroundSubtractorPAWCS.cpp) ---- */
+typedef struct opawcs opawcs_t;
+
+typedef struct {
+    size_t desc_dist_threshold_offset;   /* BGSPAWCS_DEFAULT_DESC_DIST_THRESHOLD_OFFSET = 2 */
+    size_t min_color_dist_threshold;     /* = 20 */
+    size_t max_words;                    /* BGSPAWCS_DEFAULT_MAX_NB_WORDS = 50 (global: max/2) */
+    size_t samples_for_moving_avgs;      /* = 100 */
+    float rel_lbsp_threshold;            /* = 0.333f */
+    size_t lbsp_threshold_offset;        /* = 0 */
+    int default_median_blur_kernel_size; /* = 9 */
+    uint64_t seed;
+} opawcs_params;
+
+typedef struct {
+    uint64_t frame_idx, frames_since_last_reset, model_reset_cooldown, lword_weight_offset;
+    int32_t auto_model_reset_enabled, using_moving_camera, median_blur_kernel_size, n_local_words, n_global_words;
+    float last_nonflat_ratio;
+    uint64_t n_relevant_px, orig_roi_px, ds_roi_px;
+    uint64_t stat_words_scanned, stat_gdict_events, stat_nb_updates;
+} opawcs_scalars;
+
+enum {
+    OPAWCS_MAP_R = 0, OPAWCS_MAP_V, OPAWCS_MAP_T, OPAWCS_MAP_DMIN_LT, OPAWCS_MAP_DMIN_ST, OPAWCS_MAP_RAW_LT,
+    OPAWCS_MAP_RAW_ST, OPAWCS_MAP_FIN_LT, OPAWCS_MAP_FIN_ST,                         /* float [H*W] */
+    OPAWCS_MAP_ILLUM, OPAWCS_MAP_UNSTABLE, OPAWCS_MAP_BLINKS, OPAWCS_MAP_LAST_RAW_FG, OPAWCS_MAP_LAST_FG,
+    OPAWCS_MAP_LAST_FG_DIL, OPAWCS_MAP_LAST_RAW_BLINK, OPAWCS_MAP_ROI,                 /* uint8 [H*W] */
+    OPAWCS_MAP_LAST_COLOR, OPAWCS_MAP_LAST_DESC,                                     /* [H*W*C] u8 / u16 */
+    OPAWCS_MAP_DS_LT, OPAWCS_MAP_DS_ST,                                              /* float [H/8*W/8*C] */
+    OPAWCS_MAP_LUT,                                                                  /* uint8 [256] */
+    OPAWCS_MAP_LW_COLOR, OPAWCS_MAP_LW_DESC,                                         /* [n_rel*L][C] u8 / u16 */
+    OPAWCS_MAP_LW_OCC, OPAWCS_MAP_LW_FIRST, OPAWCS_MAP_LW_LAST,                      /* uint64 [n_rel*L] */
+    OPAWCS_MAP_GW,      /* per pool word: colour u8[3], pad, desc u16[3], bits u8, pad, weight f32, slot i32 */
+    OPAWCS_MAP_GW_MAP,  /* float [G][H/2*W/2], by pool word */
+    OPAWCS_MAP_GLUT,    /* uint8 [H*W][G]: per-pixel global word order (pool indices) */
+    OPAWCS_MAP_COUNT
+};
+
+void opawcs_default_params(opawcs_params* p);
+opawcs_t* opawcs_create(const opawcs_params* p);
+void opawcs_destroy(opawcs_t* o);
+/* BackgroundSubtractorPAWCS::initialize (BackgroundSubtractorPAWCS.cpp:431-557) */
+int opawcs_initialize(opawcs_t* o, const uint8_t* img, int width, int height, int channels, const uint8_t* roi);
+/* BackgroundSubtractorPAWCS::apply (:559-1516) */
+int opawcs_apply(opawcs_t* o, const uint8_t* img, uint8_t* fgmask, double learning_rate_override);
+/* BackgroundSubtractorPAWCS::refreshModel(nBaseOccCount, fOccDecrFrac, bForceFGUpdate) (:107-429) */
+int opawcs_refresh_model(opawcs_t* o, size_t base_occ, float occ_decr_frac, int force_fg);
+int opawcs_get_background(const opawcs_t* o, uint8_t* out);               /* :1518-1545 */
+int opawcs_get_background_descriptors(const opawcs_t* o, uint16_t* out);  /* :1547-1594 */
+void opawcs_set_automatic_model_reset(opawcs_t* o, int enabled);
+int opawcs_export(const opawcs_t* o, int which, void* out, size_t bytes);
+size_t opawcs_export_bytes(const opawcs_t* o, int which);
+void opawcs_get_scalars(const opawcs_t* o, opawcs_scalars* s);
+
 /* CPU baseline: runs n independent SuBSENSE instances (one per stream) over their
  * frame sequences with a pool of n_threads workers (one instance per worker at a
  * time, like lv::WorkerPool in apps/changedet/src/main.cpp:148-154).

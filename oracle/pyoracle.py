@@ -34,6 +34,29 @@ class OScalars(C.Structure):
                 ("stat_samples_evaluated", C.c_uint64), ("stat_sample_writes", C.c_uint64)]
 
 
+PAWCS_MAP_NAMES = ["R", "V", "T", "DMIN_LT", "DMIN_ST", "RAW_LT", "RAW_ST", "FIN_LT", "FIN_ST", "ILLUM", "UNSTABLE",
+                   "BLINKS", "LAST_RAW_FG", "LAST_FG", "LAST_FG_DIL", "LAST_RAW_BLINK", "ROI", "LAST_COLOR",
+                   "LAST_DESC", "DS_LT", "DS_ST", "LUT", "LW_COLOR", "LW_DESC", "LW_OCC", "LW_FIRST", "LW_LAST", "GW",
+                   "GW_MAP", "GLUT"]
+
+
+class PParams(C.Structure):
+    _fields_ = [("desc_dist_threshold_offset", C.c_size_t), ("min_color_dist_threshold", C.c_size_t),
+                ("max_words", C.c_size_t), ("samples_for_moving_avgs", C.c_size_t),
+                ("rel_lbsp_threshold", C.c_float), ("lbsp_threshold_offset", C.c_size_t),
+                ("default_median_blur_kernel_size", C.c_int), ("seed", C.c_uint64)]
+
+
+class PScalars(C.Structure):
+    _fields_ = [("frame_idx", C.c_uint64), ("frames_since_last_reset", C.c_uint64),
+                ("model_reset_cooldown", C.c_uint64), ("lword_weight_offset", C.c_uint64),
+                ("auto_model_reset_enabled", C.c_int32), ("using_moving_camera", C.c_int32),
+                ("median_blur_kernel_size", C.c_int32), ("n_local_words", C.c_int32),
+                ("n_global_words", C.c_int32), ("last_nonflat_ratio", C.c_float), ("n_relevant_px", C.c_uint64),
+                ("orig_roi_px", C.c_uint64), ("ds_roi_px", C.c_uint64), ("stat_words_scanned", C.c_uint64),
+                ("stat_gdict_events", C.c_uint64), ("stat_nb_updates", C.c_uint64)]
+
+
 _lib = None
 
 
@@ -70,6 +93,20 @@ def lib():
         L.orun_streams.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                    C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_uint64), C.c_int,
                                    C.POINTER(C.c_void_p)]
+        L.opawcs_default_params.argtypes = [C.POINTER(PParams)]
+        L.opawcs_create.restype = C.c_void_p
+        L.opawcs_create.argtypes = [C.POINTER(PParams)]
+        L.opawcs_destroy.argtypes = [C.c_void_p]
+        L.opawcs_initialize.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        L.opawcs_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
+        L.opawcs_refresh_model.argtypes = [C.c_void_p, C.c_size_t, C.c_float, C.c_int]
+        L.opawcs_get_background.argtypes = [C.c_void_p, C.c_void_p]
+        L.opawcs_get_background_descriptors.argtypes = [C.c_void_p, C.c_void_p]
+        L.opawcs_set_automatic_model_reset.argtypes = [C.c_void_p, C.c_int]
+        L.opawcs_export.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]
+        L.opawcs_export_bytes.restype = C.c_size_t
+        L.opawcs_export_bytes.argtypes = [C.c_void_p, C.c_int]
+        L.opawcs_get_scalars.argtypes = [C.c_void_p, C.POINTER(PScalars)]
         _lib = L
     return _lib
 
@@ -150,6 +187,86 @@ class OracleSuBSENSE:
         s = OScalars()
         lib().osub_get_scalars(self._o, C.byref(s))
         return {f: getattr(s, f) for f, _ in OScalars._fields_}
+
+
+class OraclePAWCS:
+    """Sequential CPU PAWCS (the checker)."""
+
+    def __init__(self, seed=0, **params):
+        p = PParams()
+        lib().opawcs_default_params(C.byref(p))
+        p.seed = seed
+        for k, v in params.items():
+            setattr(p, k, v)
+        self.params = p
+        self._o = lib().opawcs_create(C.byref(p))
+        if not self._o:
+            raise ValueError("invalid oracle parameters")
+        self.shape = None
+
+    def close(self):
+        if self._o:
+            lib().opawcs_destroy(self._o)
+            self._o = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def initialize(self, img, roi=None):
+        img = np.ascontiguousarray(img, np.uint8)
+        H, W = img.shape[:2]
+        Cc = img.shape[2] if img.ndim == 3 else 1
+        r = None if roi is None else np.ascontiguousarray(roi, np.uint8)
+        st = lib().opawcs_initialize(self._o, img.ctypes.data_as(C.c_void_p), W, H, Cc,
+                                     r.ctypes.data_as(C.c_void_p) if r is not None else None)
+        if st != 0:
+            raise ValueError("oracle initialize failed (%d)" % st)
+        self.shape = (H, W, Cc)
+
+    def apply(self, img, lr=0.0):
+        img = np.ascontiguousarray(img, np.uint8)
+        H, W, _ = self.shape
+        mask = np.empty((H, W), np.uint8)
+        st = lib().opawcs_apply(self._o, img.ctypes.data_as(C.c_void_p), mask.ctypes.data_as(C.c_void_p), float(lr))
+        if st != 0:
+            raise ValueError("oracle apply failed (%d)" % st)
+        return mask
+
+    def refresh_model(self, base_occ, occ_decr_frac, force=False):
+        return lib().opawcs_refresh_model(self._o, int(base_occ), float(occ_decr_frac), 1 if force else 0)
+
+    def set_automatic_model_reset(self, v):
+        lib().opawcs_set_automatic_model_reset(self._o, 1 if v else 0)
+
+    def background(self):
+        H, W, Cc = self.shape
+        out = np.empty((H, W, Cc) if Cc > 1 else (H, W), np.uint8)
+        lib().opawcs_get_background(self._o, out.ctypes.data_as(C.c_void_p))
+        return out
+
+    def background_descriptors(self):
+        H, W, Cc = self.shape
+        out = np.empty((H, W, Cc) if Cc > 1 else (H, W), np.uint16)
+        lib().opawcs_get_background_descriptors(self._o, out.ctypes.data_as(C.c_void_p))
+        return out
+
+    def state_map(self, name):
+        """Raw bytes of one exported state array (layouts in oracle.h, OPAWCS_MAP_*)."""
+        which = PAWCS_MAP_NAMES.index(name)
+        n = lib().opawcs_export_bytes(self._o, which)
+        out = np.empty(n, np.uint8)
+        st = lib().opawcs_export(self._o, which, out.ctypes.data_as(C.c_void_p), n)
+        if st != 0:
+            raise ValueError("oracle export failed (%d)" % st)
+        return out
+
+    def scalars(self):
+        s = PScalars()
+        lib().opawcs_get_scalars(self._o, C.byref(s))
+        return {f: getattr(s, f) for f, _ in PScalars._fields_}
 
 
 def lbsp_compute2(img, abs_threshold=None, rel_threshold=0.333, offset=0, out=None):

@@ -18,6 +18,7 @@
  */
 #include "oracle.h"
 #include "philox.h"
+#include "common.h"
 
 #include <math.h>
 #include <stdint.h>
@@ -40,21 +41,8 @@
 #define LBSPDESC_NONZERO_RATIO_MAX (0.500f)
 #define DEFAULT_FRAME_AREA (320 * 240)
 #define DS_RATIO 8
-#define LBSP_BORDER 2
 
-/* LBSP 16-bit double-cross pattern, LBSP.hpp:297-298 (x, y offsets per bit) */
-static const int k_lbsp_dx[16] = {-2, 2, 0, 0, -2, 2, 2, -2, 0, -1, 0, 1, -1, 1, 1, -1};
-static const int k_lbsp_dy[16] = {0, 0, -2, 2, 2, -2, 2, -2, 1, 0, -1, 0, -1, 1, -1, 1};
 
-/* sampling kernels, opencv.hpp:915-923 (7x7 Gaussian weights, sum 512),
- * :945-949 (3x3 neighbours) and :958-964 (5x5 neighbours); pairs are (dx, dy) */
-static const int k_pat7[7][7] = {
-    {2, 4, 6, 7, 6, 4, 2},     {4, 8, 12, 14, 12, 8, 4}, {6, 12, 21, 25, 21, 12, 6}, {7, 14, 25, 28, 25, 14, 7},
-    {6, 12, 21, 25, 21, 12, 6}, {4, 8, 12, 14, 12, 8, 4}, {2, 4, 6, 7, 6, 4, 2}};
-static const int k_nb3[8][2] = {{-1, 1}, {0, 1}, {1, 1}, {-1, 0}, {1, 0}, {-1, -1}, {0, -1}, {1, -1}};
-static const int k_nb5[24][2] = {{-2, 2}, {-1, 2}, {0, 2},   {1, 2},   {2, 2},  {-2, 1},  {-1, 1},  {0, 1},
-                                 {1, 1},  {2, 1},  {-2, 0},  {-1, 0},  {1, 0},  {2, 0},   {-2, -1}, {-1, -1},
-                                 {0, -1}, {1, -1}, {2, -1},  {-2, -2}, {-1, -2}, {0, -2}, {1, -2},  {2, -2}};
 
 struct osub {
     osub_params p;
@@ -117,56 +105,6 @@ static void reset_draw_counters(osub_t* o) {
     o->cache_valid = 0;
 }
 
-/* saturate_cast<uchar>(float): cvRound (round half to even) then clamp */
-static uint8_t sat_u8f(float v) {
-    long r = lrintf(v);
-    return (uint8_t)(r < 0 ? 0 : r > 255 ? 255 : r);
-}
-static uint8_t sat_u8d(double v) {
-    long r = lrint(v);
-    return (uint8_t)(r < 0 ? 0 : r > 255 ? 255 : r);
-}
-static uint16_t sat_u16f(float v) {
-    long r = lrintf(v);
-    return (uint16_t)(r < 0 ? 0 : r > 65535 ? 65535 : r);
-}
-static unsigned popc16(unsigned v) { return (unsigned)__builtin_popcount(v & 0xffffu); }
-static size_t absdiff(int a, int b) { return (size_t)(a > b ? a - b : b - a); }
-static float minf_std(float a, float b) { return (b < a) ? b : a; } /* std::min */
-static float maxf_std(float a, float b) { return (a < b) ? b : a; } /* std::max */
-
-/* clampImageCoords, opencv.hpp:859-870 */
-static void clamp_coords(int* x, int* y, int border, int W, int H) {
-    if (*x < border) *x = border;
-    else if (*x >= W - border) *x = W - border - 1;
-    if (*y < border) *y = border;
-    else if (*y >= H - border) *y = H - border - 1;
-}
-/* getSamplePosition_7x7_std2 via getSamplePosition<7,7>, opencv.hpp:873-891,909-925 */
-static void sample_pos_7x7(int rnd, int* sx, int* sy, int x0, int y0, int border, int W, int H) {
-    int r = 1 + (rnd % 512), x = 0, y = 0;
-    for (y = 0; y < 7; ++y) {
-        for (x = 0; x < 7; ++x) {
-            r -= k_pat7[y][x];
-            if (r <= 0) goto stop;
-        }
-    }
-stop:
-    x += x0 - 3;
-    y += y0 - 3;
-    clamp_coords(&x, &y, border, W, H);
-    *sx = x;
-    *sy = y;
-}
-/* getNeighborPosition_3x3 / _5x5 via getNeighborPosition<N>, opencv.hpp:928-966 */
-static void neighbor_pos(int rnd, int use3x3, int* nx, int* ny, int x0, int y0, int border, int W, int H) {
-    const int r = use3x3 ? rnd % 8 : rnd % 24;
-    int x = x0 + (use3x3 ? k_nb3[r][0] : k_nb5[r][0]);
-    int y = y0 + (use3x3 ? k_nb3[r][1] : k_nb5[r][1]);
-    clamp_coords(&x, &y, border, W, H);
-    *nx = x;
-    *ny = y;
-}
 
 void osample_pos_7x7(int rnd, int x0, int y0, int W, int H, int* sx, int* sy) {
     sample_pos_7x7(rnd, sx, sy, x0, y0, LBSP_BORDER, W, H);
@@ -175,18 +113,6 @@ void oneighbor_pos(int rnd, int use3x3, int x0, int y0, int W, int H, int* nx, i
     neighbor_pos(rnd, use3x3, nx, ny, x0, y0, LBSP_BORDER, W, H);
 }
 
-/* LBSP::lookup_16bits_dbcross (LBSP.hpp:300-319) for channel c of an interleaved image */
-static void lbsp_lookup(const uint8_t* img, int W, int C, int x, int y, int c, uint8_t vals[16]) {
-    const size_t row = (size_t)W * C;
-    const uint8_t* base = img + (size_t)y * row + (size_t)x * C + c;
-    for (int n = 0; n < 16; ++n) vals[n] = base[(long)row * k_lbsp_dy[n] + (long)C * k_lbsp_dx[n]];
-}
-/* LBSP::computeDescriptor_threshold (LBSP.hpp:193-202): bit n = |val_n - ref| > thr */
-static uint16_t lbsp_threshold(const uint8_t vals[16], uint8_t ref, uint8_t thr) {
-    unsigned d = 0;
-    for (int n = 0; n < 16; ++n) d |= (unsigned)(absdiff(vals[n], ref) > thr) << n;
-    return (uint16_t)d;
-}
 
 void olbsp_compute2(const uint8_t* img, int W, int H, int C, long abs_thr, float rel_thr, size_t offset,
                     uint16_t* desc) {
@@ -246,60 +172,7 @@ void osub_set_automatic_model_reset(osub_t* o, int enabled) { o->auto_reset = en
 
 /* ---- OpenCV operations used by the path (definitions stated; parity vs OpenCV unpinned) ---- */
 
-/* cv::dilate / cv::erode with a (2r+1)x(2r+1) rectangle and the default border value
- * (morphologyDefaultBorderValue: out-of-image pixels never win), i.e. max/min over the
- * window clipped to the image. A 3x3 rectangle applied n times equals one (2n+1)^2
- * rectangle for this border rule. Computed separably (rows, then columns). */
-static void box_minmax(const uint8_t* src, uint8_t* dst, uint8_t* tmp, int W, int H, int r, int is_max) {
-    for (int y = 0; y < H; ++y)
-        for (int x = 0; x < W; ++x) {
-            int v = is_max ? 0 : 255;
-            for (int d = -r; d <= r; ++d) {
-                const int xx = x + d;
-                if (xx < 0 || xx >= W) continue;
-                const int s = src[(size_t)y * W + xx];
-                v = is_max ? (s > v ? s : v) : (s < v ? s : v);
-            }
-            tmp[(size_t)y * W + x] = (uint8_t)v;
-        }
-    for (int y = 0; y < H; ++y)
-        for (int x = 0; x < W; ++x) {
-            int v = is_max ? 0 : 255;
-            for (int d = -r; d <= r; ++d) {
-                const int yy = y + d;
-                if (yy < 0 || yy >= H) continue;
-                const int s = tmp[(size_t)yy * W + x];
-                v = is_max ? (s > v ? s : v) : (s < v ? s : v);
-            }
-            dst[(size_t)y * W + x] = (uint8_t)v;
-        }
-}
 
-/* cv::medianBlur(k) of a 0/255 mask with BORDER_REPLICATE: the median of k*k binary
- * values is 255 iff more than half of them are 255 (k is odd). */
-static void median_binary(const uint8_t* src, uint8_t* dst, uint16_t* colcnt, int W, int H, int k) {
-    const int r = k / 2;
-    for (int y = 0; y < H; ++y)
-        for (int x = 0; x < W; ++x) {
-            int cnt = 0;
-            for (int d = -r; d <= r; ++d) {
-                int yy = y + d;
-                yy = yy < 0 ? 0 : yy >= H ? H - 1 : yy;
-                cnt += src[(size_t)yy * W + x] != 0;
-            }
-            colcnt[(size_t)y * W + x] = (uint16_t)cnt;
-        }
-    for (int y = 0; y < H; ++y)
-        for (int x = 0; x < W; ++x) {
-            int cnt = 0;
-            for (int d = -r; d <= r; ++d) {
-                int xx = x + d;
-                xx = xx < 0 ? 0 : xx >= W ? W - 1 : xx;
-                cnt += colcnt[(size_t)y * W + xx];
-            }
-            dst[(size_t)y * W + x] = (2 * cnt > k * k) ? 255 : 0;
-        }
-}
 
 /* cv::floodFill(img, Point(0,0), 255) (4-connectivity, zero tolerances) followed by
  * cv::bitwise_not: the result is 255 exactly at the pixels that hold 0 and are not
@@ -329,45 +202,8 @@ static void flood_holes(osub_t* o, const uint8_t* pre, uint8_t* holes) {
     for (size_t i = 0; i < o->npx; ++i) holes[i] = (pre[i] == 0 && !o->visited[i]) ? 255 : 0;
 }
 
-/* cv::addWeighted(A (CV_32F), alpha, M (CV_8U), beta, 0, A, CV_32F): M is converted to
- * float and A = A*(float)alpha + M*(float)beta + 0 in float, no fused multiply-add. */
-static void add_weighted_mask(float* a, const uint8_t* m, size_t n, double alpha, double beta) {
-    const float fa = (float)alpha, fb = (float)beta;
-    for (size_t i = 0; i < n; ++i) {
-        const float t1 = a[i] * fa;
-        const float t2 = (float)m[i] * fb;
-        a[i] = (t1 + t2) + 0.0f;
-    }
-}
 
-/* cv::resize(src, dst, (W/8, H/8), INTER_AREA) when the scale is an exact integer
- * (OpenCV's "area fast" case): each output is the mean of its 8x8 block, computed as
- * cvRound(sum * (1.f/64)) (round half to even). Returns 0 when the scale is not integral. */
-static int resize_area_div8(const uint8_t* src, int W, int H, int C, uint8_t* dst, int dw, int dh) {
-    if (dw <= 0 || dh <= 0 || W % dw != 0 || H % dh != 0) return 0;
-    const int sx = W / dw, sy = H / dh;
-    const float scale = 1.f / (float)(sx * sy);
-    for (int y = 0; y < dh; ++y)
-        for (int x = 0; x < dw; ++x)
-            for (int c = 0; c < C; ++c) {
-                int sum = 0;
-                for (int yy = 0; yy < sy; ++yy)
-                    for (int xx = 0; xx < sx; ++xx) sum += src[((size_t)(y * sy + yy) * W + (x * sx + xx)) * C + c];
-                dst[((size_t)y * dw + x) * C + c] = sat_u8f((float)sum * scale);
-            }
-    return 1;
-}
 
-/* cv::accumulateWeighted(src, dst, alpha): dst = src*a + dst*(1-a) with a = (float)alpha,
- * in float, no fused multiply-add. */
-static void accumulate_weighted(const uint8_t* src, float* dst, size_t n, double alpha) {
-    const float a = (float)alpha, b = 1.0f - a;
-    for (size_t i = 0; i < n; ++i) {
-        const float t1 = (float)src[i] * a;
-        const float t2 = dst[i] * b;
-        dst[i] = t1 + t2;
-    }
-}
 
 /* ---- initialize ---- */
 
