@@ -203,6 +203,43 @@ lvbgs_status lvbgs_get_scalars(lvbgs_handle h, lvbgs_scalars* out);
 lvbgs_status lvbgs_debug_set_timing(lvbgs_handle h, int batched, int n_ticks);
 int lvbgs_debug_tick_profile(lvbgs_handle h, int batched, double* out_ms, int max_n);
 
+/* ---- PAWCS (BackgroundSubtractorPAWCS, modules/video/src/BackgroundSubtractorPAWCS.cpp) ----
+ * A handle created with LVBGS_ALGO_PAWCS runs PAWCS on single-channel frames (three-channel frames:
+ * LVBGS_UNSUPPORTED). lvbgs_params maps onto the constructor (BackgroundSubtractorPAWCS.hpp:47-51):
+ * desc_dist_threshold_offset (2), min_color_dist_threshold (20), bg_samples = nMaxNbWords (50; at most
+ * 51), samples_for_moving_avgs (100), rel_lbsp_threshold (0.333); required_bg_samples is unused.
+ * initialize/apply/get_background/get_background_descriptors/get_roi work as for SuBSENSE; batched
+ * steps and spilling are SuBSENSE-only for now. */
+
+/* refreshModel(nBaseOccCount, fOccDecrFrac, bForceFGUpdate) (BackgroundSubtractorPAWCS.cpp:107-429) */
+lvbgs_status lvbgs_pawcs_refresh_model(lvbgs_handle h, size_t base_occ, float occ_decr_frac, int force_fg_update);
+
+typedef struct {
+    uint64_t frame_idx, frames_since_last_reset, model_reset_cooldown, lword_weight_offset;
+    int32_t auto_model_reset_enabled, using_moving_camera, median_blur_kernel_size, n_local_words, n_global_words;
+    float last_nonflat_ratio;
+    uint64_t n_relevant_px, orig_roi_px, ds_roi_px;
+    uint64_t fixed_point_rounds; /* local-pass rounds of the last frame step */
+} lvbgs_pawcs_scalars;
+lvbgs_status lvbgs_pawcs_get_scalars(lvbgs_handle h, lvbgs_pawcs_scalars* out);
+
+/* model state export for parity checks (layouts: float [H*W] maps; uint8 [H*W] masks; LW_* planes
+ * [n_relevant_px * local words], ROI pixels in raster order, slot-minor, OCC/FIRST/LAST as uint64; GW:
+ * 20 bytes per pool word (colour u8, 3 pad, descriptor u16, 4 pad, bits u8, pad, weight f32, slot i32);
+ * GW_MAP float [G][H/2*W/2]; GLUT uint8 [H*W][G]) */
+enum {
+    LVBGS_PAWCS_MAP_R = 0, LVBGS_PAWCS_MAP_V, LVBGS_PAWCS_MAP_T, LVBGS_PAWCS_MAP_DMIN_LT, LVBGS_PAWCS_MAP_DMIN_ST,
+    LVBGS_PAWCS_MAP_RAW_LT, LVBGS_PAWCS_MAP_RAW_ST, LVBGS_PAWCS_MAP_FIN_LT, LVBGS_PAWCS_MAP_FIN_ST,
+    LVBGS_PAWCS_MAP_ILLUM, LVBGS_PAWCS_MAP_UNSTABLE, LVBGS_PAWCS_MAP_BLINKS, LVBGS_PAWCS_MAP_LAST_RAW_FG,
+    LVBGS_PAWCS_MAP_LAST_FG, LVBGS_PAWCS_MAP_LAST_FG_DIL, LVBGS_PAWCS_MAP_LAST_RAW_BLINK, LVBGS_PAWCS_MAP_ROI,
+    LVBGS_PAWCS_MAP_LAST_COLOR, LVBGS_PAWCS_MAP_LAST_DESC, LVBGS_PAWCS_MAP_DS_LT, LVBGS_PAWCS_MAP_DS_ST,
+    LVBGS_PAWCS_MAP_LUT, LVBGS_PAWCS_MAP_LW_COLOR, LVBGS_PAWCS_MAP_LW_DESC, LVBGS_PAWCS_MAP_LW_OCC,
+    LVBGS_PAWCS_MAP_LW_FIRST, LVBGS_PAWCS_MAP_LW_LAST, LVBGS_PAWCS_MAP_GW, LVBGS_PAWCS_MAP_GW_MAP,
+    LVBGS_PAWCS_MAP_GLUT
+};
+size_t lvbgs_pawcs_debug_export_bytes(lvbgs_handle h, int which);
+lvbgs_status lvbgs_pawcs_debug_export(lvbgs_handle h, int which, void* out, size_t bytes);
+
 #ifdef __cplusplus
 }
 #endif

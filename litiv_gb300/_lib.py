@@ -95,6 +95,21 @@ class SimResult(C.Structure):
                 ("peak_device_bytes", C.c_size_t), ("status", C.c_int)]
 
 
+class PawcsScalars(C.Structure):
+    _fields_ = [("frame_idx", C.c_uint64), ("frames_since_last_reset", C.c_uint64),
+                ("model_reset_cooldown", C.c_uint64), ("lword_weight_offset", C.c_uint64),
+                ("auto_model_reset_enabled", C.c_int32), ("using_moving_camera", C.c_int32),
+                ("median_blur_kernel_size", C.c_int32), ("n_local_words", C.c_int32),
+                ("n_global_words", C.c_int32), ("last_nonflat_ratio", C.c_float), ("n_relevant_px", C.c_uint64),
+                ("orig_roi_px", C.c_uint64), ("ds_roi_px", C.c_uint64), ("fixed_point_rounds", C.c_uint64)]
+
+
+# PAWCS state maps (LVBGS_PAWCS_MAP_*), same order and layouts as the oracle's OPAWCS_MAP_*
+PAWCS_MAP_NAMES = ["R", "V", "T", "DMIN_LT", "DMIN_ST", "RAW_LT", "RAW_ST", "FIN_LT", "FIN_ST", "ILLUM", "UNSTABLE",
+                   "BLINKS", "LAST_RAW_FG", "LAST_FG", "LAST_FG_DIL", "LAST_RAW_BLINK", "ROI", "LAST_COLOR",
+                   "LAST_DESC", "DS_LT", "DS_ST", "LUT", "LW_COLOR", "LW_DESC", "LW_OCC", "LW_FIRST", "LW_LAST", "GW",
+                   "GW_MAP", "GLUT"]
+
 # exported symbol -> (restype, argtypes)
 SIGNATURES = {
     "lvbgs_default_params": (C.c_int, [C.c_int, C.POINTER(LvbgsParams)]),
@@ -150,6 +165,10 @@ SIGNATURES = {
                                     C.POINTER(C.c_double), C.c_int, C.c_double, C.POINTER(C.c_int)]),
     "lvserve_default_sim_config": (C.c_int, [C.POINTER(SimConfig)]),
     "lvserve_simulate": (C.c_int, [C.POINTER(ServeConfig), C.POINTER(SimConfig), C.POINTER(SimResult)]),
+    "lvbgs_pawcs_refresh_model": (C.c_int, [C.c_void_p, C.c_size_t, C.c_float, C.c_int]),
+    "lvbgs_pawcs_get_scalars": (C.c_int, [C.c_void_p, C.POINTER(PawcsScalars)]),
+    "lvbgs_pawcs_debug_export_bytes": (C.c_size_t, [C.c_void_p, C.c_int]),
+    "lvbgs_pawcs_debug_export": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]),
     "lvsynth_preset": (C.c_int, [C.c_int, C.c_int, C.c_uint64, C.POINTER(SynthConfig)]),
     "lvsynth_create": (C.c_int, [C.POINTER(SynthConfig), C.POINTER(C.c_void_p)]),
     "lvsynth_destroy": (None, [C.c_void_p]),

@@ -175,6 +175,74 @@ class BackgroundSubtractorSuBSENSE:
         return self._shape
 
 
+class BackgroundSubtractorPAWCS:
+    """PAWCS on the GPU, single-channel frames (the lv::CUDA specialisation the reference leaves missing);
+    BackgroundSubtractorPAWCS.hpp:47-51 for the constructor parameters."""
+
+    def __init__(self, nDescDistThresholdOffset=2, nMinColorDistThreshold=20, nMaxNbWords=50,
+                 nSamplesForMovingAvgs=100, fRelLBSPThreshold=0.333, seed=0, device_id=0, nLBSPThresholdOffset=0,
+                 nDefaultMedianBlurKernelSize=9):
+        lib = L.lib()
+        p = L.LvbgsParams()
+        _check(lib.lvbgs_default_params(L.ALGO_PAWCS, C.byref(p)))
+        p.desc_dist_threshold_offset = nDescDistThresholdOffset
+        p.min_color_dist_threshold = nMinColorDistThreshold
+        p.bg_samples = nMaxNbWords
+        p.samples_for_moving_avgs = nSamplesForMovingAvgs
+        p.rel_lbsp_threshold = fRelLBSPThreshold
+        p.lbsp_threshold_offset = nLBSPThresholdOffset
+        p.default_median_blur_kernel_size = nDefaultMedianBlurKernelSize
+        p.seed = seed
+        p.device_id = device_id
+        self.params = p
+        h = C.c_void_p()
+        _check(lib.lvbgs_create(L.ALGO_PAWCS, C.byref(p), C.byref(h)))
+        self._h = h
+        self._shape = None
+
+    def close(self):
+        if self._h:
+            L.lib().lvbgs_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    initialize = BackgroundSubtractorSuBSENSE.initialize
+    apply = BackgroundSubtractorSuBSENSE.apply
+    getBackgroundImage = BackgroundSubtractorSuBSENSE.getBackgroundImage
+    getBackgroundDescriptorsImage = BackgroundSubtractorSuBSENSE.getBackgroundDescriptorsImage
+    setAutomaticModelReset = BackgroundSubtractorSuBSENSE.setAutomaticModelReset
+    getDefaultLearningRate = BackgroundSubtractorSuBSENSE.getDefaultLearningRate
+    getROICopy = BackgroundSubtractorSuBSENSE.getROICopy
+    _need_init = BackgroundSubtractorSuBSENSE._need_init
+
+    def refreshModel(self, nBaseOccCount, fOccDecrFrac, bForceFGUpdate=False):
+        _check(L.lib().lvbgs_pawcs_refresh_model(self._h, int(nBaseOccCount), float(fOccDecrFrac),
+                                                 1 if bForceFGUpdate else 0), self._h)
+
+    def state_map(self, name):
+        """Raw bytes of one model array (include/lvbgs.h, LVBGS_PAWCS_MAP_*; the oracle's layouts)."""
+        self._need_init()
+        which = L.PAWCS_MAP_NAMES.index(name)
+        n = L.lib().lvbgs_pawcs_debug_export_bytes(self._h, which)
+        out = np.empty(n, np.uint8)
+        _check(L.lib().lvbgs_pawcs_debug_export(self._h, which, out.ctypes.data_as(C.c_void_p), n), self._h)
+        return out
+
+    def scalars(self):
+        s = L.PawcsScalars()
+        _check(L.lib().lvbgs_pawcs_get_scalars(self._h, C.byref(s)), self._h)
+        return {f: getattr(s, f) for f, _ in L.PawcsScalars._fields_}
+
+
 def map_view(name, raw, W, H, Cc, N):
     """Interprets raw map bytes (reference layout) as a typed numpy array."""
     if name in ("R", "V", "T", "DLAST", "DMIN_LT", "DMIN_ST", "RAW_LT", "RAW_ST", "FIN_LT", "FIN_ST"):

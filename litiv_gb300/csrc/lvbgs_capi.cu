@@ -13,6 +13,7 @@
 
 #include "../../include/lvbgs.h"
 #include "lvbgs_internal.h"
+#include "pawcs_internal.h"
 
 namespace lvbgs {
 extern "C" __global__ void lvbgs_k_eval(TickParams P);
@@ -36,6 +37,32 @@ extern "C" __global__ void lvbgs_pack_samples(StreamDev S, const uint8_t* col, c
 extern "C" __global__ void lvbgs_init_tables();
 extern "C" __global__ void lvbgs_lbsp_dense(const uint8_t* img, int W, int H, int C, int absThr, float rel,
                                             unsigned int off, uint16_t* desc);
+// PAWCS (pawcs_kernels.cu)
+extern "C" __global__ void pw_k_local(PwParams P);
+extern "C" __global__ void pw_k_illum(PwParams P);
+extern "C" __global__ void pw_k_items(PwParams P);
+extern "C" __global__ void pw_k_gscan(PwParams P);
+extern "C" __global__ void pw_k_cells(PwParams P, int final);
+extern "C" __global__ void pw_k_nbr(PwParams P);
+extern "C" __global__ void pw_k_replace(PwParams P);
+extern "C" __global__ void pw_k_dirty(PwParams P);
+extern "C" __global__ void pw_k_commit(PwParams P);
+extern "C" __global__ void pw_k_weights(PwParams P);
+extern "C" __global__ void pw_k_gw_recalc(PwParams P);
+extern "C" __global__ void pw_k_gw_decay(PwParams P, double* rowsum);
+extern "C" __global__ void pw_k_gw_blur(PwParams P, const double* rowsum);
+extern "C" __global__ void pw_k_gw_sort(PwParams P);
+extern "C" __global__ void pw_k_lut_sort(PwParams P, int mode);
+extern "C" __global__ void pw_k_blink_close(PwParams P);
+extern "C" __global__ void pw_k_epilogue(PwParams P);
+extern "C" __global__ void pw_k_close(PwParams P);
+extern "C" __global__ void pw_k_refresh_local(PawcsDev S, uint32_t t, int buf, int baseOcc, float decr, int force,
+                                              int onlyPending, int useDil);
+extern "C" __global__ void pw_k_refresh_global(PawcsDev S, uint32_t t, int buf, int force, int onlyPending, int useDil);
+extern "C" __global__ void pw_k_reset_T(PawcsDev S, int buf);
+extern "C" __global__ void pw_k_init(PawcsDev S);
+extern "C" __global__ void pw_k_init_last(PawcsDev S, const uint8_t* img);
+extern "C" __global__ void pw_k_background(PawcsDev S, int buf, uint8_t* outCol, uint16_t* outDesc);
 }  // namespace lvbgs
 
 using namespace lvbgs;
@@ -121,6 +148,17 @@ struct lvbgs_ctx {
     cudaStream_t stream = nullptr;
     Workspace ws;       // single-stream launches
     Workspace batchWs;  // batched launches led by this handle
+    // PAWCS (algo == LVBGS_ALGO_PAWCS): device descriptor, host mirrors and launch scratch
+    PawcsDev pd{};
+    PawcsDev* d_pd = nullptr;
+    StreamDev* d_sd = nullptr;
+    TickWork* d_work = nullptr;
+    unsigned int* d_flags = nullptr;
+    double* d_rowsum = nullptr;
+    unsigned int* h_flags = nullptr;  // pinned
+    unsigned long long pw_frames = 0;
+    unsigned long long pw_offset = 1000;
+    int pw_rounds_last = 0;
 };
 
 namespace {
@@ -444,9 +482,375 @@ lvbgs_status lvbgs::report_error(lvbgs_status st, const char* msg) { return fail
 
 extern "C" {
 
+// ==========================================================================================
+// PAWCS (one channel): device layout, initialization and the frame step
+// ==========================================================================================
+namespace {
+
+enum {
+    PL_CTL = 0, PL_PCTL, PL_FM, PL_WCOLOR, PL_WDESC, PL_WOCC, PL_WFIRST, PL_WLAST, PL_ILLUM, PL_UNST, PL_ROI,
+    PL_BLINKS, PL_LASTRAWFG, PL_LASTFG, PL_DILINV, PL_LASTRAWBLINK, PL_LASTCOL, PL_LASTDESC, PL_KCTR, PL_GLUT,
+    PL_GMAP, PL_DSLT, PL_DSST, PL_DSROI,
+    // scratch (not part of the model)
+    PL_PREFLOOD, PL_COMBINED, PL_LABEL, PL_INTENT, PL_DESCT, PL_REC, PL_OUT, PL_REPB, PL_REPA, PL_UFINAL, PL_CRIT,
+    PL_GITEM, PL_CONTRIB, PL_DSFRAME, PL_FRAME, PL_MASK, PL_ROWSUM, PL_WORK, PL_FLAGS, PL_PDEV, PL_SDEV, PL_COUNT
+};
+struct PwLayout {
+    size_t off[PL_COUNT];
+    size_t persist, total;
+};
+PwLayout pw_layout(int W, int H, int L, int G) {
+    const size_t npx = (size_t)W * H, gmap = (size_t)(W / 2) * (H / 2), nds = (size_t)(W / 8) * (H / 8);
+    size_t sz[PL_COUNT];
+    sz[PL_CTL] = sizeof(StreamCtl);
+    sz[PL_PCTL] = sizeof(PawcsCtl);
+    sz[PL_FM] = 2 * kNumFloatMaps * npx * 4;
+    sz[PL_WCOLOR] = 2 * (size_t)L * npx;
+    sz[PL_WDESC] = 2 * (size_t)L * npx * 2;
+    sz[PL_WOCC] = sz[PL_WFIRST] = sz[PL_WLAST] = 2 * (size_t)L * npx * 4;
+    sz[PL_ILLUM] = sz[PL_UNST] = sz[PL_ROI] = sz[PL_BLINKS] = sz[PL_LASTRAWFG] = sz[PL_LASTFG] = sz[PL_DILINV] =
+        sz[PL_LASTRAWBLINK] = sz[PL_LASTCOL] = npx;
+    sz[PL_LASTDESC] = sz[PL_KCTR] = npx * 2;
+    sz[PL_GLUT] = npx * 16;
+    sz[PL_GMAP] = (size_t)G * std::max<size_t>(gmap, 1) * 4;
+    sz[PL_DSLT] = sz[PL_DSST] = std::max<size_t>(nds, 1) * 4;
+    sz[PL_DSROI] = std::max<size_t>(nds, 1);
+    sz[PL_PREFLOOD] = sz[PL_COMBINED] = npx;
+    sz[PL_LABEL] = sz[PL_INTENT] = npx * 4;
+    sz[PL_DESCT] = npx * 2;
+    sz[PL_REC] = npx * sizeof(PwRec);
+    sz[PL_OUT] = npx * sizeof(PwOut);
+    sz[PL_REPB] = sz[PL_REPA] = npx * 4;
+    sz[PL_UFINAL] = npx;
+    sz[PL_CRIT] = (size_t)H * ((W + 31) / 32) * 4;
+    sz[PL_GITEM] = npx * 4;
+    sz[PL_CONTRIB] = npx * 4;
+    sz[PL_DSFRAME] = std::max<size_t>(nds, 1);
+    sz[PL_FRAME] = npx;
+    sz[PL_MASK] = npx;
+    sz[PL_ROWSUM] = (size_t)kPwMaxGlobal * std::max<size_t>(gmap, 1) * 8;
+    sz[PL_WORK] = sizeof(TickWork);
+    sz[PL_FLAGS] = 64;
+    sz[PL_PDEV] = sizeof(PawcsDev);
+    sz[PL_SDEV] = sizeof(StreamDev);
+    PwLayout Lo;
+    size_t o = 0;
+    for (int i = 0; i < PL_COUNT; ++i) {
+        if (i == PL_PREFLOOD) Lo.persist = o;
+        Lo.off[i] = o;
+        o += align256(sz[i]);
+    }
+    Lo.total = o;
+    return Lo;
+}
+
+// resolution-dependent parameters of BackgroundSubtractorPAWCS::initialize (:446-466)
+struct PwGeom {
+    int L, G, median_k, big;
+};
+PwGeom pw_geometry(const lvbgs_params& prm, size_t npx, size_t orig, int C) {
+    PwGeom g;
+    size_t L = prm.bg_samples, maxG = prm.bg_samples / 2, G;
+    const int k = prm.default_median_blur_kernel_size;
+    int raw;
+    if (orig >= npx / 2 && (int)npx >= 320 * 240) {
+        const float f = (float)npx / (320 * 240);
+        raw = std::min((int)std::floor(0.5f + f) + k, k + 4);
+        G = maxG;
+        g.big = 1;
+    } else {
+        const float f = (float)orig / (320 * 240);
+        raw = std::min((int)std::floor(0.5f + (float)k * f * 2) + (k - 4), k);
+        const size_t gg = (size_t)std::pow((double)((float)maxG * f), 2) + 1;
+        G = std::min(gg, maxG);
+        g.big = 0;
+    }
+    g.median_k = (raw % 2) ? raw : raw - 1;
+    if (C == 1) {
+        L = std::max<size_t>(L / 2, 1);
+        G = std::max<size_t>(G / 2, 1);
+    }
+    g.L = (int)L;
+    g.G = (int)G;
+    return g;
+}
+
+void pw_fill(lvbgs_ctx* h, const PwLayout& Lo, int L, int G) {
+    uint8_t* b = h->dmem;
+    StreamDev& S = h->sd;
+    std::memset(&S, 0, sizeof(S));
+    S.ctl = (StreamCtl*)(b + Lo.off[PL_CTL]);
+    S.fm = (float*)(b + Lo.off[PL_FM]);
+    S.roi = b + Lo.off[PL_ROI];
+    S.blinks = b + Lo.off[PL_BLINKS];
+    S.lastRawFG = b + Lo.off[PL_LASTRAWFG];
+    S.lastFG = b + Lo.off[PL_LASTFG];
+    S.dilInv = b + Lo.off[PL_DILINV];
+    S.lastRawBlink = b + Lo.off[PL_LASTRAWBLINK];
+    S.lastCol = b + Lo.off[PL_LASTCOL];
+    S.lastDesc = (uint16_t*)(b + Lo.off[PL_LASTDESC]);
+    S.kctr = (uint16_t*)(b + Lo.off[PL_KCTR]);
+    S.dsLT = (float*)(b + Lo.off[PL_DSLT]);
+    S.dsST = (float*)(b + Lo.off[PL_DSST]);
+    S.preflood = b + Lo.off[PL_PREFLOOD];
+    S.combined = b + Lo.off[PL_COMBINED];
+    S.label = (int*)(b + Lo.off[PL_LABEL]);
+    S.intent = (uint32_t*)(b + Lo.off[PL_INTENT]);
+    h->d_frame = b + Lo.off[PL_FRAME];
+    h->d_mask = b + Lo.off[PL_MASK];
+    fill_geometry(h);
+    PawcsDev& D = h->pd;
+    D.pc = (PawcsCtl*)(b + Lo.off[PL_PCTL]);
+    D.L = L;
+    D.G = G;
+    D.gwW = h->W / 2;
+    D.gwH = h->H / 2;
+    D.minColor = (unsigned)h->prm.min_color_dist_threshold;
+    D.descOff = (unsigned)h->prm.desc_dist_threshold_offset;
+    D.nmv = (unsigned)h->prm.samples_for_moving_avgs;
+    D.relThr = h->prm.rel_lbsp_threshold;
+    D.lbspOff = (unsigned)h->prm.lbsp_threshold_offset;
+    D.wColor = b + Lo.off[PL_WCOLOR];
+    D.wDesc = (uint16_t*)(b + Lo.off[PL_WDESC]);
+    D.wOcc = (uint32_t*)(b + Lo.off[PL_WOCC]);
+    D.wFirst = (uint32_t*)(b + Lo.off[PL_WFIRST]);
+    D.wLast = (uint32_t*)(b + Lo.off[PL_WLAST]);
+    D.illum = b + Lo.off[PL_ILLUM];
+    D.unstable = b + Lo.off[PL_UNST];
+    D.glut = b + Lo.off[PL_GLUT];
+    D.gmap = (float*)(b + Lo.off[PL_GMAP]);
+    D.descT = (uint16_t*)(b + Lo.off[PL_DESCT]);
+    D.rec = (PwRec*)(b + Lo.off[PL_REC]);
+    D.out = (PwOut*)(b + Lo.off[PL_OUT]);
+    D.repBefore = (uint32_t*)(b + Lo.off[PL_REPB]);
+    D.repAfter = (uint32_t*)(b + Lo.off[PL_REPA]);
+    D.uFinal = b + Lo.off[PL_UFINAL];
+    D.critBits = (uint32_t*)(b + Lo.off[PL_CRIT]);
+    D.gitem = (uint32_t*)(b + Lo.off[PL_GITEM]);
+    D.contrib = (float*)(b + Lo.off[PL_CONTRIB]);
+    D.dsRoi = b + Lo.off[PL_DSROI];
+    D.dsFrame = b + Lo.off[PL_DSFRAME];
+    h->d_rowsum = (double*)(b + Lo.off[PL_ROWSUM]);
+    h->d_work = (TickWork*)(b + Lo.off[PL_WORK]);
+    h->d_flags = (unsigned int*)(b + Lo.off[PL_FLAGS]);
+    h->d_pd = (PawcsDev*)(b + Lo.off[PL_PDEV]);
+    h->d_sd = (StreamDev*)(b + Lo.off[PL_SDEV]);
+}
+
+PwParams pw_params(lvbgs_ctx* h, double lr) {
+    PwParams P;
+    P.streams = h->d_pd;
+    P.nStreams = 1;
+    P.totalTiles = h->sd.nTiles;
+    P.totalRows = h->H;
+    P.totalCells = h->pd.gwW * h->pd.gwH;
+    P.round = 0;
+    P.lr = lr;
+    P.flags = h->d_flags;
+    return P;
+}
+
+lvbgs_status pw_upload_desc(lvbgs_ctx* h, cudaStream_t st) {
+    h->pd.sd = h->sd;
+    LV_CUDA(h, cudaMemcpyAsync(h->d_pd, &h->pd, sizeof(PawcsDev), cudaMemcpyHostToDevice, st), "descriptor upload");
+    LV_CUDA(h, cudaMemcpyAsync(h->d_sd, &h->sd, sizeof(StreamDev), cudaMemcpyHostToDevice, st), "descriptor upload");
+    return LVBGS_OK;
+}
+
+// refreshModel(nBaseOccCount, fOccDecrFrac, bForceFGUpdate) of the dictionaries in buffer buf at frame t
+lvbgs_status pw_refresh(lvbgs_ctx* h, uint32_t t, int buf, int baseOcc, float decr, int force, int onlyPending,
+                        int useDil, cudaStream_t st) {
+    const int npx = (int)h->npx;
+    pw_k_refresh_local<<<(npx + 127) / 128, 128, 0, st>>>(h->pd, t, buf, baseOcc, decr, force, onlyPending, useDil);
+    pw_k_refresh_global<<<1, 1, 0, st>>>(h->pd, t, buf, force, onlyPending, useDil);
+    PwParams P = pw_params(h, 0.0);
+    pw_k_lut_sort<<<h->sd.nTiles, kThreads, 0, st>>>(P, onlyPending ? 2 : 1);
+    LV_CUDA(h, cudaGetLastError(), "refresh kernel launch");
+    return LVBGS_OK;
+}
+
+lvbgs_status pw_initialize(lvbgs_ctx* h, const uint8_t* img, int W, int H, int C, size_t stride,
+                           const std::vector<uint8_t>& newroi, size_t orig, size_t fin) {
+    if (C != 1) return fail(h, LVBGS_UNSUPPORTED, "PAWCS runs on single-channel frames in this implementation");
+    const size_t npx = (size_t)W * H;
+    const PwGeom g = pw_geometry(h->prm, npx, orig, C);
+    if (g.L > kPwMaxLocal || g.G > kPwMaxGlobal) return fail(h, LVBGS_UNSUPPORTED, "word counts above the supported maximum");
+    if (g.median_k > 13) return fail(h, LVBGS_UNSUPPORTED, "median kernel sizes above 13 are not supported");
+    const int dsW = W / 8, dsH = H / 8;
+    if (dsW <= 0 || dsH <= 0 || W % dsW != 0 || H % dsH != 0)
+        return fail(h, LVBGS_UNSUPPORTED,
+                    "frame-level analysis needs an integral 1/8 down-sampling (INTER_AREA fast path): width and height must be multiples of width/8 and height/8");
+    // down-sampled ROI (INTER_AREA of the validated ROI, :445) and its pixel count
+    const int sx = W / dsW, sy = H / dsH;
+    std::vector<uint8_t> dsRoi((size_t)dsW * dsH);
+    size_t dsCount = 0;
+    for (int y = 0; y < dsH; ++y)
+        for (int x = 0; x < dsW; ++x) {
+            int sum = 0;
+            for (int yy = 0; yy < sy; ++yy)
+                for (int xx = 0; xx < sx; ++xx) sum += newroi[(size_t)(y * sy + yy) * W + x * sx + xx];
+            uint8_t v = sat_round_u8((float)sum * (1.f / (float)(sx * sy)));
+            if (g.big) v |= 127;
+            dsRoi[(size_t)y * dsW + x] = v;
+            dsCount += v != 0;
+        }
+    StreamCtl ctl;
+    std::memset(&ctl, 0, sizeof(ctl));
+    ctl.auto_reset = 1;  // IIBackgroundSubtractor's default (BackgroundSubtractionUtils.cpp:67)
+    ctl.median_k = g.median_k;
+    const float rel = h->prm.rel_lbsp_threshold;
+    for (int t = 0; t <= 255; ++t)
+        ctl.lut[t] = sat_round_u8(((float)t * rel + (float)h->prm.lbsp_threshold_offset) / 3);
+    ctl.n_rel = fin;
+    ctl.orig_roi = orig;
+    {
+        // factors of frame 1 (bootstrapping: N/2 and N/8 frames)
+        const unsigned long long nlt = h->prm.samples_for_moving_avgs / 2, nst = nlt / 4;
+        ctl.fLT = 1.0f / (float)(1ull < nlt ? 1ull : nlt);
+        ctl.fST = 1.0f / (float)(1ull < nst ? 1ull : nst);
+        ctl.bLT = (float)((1.0 / 255) * (double)ctl.fLT);
+        ctl.bST = (float)((1.0 / 255) * (double)ctl.fST);
+    }
+    PawcsCtl pc;
+    std::memset(&pc, 0, sizeof(pc));
+    pc.lword_offset = 1000;
+    pc.L = g.L;
+    pc.G = g.G;
+    pc.ds_roi_count = dsCount;
+    for (int i = 0; i < kPwMaxGlobal; ++i) pc.gdict[i] = -1;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaFree(h->dmem);
+    h->dmem = nullptr;
+    h->initialized = false;
+    h->spilled = false;
+    const PwLayout Lo = pw_layout(W, H, g.L, g.G);
+    LV_CUDA(h, cudaMalloc(&h->dmem, Lo.total), "model allocation");
+    if (!h->h_flags) LV_CUDA(h, cudaHostAlloc((void**)&h->h_flags, 64, cudaHostAllocDefault), "pinned allocation");
+    h->persistBytes = Lo.persist;
+    h->totalBytes = Lo.total;
+    h->W = W;
+    h->H = H;
+    h->C = C;
+    h->npx = npx;
+    h->roi = newroi;
+    h->n_rel = fin;
+    h->orig_roi = orig;
+    h->pw_frames = 0;
+    h->pw_offset = 1000;
+    pw_fill(h, Lo, g.L, g.G);
+    cudaStream_t st = h->stream;
+    LV_CUDA(h, cudaMemsetAsync(h->dmem, 0, Lo.total, st), "model reset");
+    LV_CUDA(h, cudaMemcpyAsync(h->sd.ctl, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, st), "control upload");
+    LV_CUDA(h, cudaMemcpyAsync(h->pd.pc, &pc, sizeof(pc), cudaMemcpyHostToDevice, st), "control upload");
+    LV_CUDA(h, cudaMemcpyAsync(h->sd.roi, h->roi.data(), npx, cudaMemcpyHostToDevice, st), "roi upload");
+    LV_CUDA(h, cudaMemcpyAsync(h->pd.dsRoi, dsRoi.data(), dsRoi.size(), cudaMemcpyHostToDevice, st), "roi upload");
+    const uint8_t* dimg = nullptr;
+    lvbgs_status s = stage_frame(h, img, stride, st, &dimg);
+    if (s != LVBGS_OK) return s;
+    if ((s = pw_upload_desc(h, st)) != LVBGS_OK) return s;
+    pw_k_init<<<1024, 256, 0, st>>>(h->pd);
+    pw_k_init_last<<<1024, 256, 0, st>>>(h->pd, dimg);
+    LV_CUDA(h, cudaGetLastError(), "init kernel launch");
+    // refreshModel(1, 0) at frame 0 (:555)
+    if ((s = pw_refresh(h, 0u, 0, 1, 0.0f, 0, 0, 0, st)) != LVBGS_OK) return s;
+    LV_CUDA(h, cudaStreamSynchronize(st), "initialization");
+    h->initialized = true;
+    return LVBGS_OK;
+}
+
+// one PAWCS frame step: local passes to the raster-order fixed point, then commit, global words,
+// post-processing and the frame level
+lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* mask, double lr, cudaStream_t st) {
+    const uint8_t* dimg = nullptr;
+    lvbgs_status s = stage_frame(h, img, stride, st, &dimg);
+    if (s != LVBGS_OK) return s;
+    const bool devMask = mask && is_device_ptr(mask);
+    h->sd.frame = dimg;
+    h->sd.maskOut = devMask ? mask : h->d_mask;
+    if ((s = pw_upload_desc(h, st)) != LVBGS_OK) return s;
+    PwParams P = pw_params(h, lr);
+    const dim3 blk(kThreads);
+    const int tiles = h->sd.nTiles;
+    const int cur = (int)(h->pw_frames & 1ull), nxt = cur ^ 1;
+    LV_CUDA(h, cudaMemsetAsync(h->pd.repBefore, 0xff, h->npx * 4, st), "scratch reset");
+    LV_CUDA(h, cudaMemsetAsync(h->d_work, 0, sizeof(TickWork), st), "scratch reset");
+    int round = 0;
+    for (;; ++round) {
+        if (round >= 64) return fail(h, LVBGS_DEVICE_ERROR, "PAWCS raster-order fixed point did not converge in 64 rounds");
+        P.round = round;
+        pw_k_local<<<tiles, blk, 0, st>>>(P);
+        pw_k_illum<<<(h->H + 127) / 128, 128, 0, st>>>(P);
+        pw_k_items<<<tiles, blk, 0, st>>>(P);
+        pw_k_gscan<<<1, 32, 0, st>>>(P);
+        pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
+        pw_k_nbr<<<tiles, blk, 0, st>>>(P);
+        pw_k_replace<<<tiles, blk, 0, st>>>(P);
+        LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 4, st), "flag reset");
+        pw_k_dirty<<<tiles, blk, 0, st>>>(P);
+        LV_CUDA(h, cudaGetLastError(), "PAWCS round launch");
+        LV_CUDA(h, cudaMemcpyAsync(h->h_flags, h->d_flags, 4, cudaMemcpyDeviceToHost, st), "flag read-back");
+        LV_CUDA(h, cudaStreamSynchronize(st), "PAWCS round");
+        if (h->h_flags[0] == 0) break;
+    }
+    h->pw_rounds_last = round + 1;
+    pw_k_commit<<<tiles, blk, 0, st>>>(P);
+    pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 1);
+    pw_k_weights<<<kPwMaxGlobal, 32, 0, st>>>(P);
+    pw_k_gw_recalc<<<kPwMaxGlobal, 256, 0, st>>>(P);
+    pw_k_gw_decay<<<dim3(64, kPwMaxGlobal), 256, 0, st>>>(P, h->d_rowsum);
+    pw_k_gw_blur<<<dim3(64, kPwMaxGlobal), 256, 0, st>>>(P, h->d_rowsum);
+    pw_k_gw_sort<<<1, 32, 0, st>>>(P);
+    pw_k_lut_sort<<<tiles, blk, 0, st>>>(P, 0);
+    pw_k_blink_close<<<tiles, blk, 0, st>>>(P);
+    TickParams TP;
+    std::memset(&TP, 0, sizeof(TP));
+    TP.streams = h->d_sd;
+    TP.nStreams = 1;
+    TP.totalTiles = tiles;
+    TP.totalRows = h->H;
+    TP.work = h->d_work;
+    const int rowBlocks = (h->H + 7) / 8;
+    lvbgs_k_runs<<<rowBlocks, blk, 0, st>>>(TP);
+    lvbgs_k_vunion<<<rowBlocks, blk, 0, st>>>(TP);
+    lvbgs_k_holes<<<rowBlocks, blk, 0, st>>>(TP);
+    lvbgs_k_combine<<<tiles, blk, 0, st>>>(TP);
+    lvbgs_k_median<<<tiles, blk, 0, st>>>(TP);
+    lvbgs_k_dilate<<<tiles, blk, 0, st>>>(TP);
+    pw_k_epilogue<<<1, 256, 0, st>>>(P);
+    // automatic model reset (:1503-1508): refreshModel(offset/8, 0, true) and T(x) := 1
+    const uint32_t t = (uint32_t)(h->pw_frames + 1);
+    if ((s = pw_refresh(h, t, nxt, (int)(h->pw_offset / 8), 0.0f, 1, 1, 1, st)) != LVBGS_OK) return s;
+    pw_k_reset_T<<<256, 256, 0, st>>>(h->pd, nxt);
+    pw_k_close<<<1, 32, 0, st>>>(P);
+    LV_CUDA(h, cudaGetLastError(), "PAWCS frame step launch");
+    if (mask && !devMask) LV_CUDA(h, cudaMemcpyAsync(mask, h->d_mask, h->npx, cudaMemcpyDeviceToHost, st), "mask download");
+    LV_CUDA(h, cudaStreamSynchronize(st), "PAWCS frame step");
+    (void)cur;
+    h->pw_frames += 1;
+    TickWork w;
+    LV_CUDA(h, cudaMemcpy(&w, h->d_work, sizeof(TickWork), cudaMemcpyDeviceToHost), "status read-back");
+    return status_from_work(h, w);
+}
+
+}  // namespace
+
 lvbgs_status lvbgs_default_params(lvbgs_algo algo, lvbgs_params* out) {
     if (!out) return fail(nullptr, LVBGS_BAD_ARG, "null output");
-    if (algo != LVBGS_ALGO_SUBSENSE) return fail(nullptr, LVBGS_UNSUPPORTED, "only SuBSENSE is implemented on the GPU");
+    if (algo == LVBGS_ALGO_PAWCS) {
+        // BackgroundSubtractorPAWCS.hpp:22-29 (bg_samples carries nMaxNbWords), BackgroundSubtractorLBSP.hpp:23-28
+        out->desc_dist_threshold_offset = 2;
+        out->min_color_dist_threshold = 20;
+        out->bg_samples = 50;
+        out->required_bg_samples = 0;
+        out->samples_for_moving_avgs = 100;
+        out->rel_lbsp_threshold = 0.333f;
+        out->lbsp_threshold_offset = 0;
+        out->default_median_blur_kernel_size = 9;
+        out->seed = 0;
+        out->device_id = 0;
+        return LVBGS_OK;
+    }
+    if (algo != LVBGS_ALGO_SUBSENSE) return fail(nullptr, LVBGS_BAD_ARG, "unknown algorithm");
     out->desc_dist_threshold_offset = 3;
     out->min_color_dist_threshold = 30;
     out->bg_samples = 50;
@@ -463,10 +867,17 @@ lvbgs_status lvbgs_default_params(lvbgs_algo algo, lvbgs_params* out) {
 lvbgs_status lvbgs_create(lvbgs_algo algo, const lvbgs_params* p, lvbgs_handle* out) {
     if (!out) return fail(nullptr, LVBGS_BAD_ARG, "null output handle");
     *out = nullptr;
-    if (algo != LVBGS_ALGO_SUBSENSE) return fail(nullptr, LVBGS_UNSUPPORTED, "only SuBSENSE is implemented on the GPU");
+    if (algo != LVBGS_ALGO_SUBSENSE && algo != LVBGS_ALGO_PAWCS) return fail(nullptr, LVBGS_BAD_ARG, "unknown algorithm");
     lvbgs_params prm;
     if (p) prm = *p;
     else lvbgs_default_params(algo, &prm);
+    if (algo == LVBGS_ALGO_PAWCS) {
+        // BackgroundSubtractorPAWCS.cpp:105 (max local and global word counts positive)
+        if (prm.bg_samples / 2 == 0) return fail(nullptr, LVBGS_BAD_ARG, "max local/global word counts must be positive");
+        if (prm.bg_samples / 2 > (size_t)kPwMaxLocal)
+            return fail(nullptr, LVBGS_UNSUPPORTED, "this implementation supports at most 51 PAWCS words (25 local, 12 global)");
+        prm.required_bg_samples = 0;
+    }
     // BackgroundSubtractorSuBSENSE.cpp:76-77, BackgroundSubtractorLBSP.hpp:53
     if (prm.bg_samples == 0 || prm.required_bg_samples > prm.bg_samples)
         return fail(nullptr, LVBGS_BAD_ARG, "algo cannot require more sample matches than sample count in model");
@@ -527,6 +938,7 @@ lvbgs_status lvbgs_destroy(lvbgs_handle h) {
     cudaFree(h->dmem);
     h->ws.release();
     h->batchWs.release();
+    if (h->h_flags) cudaFreeHost(h->h_flags);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return LVBGS_OK;
@@ -566,6 +978,7 @@ lvbgs_status lvbgs_initialize(lvbgs_handle h, const uint8_t* img, int W, int H, 
     for (size_t i = 0; i < npx; ++i) fin += newroi[i] != 0;
     if (fin == 0)
         return fail(h, LVBGS_BAD_ARG, "provided ROI mat contains no useful pixels away from borders (descriptors will hit image bounds)");
+    if (h->algo == LVBGS_ALGO_PAWCS) return pw_initialize(h, img, W, H, C, stride, newroi, orig, fin);
     // resolution-dependent parameters (BackgroundSubtractorSuBSENSE.cpp:112-128)
     StreamCtl ctl;
     std::memset(&ctl, 0, sizeof(ctl));
@@ -642,6 +1055,7 @@ lvbgs_status lvbgs_apply(lvbgs_handle h, const uint8_t* img, size_t stride, uint
     if (s != LVBGS_OK) return s;
     if (!img) return fail(h, LVBGS_BAD_ARG, "null input image");
     cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : h->stream;
+    if (h->algo == LVBGS_ALGO_PAWCS) return pw_apply(h, img, stride, mask, lr, st);
     const uint8_t* dimg = nullptr;
     if ((s = stage_frame(h, img, stride, st, &dimg)) != LVBGS_OK) return s;
     const bool devMask = mask && is_device_ptr(mask);
@@ -666,6 +1080,8 @@ lvbgs_status check_batch(const lvbgs_handle* hs, const lvbgs_frame* frames, int 
         if (s != LVBGS_OK) return s;
         if (hs[i]->device != lead->device) return fail(lead, LVBGS_BAD_ARG, "batched handles must share one device");
         if (!frames[i].image) return fail(hs[i], LVBGS_BAD_ARG, "null input image");
+        if (hs[i]->algo != LVBGS_ALGO_SUBSENSE)
+            return fail(hs[i], LVBGS_UNSUPPORTED, "batched frame steps are implemented for SuBSENSE streams");
         for (int j = 0; j < i; ++j)
             if (hs[j] == hs[i]) return fail(lead, LVBGS_BAD_ARG, "a handle appears twice in the batch");
     }
@@ -860,6 +1276,15 @@ lvbgs_status lvbgs_get_background(lvbgs_handle h, uint8_t* out) {
     lvbgs_status s = check_ready(h);
     if (s != LVBGS_OK) return s;
     if (!out) return fail(h, LVBGS_BAD_ARG, "null output");
+    if (h->algo == LVBGS_ALGO_PAWCS) {
+        const bool dev = is_device_ptr(out);
+        uint8_t* d = dev ? out : h->d_frame;
+        pw_k_background<<<512, 256, 0, h->stream>>>(h->pd, (int)(h->pw_frames & 1ull), d, nullptr);
+        LV_CUDA(h, cudaGetLastError(), "background kernel");
+        if (!dev) LV_CUDA(h, cudaMemcpyAsync(out, d, h->npx, cudaMemcpyDeviceToHost, h->stream), "download");
+        LV_CUDA(h, cudaStreamSynchronize(h->stream), "background image");
+        return LVBGS_OK;
+    }
     const bool dev = is_device_ptr(out);
     uint8_t* d = dev ? out : h->d_frame;
     lvbgs_background<<<512, 256, 0, h->stream>>>(h->sd, d, nullptr);
@@ -875,7 +1300,8 @@ lvbgs_status lvbgs_get_background_descriptors(lvbgs_handle h, uint16_t* out) {
     if (!out) return fail(h, LVBGS_BAD_ARG, "null output");
     uint16_t* d = nullptr;
     LV_CUDA(h, cudaMallocAsync((void**)&d, h->npx * h->C * 2, h->stream), "temporary allocation");
-    lvbgs_background<<<512, 256, 0, h->stream>>>(h->sd, nullptr, d);
+    if (h->algo == LVBGS_ALGO_PAWCS) pw_k_background<<<512, 256, 0, h->stream>>>(h->pd, (int)(h->pw_frames & 1ull), nullptr, d);
+    else lvbgs_background<<<512, 256, 0, h->stream>>>(h->sd, nullptr, d);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, h->npx * h->C * 2, cudaMemcpyDefault, h->stream);
     cudaFreeAsync(d, h->stream);
@@ -887,6 +1313,8 @@ lvbgs_status lvbgs_get_background_descriptors(lvbgs_handle h, uint16_t* out) {
 lvbgs_status lvbgs_refresh_model(lvbgs_handle h, float frac, int force) {
     lvbgs_status s = check_ready(h);
     if (s != LVBGS_OK) return s;
+    if (h->algo == LVBGS_ALGO_PAWCS)
+        return fail(h, LVBGS_BAD_ARG, "PAWCS's refreshModel takes (base occurrences, decrement fraction, force): use lvbgs_pawcs_refresh_model");
     if (!(frac > 0.0f && frac <= 1.0f)) return fail(h, LVBGS_BAD_ARG, "model refresh must be given as a non-null fraction");
     StreamCtl ctl;
     LV_CUDA(h, cudaMemcpy(&ctl, h->sd.ctl, sizeof(ctl), cudaMemcpyDeviceToHost), "control read");
@@ -935,11 +1363,25 @@ lvbgs_status lvbgs_get_size(lvbgs_handle h, int* w, int* hh, int* c) {
 }
 
 size_t lvbgs_state_bytes(lvbgs_algo algo, int W, int H, int C, size_t N) {
+    if (algo == LVBGS_ALGO_PAWCS && W > 0 && H > 0 && C == 1) {
+        lvbgs_params prm;
+        lvbgs_default_params(LVBGS_ALGO_PAWCS, &prm);
+        if (N) prm.bg_samples = N;
+        const PwGeom g = pw_geometry(prm, (size_t)W * H, (size_t)W * H, 1);
+        return pw_layout(W, H, g.L, g.G).persist;
+    }
     if (algo != LVBGS_ALGO_SUBSENSE || W <= 0 || H <= 0 || (C != 1 && C != 3)) return 0;
     return make_layout(W, H, C, N ? N : 50).persist;
 }
 
 size_t lvbgs_device_bytes(lvbgs_algo algo, int W, int H, int C, size_t N) {
+    if (algo == LVBGS_ALGO_PAWCS && W > 0 && H > 0 && C == 1) {
+        lvbgs_params prm;
+        lvbgs_default_params(LVBGS_ALGO_PAWCS, &prm);
+        if (N) prm.bg_samples = N;
+        const PwGeom g = pw_geometry(prm, (size_t)W * H, (size_t)W * H, 1);
+        return pw_layout(W, H, g.L, g.G).total;
+    }
     if (algo != LVBGS_ALGO_SUBSENSE || W <= 0 || H <= 0 || (C != 1 && C != 3)) return 0;
     // model and scratch block, plus the handle's own workspace (status, one descriptor table,
     // four repair lists of one entry per pixel)
@@ -951,6 +1393,7 @@ size_t lvbgs_device_bytes(lvbgs_algo algo, int W, int H, int C, size_t N) {
 lvbgs_status lvbgs_spill(lvbgs_handle h, void* host, size_t bytes) {
     lvbgs_status s = check_ready(h);
     if (s != LVBGS_OK) return s;
+    if (h->algo != LVBGS_ALGO_SUBSENSE) return fail(h, LVBGS_UNSUPPORTED, "spilling is implemented for SuBSENSE streams");
     if (!host || bytes < h->persistBytes) return fail(h, LVBGS_BAD_ARG, "spill buffer is smaller than lvbgs_state_bytes()");
     LV_CUDA(h, cudaStreamSynchronize(h->stream), "spill");
     LV_CUDA(h, cudaMemcpy(host, h->dmem, h->persistBytes, cudaMemcpyDeviceToHost), "spill copy");
@@ -1147,3 +1590,189 @@ lvbgs_status lvbgs_get_scalars(lvbgs_handle h, lvbgs_scalars* out) {
 }
 
 }  // extern "C"
+
+// ---- PAWCS-specific entry points ----
+lvbgs_status lvbgs_pawcs_refresh_model(lvbgs_handle h, size_t base_occ, float decr, int force) {
+    lvbgs_status s = check_ready(h);
+    if (s != LVBGS_OK) return s;
+    if (h->algo != LVBGS_ALGO_PAWCS) return fail(h, LVBGS_BAD_ARG, "not a PAWCS handle");
+    // BackgroundSubtractorPAWCS.cpp:109-110
+    if (!(decr >= 0.0f && decr <= 1.0f))
+        return fail(h, LVBGS_BAD_ARG, "model occurrence decrementation must be given as a non-null fraction");
+    if (base_occ > 0xffffffffull) return fail(h, LVBGS_UNSUPPORTED, "base occurrence count above 2^32");
+    const int buf = (int)(h->pw_frames & 1ull);
+    if ((s = pw_upload_desc(h, h->stream)) != LVBGS_OK) return s;
+    if ((s = pw_refresh(h, (uint32_t)h->pw_frames, buf, (int)base_occ, decr, force ? 1 : 0, 0, 1, h->stream)) != LVBGS_OK)
+        return s;
+    LV_CUDA(h, cudaStreamSynchronize(h->stream), "refresh");
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_pawcs_get_scalars(lvbgs_handle h, lvbgs_pawcs_scalars* out) {
+    lvbgs_status s = check_ready(h);
+    if (s != LVBGS_OK) return s;
+    if (h->algo != LVBGS_ALGO_PAWCS || !out) return fail(h, LVBGS_BAD_ARG, "not a PAWCS handle or null output");
+    LV_CUDA(h, cudaStreamSynchronize(h->stream), "sync");
+    StreamCtl c;
+    PawcsCtl pc;
+    LV_CUDA(h, cudaMemcpy(&c, h->sd.ctl, sizeof(c), cudaMemcpyDeviceToHost), "control read");
+    LV_CUDA(h, cudaMemcpy(&pc, h->pd.pc, sizeof(pc), cudaMemcpyDeviceToHost), "control read");
+    std::memset(out, 0, sizeof(*out));
+    out->frame_idx = c.frame_idx;
+    out->frames_since_last_reset = c.frames_since_reset;
+    out->model_reset_cooldown = c.cooldown;
+    out->lword_weight_offset = pc.lword_offset;
+    out->auto_model_reset_enabled = c.auto_reset;
+    out->using_moving_camera = pc.moving_cam;
+    out->median_blur_kernel_size = c.median_k;
+    out->n_local_words = pc.L;
+    out->n_global_words = pc.G;
+    out->last_nonflat_ratio = pc.last_nonflat_ratio;
+    out->n_relevant_px = c.n_rel;
+    out->orig_roi_px = c.orig_roi;
+    out->ds_roi_px = pc.ds_roi_count;
+    out->fixed_point_rounds = (uint64_t)h->pw_rounds_last;
+    return LVBGS_OK;
+}
+
+size_t lvbgs_pawcs_debug_export_bytes(lvbgs_handle h, int which) {
+    if (!h || h->algo != LVBGS_ALGO_PAWCS || !h->initialized) return 0;
+    const size_t npx = h->npx, nw = h->n_rel * (size_t)h->pd.L, gmap = (size_t)h->pd.gwW * h->pd.gwH;
+    const size_t nds = (size_t)h->sd.dsW * h->sd.dsH;
+    switch (which) {
+    case LVBGS_PAWCS_MAP_R: case LVBGS_PAWCS_MAP_V: case LVBGS_PAWCS_MAP_T: case LVBGS_PAWCS_MAP_DMIN_LT:
+    case LVBGS_PAWCS_MAP_DMIN_ST: case LVBGS_PAWCS_MAP_RAW_LT: case LVBGS_PAWCS_MAP_RAW_ST:
+    case LVBGS_PAWCS_MAP_FIN_LT: case LVBGS_PAWCS_MAP_FIN_ST: return npx * 4;
+    case LVBGS_PAWCS_MAP_ILLUM: case LVBGS_PAWCS_MAP_UNSTABLE: case LVBGS_PAWCS_MAP_BLINKS:
+    case LVBGS_PAWCS_MAP_LAST_RAW_FG: case LVBGS_PAWCS_MAP_LAST_FG: case LVBGS_PAWCS_MAP_LAST_FG_DIL:
+    case LVBGS_PAWCS_MAP_LAST_RAW_BLINK: case LVBGS_PAWCS_MAP_ROI: case LVBGS_PAWCS_MAP_LAST_COLOR: return npx;
+    case LVBGS_PAWCS_MAP_LAST_DESC: return npx * 2;
+    case LVBGS_PAWCS_MAP_DS_LT: case LVBGS_PAWCS_MAP_DS_ST: return nds * 4;
+    case LVBGS_PAWCS_MAP_LUT: return 256;
+    case LVBGS_PAWCS_MAP_LW_COLOR: return nw;
+    case LVBGS_PAWCS_MAP_LW_DESC: return nw * 2;
+    case LVBGS_PAWCS_MAP_LW_OCC: case LVBGS_PAWCS_MAP_LW_FIRST: case LVBGS_PAWCS_MAP_LW_LAST: return nw * 8;
+    case LVBGS_PAWCS_MAP_GW: return (size_t)h->pd.G * 20;
+    case LVBGS_PAWCS_MAP_GW_MAP: return (size_t)h->pd.G * gmap * 4;
+    case LVBGS_PAWCS_MAP_GLUT: return npx * (size_t)h->pd.G;
+    default: return 0;
+    }
+}
+
+lvbgs_status lvbgs_pawcs_debug_export(lvbgs_handle h, int which, void* out, size_t bytes) {
+    lvbgs_status s = check_ready(h);
+    if (s != LVBGS_OK) return s;
+    const size_t need = lvbgs_pawcs_debug_export_bytes(h, which);
+    if (!need || !out || bytes < need) return fail(h, LVBGS_BAD_ARG, "unknown map or output too small");
+    LV_CUDA(h, cudaStreamSynchronize(h->stream), "sync");
+    const size_t npx = h->npx, L = (size_t)h->pd.L, G = (size_t)h->pd.G;
+    const size_t gmap = (size_t)h->pd.gwW * h->pd.gwH, nds = (size_t)h->sd.dsW * h->sd.dsH;
+    const int buf = (int)(h->pw_frames & 1ull);
+    auto dl = [&](void* dst, const void* src, size_t n) { return cudaMemcpy(dst, src, n, cudaMemcpyDeviceToHost); };
+    const float* fm = h->sd.fm + (size_t)buf * kNumFloatMaps * npx;
+    int fmap = -1;
+    switch (which) {
+    case LVBGS_PAWCS_MAP_R: fmap = FM_R; break;
+    case LVBGS_PAWCS_MAP_V: fmap = FM_V; break;
+    case LVBGS_PAWCS_MAP_T: fmap = FM_T; break;
+    case LVBGS_PAWCS_MAP_DMIN_LT: fmap = FM_DMIN_LT; break;
+    case LVBGS_PAWCS_MAP_DMIN_ST: fmap = FM_DMIN_ST; break;
+    case LVBGS_PAWCS_MAP_RAW_LT: fmap = FM_RAW_LT; break;
+    case LVBGS_PAWCS_MAP_RAW_ST: fmap = FM_RAW_ST; break;
+    case LVBGS_PAWCS_MAP_FIN_LT: fmap = FM_FIN_LT; break;
+    case LVBGS_PAWCS_MAP_FIN_ST: fmap = FM_FIN_ST; break;
+    default: break;
+    }
+    cudaError_t e = cudaSuccess;
+    if (fmap >= 0) {
+        e = dl(out, fm + (size_t)fmap * npx, npx * 4);
+    } else {
+        switch (which) {
+        case LVBGS_PAWCS_MAP_ILLUM: e = dl(out, h->pd.illum, npx); break;
+        case LVBGS_PAWCS_MAP_UNSTABLE: e = dl(out, h->pd.unstable, npx); break;
+        case LVBGS_PAWCS_MAP_BLINKS: e = dl(out, h->sd.blinks, npx); break;
+        case LVBGS_PAWCS_MAP_LAST_RAW_FG: e = dl(out, h->sd.lastRawFG, npx); break;
+        case LVBGS_PAWCS_MAP_LAST_FG: e = dl(out, h->sd.lastFG, npx); break;
+        case LVBGS_PAWCS_MAP_LAST_FG_DIL: {
+            // stored inverted; before the first frame the dilated mask is all clear
+            e = dl(out, h->sd.dilInv, npx);
+            uint8_t* o = (uint8_t*)out;
+            for (size_t i = 0; i < npx; ++i) o[i] = h->pw_frames ? (uint8_t)~o[i] : 0;
+            break;
+        }
+        case LVBGS_PAWCS_MAP_LAST_RAW_BLINK: e = dl(out, h->sd.lastRawBlink, npx); break;
+        case LVBGS_PAWCS_MAP_ROI: e = dl(out, h->sd.roi, npx); break;
+        case LVBGS_PAWCS_MAP_LAST_COLOR: e = dl(out, h->sd.lastCol, npx); break;
+        case LVBGS_PAWCS_MAP_LAST_DESC: e = dl(out, h->sd.lastDesc, npx * 2); break;
+        case LVBGS_PAWCS_MAP_DS_LT: e = dl(out, h->sd.dsLT, nds * 4); break;
+        case LVBGS_PAWCS_MAP_DS_ST: e = dl(out, h->sd.dsST, nds * 4); break;
+        case LVBGS_PAWCS_MAP_LUT: {
+            StreamCtl c;
+            e = dl(&c, h->sd.ctl, sizeof(c));
+            std::memcpy(out, c.lut, 256);
+            break;
+        }
+        case LVBGS_PAWCS_MAP_GW_MAP: e = dl(out, h->pd.gmap, G * gmap * 4); break;
+        case LVBGS_PAWCS_MAP_GLUT: {
+            std::vector<uint8_t> g(npx * 16);
+            e = dl(g.data(), h->pd.glut, npx * 16);
+            uint8_t* o = (uint8_t*)out;
+            for (size_t i = 0; i < npx; ++i)
+                for (size_t k = 0; k < G; ++k) o[i * G + k] = h->roi[i] ? g[i * 16 + k] : 0;
+            break;
+        }
+        case LVBGS_PAWCS_MAP_GW: {
+            PawcsCtl pc;
+            e = dl(&pc, h->pd.pc, sizeof(pc));
+            uint8_t* b = (uint8_t*)out;
+            std::memset(b, 0, G * 20);
+            for (size_t w = 0; w < G; ++w) {
+                uint8_t* r = b + w * 20;
+                r[0] = (uint8_t)pc.gw_color[w];
+                const uint16_t d = (uint16_t)pc.gw_desc[w];
+                std::memcpy(r + 4, &d, 2);
+                r[10] = (uint8_t)pc.gw_bits[w];
+                std::memcpy(r + 12, &pc.gw_weight[w], 4);
+                int32_t slot = -1;
+                for (size_t g = 0; g < G; ++g)
+                    if (pc.gdict[g] == (int)w) slot = (int32_t)g;
+                std::memcpy(r + 16, &slot, 4);
+            }
+            break;
+        }
+        case LVBGS_PAWCS_MAP_LW_COLOR: case LVBGS_PAWCS_MAP_LW_DESC: case LVBGS_PAWCS_MAP_LW_OCC:
+        case LVBGS_PAWCS_MAP_LW_FIRST: case LVBGS_PAWCS_MAP_LW_LAST: {
+            // model-major (ROI pixels in raster order), slot-minor, as the reference's dictionary
+            const size_t es = which == LVBGS_PAWCS_MAP_LW_COLOR ? 1 : which == LVBGS_PAWCS_MAP_LW_DESC ? 2 : 4;
+            const void* src = which == LVBGS_PAWCS_MAP_LW_COLOR  ? (const void*)h->pd.wColor
+                              : which == LVBGS_PAWCS_MAP_LW_DESC ? (const void*)h->pd.wDesc
+                              : which == LVBGS_PAWCS_MAP_LW_OCC  ? (const void*)h->pd.wOcc
+                              : which == LVBGS_PAWCS_MAP_LW_FIRST ? (const void*)h->pd.wFirst
+                                                                  : (const void*)h->pd.wLast;
+            std::vector<uint8_t> planes(L * npx * es);
+            e = dl(planes.data(), (const uint8_t*)src + (size_t)buf * L * npx * es, planes.size());
+            size_t m = 0;
+            for (size_t i = 0; i < npx; ++i) {
+                if (!h->roi[i]) continue;
+                for (size_t j = 0; j < L; ++j) {
+                    const size_t k = m * L + j;
+                    const uint8_t* v = planes.data() + (j * npx + i) * es;
+                    if (es == 4) {
+                        uint32_t u;
+                        std::memcpy(&u, v, 4);
+                        const uint64_t u64 = u;
+                        std::memcpy((uint8_t*)out + k * 8, &u64, 8);
+                    } else {
+                        std::memcpy((uint8_t*)out + k * es, v, es);
+                    }
+                }
+                ++m;
+            }
+            break;
+        }
+        default: return fail(h, LVBGS_BAD_ARG, "unknown map");
+        }
+    }
+    if (e != cudaSuccess) return cuda_fail(h, e, "map download");
+    return LVBGS_OK;
+}

@@ -38,7 +38,11 @@ def test_default_params_match_reference(product_lib):
             p.samples_for_moving_avgs, p.lbsp_threshold_offset, p.default_median_blur_kernel_size) == (
                 3, 30, 50, 2, 100, 0, 9)
     assert abs(p.rel_lbsp_threshold - 0.333) < 1e-7
-    assert product_lib.lvbgs_default_params(L.ALGO_PAWCS, C.byref(p)) == L.UNSUPPORTED
+    # BackgroundSubtractorPAWCS.hpp:22-29: offset 2, colour 20, 50 words, 100 frames
+    assert product_lib.lvbgs_default_params(L.ALGO_PAWCS, C.byref(p)) == L.OK
+    assert (p.desc_dist_threshold_offset, p.min_color_dist_threshold, p.bg_samples, p.samples_for_moving_avgs,
+            p.default_median_blur_kernel_size) == (2, 20, 50, 100, 9)
+    assert product_lib.lvbgs_default_params(7, C.byref(p)) == L.BAD_ARG
 
 
 def test_create_rejects_bad_parameters(product_lib):

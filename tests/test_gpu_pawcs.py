@@ -1,0 +1,145 @@
+"""GPU parity tests of PAWCS (one channel): the CUDA path through the C-ABI against the oracle.
+
+Masks, descriptors, every local and global dictionary word, the per-pixel global word tables and all
+integer maps must be identical; the FP32 maps (feedback maps, spatial occurrence maps, word weights,
+down-sampled averages) must be identical too (tolerance 0 ulp): both sides keep the reference's
+operation order without fused multiply-adds. Every compared frame checks the whole model state.
+"""
+import numpy as np
+import pytest
+
+from litiv_gb300 import BackgroundSubtractorPAWCS, LvException, SyntheticStream
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+MAPS = ["R", "V", "T", "DMIN_LT", "DMIN_ST", "RAW_LT", "RAW_ST", "FIN_LT", "FIN_ST", "ILLUM", "UNSTABLE", "BLINKS",
+        "LAST_RAW_FG", "LAST_FG", "LAST_FG_DIL", "LAST_RAW_BLINK", "ROI", "LAST_COLOR", "LAST_DESC", "DS_LT", "DS_ST",
+        "LUT", "LW_COLOR", "LW_DESC", "LW_OCC", "LW_FIRST", "LW_LAST", "GW", "GW_MAP", "GLUT"]
+SCALARS = ["frame_idx", "frames_since_last_reset", "model_reset_cooldown", "lword_weight_offset",
+           "auto_model_reset_enabled", "using_moving_camera", "median_blur_kernel_size", "n_local_words",
+           "n_global_words", "last_nonflat_ratio", "n_relevant_px", "orig_roi_px", "ds_roi_px"]
+
+
+def compare_state(gpu, ora):
+    bad = []
+    for name in MAPS:
+        a, b = gpu.state_map(name), ora.state_map(name)
+        if a.size != b.size:
+            bad.append("%s: %d vs %d bytes" % (name, a.size, b.size))
+        elif not np.array_equal(a, b):
+            idx = np.flatnonzero(a != b)
+            bad.append("%s: %d bytes differ (first at byte %d)" % (name, idx.size, idx[0]))
+    sg, so = gpu.scalars(), ora.scalars()
+    for k in SCALARS:
+        if sg[k] != so[k]:
+            bad.append("%s: %r vs %r" % (k, sg[k], so[k]))
+    return bad
+
+
+def run_pair(frames, seed=5, lrs=None, roi=None, check_every=1, **params):
+    gpu = BackgroundSubtractorPAWCS(seed=seed, **params)
+    ora = pyoracle.OraclePAWCS(seed=seed, **{_oname(k): v for k, v in params.items()})
+    gpu.initialize(frames[0], roi)
+    ora.initialize(frames[0], roi)
+    bad = compare_state(gpu, ora)
+    assert not bad, "after initialize: " + "; ".join(bad)
+    for t, f in enumerate(frames[1:], start=1):
+        lr = 0.0 if lrs is None else lrs[t]
+        mg = gpu.apply(f, learningRateOverride=lr)
+        mo = ora.apply(f, lr)
+        assert np.array_equal(mg, mo), "frame %d: mask differs at %d px" % (t, int((mg != mo).sum()))
+        if t % check_every == 0 or t == len(frames) - 1:
+            bad = compare_state(gpu, ora)
+            assert not bad, "frame %d: %s" % (t, "; ".join(bad))
+    return gpu, ora
+
+
+def _oname(k):
+    return {"nDescDistThresholdOffset": "desc_dist_threshold_offset",
+            "nMinColorDistThreshold": "min_color_dist_threshold", "nMaxNbWords": "max_words",
+            "nSamplesForMovingAvgs": "samples_for_moving_avgs", "fRelLBSPThreshold": "rel_lbsp_threshold"}[k]
+
+
+def _gray(n, seed, W, H, cfg=0):
+    s = SyntheticStream(cfg, 0, seed, width=W, height=H, channels=1)
+    return [s.render(t) for t in range(n)]
+
+
+def test_small_frame_single_global_word():
+    # 64x48: one global word (every global item depends on the replaceable word), median 5
+    run_pair(_gray(25, 31, 64, 48), seed=3)
+
+
+def test_moving_shapes_160x120():
+    run_pair(_gray(30, 32, 160, 120), seed=4, check_every=3)
+
+
+def test_thermal_scene_160x120():
+    s = SyntheticStream(2, 0, 33, width=160, height=120)
+    run_pair([s.render(t) for t in range(30)], seed=5, check_every=3)
+
+
+def test_full_roi_branch_320x240():
+    # frames of 320x240 take the reference's large-frame parameters (median 9, 12 global words,
+    # every down-sampled pixel counted)
+    s = SyntheticStream(2, 0, 34, width=320, height=240)
+    gpu, ora = run_pair([s.render(t) for t in range(17)], seed=6, check_every=8)
+    assert gpu.scalars()["median_blur_kernel_size"] == 9
+
+
+def test_roi_with_border_pixels():
+    fr = _gray(20, 35, 96, 72)
+    yy, xx = np.mgrid[0:72, 0:96]
+    roi = (((xx - 48) / 40.0) ** 2 + ((yy - 36) / 30.0) ** 2 <= 1.0).astype(np.uint8) * 255
+    run_pair(fr, seed=7, roi=roi, check_every=4)
+
+
+def test_learning_rate_overrides():
+    fr = _gray(16, 36, 96, 72)
+    lrs = [0.0] * 16
+    for t in range(4, 8):
+        lrs[t] = 1.0
+    for t in range(8, 11):
+        lrs[t] = float("inf")
+    lrs[12] = 3.5
+    run_pair(fr, seed=8, lrs=lrs, check_every=2)
+
+
+def test_automatic_model_reset():
+    # a sudden global change of the scene raises the down-sampled L1 ratio above 45 and triggers
+    # refreshModel(offset/8, 0, true) with T(x) := 1 and the cool-down
+    fr = _gray(26, 37, 96, 72)
+    for t in range(14, 26):
+        fr[t] = np.clip(fr[t].astype(int) + 120, 0, 255).astype(np.uint8)
+    gpu, ora = run_pair(fr, seed=9, check_every=2)
+    assert ora.scalars()["model_reset_cooldown"] > 0 or ora.scalars()["frames_since_last_reset"] == 0
+
+
+def test_refresh_model_and_background_images():
+    fr = _gray(14, 38, 96, 72)
+    gpu, ora = run_pair(fr[:8], seed=10)
+    gpu.refreshModel(5, 0.5, True)
+    ora.refresh_model(5, 0.5, True)
+    bad = compare_state(gpu, ora)
+    assert not bad, "after refreshModel: " + "; ".join(bad)
+    for f in fr[8:]:
+        assert np.array_equal(gpu.apply(f), ora.apply(f))
+    assert not compare_state(gpu, ora)
+    assert np.array_equal(gpu.getBackgroundImage(), ora.background())
+    assert np.array_equal(gpu.getBackgroundDescriptorsImage(), ora.background_descriptors())
+
+
+def test_api_errors():
+    b = BackgroundSubtractorPAWCS()
+    with pytest.raises(LvException):
+        b.apply(np.zeros((48, 64), np.uint8))
+    with pytest.raises(LvException):
+        b.initialize(np.zeros((48, 64, 3), np.uint8))  # three channels: not implemented
+    b.initialize(np.zeros((48, 64), np.uint8))
+    with pytest.raises(LvException):
+        b.apply(np.zeros((48, 65), np.uint8))
+    with pytest.raises(LvException):
+        b.refreshModel(1, 1.5)
+    with pytest.raises(LvException):
+        BackgroundSubtractorPAWCS(nMaxNbWords=1)
