@@ -136,6 +136,70 @@ def cpu_baseline(n_frames=6, threads=None):
                 len(frames), n_frames - 1, px / 1e6, wall)}
 
 
+def pawcs_run(n_frames, stream, cpu=True):
+    """PAWCS on the thermal-like 640x480 single-channel scene: every frame through lvbgs_apply, from
+    frames resident on the device (value) and from pinned host frames (e2e); wall clock per frame, since
+    a PAWCS frame step waits for its fixed-point rounds. The first 10 frames are warm-up."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    from litiv_gb300 import BackgroundSubtractorPAWCS, SyntheticStream
+    from litiv_gb300 import _lib as L
+    lib = L.lib()
+    s = SyntheticStream(2, 0, 1)
+    W, H = s.cfg.width, s.cfg.height
+    n = min(n_frames, s.n_frames)
+    dev = torch.empty((n, H, W), dtype=torch.uint8, device="cuda")
+    for t in range(n):
+        s.render_device(t, dev[t].data_ptr(), cuda_stream=stream.cuda_stream)
+    host = torch.empty((n, H, W), dtype=torch.uint8).pin_memory()
+    host.copy_(dev.cpu())
+    dmask = torch.empty((H, W), dtype=torch.uint8, device="cuda")
+    hmask = torch.empty((H, W), dtype=torch.uint8).pin_memory()
+    torch.cuda.synchronize()
+    out = {"workload": "PAWCS, 640x480 single-channel thermal-like scene (six warm blobs, random walks), default "
+                       "parameters, %d frames" % n}
+    for leg, frames, mask in (("device", dev, dmask), ("host", host, hmask)):
+        b = BackgroundSubtractorPAWCS(seed=1)
+        b.initialize(frames[0].cpu().numpy())
+        ms, rounds = [], []
+        for t in range(1, n):
+            t0 = time.perf_counter()
+            st = lib.lvbgs_apply(b.handle, C.c_void_p(frames[t].data_ptr()), 0, C.c_void_p(mask.data_ptr()), 0.0,
+                                 C.c_void_p(stream.cuda_stream))
+            ms.append((time.perf_counter() - t0) * 1e3)
+            if st != L.OK:
+                raise RuntimeError("PAWCS apply failed: %s" % lib.lvbgs_last_error(b.handle))
+            rounds.append(b.scalars()["fixed_point_rounds"])
+        b.close()
+        m = np.array(ms[9:])
+        r = {"value": W * H / (m.mean() / 1e3) / 1e6, "unit": "Mpix/s", "frames_per_s": 1e3 / m.mean(),
+             "ms_per_frame": float(m.mean()), "p50_frame_ms": float(np.percentile(m, 50)),
+             "p99_frame_ms": float(np.percentile(m, 99)), "rounds_mean": float(np.mean(rounds)),
+             "rounds_max": int(np.max(rounds))}
+        if leg == "device":
+            out.update(r)
+        else:
+            r["h2d_bytes_per_step"] = W * H
+            r["d2h_bytes_per_step"] = W * H
+            out["e2e"] = r
+    if cpu:
+        from oracle import pyoracle
+        threads = os.cpu_count() or 1
+        nf = 3
+        fr, seeds = [], []
+        for i in range(threads):
+            si = SyntheticStream(2, 0, 100 + i)
+            fr.append(np.stack([si.render(t) for t in range(nf)]))
+            seeds.append(100 + i)
+        wall = pyoracle.run_pawcs_streams(fr, seeds, threads)
+        px = threads * (nf - 1) * W * H
+        out["cpu_baseline"] = {"value": px / wall / 1e6, "unit": "Mpix/s", "cores": threads, "kind": "port",
+                               "sample": "%d streams of the scene (one per core), %d applied frames each after "
+                                         "initialization, %.1f Mpix in %.2f s" % (threads, nf - 1, px / 1e6, wall)}
+    return out
+
+
 def serving_run(seconds):
     """The serving workload (Poisson arrivals of 4 streams/s up to 256 live, lives U[10, 60] s, 30 fps,
     320x240/640x480/1280x720/1920x1080 with p = .3/.3/.3/.1, a quarter single-channel), started from its
@@ -187,6 +251,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--pawcs-frames", type=int, default=300,
+                    help="frames of the PAWCS workload (640x480 thermal-like scene; 0: skip)")
     ap.add_argument("--serving-seconds", type=float, default=20.0,
                     help="measured span of the serving workload run (0: skip)")
     args = ap.parse_args()
@@ -367,6 +433,9 @@ def main():
     serve = None
     if rank == 0 and args.serving_seconds > 0:
         serve = serving_run(args.serving_seconds)
+    pawcs = None
+    if rank == 0 and args.pawcs_frames > 0:
+        pawcs = pawcs_run(args.pawcs_frames, stream, cpu=not args.no_cpu_baseline)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -395,6 +464,7 @@ def main():
             "kernel_ms": kernel_ms,
             "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": 13 * args.steps,
             "serving": serve,
+            "pawcs": pawcs,
             "clocks": clk.summary(),
         }
         print(json.dumps(out))

@@ -55,6 +55,10 @@ extern "C" __global__ void pw_k_gw_sort(PwParams P);
 extern "C" __global__ void pw_k_lut_sort(PwParams P, int mode);
 extern "C" __global__ void pw_k_blink_close(PwParams P);
 extern "C" __global__ void pw_k_epilogue(PwParams P);
+extern "C" __global__ void pw_k_ds(PwParams P);
+extern "C" __global__ void pw_k_compact_count(PwParams P, int mode);
+extern "C" __global__ void pw_k_compact_offsets(PwParams P);
+extern "C" __global__ void pw_k_compact_scatter(PwParams P, int mode);
 extern "C" __global__ void pw_k_close(PwParams P);
 extern "C" __global__ void pw_k_refresh_local(PawcsDev S, uint32_t t, int buf, int baseOcc, float decr, int force,
                                               int onlyPending, int useDil);
@@ -492,8 +496,8 @@ enum {
     PL_BLINKS, PL_LASTRAWFG, PL_LASTFG, PL_DILINV, PL_LASTRAWBLINK, PL_LASTCOL, PL_LASTDESC, PL_KCTR, PL_GLUT,
     PL_GMAP, PL_DSLT, PL_DSST, PL_DSROI,
     // scratch (not part of the model)
-    PL_PREFLOOD, PL_COMBINED, PL_LABEL, PL_INTENT, PL_DESCT, PL_REC, PL_OUT, PL_REPB, PL_REPA, PL_UFINAL, PL_CRIT,
-    PL_GITEM, PL_CONTRIB, PL_DSFRAME, PL_FRAME, PL_MASK, PL_ROWSUM, PL_WORK, PL_FLAGS, PL_PDEV, PL_SDEV, PL_COUNT
+    PL_PREFLOOD, PL_COMBINED, PL_LABEL, PL_INTENT, PL_DESCT, PL_REC, PL_OUT, PL_REPB, PL_REPA, PL_UFINAL, PL_UV,
+    PL_ITEMLIST, PL_CONTRIBLIST, PL_BLKCOUNTS, PL_CATINFO, PL_DSABS, PL_GITEM, PL_CONTRIB, PL_DSFRAME, PL_FRAME, PL_MASK, PL_ROWSUM, PL_WORK, PL_FLAGS, PL_PDEV, PL_SDEV, PL_COUNT
 };
 struct PwLayout {
     size_t off[PL_COUNT];
@@ -522,7 +526,12 @@ PwLayout pw_layout(int W, int H, int L, int G) {
     sz[PL_OUT] = npx * sizeof(PwOut);
     sz[PL_REPB] = sz[PL_REPA] = npx * 4;
     sz[PL_UFINAL] = npx;
-    sz[PL_CRIT] = (size_t)H * ((W + 31) / 32) * 4;
+    sz[PL_UV] = npx;
+    sz[PL_ITEMLIST] = npx * 16;
+    sz[PL_CONTRIBLIST] = npx * 4;
+    sz[PL_BLKCOUNTS] = ((npx + kPwCompactBlk - 1) / kPwCompactBlk) * kPwCats * 4;
+    sz[PL_CATINFO] = 64 * 4;
+    sz[PL_DSABS] = std::max<size_t>(nds, 1) * 4;
     sz[PL_GITEM] = npx * 4;
     sz[PL_CONTRIB] = npx * 4;
     sz[PL_DSFRAME] = std::max<size_t>(nds, 1);
@@ -625,7 +634,12 @@ void pw_fill(lvbgs_ctx* h, const PwLayout& Lo, int L, int G) {
     D.repBefore = (uint32_t*)(b + Lo.off[PL_REPB]);
     D.repAfter = (uint32_t*)(b + Lo.off[PL_REPA]);
     D.uFinal = b + Lo.off[PL_UFINAL];
-    D.critBits = (uint32_t*)(b + Lo.off[PL_CRIT]);
+    D.uv = b + Lo.off[PL_UV];
+    D.itemList = (uint4*)(b + Lo.off[PL_ITEMLIST]);
+    D.contribList = (float*)(b + Lo.off[PL_CONTRIBLIST]);
+    D.blkCounts = (uint32_t*)(b + Lo.off[PL_BLKCOUNTS]);
+    D.catInfo = (uint32_t*)(b + Lo.off[PL_CATINFO]);
+    D.dsAbs = (float*)(b + Lo.off[PL_DSABS]);
     D.gitem = (uint32_t*)(b + Lo.off[PL_GITEM]);
     D.contrib = (float*)(b + Lo.off[PL_CONTRIB]);
     D.dsRoi = b + Lo.off[PL_DSROI];
@@ -774,13 +788,21 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
     const int cur = (int)(h->pw_frames & 1ull), nxt = cur ^ 1;
     LV_CUDA(h, cudaMemsetAsync(h->pd.repBefore, 0xff, h->npx * 4, st), "scratch reset");
     LV_CUDA(h, cudaMemsetAsync(h->d_work, 0, sizeof(TickWork), st), "scratch reset");
+    const int cblocks = (int)((h->npx + kPwCompactBlk - 1) / kPwCompactBlk);
+    // ordered compaction: mode 0 lists the critical global items, mode 1 the word weight contributions
+    auto compact = [&](int mode) {
+        pw_k_compact_count<<<cblocks, 256, 0, st>>>(P, mode);
+        pw_k_compact_offsets<<<1, 32 * kPwCats, 0, st>>>(P);
+        pw_k_compact_scatter<<<cblocks, 256, 0, st>>>(P, mode);
+    };
     int round = 0;
     for (;; ++round) {
         if (round >= 64) return fail(h, LVBGS_DEVICE_ERROR, "PAWCS raster-order fixed point did not converge in 64 rounds");
         P.round = round;
         pw_k_local<<<tiles, blk, 0, st>>>(P);
-        pw_k_illum<<<(h->H + 127) / 128, 128, 0, st>>>(P);
+        pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
         pw_k_items<<<tiles, blk, 0, st>>>(P);
+        compact(0);
         pw_k_gscan<<<1, 32, 0, st>>>(P);
         pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
         pw_k_nbr<<<tiles, blk, 0, st>>>(P);
@@ -795,7 +817,8 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
     h->pw_rounds_last = round + 1;
     pw_k_commit<<<tiles, blk, 0, st>>>(P);
     pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 1);
-    pw_k_weights<<<kPwMaxGlobal, 32, 0, st>>>(P);
+    compact(1);
+    pw_k_weights<<<kPwMaxGlobal, 256, 0, st>>>(P);
     pw_k_gw_recalc<<<kPwMaxGlobal, 256, 0, st>>>(P);
     pw_k_gw_decay<<<dim3(64, kPwMaxGlobal), 256, 0, st>>>(P, h->d_rowsum);
     pw_k_gw_blur<<<dim3(64, kPwMaxGlobal), 256, 0, st>>>(P, h->d_rowsum);
@@ -816,7 +839,9 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
     lvbgs_k_combine<<<tiles, blk, 0, st>>>(TP);
     lvbgs_k_median<<<tiles, blk, 0, st>>>(TP);
     lvbgs_k_dilate<<<tiles, blk, 0, st>>>(TP);
-    pw_k_epilogue<<<1, 256, 0, st>>>(P);
+    const int nds = (h->W / 8) * (h->H / 8);
+    if (nds > 0) pw_k_ds<<<(nds + 255) / 256, 256, 0, st>>>(P);
+    pw_k_epilogue<<<1, 32, 0, st>>>(P);
     // automatic model reset (:1503-1508): refreshModel(offset/8, 0, true) and T(x) := 1
     const uint32_t t = (uint32_t)(h->pw_frames + 1);
     if ((s = pw_refresh(h, t, nxt, (int)(h->pw_offset / 8), 0.0f, 1, 1, 1, st)) != LVBGS_OK) return s;

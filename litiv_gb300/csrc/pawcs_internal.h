@@ -96,12 +96,21 @@ struct PawcsDev {
     uint32_t* repBefore;       // latest replacement source before the pixel (kPwNone: none)
     uint32_t* repAfter;        // latest replacement source after the pixel
     uint8_t* uFinal;           // resolved illumination-update bit per pixel
-    uint32_t* critBits;        // bitmap of global items that depend on the replaceable word
     uint32_t* gitem;           // per pixel: type | fixed word | positions
     float* contrib;            // per pixel: weight contribution to its matched global word (or -1)
     uint8_t* dsRoi;            // down-sampled ROI of the frame-level analysis
     uint8_t* dsFrame;          // down-sampled frame
+    uint8_t* uv;               // illumination-update outcomes of the local pass: bit0 mask zero, bit1 non-zero
+    uint4* itemList;           // critical global items in raster order: pixel, colour|bits|fixed pos|fixed word,
+                               // colour threshold|descriptor-bits threshold, descriptor|event flags
+    float* contribList;        // word weight contributions, word-major, raster order within a word
+    uint32_t* blkCounts;       // ordered compaction: per block and category counts, then offsets
+    uint32_t* catInfo;         // [0..16] category totals, [32..48] category bases
+    float* dsAbs;              // |LT - ST| per down-sampled pixel (0 outside the down-sampled ROI)
 };
+
+constexpr int kPwCompactBlk = 1024;  // pixels per block of the ordered compactions
+constexpr int kPwCats = 17;          // compaction categories: 16 global words, or the critical items
 
 // launch parameters of the PAWCS kernels (a table of streams in device memory)
 struct PwParams {

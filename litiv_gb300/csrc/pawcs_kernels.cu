@@ -301,6 +301,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_local(PwParams P) {
         }
     }
     S.descT[p] = (uint16_t)desc;
+    S.uv[p] = (uint8_t)((mark0 ? 1 : 0) | (mark1 ? 2 : 0));
     R.sumW = sumW;
     R.thrW = thrW;
     R.rate = rate;
@@ -316,28 +317,40 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_local(PwParams P) {
 }
 
 // ------------------------------------------------------------------------------------------
-// illumination chain, one row per thread: the mask a pixel sees is 1 when its left neighbour made
-// an illumination update this frame, else its frame-start value (:686-688, :893-894)
+// illumination chain: the mask a pixel sees is 1 when its left neighbour made an illumination update
+// this frame, else its frame-start value (:686-688, :893-894). Each pixel's outcome is a function of
+// its left neighbour's (two states), so one warp per row scans the compositions 32 pixels at a time.
 // ------------------------------------------------------------------------------------------
-extern "C" __global__ void pw_k_illum(PwParams P) {
-    const int gr = blockIdx.x * blockDim.x + threadIdx.x;
+extern "C" __global__ void __launch_bounds__(256) pw_k_illum(PwParams P) {
+    const int gr = blockIdx.x * 8 + (int)threadIdx.x / 32, lane = threadIdx.x & 31;
     if (gr >= P.totalRows) return;
     const PawcsDev& S = P.streams[pw_stream_by_row(P, gr)];
     const StreamDev& D = S.sd;
     const int y = gr - D.rowBase;
-    int prevU = 0;
-    for (int x = 0; x < D.W; ++x) {
+    uint32_t carry = 0;  // outcome of the pixel before the chunk
+    for (int x0 = 0; x0 < D.W; x0 += 32) {
+        const int x = x0 + lane;
         const int p = y * D.W + x;
-        if (!D.roi[p]) {
-            prevU = 0;
-            S.uFinal[p] = 0;
-            continue;
+        const bool in = x < D.W && D.roi[p];
+        uint32_t f = 0, m0 = 0;  // f: bit0 = outcome if the left neighbour made no update, bit1 = if it did
+        if (in) {
+            const uint32_t uvp = S.uv[p];
+            m0 = S.illum[p] != 0;
+            const uint32_t u0 = uvp & 1u, u1 = (uvp >> 1) & 1u;
+            f = (m0 ? u1 : u0) | (u1 << 1);
         }
-        const uint8_t f = S.rec[p].flags;
-        const int mnz = prevU || S.illum[p] != 0;
-        const int u = mnz ? ((f & kRfU1) != 0) : ((f & kRfU0) != 0);
-        S.uFinal[p] = (uint8_t)(u | (mnz << 1));
-        prevU = u;
+        // inclusive scan: F = f_lane o f_lane-1 o ... o f_x0
+        uint32_t F = f;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t o = __shfl_up_sync(0xffffffffu, F, d);
+            if (lane >= d) F = ((F >> (o & 1u)) & 1u) | (((F >> ((o >> 1) & 1u)) & 1u) << 1);
+        }
+        const uint32_t u = (F >> carry) & 1u;
+        uint32_t prevU = __shfl_up_sync(0xffffffffu, u, 1);
+        if (lane == 0) prevU = carry;
+        if (x < D.W) S.uFinal[p] = in ? (uint8_t)(u | ((prevU || m0) ? 2u : 0u)) : (uint8_t)0;
+        carry = __shfl_sync(0xffffffffu, u, 31);
     }
 }
 
@@ -391,89 +404,188 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_items(PwParams P) {
             if (critical) O.gflags |= 4;
         }
     }
-    // bitmap of critical items: one 32-pixel word per warp (tile rows are 32-pixel aligned)
-    const unsigned ball = __ballot_sync(0xffffffffu, critical);
-    if ((threadIdx.x & 31) == 0 && y < D.H) {
-        const int wordsPerRow = (D.W + 31) / 32;
-        if ((x >> 5) < wordsPerRow) S.critBits[(size_t)y * wordsPerRow + (x >> 5)] = ball;
+    (void)critical;
+}
+
+// ------------------------------------------------------------------------------------------
+// ordered compactions (raster order kept): mode 0 lists the critical global items, mode 1 the word
+// weight contributions per word. Blocks of kPwCompactBlk pixels: counts, offsets, scatter.
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ int pw_category(const PawcsDev& S, int p, int mode, int wr, uint32_t nrep) {
+    if (!S.sd.roi[p]) return -1;
+    const PwOut& O = S.out[p];
+    if (mode == 0) return ((S.rec[p].flags & kRfItem) && (O.gflags & 4)) ? 0 : -1;
+    if (S.contrib[p] < 0.0f) return -1;
+    // the replaceable word keeps only the contributions after its last replacement of the frame
+    if (O.gword >= (uint32_t)S.G) return -1;
+    if ((int)O.gword == wr && nrep > 0 && O.epoch != nrep) return -1;
+    return (int)O.gword;
+}
+
+extern "C" __global__ void __launch_bounds__(256) pw_k_compact_count(PwParams P, int mode) {
+    const PawcsDev& S = P.streams[0];
+    const int nb = (S.sd.npx + kPwCompactBlk - 1) / kPwCompactBlk;
+    if ((int)blockIdx.x >= nb) return;
+    __shared__ uint32_t cnt[kPwCats];
+    if (threadIdx.x < kPwCats) cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int wr = S.pc->gdict[S.G - 1];
+    const uint32_t nrep = S.pc->n_repl;
+    for (int k = 0; k < kPwCompactBlk / 256; ++k) {
+        const int p = blockIdx.x * kPwCompactBlk + k * 256 + threadIdx.x;
+        if (p < S.sd.npx) {
+            const int c = pw_category(S, p, mode, wr, nrep);
+            if (c >= 0) atomicAdd(&cnt[c], 1u);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < kPwCats) S.blkCounts[(size_t)blockIdx.x * kPwCats + threadIdx.x] = cnt[threadIdx.x];
+}
+
+// per category (one warp each): exclusive offsets over the blocks (in place), totals and the
+// category bases of the word-major list
+extern "C" __global__ void __launch_bounds__(32 * kPwCats) pw_k_compact_offsets(PwParams P) {
+    const PawcsDev& S = P.streams[0];
+    const int nb = (S.sd.npx + kPwCompactBlk - 1) / kPwCompactBlk;
+    __shared__ uint32_t tot[kPwCats];
+    const int c = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t run = 0;
+    for (int b0 = 0; b0 < nb; b0 += 32) {
+        const int b = b0 + lane;
+        uint32_t* e = &S.blkCounts[(size_t)b * kPwCats + c];
+        const uint32_t v = b < nb ? *e : 0u;
+        uint32_t inc = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t o = __shfl_up_sync(0xffffffffu, inc, d);
+            if (lane >= d) inc += o;
+        }
+        if (b < nb) *e = run + inc - v;
+        run += __shfl_sync(0xffffffffu, inc, 31);
+    }
+    if (lane == 0) {
+        tot[c] = run;
+        S.catInfo[c] = run;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t base = 0;
+        for (int k = 0; k < kPwCats; ++k) {
+            S.catInfo[32 + k] = base;
+            base += tot[k];
+        }
+    }
+}
+
+extern "C" __global__ void __launch_bounds__(256) pw_k_compact_scatter(PwParams P, int mode) {
+    const PawcsDev& S = P.streams[0];
+    const StreamDev& D = S.sd;
+    const int nb = (D.npx + kPwCompactBlk - 1) / kPwCompactBlk;
+    if ((int)blockIdx.x >= nb) return;
+    __shared__ uint32_t warpCnt[8][kPwCats];
+    __shared__ uint32_t run[kPwCats], passTot[kPwCats];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int wr = S.pc->gdict[S.G - 1];
+    const uint32_t nrep = S.pc->n_repl;
+    if (threadIdx.x < kPwCats)
+        run[threadIdx.x] = S.catInfo[32 + threadIdx.x] + S.blkCounts[(size_t)blockIdx.x * kPwCats + threadIdx.x];
+    const float* fm = D.fm + (size_t)(D.ctl->frame_idx & 1ull) * kNumFloatMaps * D.npx;
+    for (int k = 0; k < kPwCompactBlk / 256; ++k) {
+        const int p = blockIdx.x * kPwCompactBlk + k * 256 + threadIdx.x;
+        const int c = p < D.npx ? pw_category(S, p, mode, wr, nrep) : -1;
+        uint32_t rank = 0;
+        const int ncat = mode == 0 ? 1 : S.G;
+        for (int j = 0; j < ncat; ++j) {
+            const unsigned m = __ballot_sync(0xffffffffu, c == j);
+            if (c == j) rank = __popc(m & ((1u << lane) - 1u));
+            if (lane == 0) warpCnt[w][j] = __popc(m);
+        }
+        __syncthreads();
+        if (threadIdx.x < ncat) {
+            // exclusive offsets of the warps within this pass, then the pass total
+            uint32_t r = 0;
+            for (int i = 0; i < 8; ++i) {
+                const uint32_t v = warpCnt[i][threadIdx.x];
+                warpCnt[i][threadIdx.x] = r;
+                r += v;
+            }
+            passTot[threadIdx.x] = r;
+        }
+        __syncthreads();
+        if (c >= 0) {
+            const uint32_t pos = run[c] + warpCnt[w][c] + rank;
+            if (mode == 0) {
+                const PwRec& R = S.rec[p];
+                const PwThr th = pw_thresholds(fm[FM_R * D.npx + p], S.unstable[p], S.minColor, S.descOff);
+                const uint32_t g = S.gitem[p];
+                const uint32_t a = (uint32_t)D.frame[p] | ((uint32_t)R.bits << 8) | (((g >> 6) & 63u) << 16) |
+                                   ((g & 63u) << 24);
+                const uint32_t b = min(th.color, 65535u) | (min(th.desc / 4u, 65535u) << 16);
+                const uint32_t d = (uint32_t)S.descT[p] | ((uint32_t)(R.flags & (kRfEvent | kRfRepDraw)) << 16);
+                S.itemList[pos] = make_uint4((uint32_t)p, a, b, d);
+            } else {
+                S.contribList[pos] = S.contrib[p];
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < ncat) run[threadIdx.x] += passTot[threadIdx.x];
+        __syncthreads();
     }
 }
 
 // ordered scan of the items that depend on the replaceable word (one warp per stream): the
-// replaceable word's features evolve with each replacement (:776-786)
+// replaceable word's features change with each replacement (:776-786). Each chunk of 32 items is
+// settled in parallel against the current features up to the first item that replaces the word,
+// which then becomes the features the rest of the chunk is matched against.
 extern "C" __global__ void pw_k_gscan(PwParams P) {
     const int si = blockIdx.x;
     if (si >= P.nStreams) return;
     const PawcsDev& S = P.streams[si];
-    const StreamDev& D = S.sd;
     PawcsCtl* pc = S.pc;
     const int lane = threadIdx.x;
     const int G = S.G;
     const int wr = pc->gdict[G - 1];
     uint32_t wrColor = pc->gw_color[wr], wrDesc = pc->gw_desc[wr], wrBits = pc->gw_bits[wr];
     uint32_t epoch = 0;
-    const int wordsPerRow = (D.W + 31) / 32;
-    const size_t nWords = (size_t)wordsPerRow * D.H;
-    const float* fm = D.fm + (size_t)(D.ctl->frame_idx & 1ull) * kNumFloatMaps * D.npx;
-    for (size_t base = 0; base < nWords; base += 32) {
-        const size_t wi = base + lane;
-        uint32_t bitsWord = wi < nWords ? S.critBits[wi] : 0u;
-        unsigned pending = __ballot_sync(0xffffffffu, bitsWord != 0u);
-        while (pending) {
-            const int src = __ffs(pending) - 1;
-            pending &= pending - 1;
-            uint32_t bw = __shfl_sync(0xffffffffu, bitsWord, src);
-            const size_t wsrc = base + src;
-            const int y = (int)(wsrc / wordsPerRow), x0 = (int)(wsrc % wordsPerRow) * 32;
-            // the lanes fetch the word's items in parallel
-            const int myBit = lane;
-            const bool has = (bw >> myBit) & 1u;
-            const int p = y * D.W + x0 + myBit;
-            uint32_t col = 0, bits = 0, gi = 0, cthr = 0, dthr = 0, fl = 0, desc = 0;
-            if (has) {
-                col = D.frame[p];
-                bits = S.rec[p].bits;
-                fl = S.rec[p].flags;
-                gi = S.gitem[p];
-                desc = S.descT[p];
-                const PwThr th = pw_thresholds(fm[FM_R * D.npx + p], S.unstable[p], S.minColor, S.descOff);
-                cthr = th.color;
-                dthr = th.desc;
+    const uint32_t n = S.catInfo[0];
+    uint4 nextIt = lane < (int)n ? S.itemList[lane] : make_uint4(0, 0, 0, 0);
+    for (uint32_t base = 0; base < n; base += 32) {
+        const uint4 it = nextIt;
+        if (base + 32 + lane < n) nextIt = S.itemList[base + 32 + lane];  // prefetch the next chunk
+        const int cnt = (int)min(32u, n - base);
+        const bool valid = lane < cnt;
+        const uint32_t col = it.y & 255u, bits = (it.y >> 8) & 255u, fixedPos = (it.y >> 16) & 255u;
+        const uint32_t fixedWord = it.y >> 24, cthr = it.z & 65535u, dq = it.z >> 16;
+        const bool evRep = ((it.w >> 16) & kRfEvent) && ((it.w >> 16) & kRfRepDraw);
+        uint32_t myWord = kPwNone, myEpoch = 0, myRepl = 0;
+        int cursor = 0;
+        while (cursor < cnt) {
+            const bool mWr = pw_absdiff(wrColor, col) <= cthr && pw_absdiff(bits, wrBits) <= dq;
+            const bool repl = valid && !mWr && (int)fixedPos >= G && evRep;
+            const unsigned cand = __ballot_sync(0xffffffffu, repl && lane >= cursor);
+            const int stop = cand ? __ffs(cand) - 1 : cnt;  // the first replacing item, or the chunk end
+            if (lane >= cursor && lane < stop) {
+                myWord = mWr ? (uint32_t)wr : ((int)fixedPos < G ? fixedWord : kPwNone);
+                myEpoch = epoch;
             }
-            while (bw) {
-                const int j = __ffs(bw) - 1;
-                bw &= bw - 1;
-                const uint32_t jc = __shfl_sync(0xffffffffu, col, j), jb = __shfl_sync(0xffffffffu, bits, j);
-                const uint32_t jg = __shfl_sync(0xffffffffu, gi, j), jf = __shfl_sync(0xffffffffu, fl, j);
-                const uint32_t jct = __shfl_sync(0xffffffffu, cthr, j), jdt = __shfl_sync(0xffffffffu, dthr, j);
-                const uint32_t jd = __shfl_sync(0xffffffffu, desc, j);
-                if (lane == 0) {
-                    const int pj = y * D.W + x0 + j;
-                    PwOut& O = S.out[pj];
-                    const bool mWr = pw_absdiff(wrColor, jc) <= jct && pw_absdiff(jb, wrBits) <= jdt / 4u;
-                    const int fixedPos = (int)((jg >> 6) & 63u);
-                    const int fixedWord = (int)(jg & 63u);
-                    if (mWr) {
-                        O.gword = (uint32_t)wr;
-                    } else if (fixedPos < G) {
-                        O.gword = (uint32_t)fixedWord;
-                    } else if ((jf & kRfEvent) && (jf & kRfRepDraw)) {
-                        wrColor = jc;
-                        wrDesc = jd;
-                        wrBits = jb;
-                        ++epoch;
-                        O.gword = (uint32_t)wr;
-                        O.gflags |= 1;
-                    } else {
-                        O.gword = kPwNone;
-                    }
-                    O.epoch = epoch;
+            if (stop < cnt) {
+                ++epoch;
+                if (lane == stop) {
+                    myWord = (uint32_t)wr;
+                    myEpoch = epoch;
+                    myRepl = 1;
                 }
-                epoch = __shfl_sync(0xffffffffu, epoch, 0);
-                wrColor = __shfl_sync(0xffffffffu, wrColor, 0);
-                wrDesc = __shfl_sync(0xffffffffu, wrDesc, 0);
-                wrBits = __shfl_sync(0xffffffffu, wrBits, 0);
+                wrColor = __shfl_sync(0xffffffffu, col, stop);
+                wrDesc = __shfl_sync(0xffffffffu, it.w & 65535u, stop);
+                wrBits = __shfl_sync(0xffffffffu, bits, stop);
             }
+            cursor = stop + 1;
+        }
+        if (valid) {
+            PwOut& O = S.out[it.x];
+            O.gword = myWord;
+            O.epoch = myEpoch;
+            if (myRepl) O.gflags |= 1;
         }
     }
     if (lane == 0) {
@@ -848,40 +960,30 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_commit(PwParams P) {
     if ((threadIdx.x & 31) == 0 && b) atomicAdd(&S.pc->nflat_acc, (unsigned long long)__popc(b));
 }
 
-// global word weights (:789-790): ordered float sums of the frame's contributions, one warp per
-// (stream, word); the replaceable word restarts from zero at the frame's last replacement
-extern "C" __global__ void pw_k_weights(PwParams P) {
+// global word weights (:789-790): ordered float sums of the frame's contributions, one block per
+// (stream, word) over the word's compacted list; the replaceable word restarts from zero at the
+// frame's last replacement (its list holds only the contributions after it)
+extern "C" __global__ void __launch_bounds__(256) pw_k_weights(PwParams P) {
     const int si = blockIdx.x / kPwMaxGlobal, w = blockIdx.x % kPwMaxGlobal;
     if (si >= P.nStreams) return;
     const PawcsDev& S = P.streams[si];
     if (w >= S.G) return;
-    const StreamDev& D = S.sd;
     PawcsCtl* pc = S.pc;
-    const int lane = threadIdx.x;
     const int wr = pc->gdict[S.G - 1];
     const uint32_t nrep = pc->n_repl;
     const bool isWr = w == wr;
+    const uint32_t n = S.catInfo[w], base = S.catInfo[32 + w];
+    __shared__ float buf[1024];
     float acc = (isWr && nrep > 0) ? 0.0f : pc->gw_weight[w];
-    for (int base = 0; base < D.npx; base += 32) {
-        const int p = base + lane;
-        float v = -1.0f;
-        bool mine = false;
-        if (p < D.npx && D.roi[p]) {
-            v = S.contrib[p];
-            if (v >= 0.0f) {
-                const PwOut& O = S.out[p];
-                mine = O.gword == (uint32_t)w && (!isWr || nrep == 0 || O.epoch == nrep);
-            }
-        }
-        unsigned m = __ballot_sync(0xffffffffu, mine);
-        while (m) {
-            const int j = __ffs(m) - 1;
-            m &= m - 1;
-            const float vj = __shfl_sync(0xffffffffu, v, j);
-            acc = acc + vj;
-        }
+    for (uint32_t c0 = 0; c0 < n; c0 += 1024) {
+        const uint32_t cnt = min(1024u, n - c0);
+        for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) buf[i] = S.contribList[base + c0 + i];
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (uint32_t i = 0; i < cnt; ++i) acc = acc + buf[i];
+        __syncthreads();
     }
-    if (lane == 0) {
+    if (threadIdx.x == 0) {
         pc->gw_weight[w] = acc;
         if (isWr && nrep > 0) {
             pc->gw_color[w] = pc->wr_color;
@@ -1088,6 +1190,32 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_blink_close(PwParams P) {
     D.preflood[q] = v;
 }
 
+// down-sampled frame (INTER_AREA, integral scale), its rolling averages (accumulateWeighted) and the
+// per-pixel |LT - ST| of the motion analysis (:1475-1478); one thread per down-sampled pixel
+extern "C" __global__ void pw_k_ds(PwParams P) {
+    const PawcsDev& S = P.streams[0];
+    const StreamDev& D = S.sd;
+    const int nds = D.dsW * D.dsH;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nds) return;
+    const uint32_t t = (uint32_t)(D.ctl->frame_idx + 1ull);
+    float fLT, fST;
+    pw_factors(t, (int)S.nmv, &fLT, &fST);
+    const int bx = i % D.dsW, by = i / D.dsW;
+    int sum = 0;
+    for (int yy = 0; yy < D.dsSY; ++yy)
+        for (int xx = 0; xx < D.dsSX; ++xx) sum += D.frame[(size_t)(by * D.dsSY + yy) * D.W + bx * D.dsSX + xx];
+    const float scale = 1.f / (float)(D.dsSX * D.dsSY);
+    const int r = __float2int_rn((float)sum * scale);
+    const uint8_t vb = (uint8_t)(r < 0 ? 0 : r > 255 ? 255 : r);
+    const float lt = (float)vb * fLT + D.dsLT[i] * (1.0f - fLT);
+    const float st = (float)vb * fST + D.dsST[i] * (1.0f - fST);
+    D.dsLT[i] = lt;
+    D.dsST[i] = st;
+    S.dsFrame[i] = vb;
+    S.dsAbs[i] = S.dsRoi[i] ? fabsf(lt - st) : 0.0f;
+}
+
 // ------------------------------------------------------------------------------------------
 // frame level (:1462-1516): LBSP threshold LUT, camera-motion analysis, automatic model reset
 // decision; one block per stream
@@ -1103,31 +1231,12 @@ extern "C" __global__ void pw_k_epilogue(PwParams P) {
     const int boot = t <= (uint32_t)kBootWin;
     float fLT, fST;
     pw_factors(t, (int)S.nmv, &fLT, &fST);
-    // down-sampled frame (INTER_AREA, integral scale) and its rolling averages
-    const int dw = D.dsW, dh = D.dsH;
-    const int nds = dw * dh;
-    for (int i = threadIdx.x; i < nds; i += blockDim.x) {
-        const int bx = i % dw, by = i / dw;
-        int sum = 0;
-        for (int yy = 0; yy < D.dsSY; ++yy)
-            for (int xx = 0; xx < D.dsSX; ++xx) sum += D.frame[(size_t)(by * D.dsSY + yy) * D.W + bx * D.dsSX + xx];
-        const float scale = 1.f / (float)(D.dsSX * D.dsSY);
-        const float v = (float)__float2int_rn((float)sum * scale);
-        const uint8_t vb = (uint8_t)(v < 0.f ? 0.f : v > 255.f ? 255.f : v);
-        const float a = fLT, b = 1.0f - fLT;
-        const float lt = (float)vb * a + D.dsLT[i] * b;
-        const float a2 = fST, b2 = 1.0f - fST;
-        const float st = (float)vb * a2 + D.dsST[i] * b2;
-        D.dsLT[i] = lt;
-        D.dsST[i] = st;
-        S.dsFrame[i] = vb;
-    }
-    __syncthreads();
     if (threadIdx.x != 0) return;
+    const int nds = D.dsW * D.dsH;
+    (void)fST;
     // ordered float sum of |LT - ST| over the down-sampled ROI (lv::L1dist, math.hpp:255-268)
     float l1 = 0.0f;
-    for (int i = 0; i < nds; ++i)
-        if (S.dsRoi[i]) l1 = l1 + fabsf(D.dsLT[i] - D.dsST[i]);
+    for (int i = 0; i < nds; ++i) l1 = l1 + S.dsAbs[i];
     const float ratio = l1 / (float)pc->ds_roi_count;
     pc->frame_ratio = ratio;
     // LBSP threshold LUT (:1462-1473)

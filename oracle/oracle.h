@@ -1,16 +1,17 @@
 /* ORACLE (test infrastructure only; never linked into the product library).
  *
- * CPU restatement of the reference's SuBSENSE per-pixel background subtraction
- * (plstcharles/litiv, modules/video/src/BackgroundSubtractorSuBSENSE.cpp) and of
- * the LBSP descriptor (modules/features2d/include/litiv/features2d/LBSP.hpp).
+ * CPU restatement of the reference's SuBSENSE and PAWCS per-pixel background
+ * subtraction (plstcharles/litiv, modules/video/src/BackgroundSubtractorSuBSENSE.cpp,
+ * BackgroundSubtractorPAWCS.cpp) and of the LBSP descriptor
+ * (modules/features2d/include/litiv/features2d/LBSP.hpp).
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it,
  * always as the checker.
  *
  * Parity pins: the LBSP descriptor is pinned by the reference's golden vector
  * (modules/features2d/test/data/test_lbsp.bin, see tests/golden/). The rest of
  * the path has no golden vectors in the reference and the reference itself
- * cannot be built here (it needs OpenCV, which is absent), so the SuBSENSE
- * model state, masks and the OpenCV image operations it calls are "parity
+ * cannot be built here (it needs OpenCV, which is absent), so the SuBSENSE and
+ * PAWCS model state, masks and the OpenCV image operations they call are "parity
  * unpinned" against the real reference; each function cites the reference
  * lines it restates and states the OpenCV definition it uses.
  */
@@ -159,6 +160,12 @@ void opawcs_get_scalars(const opawcs_t* o, opawcs_scalars* s);
 double orun_streams(int n_streams, const uint8_t* const* frames, const int* n_frames,
                     const int* widths, const int* heights, const int* channels,
                     const uint64_t* seeds, int n_threads, uint8_t* const* last_masks);
+
+/* CPU baseline for PAWCS: as orun_streams, timing the apply phase only (after every instance is
+ * initialized) */
+double orun_pawcs_streams(int n_streams, const uint8_t* const* frames, const int* n_frames,
+                          const int* widths, const int* heights, const int* channels,
+                          const uint64_t* seeds, int n_threads);
 
 #ifdef __cplusplus
 }

@@ -89,6 +89,9 @@ def lib():
         L.oneighbor_pos.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
                                     C.POINTER(C.c_int)]
         L.ophilox_block.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.orun_pawcs_streams.restype = C.c_double
+        L.orun_pawcs_streams.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                         C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_uint64), C.c_int]
         L.orun_streams.restype = C.c_double
         L.orun_streams.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                    C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_uint64), C.c_int,
@@ -300,3 +303,16 @@ def run_streams(frames_list, seeds, n_threads):
     cs = (C.c_int * n)(*[(a.shape[3] if a.ndim == 4 else 1) for a in arrs])
     sd = (C.c_uint64 * n)(*seeds)
     return lib().orun_streams(n, ptrs, nf, ws, hs, cs, sd, int(n_threads), None)
+
+
+def run_pawcs_streams(frames_list, seeds, n_threads):
+    """PAWCS CPU baseline: frames_list[i] is uint8 [F, H, W]; returns wall seconds of the apply phase."""
+    n = len(frames_list)
+    arrs = [np.ascontiguousarray(f) for f in frames_list]
+    ptrs = (C.c_void_p * n)(*[a.ctypes.data for a in arrs])
+    nf = (C.c_int * n)(*[a.shape[0] for a in arrs])
+    ws = (C.c_int * n)(*[a.shape[2] for a in arrs])
+    hs = (C.c_int * n)(*[a.shape[1] for a in arrs])
+    cs = (C.c_int * n)(*[(a.shape[3] if a.ndim == 4 else 1) for a in arrs])
+    sd = (C.c_uint64 * n)(*seeds)
+    return lib().orun_pawcs_streams(n, ptrs, nf, ws, hs, cs, sd, int(n_threads))

@@ -1,6 +1,6 @@
-/* ORACLE (test infrastructure only): CPU baseline driver.
+/* ORACLE (test infrastructure only): CPU baseline drivers.
  *
- * Runs independent SuBSENSE instances, one per stream, on a pool of worker
+ * Run independent SuBSENSE / PAWCS instances, one per stream, on a pool of worker
  * threads, the same per-sequence parallelism as lv::WorkerPool in
  * apps/changedet/src/main.cpp:148-154 (one instance per core across streams).
  */
@@ -57,5 +57,66 @@ double orun_streams(int n_streams, const uint8_t* const* frames, const int* n_fr
     for (int t = 0; t < n_threads; ++t) pthread_join(th[t], NULL);
     clock_gettime(CLOCK_MONOTONIC, &t1);
     free(th);
+    return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}
+
+/* PAWCS: thread k initializes streams k, k+T, ... then, after a barrier, applies their frames; the
+ * returned time covers the apply phase only (PAWCS's model initialization is much heavier than a
+ * frame and is not part of the per-frame throughput). */
+typedef struct {
+    job_t* j;
+    int tid, nth;
+    pthread_barrier_t* bar;
+} pjob_t;
+
+static void* pworker(void* arg) {
+    pjob_t* pj = (pjob_t*)arg;
+    job_t* j = pj->j;
+    int mine = 0;
+    for (int i = pj->tid; i < j->n; i += pj->nth) ++mine;
+    opawcs_t** os = (opawcs_t**)calloc((size_t)(mine > 0 ? mine : 1), sizeof(opawcs_t*));
+    int m = 0;
+    for (int i = pj->tid; i < j->n; i += pj->nth, ++m) {
+        opawcs_params p;
+        opawcs_default_params(&p);
+        p.seed = j->seeds[i];
+        os[m] = opawcs_create(&p);
+        opawcs_initialize(os[m], j->frames[i], j->w[i], j->h[i], j->c[i], NULL);
+    }
+    pthread_barrier_wait(pj->bar);
+    m = 0;
+    for (int i = pj->tid; i < j->n; i += pj->nth, ++m) {
+        const size_t fb = (size_t)j->w[i] * j->h[i] * j->c[i];
+        uint8_t* mask = (uint8_t*)malloc((size_t)j->w[i] * j->h[i]);
+        for (int f = 1; f < j->nf[i]; ++f) opawcs_apply(os[m], j->frames[i] + (size_t)f * fb, mask, 0.0);
+        free(mask);
+    }
+    pthread_barrier_wait(pj->bar);
+    for (int k = 0; k < mine; ++k) opawcs_destroy(os[k]);
+    free(os);
+    return NULL;
+}
+
+double orun_pawcs_streams(int n_streams, const uint8_t* const* frames, const int* n_frames, const int* widths,
+                          const int* heights, const int* channels, const uint64_t* seeds, int n_threads) {
+    job_t j = {n_streams, frames, n_frames, widths, heights, channels, seeds, NULL, 0, PTHREAD_MUTEX_INITIALIZER};
+    if (n_threads < 1) n_threads = 1;
+    pthread_barrier_t bar;
+    pthread_barrier_init(&bar, NULL, (unsigned)n_threads + 1);
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)n_threads);
+    pjob_t* pj = (pjob_t*)malloc(sizeof(pjob_t) * (size_t)n_threads);
+    for (int t = 0; t < n_threads; ++t) {
+        pj[t] = (pjob_t){&j, t, n_threads, &bar};
+        pthread_create(&th[t], NULL, pworker, &pj[t]);
+    }
+    struct timespec t0, t1;
+    pthread_barrier_wait(&bar);
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    pthread_barrier_wait(&bar);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    for (int t = 0; t < n_threads; ++t) pthread_join(th[t], NULL);
+    pthread_barrier_destroy(&bar);
+    free(th);
+    free(pj);
     return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
 }

@@ -143,3 +143,9 @@ def test_api_errors():
         b.refreshModel(1, 1.5)
     with pytest.raises(LvException):
         BackgroundSubtractorPAWCS(nMaxNbWords=1)
+
+
+def test_config2_full_size_prefix():
+    # the benchmark scene itself (640x480 thermal-like), first frames, every mask and the final state
+    s = SyntheticStream(2, 0, 1)
+    run_pair([s.render(t) for t in range(12)], seed=1, check_every=11)
