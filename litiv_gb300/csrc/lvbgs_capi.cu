@@ -56,6 +56,9 @@ extern "C" __global__ void pw_k_lut_sort(PwParams P, int mode);
 extern "C" __global__ void pw_k_blink_close(PwParams P);
 extern "C" __global__ void pw_k_epilogue(PwParams P);
 extern "C" __global__ void pw_k_ds(PwParams P);
+extern "C" __global__ void pw_k_reset_decide(PwParams P);
+extern "C" __global__ void pw_k_motion_bg(PwParams P, int buf);
+extern "C" __global__ void pw_k_motion_decide(PwParams P);
 extern "C" __global__ void pw_k_compact_count(PwParams P, int mode);
 extern "C" __global__ void pw_k_compact_offsets(PwParams P);
 extern "C" __global__ void pw_k_compact_scatter(PwParams P, int mode);
@@ -842,8 +845,22 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
     const int nds = (h->W / 8) * (h->H / 8);
     if (nds > 0) pw_k_ds<<<(nds + 255) / 256, 256, 0, st>>>(P);
     pw_k_epilogue<<<1, 32, 0, st>>>(P);
-    // automatic model reset (:1503-1508): refreshModel(offset/8, 0, true) and T(x) := 1
     const uint32_t t = (uint32_t)(h->pw_frames + 1);
+    if (nds > 0 && t % kPwBootWin == 0) {
+        // camera-motion comparison (:1480-1501): the host waits for the decision, which may switch the
+        // local word weight offset and run refreshModel(1, 1, true)
+        pw_k_motion_bg<<<(nds + 255) / 256, 256, 0, st>>>(P, nxt);
+        pw_k_motion_decide<<<1, 32, 0, st>>>(P);
+        LV_CUDA(h, cudaGetLastError(), "PAWCS camera-motion launch");
+        LV_CUDA(h, cudaMemcpyAsync(h->h_flags + 1, h->d_flags + 1, 8, cudaMemcpyDeviceToHost, st), "flag read-back");
+        LV_CUDA(h, cudaStreamSynchronize(st), "PAWCS camera-motion decision");
+        if (h->h_flags[1]) {
+            h->pw_offset = h->h_flags[2];
+            if ((s = pw_refresh(h, t, nxt, 1, 1.0f, 1, 0, 1, st)) != LVBGS_OK) return s;
+        }
+    }
+    pw_k_reset_decide<<<1, 32, 0, st>>>(P);
+    // automatic model reset (:1503-1508): refreshModel(offset/8, 0, true) and T(x) := 1
     if ((s = pw_refresh(h, t, nxt, (int)(h->pw_offset / 8), 0.0f, 1, 1, 1, st)) != LVBGS_OK) return s;
     pw_k_reset_T<<<256, 256, 0, st>>>(h->pd, nxt);
     pw_k_close<<<1, 32, 0, st>>>(P);

@@ -45,8 +45,9 @@ struct PawcsCtl {
     unsigned int n_rounds, n_dirty;           // fixed-point rounds of the frame, dirty pixels left
     unsigned long long st_words, st_events, st_nb;
     float frame_ratio;                   // mean L1 distance ratio of the frame-level analysis
-    int reset_pending;                   // automatic reset decided this frame: 1 reset, 2/3 moving camera on/off
-    int pad;
+    int reset_pending;                   // automatic reset decided this frame
+    int reset_block;                     // the frame entered the reset / camera-motion block (:1479)
+    int motion_pending;                  // camera-motion mode switched this frame (refreshModel(1, 1, true))
 };
 
 // per-pixel record of the local pass of one frame
@@ -111,6 +112,7 @@ struct PawcsDev {
 
 constexpr int kPwCompactBlk = 1024;  // pixels per block of the ordered compactions
 constexpr int kPwCats = 17;          // compaction categories: 16 global words, or the critical items
+constexpr int kPwBootWin = 500;      // BGSPAWCS bootstrap window (frames)
 
 // launch parameters of the PAWCS kernels (a table of streams in device memory)
 struct PwParams {

@@ -24,7 +24,7 @@ __constant__ int pw_nb5[24][2] = {{-2, 2}, {-1, 2}, {0, 2},   {1, 2},   {2, 2}, 
 
 constexpr float kTLower = 1.0f, kTUpper = 256.0f, kTIncr = 0.5f, kTDecr = 0.25f;
 constexpr float kVIncr = 1.0f, kVDecr = 0.1f, kRVar = 0.01f, kUnstRatio = 0.1f, kUnstR = 3.0f;
-constexpr int kBootWin = 500;
+constexpr int kBootWin = kPwBootWin;
 
 __device__ __forceinline__ int pw_stream_by_tile(const PwParams& P, int t) {
     int lo = 0, hi = P.nStreams - 1;
@@ -1260,10 +1260,24 @@ extern "C" __global__ void pw_k_epilogue(PwParams P) {
     pc->last_nonflat_ratio = nonflat;
     pc->nflat_acc = 0;
     pc->reset_pending = 0;
-    // automatic model reset (:1479-1513); the moving-camera comparison of frames 500, 1000, ...
-    // runs in pw_k_motion before this kernel
+    // automatic model reset (:1479-1513): the block is entered when the reset is enabled or the camera
+    // moves; the camera-motion comparison of frames 500, 1000, ... (pw_k_motion_*) and the reset decision
+    // (pw_k_reset_decide) follow
     if (!ctl->auto_reset && ratio >= 45.0f * 2) ctl->auto_reset = 1;
-    if (ctl->auto_reset || pc->moving_cam) {
+    pc->reset_block = ctl->auto_reset || pc->moving_cam;
+}
+
+// reset decision of the frame-level block (:1509-1513)
+extern "C" __global__ void pw_k_reset_decide(PwParams P) {
+    const int si = blockIdx.x;
+    if (si >= P.nStreams || threadIdx.x != 0) return;
+    const PawcsDev& S = P.streams[si];
+    StreamCtl* ctl = S.sd.ctl;
+    PawcsCtl* pc = S.pc;
+    const uint32_t t = (uint32_t)(ctl->frame_idx + 1ull);
+    const int boot = t <= (uint32_t)kBootWin;
+    const float ratio = pc->frame_ratio;
+    if (pc->reset_block) {
         if (ctl->frames_since_reset > (unsigned long long)kBootWin * 2) {
             ctl->auto_reset = 0;
         } else if (ratio >= 45.0f && ctl->cooldown == 0) {
@@ -1533,6 +1547,75 @@ extern "C" __global__ void pw_k_init_last(PawcsDev S, const uint8_t* img) {
         D.lastCol[p] = c;
         D.lastDesc[p] = d;
     }
+}
+
+// camera-motion comparison (:1480-1501), frames t with t % 500 == 0: the background image of the words
+// of buffer buf, area-down-sampled like the frame, against the long-term mean of the down-sampled
+// frames; one thread per down-sampled pixel writes |LT - BG| (0 outside the fully covered blocks)
+extern "C" __global__ void pw_k_motion_bg(PwParams P, int buf) {
+    const PawcsDev& S = P.streams[0];
+    const StreamDev& D = S.sd;
+    const int nds = D.dsW * D.dsH;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nds) return;
+    if (S.dsRoi[i] != 255) {
+        S.dsAbs[i] = 0.0f;
+        return;
+    }
+    const uint32_t t = (uint32_t)(D.ctl->frame_idx + 1ull);
+    const unsigned long long off = S.pc->lword_offset;
+    const int bx = i % D.dsW, by = i / D.dsW;
+    int sum = 0;
+    for (int yy = 0; yy < D.dsSY; ++yy)
+        for (int xx = 0; xx < D.dsSX; ++xx) {
+            const int p = (by * D.dsSY + yy) * D.W + bx * D.dsSX + xx;
+            if (!D.roi[p]) continue;
+            float tw = 0.0f, tc = 0.0f;
+            for (int j = 0; j < S.L; ++j) {
+                const size_t a = pw_slot(S, buf, j, p);
+                const float w = pw_weight(S.wOcc[a], S.wFirst[a], S.wLast[a], t, off);
+                tc = tc + (float)S.wColor[a] * w;
+                tw = tw + w;
+            }
+            const int r = __float2int_rn(tc / tw);
+            sum += r < 0 ? 0 : r > 255 ? 255 : r;
+        }
+    const float scale = 1.f / (float)(D.dsSX * D.dsSY);
+    const int r = __float2int_rn((float)sum * scale);
+    const uint8_t v = (uint8_t)(r < 0 ? 0 : r > 255 ? 255 : r);
+    S.dsAbs[i] = fabsf(D.dsLT[i] - (float)v);
+}
+
+// camera-motion decision: ordered L1 sum, then switch the mode on (during the bootstrap window, ratio
+// >= 45) or off (ratio < 45/4) with the local word weight offset (5 / 1000); flags[1] tells the host
+// to run refreshModel(1, 1, true), flags[2] carries the new offset. One grayscale channel: the colour
+// distance ratio is 0.
+extern "C" __global__ void pw_k_motion_decide(PwParams P) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const PawcsDev& S = P.streams[0];
+    const StreamDev& D = S.sd;
+    PawcsCtl* pc = S.pc;
+    pc->motion_pending = 0;
+    if (pc->reset_block) {
+        const uint32_t t = (uint32_t)(D.ctl->frame_idx + 1ull);
+        const int boot = t <= (uint32_t)kBootWin;
+        const int nds = D.dsW * D.dsH;
+        float l1 = 0.0f;
+        for (int i = 0; i < nds; ++i) l1 = l1 + S.dsAbs[i];
+        const float mr = l1 / (float)pc->ds_roi_count;
+        const float cr = 0.0f;
+        if (pc->moving_cam && mr < (float)(45 / 4) && cr < (float)(45 / 10 / 4)) {
+            pc->lword_offset = (unsigned long long)kBootWin * 2;
+            pc->moving_cam = 0;
+            pc->motion_pending = 1;
+        } else if (boot && !pc->moving_cam && (mr >= 45.0f || cr >= (float)(45 / 10))) {
+            pc->lword_offset = 5;
+            pc->moving_cam = 1;
+            pc->motion_pending = 1;
+        }
+    }
+    P.flags[1] = (unsigned int)pc->motion_pending;
+    P.flags[2] = (unsigned int)pc->lword_offset;
 }
 
 // background image (:1518-1545) / descriptors (:1547-1594) from the words of buffer buf

@@ -149,3 +149,33 @@ def test_config2_full_size_prefix():
     # the benchmark scene itself (640x480 thermal-like), first frames, every mask and the final state
     s = SyntheticStream(2, 0, 1)
     run_pair([s.render(t) for t in range(12)], seed=1, check_every=11)
+
+
+def test_moving_camera_mode_switch():
+    # frames 150-450 darken the scene by 120 levels while an infinite learning-rate override freezes
+    # the model: at frame 500 the background image is far from the long-term mean of the down-sampled
+    # frames (ratio >= 45 during the bootstrap window), so the moving-camera mode turns on (weight
+    # offset 5, refreshModel(1, 1, true)); at frame 1000 the model has caught up and it turns off
+    W, H = 64, 48
+    s = SyntheticStream(2, 0, 40, width=W, height=H)
+    base = [s.render(t).astype(np.int32) for t in range(8)]
+
+    def frame(t):
+        return np.clip(base[t % 8] - int(min(max(0, t - 150), 300) * 120 / 300), 0, 255).astype(np.uint8)
+
+    gpu = BackgroundSubtractorPAWCS(seed=11)
+    ora = pyoracle.OraclePAWCS(seed=11)
+    gpu.initialize(frame(0))
+    ora.initialize(frame(0))
+    modes = {}
+    for t in range(1, 1002):
+        lr = float("inf") if 150 <= t <= 500 else 0.0
+        mg = gpu.apply(frame(t), learningRateOverride=lr)
+        mo = ora.apply(frame(t), lr)
+        assert np.array_equal(mg, mo), "frame %d: mask differs at %d px" % (t, int((mg != mo).sum()))
+        if t % 100 == 0 or t in (499, 501, 999, 1001):
+            bad = compare_state(gpu, ora)
+            assert not bad, "frame %d: %s" % (t, "; ".join(bad))
+        if t in (499, 500, 999, 1000):
+            modes[t] = (gpu.scalars()["using_moving_camera"], gpu.scalars()["lword_weight_offset"])
+    assert modes == {499: (0, 1000), 500: (1, 5), 999: (1, 5), 1000: (0, 1000)}
