@@ -95,8 +95,8 @@ class ClockSampler:
         return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-KERNELS = ["eval", "resolve", "repair", "commit", "runs", "vunion", "holes", "combine", "median", "epilogue",
-           "dilate", "reset", "close"]
+KERNELS = ["eval", "resolve", "repair", "commit", "runs", "vunion", "holes", "combine", "hcount", "median",
+           "epilogue", "dilate", "reset", "close"]
 
 
 def algorithmic_bytes(px_by_c):

@@ -198,7 +198,8 @@ lvbgs_status lvbgs_get_scalars(lvbgs_handle h, lvbgs_scalars* out);
  * events around each kernel of the next n steps launched by h (batched != 0: the batched steps it
  * leads; 0 disables); lvbgs_debug_tick_profile() waits for them and returns the average duration in
  * ms of each kernel, in launch order: evaluation, ghost resolution, repair, commit/closing, row runs,
- * vertical unions, holes, erosion/combination, median, frame-level epilogue, dilation/blinks,
+ * vertical unions, holes, erosion/combination, median row-window counts, median, frame-level epilogue,
+ * dilation/blinks,
  * automatic model reset, frame close. Returns the number of values written. */
 lvbgs_status lvbgs_debug_set_timing(lvbgs_handle h, int batched, int n_ticks);
 int lvbgs_debug_tick_profile(lvbgs_handle h, int batched, double* out_ms, int max_n);

@@ -24,6 +24,7 @@ extern "C" __global__ void lvbgs_k_runs(TickParams P);
 extern "C" __global__ void lvbgs_k_vunion(TickParams P);
 extern "C" __global__ void lvbgs_k_holes(TickParams P);
 extern "C" __global__ void lvbgs_k_combine(TickParams P);
+extern "C" __global__ void lvbgs_k_hcount(TickParams P);
 extern "C" __global__ void lvbgs_k_median(TickParams P);
 extern "C" __global__ void lvbgs_k_epilogue(TickParams P);
 extern "C" __global__ void lvbgs_k_dilate(TickParams P);
@@ -205,7 +206,7 @@ enum {
     L_CTL = 0, L_FM, L_UNST, L_LASTCOL, L_LASTDESC, L_SD, L_SC, L_ROI, L_BLINKS, L_LASTRAWFG, L_LASTFG, L_DILINV,
     L_LASTRAWBLINK, L_KCTR, L_DSLT, L_DSST,
     // scratch (not spilled)
-    L_STAMPD, L_STAMPR, L_PREFLOOD, L_COMBINED, L_LABEL, L_INTENT, L_FRAME, L_MASK, L_COUNT
+    L_STAMPD, L_STAMPR, L_BITS, L_HCOUNT, L_LABEL, L_INTENT, L_FRAME, L_MASK, L_COUNT
 };
 Layout make_layout(int W, int H, int C, size_t N) {
     const size_t npx = (size_t)W * H;
@@ -222,7 +223,8 @@ Layout make_layout(int W, int H, int C, size_t N) {
     sz[L_KCTR] = npx * 2;
     sz[L_DSLT] = sz[L_DSST] = std::max<size_t>(nds, 1) * 4;
     sz[L_STAMPD] = sz[L_STAMPR] = npx * 4;
-    sz[L_PREFLOOD] = sz[L_COMBINED] = npx;
+    sz[L_BITS] = bit_planes_bytes(W, H);
+    sz[L_HCOUNT] = npx;
     sz[L_LABEL] = sz[L_INTENT] = npx * 4;
     sz[L_FRAME] = npx * C;
     sz[L_MASK] = npx;
@@ -258,8 +260,8 @@ void fill_pointers(lvbgs_ctx* h, const Layout& L) {
     S.dsST = (float*)(b + L.off[L_DSST]);
     S.stampD = (uint32_t*)(b + L.off[L_STAMPD]);
     S.stampR = (uint32_t*)(b + L.off[L_STAMPR]);
-    S.preflood = b + L.off[L_PREFLOOD];
-    S.combined = b + L.off[L_COMBINED];
+    S.bits = (uint32_t*)(b + L.off[L_BITS]);
+    S.hcount = b + L.off[L_HCOUNT];
     S.label = (int*)(b + L.off[L_LABEL]);
     S.intent = (uint32_t*)(b + L.off[L_INTENT]);
     h->d_frame = b + L.off[L_FRAME];
@@ -276,6 +278,9 @@ void fill_geometry(lvbgs_ctx* h) {
     S.tilesY = (h->H + kTileH - 1) / kTileH;
     S.nTiles = S.tilesX * S.tilesY;
     S.tileBase = 0;
+    S.rowWords = (h->W + 31) / 32;
+    S.segBase = 0;
+    S.nSegs = (h->H + kMedSegRows - 1) / kMedSegRows;
     S.dsW = h->W / 8;
     S.dsH = h->H / 8;
     S.dsSX = S.dsW > 0 ? h->W / S.dsW : 1;
@@ -292,7 +297,7 @@ void fill_geometry(lvbgs_ctx* h) {
     S.nMagic = ((1ull << 40) + S.N - 1) / (unsigned long long)S.N;
 }
 
-constexpr int kTimedKernels = 13;  // kernels of one frame step, in launch order
+constexpr int kTimedKernels = 14;  // kernels of one frame step, in launch order
 int g_coop_blocks_per_sm = -1, g_sm_count = 0;
 std::mutex g_occ_mu;
 cudaError_t coop_grid(int* maxBlocks) {
@@ -314,15 +319,18 @@ cudaError_t coop_grid(int* maxBlocks) {
 // entries. Both are host arrays the descriptor uploads read from (pinned for ticks in flight).
 lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t st, StreamDev* hS,
                          unsigned long long* hDs) {
-    int totalTiles = 0, totalRows = 0;
+    int totalTiles = 0, totalRows = 0, totalSegs = 0, maxW = 0;
     size_t totalPx = 0;
     unsigned long long ds = 0;
     for (int i = 0; i < n; ++i) {
         StreamDev& S = hS[i];
         S.tileBase = totalTiles;
         S.rowBase = totalRows;
+        S.segBase = totalSegs;
         totalTiles += S.nTiles;
         totalRows += S.H;
+        totalSegs += S.nSegs;
+        maxW = std::max(maxW, S.W);
         totalPx += (size_t)S.npx;
         hDs[i] = ds;
         // only streams with the frame-level analysis enabled down-sample
@@ -350,6 +358,8 @@ lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t s
     P.rlist[0] = ws.lists + 2 * ws.cap;
     P.rlist[1] = ws.lists + 3 * ws.cap;
     P.listCap = (unsigned)std::min<size_t>(ws.cap, 0xffffffffu);
+    P.totalSegs = totalSegs;
+    P.colBlocks = (maxW + 255) / 256;
     const unsigned long long* dsb = ws.d_dsBase;
     const dim3 blk(kThreads);
     const int rowBlocks = (totalRows + 7) / 8;
@@ -382,18 +392,20 @@ lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t s
     LV_TMARK(6);
     lvbgs_k_holes<<<rowBlocks, blk, 0, st>>>(P);
     LV_TMARK(7);
-    lvbgs_k_combine<<<totalTiles, blk, 0, st>>>(P);
+    lvbgs_k_combine<<<rowBlocks, blk, 0, st>>>(P);
     LV_TMARK(8);
-    lvbgs_k_median<<<totalTiles, blk, 0, st>>>(P);
+    lvbgs_k_hcount<<<totalRows, 128, 0, st>>>(P);
     LV_TMARK(9);
-    lvbgs_k_epilogue<<<1, 128, 0, st>>>(P);
+    lvbgs_k_median<<<dim3(P.colBlocks, std::max(1, totalSegs)), blk, 0, st>>>(P);
     LV_TMARK(10);
-    lvbgs_k_dilate<<<totalTiles, blk, 0, st>>>(P);
+    lvbgs_k_epilogue<<<1, 128, 0, st>>>(P);
     LV_TMARK(11);
-    lvbgs_k_reset<<<std::max(1, std::min(totalTiles, g_sm_count * 8)), blk, 0, st>>>(P);
+    lvbgs_k_dilate<<<totalRows, 128, 0, st>>>(P);
     LV_TMARK(12);
-    lvbgs_k_close<<<1, 128, 0, st>>>(P);
+    lvbgs_k_reset<<<std::max(1, std::min(totalTiles, g_sm_count * 8)), blk, 0, st>>>(P);
     LV_TMARK(13);
+    lvbgs_k_close<<<1, 128, 0, st>>>(P);
+    LV_TMARK(14);
 #undef LV_TMARK
     LV_CUDA(errh, cudaGetLastError(), "frame step launch");
     return LVBGS_OK;
@@ -499,7 +511,7 @@ enum {
     PL_BLINKS, PL_LASTRAWFG, PL_LASTFG, PL_DILINV, PL_LASTRAWBLINK, PL_LASTCOL, PL_LASTDESC, PL_KCTR, PL_GLUT,
     PL_GMAP, PL_DSLT, PL_DSST, PL_DSROI,
     // scratch (not part of the model)
-    PL_PREFLOOD, PL_COMBINED, PL_LABEL, PL_INTENT, PL_DESCT, PL_REC, PL_OUT, PL_REPB, PL_REPA, PL_UFINAL, PL_UV,
+    PL_BITS, PL_HCOUNT, PL_LABEL, PL_INTENT, PL_DESCT, PL_REC, PL_OUT, PL_REPB, PL_REPA, PL_UFINAL, PL_UV,
     PL_ITEMLIST, PL_CONTRIBLIST, PL_BLKCOUNTS, PL_CATINFO, PL_DSABS, PL_GITEM, PL_CONTRIB, PL_DSFRAME, PL_FRAME, PL_MASK, PL_ROWSUM, PL_WORK, PL_FLAGS, PL_PDEV, PL_SDEV, PL_COUNT
 };
 struct PwLayout {
@@ -522,7 +534,8 @@ PwLayout pw_layout(int W, int H, int L, int G) {
     sz[PL_GMAP] = (size_t)G * std::max<size_t>(gmap, 1) * 4;
     sz[PL_DSLT] = sz[PL_DSST] = std::max<size_t>(nds, 1) * 4;
     sz[PL_DSROI] = std::max<size_t>(nds, 1);
-    sz[PL_PREFLOOD] = sz[PL_COMBINED] = npx;
+    sz[PL_BITS] = bit_planes_bytes(W, H);
+    sz[PL_HCOUNT] = npx;
     sz[PL_LABEL] = sz[PL_INTENT] = npx * 4;
     sz[PL_DESCT] = npx * 2;
     sz[PL_REC] = npx * sizeof(PwRec);
@@ -548,7 +561,7 @@ PwLayout pw_layout(int W, int H, int L, int G) {
     PwLayout Lo;
     size_t o = 0;
     for (int i = 0; i < PL_COUNT; ++i) {
-        if (i == PL_PREFLOOD) Lo.persist = o;
+        if (i == PL_BITS) Lo.persist = o;
         Lo.off[i] = o;
         o += align256(sz[i]);
     }
@@ -604,8 +617,8 @@ void pw_fill(lvbgs_ctx* h, const PwLayout& Lo, int L, int G) {
     S.kctr = (uint16_t*)(b + Lo.off[PL_KCTR]);
     S.dsLT = (float*)(b + Lo.off[PL_DSLT]);
     S.dsST = (float*)(b + Lo.off[PL_DSST]);
-    S.preflood = b + Lo.off[PL_PREFLOOD];
-    S.combined = b + Lo.off[PL_COMBINED];
+    S.bits = (uint32_t*)(b + Lo.off[PL_BITS]);
+    S.hcount = b + Lo.off[PL_HCOUNT];
     S.label = (int*)(b + Lo.off[PL_LABEL]);
     S.intent = (uint32_t*)(b + Lo.off[PL_INTENT]);
     h->d_frame = b + Lo.off[PL_FRAME];
@@ -835,13 +848,16 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
     TP.totalTiles = tiles;
     TP.totalRows = h->H;
     TP.work = h->d_work;
+    TP.totalSegs = h->sd.nSegs;
+    TP.colBlocks = (h->W + 255) / 256;
     const int rowBlocks = (h->H + 7) / 8;
     lvbgs_k_runs<<<rowBlocks, blk, 0, st>>>(TP);
     lvbgs_k_vunion<<<rowBlocks, blk, 0, st>>>(TP);
     lvbgs_k_holes<<<rowBlocks, blk, 0, st>>>(TP);
-    lvbgs_k_combine<<<tiles, blk, 0, st>>>(TP);
-    lvbgs_k_median<<<tiles, blk, 0, st>>>(TP);
-    lvbgs_k_dilate<<<tiles, blk, 0, st>>>(TP);
+    lvbgs_k_combine<<<rowBlocks, blk, 0, st>>>(TP);
+    lvbgs_k_hcount<<<h->H, 128, 0, st>>>(TP);
+    lvbgs_k_median<<<dim3(TP.colBlocks, TP.totalSegs), blk, 0, st>>>(TP);
+    lvbgs_k_dilate<<<h->H, 128, 0, st>>>(TP);
     const int nds = (h->W / 8) * (h->H / 8);
     if (nds > 0) pw_k_ds<<<(nds + 255) / 256, 256, 0, st>>>(P);
     pw_k_epilogue<<<1, 32, 0, st>>>(P);

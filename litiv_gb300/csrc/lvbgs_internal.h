@@ -129,7 +129,8 @@ struct StreamCtl {
 struct StreamDev {
     int W, H, C, npx;
     int tilesX, tilesY, tileBase, nTiles;
-    int rowBase, pad0;  // first row of this stream in the batch's row index space
+    int rowBase, rowWords;  // first row of this stream in the batch's row index space; bit-plane words per row
+    int segBase, nSegs;     // first median column segment of this stream in the batch, and its count
     int dsW, dsH, dsSX, dsSY;
     int N, nreq, minColor, descOff, stabColorOff, nmv;
     float relThr;
@@ -151,7 +152,8 @@ struct StreamDev {
     uint8_t* sC;
     uint8_t* roi;
     uint8_t *blinks, *lastRawFG, *lastFG, *dilInv, *lastRawBlink;
-    uint8_t *preflood, *combined;
+    uint32_t* bits;   // mask bit planes (BP_*): rowWords words per row, bit b of word w = pixel 32w + b
+    uint8_t* hcount;  // set pixels of the combined mask in each pixel's median row window
     int* label;
     uint32_t* intent;
     uint32_t *stampD, *stampR;
@@ -183,6 +185,15 @@ struct TickParams {
     unsigned long long* dlist[2];  // (stream << 40) | pixel
     unsigned long long* rlist[2];
     unsigned int listCap;
+    int totalSegs, colBlocks;  // median: column segments of all streams; 256-pixel column blocks of the widest
 };
+
+// mask bit planes of a stream (scratch of one frame step; bits beyond the frame width are 0)
+enum { BP_CLOSED = 0, BP_RAW, BP_HOLES, BP_COMB, BP_FG, BP_COUNT };
+constexpr int kMedSegRows = 32;  // rows of one median column segment
+__host__ __device__ __forceinline__ uint32_t* bit_plane(const StreamDev& S, int i) {
+    return S.bits + (size_t)i * S.H * S.rowWords;
+}
+inline size_t bit_planes_bytes(int W, int H) { return (size_t)BP_COUNT * H * ((W + 31) / 32) * 4; }
 
 }  // namespace lvbgs

@@ -1172,22 +1172,32 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_blink_close(PwParams P) {
     __syncthreads();
     const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
     const int x = x0 + lx, y = y0 + ly;
-    if (x >= W || y >= H) return;
-    const int q = y * W + x;
-    const uint8_t r = raw[(ly + 2) * IW + lx + 2];
-    const uint8_t cb = r ^ D.lastRawFG[q];
-    D.blinks[q] = cb | D.lastRawBlink[q];
-    D.lastRawBlink[q] = cb;
-    D.lastRawFG[q] = r;
-    // erosion of the dilated mask over the clipped window
-    uint8_t v = 255;
-    for (int dy = -1; dy <= 1; ++dy)
-        for (int dx = -1; dx <= 1; ++dx) {
-            const int gx = x + dx, gy = y + dy;
-            if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
-            v &= dil[(ly + 1 + dy) * DW + lx + 1 + dx];
-        }
-    D.preflood[q] = v;
+    bool rawBit = false, closedBit = false;
+    if (x < W && y < H) {
+        const int q = y * W + x;
+        const uint8_t r = raw[(ly + 2) * IW + lx + 2];
+        const uint8_t cb = r ^ D.lastRawFG[q];
+        D.blinks[q] = cb | D.lastRawBlink[q];
+        D.lastRawBlink[q] = cb;
+        D.lastRawFG[q] = r;
+        // erosion of the dilated mask over the clipped window
+        uint8_t v = 255;
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int gx = x + dx, gy = y + dy;
+                if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+                v &= dil[(ly + 1 + dy) * DW + lx + 1 + dx];
+            }
+        rawBit = r != 0;
+        closedBit = v != 0;
+    }
+    // each warp is one 32-pixel tile row: its ballots are the row's words of the raw and closed masks
+    const unsigned rawW = __ballot_sync(0xffffffffu, rawBit), closedW = __ballot_sync(0xffffffffu, closedBit);
+    if (lx == 0 && y < H) {
+        const size_t o = (size_t)y * D.rowWords + x0 / 32;
+        bit_plane(D, BP_RAW)[o] = rawW;
+        bit_plane(D, BP_CLOSED)[o] = closedW;
+    }
 }
 
 // down-sampled frame (INTER_AREA, integral scale), its rolling averages (accumulateWeighted) and the

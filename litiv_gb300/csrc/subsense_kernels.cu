@@ -815,6 +815,7 @@ __device__ void phaseF_tile(const TickParams& P, const StreamDev& S, int lt, uin
     const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
     const int x = x0 + lx, y = y0 + ly;
     int nw = 0, ne = 0;
+    bool rawBit = false, closedBit = false;
     if (x < W && y < H) {
         const int q = y * W + x;
         // raster-ordered commit of every write targeting q (own write before own neighbour write).
@@ -857,6 +858,7 @@ __device__ void phaseF_tile(const TickParams& P, const StreamDev& S, int lt, uin
         S.blinks[q] = cb | lastRawBlink;
         S.lastRawBlink[q] = cb;
         S.lastRawFG[q] = raw;
+        rawBit = raw != 0;
         // closing: erosion of the dilated mask (out-of-frame pixels never win)
         uint8_t v = 255;
         for (int dy = -1; dy <= 1; ++dy)
@@ -865,7 +867,15 @@ __device__ void phaseF_tile(const TickParams& P, const StreamDev& S, int lt, uin
                 if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
                 v &= dil[(ly + 1 + dy) * (kTileW + 2) + lx + 1 + dx];
             }
-        __stcg(&S.preflood[q], v);
+        closedBit = v != 0;
+    }
+    // each warp is one 32-pixel tile row: its ballots are the row's words of the raw and closed masks
+    static_assert(kTileW == 32, "tile rows are bit-plane words");
+    const unsigned rawW = __ballot_sync(0xffffffffu, rawBit), closedW = __ballot_sync(0xffffffffu, closedBit);
+    if (lx == 0 && y < H) {
+        const size_t o = (size_t)y * S.rowWords + tx;
+        bit_plane(S, BP_RAW)[o] = rawW;
+        bit_plane(S, BP_CLOSED)[o] = closedW;
     }
     for (int o = 16; o > 0; o >>= 1) {
         nw += __shfl_xor_sync(0xffffffffu, nw, o);
@@ -944,22 +954,28 @@ __device__ __forceinline__ int find_stream_by_row(const TickParams& P, int r) {
     return lo;
 }
 
+// bits of word w that lie inside a frame of width W
+__device__ __forceinline__ uint32_t valid_bits(int w, int W) {
+    const int n = W - 32 * w;
+    return n >= 32 ? 0xffffffffu : (n <= 0 ? 0u : (1u << n) - 1u);
+}
+
 // runs pass: initializes the label of each run start (0 for runs touching the border ring)
 extern "C" __global__ void __launch_bounds__(256) lvbgs_k_runs(TickParams P) {
     const int gr = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x & 31;
     if (gr >= P.totalRows) return;
     const StreamDev& S = P.streams[find_stream_by_row(P, gr)];
     const int y = gr - S.rowBase, W = S.W, H = S.H;
-    const uint8_t* row = S.preflood + (size_t)y * W;
+    const uint32_t* row = bit_plane(S, BP_CLOSED) + (size_t)y * S.rowWords;
     RunTracker rt;
     rt.reset();
     int last = -1;
     bool ringOk = true;
     for (int x0 = 0; x0 < W; x0 += 32) {
         const int x = x0 + lane;
-        const bool z = x < W && __ldcg(&row[x]) == 0;
+        const uint32_t ball = ~__ldcg(&row[x0 >> 5]) & valid_bits(x0 >> 5, W);  // 0-pixels of the chunk
+        const bool z = (ball >> lane) & 1u;
         if (x < W && (x < 2 || x >= W - 2 || y < 2 || y >= H - 2) && !z) ringOk = false;
-        const uint32_t ball = __ballot_sync(0xffffffffu, z);
         const uint32_t starts = ball & ~((ball << 1) | rt.carry);
         const int rs = rt.step(ball, x0, lane);
         if ((starts >> lane) & 1u) {
@@ -981,17 +997,15 @@ extern "C" __global__ void __launch_bounds__(256) lvbgs_k_vunion(TickParams P) {
     const StreamDev& S = P.streams[find_stream_by_row(P, gr)];
     const int y = gr - S.rowBase, W = S.W;
     if (y == 0) return;
-    const uint8_t* row = S.preflood + (size_t)y * W;
-    const uint8_t* up = row - W;
+    const uint32_t* row = bit_plane(S, BP_CLOSED) + (size_t)y * S.rowWords;
+    const uint32_t* up = row - S.rowWords;
     RunTracker rc, ru;
     rc.reset();
     ru.reset();
     uint32_t ovCarry = 0;
     for (int x0 = 0; x0 < W; x0 += 32) {
-        const int x = x0 + lane;
-        const bool zc = x < W && __ldcg(&row[x]) == 0;
-        const bool zu = x < W && __ldcg(&up[x]) == 0;
-        const uint32_t bc = __ballot_sync(0xffffffffu, zc), bu = __ballot_sync(0xffffffffu, zu);
+        const uint32_t vb = valid_bits(x0 >> 5, W);
+        const uint32_t bc = ~__ldcg(&row[x0 >> 5]) & vb, bu = ~__ldcg(&up[x0 >> 5]) & vb;
         const int rsc = rc.step(bc, x0, lane), rsu = ru.step(bu, x0, lane);
         const uint32_t ov = bc & bu;
         const uint32_t segStarts = ov & ~((ov << 1) | ovCarry);
@@ -1000,137 +1014,214 @@ extern "C" __global__ void __launch_bounds__(256) lvbgs_k_vunion(TickParams P) {
     }
 }
 
-// holes pass: combined := 255 at the 0-pixels whose run is not connected to the ring, else 0
+// holes pass: the 0-pixels whose run is not connected to the ring
 extern "C" __global__ void __launch_bounds__(256) lvbgs_k_holes(TickParams P) {
     const int gr = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x & 31;
     if (gr >= P.totalRows) return;
     const StreamDev& S = P.streams[find_stream_by_row(P, gr)];
     const int y = gr - S.rowBase, W = S.W;
-    const uint8_t* row = S.preflood + (size_t)y * W;
-    RunTracker rt;
-    rt.reset();
+    const uint32_t* row = bit_plane(S, BP_CLOSED) + (size_t)y * S.rowWords;
+    uint32_t* holes = bit_plane(S, BP_HOLES) + (size_t)y * S.rowWords;
+    // one root lookup per run: at the lane where the run starts; a run that continues from the
+    // previous chunk keeps that chunk's answer
+    uint32_t carry = 0;
+    bool carryHole = false;
     for (int x0 = 0; x0 < W; x0 += 32) {
-        const int x = x0 + lane;
-        const bool z = x < W && __ldcg(&row[x]) == 0;
-        const uint32_t ball = __ballot_sync(0xffffffffu, z);
-        const int rs = rt.step(ball, x0, lane);
-        uint8_t hole = 0;
-        if (z) hole = uf_find(S.label, y * W + rs, P.work) != 0 ? 255 : 0;
-        if (x < W) S.combined[(size_t)y * W + x] = hole;
+        const uint32_t ball = ~__ldcg(&row[x0 >> 5]) & valid_bits(x0 >> 5, W);
+        const uint32_t starts = ball & ~((ball << 1) | carry);
+        const bool isStart = (starts >> lane) & 1u;
+        const bool h = isStart && uf_find(S.label, y * W + x0 + lane, P.work) != 0;
+        const uint32_t upto = starts & (0xffffffffu >> (31 - lane));
+        const int src = upto ? 31 - __clz(upto) : 0;
+        const bool hs = __shfl_sync(0xffffffffu, h, src);
+        const bool hole = ((ball >> lane) & 1u) && (upto ? hs : carryHole);
+        const uint32_t hw = __ballot_sync(0xffffffffu, hole);
+        if (lane == 0) holes[x0 >> 5] = hw;
+        carryHole = (hw >> 31) & 1u;
+        carry = ball >> 31;
     }
 }
 
-// 3-fold erosion of the closed mask and mask |= holes | eroded (:544-546)
-__device__ void phaseP3_tile(const TickParams& P, const StreamDev& S, int lt, uint8_t* smem) {
-    const int tx = lt % S.tilesX, ty = lt / S.tilesX;
-    const int x0 = tx * kTileW, y0 = ty * kTileH;
-    constexpr int HW = kTileW + 6, HH = kTileH + 6;
-    uint8_t* pf = smem;
-    uint8_t* rowmin = smem + HW * HH;
-    const int W = S.W, H = S.H;
-    for (int i = threadIdx.x; i < HW * HH; i += blockDim.x) {
-        const int gy = y0 - 3 + i / HW, gx = x0 - 3 + i % HW;
-        pf[i] = (gy >= 0 && gy < H && gx >= 0 && gx < W) ? __ldcg(&S.preflood[gy * W + gx]) : 255;  // never wins
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < kTileW * HH; i += blockDim.x) {
-        const int ry = i / kTileW, rx = i % kTileW;
-        uint8_t v = 255;
-        for (int d = 0; d < 7; ++d) v = min(v, pf[ry * HW + rx + d]);
-        rowmin[i] = v;
-    }
-    __syncthreads();
-    const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
-    const int x = x0 + lx, y = y0 + ly;
-    if (x >= W || y >= H) return;
-    const int q = y * W + x;
-    uint8_t er = 255;
-    for (int d = 0; d < 7; ++d) er = min(er, rowmin[(ly + d) * kTileW + lx]);
-    const uint8_t hole = __ldcg(&S.combined[q]);
-    const uint8_t raw = (__ldcg(&S.intent[q]) & kInFG) ? 255 : 0;
-    __stcg(&S.combined[q], (uint8_t)(raw | hole | er));
+// word w of a bit-plane row with the pixels outside [0, W) set to fill (0 or ~0)
+__device__ __forceinline__ uint32_t row_word(const uint32_t* row, int w, int RW, int W, uint32_t fill) {
+    if (w < 0 || w >= RW) return fill;
+    const uint32_t vb = valid_bits(w, W);
+    return (__ldcg(&row[w]) & vb) | (fill & ~vb);
 }
 
-// P4: median blur (binary majority, replicate border) -> final mask; final-segmentation EMAs
-// via addWeighted (:547, :552-554)
-__device__ void phaseP4_tile(const TickParams& P, const StreamDev& S, int lt, uint8_t* smem) {
-    const int tx = lt % S.tilesX, ty = lt / S.tilesX;
-    const int x0 = tx * kTileW, y0 = ty * kTileH;
-    const int k = S.ctl->median_k, r = k / 2;
-    const int HW = kTileW + 2 * r, HH = kTileH + 2 * r;
-    uint8_t* cm = smem;
-    uint8_t* colcnt = smem + HW * HH;
+// 7-pixel horizontal AND (erode) or OR (dilate) of word w of a row; pixels outside the frame take
+// the value that never wins
+template <bool AND>
+__device__ __forceinline__ uint32_t row_box7(const uint32_t* row, int w, int RW, int W) {
+    const uint32_t fill = AND ? 0xffffffffu : 0u;
+    const uint32_t L = row_word(row, w - 1, RW, W, fill), C = row_word(row, w, RW, W, fill),
+                   R = row_word(row, w + 1, RW, W, fill);
+    uint32_t v = C;
+#pragma unroll
+    for (int d = 1; d <= 3; ++d) {
+        const uint32_t a = __funnelshift_r(C, R, d), b = __funnelshift_l(L, C, d);  // pixels x+d, x-d
+        v = AND ? (v & a & b) : (v | a | b);
+    }
+    return v;
+}
+
+// 3-fold 3x3 erosion of the closed mask (a clipped 7x7 minimum) and mask |= holes | eroded (:544-546);
+// one warp per row, one thread per 32-pixel word
+extern "C" __global__ void __launch_bounds__(256) lvbgs_k_combine(TickParams P) {
+    const int gr = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x & 31;
+    if (gr >= P.totalRows) return;
+    const StreamDev& S = P.streams[find_stream_by_row(P, gr)];
+    const int y = gr - S.rowBase, W = S.W, H = S.H, RW = S.rowWords;
+    const uint32_t* closed = bit_plane(S, BP_CLOSED);
+    for (int w = lane; w < RW; w += 32) {
+        uint32_t er = 0xffffffffu;
+        for (int yy = max(0, y - 3); yy <= min(H - 1, y + 3); ++yy) er &= row_box7<true>(closed + (size_t)yy * RW, w, RW, W);
+        const size_t o = (size_t)y * RW + w;
+        bit_plane(S, BP_COMB)[o] = (__ldcg(&bit_plane(S, BP_RAW)[o]) | __ldcg(&bit_plane(S, BP_HOLES)[o]) | er) & valid_bits(w, W);
+    }
+}
+
+// median, part 1: for each pixel, the number of set pixels of the combined mask in its row window
+// [x - r, x + r] (replicate border: pixels left of 0 / right of W-1 repeat those two pixels); one
+// block per row, four 32-pixel words per warp step
+extern "C" __global__ void __launch_bounds__(256) lvbgs_k_hcount(TickParams P) {
+    const int gr = blockIdx.x, lane = threadIdx.x & 31;
+    if (gr >= P.totalRows) return;
+    const StreamDev& S = P.streams[find_stream_by_row(P, gr)];
+    const int y = gr - S.rowBase, W = S.W, RW = S.rowWords;
+    const int r = S.ctl->median_k / 2;  // <= 15
+    const uint32_t* row = bit_plane(S, BP_COMB) + (size_t)y * RW;
+    const uint32_t lastFill = ((__ldcg(&row[(W - 1) >> 5]) >> ((W - 1) & 31)) & 1u) ? 0xffffffffu : 0u;
+    const uint32_t firstFill = (__ldcg(&row[0]) & 1u) ? 0xffffffffu : 0u;
+    const unsigned long long win = (2ull << (2 * r)) - 1ull;
+    const int nw = blockDim.x >> 5;
+    for (int w0 = (threadIdx.x >> 5) * 4; w0 < RW; w0 += 4 * nw) {
+        // words w0-1 .. w0+4 first, then the four words' counts
+        uint32_t v[6];
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+            const int w = w0 - 1 + j;
+            v[j] = w < 0 ? firstFill : row_word(row, w, RW, W, lastFill);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            // bits 16..79 of the 96-bit row segment L | C | R: pixel x - r is bit 16 + lane - r
+            const unsigned long long M =
+                ((unsigned long long)v[j + 2] << 48) | ((unsigned long long)v[j + 1] << 16) | (v[j] >> 16);
+            const int x = 32 * (w0 + j) + lane;
+            if (x < W) S.hcount[(size_t)y * W + x] = (uint8_t)__popcll((M >> (16 + lane - r)) & win);
+        }
+    }
+}
+
+// median, part 2 (:547, :552-554): binary median blur (majority of the k x k window, replicate border)
+// of the combined mask -> final mask, its row words, and the final-segmentation EMAs (addWeighted).
+// One thread per pixel column of a 64-row segment, sliding the window sum down the rows.
+extern "C" __global__ void __launch_bounds__(256) lvbgs_k_median(TickParams P) {
+    const int gs = blockIdx.y;
+    if (gs >= P.totalSegs) return;
+    int lo = 0, hi = P.nStreams - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (P.streams[mid].segBase <= gs) lo = mid;
+        else hi = mid - 1;
+    }
+    const StreamDev& S = P.streams[lo];
     const int W = S.W, H = S.H, npx = S.npx;
+    const int x0 = blockIdx.x * 256;
+    if (x0 >= W) return;
+    const int x = x0 + threadIdx.x, lane = threadIdx.x & 31;
+    const bool in = x < W;
+    const int y0 = (gs - S.segBase) * kMedSegRows, y1 = min(H, y0 + kMedSegRows);
+    const int k = S.ctl->median_k, r = k / 2;
     const FrameK F = frame_consts(S);
-    const int qx = x0 + (int)threadIdx.x % kTileW, qy = y0 + (int)threadIdx.x / kTileW;
-    const bool qin = qx < W && qy < H;
-    const int qq = qy * W + qx;
     const float* fcur = S.fm + (size_t)F.cur * kNumFloatMaps * npx;
-    const float finLT = qin ? fcur[FM_FIN_LT * npx + qq] : 0.0f, finST = qin ? fcur[FM_FIN_ST * npx + qq] : 0.0f;
-    for (int i = threadIdx.x; i < HW * HH; i += blockDim.x) {
-        int gy = y0 - r + i / HW, gx = x0 - r + i % HW;
-        gy = gy < 0 ? 0 : gy >= H ? H - 1 : gy;
-        gx = gx < 0 ? 0 : gx >= W ? W - 1 : gx;
-        cm[i] = __ldcg(&S.combined[gy * W + gx]) ? 1 : 0;
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < kTileH * HW; i += blockDim.x) {
-        const int ry = i / HW, rx = i % HW;
-        int c = 0;
-        for (int d = 0; d < k; ++d) c += cm[(ry + d) * HW + rx];
-        colcnt[i] = (uint8_t)c;
-    }
-    __syncthreads();
-    const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
-    const int x = x0 + lx, y = y0 + ly;
-    if (x >= W || y >= H) return;
-    const int q = y * W + x;
-    int cnt = 0;
-    for (int d = 0; d < k; ++d) cnt += colcnt[ly * HW + lx + d];
-    const uint8_t fgv = (2 * cnt > k * k) ? 255 : 0;
-    __stcg(&S.lastFG[q], fgv);
-    if (S.maskOut) S.maskOut[q] = fgv;
     float* fn = S.fm + (size_t)F.nxt * kNumFloatMaps * npx;
     const float aL = 1.0f - F.fLT, bL = S.ctl->bLT;
     const float aS = 1.0f - F.fST, bS = S.ctl->bST;
-    const float m = (float)fgv;
-    fn[FM_FIN_LT * npx + q] = (finLT * aL + m * bL) + 0.0f;
-    fn[FM_FIN_ST * npx + q] = (finST * aS + m * bS) + 0.0f;
+    const uint8_t* hc = S.hcount + (in ? x : 0);
+    int sum = 0;
+    if (in)
+        for (int yy = y0 - r; yy <= y0 + r; ++yy) sum += __ldcg(&hc[(size_t)min(max(yy, 0), H - 1) * W]);
+    uint32_t* fgRow = bit_plane(S, BP_FG) + (x0 >> 5) + (threadIdx.x >> 5);
+    // four rows per step: every load of the step is issued before its stores
+    for (int yb = y0; yb < y1; yb += 4) {
+        int add[4], sub[4];
+        float fl[4], fs[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int y = yb + j;
+            add[j] = sub[j] = 0;
+            fl[j] = fs[j] = 0.0f;
+            if (in && y < y1) {
+                const int q = y * W + x;
+                add[j] = __ldcg(&hc[(size_t)min(y + r + 1, H - 1) * W]);
+                sub[j] = __ldcg(&hc[(size_t)max(y - r, 0) * W]);
+                fl[j] = fcur[FM_FIN_LT * npx + q];
+                fs[j] = fcur[FM_FIN_ST * npx + q];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int y = yb + j;
+            if (y >= y1) break;
+            const bool fg = in && 2 * sum > k * k;
+            const unsigned ball = __ballot_sync(0xffffffffu, fg);
+            if (in) {
+                const int q = y * W + x;
+                const uint8_t fgv = fg ? 255 : 0;
+                __stcg(&S.lastFG[q], fgv);
+                if (S.maskOut) S.maskOut[q] = fgv;
+                const float m = (float)fgv;
+                fn[FM_FIN_LT * npx + q] = (fl[j] * aL + m * bL) + 0.0f;
+                fn[FM_FIN_ST * npx + q] = (fs[j] * aS + m * bS) + 0.0f;
+                sum += add[j] - sub[j];
+            }
+            if (lane == 0 && x < W) fgRow[(size_t)y * S.rowWords] = ball;
+        }
+    }
 }
 
-// P5: 3-fold dilation of the final mask and blink masking with the previous and the new inverted
-// dilated masks (:548-551)
-__device__ void phaseP5_tile(const TickParams& P, const StreamDev& S, int lt, uint8_t* smem) {
-    const int tx = lt % S.tilesX, ty = lt / S.tilesX;
-    const int x0 = tx * kTileW, y0 = ty * kTileH;
-    constexpr int HW = kTileW + 6, HH = kTileH + 6;
-    uint8_t* fgm = smem;
-    uint8_t* rowmax = smem + HW * HH;
-    const int W = S.W, H = S.H;
-    const int qx = x0 + (int)threadIdx.x % kTileW, qy = y0 + (int)threadIdx.x / kTileW;
-    const bool qin = qx < W && qy < H;
-    const uint8_t bl0 = qin ? S.blinks[qy * W + qx] : 0, di0 = qin ? S.dilInv[qy * W + qx] : 0;
-    for (int i = threadIdx.x; i < HW * HH; i += blockDim.x) {
-        const int gy = y0 - 3 + i / HW, gx = x0 - 3 + i % HW;
-        fgm[i] = (gy >= 0 && gy < H && gx >= 0 && gx < W) ? __ldcg(&S.lastFG[gy * W + gx]) : 0;  // never wins
+// 3-fold 3x3 dilation of the final mask (a clipped 7x7 maximum) and blink masking with the previous
+// and the new inverted dilated masks (:548-551); one block per row, four 32-pixel words per warp step,
+// one lane per pixel of each
+extern "C" __global__ void __launch_bounds__(256) lvbgs_k_dilate(TickParams P) {
+    const int gr = blockIdx.x, lane = threadIdx.x & 31;
+    if (gr >= P.totalRows) return;
+    const StreamDev& S = P.streams[find_stream_by_row(P, gr)];
+    const int y = gr - S.rowBase, W = S.W, H = S.H, RW = S.rowWords;
+    const uint32_t* fgp = bit_plane(S, BP_FG);
+    const int nw = blockDim.x >> 5;
+    for (int w0 = (threadIdx.x >> 5) * 4; w0 < RW; w0 += 4 * nw) {
+        // lane l < 28 dilates row y - 3 + l/4 of word w0 + l%4; an OR over the lanes of equal l%4
+        const int j = lane & 3, yy = y - 3 + (lane >> 2);
+        uint32_t d = 0;
+        if (lane < 28 && yy >= 0 && yy < H && w0 + j < RW) d = row_box7<false>(fgp + (size_t)yy * RW, w0 + j, RW, W);
+        d |= __shfl_xor_sync(0xffffffffu, d, 4);
+        d |= __shfl_xor_sync(0xffffffffu, d, 8);
+        d |= __shfl_xor_sync(0xffffffffu, d, 16);
+        uint32_t dw[4];
+        uint8_t bl[4], di[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            dw[i] = __shfl_sync(0xffffffffu, d, i);
+            const int x = 32 * (w0 + i) + lane;
+            bl[i] = di[i] = 0;
+            if (x < W) {
+                bl[i] = S.blinks[y * W + x];
+                di[i] = S.dilInv[y * W + x];
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int x = 32 * (w0 + i) + lane;
+            if (x < W) {
+                const uint8_t inv = ((dw[i] >> lane) & 1u) ? 0 : 255;
+                S.blinks[y * W + x] = (uint8_t)(bl[i] & di[i] & inv);
+                S.dilInv[y * W + x] = inv;
+            }
+        }
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < kTileW * HH; i += blockDim.x) {
-        const int ry = i / kTileW, rx = i % kTileW;
-        uint8_t v = 0;
-        for (int d = 0; d < 7; ++d) v = max(v, fgm[ry * HW + rx + d]);
-        rowmax[i] = v;
-    }
-    __syncthreads();
-    const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
-    const int x = x0 + lx, y = y0 + ly;
-    if (x >= W || y >= H) return;
-    const int q = y * W + x;
-    uint8_t dv = 0;
-    for (int d = 0; d < 7; ++d) dv = max(dv, rowmax[(ly + d) * kTileW + lx]);
-    const uint8_t inv = (uint8_t)~dv;
-    S.blinks[q] = (uint8_t)(bl0 & di0 & inv);
-    S.dilInv[q] = inv;
 }
 
 // frame-level epilogue of one stream (:555-611): LBSP threshold LUT adaptation, camera-motion
@@ -1322,17 +1413,7 @@ extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_commit(TickParams
     else phaseF_tile<1>(P, S, lt, smem);
 }
 
-extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_combine(TickParams P) {
-    __shared__ __align__(16) uint8_t smem[(kTileW + 6) * (kTileH + 6) + kTileW * (kTileH + 6)];
-    LV_TILE_KERNEL_PROLOGUE
-    phaseP3_tile(P, S, lt, smem);
-}
 
-extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_median(TickParams P) {
-    __shared__ __align__(16) uint8_t smem[(kTileW + 30) * (kTileH + 30) + kTileH * (kTileW + 30)];
-    LV_TILE_KERNEL_PROLOGUE
-    phaseP4_tile(P, S, lt, smem);
-}
 
 // frame-level epilogue of every stream (one thread per stream)
 extern "C" __global__ void lvbgs_k_epilogue(TickParams P) {
@@ -1351,11 +1432,6 @@ extern "C" __global__ void lvbgs_k_epilogue(TickParams P) {
     }
 }
 
-extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_dilate(TickParams P) {
-    __shared__ __align__(16) uint8_t smem[(kTileW + 6) * (kTileH + 6) + kTileW * (kTileH + 6)];
-    LV_TILE_KERNEL_PROLOGUE
-    phaseP5_tile(P, S, lt, smem);
-}
 
 // automatic model reset: refreshModel(0.1) and T(x) := 1 everywhere (:588-593); a small grid
 // strides over the tiles of the streams that reset this frame
