@@ -197,7 +197,7 @@ lvbgs_status lvbgs_get_scalars(lvbgs_handle h, lvbgs_scalars* out);
 /* Per-kernel timing of frame steps (inspection): lvbgs_debug_set_timing(h, batched, n) records CUDA
  * events around each kernel of the next n steps launched by h (batched != 0: the batched steps it
  * leads; 0 disables); lvbgs_debug_tick_profile() waits for them and returns the average duration in
- * ms of each kernel, in launch order: evaluation, ghost resolution, repair, commit/closing, row runs,
+ * ms of each kernel, in launch order: evaluation, long sample scans, ghost resolution, repair, commit/closing, row runs,
  * vertical unions, holes, erosion/combination, median row-window counts, median, frame-level epilogue,
  * dilation/blinks,
  * automatic model reset, frame close. Returns the number of values written. */

@@ -17,6 +17,7 @@
 
 namespace lvbgs {
 extern "C" __global__ void lvbgs_k_eval(TickParams P);
+extern "C" __global__ void lvbgs_k_longscan(TickParams P);
 extern "C" __global__ void lvbgs_k_resolve(TickParams P, unsigned long long dsTotal, const unsigned long long* dsBase);
 extern "C" __global__ void lvbgs_k_repair(TickParams P);
 extern "C" __global__ void lvbgs_k_commit(TickParams P);
@@ -297,7 +298,7 @@ void fill_geometry(lvbgs_ctx* h) {
     S.nMagic = ((1ull << 40) + S.N - 1) / (unsigned long long)S.N;
 }
 
-constexpr int kTimedKernels = 14;  // kernels of one frame step, in launch order
+constexpr int kTimedKernels = 15;  // kernels of one frame step, in launch order
 int g_coop_blocks_per_sm = -1, g_sm_count = 0;
 std::mutex g_occ_mu;
 cudaError_t coop_grid(int* maxBlocks) {
@@ -375,37 +376,43 @@ lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t s
     LV_TMARK(0);
     lvbgs_k_eval<<<totalTiles, blk, 0, st>>>(P);
     LV_TMARK(1);
+    {
+        // long scans: a grid sized to the device, striding over the list the evaluation built
+        const int longBlocks = std::max(1, std::min(g_sm_count * 8, (int)((totalPx + kThreads - 1) / kThreads)));
+        lvbgs_k_longscan<<<longBlocks, blk, 0, st>>>(P);
+        LV_TMARK(2);
+    }
     lvbgs_k_resolve<<<totalTiles + dsBlocks, blk, 0, st>>>(P, ds, dsb);
-    LV_TMARK(2);
+    LV_TMARK(3);
     {
         const int grid = std::max(1, std::min(maxBlocks, std::max(1, totalTiles)));
         void* args[] = {&P};
         LV_CUDA(errh, cudaLaunchCooperativeKernel((const void*)lvbgs_k_repair, dim3(grid), blk, args, 0, st),
                 "repair kernel launch");
     }
-    LV_TMARK(3);
-    lvbgs_k_commit<<<totalTiles, blk, 0, st>>>(P);
     LV_TMARK(4);
-    lvbgs_k_runs<<<rowBlocks, blk, 0, st>>>(P);
+    lvbgs_k_commit<<<totalTiles, blk, 0, st>>>(P);
     LV_TMARK(5);
-    lvbgs_k_vunion<<<rowBlocks, blk, 0, st>>>(P);
+    lvbgs_k_runs<<<rowBlocks, blk, 0, st>>>(P);
     LV_TMARK(6);
-    lvbgs_k_holes<<<rowBlocks, blk, 0, st>>>(P);
+    lvbgs_k_vunion<<<rowBlocks, blk, 0, st>>>(P);
     LV_TMARK(7);
-    lvbgs_k_combine<<<rowBlocks, blk, 0, st>>>(P);
+    lvbgs_k_holes<<<rowBlocks, blk, 0, st>>>(P);
     LV_TMARK(8);
-    lvbgs_k_hcount<<<totalRows, 128, 0, st>>>(P);
+    lvbgs_k_combine<<<rowBlocks, blk, 0, st>>>(P);
     LV_TMARK(9);
-    lvbgs_k_median<<<dim3(P.colBlocks, std::max(1, totalSegs)), blk, 0, st>>>(P);
+    lvbgs_k_hcount<<<totalRows, 128, 0, st>>>(P);
     LV_TMARK(10);
-    lvbgs_k_epilogue<<<1, 128, 0, st>>>(P);
+    lvbgs_k_median<<<dim3(P.colBlocks, std::max(1, totalSegs)), blk, 0, st>>>(P);
     LV_TMARK(11);
-    lvbgs_k_dilate<<<totalRows, 128, 0, st>>>(P);
+    lvbgs_k_epilogue<<<1, 128, 0, st>>>(P);
     LV_TMARK(12);
-    lvbgs_k_reset<<<std::max(1, std::min(totalTiles, g_sm_count * 8)), blk, 0, st>>>(P);
+    lvbgs_k_dilate<<<totalRows, 128, 0, st>>>(P);
     LV_TMARK(13);
-    lvbgs_k_close<<<1, 128, 0, st>>>(P);
+    lvbgs_k_reset<<<std::max(1, std::min(totalTiles, g_sm_count * 8)), blk, 0, st>>>(P);
     LV_TMARK(14);
+    lvbgs_k_close<<<1, 128, 0, st>>>(P);
+    LV_TMARK(15);
 #undef LV_TMARK
     LV_CUDA(errh, cudaGetLastError(), "frame step launch");
     return LVBGS_OK;

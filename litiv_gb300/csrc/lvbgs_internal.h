@@ -171,6 +171,7 @@ struct TickWork {
     unsigned long long rematched;
     unsigned long long ts[40];  // %globaltimer after each grid barrier (CTA 0), for the phase profile
     unsigned int nts, anyReset;  // anyReset: some stream refreshes its model this frame
+    unsigned int lcount, pad;    // long sample scans deferred by the evaluation (list in rlist[0..1])
 };
 
 // error codes reported in TickWork::err
@@ -191,6 +192,7 @@ struct TickParams {
 // mask bit planes of a stream (scratch of one frame step; bits beyond the frame width are 0)
 enum { BP_CLOSED = 0, BP_RAW, BP_HOLES, BP_COMB, BP_FG, BP_COUNT };
 constexpr int kMedSegRows = 32;  // rows of one median column segment
+constexpr int kScanCap = 8;      // samples the evaluation scans per pixel before deferring to a long scan
 __host__ __device__ __forceinline__ uint32_t* bit_plane(const StreamDev& S, int i) {
     return S.bits + (size_t)i * S.H * S.rowWords;
 }

@@ -240,121 +240,148 @@ __device__ __forceinline__ void load_pix(const StreamDev& S, const FrameK& F, in
     }
 }
 
+// thresholds of one evaluation from R(x) and the previous unstable flag, and the new unstable flag
+struct EvalThr {
+    uint32_t colThr;
+    unsigned long long descThr;
+    uint32_t uNew;
+};
+__device__ __forceinline__ EvalThr eval_thresholds(const StreamDev& S, float R, float RwLT, float RwST, float FnLT,
+                                                   float FnST, uint32_t uOld) {
+    EvalThr t;
+    t.colThr =
+        (uint32_t)__float2ull_rz(R * (float)S.minColor - (float)((uint32_t)(uOld == 0u) * (uint32_t)S.stabColorOff));
+    t.descThr = (1ull << (unsigned)__float2ull_rz(floorf(R + 0.5f))) + (unsigned long long)S.descOff +
+                (unsigned long long)uOld * S.descOff;
+    t.uNew = (R > 3.000f || (RwLT - FnLT) > 0.100f || (RwST - FnST) > 0.100f) ? 1u : 0u;
+    return t;
+}
+
+// state of the ordered sample scan: next sample, good samples so far, minima over the good ones
+struct ScanSt {
+    int s, nGood;
+    uint32_t minDesc, minSum;
+};
+
+// one sample against the pixel (the body of the sample loops, :226-250 / :357-393): whether it is a
+// good match, and its descriptor and summed distances
+template <int C>
+__device__ __forceinline__ bool sample_match(const uint8_t* __restrict__ lut, const uint32_t (&vals)[C][4],
+                                             const uint32_t (&curr)[C], const uint32_t (&intra)[C],
+                                             const EvalThr& th, uint64_t d, uint32_t c2, uint32_t& dd,
+                                             uint32_t& sd) {
+    if (C == 1) {
+        const uint32_t cthr = th.colThr / 2u;
+        const uint32_t bgc = c2, bgd = (uint32_t)d;
+        const uint32_t colDist = (uint32_t)abs((int)curr[0] - (int)bgc);
+        if (colDist > cthr) return false;
+        const uint32_t intraD = __popc(intra[0] ^ bgd);
+        const uint32_t interD = __popc(lbsp_thr(vals[0], bgc, lut[bgc]) ^ bgd);
+        const uint32_t descDist = (intraD + interD) / 2u;
+        if ((unsigned long long)descDist > th.descThr) return false;
+        uint32_t sumDist = (descDist / 4u) * 15u + colDist;
+        if (sumDist > 255u) sumDist = 255u;
+        if (sumDist > cthr) return false;
+        dd = descDist;
+        sd = sumDist;
+        return true;
+    } else {
+        const uint32_t totColThr = th.colThr * 3u, scThr = totColThr / 2u;
+        const unsigned long long totDescThr = th.descThr * 3ull;
+        uint32_t totDesc = 0, totSum = 0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const uint32_t bgc = c == 0 ? (uint32_t)(d >> 48) & 0xffu : c == 1 ? (uint32_t)(d >> 56) & 0xffu : c2;
+            const uint32_t bgd = (uint32_t)(d >> (16 * c)) & 0xffffu;
+            const uint32_t colDist = (uint32_t)abs((int)curr[c] - (int)bgc);
+            if (colDist > scThr) return false;
+            const uint32_t intraD = __popc(intra[c] ^ bgd);
+            const uint32_t interD = __popc(lbsp_thr(vals[c], bgc, lut[bgc]) ^ bgd);
+            const uint32_t descDist = (intraD + interD) / 2u;
+            uint32_t sumDist = (descDist / 2u) * 15u + colDist;
+            if (sumDist > 255u) sumDist = 255u;
+            if (sumDist > scThr) return false;
+            totDesc += descDist;
+            totSum += sumDist;
+        }
+        if ((unsigned long long)totDesc > totDescThr || totSum > totColThr) return false;
+        dd = totDesc;
+        sd = totSum;
+        return true;
+    }
+}
+
+// the ordered sample scan, continued from state st until nreq good samples or sample sEnd; dA/cA and
+// dB/cB hold samples st.s and st.s+1 (they arrive with the feedback maps), and the loop requests
+// sample s+2 while it evaluates sample s. OVR: the samples that earlier pixels overwrite this frame
+// (repair)
+template <int C>
+__device__ __forceinline__ void scan_init(ScanSt& st) {
+    st.s = 0;
+    st.nGood = 0;
+    st.minDesc = C == 1 ? 16u : 48u;
+    st.minSum = C == 1 ? 255u : 765u;
+}
 template <int C, bool OVR>
-__device__ uint32_t eval_pixel(const StreamDev& S, const FrameK& F, const uint8_t* __restrict__ lut, int x, int y,
-                               int p, const PixIn<C>& in, const uint32_t (&vals)[C][4], const uint32_t (&curr)[C],
-                               const uint32_t (&intra)[C], const Ovr* ov, int nov, uint64_t ovmask, int& nz,
-                               int& e_out) {
+__device__ __forceinline__ void scan_samples(const StreamDev& S, const uint8_t* __restrict__ lut, int p,
+                                             const uint32_t (&vals)[C][4], const uint32_t (&curr)[C],
+                                             const uint32_t (&intra)[C], const EvalThr& th, const Ovr* ov, int nov,
+                                             uint64_t ovmask, int sEnd, uint64_t dA, uint32_t cA, uint64_t dB,
+                                             uint32_t cB, ScanSt& st) {
+    const int npx = S.npx, N = S.N, nreq = S.nreq;
+    const int sMax = sEnd < N ? sEnd : N;
+    int nGood = st.nGood, s = st.s;
+    uint32_t minDesc = st.minDesc, minSum = st.minSum;
+    while (nGood < nreq && s < sMax) {
+        uint64_t d = dA;
+        uint32_t c2 = cA;
+        dA = dB;
+        cA = cB;
+        if (s + 2 < N) {
+            dB = C == 3 ? ((const uint64_t*)S.sD)[(size_t)(s + 2) * npx + p]
+                        : (uint64_t)((const uint16_t*)S.sD)[(size_t)(s + 2) * npx + p];
+            cB = S.sC[(size_t)(s + 2) * npx + p];
+        }
+        if (OVR && ((ovmask >> s) & 1ull)) {
+            int k = nov - 1;
+            while (ov[k].s != s) --k;
+            if (C == 3) {
+                d = ov[k].desc | ((uint64_t)(ov[k].col & 0xffffu) << 48);
+                c2 = (ov[k].col >> 16) & 0xffu;
+            } else {
+                d = ov[k].desc & 0xffffu;
+                c2 = ov[k].col & 0xffu;
+            }
+        }
+        uint32_t dd, sd;
+        if (sample_match<C>(lut, vals, curr, intra, th, d, c2, dd, sd)) {
+            if (minDesc > dd) minDesc = dd;
+            if (minSum > sd) minSum = sd;
+            ++nGood;
+        }
+        ++s;
+    }
+    st.s = s;
+    st.nGood = nGood;
+    st.minDesc = minDesc;
+    st.minSum = minSum;
+}
+
+// the rest of one evaluation after the sample scan (:254-330 / :396-481): D_last, D_min, the raw
+// segmentation averages, the model/neighbour update decisions and draws, T, v and R; writes the
+// next-frame maps and returns the intent word
+template <int C>
+__device__ uint32_t eval_tail(const StreamDev& S, const FrameK& F, int x, int y, int p, const PixIn<C>& in,
+                              const uint32_t (&curr)[C], const uint32_t (&intra)[C], uint32_t uNew,
+                              const ScanSt& st) {
     const int npx = S.npx;
     float* fn = S.fm + (size_t)F.nxt * kNumFloatMaps * npx;
     float R = in.R, V = in.V, T = in.T;
     const float DL = in.DL;
     float DmLT = in.DmLT, DmST = in.DmST, RwLT = in.RwLT, RwST = in.RwST;
-    const float FnLT = in.FnLT, FnST = in.FnST;
-    const uint32_t uOld = in.uOld, lastFG = in.lastFG, blink = in.blink;
-
-    // thresholds from R(x) and the previous unstable flag
-    const uint32_t colThr =
-        (uint32_t)__float2ull_rz(R * (float)S.minColor - (float)((uint32_t)(uOld == 0u) * (uint32_t)S.stabColorOff));
-    const unsigned long long descThr = (1ull << (unsigned)__float2ull_rz(floorf(R + 0.5f))) +
-                                       (unsigned long long)S.descOff + (unsigned long long)uOld * S.descOff;
-    const uint32_t uNew =
-        (R > 3.000f || (RwLT - FnLT) > 0.100f || (RwST - FnST) > 0.100f) ? 1u : 0u;
-
-    const int N = S.N, nreq = S.nreq;
-    int nGood = 0, s = 0;
-    uint32_t minDesc = C == 1 ? 16u : 48u, minSum = C == 1 ? 255u : 765u;
-    // Samples 0 and 1 arrive with the feedback maps; the loop then requests sample s+2 while it
-    // evaluates sample s (a rotating pair). The kernel is latency-bound, so the up-to-two wasted
-    // sample reads of an early exit are cheaper than waiting on a load.
-    if (C == 1) {
-        const uint32_t cthr = colThr / 2u;
-        const uint16_t* sD = (const uint16_t*)S.sD;
-        uint32_t dA = (uint32_t)in.d0, dB = (uint32_t)in.d1, cA = in.c0, cB = in.c1;
-        while (nGood < nreq && s < N) {
-            uint32_t bgc = cA, bgd = dA;
-            dA = dB;
-            cA = cB;
-            if (s + 2 < N) {
-                dB = sD[(size_t)(s + 2) * npx + p];
-                cB = S.sC[(size_t)(s + 2) * npx + p];
-            }
-            if (OVR && ((ovmask >> s) & 1ull)) {
-                int k = nov - 1;
-                while (ov[k].s != s) --k;
-                bgc = ov[k].col & 0xffu;
-                bgd = (uint32_t)(ov[k].desc & 0xffffu);
-            }
-            const uint32_t colDist = (uint32_t)abs((int)curr[0] - (int)bgc);
-            if (colDist <= cthr) {
-                const uint32_t intraD = __popc(intra[0] ^ bgd);
-                const uint32_t interD = __popc(lbsp_thr(vals[0], bgc, lut[bgc]) ^ bgd);
-                const uint32_t descDist = (intraD + interD) / 2u;
-                if ((unsigned long long)descDist <= descThr) {
-                    uint32_t sumDist = (descDist / 4u) * 15u + colDist;
-                    if (sumDist > 255u) sumDist = 255u;
-                    if (sumDist <= cthr) {
-                        if (minDesc > descDist) minDesc = descDist;
-                        if (minSum > sumDist) minSum = sumDist;
-                        ++nGood;
-                    }
-                }
-            }
-            ++s;
-        }
-    } else {
-        const uint32_t totColThr = colThr * 3u, scThr = totColThr / 2u;
-        const unsigned long long totDescThr = descThr * 3ull;
-        const uint64_t* sD = (const uint64_t*)S.sD;
-        uint64_t dA = in.d0, dB = in.d1;
-        uint32_t cA = in.c0, cB = in.c1;
-        while (nGood < nreq && s < N) {
-            uint64_t d = dA;
-            uint32_t c2 = cA;
-            dA = dB;
-            cA = cB;
-            if (s + 2 < N) {
-                dB = sD[(size_t)(s + 2) * npx + p];
-                cB = S.sC[(size_t)(s + 2) * npx + p];
-            }
-            if (OVR && ((ovmask >> s) & 1ull)) {
-                int k = nov - 1;
-                while (ov[k].s != s) --k;
-                d = ov[k].desc | ((uint64_t)(ov[k].col & 0xffffu) << 48);
-                c2 = (ov[k].col >> 16) & 0xffu;
-            }
-            uint32_t totDesc = 0, totSum = 0;
-            bool ok = true;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const uint32_t bgc = c == 0 ? (uint32_t)(d >> 48) & 0xffu : c == 1 ? (uint32_t)(d >> 56) & 0xffu : c2;
-                const uint32_t bgd = (uint32_t)(d >> (16 * c)) & 0xffffu;
-                const uint32_t colDist = (uint32_t)abs((int)curr[c] - (int)bgc);
-                if (colDist > scThr) {
-                    ok = false;
-                    break;
-                }
-                const uint32_t intraD = __popc(intra[c] ^ bgd);
-                const uint32_t interD = __popc(lbsp_thr(vals[c], bgc, lut[bgc]) ^ bgd);
-                const uint32_t descDist = (intraD + interD) / 2u;
-                uint32_t sumDist = (descDist / 2u) * 15u + colDist;
-                if (sumDist > 255u) sumDist = 255u;
-                if (sumDist > scThr) {
-                    ok = false;
-                    break;
-                }
-                totDesc += descDist;
-                totSum += sumDist;
-            }
-            if (ok && !((unsigned long long)totDesc > totDescThr || totSum > totColThr)) {
-                if (minDesc > totDesc) minDesc = totDesc;
-                if (minSum > totSum) minSum = totSum;
-                ++nGood;
-            }
-            ++s;
-        }
-    }
-    e_out = s;
+    const uint32_t lastFG = in.lastFG, blink = in.blink;
+    const int nreq = S.nreq, nGood = st.nGood, s = st.s;
+    const uint32_t minDesc = st.minDesc, minSum = st.minSum;
 
     // D_last (:254-255 / :396-397): depends on the pixel alone
     uint32_t l1 = 0, hd = 0;
@@ -447,11 +474,6 @@ __device__ uint32_t eval_pixel(const StreamDev& S, const FrameK& F, const uint8_
         R -= 0.01f / V;
         if (R < 1.0f) R = 1.0f;
     }
-    uint32_t pc = 0;
-#pragma unroll
-    for (int c = 0; c < C; ++c) pc += __popc(intra[c]);
-    nz = pc >= (C == 1 ? 2u : 4u) ? 1 : 0;
-
     fn[FM_R * npx + p] = R;
     fn[FM_V * npx + p] = V;
     fn[FM_T * npx + p] = T;
@@ -469,6 +491,28 @@ __device__ uint32_t eval_pixel(const StreamDev& S, const FrameK& F, const uint8_
         __stcg(&ldn[c], (uint16_t)intra[c]);
     }
     return intent;
+}
+
+// a full evaluation: thresholds, the whole ordered scan, the tail (the repair's re-match)
+template <int C, bool OVR>
+__device__ uint32_t eval_pixel(const StreamDev& S, const FrameK& F, const uint8_t* __restrict__ lut, int x, int y,
+                               int p, const PixIn<C>& in, const uint32_t (&vals)[C][4], const uint32_t (&curr)[C],
+                               const uint32_t (&intra)[C], const Ovr* ov, int nov, uint64_t ovmask, int& e_out) {
+    const EvalThr th = eval_thresholds(S, in.R, in.RwLT, in.RwST, in.FnLT, in.FnST, in.uOld);
+    ScanSt st;
+    scan_init<C>(st);
+    scan_samples<C, OVR>(S, lut, p, vals, curr, intra, th, ov, nov, ovmask, S.N, in.d0, in.c0, in.d1, in.c1, st);
+    e_out = st.s;
+    return eval_tail<C>(S, F, x, y, p, in, curr, intra, th.uNew, st);
+}
+
+// non-zero LBSP descriptor test of the frame-level statistics (:264-265 / :405-407)
+template <int C>
+__device__ __forceinline__ int desc_nonzero(const uint32_t (&intra)[C]) {
+    uint32_t pc = 0;
+#pragma unroll
+    for (int c = 0; c < C; ++c) pc += __popc(intra[c]);
+    return pc >= (C == 1 ? 2u : 4u) ? 1 : 0;
 }
 
 // gathers the 16 LBSP taps of channel c at (x, y) from a byte image (tile or frame)
@@ -490,7 +534,7 @@ __device__ __forceinline__ void gather_taps(const uint8_t* base, int rowStride, 
 // phase A: evaluate every pixel of a tile against the frame-start model
 // ------------------------------------------------------------------------------------------
 template <int C>
-__device__ void phaseA_tile(const TickParams& P, const StreamDev& S, int lt, uint8_t* smem) {
+__device__ void phaseA_tile(const TickParams& P, int si, const StreamDev& S, int lt, uint8_t* smem) {
     const int tx = lt % S.tilesX, ty = lt / S.tilesX;
     const int x0 = tx * kTileW, y0 = ty * kTileH;
     // The tile holds rows y0-2 .. y0+9 of the frame; row r of the tile starts at frame byte
@@ -535,7 +579,9 @@ __device__ void phaseA_tile(const TickParams& P, const StreamDev& S, int lt, uin
         *(uint32_t*)(tile + r * RW + 4 * wi) = v;
     }
     __syncthreads();
-    int nz = 0, e = 0;
+    int nz = 0;
+    bool defer = false;
+    unsigned long long scanWord = 0;
     if (inFrame) {
         uint32_t intent = 0;
         if (active) {
@@ -547,9 +593,42 @@ __device__ void phaseA_tile(const TickParams& P, const StreamDev& S, int lt, uin
                 curr[c] = base[c];
                 intra[c] = lbsp_thr(vals[c], curr[c], lut[curr[c]]);
             }
-            intent = eval_pixel<C, false>(S, F, lut, x, y, p, in, vals, curr, intra, nullptr, 0, 0ull, nz, e);
+            nz = desc_nonzero<C>(intra);
+            const EvalThr th = eval_thresholds(S, in.R, in.RwLT, in.RwST, in.FnLT, in.FnST, in.uOld);
+            ScanSt st;
+            scan_init<C>(st);
+            scan_samples<C, false>(S, lut, p, vals, curr, intra, th, nullptr, 0, 0ull, kScanCap, in.d0, in.c0, in.d1,
+                                   in.c1, st);
+            if (st.nGood < S.nreq && st.s < S.N) {
+                // a long scan: continued and finished by lvbgs_k_longscan over the compacted list, so
+                // that its warps hold only long scans
+                defer = true;
+                scanWord = (unsigned long long)st.s | ((unsigned long long)st.nGood << 16) |
+                           ((unsigned long long)st.minDesc << 32) | ((unsigned long long)st.minSum << 48);
+            } else {
+                intent = eval_tail<C>(S, F, x, y, p, in, curr, intra, th.uNew, st);
+            }
         }
         __stcg(&S.intent[p], intent);
+    }
+    {
+        // warp-aggregated append to the long-scan list (pixel key, scan state)
+        const unsigned m = __ballot_sync(0xffffffffu, defer);
+        if (m) {
+            const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+            unsigned int base = 0;
+            if (lane == leader) base = atomicAdd(&P.work->lcount, (unsigned int)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (defer) {
+                const unsigned int i = base + (unsigned int)__popc(m & ((1u << lane) - 1u));
+                if (i < P.listCap) {
+                    P.rlist[0][i] = ((unsigned long long)si << 40) | (unsigned long long)(unsigned)p;
+                    P.rlist[1][i] = scanWord;
+                } else {
+                    atomicOr(&P.work->err, ERR_REPAIR_LIMIT);
+                }
+            }
+        }
     }
     // per-warp reduction of the non-zero descriptor count (final: the descriptor does not depend
     // on the repair)
@@ -722,10 +801,10 @@ __device__ void rematch_item(const TickParams& P, int si, const StreamDev& S, in
         intra[c] = lbsp_thr(vals[c], curr[c], S.ctl->lut[curr[c]]);
     }
     atomicAdd(&S.ctl->st_rematched, 1ull);
-    int nz = 0, e = 0;
+    int e = 0;
     PixIn<C> in;
     load_pix<C>(S, F, q, in);
-    uint32_t wNew = eval_pixel<C, true>(S, F, S.ctl->lut, x, y, q, in, vals, curr, intra, ov, nov, mask, nz, e);
+    uint32_t wNew = eval_pixel<C, true>(S, F, S.ctl->lut, x, y, q, in, vals, curr, intra, ov, nov, mask, e);
     const bool decChanged = ((wNew ^ wOld) & kInFG) != 0u;
     if (!decChanged) {
         // same decision: same draws, same updates; keep the resolved neighbour state
@@ -1341,8 +1420,64 @@ __device__ void refresh_pixel(const StreamDev& S, int p, uint32_t frame, int sta
 extern "C" __global__ void __launch_bounds__(kThreads, 3) lvbgs_k_eval(TickParams P) {
     __shared__ __align__(16) uint8_t smem[((((kTileW + 4) * 3 + 2 + 3) / 4) * 4) * (kTileH + 4) + 256];
     LV_TILE_KERNEL_PROLOGUE
-    if (S.C == 3) phaseA_tile<3>(P, S, lt, smem);
-    else phaseA_tile<1>(P, S, lt, smem);
+    if (S.C == 3) phaseA_tile<3>(P, si, S, lt, smem);
+    else phaseA_tile<1>(P, si, S, lt, smem);
+}
+
+// ------------------------------------------------------------------------------------------
+// long sample scans: the pixels whose ordered scan did not settle within the first kScanCap samples
+// (foreground pixels scan all N) continue here, one thread per pixel of the compacted list, from the
+// saved scan state; then the rest of their evaluation. Spatially sparse long scans would otherwise
+// keep whole warps of the evaluation waiting on a few lanes.
+// ------------------------------------------------------------------------------------------
+template <int C>
+__device__ void longscan_item(const TickParams& P, unsigned int i) {
+    const unsigned long long key = __ldcg(&P.rlist[0][i]);
+    const unsigned long long sw = __ldcg(&P.rlist[1][i]);
+    const int si = (int)(key >> 40), p = (int)(key & 0xffffffffffull);
+    const StreamDev& S = P.streams[si];
+    const FrameK F = frame_consts(S);
+    const int W = S.W, x = p % W, y = p / W, npx = S.npx, N = S.N;
+    ScanSt st;
+    st.s = (int)(sw & 0xffffu);
+    st.nGood = (int)((sw >> 16) & 0xffffu);
+    st.minDesc = (uint32_t)((sw >> 32) & 0xffffu);
+    st.minSum = (uint32_t)(sw >> 48);
+    // samples s and s+1 with the feedback maps
+    uint64_t dA = 0, dB = 0;
+    uint32_t cA = 0, cB = 0;
+    if (st.s < N) {
+        dA = C == 3 ? ((const uint64_t*)S.sD)[(size_t)st.s * npx + p] : (uint64_t)((const uint16_t*)S.sD)[(size_t)st.s * npx + p];
+        cA = S.sC[(size_t)st.s * npx + p];
+    }
+    if (st.s + 1 < N) {
+        dB = C == 3 ? ((const uint64_t*)S.sD)[(size_t)(st.s + 1) * npx + p]
+                    : (uint64_t)((const uint16_t*)S.sD)[(size_t)(st.s + 1) * npx + p];
+        cB = S.sC[(size_t)(st.s + 1) * npx + p];
+    }
+    PixIn<C> in;
+    load_pix<C>(S, F, p, in);
+    uint32_t vals[C][4], curr[C], intra[C];
+    const uint8_t* base = S.frame + (size_t)p * C;
+    const uint8_t* lut = S.ctl->lut;
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        gather_taps<C>(base, W * C, c, vals[c]);
+        curr[c] = __ldg(base + c);
+        intra[c] = lbsp_thr(vals[c], curr[c], lut[curr[c]]);
+    }
+    const EvalThr th = eval_thresholds(S, in.R, in.RwLT, in.RwST, in.FnLT, in.FnST, in.uOld);
+    scan_samples<C, false>(S, lut, p, vals, curr, intra, th, nullptr, 0, 0ull, N, dA, cA, dB, cB, st);
+    __stcg(&S.intent[p], eval_tail<C>(S, F, x, y, p, in, curr, intra, th.uNew, st));
+}
+
+extern "C" __global__ void __launch_bounds__(256) lvbgs_k_longscan(TickParams P) {
+    const unsigned int n = min(ld_volatile(&P.work->lcount), P.listCap);
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int si = (int)(__ldcg(&P.rlist[0][i]) >> 40);
+        if (P.streams[si].C == 3) longscan_item<3>(P, i);
+        else longscan_item<1>(P, i);
+    }
 }
 
 extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_resolve(TickParams P, unsigned long long dsTotal,
