@@ -23,11 +23,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "SuBSENSE Mpix/s: batched 64-stream vs plain 1-stream on GB300; p99 frame ms"
-# DRAM bytes (read + write) of one evaluation-kernel launch per pixel, from an ncu capture of
-# dram__bytes_read.sum + dram__bytes_write.sum on six streams of the mix (indices 52-57: four
-# 1280x720, one of them gray, and two 1920x1080; 7,833,600 px): 1,047,309,312 + 335,310,592 bytes.
-# roofline.traffic scales it to the launch by pixels.
-EVAL_DRAM_BYTES_PER_PX = (1047309312 + 335310592) / 7833600
+# DRAM bytes (read + write) of the evaluation per pixel (lvbgs_k_eval + lvbgs_k_longscan), from an
+# ncu capture of dram__bytes_read.sum + dram__bytes_write.sum on six streams of the mix (indices
+# 52-57: four 1280x720, one of them gray, and two 1920x1080; 7,833,600 px): eval 902,353,152 +
+# 335,219,456 bytes, long scans 351,425,792 + 36,874,240 bytes. roofline.traffic scales it to a tick
+# by pixels.
+EVAL_DRAM_BYTES_PER_PX = (902353152 + 335219456 + 351425792 + 36874240) / 7833600
 WORKLOAD = ("subsense-mix64: 16x320x240 + 24x640x480 + 16x1280x720 + 8x1920x1080, 48 BGR + 16 gray, "
             "default parameters, synthetic seeded scenes")
 # CPU sample: 4 streams of each resolution class
@@ -255,9 +256,18 @@ def main():
                     help="frames of the PAWCS workload (640x480 thermal-like scene; 0: skip)")
     ap.add_argument("--serving-seconds", type=float, default=20.0,
                     help="measured span of the serving workload run (0: skip)")
+    ap.add_argument("--pawcs-only", action="store_true",
+                    help="run the PAWCS workload alone and print its object (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.pawcs_only:
+        import torch
+        torch.cuda.set_device(0)
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        print(json.dumps(pawcs_run(args.pawcs_frames, stream, cpu=not args.no_cpu_baseline)))
+        return
 
     import numpy as np
     import torch

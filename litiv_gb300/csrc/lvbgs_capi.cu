@@ -382,7 +382,7 @@ lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t s
         lvbgs_k_longscan<<<longBlocks, blk, 0, st>>>(P);
         LV_TMARK(2);
     }
-    lvbgs_k_resolve<<<totalTiles + dsBlocks, blk, 0, st>>>(P, ds, dsb);
+    lvbgs_k_resolve<<<(totalTiles + kResolveTiles - 1) / kResolveTiles + dsBlocks, blk, 0, st>>>(P, ds, dsb);
     LV_TMARK(3);
     {
         const int grid = std::max(1, std::min(maxBlocks, std::max(1, totalTiles)));

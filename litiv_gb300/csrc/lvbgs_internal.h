@@ -192,6 +192,7 @@ struct TickParams {
 // mask bit planes of a stream (scratch of one frame step; bits beyond the frame width are 0)
 enum { BP_CLOSED = 0, BP_RAW, BP_HOLES, BP_COMB, BP_FG, BP_COUNT };
 constexpr int kMedSegRows = 32;  // rows of one median column segment
+constexpr int kResolveTiles = 4;  // tiles per block of the ghost-resolution kernel
 constexpr int kScanCap = 8;      // samples the evaluation scans per pixel before deferring to a long scan
 __host__ __device__ __forceinline__ uint32_t* bit_plane(const StreamDev& S, int i) {
     return S.bits + (size_t)i * S.H * S.rowWords;

@@ -315,6 +315,17 @@ __device__ __forceinline__ bool sample_match(const uint8_t* __restrict__ lut, co
 // dB/cB hold samples st.s and st.s+1 (they arrive with the feedback maps), and the loop requests
 // sample s+2 while it evaluates sample s. OVR: the samples that earlier pixels overwrite this frame
 // (repair)
+// L2 prefetch of sample k of pixel p (both planes): a hint without registers, so that a long scan keeps
+// several samples in flight
+template <int C>
+__device__ __forceinline__ void prefetch_sample(const StreamDev& S, int k, int p) {
+    const void* a = C == 3 ? (const void*)((const uint64_t*)S.sD + (size_t)k * S.npx + p)
+                           : (const void*)((const uint16_t*)S.sD + (size_t)k * S.npx + p);
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(S.sC + (size_t)k * S.npx + p));
+}
+constexpr int kScanPrefetch = 8;  // samples prefetched ahead of the loads of a long scan
+
 template <int C>
 __device__ __forceinline__ void scan_init(ScanSt& st) {
     st.s = 0;
@@ -332,6 +343,10 @@ __device__ __forceinline__ void scan_samples(const StreamDev& S, const uint8_t* 
     const int sMax = sEnd < N ? sEnd : N;
     int nGood = st.nGood, s = st.s;
     uint32_t minDesc = st.minDesc, minSum = st.minSum;
+    // scans that may run past the evaluation's cap (long scans, repair) prefetch ahead into L2
+    const bool deep = sMax > kScanCap;
+    if (deep && nGood < nreq)
+        for (int k = s + 2; k < min(N, s + 2 + kScanPrefetch); ++k) prefetch_sample<C>(S, k, p);
     while (nGood < nreq && s < sMax) {
         uint64_t d = dA;
         uint32_t c2 = cA;
@@ -341,6 +356,7 @@ __device__ __forceinline__ void scan_samples(const StreamDev& S, const uint8_t* 
             dB = C == 3 ? ((const uint64_t*)S.sD)[(size_t)(s + 2) * npx + p]
                         : (uint64_t)((const uint16_t*)S.sD)[(size_t)(s + 2) * npx + p];
             cB = S.sC[(size_t)(s + 2) * npx + p];
+            if (deep && s + 2 + kScanPrefetch < N) prefetch_sample<C>(S, s + 2 + kScanPrefetch, p);
         }
         if (OVR && ((ovmask >> s) & 1ull)) {
             int k = nov - 1;
@@ -515,6 +531,56 @@ __device__ __forceinline__ int desc_nonzero(const uint32_t (&intra)[C]) {
     return pc >= (C == 1 ? 2u : 4u) ? 1 : 0;
 }
 
+// adds two per-thread counts of a tile block to per-stream counters with one atomic each per block
+// (every thread of the block calls it; b may be null)
+__device__ __forceinline__ void block_add_stats(unsigned long long* a, unsigned long long va, unsigned long long* b,
+                                                unsigned long long vb) {
+    __shared__ unsigned long long red[2][kThreads / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        va += __shfl_xor_sync(0xffffffffu, va, o);
+        vb += __shfl_xor_sync(0xffffffffu, vb, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = va;
+        red[1][threadIdx.x >> 5] = vb;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long sa = 0, sb = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            sa += red[0][i];
+            sb += red[1][i];
+        }
+        if (sa) atomicAdd(a, sa);
+        if (b && sb) atomicAdd(b, sb);
+    }
+}
+
+// block-aggregated list reservation: every thread of the block calls it; returns this thread's slot
+// (or ~0u when it does not want one). One counter atomic per block: the lists' counters are shared by
+// all streams of the batch, and same-address atomics serialize.
+__device__ __forceinline__ unsigned int block_reserve(bool want, unsigned int* count) {
+    __shared__ unsigned int sWarp[32];
+    __shared__ unsigned int sBase;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned m = __ballot_sync(0xffffffffu, want);
+    if (lane == 0) sWarp[warp] = __popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int run = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            const unsigned int v = sWarp[i];
+            sWarp[i] = run;
+            run += v;
+        }
+        sBase = run ? atomicAdd(count, run) : 0u;
+    }
+    __syncthreads();
+    const unsigned int r = want ? sBase + sWarp[warp] + (unsigned int)__popc(m & ((1u << lane) - 1u)) : ~0u;
+    __syncthreads();  // the shared slots are reused by the next call
+    return r;
+}
+
 // gathers the 16 LBSP taps of channel c at (x, y) from a byte image (tile or frame)
 template <int C>
 __device__ __forceinline__ void gather_taps(const uint8_t* base, int rowStride, int c, uint32_t (&v)[4]) {
@@ -639,25 +705,6 @@ __device__ void phaseA_tile(const TickParams& P, int si, const StreamDev& S, int
 // ------------------------------------------------------------------------------------------
 // list helpers for the repair loop
 // ------------------------------------------------------------------------------------------
-// warp-aggregated push: every lane of the warp calls it (want = whether this lane pushes); one
-// counter atomic per warp instead of one per item
-__device__ __forceinline__ void push_item_warp(bool want, unsigned long long* list, unsigned int* count,
-                                               unsigned int cap, uint32_t* stamps, uint32_t stamp, int si, int p,
-                                               TickWork* w) {
-    const bool ok = want && atomicExch(&stamps[p], stamp) != stamp;
-    const unsigned int m = __ballot_sync(0xffffffffu, ok);
-    if (!m) return;
-    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
-    unsigned int base = 0;
-    if (lane == leader) base = atomicAdd(count, (unsigned int)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (ok) {
-        const unsigned int i = base + (unsigned int)__popc(m & ((1u << lane) - 1u));
-        if (i < cap) list[i] = ((unsigned long long)si << 40) | (unsigned long long)(unsigned)p;
-        else atomicOr(&w->err, ERR_REPAIR_LIMIT);
-    }
-}
-
 __device__ __forceinline__ void push_item(unsigned long long* list, unsigned int* count, unsigned int cap,
                                           uint32_t* stamps, uint32_t stamp, int si, int p, TickWork* w) {
     if (atomicExch(&stamps[p], stamp) == stamp) return;
@@ -689,31 +736,76 @@ __device__ __forceinline__ uint32_t set_nst(uint32_t w, uint32_t st) {
 }
 
 // phase B: resolve pending ghost tests with the phase-A values; mark the pixels whose evaluated
-// samples an earlier pixel overwrites (initial repair frontier)
-__device__ void phaseB_tile(const TickParams& P, int si, const StreamDev& S, int lt) {
-    const int tx = lt % S.tilesX, ty = lt / S.tilesX;
-    const int x = tx * kTileW + threadIdx.x % kTileW, y = ty * kTileH + threadIdx.x / kTileW;
-    const bool in = x < S.W && y < S.H;
-    const int p = y * S.W + x;
-    uint32_t w = in ? __ldcg(&S.intent[p]) : 0u;
-    bool want = false;
-    int q = 0;
-    if (w & kInValid) {
-        if (in_nst(w) == NB_PENDING) {
-            const FrameK F = frame_consts(S);
-            w = set_nst(w, resolve_ghost(S, F, p, code_target((int)in_code(w), x, y, S.W)));
-            __stcg(&S.intent[p], w);
+// samples an earlier pixel overwrites (initial repair frontier). A block takes kResolveTiles tiles,
+// one pixel of each per thread, with the loads of all of them issued before any is used: the work
+// is a short chain of dependent loads per pixel, so more pixels in flight per thread hide it.
+__device__ void phaseB_tiles(const TickParams& P, int t0) {
+    // the stream of each tile and its stamp, found once per block
+    __shared__ int sSi[kResolveTiles];
+    __shared__ uint32_t sStamp[kResolveTiles];
+    if (threadIdx.x < kResolveTiles) {
+        const int t = t0 + (int)threadIdx.x;
+        int si = 0;
+        uint32_t stamp = 0;
+        if (t < P.totalTiles) {
+            si = find_stream_by_tile(P, t);
+            stamp = P.streams[si].ctl->stamp_base + 1u;
         }
-        if (in_nb_writes(w)) {
-            q = code_target((int)in_code(w), x, y, S.W);
-            if (q > p) {
-                const uint32_t wq = __ldcg(&S.intent[q]);
-                want = (wq & kInValid) && in_snb(w) < in_e(wq);
+        sSi[threadIdx.x] = si;
+        sStamp[threadIdx.x] = stamp;
+    }
+    __syncthreads();
+    uint32_t w[kResolveTiles];
+    int ps[kResolveTiles], xs[kResolveTiles], ys[kResolveTiles];
+#pragma unroll
+    for (int j = 0; j < kResolveTiles; ++j) {
+        const int t = t0 + j;
+        w[j] = 0u;
+        ps[j] = xs[j] = ys[j] = 0;
+        if (t < P.totalTiles) {
+            const StreamDev& S = P.streams[sSi[j]];
+            const int lt = t - S.tileBase;
+            const int x = (lt % S.tilesX) * kTileW + threadIdx.x % kTileW;
+            const int y = (lt / S.tilesX) * kTileH + threadIdx.x / kTileW;
+            xs[j] = x;
+            ys[j] = y;
+            if (x < S.W && y < S.H) {
+                ps[j] = y * S.W + x;
+                w[j] = __ldcg(&S.intent[ps[j]]);
             }
         }
     }
-    // all lanes of the warp reach the aggregated push
-    push_item_warp(want, P.dlist[0], &P.work->dcount[0], P.listCap, S.stampD, S.ctl->stamp_base + 1u, si, q, P.work);
+    int qs[kResolveTiles];
+    uint32_t wq[kResolveTiles];
+#pragma unroll
+    for (int j = 0; j < kResolveTiles; ++j) {
+        qs[j] = 0;
+        wq[j] = 0u;
+        if (!(w[j] & kInValid)) continue;
+        const StreamDev& S = P.streams[sSi[j]];
+        if (in_nst(w[j]) == NB_PENDING) {
+            const FrameK F = frame_consts(S);
+            w[j] = set_nst(w[j], resolve_ghost(S, F, ps[j], code_target((int)in_code(w[j]), xs[j], ys[j], S.W)));
+            __stcg(&S.intent[ps[j]], w[j]);
+        }
+        if (in_nb_writes(w[j])) {
+            qs[j] = code_target((int)in_code(w[j]), xs[j], ys[j], S.W);
+            if (qs[j] > ps[j]) wq[j] = __ldcg(&S.intent[qs[j]]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < kResolveTiles; ++j) {
+        if (t0 + j >= P.totalTiles) break;  // uniform over the block
+        const bool want = (w[j] & kInValid) && in_nb_writes(w[j]) && qs[j] > ps[j] && (wq[j] & kInValid) &&
+                          in_snb(w[j]) < in_e(wq[j]);
+        // one list item per target and stamp generation; slots reserved once per block
+        const bool ok = want && atomicExch(&P.streams[sSi[j]].stampD[qs[j]], sStamp[j]) != sStamp[j];
+        const unsigned int i = block_reserve(ok, &P.work->dcount[0]);
+        if (ok) {
+            if (i < P.listCap) P.dlist[0][i] = ((unsigned long long)sSi[j] << 40) | (unsigned long long)(unsigned)qs[j];
+            else atomicOr(&P.work->err, ERR_REPAIR_LIMIT);
+        }
+    }
 }
 
 // frame down-sampling for the frame-level analysis (:568-584): one output pixel per thread
@@ -750,12 +842,12 @@ __device__ void ds_item(const StreamDev& S, int i) {
 // repair loop bodies
 // ------------------------------------------------------------------------------------------
 template <int C>
-__device__ void rematch_item(const TickParams& P, int si, const StreamDev& S, int q, uint32_t stampNext,
+__device__ bool rematch_item(const TickParams& P, int si, const StreamDev& S, int q, uint32_t stampNext,
                              int iterParity) {
     const int W = S.W, x = q % W, y = q / W;
     const FrameK F = frame_consts(S);
     const uint32_t wOld = __ldcg(&S.intent[q]);
-    if (!(wOld & kInValid)) return;
+    if (!(wOld & kInValid)) return false;
     // overrides: earlier pixels of the 5x5 window whose neighbour update targets q, raster order
     Ovr ov[12];
     int nov = 0;
@@ -800,7 +892,6 @@ __device__ void rematch_item(const TickParams& P, int si, const StreamDev& S, in
         curr[c] = __ldg(base + c);
         intra[c] = lbsp_thr(vals[c], curr[c], S.ctl->lut[curr[c]]);
     }
-    atomicAdd(&S.ctl->st_rematched, 1ull);
     int e = 0;
     PixIn<C> in;
     load_pix<C>(S, F, q, in);
@@ -810,7 +901,7 @@ __device__ void rematch_item(const TickParams& P, int si, const StreamDev& S, in
         // same decision: same draws, same updates; keep the resolved neighbour state
         wNew = (wOld & ~(127u << kInEShift)) | ((uint32_t)e << kInEShift);
         __stcg(&S.intent[q], wNew);
-        return;
+        return true;
     }
     __stcg(&S.intent[q], wNew);
     unsigned int* dcnt = &P.work->dcount[iterParity ^ 1];
@@ -840,6 +931,7 @@ __device__ void rematch_item(const TickParams& P, int si, const StreamDev& S, in
                 push_item(rl, rcnt, P.listCap, S.stampR, rstamp, si, p, P.work);
         }
     if (in_nst(wNew) == NB_PENDING) push_item(rl, rcnt, P.listCap, S.stampR, rstamp, si, q, P.work);
+    return true;
 }
 
 __device__ void reresolve_item(const TickParams& P, int si, const StreamDev& S, int p, uint32_t stampNext,
@@ -956,14 +1048,7 @@ __device__ void phaseF_tile(const TickParams& P, const StreamDev& S, int lt, uin
         bit_plane(S, BP_RAW)[o] = rawW;
         bit_plane(S, BP_CLOSED)[o] = closedW;
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        nw += __shfl_xor_sync(0xffffffffu, nw, o);
-        ne += __shfl_xor_sync(0xffffffffu, ne, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        if (nw) atomicAdd(&S.ctl->st_writes, (unsigned long long)nw);
-        if (ne) atomicAdd(&S.ctl->st_samples, (unsigned long long)ne);
-    }
+    block_add_stats(&S.ctl->st_writes, (unsigned long long)nw, &S.ctl->st_samples, (unsigned long long)ne);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1455,23 +1540,31 @@ __device__ void longscan_item(const TickParams& P, unsigned int i) {
                     : (uint64_t)((const uint16_t*)S.sD)[(size_t)(st.s + 1) * npx + p];
         cB = S.sC[(size_t)(st.s + 1) * npx + p];
     }
+    // the scan needs the thresholds only; the feedback maps of the tail are loaded after it, which
+    // keeps the register peak (and so the occupancy) of this latency-bound kernel down
+    const float* fc = S.fm + (size_t)F.cur * kNumFloatMaps * npx;
+    const EvalThr th = eval_thresholds(S, fc[FM_R * npx + p], fc[FM_RAW_LT * npx + p], fc[FM_RAW_ST * npx + p],
+                                       fc[FM_FIN_LT * npx + p], fc[FM_FIN_ST * npx + p],
+                                       S.unst[(size_t)F.cur * npx + p]);
+    uint32_t curr[C], intra[C];
+    {
+        uint32_t vals[C][4];
+        const uint8_t* base = S.frame + (size_t)p * C;
+        const uint8_t* lut = S.ctl->lut;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            gather_taps<C>(base, W * C, c, vals[c]);
+            curr[c] = __ldg(base + c);
+            intra[c] = lbsp_thr(vals[c], curr[c], lut[curr[c]]);
+        }
+        scan_samples<C, false>(S, lut, p, vals, curr, intra, th, nullptr, 0, 0ull, N, dA, cA, dB, cB, st);
+    }
     PixIn<C> in;
     load_pix<C>(S, F, p, in);
-    uint32_t vals[C][4], curr[C], intra[C];
-    const uint8_t* base = S.frame + (size_t)p * C;
-    const uint8_t* lut = S.ctl->lut;
-#pragma unroll
-    for (int c = 0; c < C; ++c) {
-        gather_taps<C>(base, W * C, c, vals[c]);
-        curr[c] = __ldg(base + c);
-        intra[c] = lbsp_thr(vals[c], curr[c], lut[curr[c]]);
-    }
-    const EvalThr th = eval_thresholds(S, in.R, in.RwLT, in.RwST, in.FnLT, in.FnST, in.uOld);
-    scan_samples<C, false>(S, lut, p, vals, curr, intra, th, nullptr, 0, 0ull, N, dA, cA, dB, cB, st);
     __stcg(&S.intent[p], eval_tail<C>(S, F, x, y, p, in, curr, intra, th.uNew, st));
 }
 
-extern "C" __global__ void __launch_bounds__(256) lvbgs_k_longscan(TickParams P) {
+extern "C" __global__ void __launch_bounds__(256, 3) lvbgs_k_longscan(TickParams P) {
     const unsigned int n = min(ld_volatile(&P.work->lcount), P.listCap);
     for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int si = (int)(__ldcg(&P.rlist[0][i]) >> 40);
@@ -1482,13 +1575,12 @@ extern "C" __global__ void __launch_bounds__(256) lvbgs_k_longscan(TickParams P)
 
 extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_resolve(TickParams P, unsigned long long dsTotal,
                                                                        const unsigned long long* dsBase) {
-    if ((int)blockIdx.x < P.totalTiles) {
-        const int t = blockIdx.x;
-        const int si = find_stream_by_tile(P, t);
-        phaseB_tile(P, si, P.streams[si], t - P.streams[si].tileBase);
+    const int tileBlocks = (P.totalTiles + kResolveTiles - 1) / kResolveTiles;
+    if ((int)blockIdx.x < tileBlocks) {
+        phaseB_tiles(P, blockIdx.x * kResolveTiles);
         return;
     }
-    const unsigned long long i = (unsigned long long)(blockIdx.x - P.totalTiles) * blockDim.x + threadIdx.x;
+    const unsigned long long i = (unsigned long long)(blockIdx.x - tileBlocks) * blockDim.x + threadIdx.x;
     if (i >= dsTotal) return;
     int lo = 0, hi = P.nStreams - 1;
     while (lo < hi) {
@@ -1522,8 +1614,13 @@ extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_repair(TickParams
             const int si = (int)(item >> 40), q = (int)(item & 0xffffffffffull);
             const StreamDev& S = P.streams[si];
             const uint32_t stampNext = S.ctl->stamp_base + (uint32_t)iter + 2u;
-            if (S.C == 3) rematch_item<3>(P, si, S, q, stampNext, par);
-            else rematch_item<1>(P, si, S, q, stampNext, par);
+            const bool counted = S.C == 3 ? rematch_item<3>(P, si, S, q, stampNext, par)
+                                          : rematch_item<1>(P, si, S, q, stampNext, par);
+            // re-match statistics: one atomic per stream among the lanes here
+            const unsigned am = __activemask();
+            const unsigned grp = __match_any_sync(am, counted ? si : -1 - (int)(threadIdx.x & 31));
+            if (counted && (int)(threadIdx.x & 31) == __ffs(grp) - 1)
+                atomicAdd(&S.ctl->st_rematched, (unsigned long long)__popc(grp));
         }
         if (!grid_sync(w)) return;
         const unsigned int nr0 = ld_volatile(&w->rcount[par]);
