@@ -376,6 +376,9 @@ def main():
     nprof = lib.lvbgs_debug_tick_profile(hs[0], 1, prof, 16)
     kernel_ms = {KERNELS[i]: round(prof[i], 4) for i in range(nprof)}
     lib.lvbgs_debug_set_timing(hs[0], 1, 0)
+    ph = (C.c_double * 40)()
+    nph = lib.lvbgs_debug_repair_phases(hs[0], 1, ph, 40)
+    repair_phases = [round(ph[i], 1) for i in range(nph)]
     # the evaluation spans two kernels: the capped scan of every pixel, then the long scans
     eval_ms = sum(kernel_ms.get(k, 0.0) for k in ("eval", "longscan")) or float("nan")
     eval_achieved = eval_bytes_step / (eval_ms / 1e3) / 1e9
@@ -473,7 +476,8 @@ def main():
                                  "bandwidth (of measured)"},
             "path_roofline": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                               "note": "algorithmic bytes of the whole frame step / tick time"},
-            "repair": {"rounds_per_tick": rounds, "rematched_px_per_tick": remat},
+            "repair": {"rounds_per_tick": rounds, "rematched_px_per_tick": remat,
+                       "phases_us_last_tick": repair_phases},
             "kernel_ms": kernel_ms,
             "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": len(KERNELS) * args.steps,
             "serving": serve,

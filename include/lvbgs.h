@@ -203,6 +203,12 @@ lvbgs_status lvbgs_get_scalars(lvbgs_handle h, lvbgs_scalars* out);
  * automatic model reset, frame close. Returns the number of values written. */
 lvbgs_status lvbgs_debug_set_timing(lvbgs_handle h, int batched, int n_ticks);
 int lvbgs_debug_tick_profile(lvbgs_handle h, int batched, double* out_ms, int max_n);
+/* Phase durations (microseconds) of the repair kernel of the last step launched by h (batched != 0:
+ * its last batched step): the device timer at kernel entry and after every grid barrier, as
+ * differences: re-match of round 0, re-resolution of round 0, re-match of round 1, ...; then the
+ * number of re-matched pixels of each round. Waits for the device. Returns the number of values
+ * written. */
+int lvbgs_debug_repair_phases(lvbgs_handle h, int batched, double* out_us, int max_n);
 
 /* ---- PAWCS (BackgroundSubtractorPAWCS, modules/video/src/BackgroundSubtractorPAWCS.cpp) ----
  * A handle created with LVBGS_ALGO_PAWCS runs PAWCS on single-channel frames (three-channel frames:

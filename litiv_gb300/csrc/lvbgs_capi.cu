@@ -207,7 +207,7 @@ enum {
     L_CTL = 0, L_FM, L_UNST, L_LASTCOL, L_LASTDESC, L_SD, L_SC, L_ROI, L_BLINKS, L_LASTRAWFG, L_LASTFG, L_DILINV,
     L_LASTRAWBLINK, L_KCTR, L_DSLT, L_DSST,
     // scratch (not spilled)
-    L_STAMPD, L_STAMPR, L_BITS, L_HCOUNT, L_LABEL, L_INTENT, L_FRAME, L_MASK, L_COUNT
+    L_STAMPD, L_STAMPR, L_GOODREC, L_BITS, L_HCOUNT, L_LABEL, L_INTENT, L_FRAME, L_MASK, L_COUNT
 };
 Layout make_layout(int W, int H, int C, size_t N) {
     const size_t npx = (size_t)W * H;
@@ -224,6 +224,7 @@ Layout make_layout(int W, int H, int C, size_t N) {
     sz[L_KCTR] = npx * 2;
     sz[L_DSLT] = sz[L_DSST] = std::max<size_t>(nds, 1) * 4;
     sz[L_STAMPD] = sz[L_STAMPR] = npx * 4;
+    sz[L_GOODREC] = npx * 16;
     sz[L_BITS] = bit_planes_bytes(W, H);
     sz[L_HCOUNT] = npx;
     sz[L_LABEL] = sz[L_INTENT] = npx * 4;
@@ -261,6 +262,7 @@ void fill_pointers(lvbgs_ctx* h, const Layout& L) {
     S.dsST = (float*)(b + L.off[L_DSST]);
     S.stampD = (uint32_t*)(b + L.off[L_STAMPD]);
     S.stampR = (uint32_t*)(b + L.off[L_STAMPR]);
+    S.goodRec = (uint4*)(b + L.off[L_GOODREC]);
     S.bits = (uint32_t*)(b + L.off[L_BITS]);
     S.hcount = b + L.off[L_HCOUNT];
     S.label = (int*)(b + L.off[L_LABEL]);
@@ -1623,6 +1625,22 @@ int lvbgs_debug_tick_profile(lvbgs_handle h, int batched, double* out_ms, int ma
     ws.tevRecorded = 0;
     ws.tevNext = 0;
     return n;
+}
+
+int lvbgs_debug_repair_phases(lvbgs_handle h, int batched, double* out_us, int max_n) {
+    if (!h || !out_us || max_n <= 0) return 0;
+    cudaSetDevice(h->device);
+    Workspace& ws = batched ? h->batchWs : h->ws;
+    if (!ws.work) return 0;
+    TickWork w;
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return 0;
+    if (cudaMemcpy(&w, ws.work, sizeof(w), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+    const int n = std::min<int>(max_n, (int)std::min<unsigned>(w.nts, 40u) - 1);
+    for (int k = 0; k < n; ++k) out_us[k] = (double)(w.ts[k + 1] - w.ts[k]) / 1e3;
+    // then the re-matched items of each round
+    int m = std::max(n, 0);
+    for (unsigned r = 0; r < std::min(w.iters, 16u) && m < max_n; ++r) out_us[m++] = (double)w.phase_ctr[r];
+    return m;
 }
 
 lvbgs_status lvbgs_get_scalars(lvbgs_handle h, lvbgs_scalars* out) {

@@ -157,6 +157,7 @@ struct StreamDev {
     int* label;
     uint32_t* intent;
     uint32_t *stampD, *stampR;
+    uint4* goodRec;  // long scans of the frame: frame tag, stop position, good samples (index, distances)
     uint16_t* kctr;
     float *dsLT, *dsST;
     StreamCtl* ctl;
@@ -165,7 +166,7 @@ struct StreamDev {
 // Per-launch work area (reset before every launch).
 struct TickWork {
     unsigned int bar_count, bar_gen, err, err_info;
-    unsigned int phase_ctr[16];
+    unsigned int phase_ctr[16];  // repair: re-matched items of rounds 0..15 (phase profile)
     unsigned int dcount[2], rcount[2];
     unsigned int done_ctas, iters;
     unsigned long long rematched;

@@ -261,6 +261,8 @@ __device__ __forceinline__ EvalThr eval_thresholds(const StreamDev& S, float R, 
 struct ScanSt {
     int s, nGood;
     uint32_t minDesc, minSum;
+    int g0, g1;                   // indices of the first two good samples (-1: none)
+    uint32_t g0d, g0s, g1d, g1s;  // their descriptor and summed distances
 };
 
 // one sample against the pixel (the body of the sample loops, :226-250 / :357-393): whether it is a
@@ -330,6 +332,8 @@ template <int C>
 __device__ __forceinline__ void scan_init(ScanSt& st) {
     st.s = 0;
     st.nGood = 0;
+    st.g0 = st.g1 = -1;
+    st.g0d = st.g0s = st.g1d = st.g1s = 0;
     st.minDesc = C == 1 ? 16u : 48u;
     st.minSum = C == 1 ? 255u : 765u;
 }
@@ -343,6 +347,8 @@ __device__ __forceinline__ void scan_samples(const StreamDev& S, const uint8_t* 
     const int sMax = sEnd < N ? sEnd : N;
     int nGood = st.nGood, s = st.s;
     uint32_t minDesc = st.minDesc, minSum = st.minSum;
+    int g0 = st.g0, g1 = st.g1;
+    uint32_t g0d = st.g0d, g0s = st.g0s, g1d = st.g1d, g1s = st.g1s;
     // scans that may run past the evaluation's cap (long scans, repair) prefetch ahead into L2
     const bool deep = sMax > kScanCap;
     if (deep && nGood < nreq)
@@ -373,6 +379,15 @@ __device__ __forceinline__ void scan_samples(const StreamDev& S, const uint8_t* 
         if (sample_match<C>(lut, vals, curr, intra, th, d, c2, dd, sd)) {
             if (minDesc > dd) minDesc = dd;
             if (minSum > sd) minSum = sd;
+            if (g0 < 0) {
+                g0 = s;
+                g0d = dd;
+                g0s = sd;
+            } else if (g1 < 0) {
+                g1 = s;
+                g1d = dd;
+                g1s = sd;
+            }
             ++nGood;
         }
         ++s;
@@ -381,6 +396,29 @@ __device__ __forceinline__ void scan_samples(const StreamDev& S, const uint8_t* 
     st.nGood = nGood;
     st.minDesc = minDesc;
     st.minSum = minSum;
+    st.g0 = g0;
+    st.g0d = g0d;
+    st.g0s = g0s;
+    st.g1 = g1;
+    st.g1d = g1d;
+    st.g1s = g1s;
+}
+
+// With nreq <= 2 a scan's outcome is fixed by its stop position and its (at most two) good samples:
+// every other sample it evaluated is bad. Recording them for the long scans lets the repair re-match
+// such a pixel from the samples that earlier pixels overwrite (the others keep their frame-start
+// values, so their verdicts), scanning on only when an overwrite removed a good sample.
+// Record: frame tag | stop | count | indices | descriptor distances | summed distances.
+__device__ __forceinline__ void record_scan(const StreamDev& S, const FrameK& F, int p, const ScanSt& st) {
+    if (S.nreq > 2) return;
+    const int n = st.nGood < 2 ? st.nGood : 2;
+    uint4 r;
+    r.x = F.frame;
+    r.y = (uint32_t)st.s | ((uint32_t)n << 8) | ((uint32_t)(st.g0 < 0 ? 255 : st.g0) << 16) |
+          ((uint32_t)(st.g1 < 0 ? 255 : st.g1) << 24);
+    r.z = (st.g0d & 0xffffu) | (st.g1d << 16);
+    r.w = (st.g0s & 0xffffu) | (st.g1s << 16);
+    S.goodRec[p] = r;
 }
 
 // the rest of one evaluation after the sample scan (:254-330 / :396-481): D_last, D_min, the raw
@@ -669,9 +707,12 @@ __device__ void phaseA_tile(const TickParams& P, int si, const StreamDev& S, int
                 // a long scan: continued and finished by lvbgs_k_longscan over the compacted list, so
                 // that its warps hold only long scans
                 defer = true;
-                scanWord = (unsigned long long)st.s | ((unsigned long long)st.nGood << 16) |
+                // s | nGood | first good index (255: none) | minDesc | minSum
+                scanWord = (unsigned long long)st.s | ((unsigned long long)st.nGood << 8) |
+                           ((unsigned long long)(st.g0 < 0 ? 255 : st.g0) << 16) |
                            ((unsigned long long)st.minDesc << 32) | ((unsigned long long)st.minSum << 48);
             } else {
+                if (st.s >= S.N) record_scan(S, F, p, st);  // a foreground scan that ended within the cap
                 intent = eval_tail<C>(S, F, x, y, p, in, curr, intra, th.uNew, st);
             }
         }
@@ -705,10 +746,17 @@ __device__ void phaseA_tile(const TickParams& P, int si, const StreamDev& S, int
 // ------------------------------------------------------------------------------------------
 // list helpers for the repair loop
 // ------------------------------------------------------------------------------------------
+// push of one item from divergent code: the lanes that arrive together share one counter atomic
+// (the counters are shared by all streams, and same-address atomics serialize)
 __device__ __forceinline__ void push_item(unsigned long long* list, unsigned int* count, unsigned int cap,
                                           uint32_t* stamps, uint32_t stamp, int si, int p, TickWork* w) {
     if (atomicExch(&stamps[p], stamp) == stamp) return;
-    const unsigned int i = atomicAdd(count, 1u);
+    const unsigned am = __activemask();
+    const int lane = threadIdx.x & 31, leader = __ffs(am) - 1;
+    unsigned int base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned int)__popc(am));
+    base = __shfl_sync(am, base, leader);
+    const unsigned int i = base + (unsigned int)__popc(am & ((1u << lane) - 1u));
     if (i < cap) list[i] = ((unsigned long long)si << 40) | (unsigned long long)(unsigned)p;
     else atomicOr(&w->err, ERR_REPAIR_LIMIT);
 }
@@ -895,7 +943,82 @@ __device__ bool rematch_item(const TickParams& P, int si, const StreamDev& S, in
     int e = 0;
     PixIn<C> in;
     load_pix<C>(S, F, q, in);
-    uint32_t wNew = eval_pixel<C, true>(S, F, S.ctl->lut, x, y, q, in, vals, curr, intra, ov, nov, mask, e);
+    uint32_t wNew;
+    const uint4 gr = S.nreq <= 2 ? __ldcg(&S.goodRec[q]) : make_uint4(0u, 0u, 0u, 0u);
+    if (S.nreq <= 2 && gr.x == F.frame) {
+        // q's frame-start scan is recorded: up to its stop eA, its good samples are the recorded ones
+        // not overwritten and the overwritten ones that match now. The ordered scan over them stops
+        // at the nreq-th good index, with minima over the good samples up to there; with fewer, it
+        // goes on from eA (with the overwrites) as a scan from the start would.
+        const EvalThr th = eval_thresholds(S, in.R, in.RwLT, in.RwST, in.FnLT, in.FnST, in.uOld);
+        const int eA = (int)(gr.y & 255u), nA = (int)((gr.y >> 8) & 255u);
+        int gi[2] = {S.N, S.N};  // the two smallest good indices
+        uint32_t gd[2] = {0u, 0u}, gs[2] = {0u, 0u};
+        int cnt = 0;
+        auto add = [&](int idx, uint32_t dd, uint32_t sd) {
+            ++cnt;
+            if (idx < gi[0]) {
+                gi[1] = gi[0];
+                gd[1] = gd[0];
+                gs[1] = gs[0];
+                gi[0] = idx;
+                gd[0] = dd;
+                gs[0] = sd;
+            } else if (idx < gi[1]) {
+                gi[1] = idx;
+                gd[1] = dd;
+                gs[1] = sd;
+            }
+        };
+        for (int j = 0; j < nA; ++j) {
+            const int g = (int)((gr.y >> (16 + 8 * j)) & 255u);
+            if (!((mask >> g) & 1ull)) add(g, (j ? gr.z >> 16 : gr.z) & 0xffffu, (j ? gr.w >> 16 : gr.w) & 0xffffu);
+        }
+        for (int k = 0; k < nov; ++k) {
+            if (ov[k].s >= eA) continue;
+            uint64_t d;
+            uint32_t c2;
+            if (C == 3) {
+                d = ov[k].desc | ((uint64_t)(ov[k].col & 0xffffu) << 48);
+                c2 = (ov[k].col >> 16) & 0xffu;
+            } else {
+                d = ov[k].desc & 0xffffu;
+                c2 = ov[k].col & 0xffu;
+            }
+            uint32_t dd, sd;
+            if (sample_match<C>(S.ctl->lut, vals, curr, intra, th, d, c2, dd, sd)) add(ov[k].s, dd, sd);
+        }
+        ScanSt st;
+        scan_init<C>(st);
+        const int take = cnt < S.nreq ? cnt : S.nreq;
+        for (int j = 0; j < take; ++j) {
+            if (st.minDesc > gd[j]) st.minDesc = gd[j];
+            if (st.minSum > gs[j]) st.minSum = gs[j];
+        }
+        st.nGood = take;
+        if (cnt >= S.nreq) {
+            st.s = gi[S.nreq - 1] + 1;
+        } else {
+            st.s = eA;
+            if (eA < S.N) {
+                const int npx = S.npx;
+                uint64_t dA = 0, dB = 0;
+                uint32_t cA = 0, cB = 0;
+                dA = C == 3 ? ((const uint64_t*)S.sD)[(size_t)eA * npx + q] : (uint64_t)((const uint16_t*)S.sD)[(size_t)eA * npx + q];
+                cA = S.sC[(size_t)eA * npx + q];
+                if (eA + 1 < S.N) {
+                    dB = C == 3 ? ((const uint64_t*)S.sD)[(size_t)(eA + 1) * npx + q]
+                                : (uint64_t)((const uint16_t*)S.sD)[(size_t)(eA + 1) * npx + q];
+                    cB = S.sC[(size_t)(eA + 1) * npx + q];
+                }
+                scan_samples<C, true>(S, S.ctl->lut, q, vals, curr, intra, th, ov, nov, mask, S.N, dA, cA, dB, cB, st);
+            }
+        }
+        e = st.s;
+        wNew = eval_tail<C>(S, F, x, y, q, in, curr, intra, th.uNew, st);
+    } else {
+        wNew = eval_pixel<C, true>(S, F, S.ctl->lut, x, y, q, in, vals, curr, intra, ov, nov, mask, e);
+    }
     const bool decChanged = ((wNew ^ wOld) & kInFG) != 0u;
     if (!decChanged) {
         // same decision: same draws, same updates; keep the resolved neighbour state
@@ -1524,10 +1647,17 @@ __device__ void longscan_item(const TickParams& P, unsigned int i) {
     const FrameK F = frame_consts(S);
     const int W = S.W, x = p % W, y = p / W, npx = S.npx, N = S.N;
     ScanSt st;
-    st.s = (int)(sw & 0xffffu);
-    st.nGood = (int)((sw >> 16) & 0xffffu);
+    st.s = (int)(sw & 0xffu);
+    st.nGood = (int)((sw >> 8) & 0xffu);
+    const int g0 = (int)((sw >> 16) & 0xffu);
+    st.g0 = g0 == 255 ? -1 : g0;
     st.minDesc = (uint32_t)((sw >> 32) & 0xffffu);
     st.minSum = (uint32_t)(sw >> 48);
+    // a deferred scan has fewer than nreq good samples; with one, the minima are its distances
+    st.g0d = st.minDesc;
+    st.g0s = st.minSum;
+    st.g1 = -1;
+    st.g1d = st.g1s = 0;
     // samples s and s+1 with the feedback maps
     uint64_t dA = 0, dB = 0;
     uint32_t cA = 0, cB = 0;
@@ -1559,6 +1689,7 @@ __device__ void longscan_item(const TickParams& P, unsigned int i) {
         }
         scan_samples<C, false>(S, lut, p, vals, curr, intra, th, nullptr, 0, 0ull, N, dA, cA, dB, cB, st);
     }
+    record_scan(S, F, p, st);
     PixIn<C> in;
     load_pix<C>(S, F, p, in);
     __stcg(&S.intent[p], eval_tail<C>(S, F, x, y, p, in, curr, intra, th.uNew, st));
@@ -1594,6 +1725,7 @@ extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_resolve(TickParam
 // repair to the raster-order fixed point (cooperative launch: all CTAs resident)
 extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_repair(TickParams P) {
     TickWork* w = P.work;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && w->nts < 40u) w->ts[w->nts++] = gtimer();  // phase profile
     int iter = 0;
     for (;;) {
         const int par = iter & 1;
@@ -1607,6 +1739,7 @@ extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_repair(TickParams
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             w->rcount[par ^ 1] = 0u;
             w->rematched += nItems;
+            if (iter < 16) w->phase_ctr[iter] = nItems;
         }
         const unsigned int nth = gridDim.x * blockDim.x;
         for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < nItems; i += nth) {
