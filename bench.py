@@ -25,10 +25,10 @@ sys.path.insert(0, ROOT)
 METRIC = "SuBSENSE Mpix/s: batched 64-stream vs plain 1-stream on GB300; p99 frame ms"
 # DRAM bytes (read + write) of the evaluation per pixel (lvbgs_k_eval + lvbgs_k_longscan), from an
 # ncu capture of dram__bytes_read.sum + dram__bytes_write.sum on six streams of the mix (indices
-# 52-57: four 1280x720, one of them gray, and two 1920x1080; 7,833,600 px): eval 902,353,152 +
-# 335,219,456 bytes, long scans 351,425,792 + 36,874,240 bytes. roofline.traffic scales it to a tick
+# 52-57: four 1280x720, one of them gray, and two 1920x1080; 7,833,600 px): eval 903,555,328 +
+# 341,958,912 bytes, long scans 437,656,576 + 46,936,064 bytes. roofline.traffic scales it to a tick
 # by pixels.
-EVAL_DRAM_BYTES_PER_PX = (902353152 + 335219456 + 351425792 + 36874240) / 7833600
+EVAL_DRAM_BYTES_PER_PX = (903555328 + 341958912 + 437656576 + 46936064) / 7833600
 WORKLOAD = ("subsense-mix64: 16x320x240 + 24x640x480 + 16x1280x720 + 8x1920x1080, 48 BGR + 16 gray, "
             "default parameters, synthetic seeded scenes")
 # CPU sample: 4 streams of each resolution class
