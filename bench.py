@@ -201,6 +201,55 @@ def pawcs_run(n_frames, stream, cpu=True):
     return out
 
 
+def single_stream_run(config, n_frames, stream, cpu=True, cpu_frames=4):
+    """SuBSENSE configs 0 and 1 of the benchmark (one seeded stream: 320x240 BGR, 200 frames; 1920x1080
+    BGR, 500 frames): every frame through lvbgs_apply from frames resident on the device, wall clock
+    per frame (the first 10 frames are warm-up); the CPU baseline is the oracle on one core (one
+    instance per sequence, as the reference's apps run it) over the first cpu_frames frames."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    from litiv_gb300 import BackgroundSubtractorSuBSENSE, SyntheticStream
+    from litiv_gb300 import _lib as L
+    lib = L.lib()
+    s = SyntheticStream(config, 0, 1)
+    W, H = s.cfg.width, s.cfg.height
+    n = min(n_frames, s.n_frames)
+    dev = torch.empty((n,) + s.shape, dtype=torch.uint8, device="cuda")
+    for t in range(n):
+        s.render_device(t, dev[t].data_ptr(), cuda_stream=stream.cuda_stream)
+    dmask = torch.empty((H, W), dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    b = BackgroundSubtractorSuBSENSE(seed=1)
+    b.initialize(dev[0])
+    ms = []
+    for t in range(1, n):
+        t0 = time.perf_counter()
+        st = lib.lvbgs_apply(b.handle, C.c_void_p(dev[t].data_ptr()), 0, C.c_void_p(dmask.data_ptr()), 0.0,
+                             C.c_void_p(stream.cuda_stream))
+        torch.cuda.current_stream().synchronize()
+        stream.synchronize()
+        ms.append((time.perf_counter() - t0) * 1e3)
+        if st != L.OK:
+            raise RuntimeError("apply failed: %s" % lib.lvbgs_last_error(b.handle))
+    b.close()
+    m = np.array(ms[9:])
+    out = {"workload": "SuBSENSE config %d: one %dx%d %s stream, %d frames, default parameters" % (
+               config, W, H, "BGR" if s.cfg.channels == 3 else "gray", n),
+           "value": W * H / (m.mean() / 1e3) / 1e6, "unit": "Mpix/s", "frames_per_s": 1e3 / m.mean(),
+           "ms_per_frame": float(m.mean()), "p50_frame_ms": float(np.percentile(m, 50)),
+           "p99_frame_ms": float(np.percentile(m, 99))}
+    if cpu:
+        from oracle import pyoracle
+        fr = np.stack([s.render(t) for t in range(cpu_frames + 1)])
+        wall = pyoracle.run_streams([fr], [1], 1)
+        px = W * H * cpu_frames
+        out["cpu_baseline"] = {"value": px / wall / 1e6, "unit": "Mpix/s", "cores": 1, "kind": "port",
+                               "sample": "the first %d applied frames on one core, %.1f Mpix in %.2f s" % (
+                                   cpu_frames, px / 1e6, wall)}
+    return out
+
+
 def serving_run(seconds):
     """The serving workload (Poisson arrivals of 4 streams/s up to 256 live, lives U[10, 60] s, 30 fps,
     320x240/640x480/1280x720/1920x1080 with p = .3/.3/.3/.1, a quarter single-channel), started from its
@@ -256,6 +305,8 @@ def main():
                     help="frames of the PAWCS workload (640x480 thermal-like scene; 0: skip)")
     ap.add_argument("--serving-seconds", type=float, default=20.0,
                     help="measured span of the serving workload run (0: skip)")
+    ap.add_argument("--single-frames", type=int, default=100,
+                    help="frames of the single-stream SuBSENSE configs 0 and 1 (0: skip)")
     ap.add_argument("--pawcs-only", action="store_true",
                     help="run the PAWCS workload alone and print its object (profiling)")
     args = ap.parse_args()
@@ -450,6 +501,12 @@ def main():
     pawcs = None
     if rank == 0 and args.pawcs_frames > 0:
         pawcs = pawcs_run(args.pawcs_frames, stream, cpu=not args.no_cpu_baseline)
+    singles = None
+    if rank == 0 and args.single_frames > 0:
+        singles = {"config0": single_stream_run(0, args.single_frames, stream, cpu=not args.no_cpu_baseline,
+                                                cpu_frames=10),
+                   "config1": single_stream_run(1, args.single_frames, stream, cpu=not args.no_cpu_baseline,
+                                                cpu_frames=2)}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -482,6 +539,7 @@ def main():
             "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": len(KERNELS) * args.steps,
             "serving": serve,
             "pawcs": pawcs,
+            "single_stream": singles,
             "clocks": clk.summary(),
         }
         print(json.dumps(out))

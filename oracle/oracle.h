@@ -152,11 +152,11 @@ size_t opawcs_export_bytes(const opawcs_t* o, int which);
 void opawcs_get_scalars(const opawcs_t* o, opawcs_scalars* s);
 
 /* CPU baseline: runs n independent SuBSENSE instances (one per stream) over their
- * frame sequences with a pool of n_threads workers (one instance per worker at a
- * time, like lv::WorkerPool in apps/changedet/src/main.cpp:148-154).
+ * frame sequences on n_threads workers (streams k, k+T, ... on worker k, like the
+ * per-sequence lv::WorkerPool of apps/changedet/src/main.cpp:148-154).
  * frames[i] holds n_frames[i] frames of widths[i]*heights[i]*channels[i] bytes;
  * the first frame initializes, the others are applied. Returns the wall time in
- * seconds of the whole run; masks may be NULL. */
+ * seconds of the apply phase (after every instance is initialized); masks may be NULL. */
 double orun_streams(int n_streams, const uint8_t* const* frames, const int* n_frames,
                     const int* widths, const int* heights, const int* channels,
                     const uint64_t* seeds, int n_threads, uint8_t* const* last_masks);

@@ -21,26 +21,41 @@ typedef struct {
     pthread_mutex_t mu;
 } job_t;
 
-static void* worker(void* arg) {
-    job_t* j = (job_t*)arg;
-    for (;;) {
-        pthread_mutex_lock(&j->mu);
-        const int i = j->next++;
-        pthread_mutex_unlock(&j->mu);
-        if (i >= j->n) break;
+/* Thread k initializes streams k, k+T, ... then, after a barrier, applies their frames; the returned
+ * time covers the apply phase only (the per-frame throughput, without the model initialization). */
+typedef struct {
+    job_t* j;
+    int tid, nth;
+    pthread_barrier_t* bar;
+} pjob_t;
+
+static void* sworker(void* arg) {
+    pjob_t* pj = (pjob_t*)arg;
+    job_t* j = pj->j;
+    int mine = 0;
+    for (int i = pj->tid; i < j->n; i += pj->nth) ++mine;
+    osub_t** os = (osub_t**)calloc((size_t)(mine > 0 ? mine : 1), sizeof(osub_t*));
+    int m = 0;
+    for (int i = pj->tid; i < j->n; i += pj->nth, ++m) {
         osub_params p;
         osub_default_params(&p);
         p.seed = j->seeds[i];
-        osub_t* o = osub_create(&p);
+        os[m] = osub_create(&p);
+        osub_initialize(os[m], j->frames[i], j->w[i], j->h[i], j->c[i], NULL);
+    }
+    pthread_barrier_wait(pj->bar);
+    m = 0;
+    for (int i = pj->tid; i < j->n; i += pj->nth, ++m) {
         const size_t fb = (size_t)j->w[i] * j->h[i] * j->c[i];
         uint8_t* mask = (uint8_t*)malloc((size_t)j->w[i] * j->h[i]);
-        osub_initialize(o, j->frames[i], j->w[i], j->h[i], j->c[i], NULL);
-        for (int f = 1; f < j->nf[i]; ++f) osub_apply(o, j->frames[i] + (size_t)f * fb, mask, 0.0);
+        for (int f = 1; f < j->nf[i]; ++f) osub_apply(os[m], j->frames[i] + (size_t)f * fb, mask, 0.0);
         if (j->last_masks && j->last_masks[i])
             for (size_t k = 0; k < (size_t)j->w[i] * j->h[i]; ++k) j->last_masks[i][k] = mask[k];
         free(mask);
-        osub_destroy(o);
     }
+    pthread_barrier_wait(pj->bar);
+    for (int k = 0; k < mine; ++k) osub_destroy(os[k]);
+    free(os);
     return NULL;
 }
 
@@ -50,24 +65,28 @@ double orun_streams(int n_streams, const uint8_t* const* frames, const int* n_fr
     job_t j = {n_streams, frames, n_frames, widths, heights, channels, seeds, last_masks, 0,
                PTHREAD_MUTEX_INITIALIZER};
     if (n_threads < 1) n_threads = 1;
+    pthread_barrier_t bar;
+    pthread_barrier_init(&bar, NULL, (unsigned)n_threads + 1);
     pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)n_threads);
+    pjob_t* pj = (pjob_t*)malloc(sizeof(pjob_t) * (size_t)n_threads);
+    for (int t = 0; t < n_threads; ++t) {
+        pj[t] = (pjob_t){&j, t, n_threads, &bar};
+        pthread_create(&th[t], NULL, sworker, &pj[t]);
+    }
     struct timespec t0, t1;
+    pthread_barrier_wait(&bar);
     clock_gettime(CLOCK_MONOTONIC, &t0);
-    for (int t = 0; t < n_threads; ++t) pthread_create(&th[t], NULL, worker, &j);
-    for (int t = 0; t < n_threads; ++t) pthread_join(th[t], NULL);
+    pthread_barrier_wait(&bar);
     clock_gettime(CLOCK_MONOTONIC, &t1);
+    for (int t = 0; t < n_threads; ++t) pthread_join(th[t], NULL);
+    pthread_barrier_destroy(&bar);
     free(th);
+    free(pj);
     return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
 }
 
-/* PAWCS: thread k initializes streams k, k+T, ... then, after a barrier, applies their frames; the
- * returned time covers the apply phase only (PAWCS's model initialization is much heavier than a
- * frame and is not part of the per-frame throughput). */
-typedef struct {
-    job_t* j;
-    int tid, nth;
-    pthread_barrier_t* bar;
-} pjob_t;
+/* PAWCS: the same scheme (PAWCS's model initialization is much heavier than a frame and is not part
+ * of the per-frame throughput). */
 
 static void* pworker(void* arg) {
     pjob_t* pj = (pjob_t*)arg;
