@@ -1625,7 +1625,7 @@ __device__ void refresh_pixel(const StreamDev& S, int p, uint32_t frame, int sta
     const StreamDev& S = P.streams[si];                                     \
     const int lt = t - S.tileBase;
 
-extern "C" __global__ void __launch_bounds__(kThreads, 3) lvbgs_k_eval(TickParams P) {
+extern "C" __global__ void __launch_bounds__(kThreads, 4) lvbgs_k_eval(TickParams P) {
     __shared__ __align__(16) uint8_t smem[((((kTileW + 4) * 3 + 2 + 3) / 4) * 4) * (kTileH + 4) + 256];
     LV_TILE_KERNEL_PROLOGUE
     if (S.C == 3) phaseA_tile<3>(P, si, S, lt, smem);
