@@ -40,7 +40,8 @@ def _oname(k):
     return {"nDescDistThresholdOffset": "desc_dist_threshold_offset",
             "nMinColorDistThreshold": "min_color_dist_threshold", "nBGSamples": "bg_samples",
             "nRequiredBGSamples": "required_bg_samples", "nSamplesForMovingAvgs": "samples_for_moving_avgs",
-            "fRelLBSPThreshold": "rel_lbsp_threshold"}[k]
+            "fRelLBSPThreshold": "rel_lbsp_threshold",
+            "nDefaultMedianBlurKernelSize": "default_median_blur_kernel_size"}[k]
 
 
 def frames_of(stream, n, t0=0):
@@ -174,3 +175,19 @@ def test_api_errors():
     with pytest.raises(LvException):
         g.refreshModel(0.0)
     assert g.getDefaultLearningRate() == 0.0
+
+
+@pytest.mark.parametrize("channels", [1, 3])
+def test_odd_width_wide_median(channels):
+    # 70 px rows: the bit planes end in a partial word (6 bits) and the rows of the byte maps are not
+    # 4-byte aligned; a 15x15 median (row window 15, sliding column sums over 15 rows)
+    s = SyntheticStream(0, seed=51, width=70, height=50, shape_min=8, shape_max=20, channels=channels)
+    run_pair(frames_of(s, 24), seed=52, nDefaultMedianBlurKernelSize=15)
+
+
+def test_frame_level_analysis_with_partial_words():
+    # 344x256: large enough for the frame-level analysis (integral 1/8 down-sampling: 43x32 blocks of
+    # 8x8) while the rows end in a partial 24-bit word; median 9
+    s = SyntheticStream(0, seed=53, width=344, height=256)
+    run_pair(frames_of(s, 14), seed=54, check_every=6)
+

@@ -179,3 +179,8 @@ def test_moving_camera_mode_switch():
         if t in (499, 500, 999, 1000):
             modes[t] = (gpu.scalars()["using_moving_camera"], gpu.scalars()["lword_weight_offset"])
     assert modes == {499: (0, 1000), 500: (1, 5), 999: (1, 5), 1000: (0, 1000)}
+
+
+def test_partial_word_rows_72x56():
+    # 72 px rows end in a partial bit-plane word (8 bits) in the post-processing kernels
+    run_pair(_gray(20, 39, 72, 56), seed=12, check_every=4)
