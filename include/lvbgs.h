@@ -125,6 +125,12 @@ lvbgs_status lvbgs_refresh_model(lvbgs_handle h, float fraction, int force_fg_up
 lvbgs_status lvbgs_set_automatic_model_reset(lvbgs_handle h, int enabled);
 /* getDefaultLearningRate (BackgroundSubtractorSuBSENSE.hpp:69): always 0 */
 double lvbgs_get_default_learning_rate(lvbgs_handle h);
+/* setROI (BackgroundSubtractionUtils.cpp:38-48) with validateROI (:28-36): the ROI (width*height bytes,
+ * host or device memory) loses its 2-pixel border ring and must keep a pixel; on an initialized
+ * handle the model is re-initialized from the latest background image with it, otherwise it is kept
+ * for the next lvbgs_initialize() of the same size that passes no ROI (which also reuses the last
+ * validated ROI, :86-87). */
+lvbgs_status lvbgs_set_roi(lvbgs_handle h, const uint8_t* roi, int width, int height);
 /* getROICopy (BackgroundSubtractionUtils.cpp:50-52): the validated ROI, width*height bytes */
 lvbgs_status lvbgs_get_roi(lvbgs_handle h, uint8_t* out);
 

@@ -139,6 +139,33 @@ class BackgroundSubtractorSuBSENSE:
         _check(L.lib().lvbgs_get_roi(self._h, out.ctypes.data_as(C.c_void_p)), self._h)
         return out
 
+    def validateROI(self, oROI):
+        """validateROI (BackgroundSubtractionUtils.cpp:28-36): a copy of the 8UC1 ROI with its 2-pixel
+        border ring (the LBSP pattern's reach) cleared."""
+        r = np.array(oROI, dtype=np.uint8, copy=True)
+        if r.ndim != 2 or r.size == 0:
+            raise LvException(L.BAD_ARG, "provided ROI must be non-empty and of type 8UC1")
+        r[:2, :] = 0
+        r[-2:, :] = 0
+        r[:, :2] = 0
+        r[:, -2:] = 0
+        return r
+
+    def setROI(self, oROI):
+        """setROI (BackgroundSubtractionUtils.cpp:38-48): on an initialized model, re-initializes it from
+        the latest background image with the new ROI; otherwise keeps the ROI for initialize()."""
+        r = np.ascontiguousarray(oROI, dtype=np.uint8)
+        if r.ndim != 2 or r.size == 0:
+            raise LvException(L.BAD_ARG, "provided ROI must be non-empty and of type 8UC1")
+        _check(L.lib().lvbgs_set_roi(self._h, r.ctypes.data_as(C.c_void_p), r.shape[1], r.shape[0]), self._h)
+
+    # -- lv::IParallelAlgo_<lv::CUDA> (modules/utils/include/litiv/utils/algo.hpp:82-129) --
+    def isParallel(self):
+        return True
+
+    def getParallelAlgoType(self):
+        return "CUDA"
+
     # -- serving helpers --
     def state_bytes(self):
         H, W, Cc = self._need_init()
@@ -222,6 +249,10 @@ class BackgroundSubtractorPAWCS:
     setAutomaticModelReset = BackgroundSubtractorSuBSENSE.setAutomaticModelReset
     getDefaultLearningRate = BackgroundSubtractorSuBSENSE.getDefaultLearningRate
     getROICopy = BackgroundSubtractorSuBSENSE.getROICopy
+    validateROI = BackgroundSubtractorSuBSENSE.validateROI
+    setROI = BackgroundSubtractorSuBSENSE.setROI
+    isParallel = BackgroundSubtractorSuBSENSE.isParallel
+    getParallelAlgoType = BackgroundSubtractorSuBSENSE.getParallelAlgoType
     _need_init = BackgroundSubtractorSuBSENSE._need_init
 
     def refreshModel(self, nBaseOccCount, fOccDecrFrac, bForceFGUpdate=False):

@@ -143,6 +143,7 @@ struct lvbgs_ctx {
     int device = 0;
     std::string err;
     bool initialized = false;
+    int roiW = 0, roiH = 0;  // size of the ROI kept in `roi` (the last validated one, or set before initialize)
     bool spilled = false;
     int W = 0, H = 0, C = 0;
     size_t npx = 0;
@@ -772,6 +773,8 @@ lvbgs_status pw_initialize(lvbgs_ctx* h, const uint8_t* img, int W, int H, int C
     h->C = C;
     h->npx = npx;
     h->roi = newroi;
+    h->roiW = W;
+    h->roiH = H;
     h->n_rel = fin;
     h->orig_roi = orig;
     h->pw_frames = 0;
@@ -1024,7 +1027,10 @@ lvbgs_status lvbgs_initialize(lvbgs_handle h, const uint8_t* img, int W, int H, 
     if (stride < row) return fail(h, LVBGS_BAD_ARG, "image stride is smaller than width*channels");
     // ROI handling (BackgroundSubtractionUtils.cpp:83-101, validateROI :28-36)
     std::vector<uint8_t> newroi(npx, 255);
-    if (roi) {
+    if (!roi && h->roi.size() == npx && h->roiW == W && h->roiH == H) {
+        // no new ROI and the same size: the last validated ROI is reused (:86-87)
+        newroi = h->roi;
+    } else if (roi) {
         const bool devRoi = is_device_ptr(roi);
         std::vector<uint8_t> r(npx);
         if (devRoi) LV_CUDA(h, cudaMemcpy(r.data(), roi, npx, cudaMemcpyDeviceToHost), "roi download");
@@ -1094,6 +1100,8 @@ lvbgs_status lvbgs_initialize(lvbgs_handle h, const uint8_t* img, int W, int H, 
     h->C = C;
     h->npx = npx;
     h->roi = newroi;
+    h->roiW = W;
+    h->roiH = H;
     h->n_rel = fin;
     h->orig_roi = orig;
     fill_pointers(h, L);
@@ -1412,6 +1420,34 @@ lvbgs_status lvbgs_set_automatic_model_reset(lvbgs_handle h, int enabled) {
 }
 
 double lvbgs_get_default_learning_rate(lvbgs_handle) { return 0.0; }
+
+lvbgs_status lvbgs_set_roi(lvbgs_handle h, const uint8_t* roi, int width, int height) {
+    if (!h || !roi || width <= 0 || height <= 0) return fail(h, LVBGS_BAD_ARG, "null or empty ROI");
+    const size_t npx = (size_t)width * height;
+    std::vector<uint8_t> r(npx);
+    if (is_device_ptr(roi)) LV_CUDA(h, cudaMemcpy(r.data(), roi, npx, cudaMemcpyDeviceToHost), "roi download");
+    else std::memcpy(r.data(), roi, npx);
+    // validateROI (:28-36): only [2, W-2) x [2, H-2) may stay in the ROI
+    for (int y = 0; y < height; ++y)
+        for (int x = 0; x < width; ++x)
+            if (x < kBorder || y < kBorder || x >= width - kBorder || y >= height - kBorder) r[(size_t)y * width + x] = 0;
+    size_t nz = 0;
+    for (size_t i = 0; i < npx; ++i) nz += r[i] != 0;
+    if (nz == 0) return fail(h, LVBGS_BAD_ARG, "provided ROI must have at least one valid pixel");
+    if (h->initialized) {
+        // re-initialize from the latest background image with the new ROI (:40-44)
+        if (width != h->W || height != h->H)
+            return fail(h, LVBGS_BAD_SIZE, "provided ROI mat size must be equal to the init frame size");
+        std::vector<uint8_t> bg(npx * h->C);
+        lvbgs_status s = lvbgs_get_background(h, bg.data());
+        if (s != LVBGS_OK) return s;
+        return lvbgs_initialize(h, bg.data(), width, height, h->C, 0, r.data());
+    }
+    h->roi = r;
+    h->roiW = width;
+    h->roiH = height;
+    return LVBGS_OK;
+}
 
 lvbgs_status lvbgs_get_roi(lvbgs_handle h, uint8_t* out) {
     if (!h || !out) return fail(h, LVBGS_BAD_ARG, "null argument");

@@ -78,6 +78,7 @@ int osub_apply(osub_t* o, const uint8_t* img, uint8_t* fgmask, double learning_r
 /* BackgroundSubtractorSuBSENSE::refreshModel (BackgroundSubtractorSuBSENSE.cpp:80-105) */
 int osub_refresh_model(osub_t* o, float frac, int force_fg);
 int osub_get_background(const osub_t* o, uint8_t* out);               /* :614-630 */
+int osub_set_roi(osub_t* o, const uint8_t* roi, int width, int height); /* BackgroundSubtractionUtils.cpp:38-48 */
 int osub_get_background_descriptors(const osub_t* o, uint16_t* out);  /* :632-649 */
 void osub_set_automatic_model_reset(osub_t* o, int enabled);          /* BackgroundSubtractionUtils.cpp:24-26 */
 const void* osub_map(const osub_t* o, int which, size_t* nbytes);
@@ -145,6 +146,7 @@ int opawcs_apply(opawcs_t* o, const uint8_t* img, uint8_t* fgmask, double learni
 /* BackgroundSubtractorPAWCS::refreshModel(nBaseOccCount, fOccDecrFrac, bForceFGUpdate) (:107-429) */
 int opawcs_refresh_model(opawcs_t* o, size_t base_occ, float occ_decr_frac, int force_fg);
 int opawcs_get_background(const opawcs_t* o, uint8_t* out);               /* :1518-1545 */
+int opawcs_set_roi(opawcs_t* o, const uint8_t* roi, int width, int height);
 int opawcs_get_background_descriptors(const opawcs_t* o, uint16_t* out);  /* :1547-1594 */
 void opawcs_set_automatic_model_reset(opawcs_t* o, int enabled);
 int opawcs_export(const opawcs_t* o, int which, void* out, size_t bytes);

@@ -461,7 +461,10 @@ int opawcs_initialize(opawcs_t* o, const uint8_t* img, int W, int H, int C, cons
     const size_t npx = (size_t)W * H;
     /* IIBackgroundSubtractor::initialize_common, BackgroundSubtractionUtils.cpp:70-155 */
     uint8_t* newroi = (uint8_t*)malloc(npx);
-    if (!roi) {
+    if (!roi && o->roi && o->W == W && o->H == H) {
+        /* no new ROI and the same size: the last validated ROI is reused (:86-87) */
+        memcpy(newroi, o->roi, npx);
+    } else if (!roi) {
         memset(newroi, 255, npx);
     } else {
         for (size_t i = 0; i < npx; ++i)
@@ -1069,6 +1072,41 @@ int opawcs_apply(opawcs_t* o, const uint8_t* img, uint8_t* mask, double lr) {
 }
 
 /* getBackgroundImage, :1535-1567: weight-averaged word colours, convertTo(CV_8U) */
+/* setROI, BackgroundSubtractionUtils.cpp:38-48, with validateROI :28-36 */
+int opawcs_set_roi(opawcs_t* o, const uint8_t* roi, int W, int H) {
+    if (!roi || W <= 0 || H <= 0) return OSUB_EBADARG;
+    const size_t npx = (size_t)W * H;
+    uint8_t* r = (uint8_t*)malloc(npx);
+    size_t nz = 0;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t i = (size_t)y * W + x;
+            r[i] = (x < LBSP_BORDER || y < LBSP_BORDER || x >= W - LBSP_BORDER || y >= H - LBSP_BORDER) ? 0 : roi[i];
+            nz += r[i] != 0;
+        }
+    if (nz == 0) {
+        free(r);
+        return OSUB_EBADARG;
+    }
+    if (o->initialized) {
+        if (W != o->W || H != o->H) {
+            free(r);
+            return OSUB_EBADARG;
+        }
+        uint8_t* bg = (uint8_t*)malloc(npx * (size_t)o->C);
+        opawcs_get_background(o, bg);
+        const int st = opawcs_initialize(o, bg, W, H, o->C, r);
+        free(bg);
+        free(r);
+        return st;
+    }
+    free(o->roi);
+    o->roi = r;
+    o->W = W;
+    o->H = H;
+    return OSUB_OK;
+}
+
 int opawcs_get_background(const opawcs_t* o, uint8_t* out) {
     if (!o->initialized) return OSUB_ENOTINIT;
     const int C = o->C;

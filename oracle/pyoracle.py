@@ -77,6 +77,7 @@ def lib():
         L.osub_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
         L.osub_refresh_model.argtypes = [C.c_void_p, C.c_float, C.c_int]
         L.osub_get_background.argtypes = [C.c_void_p, C.c_void_p]
+        L.osub_set_roi.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
         L.osub_get_background_descriptors.argtypes = [C.c_void_p, C.c_void_p]
         L.osub_set_automatic_model_reset.argtypes = [C.c_void_p, C.c_int]
         L.osub_map.restype = C.c_void_p
@@ -104,6 +105,7 @@ def lib():
         L.opawcs_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
         L.opawcs_refresh_model.argtypes = [C.c_void_p, C.c_size_t, C.c_float, C.c_int]
         L.opawcs_get_background.argtypes = [C.c_void_p, C.c_void_p]
+        L.opawcs_set_roi.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
         L.opawcs_get_background_descriptors.argtypes = [C.c_void_p, C.c_void_p]
         L.opawcs_set_automatic_model_reset.argtypes = [C.c_void_p, C.c_int]
         L.opawcs_export.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]
@@ -171,6 +173,11 @@ class OracleSuBSENSE:
         out = np.empty((H, W, Cc) if Cc > 1 else (H, W), np.uint8)
         lib().osub_get_background(self._o, out.ctypes.data_as(C.c_void_p))
         return out
+
+    def set_roi(self, roi):
+        r = np.ascontiguousarray(roi, dtype=np.uint8)
+        if lib().osub_set_roi(self._o, r.ctypes.data_as(C.c_void_p), r.shape[1], r.shape[0]) != 0:
+            raise ValueError("oracle setROI failed")
 
     def background_descriptors(self):
         H, W, Cc = self.shape
@@ -249,6 +256,11 @@ class OraclePAWCS:
         out = np.empty((H, W, Cc) if Cc > 1 else (H, W), np.uint8)
         lib().opawcs_get_background(self._o, out.ctypes.data_as(C.c_void_p))
         return out
+
+    def set_roi(self, roi):
+        r = np.ascontiguousarray(roi, dtype=np.uint8)
+        if lib().opawcs_set_roi(self._o, r.ctypes.data_as(C.c_void_p), r.shape[1], r.shape[0]) != 0:
+            raise ValueError("oracle setROI failed")
 
     def background_descriptors(self):
         H, W, Cc = self.shape

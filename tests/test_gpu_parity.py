@@ -191,3 +191,56 @@ def test_frame_level_analysis_with_partial_words():
     s = SyntheticStream(0, seed=53, width=344, height=256)
     run_pair(frames_of(s, 14), seed=54, check_every=6)
 
+
+
+def _ellipse_roi(W, H):
+    yy, xx = np.mgrid[0:H, 0:W]
+    return ((((xx - W / 2) / (W * 0.42)) ** 2 + ((yy - H / 2) / (H * 0.42)) ** 2) <= 1.0).astype(np.uint8) * 255
+
+
+def _step_and_compare(gpu, ora, frames, t0):
+    for t, f in enumerate(frames, start=t0):
+        mg, mo = gpu.apply(f), ora.apply(f, 0.0)
+        assert np.array_equal(mg, mo), "frame %d: mask differs at %d px" % (t, int((mg != mo).sum()))
+    bad = compare_state(gpu, ora)
+    assert not bad, "; ".join(bad)
+
+
+def test_set_roi_reinitializes_from_background():
+    # setROI on an initialized model: initialize(getBackgroundImage(), validated ROI)
+    s = SyntheticStream(0, seed=61, width=96, height=72, shape_min=10, shape_max=24)
+    fr = frames_of(s, 16)
+    gpu, ora = BackgroundSubtractorSuBSENSE(seed=62), pyoracle.OracleSuBSENSE(seed=62)
+    gpu.initialize(fr[0])
+    ora.initialize(fr[0])
+    _step_and_compare(gpu, ora, fr[1:6], 1)
+    roi = _ellipse_roi(96, 72)
+    gpu.setROI(roi)
+    ora.set_roi(roi)
+    assert np.array_equal(gpu.getROICopy(), ora.state_map("ROI"))
+    assert not compare_state(gpu, ora)
+    _step_and_compare(gpu, ora, fr[6:], 6)
+
+
+def test_set_roi_before_initialize_and_roi_reuse():
+    # a ROI set before initialize() is used as is (validated, not dilated); a later initialize()
+    # without a ROI of the same size reuses the last validated ROI
+    s = SyntheticStream(0, seed=63, width=96, height=72, shape_min=10, shape_max=24)
+    fr = frames_of(s, 14)
+    gpu, ora = BackgroundSubtractorSuBSENSE(seed=64), pyoracle.OracleSuBSENSE(seed=64)
+    roi = _ellipse_roi(96, 72)
+    gpu.setROI(roi)
+    ora.set_roi(roi)
+    gpu.initialize(fr[0])
+    ora.initialize(fr[0])
+    assert np.array_equal(gpu.getROICopy(), gpu.validateROI(roi))
+    assert not compare_state(gpu, ora)
+    _step_and_compare(gpu, ora, fr[1:7], 1)
+    gpu.initialize(fr[7])
+    ora.initialize(fr[7])
+    assert np.array_equal(gpu.getROICopy(), gpu.validateROI(roi))
+    assert not compare_state(gpu, ora)
+    _step_and_compare(gpu, ora, fr[8:], 8)
+    assert gpu.isParallel() and gpu.getParallelAlgoType() == "CUDA"
+    with pytest.raises(LvException):
+        gpu.setROI(np.zeros((72, 96), np.uint8))

@@ -184,3 +184,21 @@ def test_moving_camera_mode_switch():
 def test_partial_word_rows_72x56():
     # 72 px rows end in a partial bit-plane word (8 bits) in the post-processing kernels
     run_pair(_gray(20, 39, 72, 56), seed=12, check_every=4)
+
+
+def test_set_roi_reinitializes_from_background():
+    fr = _gray(14, 40, 96, 72)
+    gpu, ora = BackgroundSubtractorPAWCS(seed=13), pyoracle.OraclePAWCS(seed=13)
+    gpu.initialize(fr[0])
+    ora.initialize(fr[0])
+    for f in fr[1:6]:
+        assert np.array_equal(gpu.apply(f), ora.apply(f, 0.0))
+    yy, xx = np.mgrid[0:72, 0:96]
+    roi = ((((xx - 48) / 40.0) ** 2 + ((yy - 36) / 30.0) ** 2) <= 1.0).astype(np.uint8) * 255
+    gpu.setROI(roi)
+    ora.set_roi(roi)
+    bad = compare_state(gpu, ora)
+    assert not bad, "after setROI: " + "; ".join(bad)
+    for f in fr[6:]:
+        assert np.array_equal(gpu.apply(f), ora.apply(f, 0.0))
+    assert not compare_state(gpu, ora)

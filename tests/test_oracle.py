@@ -171,3 +171,27 @@ def test_oracle_roi_excludes_pixels(product_lib):
         o.apply(s.render(t))
     raw = o.state_map("LAST_RAW_FG")
     assert raw[r == 0].max() == 0
+
+
+def test_oracle_roi_rules():
+    # setROI before initialize keeps the validated ROI as is; initialize() without a ROI of the same size
+    # reuses the last validated ROI; setROI on an initialized model re-initializes (edge pixels 127)
+    from litiv_gb300 import SyntheticStream
+    s = SyntheticStream(0, seed=63, width=96, height=72, shape_min=10, shape_max=24)
+    fr = [s.render(t) for t in range(3)]
+    yy, xx = np.mgrid[0:72, 0:96]
+    roi = ((((xx - 48) / 40.0) ** 2 + ((yy - 36) / 30.0) ** 2) <= 1.0).astype(np.uint8) * 255
+    v = roi.copy()
+    v[:2] = 0
+    v[-2:] = 0
+    v[:, :2] = 0
+    v[:, -2:] = 0
+    o = pyoracle.OracleSuBSENSE(seed=1)
+    o.set_roi(roi)
+    o.initialize(fr[0])
+    assert np.array_equal(o.state_map("ROI"), v)
+    o.apply(fr[1], 0.0)
+    o.initialize(fr[2])
+    assert np.array_equal(o.state_map("ROI"), v)
+    o.set_roi(roi)
+    assert set(np.unique(o.state_map("ROI")).tolist()) == {0, 127, 255}
