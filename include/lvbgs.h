@@ -108,6 +108,10 @@ lvbgs_status lvbgs_batch_create(int device_id, size_t reserve_px, int reserve_st
 lvbgs_status lvbgs_batch_destroy(lvbgs_batch b);
 lvbgs_status lvbgs_batch_reserve(lvbgs_batch b, size_t px, int n_streams);
 /* enqueues one tick over n streams on cuda_stream (required, non-NULL); *ticket names it */
+/* The repair kernel of this context's ticks is a cooperative launch, which starts only once all of its
+ * blocks can be resident; with other work on the device (PAWCS frame steps on other streams, say) a
+ * grid of every co-resident block can wait a long time. This gives it 1/divisor of them (default 1). */
+lvbgs_status lvbgs_batch_set_repair_share(lvbgs_batch b, int divisor);
 lvbgs_status lvbgs_batch_submit(lvbgs_batch b, const lvbgs_handle* handles, const lvbgs_frame* frames, int n,
                                 void* cuda_stream, uint64_t* ticket);
 /* 1: the tick has completed, 0: not yet, -1: unknown ticket or device error */

@@ -44,6 +44,7 @@ typedef struct {
     int max_queue;                  /* queued frames per stream before lvserve_submit answers LVBGS_BUSY; 8 */
     double idle_spill_ms;           /* a stream idle this long may be spilled to make room; 500 */
     int max_inflight;               /* ticks in flight, 1..LVBGS_BATCH_MAX_INFLIGHT; 2 */
+    int pawcs_lanes;                /* host threads running PAWCS frame steps beside the batched ticks; 2 */
 } lvserve_config;
 
 typedef struct {
@@ -59,7 +60,8 @@ typedef struct {
     size_t device_bytes_in_use; /* resident streams + batch work area, as accounted against the budget */
     size_t peak_device_bytes;
     double mean_tick_streams;   /* streams per tick */
-    double busy_ms;             /* wall time with at least one tick in flight */
+    double busy_ms;             /* wall time with at least one tick (or PAWCS frame step) in flight */
+    uint64_t pawcs_frames;      /* frames of PAWCS streams done (on the PAWCS lanes) */
 } lvserve_stats;
 
 lvbgs_status lvserve_default_config(lvserve_config* out);
@@ -67,9 +69,11 @@ lvbgs_status lvserve_create(const lvserve_config* cfg, lvserve_handle* out);
 /* finishes the frames in flight and queued, then frees every stream */
 lvbgs_status lvserve_destroy(lvserve_handle s);
 
-/* Opens a stream (BackgroundSubtractorSuBSENSE_ constructor + initialize(img, roi)); the image and
- * roi are copied, and initialize() runs when the stream is admitted. LVBGS_BUSY at max_live;
- * LVBGS_BAD_SIZE if the stream alone can never fit the budget. */
+/* Opens a stream (BackgroundSubtractorSuBSENSE_ / BackgroundSubtractorPAWCS_ constructor +
+ * initialize(img, roi)); the image and roi are copied, and initialize() runs when the stream is
+ * admitted. SuBSENSE streams are batched into ticks; PAWCS streams (single-channel) run frame by
+ * frame on the PAWCS lanes and are never spilled. LVBGS_BUSY at max_live; LVBGS_BAD_SIZE if the
+ * stream alone can never fit the budget. */
 lvbgs_status lvserve_open(lvserve_handle s, lvbgs_algo algo, const lvbgs_params* params, const uint8_t* init_image,
                           int width, int height, int channels, size_t stride, const uint8_t* roi, int* stream_id);
 /* Queues one frame (apply(img, fgmask, learning_rate)); LVBGS_BUSY if max_queue frames are queued. */
@@ -109,6 +113,7 @@ typedef struct {
     double fps;           /* 30 */
     double res_prob[4];   /* .3 .3 .3 .1 */
     double gray_prob;     /* .25 */
+    double pawcs_prob;    /* share of the single-channel streams that run PAWCS: .1 */
     int prefill;          /* 1: start from the stationary population (Poisson(rate * mean life) streams with residual lives) */
     int pool_frames;      /* 4 */
     int render_threads;   /* 4 */
@@ -123,6 +128,8 @@ typedef struct {
     double offered_mpix_per_s; /* W*H of the frames submitted in the window per second */
     double p50_ms, p90_ms, p99_ms, max_ms; /* latency of frames submitted in the window */
     double admit_wait_p50_ms, admit_wait_p99_ms; /* open -> admitted */
+    double pawcs_p50_ms, pawcs_p99_ms;           /* latency of the PAWCS streams' frames */
+    uint64_t pawcs_frames;                       /* PAWCS frames finished in the window */
     double mean_live, mean_resident, mean_tick_streams, gpu_busy_frac;
     uint64_t ticks, arrivals, admitted, rejected, dropped, spills, restores, late_frames;
     int peak_live;

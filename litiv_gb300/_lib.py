@@ -60,7 +60,7 @@ class SynthConfig(C.Structure):
 class ServeConfig(C.Structure):
     _fields_ = [("device_id", C.c_int), ("hbm_budget_bytes", C.c_size_t), ("host_spill_budget_bytes", C.c_size_t),
                 ("max_live", C.c_int), ("max_queue", C.c_int), ("idle_spill_ms", C.c_double),
-                ("max_inflight", C.c_int)]
+                ("max_inflight", C.c_int), ("pawcs_lanes", C.c_int)]
 
 
 class ServeResult(C.Structure):
@@ -73,13 +73,14 @@ class ServeStats(C.Structure):
                 ("spills", C.c_uint64), ("restores", C.c_uint64), ("closed", C.c_uint64), ("live", C.c_int),
                 ("waiting", C.c_int), ("resident", C.c_int), ("spilled", C.c_int),
                 ("device_bytes_in_use", C.c_size_t), ("peak_device_bytes", C.c_size_t),
-                ("mean_tick_streams", C.c_double), ("busy_ms", C.c_double)]
+                ("mean_tick_streams", C.c_double), ("busy_ms", C.c_double), ("pawcs_frames", C.c_uint64)]
 
 
 class SimConfig(C.Structure):
     _fields_ = [("duration_s", C.c_double), ("warmup_s", C.c_double), ("arrival_rate", C.c_double),
                 ("life_min_s", C.c_double), ("life_max_s", C.c_double), ("fps", C.c_double),
-                ("res_prob", C.c_double * 4), ("gray_prob", C.c_double), ("prefill", C.c_int),
+                ("res_prob", C.c_double * 4), ("gray_prob", C.c_double), ("pawcs_prob", C.c_double),
+                ("prefill", C.c_int),
                 ("pool_frames", C.c_int), ("render_threads", C.c_int), ("seed", C.c_uint64)]
 
 
@@ -87,7 +88,9 @@ class SimResult(C.Structure):
     _fields_ = [("window_s", C.c_double), ("frames", C.c_uint64), ("mpix_per_s", C.c_double),
                 ("frames_per_s", C.c_double), ("offered_mpix_per_s", C.c_double), ("p50_ms", C.c_double),
                 ("p90_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double),
-                ("admit_wait_p50_ms", C.c_double), ("admit_wait_p99_ms", C.c_double), ("mean_live", C.c_double),
+                ("admit_wait_p50_ms", C.c_double), ("admit_wait_p99_ms", C.c_double),
+                ("pawcs_p50_ms", C.c_double), ("pawcs_p99_ms", C.c_double), ("pawcs_frames", C.c_uint64),
+                ("mean_live", C.c_double),
                 ("mean_resident", C.c_double), ("mean_tick_streams", C.c_double), ("gpu_busy_frac", C.c_double),
                 ("ticks", C.c_uint64), ("arrivals", C.c_uint64), ("admitted", C.c_uint64),
                 ("rejected", C.c_uint64), ("dropped", C.c_uint64), ("spills", C.c_uint64),
@@ -140,6 +143,7 @@ SIGNATURES = {
     "lvbgs_debug_tick_profile": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int]),
     "lvbgs_debug_repair_phases": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int]),
     "lvbgs_set_roi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
+    "lvbgs_batch_set_repair_share": (C.c_int, [C.c_void_p, C.c_int]),
     "lvbgs_debug_set_timing": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "lvbgs_device_bytes": (C.c_size_t, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_size_t]),
     "lvbgs_batch_create": (C.c_int, [C.c_int, C.c_size_t, C.c_int, C.POINTER(C.c_void_p)]),

@@ -91,6 +91,7 @@ struct Workspace {
     unsigned long long* lists = nullptr;  // 4 lists of `cap` entries
     size_t cap = 0;
     int nStreamsCap = 0;
+    int repairDiv = 1;  // the repair kernel's cooperative grid: 1/repairDiv of the co-resident blocks
     std::vector<StreamDev> h_streams;
     std::vector<unsigned long long> h_dsBase;
     // optional per-kernel timing: a ring of kTimedKernels+1 events per tick
@@ -388,7 +389,7 @@ lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t s
     lvbgs_k_resolve<<<(totalTiles + kResolveTiles - 1) / kResolveTiles + dsBlocks, blk, 0, st>>>(P, ds, dsb);
     LV_TMARK(3);
     {
-        const int grid = std::max(1, std::min(maxBlocks, std::max(1, totalTiles)));
+        const int grid = std::max(1, std::min(maxBlocks / std::max(1, ws.repairDiv), std::max(1, totalTiles)));
         void* args[] = {&P};
         LV_CUDA(errh, cudaLaunchCooperativeKernel((const void*)lvbgs_k_repair, dim3(grid), blk, args, 0, st),
                 "repair kernel launch");
@@ -1289,6 +1290,12 @@ lvbgs_status lvbgs_batch_reserve(lvbgs_batch b, size_t px, int n_streams) {
     if (b->inflight > 0 && (px > b->ws.cap || n_streams > b->ws.nStreamsCap))
         return fail(nullptr, LVBGS_BAD_ARG, "cannot grow a batch context with ticks in flight");
     LV_CUDA(nullptr, b->ws.ensure(std::max<size_t>(px, 1), std::max(n_streams, 1)), "batch workspace allocation");
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_batch_set_repair_share(lvbgs_batch b, int divisor) {
+    if (!b || divisor < 1 || divisor > 64) return fail(nullptr, LVBGS_BAD_ARG, "repair share divisor must be 1..64");
+    b->ws.repairDiv = divisor;
     return LVBGS_OK;
 }
 

@@ -77,6 +77,7 @@ struct lvserve_ctx {
     std::mutex mu;
     std::condition_variable cvWork, cvDone;
     std::thread th;
+    std::vector<std::thread> lanes;  // PAWCS lanes
     bool stop = false;
     std::map<int, std::unique_ptr<SStream>> streams;
     std::deque<SStream*> admitQ;
@@ -212,6 +213,7 @@ bool make_room(lvserve_ctx* s, size_t need, const SStream* except) {
         for (auto& kv : s->streams) {
             SStream* x = kv.second.get();
             if (x == except || x->state != S_RESIDENT || x->inFlight || !x->q.empty()) continue;
+            if (x->algo != LVBGS_ALGO_SUBSENSE) continue;  // spilling is implemented for SuBSENSE streams
             if (s->cfg.host_spill_budget_bytes && s->hostSpilled + x->stateBytes > s->cfg.host_spill_budget_bytes)
                 continue;
             cand.push_back(x);
@@ -342,6 +344,7 @@ bool launch(lvserve_ctx* s, std::vector<lvbgs_handle>& hs, std::vector<lvbgs_fra
         std::lock_guard<std::mutex> lk(s->mu);
         for (auto& kv : s->streams) {
             SStream* x = kv.second.get();
+            if (x->algo != LVBGS_ALGO_SUBSENSE) continue;  // PAWCS streams run on the PAWCS lanes
             if (x->state != S_RESIDENT || x->inFlight || x->q.empty() || x->failed) continue;
             t.ss.push_back(x);
             px += x->npx();
@@ -407,6 +410,62 @@ bool launch(lvserve_ctx* s, std::vector<lvbgs_handle>& hs, std::vector<lvbgs_fra
     return true;
 }
 
+// A PAWCS lane: PAWCS frame steps wait on the host for their fixed-point rounds, so they cannot join
+// a batched tick; each lane takes the oldest queued frame of a resident PAWCS stream and runs it on
+// that stream's own CUDA stream, beside the batched SuBSENSE ticks. A stream's frames run in
+// submission order (one in flight per stream), so its results are those of the stream alone.
+void pawcs_lane(lvserve_ctx* s) {
+    cudaSetDevice(s->cfg.device_id);
+    for (;;) {
+        SStream* x = nullptr;
+        Req r;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            for (auto& kv : s->streams) {
+                SStream* y = kv.second.get();
+                if (y->algo != LVBGS_ALGO_PAWCS || y->state != S_RESIDENT || y->inFlight || y->q.empty() || y->failed)
+                    continue;
+                if (!x || y->q.front().t0 < x->q.front().t0) x = y;
+            }
+            if (!x) {
+                if (s->stop && s->streams.empty()) break;
+                s->cvWork.wait_for(lk, std::chrono::microseconds(1000));
+                continue;
+            }
+            r = x->q.front();
+            x->q.pop_front();
+            --s->queued;
+            x->inFlight = true;
+            if (s->inflightN == 0) s->busySince = Clock::now();
+            ++s->inflightN;
+        }
+        const lvbgs_status st = lvbgs_apply(x->h, r.img, r.stride, r.mask, r.lr, nullptr);
+        const Clock::time_point now = Clock::now();
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            if (st != LVBGS_OK && s->err.empty()) s->err = lvbgs_last_error(x->h);
+            x->inFlight = false;
+            x->lastActive = now;
+            const double l = ms_between(r.t0, now);
+            if (s->lat.size() < kLatCap) s->lat.push_back(l);
+            else s->lat[s->latPos++ % kLatCap] = l;
+            if (s->results.size() < s->maxResults) s->results.push_back({x->id, r.tag, (int)st, l});
+            ++s->st.frames_done;
+            s->st.px_done += x->npx();
+            ++s->st.pawcs_frames;
+            if (s->onDone) s->onDone(*x, r, now, (int)st);
+            if (st != LVBGS_OK) {
+                x->failed = true;
+                fail_queue(s, x, (int)st);
+            }
+            --s->inflightN;
+            if (s->inflightN == 0) s->st.busy_ms += ms_between(s->busySince, now);
+        }
+        s->cvDone.notify_all();
+        s->cvWork.notify_all();
+    }
+}
+
 void scheduler(lvserve_ctx* s) {
     cudaSetDevice(s->cfg.device_id);
     std::vector<lvbgs_handle> hs;
@@ -431,7 +490,7 @@ extern "C" {
 
 lvbgs_status lvserve_default_config(lvserve_config* out) {
     if (!out) return LVBGS_BAD_ARG;
-    *out = lvserve_config{0, 0, 0, 256, 8, 500.0, 2};
+    *out = lvserve_config{0, 0, 0, 256, 8, 500.0, 2, 2};
     return LVBGS_OK;
 }
 
@@ -442,7 +501,7 @@ lvbgs_status lvserve_create(const lvserve_config* cfg, lvserve_handle* out) {
     lvserve_default_config(&c);
     if (cfg) c = *cfg;
     if (c.max_live <= 0 || c.max_queue <= 0 || c.max_inflight < 1 || c.max_inflight > LVBGS_BATCH_MAX_INFLIGHT ||
-        c.idle_spill_ms < 0)
+        c.idle_spill_ms < 0 || c.pawcs_lanes < 0 || c.pawcs_lanes > 64)
         return LVBGS_BAD_ARG;
     if (cudaSetDevice(c.device_id) != cudaSuccess) return LVBGS_DEVICE_ERROR;
     if (c.hbm_budget_bytes == 0) {
@@ -456,11 +515,15 @@ lvbgs_status lvserve_create(const lvserve_config* cfg, lvserve_handle* out) {
     s->reservedStreams = 64;
     if (lvbgs_batch_create(c.device_id, s->reservedPx, s->reservedStreams, &s->batch) != LVBGS_OK)
         return LVBGS_OOM;
+    // with PAWCS lanes, the ticks share the device: the cooperative repair grid takes half of the
+    // co-resident blocks so that it can start beside the lanes' kernels
+    if (c.pawcs_lanes > 0) lvbgs_batch_set_repair_share(s->batch, 2);
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
         lvbgs_batch_destroy(s->batch);
         return LVBGS_DEVICE_ERROR;
     }
     s->th = std::thread(scheduler, s.get());
+    for (int i = 0; i < c.pawcs_lanes; ++i) s->lanes.emplace_back(pawcs_lane, s.get());
     *out = s.release();
     return LVBGS_OK;
 }
@@ -477,6 +540,11 @@ lvbgs_status lvserve_destroy(lvserve_handle s) {
         s->cvWork.notify_all();
     }
     s->th.join();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->cvWork.notify_all();
+    }
+    for (std::thread& t : s->lanes) t.join();
     lvbgs_batch_destroy(s->batch);
     cudaStreamDestroy(s->stream);
     for (auto& kv : s->pinnedFree) cudaFreeHost(kv.second);
@@ -488,6 +556,11 @@ lvbgs_status lvserve_open(lvserve_handle s, lvbgs_algo algo, const lvbgs_params*
                           int H, int C, size_t stride, const uint8_t* roi, int* id) {
     if (!s || !img || !id || W <= 0 || H <= 0) return LVBGS_BAD_ARG;
     if (C != 1 && C != 3) return LVBGS_BAD_TYPE;
+    if (algo == LVBGS_ALGO_PAWCS && s->cfg.pawcs_lanes == 0) {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->err = "PAWCS streams need pawcs_lanes > 0";
+        return LVBGS_UNSUPPORTED;
+    }
     const size_t dev = lvbgs_device_bytes(algo, W, H, C, params ? params->bg_samples : 50);
     if (dev == 0) return LVBGS_UNSUPPORTED;
     std::unique_ptr<SStream> x(new SStream());
@@ -675,6 +748,7 @@ struct SimStream {
     size_t idx = 0;  // position in the population (frame tags carry it)
     int cls = 0;  // 2 * resolution class + gray
     int W = 0, H = 0, C = 0;
+    lvbgs_algo algo = LVBGS_ALGO_SUBSENSE;
     uint64_t seed = 0;
     int id = -1;
     bool rejected = false;
@@ -729,7 +803,7 @@ extern "C" {
 
 lvbgs_status lvserve_default_sim_config(lvserve_sim_config* o) {
     if (!o) return LVBGS_BAD_ARG;
-    *o = lvserve_sim_config{20.0, 3.0, 4.0, 10.0, 60.0, 30.0, {0.3, 0.3, 0.3, 0.1}, 0.25, 1, 4, 4, 1};
+    *o = lvserve_sim_config{20.0, 3.0, 4.0, 10.0, 60.0, 30.0, {0.3, 0.3, 0.3, 0.1}, 0.25, 0.1, 1, 4, 4, 1};
     return LVBGS_OK;
 }
 
@@ -740,7 +814,8 @@ lvbgs_status lvserve_simulate(const lvserve_config* cfg, const lvserve_sim_confi
     lvserve_default_sim_config(&sim);
     if (simIn) sim = *simIn;
     if (sim.duration_s <= 0 || sim.warmup_s < 0 || sim.arrival_rate < 0 || sim.life_min_s <= 0 ||
-        sim.life_max_s < sim.life_min_s || sim.fps <= 0 || sim.pool_frames < 1 || sim.render_threads < 1)
+        sim.life_max_s < sim.life_min_s || sim.fps <= 0 || sim.pool_frames < 1 || sim.render_threads < 1 ||
+        !(sim.pawcs_prob >= 0.0 && sim.pawcs_prob <= 1.0))
         return LVBGS_BAD_ARG;
     static const int kW[4] = {320, 640, 1280, 1920}, kH[4] = {240, 480, 720, 1080};
     const double horizon = sim.warmup_s + sim.duration_s;
@@ -760,6 +835,8 @@ lvbgs_status lvserve_simulate(const lvserve_config* cfg, const lvserve_sim_confi
             }
         }
         const int gray = rng.uni() < sim.gray_prob ? 1 : 0;
+        // PAWCS runs on single-channel frames; a share of them run it
+        z->algo = (gray && rng.uni() < sim.pawcs_prob) ? LVBGS_ALGO_PAWCS : LVBGS_ALGO_SUBSENSE;
         z->cls = 2 * r + gray;
         z->W = kW[r];
         z->H = kH[r];
@@ -789,8 +866,8 @@ lvbgs_status lvserve_simulate(const lvserve_config* cfg, const lvserve_sim_confi
     Slabs slabs;
     const int K = sim.pool_frames;
     // latency records of frames submitted in the measured window (guarded by the server's mutex)
-    std::vector<double> lat, admitWait;
-    uint64_t donePx = 0, doneFrames = 0;
+    std::vector<double> lat, admitWait, pawcsLat;
+    uint64_t donePx = 0, doneFrames = 0, pawcsFrames = 0;
     int firstErr = 0;
     Clock::time_point T0;
     std::atomic<bool> clockSet{false};
@@ -803,10 +880,14 @@ lvbgs_status lvserve_simulate(const lvserve_config* cfg, const lvserve_sim_confi
     srv->onDone = [&](const SStream& x, const Req& r, Clock::time_point now, int status) {
         if (status != 0 && !firstErr) firstErr = status;
         SimStream* z = ss[(size_t)(r.tag >> 20)].get();
-        if (in_window(r.t0)) lat.push_back(ms_between(r.t0, now));
+        if (in_window(r.t0)) {
+            lat.push_back(ms_between(r.t0, now));
+            if (x.algo == LVBGS_ALGO_PAWCS) pawcsLat.push_back(ms_between(r.t0, now));
+        }
         if (in_window(now)) {
             donePx += x.npx();
             ++doneFrames;
+            if (x.algo == LVBGS_ALGO_PAWCS) ++pawcsFrames;
         }
         if (--z->outstanding == 0 && z->closed) slabs.put(z->cls, z->pool);
     };
@@ -899,10 +980,9 @@ lvbgs_status lvserve_simulate(const lvserve_config* cfg, const lvserve_sim_confi
             if (z->ready < 0) continue;
             int id = -1;
             lvbgs_params prm;
-            lvbgs_default_params(LVBGS_ALGO_SUBSENSE, &prm);
+            lvbgs_default_params(z->algo, &prm);
             prm.seed = z->seed;
-            const lvbgs_status r =
-                lvserve_open(srv, LVBGS_ALGO_SUBSENSE, &prm, z->pool, z->W, z->H, z->C, 0, nullptr, &id);
+            const lvbgs_status r = lvserve_open(srv, z->algo, &prm, z->pool, z->W, z->H, z->C, 0, nullptr, &id);
             if (r != LVBGS_OK) {
                 z->rejected = true;
                 ++rejected;
@@ -971,6 +1051,9 @@ lvbgs_status lvserve_simulate(const lvserve_config* cfg, const lvserve_sim_confi
         out->max_ms = lat.empty() ? 0.0 : *std::max_element(lat.begin(), lat.end());
         out->admit_wait_p50_ms = quantile(admitWait, 0.50);
         out->admit_wait_p99_ms = quantile(admitWait, 0.99);
+        out->pawcs_p50_ms = quantile(pawcsLat, 0.50);
+        out->pawcs_p99_ms = quantile(pawcsLat, 0.99);
+        out->pawcs_frames = pawcsFrames;
         out->status = firstErr;
     }
     out->offered_mpix_per_s = (double)offeredPx / 1e6 / sim.duration_s;

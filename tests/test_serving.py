@@ -19,19 +19,21 @@ GiB = 1 << 30
 
 def test_default_config_and_workload():
     cfg = serving.default_config()
-    assert (cfg.max_live, cfg.max_queue, cfg.max_inflight) == (256, 8, 2)
+    assert (cfg.max_live, cfg.max_queue, cfg.max_inflight, cfg.pawcs_lanes) == (256, 8, 2, 2)
     assert cfg.idle_spill_ms == 500.0
     sim = serving.default_sim_config()
     # Poisson arrivals at 4 streams/s, lives U[10, 60] s, 30 fps, resolution mix .3/.3/.3/.1
     assert (sim.arrival_rate, sim.life_min_s, sim.life_max_s, sim.fps) == (4.0, 10.0, 60.0, 30.0)
     assert [round(p, 6) for p in sim.res_prob] == [0.3, 0.3, 0.3, 0.1]
+    # a quarter single-channel, a tenth of those running PAWCS (SuBSENSE/PAWCS mixed)
+    assert (sim.gray_prob, sim.pawcs_prob) == (0.25, 0.1)
 
 
 def test_create_rejects_bad_config():
     lib = L.lib()
     h = C.c_void_p()
     for field, value in [("max_live", 0), ("max_queue", 0), ("max_inflight", 0), ("max_inflight", 5),
-                         ("idle_spill_ms", -1.0)]:
+                         ("idle_spill_ms", -1.0), ("pawcs_lanes", -1)]:
         cfg = serving.default_config(**{field: value})
         assert lib.lvserve_create(C.byref(cfg), C.byref(h)) == L.BAD_ARG, field
     assert lib.lvserve_submit(None, 1, None, 0, None, 0.0, 0) == L.BAD_ARG
@@ -169,3 +171,40 @@ def test_serving_workload_simulation_short():
     assert 0 < r["p50_ms"] <= r["p99_ms"] <= r["max_ms"]
     assert r["admitted"] >= 1 and r["ticks"] >= 1
     assert r["dropped"] == 0
+
+
+@pytest.mark.gpu
+def test_pawcs_and_subsense_streams_served_together_equal_alone():
+    # SuBSENSE/PAWCS mixed: PAWCS frames run on the PAWCS lanes beside the batched SuBSENSE ticks;
+    # every mask must equal the same stream run alone
+    from litiv_gb300 import BackgroundSubtractorPAWCS
+    mix = [(L.ALGO_SUBSENSE, 96, 64, 3, 31), (L.ALGO_PAWCS, 96, 72, 1, 32), (L.ALGO_SUBSENSE, 64, 48, 1, 33),
+           (L.ALGO_PAWCS, 160, 120, 1, 34)]
+    n_frames = 10
+    data = [_frames(W, H, Cn, seed, n_frames) for (_, W, H, Cn, seed) in mix]
+    alone = []
+    for (algo, _, _, _, seed), fr in zip(mix, data):
+        if algo == L.ALGO_PAWCS:
+            b = BackgroundSubtractorPAWCS(seed=seed)
+            b.initialize(fr[0])
+            alone.append([b.apply(f) for f in fr[1:]])
+        else:
+            alone.append(_alone(fr, seed))
+    with serving.StreamServer(max_queue=64, pawcs_lanes=2) as srv:
+        ids = [srv.open(fr[0], params={"seed": seed}, algo=algo) for fr, (algo, _, _, _, seed) in zip(data, mix)]
+        masks = {}
+        for t in range(1, n_frames):
+            for i, (_, W, H, _, _) in enumerate(mix):
+                m = np.full((H, W), 77, np.uint8)
+                masks[(i, t)] = m
+                assert srv.submit(ids[i], data[i][t], m, tag=t)
+        srv.drain()
+        results = srv.poll(4096)
+        st = srv.stats()
+    assert all(r[2] == L.OK for r in results), [r for r in results if r[2] != L.OK][:3]
+    assert len(results) == len(masks)
+    for (i, t), m in masks.items():
+        diff = int((m != alone[i][t - 1]).sum())
+        assert diff == 0, "stream %d frame %d: served mask differs from the stream alone at %d px" % (i, t, diff)
+    assert st["pawcs_frames"] == 2 * (n_frames - 1)
+
