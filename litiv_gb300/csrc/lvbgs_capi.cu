@@ -47,6 +47,7 @@ extern "C" __global__ void pw_k_gscan(PwParams P);
 extern "C" __global__ void pw_k_cells(PwParams P, int final);
 extern "C" __global__ void pw_k_nbr(PwParams P);
 extern "C" __global__ void pw_k_replace(PwParams P);
+extern "C" __global__ void pw_k_nbr_loops(PwParams P);
 extern "C" __global__ void pw_k_dirty(PwParams P);
 extern "C" __global__ void pw_k_commit(PwParams P);
 extern "C" __global__ void pw_k_weights(PwParams P);
@@ -523,7 +524,7 @@ enum {
     PL_GMAP, PL_DSLT, PL_DSST, PL_DSROI,
     // scratch (not part of the model)
     PL_BITS, PL_HCOUNT, PL_LABEL, PL_INTENT, PL_DESCT, PL_REC, PL_OUT, PL_REPB, PL_REPA, PL_UFINAL, PL_UV,
-    PL_ITEMLIST, PL_CONTRIBLIST, PL_BLKCOUNTS, PL_CATINFO, PL_DSABS, PL_GITEM, PL_CONTRIB, PL_DSFRAME, PL_FRAME, PL_MASK, PL_ROWSUM, PL_WORK, PL_FLAGS, PL_PDEV, PL_SDEV, PL_COUNT
+    PL_ITEMLIST, PL_CONTRIBLIST, PL_BLKCOUNTS, PL_CATINFO, PL_DSABS, PL_UPDLIST, PL_GITEM, PL_CONTRIB, PL_DSFRAME, PL_FRAME, PL_MASK, PL_ROWSUM, PL_WORK, PL_FLAGS, PL_PDEV, PL_SDEV, PL_COUNT
 };
 struct PwLayout {
     size_t off[PL_COUNT];
@@ -559,6 +560,7 @@ PwLayout pw_layout(int W, int H, int L, int G) {
     sz[PL_BLKCOUNTS] = ((npx + kPwCompactBlk - 1) / kPwCompactBlk) * kPwCats * 4;
     sz[PL_CATINFO] = 64 * 4;
     sz[PL_DSABS] = std::max<size_t>(nds, 1) * 4;
+    sz[PL_UPDLIST] = npx * 4;
     sz[PL_GITEM] = npx * 4;
     sz[PL_CONTRIB] = npx * 4;
     sz[PL_DSFRAME] = std::max<size_t>(nds, 1);
@@ -667,6 +669,7 @@ void pw_fill(lvbgs_ctx* h, const PwLayout& Lo, int L, int G) {
     D.blkCounts = (uint32_t*)(b + Lo.off[PL_BLKCOUNTS]);
     D.catInfo = (uint32_t*)(b + Lo.off[PL_CATINFO]);
     D.dsAbs = (float*)(b + Lo.off[PL_DSABS]);
+    D.updList = (uint32_t*)(b + Lo.off[PL_UPDLIST]);
     D.gitem = (uint32_t*)(b + Lo.off[PL_GITEM]);
     D.contrib = (float*)(b + Lo.off[PL_CONTRIB]);
     D.dsRoi = b + Lo.off[PL_DSROI];
@@ -835,6 +838,8 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
         pw_k_gscan<<<1, 32, 0, st>>>(P);
         pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
         pw_k_nbr<<<tiles, blk, 0, st>>>(P);
+        compact(2);
+        pw_k_nbr_loops<<<std::max(1, std::min(cblocks * 4, 1216)), 256, 0, st>>>(P);
         pw_k_replace<<<tiles, blk, 0, st>>>(P);
         LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 4, st), "flag reset");
         pw_k_dirty<<<tiles, blk, 0, st>>>(P);
@@ -873,7 +878,7 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
     lvbgs_k_dilate<<<h->H, 128, 0, st>>>(TP);
     const int nds = (h->W / 8) * (h->H / 8);
     if (nds > 0) pw_k_ds<<<(nds + 255) / 256, 256, 0, st>>>(P);
-    pw_k_epilogue<<<1, 32, 0, st>>>(P);
+    pw_k_epilogue<<<1, 256, 0, st>>>(P);
     const uint32_t t = (uint32_t)(h->pw_frames + 1);
     if (nds > 0 && t % kPwBootWin == 0) {
         // camera-motion comparison (:1480-1501): the host waits for the decision, which may switch the

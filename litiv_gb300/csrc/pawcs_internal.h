@@ -74,6 +74,9 @@ struct PwOut {
     uint16_t kLoop;      // draw counter at the start of the neighbour loop
     uint8_t segm;        // raw decision (0/255)
     uint8_t gflags;      // bit0 replaced the replaceable word, bit1 contributed to the word weight, bit2 critical
+    uint16_t kEnd;       // draw counter after the neighbour loop
+    uint8_t rflags;      // neighbour loop: bit0 replaces the target's last word, bit1 reached the last word
+    uint8_t pad;
 };
 
 struct PawcsDev {
@@ -108,6 +111,7 @@ struct PawcsDev {
     uint32_t* blkCounts;       // ordered compaction: per block and category counts, then offsets
     uint32_t* catInfo;         // [0..16] category totals, [32..48] category bases
     float* dsAbs;              // |LT - ST| per down-sampled pixel (0 outside the down-sampled ROI)
+    uint32_t* updList;         // pixels that update a neighbour this round, raster order
 };
 
 constexpr int kPwCompactBlk = 1024;  // pixels per block of the ordered compactions

@@ -409,12 +409,14 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_items(PwParams P) {
 
 // ------------------------------------------------------------------------------------------
 // ordered compactions (raster order kept): mode 0 lists the critical global items, mode 1 the word
-// weight contributions per word. Blocks of kPwCompactBlk pixels: counts, offsets, scatter.
+// weight contributions per word, mode 2 the pixels that update a neighbour. Blocks of kPwCompactBlk
+// pixels: counts, offsets, scatter.
 // ------------------------------------------------------------------------------------------
 __device__ __forceinline__ int pw_category(const PawcsDev& S, int p, int mode, int wr, uint32_t nrep) {
     if (!S.sd.roi[p]) return -1;
     const PwOut& O = S.out[p];
     if (mode == 0) return ((S.rec[p].flags & kRfItem) && (O.gflags & 4)) ? 0 : -1;
+    if (mode == 2) return O.q != kPwNone ? 0 : -1;
     if (S.contrib[p] < 0.0f) return -1;
     // the replaceable word keeps only the contributions after its last replacement of the frame
     if (O.gword >= (uint32_t)S.G) return -1;
@@ -494,7 +496,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_compact_scatter(PwParams 
         const int p = blockIdx.x * kPwCompactBlk + k * 256 + threadIdx.x;
         const int c = p < D.npx ? pw_category(S, p, mode, wr, nrep) : -1;
         uint32_t rank = 0;
-        const int ncat = mode == 0 ? 1 : S.G;
+        const int ncat = mode == 1 ? S.G : 1;
         for (int j = 0; j < ncat; ++j) {
             const unsigned m = __ballot_sync(0xffffffffu, c == j);
             if (c == j) rank = __popc(m & ((1u << lane) - 1u));
@@ -523,6 +525,8 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_compact_scatter(PwParams 
                 const uint32_t b = min(th.color, 65535u) | (min(th.desc / 4u, 65535u) << 16);
                 const uint32_t d = (uint32_t)S.descT[p] | ((uint32_t)(R.flags & (kRfEvent | kRfRepDraw)) << 16);
                 S.itemList[pos] = make_uint4((uint32_t)p, a, b, d);
+            } else if (mode == 2) {
+                S.updList[pos] = (uint32_t)p;
             } else {
                 S.contribList[pos] = S.contrib[p];
             }
@@ -732,6 +736,88 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_nbr(PwParams P) {
     O.kLoop = (uint16_t)k;
 }
 
+// the neighbour-update loop of updater p on target q (:847-880; one channel: the reference updates a
+// copy of each word, so only the weight sum and the draws count). p sees q's dictionary before q's own
+// scan (p < q: frame-start words, the last one replaced by the earlier updater rs, if any) or after it
+// (p >= q: the scanned words with their illumination marks). Returns the weight sum; k advances by
+// the loop's draws; reachedLast tells whether the loop looked at the last word (the only one rs changes).
+__device__ float pw_nbr_loop(const PawcsDev& S, uint32_t t, int cur, int nxt, int boot, unsigned long long off, int p,
+                             int q, uint32_t rs, uint32_t& k, bool& reachedLast) {
+    const StreamDev& D = S.sd;
+    const float* fm = D.fm + (size_t)cur * kNumFloatMaps * D.npx;
+    const PwRec& R = S.rec[p];
+    const uint32_t col = D.frame[p], desc = S.descT[p];
+    const PwThr th = pw_thresholds(fm[FM_R * D.npx + p], S.unstable[p], S.minColor, S.descOff);
+    const int flat = (R.flags & kRfFlat) != 0;
+    PwWordSrc ws;
+    ws.S = &S;
+    ws.q = q;
+    ws.L = S.L;
+    ws.t = t;
+    ws.qcol = D.frame[q];
+    ws.qdesc = S.descT[q];
+    uint8_t segmQ;
+    uint32_t lastDescQ;
+    if (p < q) {
+        ws.buf = cur;
+        ws.m = 0;
+        segmQ = 0;
+        lastDescQ = D.lastDesc[q];
+    } else {
+        const PwRec& Rq = S.rec[q];
+        ws.buf = nxt;
+        ws.m = (S.uFinal[q] & 2) ? Rq.m1 : Rq.m0;
+        segmQ = S.out[q].segm;
+        // the pixel's last descriptor is updated at the end of its own processing (:925-926)
+        lastDescQ = p == q ? D.lastDesc[q] : S.descT[q];
+    }
+    ws.repl = rs != kPwNone;
+    if (ws.repl) {
+        ws.rcol = D.frame[rs];
+        ws.rdesc = S.descT[rs];
+        ws.rincr = S.rec[rs].incr;
+    }
+    float nsum = 0.0f;
+    reachedLast = false;
+    for (int j = 0; j < S.L && nsum < R.thrW; ++j) {
+        if (j == S.L - 1) reachedLast = true;
+        uint32_t c, d, o, f, l;
+        pw_word(ws, j, c, d, o, f, l);
+        const uint32_t cd = pw_absdiff(col, c);
+        if (cd <= th.color && (uint32_t)__popc(desc ^ d) <= th.desc) {
+            nsum += pw_weight(o, f, l, t, off);
+        } else if (!segmQ && flat && (boot || pw_mod(pw_draw(D.seed, t, (uint32_t)p, k++), R.rate) == 0u)) {
+            if (cd <= th.color && (uint32_t)__popc(desc ^ lastDescQ) <= th.desc / 2u) nsum += pw_weight(o, f, l, t, off);
+        }
+    }
+    return nsum;
+}
+
+// neighbour updates, pass 1: every updater's loop (one thread each, over the compacted list), as if no
+// earlier updater of its target had replaced the target's last word
+extern "C" __global__ void __launch_bounds__(256) pw_k_nbr_loops(PwParams P) {
+    const PawcsDev& S = P.streams[0];
+    const StreamDev& D = S.sd;
+    const uint32_t n = S.catInfo[0];
+    const uint32_t t = (uint32_t)(D.ctl->frame_idx + 1ull);
+    const int cur = (int)(D.ctl->frame_idx & 1ull), nxt = cur ^ 1;
+    const int boot = t <= (uint32_t)kBootWin;
+    const unsigned long long off = S.pc->lword_offset;
+    const float initW = 1.0f / (float)off;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int p = (int)S.updList[i];
+        PwOut& O = S.out[p];
+        uint32_t k = O.kLoop;
+        bool reachedLast;
+        const float nsum = pw_nbr_loop(S, t, cur, nxt, boot, off, p, (int)O.q, kPwNone, k, reachedLast);
+        O.kEnd = (uint16_t)k;
+        O.rflags = (uint8_t)((nsum < initW ? 1 : 0) | (reachedLast ? 2 : 0));
+    }
+}
+
+// neighbour updates, pass 2 (per target, raster order over its <= 25 updaters): the latest updater of
+// each group that replaces the last word is the replacement source the next ones see; a later updater
+// whose loop reached that word is redone with it (the earlier words are the same either way)
 extern "C" __global__ void __launch_bounds__(256) pw_k_replace(PwParams P) {
     const int t0 = blockIdx.x;
     if (t0 >= P.totalTiles) return;
@@ -749,11 +835,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_replace(PwParams P) {
     const int boot = t <= (uint32_t)kBootWin;
     const unsigned long long off = S.pc->lword_offset;
     const float initW = 1.0f / (float)off;
-    const float* fm = D.fm + (size_t)cur * kNumFloatMaps * D.npx;
     uint32_t before = kPwNone, after = kPwNone;
-    const uint8_t uq = S.uFinal[q];
-    const PwRec& Rq = S.rec[q];
-    const uint32_t qm = (uq & 2) ? Rq.m1 : Rq.m0;
     for (int dy = -2; dy <= 2; ++dy)
         for (int dx = -2; dx <= 2; ++dx) {
             const int px = qx + dx, py = qy + dy;
@@ -764,55 +846,17 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_replace(PwParams P) {
             // the ROI's outer rows and columns): the update then follows the pixel's own processing
             PwOut& O = S.out[p];
             if (O.q != (uint32_t)q) continue;
-            const PwRec& R = S.rec[p];
-            const uint32_t col = D.frame[p], desc = S.descT[p];
-            const PwThr th = pw_thresholds(fm[FM_R * D.npx + p], S.unstable[p], S.minColor, S.descOff);
-            const int flat = (R.flags & kRfFlat) != 0;
-            PwWordSrc ws;
-            ws.S = &S;
-            ws.q = q;
-            ws.L = S.L;
-            ws.t = t;
-            ws.qcol = D.frame[q];
-            ws.qdesc = S.descT[q];
-            uint32_t rs;
-            uint8_t segmQ;
-            uint32_t lastDescQ;
-            if (p < q) {
-                ws.buf = cur;
-                ws.m = 0;
-                rs = before;
-                segmQ = 0;
-                lastDescQ = D.lastDesc[q];
-            } else {
-                ws.buf = nxt;
-                ws.m = qm;
-                rs = after;
-                segmQ = S.out[q].segm;
-                // the pixel's last descriptor is updated at the end of its own processing (:925-926)
-                lastDescQ = p == q ? D.lastDesc[q] : S.descT[q];
+            const uint32_t rs = p < q ? before : after;
+            uint8_t rf = O.rflags;
+            if (rs != kPwNone && (rf & 2)) {
+                uint32_t k = O.kLoop;
+                bool reachedLast;
+                const float nsum = pw_nbr_loop(S, t, cur, nxt, boot, off, p, q, rs, k, reachedLast);
+                rf = (uint8_t)((nsum < initW ? 1 : 0) | (reachedLast ? 2 : 0));
+                O.kEnd = (uint16_t)k;
+                O.rflags = rf;
             }
-            ws.repl = rs != kPwNone;
-            if (ws.repl) {
-                ws.rcol = D.frame[rs];
-                ws.rdesc = S.descT[rs];
-                ws.rincr = S.rec[rs].incr;
-            }
-            uint32_t k = O.kLoop;
-            float nsum = 0.0f;
-            for (int j = 0; j < S.L && nsum < R.thrW; ++j) {
-                uint32_t c, d, o, f, l;
-                pw_word(ws, j, c, d, o, f, l);
-                const uint32_t cd = pw_absdiff(col, c);
-                if (cd <= th.color && (uint32_t)__popc(desc ^ d) <= th.desc) {
-                    nsum += pw_weight(o, f, l, t, off);
-                } else if (!segmQ && flat && (boot || pw_mod(pw_draw(D.seed, t, (uint32_t)p, k++), R.rate) == 0u)) {
-                    if (cd <= th.color && (uint32_t)__popc(desc ^ lastDescQ) <= th.desc / 2u)
-                        nsum += pw_weight(o, f, l, t, off);
-                }
-            }
-            O.kLoop = (uint16_t)k;  // now the draw count after the loop
-            if (nsum < initW) {
+            if (rf & 1) {
                 if (p < q) before = (uint32_t)p;
                 else after = (uint32_t)p;
             }
@@ -952,7 +996,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_commit(PwParams P) {
         D.lastCol[p] = (uint8_t)col;
         D.lastDesc[p] = (uint16_t)desc;
         D.intent[p] = O.segm ? (kInValid | kInFG) : kInValid;
-        D.kctr[p] = O.q != kPwNone ? O.kLoop : O.kLoop;  // the draw count after the pixel's updates
+        D.kctr[p] = O.q != kPwNone ? O.kEnd : O.kLoop;  // the draw count after the pixel's updates
     } else if (in) {
         D.intent[p] = 0u;
     }
@@ -1241,12 +1285,21 @@ extern "C" __global__ void pw_k_epilogue(PwParams P) {
     const int boot = t <= (uint32_t)kBootWin;
     float fLT, fST;
     pw_factors(t, (int)S.nmv, &fLT, &fST);
-    if (threadIdx.x != 0) return;
-    const int nds = D.dsW * D.dsH;
     (void)fST;
-    // ordered float sum of |LT - ST| over the down-sampled ROI (lv::L1dist, math.hpp:255-268)
+    const int nds = D.dsW * D.dsH;
+    // ordered float sum of |LT - ST| over the down-sampled ROI (lv::L1dist, math.hpp:255-268): the
+    // block stages the terms in shared memory, one thread adds them in order
+    __shared__ float terms[2048];
     float l1 = 0.0f;
-    for (int i = 0; i < nds; ++i) l1 = l1 + S.dsAbs[i];
+    for (int c0 = 0; c0 < nds; c0 += 2048) {
+        const int cnt = min(2048, nds - c0);
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) terms[i] = S.dsAbs[c0 + i];
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int i = 0; i < cnt; ++i) l1 = l1 + terms[i];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
     const float ratio = l1 / (float)pc->ds_roi_count;
     pc->frame_ratio = ratio;
     // LBSP threshold LUT (:1462-1473)
