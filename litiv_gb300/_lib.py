@@ -144,6 +144,7 @@ SIGNATURES = {
     "lvbgs_debug_repair_phases": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int]),
     "lvbgs_set_roi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
     "lvbgs_batch_set_repair_share": (C.c_int, [C.c_void_p, C.c_int]),
+    "lvbgs_set_batch_groups": (C.c_int, [C.c_int]),
     "lvbgs_debug_set_timing": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "lvbgs_device_bytes": (C.c_size_t, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_size_t]),
     "lvbgs_batch_create": (C.c_int, [C.c_int, C.c_size_t, C.c_int, C.POINTER(C.c_void_p)]),

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -158,6 +159,8 @@ struct lvbgs_ctx {
     uint8_t* d_frame = nullptr;
     uint8_t* d_mask = nullptr;
     cudaStream_t stream = nullptr;
+    cudaStream_t aux = nullptr;                          // second group of a split batch (lazily created)
+    cudaEvent_t evFork = nullptr, evJoin = nullptr;      // fork / join of the split batch's two streams
     Workspace ws;       // single-stream launches
     Workspace batchWs;  // batched launches led by this handle
     // PAWCS (algo == LVBGS_ALGO_PAWCS): device descriptor, host mirrors and launch scratch
@@ -1015,6 +1018,12 @@ lvbgs_status lvbgs_destroy(lvbgs_handle h) {
     h->ws.release();
     h->batchWs.release();
     if (h->h_flags) cudaFreeHost(h->h_flags);
+    if (h->aux) {
+        cudaStreamSynchronize(h->aux);
+        cudaStreamDestroy(h->aux);
+    }
+    if (h->evFork) cudaEventDestroy(h->evFork);
+    if (h->evJoin) cudaEventDestroy(h->evJoin);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return LVBGS_OK;
@@ -1194,17 +1203,87 @@ lvbgs_status download_masks(const lvbgs_handle* hs, const lvbgs_frame* frames, i
 }
 }  // namespace
 
+namespace {
+std::atomic<int> g_batch_groups{2};
+constexpr int kSplitMinStreams = 8;
+constexpr size_t kSplitMinPx = (size_t)4 << 20;
+
+// Large batches run as two groups of about half the pixels each (the largest streams first, each to
+// the lighter group; the order within a group is the batch's): one group's latency-bound phases (the
+// repair rounds, the hole-fill row walks) then overlap the other group's work. Returns false for a
+// single group.
+bool split_batch(const lvbgs_handle* hs, int n, std::vector<int>& ga, std::vector<int>& gb) {
+    if (g_batch_groups.load() < 2 || n < kSplitMinStreams) return false;
+    size_t total = 0;
+    for (int i = 0; i < n; ++i) total += hs[i]->npx;
+    if (total < kSplitMinPx) return false;
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hs[a]->npx > hs[b]->npx; });
+    std::vector<char> inB(n, 0);
+    size_t pa = 0, pb = 0;
+    for (int i : order) {
+        if (pb < pa) {
+            inB[i] = 1;
+            pb += hs[i]->npx;
+        } else {
+            pa += hs[i]->npx;
+        }
+    }
+    ga.clear();
+    gb.clear();
+    for (int i = 0; i < n; ++i) (inB[i] ? gb : ga).push_back(i);
+    return !ga.empty() && !gb.empty();
+}
+
+lvbgs_status batch_group(const lvbgs_handle* hs, const lvbgs_frame* frames, int n, cudaStream_t st, int repairDiv) {
+    lvbgs_handle lead = hs[0];
+    Workspace& ws = lead->batchWs;
+    ws.repairDiv = repairDiv;
+    ws.h_streams.resize(n);
+    lvbgs_status s = prepare_batch(hs, frames, n, st, ws.h_streams.data());
+    if (s != LVBGS_OK) return s;
+    if ((s = launch_tick(lead, ws, n, st)) != LVBGS_OK) return s;
+    return download_masks(hs, frames, n, st);
+}
+}  // namespace
+
+lvbgs_status lvbgs_set_batch_groups(int groups) {
+    if (groups != 1 && groups != 2) return fail(nullptr, LVBGS_BAD_ARG, "batch groups must be 1 or 2");
+    g_batch_groups = groups;
+    return LVBGS_OK;
+}
+
 lvbgs_status lvbgs_batch_apply(const lvbgs_handle* hs, const lvbgs_frame* frames, int n, void* cuda_stream) {
     lvbgs_status s = check_batch(hs, frames, n);
     if (s != LVBGS_OK) return s;
     lvbgs_handle lead = hs[0];
     cudaSetDevice(lead->device);
     cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : lead->stream;
-    Workspace& ws = lead->batchWs;
-    ws.h_streams.resize(n);
-    if ((s = prepare_batch(hs, frames, n, st, ws.h_streams.data())) != LVBGS_OK) return s;
-    if ((s = launch_tick(lead, ws, n, st)) != LVBGS_OK) return s;
-    return download_masks(hs, frames, n, st);
+    std::vector<int> ga, gb;
+    if (!split_batch(hs, n, ga, gb)) return batch_group(hs, frames, n, st, 1);
+    // the second group runs on the lead's second stream, forked from and joined back into st; each
+    // group's cooperative repair grid takes half of the co-resident blocks so that both fit
+    if (!lead->aux) LV_CUDA(lead, cudaStreamCreateWithFlags(&lead->aux, cudaStreamNonBlocking), "stream creation");
+    if (!lead->evFork) LV_CUDA(lead, cudaEventCreateWithFlags(&lead->evFork, cudaEventDisableTiming), "event creation");
+    if (!lead->evJoin) LV_CUDA(lead, cudaEventCreateWithFlags(&lead->evJoin, cudaEventDisableTiming), "event creation");
+    std::vector<lvbgs_handle> ha, hb;
+    std::vector<lvbgs_frame> fa, fb;
+    for (int i : ga) {
+        ha.push_back(hs[i]);
+        fa.push_back(frames[i]);
+    }
+    for (int i : gb) {
+        hb.push_back(hs[i]);
+        fb.push_back(frames[i]);
+    }
+    LV_CUDA(lead, cudaEventRecord(lead->evFork, st), "fork");
+    LV_CUDA(lead, cudaStreamWaitEvent(lead->aux, lead->evFork, 0), "fork");
+    if ((s = batch_group(ha.data(), fa.data(), (int)ha.size(), st, 2)) != LVBGS_OK) return s;
+    if ((s = batch_group(hb.data(), fb.data(), (int)hb.size(), lead->aux, 2)) != LVBGS_OK) return s;
+    LV_CUDA(lead, cudaEventRecord(lead->evJoin, lead->aux), "join");
+    LV_CUDA(lead, cudaStreamWaitEvent(st, lead->evJoin, 0), "join");
+    return LVBGS_OK;
 }
 
 lvbgs_status lvbgs_batch_wait(const lvbgs_handle* hs, int n, void* cuda_stream) {
@@ -1213,6 +1292,13 @@ lvbgs_status lvbgs_batch_wait(const lvbgs_handle* hs, int n, void* cuda_stream) 
     cudaSetDevice(lead->device);
     cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : lead->stream;
     LV_CUDA(lead, cudaStreamSynchronize(st), "batched frame step");
+    std::vector<int> ga, gb;
+    if (split_batch(hs, n, ga, gb)) {
+        // the status of each group's work area (the groups' leads)
+        lvbgs_status s = read_work_status(hs[ga[0]], hs[ga[0]]->batchWs);
+        if (s != LVBGS_OK) return s;
+        return read_work_status(hs[gb[0]], hs[gb[0]]->batchWs);
+    }
     return read_work_status(lead, lead->batchWs);
 }
 

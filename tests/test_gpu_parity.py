@@ -244,3 +244,23 @@ def test_set_roi_before_initialize_and_roi_reuse():
     assert gpu.isParallel() and gpu.getParallelAlgoType() == "CUDA"
     with pytest.raises(LvException):
         gpu.setROI(np.zeros((72, 96), np.uint8))
+
+
+def test_split_batch_groups_equal_streams_alone():
+    # >= 8 streams and >= 4 Mi pixels: lvbgs_batch_apply runs the batch as two concurrent groups (two
+    # CUDA streams, half-device repair grids); every mask and model map must equal the stream alone
+    specs = [(1280, 720, 3)] * 4 + [(640, 480, 1)] * 4 + [(320, 240, 3)] * 2
+    streams = [SyntheticStream(0, seed=71 + i, width=W, height=H, channels=Cn) for i, (W, H, Cn) in enumerate(specs)]
+    frames = [frames_of(s, 6) for s in streams]
+    batched = [BackgroundSubtractorSuBSENSE(seed=200 + i) for i in range(len(specs))]
+    alone = [BackgroundSubtractorSuBSENSE(seed=200 + i) for i in range(len(specs))]
+    for b, a, f in zip(batched, alone, frames):
+        b.initialize(f[0])
+        a.initialize(f[0])
+    for t in range(1, 6):
+        masks = batch_apply(batched, [f[t] for f in frames])
+        for i in range(len(specs)):
+            assert np.array_equal(masks[i], alone[i].apply(frames[i][t])), "stream %d frame %d" % (i, t)
+    for b, a in zip(batched, alone):
+        for name in ("R", "T", "V", "DMIN_LT", "UNSTABLE", "LAST_FG", "SAMPLE_COLOR", "SAMPLE_DESC"):
+            assert np.array_equal(b.state_map(name), a.state_map(name)), name
