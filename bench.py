@@ -300,6 +300,8 @@ def main():
     ap.add_argument("--streams", type=int, default=64, help="number of streams of the mix (profiling: fewer)")
     ap.add_argument("--first", type=int, default=0, help="index of the first stream of the mix (profiling)")
     ap.add_argument("--plain-steps", type=int, default=5)
+    ap.add_argument("--batch-groups", type=int, default=4,
+                    help="concurrent groups a large batch is split into (lvbgs_set_batch_groups, 1..4)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--pawcs-frames", type=int, default=300,
@@ -346,6 +348,10 @@ def main():
         dev_frames.append(buf)
     torch.cuda.synchronize()
     px_step = sum(s.cfg.width * s.cfg.height for s in synth)
+    # groups the library splits each tick into (lvbgs_batch_apply: >= 8 streams, >= 4 Mi px, >= 4 per group)
+    groups = min(args.batch_groups, n // 4) if n >= 8 and px_step >= (4 << 20) else 1
+    if lib.lvbgs_set_batch_groups(args.batch_groups) != 0:
+        raise SystemExit("--batch-groups must be 1..4")
     # a dedicated stream: the library launches on it and the CUDA events are recorded on it (a NULL
     # stream pointer would mean "the handle's own stream" to the C-ABI)
     stream = torch.cuda.Stream()
@@ -425,7 +431,7 @@ def main():
     p50 = tick_sorted[len(tick_sorted) // 2]
     p99 = tick_sorted[min(len(tick_sorted) - 1, int(round(0.99 * (len(tick_sorted) - 1))))]
     # per-kernel profile: a few more ticks run as one group (the timed ticks split large batches into
-    # two concurrent groups, whose kernels overlap), CUDA events around each kernel
+    # concurrent groups, whose kernels overlap), CUDA events around each kernel
     check(lib.lvbgs_set_batch_groups(1), None)
     check(lib.lvbgs_debug_set_timing(hs[0], 1, prof_steps), hs[0])
     pe = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
@@ -436,7 +442,7 @@ def main():
     check(lib.lvbgs_batch_wait(hs, n, sptr), hs[0])
     torch.cuda.synchronize()
     one_group_ms = pe[0].elapsed_time(pe[1]) / prof_steps
-    check(lib.lvbgs_set_batch_groups(2), None)
+    check(lib.lvbgs_set_batch_groups(args.batch_groups), None)
     prof = (C.c_double * 16)()
     nprof = lib.lvbgs_debug_tick_profile(hs[0], 1, prof, 16)
     kernel_ms = {KERNELS[i]: round(prof[i], 4) for i in range(nprof)}
@@ -532,8 +538,8 @@ def main():
             "vs_baseline": None, "dtype": "u8/f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "streams": n, "px_per_step": px_step,
                        "l2": "inputs and model state (GBs) exceed L2; no flush",
-                       "parallelism": "one batched frame step per tick: two concurrent groups of about half the pixels, "
-                                      "%d kernel launches each" % len(KERNELS)},
+                       "parallelism": "one batched frame step per tick: %d concurrent groups of about equal "
+                                      "pixels, %d kernel launches each" % (groups, len(KERNELS))},
             "frames_per_s": n * args.steps * world / (total_ms / 1e3),
             "p50_frame_ms": p50, "p99_frame_ms": p99,
             "plain": plain,
@@ -553,9 +559,9 @@ def main():
             "kernel_ms": kernel_ms,
             "profile": {"ms_per_step_one_group": one_group_ms,
                         "note": "kernel_ms and roofline come from %d ticks run as one group with per-kernel CUDA "
-                                "events; the timed ticks run large batches as two concurrent groups of about half "
-                                "the pixels (lvbgs_set_batch_groups)" % prof_steps},
-            "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": 2 * len(KERNELS) * args.steps,
+                                "events; the timed ticks run large batches as %d concurrent groups of about equal "
+                                "pixels (lvbgs_set_batch_groups)" % (prof_steps, groups)},
+            "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": groups * len(KERNELS) * args.steps,
             "serving": serve,
             "pawcs": pawcs,
             "single_stream": singles,

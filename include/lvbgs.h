@@ -92,11 +92,11 @@ lvbgs_status lvbgs_apply(lvbgs_handle h, const uint8_t* image, size_t stride, ui
  * (handles on the same device, all initialized). Results are identical to n separate
  * lvbgs_apply calls. Enqueued on cuda_stream; lvbgs_batch_wait() waits and reports device errors.
  * Host buffers referenced by `frames` must stay valid until the wait returns. */
-/* How lvbgs_batch_apply runs large batches (>= 8 streams and >= 4 Mi pixels): 2 (default) splits them
- * into two groups of about half the pixels each, run on the caller's stream and on a second stream
- * of the first handle (forked and joined with events), so that one group's latency-bound phases
- * overlap the other's work; 1 runs every batch as one group (one set of kernels, as the per-kernel
- * timing of lvbgs_debug_set_timing expects). Process-wide. */
+/* How lvbgs_batch_apply runs large batches (>= 8 streams and >= 4 Mi pixels): G in 2..4 (default 4)
+ * splits them into up to G groups of about equal pixels (at least 4 streams each), run on the
+ * caller's stream and on further streams of the first handle (forked and joined with events), so
+ * that one group's latency-bound phases overlap the others' work; 1 runs every batch as one group
+ * (one set of kernels, as the per-kernel timing of lvbgs_debug_set_timing expects). Process-wide. */
 lvbgs_status lvbgs_set_batch_groups(int groups);
 lvbgs_status lvbgs_batch_apply(const lvbgs_handle* handles, const lvbgs_frame* frames, int n, void* cuda_stream);
 lvbgs_status lvbgs_batch_wait(const lvbgs_handle* handles, int n, void* cuda_stream);

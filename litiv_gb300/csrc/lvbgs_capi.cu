@@ -159,8 +159,8 @@ struct lvbgs_ctx {
     uint8_t* d_frame = nullptr;
     uint8_t* d_mask = nullptr;
     cudaStream_t stream = nullptr;
-    cudaStream_t aux = nullptr;                          // second group of a split batch (lazily created)
-    cudaEvent_t evFork = nullptr, evJoin = nullptr;      // fork / join of the split batch's two streams
+    cudaStream_t aux[3] = {nullptr, nullptr, nullptr};   // streams of a split batch's further groups (lazily created)
+    cudaEvent_t evFork = nullptr, evJoin[3] = {nullptr, nullptr, nullptr};  // fork / joins of a split batch
     Workspace ws;       // single-stream launches
     Workspace batchWs;  // batched launches led by this handle
     // PAWCS (algo == LVBGS_ALGO_PAWCS): device descriptor, host mirrors and launch scratch
@@ -1018,12 +1018,14 @@ lvbgs_status lvbgs_destroy(lvbgs_handle h) {
     h->ws.release();
     h->batchWs.release();
     if (h->h_flags) cudaFreeHost(h->h_flags);
-    if (h->aux) {
-        cudaStreamSynchronize(h->aux);
-        cudaStreamDestroy(h->aux);
+    for (int g = 0; g < 3; ++g) {
+        if (h->aux[g]) {
+            cudaStreamSynchronize(h->aux[g]);
+            cudaStreamDestroy(h->aux[g]);
+        }
+        if (h->evJoin[g]) cudaEventDestroy(h->evJoin[g]);
     }
     if (h->evFork) cudaEventDestroy(h->evFork);
-    if (h->evJoin) cudaEventDestroy(h->evJoin);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return LVBGS_OK;
@@ -1204,36 +1206,35 @@ lvbgs_status download_masks(const lvbgs_handle* hs, const lvbgs_frame* frames, i
 }  // namespace
 
 namespace {
-std::atomic<int> g_batch_groups{2};
+std::atomic<int> g_batch_groups{4};
+constexpr int kMaxBatchGroups = 4;
 constexpr int kSplitMinStreams = 8;
 constexpr size_t kSplitMinPx = (size_t)4 << 20;
 
-// Large batches run as two groups of about half the pixels each (the largest streams first, each to
-// the lighter group; the order within a group is the batch's): one group's latency-bound phases (the
-// repair rounds, the hole-fill row walks) then overlap the other group's work. Returns false for a
-// single group.
-bool split_batch(const lvbgs_handle* hs, int n, std::vector<int>& ga, std::vector<int>& gb) {
-    if (g_batch_groups.load() < 2 || n < kSplitMinStreams) return false;
+// Large batches run as G groups of about equal pixels (the largest streams first, each to the lightest
+// group; the order within a group is the batch's): one group's latency-bound phases (the repair rounds,
+// the hole-fill row walks) then overlap the other groups' work. Returns the number of groups (1: no
+// split).
+int split_batch(const lvbgs_handle* hs, int n, std::vector<std::vector<int>>& groups) {
+    const int G = std::min(g_batch_groups.load(), n / (kSplitMinStreams / 2));
     size_t total = 0;
     for (int i = 0; i < n; ++i) total += hs[i]->npx;
-    if (total < kSplitMinPx) return false;
+    if (G < 2 || n < kSplitMinStreams || total < kSplitMinPx) return 1;
     std::vector<int> order(n);
     for (int i = 0; i < n; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hs[a]->npx > hs[b]->npx; });
-    std::vector<char> inB(n, 0);
-    size_t pa = 0, pb = 0;
+    std::vector<int> gof(n, 0);
+    std::vector<size_t> load(G, 0);
     for (int i : order) {
-        if (pb < pa) {
-            inB[i] = 1;
-            pb += hs[i]->npx;
-        } else {
-            pa += hs[i]->npx;
-        }
+        int g = 0;
+        for (int k = 1; k < G; ++k)
+            if (load[k] < load[g]) g = k;
+        gof[i] = g;
+        load[g] += hs[i]->npx;
     }
-    ga.clear();
-    gb.clear();
-    for (int i = 0; i < n; ++i) (inB[i] ? gb : ga).push_back(i);
-    return !ga.empty() && !gb.empty();
+    groups.assign(G, std::vector<int>());
+    for (int i = 0; i < n; ++i) groups[gof[i]].push_back(i);
+    return G;
 }
 
 lvbgs_status batch_group(const lvbgs_handle* hs, const lvbgs_frame* frames, int n, cudaStream_t st, int repairDiv) {
@@ -1249,7 +1250,7 @@ lvbgs_status batch_group(const lvbgs_handle* hs, const lvbgs_frame* frames, int 
 }  // namespace
 
 lvbgs_status lvbgs_set_batch_groups(int groups) {
-    if (groups != 1 && groups != 2) return fail(nullptr, LVBGS_BAD_ARG, "batch groups must be 1 or 2");
+    if (groups < 1 || groups > kMaxBatchGroups) return fail(nullptr, LVBGS_BAD_ARG, "batch groups must be 1..4");
     g_batch_groups = groups;
     return LVBGS_OK;
 }
@@ -1260,29 +1261,35 @@ lvbgs_status lvbgs_batch_apply(const lvbgs_handle* hs, const lvbgs_frame* frames
     lvbgs_handle lead = hs[0];
     cudaSetDevice(lead->device);
     cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : lead->stream;
-    std::vector<int> ga, gb;
-    if (!split_batch(hs, n, ga, gb)) return batch_group(hs, frames, n, st, 1);
-    // the second group runs on the lead's second stream, forked from and joined back into st; each
-    // group's cooperative repair grid takes half of the co-resident blocks so that both fit
-    if (!lead->aux) LV_CUDA(lead, cudaStreamCreateWithFlags(&lead->aux, cudaStreamNonBlocking), "stream creation");
+    std::vector<std::vector<int>> groups;
+    const int G = split_batch(hs, n, groups);
+    if (G == 1) return batch_group(hs, frames, n, st, 1);
+    // group 0 runs on st, the others on the lead's further streams, forked from and joined back into
+    // st; each group's cooperative repair grid takes 1/G of the co-resident blocks so that all fit
     if (!lead->evFork) LV_CUDA(lead, cudaEventCreateWithFlags(&lead->evFork, cudaEventDisableTiming), "event creation");
-    if (!lead->evJoin) LV_CUDA(lead, cudaEventCreateWithFlags(&lead->evJoin, cudaEventDisableTiming), "event creation");
-    std::vector<lvbgs_handle> ha, hb;
-    std::vector<lvbgs_frame> fa, fb;
-    for (int i : ga) {
-        ha.push_back(hs[i]);
-        fa.push_back(frames[i]);
-    }
-    for (int i : gb) {
-        hb.push_back(hs[i]);
-        fb.push_back(frames[i]);
+    for (int g = 0; g < G - 1; ++g) {
+        if (!lead->aux[g]) LV_CUDA(lead, cudaStreamCreateWithFlags(&lead->aux[g], cudaStreamNonBlocking), "stream creation");
+        if (!lead->evJoin[g])
+            LV_CUDA(lead, cudaEventCreateWithFlags(&lead->evJoin[g], cudaEventDisableTiming), "event creation");
     }
     LV_CUDA(lead, cudaEventRecord(lead->evFork, st), "fork");
-    LV_CUDA(lead, cudaStreamWaitEvent(lead->aux, lead->evFork, 0), "fork");
-    if ((s = batch_group(ha.data(), fa.data(), (int)ha.size(), st, 2)) != LVBGS_OK) return s;
-    if ((s = batch_group(hb.data(), fb.data(), (int)hb.size(), lead->aux, 2)) != LVBGS_OK) return s;
-    LV_CUDA(lead, cudaEventRecord(lead->evJoin, lead->aux), "join");
-    LV_CUDA(lead, cudaStreamWaitEvent(st, lead->evJoin, 0), "join");
+    for (int g = 0; g < G - 1; ++g) LV_CUDA(lead, cudaStreamWaitEvent(lead->aux[g], lead->evFork, 0), "fork");
+    std::vector<lvbgs_handle> hg;
+    std::vector<lvbgs_frame> fg;
+    for (int g = 0; g < G; ++g) {
+        hg.clear();
+        fg.clear();
+        for (int i : groups[g]) {
+            hg.push_back(hs[i]);
+            fg.push_back(frames[i]);
+        }
+        if ((s = batch_group(hg.data(), fg.data(), (int)hg.size(), g == 0 ? st : lead->aux[g - 1], G)) != LVBGS_OK)
+            return s;
+    }
+    for (int g = 0; g < G - 1; ++g) {
+        LV_CUDA(lead, cudaEventRecord(lead->evJoin[g], lead->aux[g]), "join");
+        LV_CUDA(lead, cudaStreamWaitEvent(st, lead->evJoin[g], 0), "join");
+    }
     return LVBGS_OK;
 }
 
@@ -1292,14 +1299,16 @@ lvbgs_status lvbgs_batch_wait(const lvbgs_handle* hs, int n, void* cuda_stream) 
     cudaSetDevice(lead->device);
     cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : lead->stream;
     LV_CUDA(lead, cudaStreamSynchronize(st), "batched frame step");
-    std::vector<int> ga, gb;
-    if (split_batch(hs, n, ga, gb)) {
+    std::vector<std::vector<int>> groups;
+    const int G = split_batch(hs, n, groups);
+    if (G == 1) return read_work_status(lead, lead->batchWs);
+    for (int g = 0; g < G; ++g) {
         // the status of each group's work area (the groups' leads)
-        lvbgs_status s = read_work_status(hs[ga[0]], hs[ga[0]]->batchWs);
+        const lvbgs_handle gl = hs[groups[g][0]];
+        lvbgs_status s = read_work_status(gl, gl->batchWs);
         if (s != LVBGS_OK) return s;
-        return read_work_status(hs[gb[0]], hs[gb[0]]->batchWs);
     }
-    return read_work_status(lead, lead->batchWs);
+    return LVBGS_OK;
 }
 
 // ---- batch contexts: a work area owned apart from the streams, with ticks kept in flight ----

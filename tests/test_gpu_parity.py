@@ -246,10 +246,22 @@ def test_set_roi_before_initialize_and_roi_reuse():
         gpu.setROI(np.zeros((72, 96), np.uint8))
 
 
-def test_split_batch_groups_equal_streams_alone():
-    # >= 8 streams and >= 4 Mi pixels: lvbgs_batch_apply runs the batch as two concurrent groups (two
-    # CUDA streams, half-device repair grids); every mask and model map must equal the stream alone
-    specs = [(1280, 720, 3)] * 4 + [(640, 480, 1)] * 4 + [(320, 240, 3)] * 2
+@pytest.mark.parametrize("groups", [2, 4])
+def test_split_batch_groups_equal_streams_alone(groups):
+    # >= 8 streams and >= 4 Mi pixels: lvbgs_batch_apply runs the batch as concurrent groups (one CUDA
+    # stream each, repair grids of 1/groups of the device); every mask and model map must equal the
+    # stream alone
+    from litiv_gb300 import _lib
+    lib = _lib.lib()
+    assert lib.lvbgs_set_batch_groups(groups) == 0
+    try:
+        _split_batch_case(groups)
+    finally:
+        lib.lvbgs_set_batch_groups(4)
+
+
+def _split_batch_case(groups):
+    specs = [(1280, 720, 3)] * 4 + [(640, 480, 1)] * (8 if groups > 2 else 4) + [(320, 240, 3)] * (4 if groups > 2 else 2)
     streams = [SyntheticStream(0, seed=71 + i, width=W, height=H, channels=Cn) for i, (W, H, Cn) in enumerate(specs)]
     frames = [frames_of(s, 6) for s in streams]
     batched = [BackgroundSubtractorSuBSENSE(seed=200 + i) for i in range(len(specs))]
