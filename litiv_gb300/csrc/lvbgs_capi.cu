@@ -74,6 +74,21 @@ extern "C" __global__ void pw_k_reset_T(PawcsDev S, int buf);
 extern "C" __global__ void pw_k_init(PawcsDev S);
 extern "C" __global__ void pw_k_init_last(PawcsDev S, const uint8_t* img);
 extern "C" __global__ void pw_k_background(PawcsDev S, int buf, uint8_t* outCol, uint16_t* outDesc);
+// PAWCS, three channels (pawcs3_kernels.cu)
+extern "C" __global__ void pw3_k_local(PwParams P);
+extern "C" __global__ void pw3_k_items(PwParams P);
+extern "C" __global__ void pw3_k_gscan(PwParams P);
+extern "C" __global__ void pw3_k_dirty(PwParams P);
+extern "C" __global__ void pw3_k_later(PwParams P);
+extern "C" __global__ void pw3_k_commit(PwParams P);
+extern "C" __global__ void pw3_k_ds(PwParams P);
+extern "C" __global__ void pw3_k_motion_bg(PwParams P, int buf);
+extern "C" __global__ void pw3_k_refresh_local(PawcsDev S, uint32_t t, int buf, int baseOcc, float decr, int force,
+                                               int onlyPending, int useDil);
+extern "C" __global__ void pw3_k_refresh_global(PawcsDev S, uint32_t t, int buf, int force, int onlyPending, int useDil);
+extern "C" __global__ void pw3_k_init(PawcsDev S);
+extern "C" __global__ void pw3_k_init_last(PawcsDev S, const uint8_t* img);
+extern "C" __global__ void pw3_k_background(PawcsDev S, int buf, uint8_t* outCol, uint16_t* outDesc);
 }  // namespace lvbgs
 
 using namespace lvbgs;
@@ -527,53 +542,57 @@ enum {
     PL_GMAP, PL_DSLT, PL_DSST, PL_DSROI,
     // scratch (not part of the model)
     PL_BITS, PL_HCOUNT, PL_LABEL, PL_INTENT, PL_DESCT, PL_REC, PL_OUT, PL_REPB, PL_REPA, PL_UFINAL, PL_UV,
-    PL_ITEMLIST, PL_CONTRIBLIST, PL_BLKCOUNTS, PL_CATINFO, PL_DSABS, PL_UPDLIST, PL_GITEM, PL_CONTRIB, PL_DSFRAME, PL_FRAME, PL_MASK, PL_ROWSUM, PL_WORK, PL_FLAGS, PL_PDEV, PL_SDEV, PL_COUNT
+    PL_ITEMLIST, PL_CONTRIBLIST, PL_BLKCOUNTS, PL_CATINFO, PL_DSABS, PL_UPDLIST, PL_GITEM, PL_CONTRIB, PL_DSFRAME, PL_FRAME, PL_MASK, PL_ROWSUM, PL_WORK, PL_FLAGS, PL_PDEV, PL_SDEV, PL_DIRTY, PL_COUNT
 };
 struct PwLayout {
     size_t off[PL_COUNT];
     size_t persist, total;
 };
-PwLayout pw_layout(int W, int H, int L, int G) {
+PwLayout pw_layout(int W, int H, int C, int L, int G) {
     const size_t npx = (size_t)W * H, gmap = (size_t)(W / 2) * (H / 2), nds = (size_t)(W / 8) * (H / 8);
     size_t sz[PL_COUNT];
     sz[PL_CTL] = sizeof(StreamCtl);
     sz[PL_PCTL] = sizeof(PawcsCtl);
     sz[PL_FM] = 2 * kNumFloatMaps * npx * 4;
-    sz[PL_WCOLOR] = 2 * (size_t)L * npx;
-    sz[PL_WDESC] = 2 * (size_t)L * npx * 2;
+    // word colours / descriptors: [2][L][npx] one channel, [2][L][npx][3] three (channel-minor)
+    sz[PL_WCOLOR] = 2 * (size_t)L * npx * C;
+    sz[PL_WDESC] = 2 * (size_t)L * npx * 2 * C;
     sz[PL_WOCC] = sz[PL_WFIRST] = sz[PL_WLAST] = 2 * (size_t)L * npx * 4;
     sz[PL_ILLUM] = sz[PL_UNST] = sz[PL_ROI] = sz[PL_BLINKS] = sz[PL_LASTRAWFG] = sz[PL_LASTFG] = sz[PL_DILINV] =
-        sz[PL_LASTRAWBLINK] = sz[PL_LASTCOL] = npx;
-    sz[PL_LASTDESC] = sz[PL_KCTR] = npx * 2;
-    sz[PL_GLUT] = npx * 16;
+        sz[PL_LASTRAWBLINK] = npx;
+    sz[PL_LASTCOL] = npx * C;
+    sz[PL_LASTDESC] = npx * 2 * C;
+    sz[PL_KCTR] = npx * 2;
+    sz[PL_GLUT] = npx * kPwGlutStride;
     sz[PL_GMAP] = (size_t)G * std::max<size_t>(gmap, 1) * 4;
-    sz[PL_DSLT] = sz[PL_DSST] = std::max<size_t>(nds, 1) * 4;
+    sz[PL_DSLT] = sz[PL_DSST] = std::max<size_t>(nds, 1) * 4 * C;
     sz[PL_DSROI] = std::max<size_t>(nds, 1);
     sz[PL_BITS] = bit_planes_bytes(W, H);
     sz[PL_HCOUNT] = npx;
     sz[PL_LABEL] = sz[PL_INTENT] = npx * 4;
-    sz[PL_DESCT] = npx * 2;
+    sz[PL_DESCT] = npx * 2 * C;
     sz[PL_REC] = npx * sizeof(PwRec);
     sz[PL_OUT] = npx * sizeof(PwOut);
     sz[PL_REPB] = sz[PL_REPA] = npx * 4;
     sz[PL_UFINAL] = npx;
     sz[PL_UV] = npx;
-    sz[PL_ITEMLIST] = npx * 16;
+    sz[PL_ITEMLIST] = npx * 16 * (C == 3 ? 2 : 1);
     sz[PL_CONTRIBLIST] = npx * 4;
     sz[PL_BLKCOUNTS] = ((npx + kPwCompactBlk - 1) / kPwCompactBlk) * kPwCats * 4;
-    sz[PL_CATINFO] = 64 * 4;
+    sz[PL_CATINFO] = 2 * kPwCatBase * 4;
     sz[PL_DSABS] = std::max<size_t>(nds, 1) * 4;
     sz[PL_UPDLIST] = npx * 4;
     sz[PL_GITEM] = npx * 4;
     sz[PL_CONTRIB] = npx * 4;
-    sz[PL_DSFRAME] = std::max<size_t>(nds, 1);
-    sz[PL_FRAME] = npx;
+    sz[PL_DSFRAME] = std::max<size_t>(nds, 1) * C;
+    sz[PL_FRAME] = npx * C;
     sz[PL_MASK] = npx;
     sz[PL_ROWSUM] = (size_t)kPwMaxGlobal * std::max<size_t>(gmap, 1) * 8;
     sz[PL_WORK] = sizeof(TickWork);
     sz[PL_FLAGS] = 64;
     sz[PL_PDEV] = sizeof(PawcsDev);
     sz[PL_SDEV] = sizeof(StreamDev);
+    sz[PL_DIRTY] = npx;
     PwLayout Lo;
     size_t o = 0;
     for (int i = 0; i < PL_COUNT; ++i) {
@@ -677,6 +696,7 @@ void pw_fill(lvbgs_ctx* h, const PwLayout& Lo, int L, int G) {
     D.contrib = (float*)(b + Lo.off[PL_CONTRIB]);
     D.dsRoi = b + Lo.off[PL_DSROI];
     D.dsFrame = b + Lo.off[PL_DSFRAME];
+    D.dirty = b + Lo.off[PL_DIRTY];
     h->d_rowsum = (double*)(b + Lo.off[PL_ROWSUM]);
     h->d_work = (TickWork*)(b + Lo.off[PL_WORK]);
     h->d_flags = (unsigned int*)(b + Lo.off[PL_FLAGS]);
@@ -708,8 +728,13 @@ lvbgs_status pw_upload_desc(lvbgs_ctx* h, cudaStream_t st) {
 lvbgs_status pw_refresh(lvbgs_ctx* h, uint32_t t, int buf, int baseOcc, float decr, int force, int onlyPending,
                         int useDil, cudaStream_t st) {
     const int npx = (int)h->npx;
-    pw_k_refresh_local<<<(npx + 127) / 128, 128, 0, st>>>(h->pd, t, buf, baseOcc, decr, force, onlyPending, useDil);
-    pw_k_refresh_global<<<1, 1, 0, st>>>(h->pd, t, buf, force, onlyPending, useDil);
+    if (h->C == 3) {
+        pw3_k_refresh_local<<<(npx + 127) / 128, 128, 0, st>>>(h->pd, t, buf, baseOcc, decr, force, onlyPending, useDil);
+        pw3_k_refresh_global<<<1, 1, 0, st>>>(h->pd, t, buf, force, onlyPending, useDil);
+    } else {
+        pw_k_refresh_local<<<(npx + 127) / 128, 128, 0, st>>>(h->pd, t, buf, baseOcc, decr, force, onlyPending, useDil);
+        pw_k_refresh_global<<<1, 1, 0, st>>>(h->pd, t, buf, force, onlyPending, useDil);
+    }
     PwParams P = pw_params(h, 0.0);
     pw_k_lut_sort<<<h->sd.nTiles, kThreads, 0, st>>>(P, onlyPending ? 2 : 1);
     LV_CUDA(h, cudaGetLastError(), "refresh kernel launch");
@@ -718,10 +743,11 @@ lvbgs_status pw_refresh(lvbgs_ctx* h, uint32_t t, int buf, int baseOcc, float de
 
 lvbgs_status pw_initialize(lvbgs_ctx* h, const uint8_t* img, int W, int H, int C, size_t stride,
                            const std::vector<uint8_t>& newroi, size_t orig, size_t fin) {
-    if (C != 1) return fail(h, LVBGS_UNSUPPORTED, "PAWCS runs on single-channel frames in this implementation");
+    if (C != 1 && C != 3) return fail(h, LVBGS_UNSUPPORTED, "PAWCS runs on single- and three-channel frames");
     const size_t npx = (size_t)W * H;
     const PwGeom g = pw_geometry(h->prm, npx, orig, C);
-    if (g.L > kPwMaxLocal || g.G > kPwMaxGlobal) return fail(h, LVBGS_UNSUPPORTED, "word counts above the supported maximum");
+    if (g.L > (C == 3 ? kPw3MaxLocal : kPwMaxLocal) || g.G > kPwMaxGlobal)
+        return fail(h, LVBGS_UNSUPPORTED, "word counts above the supported maximum");
     if (g.median_k > 13) return fail(h, LVBGS_UNSUPPORTED, "median kernel sizes above 13 are not supported");
     const int dsW = W / 8, dsH = H / 8;
     if (dsW <= 0 || dsH <= 0 || W % dsW != 0 || H % dsH != 0)
@@ -746,8 +772,10 @@ lvbgs_status pw_initialize(lvbgs_ctx* h, const uint8_t* img, int W, int H, int C
     ctl.auto_reset = 1;  // IIBackgroundSubtractor's default (BackgroundSubtractionUtils.cpp:67)
     ctl.median_k = g.median_k;
     const float rel = h->prm.rel_lbsp_threshold;
+    // BackgroundSubtractorLBSP.cpp:30-34: one channel divides the threshold by 3
     for (int t = 0; t <= 255; ++t)
-        ctl.lut[t] = sat_round_u8(((float)t * rel + (float)h->prm.lbsp_threshold_offset) / 3);
+        ctl.lut[t] = C == 1 ? sat_round_u8(((float)t * rel + (float)h->prm.lbsp_threshold_offset) / 3)
+                            : sat_round_u8((float)t * rel + (float)h->prm.lbsp_threshold_offset);
     ctl.n_rel = fin;
     ctl.orig_roi = orig;
     {
@@ -770,7 +798,7 @@ lvbgs_status pw_initialize(lvbgs_ctx* h, const uint8_t* img, int W, int H, int C
     h->dmem = nullptr;
     h->initialized = false;
     h->spilled = false;
-    const PwLayout Lo = pw_layout(W, H, g.L, g.G);
+    const PwLayout Lo = pw_layout(W, H, C, g.L, g.G);
     LV_CUDA(h, cudaMalloc(&h->dmem, Lo.total), "model allocation");
     if (!h->h_flags) LV_CUDA(h, cudaHostAlloc((void**)&h->h_flags, 64, cudaHostAllocDefault), "pinned allocation");
     h->persistBytes = Lo.persist;
@@ -797,8 +825,13 @@ lvbgs_status pw_initialize(lvbgs_ctx* h, const uint8_t* img, int W, int H, int C
     lvbgs_status s = stage_frame(h, img, stride, st, &dimg);
     if (s != LVBGS_OK) return s;
     if ((s = pw_upload_desc(h, st)) != LVBGS_OK) return s;
-    pw_k_init<<<1024, 256, 0, st>>>(h->pd);
-    pw_k_init_last<<<1024, 256, 0, st>>>(h->pd, dimg);
+    if (C == 3) {
+        pw3_k_init<<<1024, 256, 0, st>>>(h->pd);
+        pw3_k_init_last<<<1024, 256, 0, st>>>(h->pd, dimg);
+    } else {
+        pw_k_init<<<1024, 256, 0, st>>>(h->pd);
+        pw_k_init_last<<<1024, 256, 0, st>>>(h->pd, dimg);
+    }
     LV_CUDA(h, cudaGetLastError(), "init kernel launch");
     // refreshModel(1, 0) at frame 0 (:555)
     if ((s = pw_refresh(h, 0u, 0, 1, 0.0f, 0, 0, 0, st)) != LVBGS_OK) return s;
@@ -827,32 +860,51 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
     // ordered compaction: mode 0 lists the critical global items, mode 1 the word weight contributions
     auto compact = [&](int mode) {
         pw_k_compact_count<<<cblocks, 256, 0, st>>>(P, mode);
-        pw_k_compact_offsets<<<1, 32 * kPwCats, 0, st>>>(P);
+        pw_k_compact_offsets<<<1, 1024, 0, st>>>(P);
         pw_k_compact_scatter<<<cblocks, 256, 0, st>>>(P, mode);
     };
+    const bool c3 = h->C == 3;
     int round = 0;
     for (;; ++round) {
         if (round >= 64) return fail(h, LVBGS_DEVICE_ERROR, "PAWCS raster-order fixed point did not converge in 64 rounds");
         P.round = round;
-        pw_k_local<<<tiles, blk, 0, st>>>(P);
-        pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
-        pw_k_items<<<tiles, blk, 0, st>>>(P);
-        compact(0);
-        pw_k_gscan<<<1, 32, 0, st>>>(P);
-        pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
-        pw_k_nbr<<<tiles, blk, 0, st>>>(P);
-        compact(2);
-        pw_k_nbr_loops<<<std::max(1, std::min(cblocks * 4, 1216)), 256, 0, st>>>(P);
-        pw_k_replace<<<tiles, blk, 0, st>>>(P);
-        LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 4, st), "flag reset");
-        pw_k_dirty<<<tiles, blk, 0, st>>>(P);
+        if (c3) {
+            // three channels: the local pass applies the earlier updaters' loops itself
+            pw3_k_local<<<tiles, blk, 0, st>>>(P);
+            pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
+            pw3_k_items<<<tiles, blk, 0, st>>>(P);
+            compact(0);
+            pw3_k_gscan<<<1, 32, 0, st>>>(P);
+            pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
+            pw_k_nbr<<<tiles, blk, 0, st>>>(P);
+            LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 4, st), "flag reset");
+            pw3_k_dirty<<<tiles, blk, 0, st>>>(P);
+        } else {
+            pw_k_local<<<tiles, blk, 0, st>>>(P);
+            pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
+            pw_k_items<<<tiles, blk, 0, st>>>(P);
+            compact(0);
+            pw_k_gscan<<<1, 32, 0, st>>>(P);
+            pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
+            pw_k_nbr<<<tiles, blk, 0, st>>>(P);
+            compact(2);
+            pw_k_nbr_loops<<<std::max(1, std::min(cblocks * 4, 1216)), 256, 0, st>>>(P);
+            pw_k_replace<<<tiles, blk, 0, st>>>(P);
+            LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 4, st), "flag reset");
+            pw_k_dirty<<<tiles, blk, 0, st>>>(P);
+        }
         LV_CUDA(h, cudaGetLastError(), "PAWCS round launch");
         LV_CUDA(h, cudaMemcpyAsync(h->h_flags, h->d_flags, 4, cudaMemcpyDeviceToHost, st), "flag read-back");
         LV_CUDA(h, cudaStreamSynchronize(st), "PAWCS round");
         if (h->h_flags[0] == 0) break;
     }
     h->pw_rounds_last = round + 1;
-    pw_k_commit<<<tiles, blk, 0, st>>>(P);
+    if (c3) {
+        pw3_k_later<<<tiles, blk, 0, st>>>(P);
+        pw3_k_commit<<<tiles, blk, 0, st>>>(P);
+    } else {
+        pw_k_commit<<<tiles, blk, 0, st>>>(P);
+    }
     pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 1);
     compact(1);
     pw_k_weights<<<kPwMaxGlobal, 256, 0, st>>>(P);
@@ -880,13 +932,17 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
     lvbgs_k_median<<<dim3(TP.colBlocks, TP.totalSegs), blk, 0, st>>>(TP);
     lvbgs_k_dilate<<<h->H, 128, 0, st>>>(TP);
     const int nds = (h->W / 8) * (h->H / 8);
-    if (nds > 0) pw_k_ds<<<(nds + 255) / 256, 256, 0, st>>>(P);
+    if (nds > 0) {
+        if (c3) pw3_k_ds<<<(nds + 255) / 256, 256, 0, st>>>(P);
+        else pw_k_ds<<<(nds + 255) / 256, 256, 0, st>>>(P);
+    }
     pw_k_epilogue<<<1, 256, 0, st>>>(P);
     const uint32_t t = (uint32_t)(h->pw_frames + 1);
     if (nds > 0 && t % kPwBootWin == 0) {
         // camera-motion comparison (:1480-1501): the host waits for the decision, which may switch the
         // local word weight offset and run refreshModel(1, 1, true)
-        pw_k_motion_bg<<<(nds + 255) / 256, 256, 0, st>>>(P, nxt);
+        if (c3) pw3_k_motion_bg<<<(nds + 255) / 256, 256, 0, st>>>(P, nxt);
+        else pw_k_motion_bg<<<(nds + 255) / 256, 256, 0, st>>>(P, nxt);
         pw_k_motion_decide<<<1, 32, 0, st>>>(P);
         LV_CUDA(h, cudaGetLastError(), "PAWCS camera-motion launch");
         LV_CUDA(h, cudaMemcpyAsync(h->h_flags + 1, h->d_flags + 1, 8, cudaMemcpyDeviceToHost, st), "flag read-back");
@@ -1461,9 +1517,10 @@ lvbgs_status lvbgs_get_background(lvbgs_handle h, uint8_t* out) {
     if (h->algo == LVBGS_ALGO_PAWCS) {
         const bool dev = is_device_ptr(out);
         uint8_t* d = dev ? out : h->d_frame;
-        pw_k_background<<<512, 256, 0, h->stream>>>(h->pd, (int)(h->pw_frames & 1ull), d, nullptr);
+        if (h->C == 3) pw3_k_background<<<512, 256, 0, h->stream>>>(h->pd, (int)(h->pw_frames & 1ull), d, nullptr);
+        else pw_k_background<<<512, 256, 0, h->stream>>>(h->pd, (int)(h->pw_frames & 1ull), d, nullptr);
         LV_CUDA(h, cudaGetLastError(), "background kernel");
-        if (!dev) LV_CUDA(h, cudaMemcpyAsync(out, d, h->npx, cudaMemcpyDeviceToHost, h->stream), "download");
+        if (!dev) LV_CUDA(h, cudaMemcpyAsync(out, d, h->npx * h->C, cudaMemcpyDeviceToHost, h->stream), "download");
         LV_CUDA(h, cudaStreamSynchronize(h->stream), "background image");
         return LVBGS_OK;
     }
@@ -1482,7 +1539,10 @@ lvbgs_status lvbgs_get_background_descriptors(lvbgs_handle h, uint16_t* out) {
     if (!out) return fail(h, LVBGS_BAD_ARG, "null output");
     uint16_t* d = nullptr;
     LV_CUDA(h, cudaMallocAsync((void**)&d, h->npx * h->C * 2, h->stream), "temporary allocation");
-    if (h->algo == LVBGS_ALGO_PAWCS) pw_k_background<<<512, 256, 0, h->stream>>>(h->pd, (int)(h->pw_frames & 1ull), nullptr, d);
+    if (h->algo == LVBGS_ALGO_PAWCS && h->C == 3)
+        pw3_k_background<<<512, 256, 0, h->stream>>>(h->pd, (int)(h->pw_frames & 1ull), nullptr, d);
+    else if (h->algo == LVBGS_ALGO_PAWCS)
+        pw_k_background<<<512, 256, 0, h->stream>>>(h->pd, (int)(h->pw_frames & 1ull), nullptr, d);
     else lvbgs_background<<<512, 256, 0, h->stream>>>(h->sd, nullptr, d);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, h->npx * h->C * 2, cudaMemcpyDefault, h->stream);
@@ -1573,24 +1633,24 @@ lvbgs_status lvbgs_get_size(lvbgs_handle h, int* w, int* hh, int* c) {
 }
 
 size_t lvbgs_state_bytes(lvbgs_algo algo, int W, int H, int C, size_t N) {
-    if (algo == LVBGS_ALGO_PAWCS && W > 0 && H > 0 && C == 1) {
+    if (algo == LVBGS_ALGO_PAWCS && W > 0 && H > 0 && (C == 1 || C == 3)) {
         lvbgs_params prm;
         lvbgs_default_params(LVBGS_ALGO_PAWCS, &prm);
         if (N) prm.bg_samples = N;
-        const PwGeom g = pw_geometry(prm, (size_t)W * H, (size_t)W * H, 1);
-        return pw_layout(W, H, g.L, g.G).persist;
+        const PwGeom g = pw_geometry(prm, (size_t)W * H, (size_t)W * H, C);
+        return pw_layout(W, H, C, g.L, g.G).persist;
     }
     if (algo != LVBGS_ALGO_SUBSENSE || W <= 0 || H <= 0 || (C != 1 && C != 3)) return 0;
     return make_layout(W, H, C, N ? N : 50).persist;
 }
 
 size_t lvbgs_device_bytes(lvbgs_algo algo, int W, int H, int C, size_t N) {
-    if (algo == LVBGS_ALGO_PAWCS && W > 0 && H > 0 && C == 1) {
+    if (algo == LVBGS_ALGO_PAWCS && W > 0 && H > 0 && (C == 1 || C == 3)) {
         lvbgs_params prm;
         lvbgs_default_params(LVBGS_ALGO_PAWCS, &prm);
         if (N) prm.bg_samples = N;
-        const PwGeom g = pw_geometry(prm, (size_t)W * H, (size_t)W * H, 1);
-        return pw_layout(W, H, g.L, g.G).total;
+        const PwGeom g = pw_geometry(prm, (size_t)W * H, (size_t)W * H, C);
+        return pw_layout(W, H, C, g.L, g.G).total;
     }
     if (algo != LVBGS_ALGO_SUBSENSE || W <= 0 || H <= 0 || (C != 1 && C != 3)) return 0;
     // model and scratch block, plus the handle's own workspace (status, one descriptor table,
@@ -1871,12 +1931,13 @@ size_t lvbgs_pawcs_debug_export_bytes(lvbgs_handle h, int which) {
     case LVBGS_PAWCS_MAP_FIN_LT: case LVBGS_PAWCS_MAP_FIN_ST: return npx * 4;
     case LVBGS_PAWCS_MAP_ILLUM: case LVBGS_PAWCS_MAP_UNSTABLE: case LVBGS_PAWCS_MAP_BLINKS:
     case LVBGS_PAWCS_MAP_LAST_RAW_FG: case LVBGS_PAWCS_MAP_LAST_FG: case LVBGS_PAWCS_MAP_LAST_FG_DIL:
-    case LVBGS_PAWCS_MAP_LAST_RAW_BLINK: case LVBGS_PAWCS_MAP_ROI: case LVBGS_PAWCS_MAP_LAST_COLOR: return npx;
-    case LVBGS_PAWCS_MAP_LAST_DESC: return npx * 2;
-    case LVBGS_PAWCS_MAP_DS_LT: case LVBGS_PAWCS_MAP_DS_ST: return nds * 4;
+    case LVBGS_PAWCS_MAP_LAST_RAW_BLINK: case LVBGS_PAWCS_MAP_ROI: return npx;
+    case LVBGS_PAWCS_MAP_LAST_COLOR: return npx * h->C;
+    case LVBGS_PAWCS_MAP_LAST_DESC: return npx * 2 * h->C;
+    case LVBGS_PAWCS_MAP_DS_LT: case LVBGS_PAWCS_MAP_DS_ST: return nds * 4 * h->C;
     case LVBGS_PAWCS_MAP_LUT: return 256;
-    case LVBGS_PAWCS_MAP_LW_COLOR: return nw;
-    case LVBGS_PAWCS_MAP_LW_DESC: return nw * 2;
+    case LVBGS_PAWCS_MAP_LW_COLOR: return nw * h->C;
+    case LVBGS_PAWCS_MAP_LW_DESC: return nw * 2 * h->C;
     case LVBGS_PAWCS_MAP_LW_OCC: case LVBGS_PAWCS_MAP_LW_FIRST: case LVBGS_PAWCS_MAP_LW_LAST: return nw * 8;
     case LVBGS_PAWCS_MAP_GW: return (size_t)h->pd.G * 20;
     case LVBGS_PAWCS_MAP_GW_MAP: return (size_t)h->pd.G * gmap * 4;
@@ -1928,10 +1989,10 @@ lvbgs_status lvbgs_pawcs_debug_export(lvbgs_handle h, int which, void* out, size
         }
         case LVBGS_PAWCS_MAP_LAST_RAW_BLINK: e = dl(out, h->sd.lastRawBlink, npx); break;
         case LVBGS_PAWCS_MAP_ROI: e = dl(out, h->sd.roi, npx); break;
-        case LVBGS_PAWCS_MAP_LAST_COLOR: e = dl(out, h->sd.lastCol, npx); break;
-        case LVBGS_PAWCS_MAP_LAST_DESC: e = dl(out, h->sd.lastDesc, npx * 2); break;
-        case LVBGS_PAWCS_MAP_DS_LT: e = dl(out, h->sd.dsLT, nds * 4); break;
-        case LVBGS_PAWCS_MAP_DS_ST: e = dl(out, h->sd.dsST, nds * 4); break;
+        case LVBGS_PAWCS_MAP_LAST_COLOR: e = dl(out, h->sd.lastCol, npx * h->C); break;
+        case LVBGS_PAWCS_MAP_LAST_DESC: e = dl(out, h->sd.lastDesc, npx * 2 * h->C); break;
+        case LVBGS_PAWCS_MAP_DS_LT: e = dl(out, h->sd.dsLT, nds * 4 * h->C); break;
+        case LVBGS_PAWCS_MAP_DS_ST: e = dl(out, h->sd.dsST, nds * 4 * h->C); break;
         case LVBGS_PAWCS_MAP_LUT: {
             StreamCtl c;
             e = dl(&c, h->sd.ctl, sizeof(c));
@@ -1940,11 +2001,11 @@ lvbgs_status lvbgs_pawcs_debug_export(lvbgs_handle h, int which, void* out, size
         }
         case LVBGS_PAWCS_MAP_GW_MAP: e = dl(out, h->pd.gmap, G * gmap * 4); break;
         case LVBGS_PAWCS_MAP_GLUT: {
-            std::vector<uint8_t> g(npx * 16);
-            e = dl(g.data(), h->pd.glut, npx * 16);
+            std::vector<uint8_t> g(npx * kPwGlutStride);
+            e = dl(g.data(), h->pd.glut, npx * kPwGlutStride);
             uint8_t* o = (uint8_t*)out;
             for (size_t i = 0; i < npx; ++i)
-                for (size_t k = 0; k < G; ++k) o[i * G + k] = h->roi[i] ? g[i * 16 + k] : 0;
+                for (size_t k = 0; k < G; ++k) o[i * G + k] = h->roi[i] ? g[i * kPwGlutStride + k] : 0;
             break;
         }
         case LVBGS_PAWCS_MAP_GW: {
@@ -1954,9 +2015,11 @@ lvbgs_status lvbgs_pawcs_debug_export(lvbgs_handle h, int which, void* out, size
             std::memset(b, 0, G * 20);
             for (size_t w = 0; w < G; ++w) {
                 uint8_t* r = b + w * 20;
-                r[0] = (uint8_t)pc.gw_color[w];
-                const uint16_t d = (uint16_t)pc.gw_desc[w];
-                std::memcpy(r + 4, &d, 2);
+                const uint16_t d[3] = {(uint16_t)pc.gw_desc[w], (uint16_t)(pc.gw_desc[w] >> 16), (uint16_t)pc.gw_desc2[w]};
+                for (int c = 0; c < h->C; ++c) {
+                    r[c] = (uint8_t)(pc.gw_color[w] >> (8 * c));
+                    std::memcpy(r + 4 + 2 * c, &d[c], 2);
+                }
                 r[10] = (uint8_t)pc.gw_bits[w];
                 std::memcpy(r + 12, &pc.gw_weight[w], 4);
                 int32_t slot = -1;
@@ -1969,7 +2032,9 @@ lvbgs_status lvbgs_pawcs_debug_export(lvbgs_handle h, int which, void* out, size
         case LVBGS_PAWCS_MAP_LW_COLOR: case LVBGS_PAWCS_MAP_LW_DESC: case LVBGS_PAWCS_MAP_LW_OCC:
         case LVBGS_PAWCS_MAP_LW_FIRST: case LVBGS_PAWCS_MAP_LW_LAST: {
             // model-major (ROI pixels in raster order), slot-minor, as the reference's dictionary
-            const size_t es = which == LVBGS_PAWCS_MAP_LW_COLOR ? 1 : which == LVBGS_PAWCS_MAP_LW_DESC ? 2 : 4;
+            const size_t es = which == LVBGS_PAWCS_MAP_LW_COLOR  ? (size_t)h->C
+                              : which == LVBGS_PAWCS_MAP_LW_DESC ? 2 * (size_t)h->C
+                                                                 : 4;
             const void* src = which == LVBGS_PAWCS_MAP_LW_COLOR  ? (const void*)h->pd.wColor
                               : which == LVBGS_PAWCS_MAP_LW_DESC ? (const void*)h->pd.wDesc
                               : which == LVBGS_PAWCS_MAP_LW_OCC  ? (const void*)h->pd.wOcc

@@ -1,4 +1,4 @@
-// Device-side state of the PAWCS path (BackgroundSubtractorPAWCS, one channel).
+// Device-side state of the PAWCS path (BackgroundSubtractorPAWCS, one and three channels).
 //
 // Exactness scheme. The reference scans pixels in raster order; a pixel reads state that earlier
 // pixels of the same frame wrote in five ways, and each is resolved explicitly:
@@ -15,13 +15,20 @@
 //      pixel over its (at most 24) updaters in raster order;
 //  (5) draw indices: every rand() of the reference is draw k of (seed, frame, pixel), and each
 //      stage knows how many draws precede it.
+// Three channels: the neighbour update edits the target's words themselves (last frame,
+// occurrences, descriptor, colour), so (1) becomes "the frame-start dictionary after the loops of
+// every earlier updater, applied in raster order by the target's own local pass", a pixel is rerun
+// when an earlier updater's loop inputs (target, loop draw start, weight threshold) changed, and the
+// loops of later updaters run once the fixed point is reached (pawcs3_kernels.cu).
 #pragma once
 #include "lvbgs_internal.h"
 
 namespace lvbgs {
 
 constexpr int kPwMaxLocal = 25;   // local words of a one-channel stream (50/2)
-constexpr int kPwMaxGlobal = 16;  // global words supported (12 at the default 50 words)
+constexpr int kPw3MaxLocal = 50;  // local words of a three-channel stream (50)
+constexpr int kPwMaxGlobal = 32;  // global words supported (12 / 25 at the default 50 words)
+constexpr int kPwGlutStride = 32; // bytes per pixel of the global sort tables
 constexpr uint32_t kPwNone = 0xffffffffu;
 
 // frame-level state specific to PAWCS (the common part lives in StreamCtl)
@@ -34,13 +41,14 @@ struct PawcsCtl {
     unsigned long long ds_roi_count;     // m_nDownSampledROIPxCount
     // global words by pool identity
     unsigned int gw_color[kPwMaxGlobal];
-    unsigned int gw_desc[kPwMaxGlobal];
+    unsigned int gw_desc[kPwMaxGlobal];   // channels 0 and 1 (16 bits each)
+    unsigned int gw_desc2[kPwMaxGlobal];  // channel 2 (three channels)
     unsigned int gw_bits[kPwMaxGlobal];
     float gw_weight[kPwMaxGlobal];
     int gdict[kPwMaxGlobal];             // dictionary slot -> pool word
     int gnext;                           // next unused pool word (initialization)
     // global scan results of the frame in flight
-    unsigned int wr_color, wr_desc, wr_bits;  // replaceable word's features after the frame's items
+    unsigned int wr_color, wr_desc, wr_desc2, wr_bits;  // replaceable word's features after the frame's items
     unsigned int n_repl;                      // replacements of the replaceable word this frame
     unsigned int n_rounds, n_dirty;           // fixed-point rounds of the frame, dirty pixels left
     unsigned long long st_words, st_events, st_nb;
@@ -56,10 +64,11 @@ struct PwRec {
     float thrW;               // fLocalWordsWeightSumThreshold
     unsigned long long rate;  // nCurrLocalWordUpdateRate (size_t; SIZE_MAX for an infinite override)
     uint32_t m0, m1;          // final slots illumination-updated when the mask is zero / non-zero
+    uint32_t m0hi, m1hi;      // the same for slots 32..63 (three channels)
     uint32_t rsrc;            // replacement source of the own last slot used by the local pass
     uint16_t kScan;           // draw counter after the word scan
     uint16_t incr;            // nCurrWordOccIncr
-    uint8_t minColor, minDesc;
+    uint16_t minColor, minDesc;
     uint8_t flags;            // kRf*
     uint8_t bits;             // popcount of the current descriptor
 };
@@ -76,7 +85,9 @@ struct PwOut {
     uint8_t gflags;      // bit0 replaced the replaceable word, bit1 contributed to the word weight, bit2 critical
     uint16_t kEnd;       // draw counter after the neighbour loop
     uint8_t rflags;      // neighbour loop: bit0 replaces the target's last word, bit1 reached the last word
-    uint8_t pad;
+    uint8_t chg;         // three channels: the loop inputs (target, kLoop, thrW) changed this round
+    float thrW;          // weight threshold of the loop (snapshot of the round's local pass)
+    uint32_t qPrev;      // target of the previous round
 };
 
 struct PawcsDev {
@@ -112,10 +123,12 @@ struct PawcsDev {
     uint32_t* catInfo;         // [0..16] category totals, [32..48] category bases
     float* dsAbs;              // |LT - ST| per down-sampled pixel (0 outside the down-sampled ROI)
     uint32_t* updList;         // pixels that update a neighbour this round, raster order
+    uint8_t* dirty;            // three channels: pixels whose local pass reruns next round
 };
 
 constexpr int kPwCompactBlk = 1024;  // pixels per block of the ordered compactions
-constexpr int kPwCats = 17;          // compaction categories: 16 global words, or the critical items
+constexpr int kPwCats = kPwMaxGlobal + 1;  // compaction categories: the global words, or the critical items
+constexpr int kPwCatBase = 64;       // catInfo: [0, kPwCats) category totals, [kPwCatBase, +kPwCats) bases
 constexpr int kPwBootWin = 500;      // BGSPAWCS bootstrap window (frames)
 
 // launch parameters of the PAWCS kernels (a table of streams in device memory)

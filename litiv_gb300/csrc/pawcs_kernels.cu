@@ -8,99 +8,9 @@
 #include <float.h>
 #include <stdint.h>
 
-#include "pawcs_internal.h"
+#include "pawcs_device.cuh"
 
 namespace lvbgs {
-
-// LBSP double-cross taps (LBSP.hpp:297-298), sampling tables (opencv.hpp:915-964)
-__constant__ int pw_dx[16] = {-2, 2, 0, 0, -2, 2, 2, -2, 0, -1, 0, 1, -1, 1, 1, -1};
-__constant__ int pw_dy[16] = {0, 0, -2, 2, 2, -2, 2, -2, 1, 0, -1, 0, -1, 1, -1, 1};
-__constant__ int pw_pat7[49] = {2, 4, 6, 7, 6, 4, 2, 4, 8, 12, 14, 12, 8, 4, 6, 12, 21, 25, 21, 12, 6, 7, 14, 25, 28,
-                                25, 14, 7, 6, 12, 21, 25, 21, 12, 6, 4, 8, 12, 14, 12, 8, 4, 2, 4, 6, 7, 6, 4, 2};
-__constant__ int pw_nb3[8][2] = {{-1, 1}, {0, 1}, {1, 1}, {-1, 0}, {1, 0}, {-1, -1}, {0, -1}, {1, -1}};
-__constant__ int pw_nb5[24][2] = {{-2, 2}, {-1, 2}, {0, 2},   {1, 2},   {2, 2},   {-2, 1},  {-1, 1}, {0, 1},
-                                  {1, 1},  {2, 1},  {-2, 0},  {-1, 0},  {1, 0},   {2, 0},   {-2, -1}, {-1, -1},
-                                  {0, -1}, {1, -1}, {2, -1},  {-2, -2}, {-1, -2}, {0, -2},  {1, -2},  {2, -2}};
-
-constexpr float kTLower = 1.0f, kTUpper = 256.0f, kTIncr = 0.5f, kTDecr = 0.25f;
-constexpr float kVIncr = 1.0f, kVDecr = 0.1f, kRVar = 0.01f, kUnstRatio = 0.1f, kUnstR = 3.0f;
-constexpr int kBootWin = kPwBootWin;
-
-__device__ __forceinline__ int pw_stream_by_tile(const PwParams& P, int t) {
-    int lo = 0, hi = P.nStreams - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (P.streams[mid].sd.tileBase <= t) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-__device__ __forceinline__ int pw_stream_by_row(const PwParams& P, int r) {
-    int lo = 0, hi = P.nStreams - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (P.streams[mid].sd.rowBase <= r) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
-// one rand() of the reference: draw k of pixel px in frame f
-__device__ __forceinline__ uint32_t pw_draw(unsigned long long seed, uint32_t f, uint32_t px, uint32_t k) {
-    uint32_t c[4] = {k >> 2, px, f, 0u};
-    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
-    return c[k & 3u] & 0x7fffffffu;
-}
-// draw % m for the reference's size_t moduli (rand() < 2^31, so a modulus above 2^32 leaves it as is)
-__device__ __forceinline__ uint32_t pw_mod(uint32_t r, unsigned long long m) {
-    return m > 0xffffffffull ? r : r % (uint32_t)m;
-}
-
-// GetLocalWordWeight (:1596-1598): (float)occ / (float)((last-first) + (t-last)*2 + offset)
-__device__ __forceinline__ float pw_weight(uint32_t occ, uint32_t first, uint32_t last, uint32_t t,
-                                           unsigned long long off) {
-    const unsigned long long den = (unsigned long long)(last - first) + (unsigned long long)(t - last) * 2ull + off;
-    return (float)occ / (float)den;
-}
-
-struct PwThr {
-    uint32_t color, desc;
-};
-// nCurrColorDistThreshold / nCurrDescDistThreshold of one channel (:633-634)
-__device__ __forceinline__ PwThr pw_thresholds(float R, uint32_t unstable, uint32_t minColor, uint32_t descOff) {
-    PwThr t;
-    t.color = (uint32_t)(__fsqrt_rn(R) * (float)minColor) / 2u;
-    const unsigned long long sh = (unsigned long long)floorf(R + 0.5f);
-    const unsigned long long d = (sh < 64 ? (1ull << sh) : 0ull) + descOff + (unsigned long long)unstable * descOff;
-    t.desc = d > 0xffffffffull ? 0xffffffffu : (uint32_t)d;
-    return t;
-}
-
-__device__ __forceinline__ uint32_t pw_absdiff(uint32_t a, uint32_t b) { return a > b ? a - b : b - a; }
-
-// current frame: LBSP lookups of pixel (x, y) and its descriptor
-__device__ __forceinline__ void pw_taps(const uint8_t* img, int W, int x, int y, uint8_t taps[16]) {
-#pragma unroll
-    for (int n = 0; n < 16; ++n) taps[n] = __ldg(img + (size_t)(y + pw_dy[n]) * W + (x + pw_dx[n]));
-}
-__device__ __forceinline__ uint32_t pw_lbsp(const uint8_t taps[16], uint32_t ref, uint32_t thr) {
-    uint32_t d = 0;
-#pragma unroll
-    for (int n = 0; n < 16; ++n) d |= (uint32_t)(pw_absdiff(taps[n], ref) > thr) << n;
-    return d;
-}
-
-// rolling-average factors of frame f (:570-573)
-__device__ __forceinline__ void pw_factors(unsigned long long f, int nmv, float* fLT, float* fST) {
-    const int boot = f <= (unsigned long long)kBootWin;
-    const unsigned long long nlt = boot ? (unsigned long long)(nmv / 2) : (unsigned long long)nmv, nst = nlt / 4;
-    *fLT = 1.0f / (float)(f < nlt ? f : nlt);
-    *fST = 1.0f / (float)(f < nst ? f : nst);
-}
-
-__device__ __forceinline__ size_t pw_slot(const PawcsDev& S, int buf, int j, int p) {
-    return ((size_t)buf * S.L + j) * S.sd.npx + p;
-}
 
 // the neighbour-update loop of updater p over target q's words (:850-878, one channel: the
 // reference updates a copy of each word, so only the weight sum and the draws matter); returns
@@ -310,8 +220,10 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_local(PwParams P) {
     R.rsrc = rsrc;
     R.kScan = (uint16_t)k;
     R.incr = (uint16_t)incr;
-    R.minColor = (uint8_t)minColor;
-    R.minDesc = (uint8_t)minDesc;
+    R.minColor = (uint16_t)minColor;
+    R.minDesc = (uint16_t)minDesc;
+    R.m0hi = 0;
+    R.m1hi = 0;
     R.flags = flags;
     R.bits = (uint8_t)bits;
 }
@@ -384,7 +296,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_items(PwParams P) {
             const float* fm = D.fm + (size_t)(D.ctl->frame_idx & 1ull) * kNumFloatMaps * D.npx;
             const PwThr th = pw_thresholds(fm[FM_R * D.npx + p], S.unstable[p], S.minColor, S.descOff);
             const uint32_t col = D.frame[p], bits = R.bits;
-            const uint8_t* lut = S.glut + (size_t)p * 16;
+            const uint8_t* lut = S.glut + (size_t)p * kPwGlutStride;
             int fixedPos = G, wrPos = G, fixedWord = -1;
             for (int g = 0; g < G; ++g) {
                 const int w = lut[g];
@@ -444,36 +356,38 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_compact_count(PwParams P,
     if (threadIdx.x < kPwCats) S.blkCounts[(size_t)blockIdx.x * kPwCats + threadIdx.x] = cnt[threadIdx.x];
 }
 
-// per category (one warp each): exclusive offsets over the blocks (in place), totals and the
-// category bases of the word-major list
-extern "C" __global__ void __launch_bounds__(32 * kPwCats) pw_k_compact_offsets(PwParams P) {
+// per category (one warp each, 32 warps): exclusive offsets over the blocks (in place), totals and
+// the category bases of the word-major list
+extern "C" __global__ void __launch_bounds__(1024) pw_k_compact_offsets(PwParams P) {
     const PawcsDev& S = P.streams[0];
     const int nb = (S.sd.npx + kPwCompactBlk - 1) / kPwCompactBlk;
     __shared__ uint32_t tot[kPwCats];
-    const int c = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint32_t run = 0;
-    for (int b0 = 0; b0 < nb; b0 += 32) {
-        const int b = b0 + lane;
-        uint32_t* e = &S.blkCounts[(size_t)b * kPwCats + c];
-        const uint32_t v = b < nb ? *e : 0u;
-        uint32_t inc = v;
+    const int lane = threadIdx.x & 31;
+    for (int c = threadIdx.x >> 5; c < kPwCats; c += 32) {
+        uint32_t run = 0;
+        for (int b0 = 0; b0 < nb; b0 += 32) {
+            const int b = b0 + lane;
+            uint32_t* e = &S.blkCounts[(size_t)b * kPwCats + c];
+            const uint32_t v = b < nb ? *e : 0u;
+            uint32_t inc = v;
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t o = __shfl_up_sync(0xffffffffu, inc, d);
-            if (lane >= d) inc += o;
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t o = __shfl_up_sync(0xffffffffu, inc, d);
+                if (lane >= d) inc += o;
+            }
+            if (b < nb) *e = run + inc - v;
+            run += __shfl_sync(0xffffffffu, inc, 31);
         }
-        if (b < nb) *e = run + inc - v;
-        run += __shfl_sync(0xffffffffu, inc, 31);
-    }
-    if (lane == 0) {
-        tot[c] = run;
-        S.catInfo[c] = run;
+        if (lane == 0) {
+            tot[c] = run;
+            S.catInfo[c] = run;
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t base = 0;
         for (int k = 0; k < kPwCats; ++k) {
-            S.catInfo[32 + k] = base;
+            S.catInfo[kPwCatBase + k] = base;
             base += tot[k];
         }
     }
@@ -490,7 +404,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_compact_scatter(PwParams 
     const int wr = S.pc->gdict[S.G - 1];
     const uint32_t nrep = S.pc->n_repl;
     if (threadIdx.x < kPwCats)
-        run[threadIdx.x] = S.catInfo[32 + threadIdx.x] + S.blkCounts[(size_t)blockIdx.x * kPwCats + threadIdx.x];
+        run[threadIdx.x] = S.catInfo[kPwCatBase + threadIdx.x] + S.blkCounts[(size_t)blockIdx.x * kPwCats + threadIdx.x];
     const float* fm = D.fm + (size_t)(D.ctl->frame_idx & 1ull) * kNumFloatMaps * D.npx;
     for (int k = 0; k < kPwCompactBlk / 256; ++k) {
         const int p = blockIdx.x * kPwCompactBlk + k * 256 + threadIdx.x;
@@ -516,7 +430,20 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_compact_scatter(PwParams 
         __syncthreads();
         if (c >= 0) {
             const uint32_t pos = run[c] + warpCnt[w][c] + rank;
-            if (mode == 0) {
+            if (mode == 0 && D.C == 3) {
+                // three channels: two records per item (pixel, colour|bits, thresholds, descriptors 0-1;
+                // descriptor 2|event flags, fixed position|word)
+                const PwRec& R = S.rec[p];
+                const PwThr th = pw3_thresholds(fm[FM_R * D.npx + p], S.unstable[p], S.minColor, S.descOff);
+                const uint32_t g = S.gitem[p];
+                const uint16_t* dt = S.descT + (size_t)p * 3;
+                const uint32_t a = pw3_color(D.frame, p) | ((uint32_t)R.bits << 24);
+                const uint32_t b = min(th.color, 65535u) | (min(th.desc / 4u, 65535u) << 16);
+                S.itemList[2 * pos] = make_uint4((uint32_t)p, a, b, (uint32_t)dt[0] | ((uint32_t)dt[1] << 16));
+                S.itemList[2 * pos + 1] =
+                    make_uint4((uint32_t)dt[2] | ((uint32_t)(R.flags & (kRfEvent | kRfRepDraw)) << 16),
+                               ((g >> 6) & 63u) | ((g & 63u) << 8), 0u, 0u);
+            } else if (mode == 0) {
                 const PwRec& R = S.rec[p];
                 const PwThr th = pw_thresholds(fm[FM_R * D.npx + p], S.unstable[p], S.minColor, S.descOff);
                 const uint32_t g = S.gitem[p];
@@ -595,6 +522,7 @@ extern "C" __global__ void pw_k_gscan(PwParams P) {
     if (lane == 0) {
         pc->wr_color = wrColor;
         pc->wr_desc = wrDesc;
+        pc->wr_desc2 = 0u;
         pc->wr_bits = wrBits;
         pc->n_repl = epoch;
     }
@@ -715,6 +643,10 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_nbr(PwParams P) {
     bool upd = false;
     if (!segm) upd = pw_mod(pw_draw(D.seed, t, (uint32_t)p, k++), R.rate) == 0u;
     upd = upd || border || moving;
+    // the previous round's loop inputs (round 0: no update known to the targets' local passes)
+    const uint32_t oldQ = P.round == 0 ? kPwNone : O.q;
+    const uint16_t oldK = O.kLoop;
+    const float oldThr = O.thrW;
     O.q = kPwNone;
     if (upd) {
         const uint32_t r = pw_draw(D.seed, t, (uint32_t)p, k++);
@@ -734,6 +666,9 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_nbr(PwParams P) {
         if (D.roi[q]) O.q = (uint32_t)q;
     }
     O.kLoop = (uint16_t)k;
+    O.thrW = R.thrW;
+    O.qPrev = oldQ;
+    O.chg = (uint8_t)(O.q != oldQ || (O.q != kPwNone && (O.kLoop != oldK || O.thrW != oldThr)));
 }
 
 // the neighbour-update loop of updater p on target q (:847-880; one channel: the reference updates a
@@ -1016,7 +951,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_weights(PwParams P) {
     const int wr = pc->gdict[S.G - 1];
     const uint32_t nrep = pc->n_repl;
     const bool isWr = w == wr;
-    const uint32_t n = S.catInfo[w], base = S.catInfo[32 + w];
+    const uint32_t n = S.catInfo[w], base = S.catInfo[kPwCatBase + w];
     __shared__ float buf[1024];
     float acc = (isWr && nrep > 0) ? 0.0f : pc->gw_weight[w];
     for (uint32_t c0 = 0; c0 < n; c0 += 1024) {
@@ -1032,6 +967,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_weights(PwParams P) {
         if (isWr && nrep > 0) {
             pc->gw_color[w] = pc->wr_color;
             pc->gw_desc[w] = pc->wr_desc;
+            pc->gw_desc2[w] = pc->wr_desc2;
             pc->gw_bits[w] = pc->wr_bits;
         }
     }
@@ -1171,7 +1107,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_lut_sort(PwParams P, int 
     if (!D.roi[p]) return;
     const size_t n = (size_t)S.gwW * S.gwH;
     const size_t cidx = (size_t)(y / 2) * S.gwW + (x / 2);
-    uint8_t* lut = S.glut + (size_t)p * 16;
+    uint8_t* lut = S.glut + (size_t)p * kPwGlutStride;
     uint8_t o[kPwMaxGlobal];
     for (int g = 0; g < S.G; ++g) o[g] = lut[g];
     float last = S.gmap[(size_t)o[0] * n + cidx];
@@ -1587,7 +1523,7 @@ extern "C" __global__ void pw_k_init(PawcsDev S) {
         D.dilInv[p] = 0;
         D.lastRawBlink[p] = 0;
         D.kctr[p] = 0;
-        for (int g = 0; g < 16; ++g) S.glut[(size_t)p * 16 + g] = (uint8_t)g;
+        for (int g = 0; g < kPwGlutStride; ++g) S.glut[(size_t)p * kPwGlutStride + g] = (uint8_t)g;
     }
 }
 
@@ -1652,7 +1588,7 @@ extern "C" __global__ void pw_k_motion_bg(PwParams P, int buf) {
 // camera-motion decision: ordered L1 sum, then switch the mode on (during the bootstrap window, ratio
 // >= 45) or off (ratio < 45/4) with the local word weight offset (5 / 1000); flags[1] tells the host
 // to run refreshModel(1, 1, true), flags[2] carries the new offset. One grayscale channel: the colour
-// distance ratio is 0.
+// distance ratio is 0; three channels: the mean colour distortion of pw3_k_motion_bg.
 extern "C" __global__ void pw_k_motion_decide(PwParams P) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const PawcsDev& S = P.streams[0];
@@ -1666,7 +1602,13 @@ extern "C" __global__ void pw_k_motion_decide(PwParams P) {
         float l1 = 0.0f;
         for (int i = 0; i < nds; ++i) l1 = l1 + S.dsAbs[i];
         const float mr = l1 / (float)pc->ds_roi_count;
-        const float cr = 0.0f;
+        float cr = 0.0f;
+        if (D.C == 3) {
+            // three channels: the ordered sum of the colour distortions (written beside the L1 terms)
+            float cs = 0.0f;
+            for (int i = 0; i < nds; ++i) cs = cs + S.contrib[i];
+            cr = cs / (float)pc->ds_roi_count;
+        }
         if (pc->moving_cam && mr < (float)(45 / 4) && cr < (float)(45 / 10 / 4)) {
             pc->lword_offset = (unsigned long long)kBootWin * 2;
             pc->moving_cam = 0;

@@ -1,4 +1,4 @@
-"""GPU parity tests of PAWCS (one channel): the CUDA path through the C-ABI against the oracle.
+"""GPU parity tests of PAWCS (one and three channels): the CUDA path through the C-ABI against the oracle.
 
 Masks, descriptors, every local and global dictionary word, the per-pixel global word tables and all
 integer maps must be identical; the FP32 maps (feedback maps, spatial occurrence maps, word weights,
@@ -135,7 +135,7 @@ def test_api_errors():
     with pytest.raises(LvException):
         b.apply(np.zeros((48, 64), np.uint8))
     with pytest.raises(LvException):
-        b.initialize(np.zeros((48, 64, 3), np.uint8))  # three channels: not implemented
+        b.initialize(np.zeros((48, 64, 4), np.uint8))  # four channels: the reference's apply has no such loop
     b.initialize(np.zeros((48, 64), np.uint8))
     with pytest.raises(LvException):
         b.apply(np.zeros((48, 65), np.uint8))
@@ -202,3 +202,39 @@ def test_set_roi_reinitializes_from_background():
     for f in fr[6:]:
         assert np.array_equal(gpu.apply(f), ora.apply(f, 0.0))
     assert not compare_state(gpu, ora)
+
+
+# ---- three channels (the pixel loop :935-1299: mixed colour distances, neighbour updates that edit the
+# target's words) ----
+
+def _bgr(n, seed, W, H, cfg=0):
+    s = SyntheticStream(cfg, 0, seed, width=W, height=H, channels=3)
+    return [s.render(t) for t in range(n)]
+
+
+def test_three_channel_small_frame():
+    # 64x48: two global words, every frame's whole state
+    run_pair(_bgr(20, 51, 64, 48), seed=6)
+
+
+def test_three_channel_moving_shapes_160x120():
+    run_pair(_bgr(30, 52, 160, 120), seed=7, check_every=3)
+
+
+def test_three_channel_lr_schedule_roi_and_background():
+    # the application's schedule (learning rate 1 for the first frames), an elliptic ROI, then
+    # refreshModel and the background images
+    fr = _bgr(18, 53, 96, 72)
+    yy, xx = np.mgrid[0:72, 0:96]
+    roi = ((((xx - 48) / 44.0) ** 2 + ((yy - 36) / 32.0) ** 2) <= 1.0).astype(np.uint8) * 255
+    lrs = [1.0 if t <= 6 else 0.0 for t in range(12)]
+    gpu, ora = run_pair(fr[:12], seed=14, lrs=lrs, roi=roi, check_every=2)
+    gpu.refreshModel(3, 0.25, True)
+    ora.refresh_model(3, 0.25, True)
+    bad = compare_state(gpu, ora)
+    assert not bad, "after refreshModel: " + "; ".join(bad)
+    for f in fr[12:]:
+        assert np.array_equal(gpu.apply(f), ora.apply(f))
+    assert not compare_state(gpu, ora)
+    assert np.array_equal(gpu.getBackgroundImage(), ora.background())
+    assert np.array_equal(gpu.getBackgroundDescriptorsImage(), ora.background_descriptors())
