@@ -137,29 +137,32 @@ def cpu_baseline(n_frames=6, threads=None):
                 len(frames), n_frames - 1, px / 1e6, wall)}
 
 
-def pawcs_run(n_frames, stream, cpu=True):
-    """PAWCS on the thermal-like 640x480 single-channel scene: every frame through lvbgs_apply, from
-    frames resident on the device (value) and from pinned host frames (e2e); wall clock per frame, since
-    a PAWCS frame step waits for its fixed-point rounds. The first 10 frames are warm-up."""
+def pawcs_run(n_frames, stream, cpu=True, channels=1):
+    """PAWCS on the thermal-like 640x480 single-channel scene (channels=3: a 640x480 BGR scene of moving
+    shapes on a smoothed texture): every frame through lvbgs_apply, from frames resident on the device
+    (value) and from pinned host frames (e2e); wall clock per frame, since a PAWCS frame step waits for
+    its fixed-point rounds. The first 10 frames are warm-up."""
     import ctypes as C
     import numpy as np
     import torch
     from litiv_gb300 import BackgroundSubtractorPAWCS, SyntheticStream
     from litiv_gb300 import _lib as L
     lib = L.lib()
-    s = SyntheticStream(2, 0, 1)
+    s = SyntheticStream(2, 0, 1) if channels == 1 else SyntheticStream(0, 0, 1, width=640, height=480, channels=3)
     W, H = s.cfg.width, s.cfg.height
     n = min(n_frames, s.n_frames)
-    dev = torch.empty((n, H, W), dtype=torch.uint8, device="cuda")
+    shp = (H, W) if channels == 1 else (H, W, 3)
+    dev = torch.empty((n,) + shp, dtype=torch.uint8, device="cuda")
     for t in range(n):
         s.render_device(t, dev[t].data_ptr(), cuda_stream=stream.cuda_stream)
-    host = torch.empty((n, H, W), dtype=torch.uint8).pin_memory()
+    host = torch.empty((n,) + shp, dtype=torch.uint8).pin_memory()
     host.copy_(dev.cpu())
     dmask = torch.empty((H, W), dtype=torch.uint8, device="cuda")
     hmask = torch.empty((H, W), dtype=torch.uint8).pin_memory()
     torch.cuda.synchronize()
-    out = {"workload": "PAWCS, 640x480 single-channel thermal-like scene (six warm blobs, random walks), default "
-                       "parameters, %d frames" % n}
+    scene = ("640x480 single-channel thermal-like scene (six warm blobs, random walks)" if channels == 1 else
+             "640x480 BGR scene (moving shapes on a smoothed texture, the SuBSENSE config 0 generator)")
+    out = {"workload": "PAWCS, %s, default parameters, %d frames" % (scene, n)}
     for leg, frames, mask in (("device", dev, dmask), ("host", host, hmask)):
         b = BackgroundSubtractorPAWCS(seed=1)
         b.initialize(frames[0].cpu().numpy())
@@ -181,7 +184,7 @@ def pawcs_run(n_frames, stream, cpu=True):
         if leg == "device":
             out.update(r)
         else:
-            r["h2d_bytes_per_step"] = W * H
+            r["h2d_bytes_per_step"] = W * H * channels
             r["d2h_bytes_per_step"] = W * H
             out["e2e"] = r
     if cpu:
@@ -190,7 +193,8 @@ def pawcs_run(n_frames, stream, cpu=True):
         nf = 3
         fr, seeds = [], []
         for i in range(threads):
-            si = SyntheticStream(2, 0, 100 + i)
+            si = (SyntheticStream(2, 0, 100 + i) if channels == 1 else
+                  SyntheticStream(0, 0, 100 + i, width=640, height=480, channels=3))
             fr.append(np.stack([si.render(t) for t in range(nf)]))
             seeds.append(100 + i)
         wall = pyoracle.run_pawcs_streams(fr, seeds, threads)
@@ -262,8 +266,8 @@ def serving_run(seconds):
             "rejected", "dropped", "spills", "restores", "late_frames", "peak_live", "peak_device_bytes", "status"]
     out = {k: r[k] for k in keep}
     out["workload"] = ("SuBSENSE/PAWCS mixed: Poisson arrivals 4/s (max 256 live), lives U[10,60] s, 30 fps, "
-                       "320x240/640x480/1280x720/1920x1080 at .3/.3/.3/.1, 1/4 single-channel and 1/10 of those on "
-                       "PAWCS (PAWCS runs single-channel frames), frames of PAWCS streams on 2 PAWCS lanes beside the "
+                       "320x240/640x480/1280x720/1920x1080 at .3/.3/.3/.1, 1/4 single-channel, 2.5 % of the streams "
+                       "(either channel count) on PAWCS, frames of PAWCS streams on 2 PAWCS lanes beside the "
                        "batched SuBSENSE ticks; stationary start; latency = submit -> mask in pinned host memory")
     return out
 
@@ -320,7 +324,9 @@ def main():
         torch.cuda.set_device(0)
         stream = torch.cuda.Stream()
         torch.cuda.set_stream(stream)
-        print(json.dumps(pawcs_run(args.pawcs_frames, stream, cpu=not args.no_cpu_baseline)))
+        out = pawcs_run(args.pawcs_frames, stream, cpu=not args.no_cpu_baseline)
+        out["bgr"] = pawcs_run(min(args.pawcs_frames, 100), stream, cpu=not args.no_cpu_baseline, channels=3)
+        print(json.dumps(out))
         return
 
     import numpy as np
@@ -521,6 +527,7 @@ def main():
     pawcs = None
     if rank == 0 and args.pawcs_frames > 0:
         pawcs = pawcs_run(args.pawcs_frames, stream, cpu=not args.no_cpu_baseline)
+        pawcs["bgr"] = pawcs_run(min(args.pawcs_frames, 100), stream, cpu=not args.no_cpu_baseline, channels=3)
     singles = None
     if rank == 0 and args.single_frames > 0:
         singles = {"config0": single_stream_run(0, args.single_frames, stream, cpu=not args.no_cpu_baseline,

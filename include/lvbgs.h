@@ -227,10 +227,11 @@ int lvbgs_debug_tick_profile(lvbgs_handle h, int batched, double* out_ms, int ma
 int lvbgs_debug_repair_phases(lvbgs_handle h, int batched, double* out_us, int max_n);
 
 /* ---- PAWCS (BackgroundSubtractorPAWCS, modules/video/src/BackgroundSubtractorPAWCS.cpp) ----
- * A handle created with LVBGS_ALGO_PAWCS runs PAWCS on single-channel frames (three-channel frames:
- * LVBGS_UNSUPPORTED). lvbgs_params maps onto the constructor (BackgroundSubtractorPAWCS.hpp:47-51):
+ * A handle created with LVBGS_ALGO_PAWCS runs PAWCS on single-channel (:608-934) and three-channel
+ * (:935-1299) frames. lvbgs_params maps onto the constructor (BackgroundSubtractorPAWCS.hpp:47-51):
  * desc_dist_threshold_offset (2), min_color_dist_threshold (20), bg_samples = nMaxNbWords (50; at most
- * 51), samples_for_moving_avgs (100), rel_lbsp_threshold (0.333); required_bg_samples is unused.
+ * 51 for single-channel and 50 for three-channel frames), samples_for_moving_avgs (100),
+ * rel_lbsp_threshold (0.333); required_bg_samples is unused.
  * initialize/apply/get_background/get_background_descriptors/get_roi work as for SuBSENSE; batched
  * steps and spilling are SuBSENSE-only for now. */
 

@@ -113,7 +113,7 @@ typedef struct {
     double fps;           /* 30 */
     double res_prob[4];   /* .3 .3 .3 .1 */
     double gray_prob;     /* .25 */
-    double pawcs_prob;    /* share of the single-channel streams that run PAWCS: .1 */
+    double pawcs_prob;    /* share of the streams (one or three channels) that run PAWCS: .025 */
     int prefill;          /* 1: start from the stationary population (Poisson(rate * mean life) streams with residual lives) */
     int pool_frames;      /* 4 */
     int render_threads;   /* 4 */

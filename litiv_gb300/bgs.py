@@ -203,7 +203,7 @@ class BackgroundSubtractorSuBSENSE:
 
 
 class BackgroundSubtractorPAWCS:
-    """PAWCS on the GPU, single-channel frames (the lv::CUDA specialisation the reference leaves missing);
+    """PAWCS on the GPU, single- and three-channel frames (the lv::CUDA specialisation the reference leaves missing);
     BackgroundSubtractorPAWCS.hpp:47-51 for the constructor parameters."""
 
     def __init__(self, nDescDistThresholdOffset=2, nMinColorDistThreshold=20, nMaxNbWords=50,

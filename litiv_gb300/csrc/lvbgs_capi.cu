@@ -77,7 +77,9 @@ extern "C" __global__ void pw_k_background(PawcsDev S, int buf, uint8_t* outCol,
 // PAWCS, three channels (pawcs3_kernels.cu)
 extern "C" __global__ void pw3_k_local(PwParams P);
 extern "C" __global__ void pw3_k_items(PwParams P);
-extern "C" __global__ void pw3_k_gscan(PwParams P);
+extern "C" __global__ void pw3_k_gscan_seg(PwParams P);
+extern "C" __global__ void pw3_k_gscan_walk(PwParams P);
+extern "C" __global__ void pw3_k_gscan_fix(PwParams P);
 extern "C" __global__ void pw3_k_dirty(PwParams P);
 extern "C" __global__ void pw3_k_later(PwParams P);
 extern "C" __global__ void pw3_k_commit(PwParams P);
@@ -874,7 +876,9 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
             pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
             pw3_k_items<<<tiles, blk, 0, st>>>(P);
             compact(0);
-            pw3_k_gscan<<<1, 32, 0, st>>>(P);
+            pw3_k_gscan_seg<<<(int)((h->npx + 4 * 1024 - 1) / (4 * 1024)), 128, 0, st>>>(P);
+            pw3_k_gscan_walk<<<1, 32, 0, st>>>(P);
+            pw3_k_gscan_fix<<<(int)((h->npx + 255) / 256), 256, 0, st>>>(P);
             pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
             pw_k_nbr<<<tiles, blk, 0, st>>>(P);
             LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 4, st), "flag reset");

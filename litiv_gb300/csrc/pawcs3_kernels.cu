@@ -385,67 +385,214 @@ extern "C" __global__ void __launch_bounds__(256) pw3_k_items(PwParams P) {
     if (critical) O.gflags |= 4;
 }
 
-// ordered scan of the critical items (one warp): pw_k_gscan with the three-channel records (two
-// uint4 per item: pixel, colour|bits, thresholds, descriptors 0-1; descriptor 2|event flags, fixed
-// position|word)
-extern "C" __global__ void pw3_k_gscan(PwParams P) {
-    const int si = blockIdx.x;
-    if (si >= P.nStreams) return;
-    const PawcsDev& S = P.streams[si];
-    PawcsCtl* pc = S.pc;
-    const int lane = threadIdx.x;
-    const int G = S.G;
-    const int wr = pc->gdict[G - 1];
-    uint32_t wrColor = pc->gw_color[wr], wrDesc = pc->gw_desc[wr], wrDesc2 = pc->gw_desc2[wr], wrBits = pc->gw_bits[wr];
-    uint32_t epoch = 0;
-    const uint32_t n = S.catInfo[0];
-    for (uint32_t base = 0; base < n; base += 32) {
-        const int cnt = (int)min(32u, n - base);
+// ------------------------------------------------------------------------------------------
+// ordered scan of the critical items (:1127-1150), three channels, segment-parallel. The replaceable
+// word's features change at each replacement; after a replacement they no longer depend on anything
+// before it. So each segment of kPw3Seg items is scanned by its own warp on the speculation that its
+// first candidate (an event with the replacement draw and no fixed match) replaces the word. Two scans
+// that both see an item replace the word agree from there on, so one warp then walks the segments in
+// order with the true incoming features, each only up to its first item that replaces the word in both
+// scans (usually the candidate itself); a last pass shifts the later items' epochs.
+// Records: two uint4 per item (pixel, colour|bits, thresholds, descriptors 0-1; descriptor 2|event
+// flags, fixed position|word).
+// ------------------------------------------------------------------------------------------
+constexpr int kPw3Seg = 1024;
+struct Pw3GFeat {
+    uint32_t col, d01, d2, bits;
+};
+struct Pw3Item {
+    uint32_t p, col, bits, cthr, dq, d01, d2, fixedPos, fixedWord;
+    bool evRep;
+};
+__device__ __forceinline__ Pw3Item pw3_item(const PawcsDev& S, uint32_t i) {
+    const uint4 a = S.itemList[2 * i], b = S.itemList[2 * i + 1];
+    Pw3Item it;
+    it.p = a.x;
+    it.col = a.y & 0xffffffu;
+    it.bits = a.y >> 24;
+    it.cthr = a.z & 65535u;
+    it.dq = a.z >> 16;
+    it.d01 = a.w;
+    it.d2 = b.x & 65535u;
+    it.evRep = ((b.x >> 16) & kRfEvent) && ((b.x >> 16) & kRfRepDraw);
+    it.fixedPos = b.y & 255u;
+    it.fixedWord = (b.y >> 8) & 255u;
+    return it;
+}
+__device__ __forceinline__ bool pw3_gmatch(const Pw3Item& it, const Pw3GFeat& f) {
+    return pw_absdiff(it.bits, f.bits) <= it.dq && pw3_cmix(it.col, f.col) <= it.cthr;
+}
+// per-segment scratch (in blkCounts, free between the ordered compaction and the next round):
+// [0] first candidate (or kPwNone), [1] replacements of the speculative scan, [2..5] features after its
+// last one, [6] epoch shift and [7] synchronization item of the walk (kPwNone: none)
+__device__ __forceinline__ uint32_t* pw3_segw(const PawcsDev& S, int s) { return S.blkCounts + (size_t)s * 8; }
+
+// the serial warp scan of items [a, b) from features f and epoch e (pw_k_gscan's chunk loop); writes
+// every item's outcome, returns the final features and epoch. With sync, the scan stops at the first
+// item that replaces the word both here and in the segment's speculative scan (bit 0 of gflags and
+// the epoch that pass wrote): from there on both scans agree, so the later items keep the speculative
+// outcomes with their epochs shifted by *offset; *syncIdx is that item (kPwNone: no such item).
+__device__ void pw3_gscan_range(const PawcsDev& S, int G, int wr, uint32_t a, uint32_t b, Pw3GFeat& f, uint32_t& e,
+                                bool sync, uint32_t* syncIdx, uint32_t* offset) {
+    const int lane = threadIdx.x & 31;
+    if (syncIdx) *syncIdx = kPwNone;
+    for (uint32_t base = a; base < b; base += 32) {
+        const int cnt = (int)min(32u, b - base);
         const bool valid = lane < cnt;
-        const uint4 a = valid ? S.itemList[2 * (base + lane)] : make_uint4(0, 0, 0, 0);
-        const uint4 b = valid ? S.itemList[2 * (base + lane) + 1] : make_uint4(0, 0, 0, 0);
-        const uint32_t col = a.y & 0xffffffu, bits = a.y >> 24, cthr = a.z & 65535u, dq = a.z >> 16;
-        const uint32_t fixedPos = b.y & 255u, fixedWord = (b.y >> 8) & 255u;
-        const bool evRep = ((b.x >> 16) & kRfEvent) && ((b.x >> 16) & kRfRepDraw);
+        Pw3Item it;
+        uint32_t specRepl = 0, specEpoch = 0;
+        if (valid) {
+            it = pw3_item(S, base + lane);
+            const PwOut& O = S.out[it.p];
+            specRepl = O.gflags & 1u;
+            specEpoch = O.epoch;
+        } else {
+            it.p = 0;
+            it.col = it.bits = it.cthr = it.dq = it.d01 = it.d2 = it.fixedPos = it.fixedWord = 0;
+            it.evRep = false;
+        }
         uint32_t myWord = kPwNone, myEpoch = 0, myRepl = 0;
-        int cursor = 0;
+        int cursor = 0, last = cnt - 1;
+        bool synced = false;
         while (cursor < cnt) {
-            const bool mWr = pw_absdiff(bits, wrBits) <= dq && pw3_cmix(col, wrColor) <= cthr;
-            const bool repl = valid && !mWr && (int)fixedPos >= G && evRep;
+            const bool mWr = pw3_gmatch(it, f);
+            const bool repl = valid && !mWr && (int)it.fixedPos >= G && it.evRep;
             const unsigned cand = __ballot_sync(0xffffffffu, repl && lane >= cursor);
             const int stop = cand ? __ffs(cand) - 1 : cnt;
             if (lane >= cursor && lane < stop) {
-                myWord = mWr ? (uint32_t)wr : ((int)fixedPos < G ? fixedWord : kPwNone);
-                myEpoch = epoch;
+                myWord = mWr ? (uint32_t)wr : ((int)it.fixedPos < G ? it.fixedWord : kPwNone);
+                myEpoch = e;
             }
             if (stop < cnt) {
-                ++epoch;
+                ++e;
                 if (lane == stop) {
                     myWord = (uint32_t)wr;
-                    myEpoch = epoch;
+                    myEpoch = e;
                     myRepl = 1;
                 }
-                wrColor = __shfl_sync(0xffffffffu, col, stop);
-                wrDesc = __shfl_sync(0xffffffffu, a.w, stop);
-                wrDesc2 = __shfl_sync(0xffffffffu, b.x & 65535u, stop);
-                wrBits = __shfl_sync(0xffffffffu, bits, stop);
+                f.col = __shfl_sync(0xffffffffu, it.col, stop);
+                f.d01 = __shfl_sync(0xffffffffu, it.d01, stop);
+                f.d2 = __shfl_sync(0xffffffffu, it.d2, stop);
+                f.bits = __shfl_sync(0xffffffffu, it.bits, stop);
+                if (sync && __shfl_sync(0xffffffffu, specRepl, stop)) {
+                    *syncIdx = base + (uint32_t)stop;
+                    *offset = e - __shfl_sync(0xffffffffu, specEpoch, stop);
+                    last = stop;
+                    synced = true;
+                    break;
+                }
             }
             cursor = stop + 1;
         }
-        if (valid) {
-            PwOut& O = S.out[a.x];
+        if (valid && lane <= last) {
+            PwOut& O = S.out[it.p];
             O.gword = myWord;
             O.epoch = myEpoch;
-            if (myRepl) O.gflags |= 1;
+            O.gflags = (uint8_t)((O.gflags & ~1u) | myRepl);
+        }
+        if (synced) return;
+    }
+}
+
+// phase 1: one warp per segment, on the speculation that the segment's first candidate replaces
+extern "C" __global__ void __launch_bounds__(128) pw3_k_gscan_seg(PwParams P) {
+    const PawcsDev& S = P.streams[0];
+    const uint32_t n = S.catInfo[0];
+    const int s = blockIdx.x * 4 + (int)(threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const uint32_t a = (uint32_t)s * kPw3Seg;
+    if (a >= n) return;
+    const uint32_t b = min(n, a + (uint32_t)kPw3Seg);
+    const int G = S.G;
+    const int wr = S.pc->gdict[G - 1];
+    uint32_t* sw = pw3_segw(S, s);
+    // first candidate of the segment
+    uint32_t c0 = kPwNone;
+    for (uint32_t base = a; base < b && c0 == kPwNone; base += 32) {
+        bool cand = false;
+        if (base + lane < b) {
+            const Pw3Item it = pw3_item(S, base + lane);
+            cand = (int)it.fixedPos >= G && it.evRep;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, cand);
+        if (m) c0 = base + (uint32_t)(__ffs(m) - 1);
+    }
+    if (lane == 0) sw[0] = c0;
+    if (c0 == kPwNone) return;
+    const Pw3Item it0 = pw3_item(S, c0);
+    if (lane == 0) {
+        PwOut& O = S.out[it0.p];
+        O.gword = (uint32_t)wr;
+        O.epoch = 1u;
+        O.gflags = (uint8_t)(O.gflags | 1u);
+    }
+    Pw3GFeat f;
+    f.col = it0.col;
+    f.d01 = it0.d01;
+    f.d2 = it0.d2;
+    f.bits = it0.bits;
+    uint32_t e = 1;
+    pw3_gscan_range(S, G, wr, c0 + 1, b, f, e, false, nullptr, nullptr);
+    if (lane == 0) {
+        sw[1] = e;
+        sw[2] = f.col;
+        sw[3] = f.d01;
+        sw[4] = f.d2;
+        sw[5] = f.bits;
+    }
+}
+
+// phase 2: one warp walks the segments in order with the true incoming features, each up to its
+// first item that replaces the word in both scans
+extern "C" __global__ void pw3_k_gscan_walk(PwParams P) {
+    const PawcsDev& S = P.streams[0];
+    PawcsCtl* pc = S.pc;
+    const int lane = threadIdx.x & 31;
+    const uint32_t n = S.catInfo[0];
+    const int G = S.G;
+    const int wr = pc->gdict[G - 1];
+    Pw3GFeat f;
+    f.col = pc->gw_color[wr];
+    f.d01 = pc->gw_desc[wr];
+    f.d2 = pc->gw_desc2[wr];
+    f.bits = pc->gw_bits[wr];
+    uint32_t e = 0;
+    const int nseg = (int)((n + kPw3Seg - 1) / kPw3Seg);
+    for (int s = 0; s < nseg; ++s) {
+        uint32_t* sw = pw3_segw(S, s);
+        const uint32_t a = (uint32_t)s * kPw3Seg, b = min(n, a + (uint32_t)kPw3Seg);
+        uint32_t syncIdx = kPwNone, offset = 0;
+        pw3_gscan_range(S, G, wr, a, b, f, e, sw[0] != kPwNone, &syncIdx, &offset);
+        if (syncIdx != kPwNone) {
+            // the rest of the segment follows the speculative scan
+            e = sw[1] + offset;
+            f.col = sw[2];
+            f.d01 = sw[3];
+            f.d2 = sw[4];
+            f.bits = sw[5];
+        }
+        if (lane == 0) {
+            sw[6] = offset;
+            sw[7] = syncIdx;
         }
     }
     if (lane == 0) {
-        pc->wr_color = wrColor;
-        pc->wr_desc = wrDesc;
-        pc->wr_desc2 = wrDesc2;
-        pc->wr_bits = wrBits;
-        pc->n_repl = epoch;
+        pc->wr_color = f.col;
+        pc->wr_desc = f.d01;
+        pc->wr_desc2 = f.d2;
+        pc->wr_bits = f.bits;
+        pc->n_repl = e;
     }
+}
+
+// phase 3: the epoch shift of the items after each segment's synchronization item
+extern "C" __global__ void __launch_bounds__(256) pw3_k_gscan_fix(PwParams P) {
+    const PawcsDev& S = P.streams[0];
+    const uint32_t n = S.catInfo[0];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t* sw = pw3_segw(S, (int)(i / kPw3Seg));
+    if (sw[7] == kPwNone || i <= sw[7]) return;
+    S.out[S.itemList[2 * i].x].epoch += sw[6];
 }
 
 // pixels rerun next round: an earlier updater in the 5x5 window whose loop inputs changed this

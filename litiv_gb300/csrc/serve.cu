@@ -803,7 +803,7 @@ extern "C" {
 
 lvbgs_status lvserve_default_sim_config(lvserve_sim_config* o) {
     if (!o) return LVBGS_BAD_ARG;
-    *o = lvserve_sim_config{20.0, 3.0, 4.0, 10.0, 60.0, 30.0, {0.3, 0.3, 0.3, 0.1}, 0.25, 0.1, 1, 4, 4, 1};
+    *o = lvserve_sim_config{20.0, 3.0, 4.0, 10.0, 60.0, 30.0, {0.3, 0.3, 0.3, 0.1}, 0.25, 0.025, 1, 4, 4, 1};
     return LVBGS_OK;
 }
 
@@ -835,8 +835,8 @@ lvbgs_status lvserve_simulate(const lvserve_config* cfg, const lvserve_sim_confi
             }
         }
         const int gray = rng.uni() < sim.gray_prob ? 1 : 0;
-        // PAWCS runs on single-channel frames; a share of them run it
-        z->algo = (gray && rng.uni() < sim.pawcs_prob) ? LVBGS_ALGO_PAWCS : LVBGS_ALGO_SUBSENSE;
+        // a share of the streams (of either channel count) run PAWCS
+        z->algo = rng.uni() < sim.pawcs_prob ? LVBGS_ALGO_PAWCS : LVBGS_ALGO_SUBSENSE;
         z->cls = 2 * r + gray;
         z->W = kW[r];
         z->H = kH[r];

@@ -238,3 +238,52 @@ def test_three_channel_lr_schedule_roi_and_background():
     assert not compare_state(gpu, ora)
     assert np.array_equal(gpu.getBackgroundImage(), ora.background())
     assert np.array_equal(gpu.getBackgroundDescriptorsImage(), ora.background_descriptors())
+
+
+def test_three_channel_fixed_point_rounds_and_partial_words():
+    # 72 px rows (partial bit-plane words); the earlier updaters' word edits need more than one round
+    gpu, ora = run_pair(_bgr(16, 54, 72, 56), seed=15, check_every=3)
+    rounds = []
+    s = SyntheticStream(0, 0, 55, width=72, height=56, channels=3)
+    g2 = BackgroundSubtractorPAWCS(seed=16)
+    g2.initialize(s.render(0))
+    for t in range(1, 8):
+        g2.apply(s.render(t))
+        rounds.append(g2.scalars()["fixed_point_rounds"])
+    assert max(rounds) >= 2, rounds
+
+
+def test_three_channel_full_size_prefix():
+    # a 640x480 BGR scene: the three-channel geometry at full size (50 local, 25 global words, median 13)
+    s = SyntheticStream(0, 0, 56, width=640, height=480, channels=3)
+    gpu, ora = run_pair([s.render(t) for t in range(6)], seed=17, check_every=5)
+    sc = gpu.scalars()
+    assert (sc["n_local_words"], sc["n_global_words"]) == (50, 25)
+
+
+def test_three_channel_moving_camera_mode_switch():
+    # as the one-channel case, on BGR frames: the camera-motion comparison adds the colour distortion
+    # ratio of the down-sampled background image (lv::cdist on floats)
+    W, H = 64, 48
+    s = SyntheticStream(0, 0, 57, width=W, height=H, channels=3)
+    base = [s.render(t).astype(np.int32) for t in range(8)]
+
+    def frame(t):
+        return np.clip(base[t % 8] - int(min(max(0, t - 150), 300) * 120 / 300), 0, 255).astype(np.uint8)
+
+    gpu = BackgroundSubtractorPAWCS(seed=18)
+    ora = pyoracle.OraclePAWCS(seed=18)
+    gpu.initialize(frame(0))
+    ora.initialize(frame(0))
+    modes = {}
+    for t in range(1, 1002):
+        lr = float("inf") if 150 <= t <= 500 else 0.0
+        mg = gpu.apply(frame(t), learningRateOverride=lr)
+        mo = ora.apply(frame(t), lr)
+        assert np.array_equal(mg, mo), "frame %d: mask differs at %d px" % (t, int((mg != mo).sum()))
+        if t % 100 == 0 or t in (499, 501, 999, 1001):
+            bad = compare_state(gpu, ora)
+            assert not bad, "frame %d: %s" % (t, "; ".join(bad))
+        if t in (499, 500, 999, 1000):
+            modes[t] = gpu.scalars()["using_moving_camera"]
+    assert modes[499] == 0 and modes[500] == 1, modes

@@ -25,8 +25,8 @@ def test_default_config_and_workload():
     # Poisson arrivals at 4 streams/s, lives U[10, 60] s, 30 fps, resolution mix .3/.3/.3/.1
     assert (sim.arrival_rate, sim.life_min_s, sim.life_max_s, sim.fps) == (4.0, 10.0, 60.0, 30.0)
     assert [round(p, 6) for p in sim.res_prob] == [0.3, 0.3, 0.3, 0.1]
-    # a quarter single-channel, a tenth of those running PAWCS (SuBSENSE/PAWCS mixed)
-    assert (sim.gray_prob, sim.pawcs_prob) == (0.25, 0.1)
+    # a quarter single-channel; 2.5 % of the streams (either channel count) run PAWCS (SuBSENSE/PAWCS mixed)
+    assert (sim.gray_prob, sim.pawcs_prob) == (0.25, 0.025)
 
 
 def test_create_rejects_bad_config():
@@ -179,7 +179,7 @@ def test_pawcs_and_subsense_streams_served_together_equal_alone():
     # every mask must equal the same stream run alone
     from litiv_gb300 import BackgroundSubtractorPAWCS
     mix = [(L.ALGO_SUBSENSE, 96, 64, 3, 31), (L.ALGO_PAWCS, 96, 72, 1, 32), (L.ALGO_SUBSENSE, 64, 48, 1, 33),
-           (L.ALGO_PAWCS, 160, 120, 1, 34)]
+           (L.ALGO_PAWCS, 160, 120, 3, 34)]
     n_frames = 10
     data = [_frames(W, H, Cn, seed, n_frames) for (_, W, H, Cn, seed) in mix]
     alone = []
