@@ -580,7 +580,9 @@ PwLayout pw_layout(int W, int H, int C, int L, int G) {
     sz[PL_UV] = npx;
     sz[PL_ITEMLIST] = npx * 16 * (C == 3 ? 2 : 1);
     sz[PL_CONTRIBLIST] = npx * 4;
-    sz[PL_BLKCOUNTS] = ((npx + kPwCompactBlk - 1) / kPwCompactBlk) * kPwCats * 4;
+    // ordered-compaction counts; also the three-channel global scan's per-segment scratch (16 words
+    // per 512 items)
+    sz[PL_BLKCOUNTS] = std::max(((npx + kPwCompactBlk - 1) / kPwCompactBlk) * kPwCats * 4, (npx / 512 + 1) * 16 * 4);
     sz[PL_CATINFO] = 2 * kPwCatBase * 4;
     sz[PL_DSABS] = std::max<size_t>(nds, 1) * 4;
     sz[PL_UPDLIST] = npx * 4;
@@ -876,7 +878,7 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
             pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
             pw3_k_items<<<tiles, blk, 0, st>>>(P);
             compact(0);
-            pw3_k_gscan_seg<<<(int)((h->npx + 4 * 1024 - 1) / (4 * 1024)), 128, 0, st>>>(P);
+            pw3_k_gscan_seg<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
             pw3_k_gscan_walk<<<1, 32, 0, st>>>(P);
             pw3_k_gscan_fix<<<(int)((h->npx + 255) / 256), 256, 0, st>>>(P);
             pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);

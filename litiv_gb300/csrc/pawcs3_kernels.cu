@@ -386,26 +386,27 @@ extern "C" __global__ void __launch_bounds__(256) pw3_k_items(PwParams P) {
 }
 
 // ------------------------------------------------------------------------------------------
-// ordered scan of the critical items (:1127-1150), three channels, segment-parallel. The replaceable
-// word's features change at each replacement; after a replacement they no longer depend on anything
-// before it. So each segment of kPw3Seg items is scanned by its own warp on the speculation that its
-// first candidate (an event with the replacement draw and no fixed match) replaces the word. Two scans
-// that both see an item replace the word agree from there on, so one warp then walks the segments in
-// order with the true incoming features, each only up to its first item that replaces the word in both
-// scans (usually the candidate itself); a last pass shifts the later items' epochs.
+// ordered scan of the critical items (:1127-1150), three channels, segment-parallel. The scan's state
+// is only the replaceable word's features (those of its last replacement), and two scans that both see
+// an item replace the word agree from there on. So each segment of kPw3Seg items is scanned by its
+// own warp from kPw3Warm items before its start, from a guessed state (the first of those items'
+// features): with replacements frequent, the scan reaches the segment in the true state. One warp
+// then walks the segments in order: a segment whose speculative state at its start equals the true
+// incoming features keeps its speculative outcomes (one comparison); otherwise it is rescanned up to
+// its first item that replaces the word in both scans. A last parallel pass writes the outcomes.
 // Records: two uint4 per item (pixel, colour|bits, thresholds, descriptors 0-1; descriptor 2|event
-// flags, fixed position|word).
+// flags, fixed position|word, speculative word, speculative epoch | replaced << 31).
 // ------------------------------------------------------------------------------------------
-constexpr int kPw3Seg = 1024;
+constexpr int kPw3Seg = 512;
+constexpr int kPw3Warm = 128;
 struct Pw3GFeat {
     uint32_t col, d01, d2, bits;
 };
 struct Pw3Item {
-    uint32_t p, col, bits, cthr, dq, d01, d2, fixedPos, fixedWord;
+    uint32_t p, col, bits, cthr, dq, d01, d2, fixedPos, fixedWord, specWord, specEpoch;
     bool evRep;
 };
-__device__ __forceinline__ Pw3Item pw3_item(const PawcsDev& S, uint32_t i) {
-    const uint4 a = S.itemList[2 * i], b = S.itemList[2 * i + 1];
+__device__ __forceinline__ Pw3Item pw3_item_of(const uint4 a, const uint4 b) {
     Pw3Item it;
     it.p = a.x;
     it.col = a.y & 0xffffffu;
@@ -417,40 +418,44 @@ __device__ __forceinline__ Pw3Item pw3_item(const PawcsDev& S, uint32_t i) {
     it.evRep = ((b.x >> 16) & kRfEvent) && ((b.x >> 16) & kRfRepDraw);
     it.fixedPos = b.y & 255u;
     it.fixedWord = (b.y >> 8) & 255u;
+    it.specWord = b.z;
+    it.specEpoch = b.w;
     return it;
+}
+__device__ __forceinline__ Pw3Item pw3_item(const PawcsDev& S, uint32_t i) {
+    return pw3_item_of(S.itemList[2 * i], S.itemList[2 * i + 1]);
 }
 __device__ __forceinline__ bool pw3_gmatch(const Pw3Item& it, const Pw3GFeat& f) {
     return pw_absdiff(it.bits, f.bits) <= it.dq && pw3_cmix(it.col, f.col) <= it.cthr;
 }
+__device__ __forceinline__ void pw3_set_out(const PawcsDev& S, uint32_t p, uint32_t word, uint32_t epoch, uint32_t repl) {
+    PwOut& O = S.out[p];
+    O.gword = word;
+    O.epoch = epoch;
+    O.gflags = (uint8_t)((O.gflags & ~1u) | repl);
+}
 // per-segment scratch (in blkCounts, free between the ordered compaction and the next round):
-// [0] first candidate (or kPwNone), [1] replacements of the speculative scan, [2..5] features after its
-// last one, [6] epoch shift and [7] synchronization item of the walk (kPwNone: none)
-__device__ __forceinline__ uint32_t* pw3_segw(const PawcsDev& S, int s) { return S.blkCounts + (size_t)s * 8; }
+// [0] replacements of the speculative scan in the segment, [1..4] its state at the segment's start,
+// [5..8] its state at the end; from the walk: [9] mode (1 kept, 2 rescanned), [10] epoch base (mode 1)
+// or shift (mode 2), [11] synchronization item (mode 2; kPwNone: none)
+constexpr int kPw3SegWords = 16;
+__device__ __forceinline__ uint32_t* pw3_segw(const PawcsDev& S, int s) { return S.blkCounts + (size_t)s * kPw3SegWords; }
 
-// the serial warp scan of items [a, b) from features f and epoch e (pw_k_gscan's chunk loop); writes
-// every item's outcome, returns the final features and epoch. With sync, the scan stops at the first
-// item that replaces the word both here and in the segment's speculative scan (bit 0 of gflags and
-// the epoch that pass wrote): from there on both scans agree, so the later items keep the speculative
-// outcomes with their epochs shifted by *offset; *syncIdx is that item (kPwNone: no such item).
+enum { kGsDry = 0, kGsSpec = 1, kGsRescan = 2 };
+// the serial warp scan of items [a, b) from features f and epoch e (pw_k_gscan's chunk loop).
+// kGsDry: no outcome written (warm-up); kGsSpec: outcomes into the item records; kGsRescan: outcomes
+// into the pixels, stopping at the first item that replaces the word both here and in the speculative
+// scan (*syncIdx, kPwNone: none), *offset being the epoch shift of the later items.
 __device__ void pw3_gscan_range(const PawcsDev& S, int G, int wr, uint32_t a, uint32_t b, Pw3GFeat& f, uint32_t& e,
-                                bool sync, uint32_t* syncIdx, uint32_t* offset) {
+                                int mode, uint32_t* syncIdx, uint32_t* offset) {
     const int lane = threadIdx.x & 31;
     if (syncIdx) *syncIdx = kPwNone;
     for (uint32_t base = a; base < b; base += 32) {
         const int cnt = (int)min(32u, b - base);
         const bool valid = lane < cnt;
         Pw3Item it;
-        uint32_t specRepl = 0, specEpoch = 0;
-        if (valid) {
-            it = pw3_item(S, base + lane);
-            const PwOut& O = S.out[it.p];
-            specRepl = O.gflags & 1u;
-            specEpoch = O.epoch;
-        } else {
-            it.p = 0;
-            it.col = it.bits = it.cthr = it.dq = it.d01 = it.d2 = it.fixedPos = it.fixedWord = 0;
-            it.evRep = false;
-        }
+        if (valid) it = pw3_item(S, base + lane);
+        else it = pw3_item_of(make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0));
         uint32_t myWord = kPwNone, myEpoch = 0, myRepl = 0;
         int cursor = 0, last = cnt - 1;
         bool synced = false;
@@ -474,9 +479,9 @@ __device__ void pw3_gscan_range(const PawcsDev& S, int G, int wr, uint32_t a, ui
                 f.d01 = __shfl_sync(0xffffffffu, it.d01, stop);
                 f.d2 = __shfl_sync(0xffffffffu, it.d2, stop);
                 f.bits = __shfl_sync(0xffffffffu, it.bits, stop);
-                if (sync && __shfl_sync(0xffffffffu, specRepl, stop)) {
+                if (mode == kGsRescan && (__shfl_sync(0xffffffffu, it.specEpoch, stop) >> 31)) {
                     *syncIdx = base + (uint32_t)stop;
-                    *offset = e - __shfl_sync(0xffffffffu, specEpoch, stop);
+                    *offset = e - (__shfl_sync(0xffffffffu, it.specEpoch, stop) & 0x7fffffffu);
                     last = stop;
                     synced = true;
                     break;
@@ -485,16 +490,19 @@ __device__ void pw3_gscan_range(const PawcsDev& S, int G, int wr, uint32_t a, ui
             cursor = stop + 1;
         }
         if (valid && lane <= last) {
-            PwOut& O = S.out[it.p];
-            O.gword = myWord;
-            O.epoch = myEpoch;
-            O.gflags = (uint8_t)((O.gflags & ~1u) | myRepl);
+            if (mode == kGsRescan) {
+                pw3_set_out(S, it.p, myWord, myEpoch, myRepl);
+            } else if (mode == kGsSpec) {
+                uint4& r = S.itemList[2 * (base + lane) + 1];
+                r.z = myWord;
+                r.w = myEpoch | (myRepl << 31);
+            }
         }
         if (synced) return;
     }
 }
 
-// phase 1: one warp per segment, on the speculation that the segment's first candidate replaces
+// phase 1: one warp per segment, from a guessed state kPw3Warm items before the segment
 extern "C" __global__ void __launch_bounds__(128) pw3_k_gscan_seg(PwParams P) {
     const PawcsDev& S = P.streams[0];
     const uint32_t n = S.catInfo[0];
@@ -502,47 +510,45 @@ extern "C" __global__ void __launch_bounds__(128) pw3_k_gscan_seg(PwParams P) {
     const uint32_t a = (uint32_t)s * kPw3Seg;
     if (a >= n) return;
     const uint32_t b = min(n, a + (uint32_t)kPw3Seg);
+    const PawcsCtl* pc = S.pc;
     const int G = S.G;
-    const int wr = S.pc->gdict[G - 1];
+    const int wr = pc->gdict[G - 1];
     uint32_t* sw = pw3_segw(S, s);
-    // first candidate of the segment
-    uint32_t c0 = kPwNone;
-    for (uint32_t base = a; base < b && c0 == kPwNone; base += 32) {
-        bool cand = false;
-        if (base + lane < b) {
-            const Pw3Item it = pw3_item(S, base + lane);
-            cand = (int)it.fixedPos >= G && it.evRep;
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, cand);
-        if (m) c0 = base + (uint32_t)(__ffs(m) - 1);
-    }
-    if (lane == 0) sw[0] = c0;
-    if (c0 == kPwNone) return;
-    const Pw3Item it0 = pw3_item(S, c0);
-    if (lane == 0) {
-        PwOut& O = S.out[it0.p];
-        O.gword = (uint32_t)wr;
-        O.epoch = 1u;
-        O.gflags = (uint8_t)(O.gflags | 1u);
-    }
     Pw3GFeat f;
-    f.col = it0.col;
-    f.d01 = it0.d01;
-    f.d2 = it0.d2;
-    f.bits = it0.bits;
-    uint32_t e = 1;
-    pw3_gscan_range(S, G, wr, c0 + 1, b, f, e, false, nullptr, nullptr);
+    uint32_t e = 0;
+    if (a == 0) {
+        f.col = pc->gw_color[wr];
+        f.d01 = pc->gw_desc[wr];
+        f.d2 = pc->gw_desc2[wr];
+        f.bits = pc->gw_bits[wr];
+    } else {
+        const uint32_t w0 = a > (uint32_t)kPw3Warm ? a - (uint32_t)kPw3Warm : 0u;
+        const Pw3Item g = pw3_item(S, w0);
+        f.col = g.col;
+        f.d01 = g.d01;
+        f.d2 = g.d2;
+        f.bits = g.bits;
+        pw3_gscan_range(S, G, wr, w0 + 1, a, f, e, kGsDry, nullptr, nullptr);
+        e = 0;
+    }
     if (lane == 0) {
-        sw[1] = e;
-        sw[2] = f.col;
-        sw[3] = f.d01;
-        sw[4] = f.d2;
-        sw[5] = f.bits;
+        sw[1] = f.col;
+        sw[2] = f.d01;
+        sw[3] = f.d2;
+        sw[4] = f.bits;
+    }
+    pw3_gscan_range(S, G, wr, a, b, f, e, kGsSpec, nullptr, nullptr);
+    if (lane == 0) {
+        sw[0] = e;
+        sw[5] = f.col;
+        sw[6] = f.d01;
+        sw[7] = f.d2;
+        sw[8] = f.bits;
     }
 }
 
-// phase 2: one warp walks the segments in order with the true incoming features, each up to its
-// first item that replaces the word in both scans
+// phase 2: one warp walks the segments in order with the true incoming features; 32 segments' data
+// are loaded at once, one per lane
 extern "C" __global__ void pw3_k_gscan_walk(PwParams P) {
     const PawcsDev& S = P.streams[0];
     PawcsCtl* pc = S.pc;
@@ -557,22 +563,45 @@ extern "C" __global__ void pw3_k_gscan_walk(PwParams P) {
     f.bits = pc->gw_bits[wr];
     uint32_t e = 0;
     const int nseg = (int)((n + kPw3Seg - 1) / kPw3Seg);
-    for (int s = 0; s < nseg; ++s) {
-        uint32_t* sw = pw3_segw(S, s);
-        const uint32_t a = (uint32_t)s * kPw3Seg, b = min(n, a + (uint32_t)kPw3Seg);
-        uint32_t syncIdx = kPwNone, offset = 0;
-        pw3_gscan_range(S, G, wr, a, b, f, e, sw[0] != kPwNone, &syncIdx, &offset);
-        if (syncIdx != kPwNone) {
-            // the rest of the segment follows the speculative scan
-            e = sw[1] + offset;
-            f.col = sw[2];
-            f.d01 = sw[3];
-            f.d2 = sw[4];
-            f.bits = sw[5];
+    for (int s0 = 0; s0 < nseg; s0 += 32) {
+        const int sl = s0 + lane;
+        uint32_t v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if (sl < nseg) {
+            const uint32_t* sw = pw3_segw(S, sl);
+#pragma unroll
+            for (int j = 0; j < 9; ++j) v[j] = sw[j];
         }
-        if (lane == 0) {
-            sw[6] = offset;
-            sw[7] = syncIdx;
+        const int cnt = min(32, nseg - s0);
+        for (int k = 0; k < cnt; ++k) {
+            const int s = s0 + k;
+            uint32_t w[9];
+#pragma unroll
+            for (int j = 0; j < 9; ++j) w[j] = __shfl_sync(0xffffffffu, v[j], k);
+            uint32_t mode, val, sync = kPwNone;
+            if (w[1] == f.col && w[2] == f.d01 && w[3] == f.d2 && w[4] == f.bits) {
+                mode = 1;  // the speculative scan entered the segment in the true state
+                val = e;
+                e += w[0];
+            } else {
+                mode = 2;
+                const uint32_t a = (uint32_t)s * kPw3Seg, b = min(n, a + (uint32_t)kPw3Seg);
+                uint32_t offset = 0;
+                pw3_gscan_range(S, G, wr, a, b, f, e, kGsRescan, &sync, &offset);
+                val = offset;
+                if (sync != kPwNone) e = w[0] + offset;
+            }
+            if (mode == 1 || sync != kPwNone) {
+                f.col = w[5];
+                f.d01 = w[6];
+                f.d2 = w[7];
+                f.bits = w[8];
+            }
+            if (lane == 0) {
+                uint32_t* sw = pw3_segw(S, s);
+                sw[9] = mode;
+                sw[10] = val;
+                sw[11] = sync;
+            }
         }
     }
     if (lane == 0) {
@@ -584,15 +613,16 @@ extern "C" __global__ void pw3_k_gscan_walk(PwParams P) {
     }
 }
 
-// phase 3: the epoch shift of the items after each segment's synchronization item
+// phase 3: the outcomes of the kept segments, and of the rescanned ones after their synchronization
 extern "C" __global__ void __launch_bounds__(256) pw3_k_gscan_fix(PwParams P) {
     const PawcsDev& S = P.streams[0];
     const uint32_t n = S.catInfo[0];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t* sw = pw3_segw(S, (int)(i / kPw3Seg));
-    if (sw[7] == kPwNone || i <= sw[7]) return;
-    S.out[S.itemList[2 * i].x].epoch += sw[6];
+    if (sw[9] == 2u && (sw[11] == kPwNone || i <= sw[11])) return;
+    const Pw3Item it = pw3_item(S, i);
+    pw3_set_out(S, it.p, it.specWord, (it.specEpoch & 0x7fffffffu) + sw[10], it.specEpoch >> 31);
 }
 
 // pixels rerun next round: an earlier updater in the 5x5 window whose loop inputs changed this
