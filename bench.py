@@ -314,6 +314,8 @@ def main():
                     help="measured span of the serving workload run (0: skip)")
     ap.add_argument("--single-frames", type=int, default=100,
                     help="frames of the single-stream SuBSENSE configs 0 and 1 (0: skip)")
+    ap.add_argument("--pawcs-channels", default="both", choices=["1", "3", "both"],
+                    help="PAWCS legs: the single-channel scene (config 2), the BGR scene, or both")
     ap.add_argument("--pawcs-only", action="store_true",
                     help="run the PAWCS workload alone and print its object (profiling)")
     args = ap.parse_args()
@@ -324,8 +326,11 @@ def main():
         torch.cuda.set_device(0)
         stream = torch.cuda.Stream()
         torch.cuda.set_stream(stream)
-        out = pawcs_run(args.pawcs_frames, stream, cpu=not args.no_cpu_baseline)
-        out["bgr"] = pawcs_run(min(args.pawcs_frames, 100), stream, cpu=not args.no_cpu_baseline, channels=3)
+        out = {}
+        if args.pawcs_channels != "3":
+            out = pawcs_run(args.pawcs_frames, stream, cpu=not args.no_cpu_baseline)
+        if args.pawcs_channels != "1":
+            out["bgr"] = pawcs_run(min(args.pawcs_frames, 100), stream, cpu=not args.no_cpu_baseline, channels=3)
         print(json.dumps(out))
         return
 

@@ -44,7 +44,6 @@ extern "C" __global__ void lvbgs_lbsp_dense(const uint8_t* img, int W, int H, in
 extern "C" __global__ void pw_k_local(PwParams P);
 extern "C" __global__ void pw_k_illum(PwParams P);
 extern "C" __global__ void pw_k_items(PwParams P);
-extern "C" __global__ void pw_k_gscan(PwParams P);
 extern "C" __global__ void pw_k_cells(PwParams P, int final);
 extern "C" __global__ void pw_k_nbr(PwParams P);
 extern "C" __global__ void pw_k_replace(PwParams P);
@@ -64,7 +63,7 @@ extern "C" __global__ void pw_k_reset_decide(PwParams P);
 extern "C" __global__ void pw_k_motion_bg(PwParams P, int buf);
 extern "C" __global__ void pw_k_motion_decide(PwParams P);
 extern "C" __global__ void pw_k_compact_count(PwParams P, int mode);
-extern "C" __global__ void pw_k_compact_offsets(PwParams P);
+extern "C" __global__ void pw_k_compact_offsets(PwParams P, int ncat);
 extern "C" __global__ void pw_k_compact_scatter(PwParams P, int mode);
 extern "C" __global__ void pw_k_close(PwParams P);
 extern "C" __global__ void pw_k_refresh_local(PawcsDev S, uint32_t t, int buf, int baseOcc, float decr, int force,
@@ -578,7 +577,7 @@ PwLayout pw_layout(int W, int H, int C, int L, int G) {
     sz[PL_REPB] = sz[PL_REPA] = npx * 4;
     sz[PL_UFINAL] = npx;
     sz[PL_UV] = npx;
-    sz[PL_ITEMLIST] = npx * 16 * (C == 3 ? 2 : 1);
+    sz[PL_ITEMLIST] = npx * 32;
     sz[PL_CONTRIBLIST] = npx * 4;
     // ordered-compaction counts; also the three-channel global scan's per-segment scratch (16 words
     // per 512 items)
@@ -864,7 +863,8 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
     // ordered compaction: mode 0 lists the critical global items, mode 1 the word weight contributions
     auto compact = [&](int mode) {
         pw_k_compact_count<<<cblocks, 256, 0, st>>>(P, mode);
-        pw_k_compact_offsets<<<1, 1024, 0, st>>>(P);
+        const int ncat = mode == 1 ? h->pd.G : 1;
+        pw_k_compact_offsets<<<1, 32 * std::min(ncat, 32), 0, st>>>(P, ncat);
         pw_k_compact_scatter<<<cblocks, 256, 0, st>>>(P, mode);
     };
     const bool c3 = h->C == 3;
@@ -890,7 +890,9 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
             pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
             pw_k_items<<<tiles, blk, 0, st>>>(P);
             compact(0);
-            pw_k_gscan<<<1, 32, 0, st>>>(P);
+            pw3_k_gscan_seg<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
+            pw3_k_gscan_walk<<<1, 32, 0, st>>>(P);
+            pw3_k_gscan_fix<<<(int)((h->npx + 255) / 256), 256, 0, st>>>(P);
             pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
             pw_k_nbr<<<tiles, blk, 0, st>>>(P);
             compact(2);

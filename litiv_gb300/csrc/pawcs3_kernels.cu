@@ -386,7 +386,7 @@ extern "C" __global__ void __launch_bounds__(256) pw3_k_items(PwParams P) {
 }
 
 // ------------------------------------------------------------------------------------------
-// ordered scan of the critical items (:1127-1150), three channels, segment-parallel. The scan's state
+// ordered scan of the critical items (:776-786 one channel, :1139-1150 three), segment-parallel. The scan's state
 // is only the replaceable word's features (those of its last replacement), and two scans that both see
 // an item replace the word agree from there on. So each segment of kPw3Seg items is scanned by its
 // own warp from kPw3Warm items before its start, from a guessed state (the first of those items'
@@ -425,7 +425,10 @@ __device__ __forceinline__ Pw3Item pw3_item_of(const uint4 a, const uint4 b) {
 __device__ __forceinline__ Pw3Item pw3_item(const PawcsDev& S, uint32_t i) {
     return pw3_item_of(S.itemList[2 * i], S.itemList[2 * i + 1]);
 }
-__device__ __forceinline__ bool pw3_gmatch(const Pw3Item& it, const Pw3GFeat& f) {
+// an item matches the replaceable word: one channel (:776-777) colour distance and descriptor bits;
+// three (:1141-1142) descriptor bits and the mixed colour distance
+__device__ __forceinline__ bool pw3_gmatch(const Pw3Item& it, const Pw3GFeat& f, bool c3) {
+    if (!c3) return pw_absdiff(it.col, f.col) <= it.cthr && pw_absdiff(it.bits, f.bits) <= it.dq;
     return pw_absdiff(it.bits, f.bits) <= it.dq && pw3_cmix(it.col, f.col) <= it.cthr;
 }
 __device__ __forceinline__ void pw3_set_out(const PawcsDev& S, uint32_t p, uint32_t word, uint32_t epoch, uint32_t repl) {
@@ -442,7 +445,7 @@ constexpr int kPw3SegWords = 16;
 __device__ __forceinline__ uint32_t* pw3_segw(const PawcsDev& S, int s) { return S.blkCounts + (size_t)s * kPw3SegWords; }
 
 enum { kGsDry = 0, kGsSpec = 1, kGsRescan = 2 };
-// the serial warp scan of items [a, b) from features f and epoch e (pw_k_gscan's chunk loop).
+// the serial warp scan of items [a, b) from features f and epoch e, 32 items at a time.
 // kGsDry: no outcome written (warm-up); kGsSpec: outcomes into the item records; kGsRescan: outcomes
 // into the pixels, stopping at the first item that replaces the word both here and in the speculative
 // scan (*syncIdx, kPwNone: none), *offset being the epoch shift of the later items.
@@ -460,7 +463,7 @@ __device__ void pw3_gscan_range(const PawcsDev& S, int G, int wr, uint32_t a, ui
         int cursor = 0, last = cnt - 1;
         bool synced = false;
         while (cursor < cnt) {
-            const bool mWr = pw3_gmatch(it, f);
+            const bool mWr = pw3_gmatch(it, f, S.sd.C == 3);
             const bool repl = valid && !mWr && (int)it.fixedPos >= G && it.evRep;
             const unsigned cand = __ballot_sync(0xffffffffu, repl && lane >= cursor);
             const int stop = cand ? __ffs(cand) - 1 : cnt;

@@ -116,8 +116,9 @@ struct PawcsDev {
     uint8_t* dsRoi;            // down-sampled ROI of the frame-level analysis
     uint8_t* dsFrame;          // down-sampled frame
     uint8_t* uv;               // illumination-update outcomes of the local pass: bit0 mask zero, bit1 non-zero
-    uint4* itemList;           // critical global items in raster order: pixel, colour|bits|fixed pos|fixed word,
-                               // colour threshold|descriptor-bits threshold, descriptor|event flags
+    uint4* itemList;           // critical global items in raster order, two records each: pixel, colour|bits << 24,
+                               // colour threshold|descriptor-bits threshold << 16, descriptors 0-1; descriptor 2|
+                               // event flags << 16, fixed position|fixed word << 8, speculative word and epoch
     float* contribList;        // word weight contributions, word-major, raster order within a word
     uint32_t* blkCounts;       // ordered compaction: per block and category counts, then offsets
     uint32_t* catInfo;         // [0..16] category totals, [32..48] category bases

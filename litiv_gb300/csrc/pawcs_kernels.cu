@@ -356,14 +356,16 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_compact_count(PwParams P,
     if (threadIdx.x < kPwCats) S.blkCounts[(size_t)blockIdx.x * kPwCats + threadIdx.x] = cnt[threadIdx.x];
 }
 
-// per category (one warp each, 32 warps): exclusive offsets over the blocks (in place), totals and
-// the category bases of the word-major list
-extern "C" __global__ void __launch_bounds__(1024) pw_k_compact_offsets(PwParams P) {
+// per category (one warp each): exclusive offsets over the blocks (in place), totals and the category
+// bases of the word-major list; the compaction uses categories [0, ncat), the others are left empty
+extern "C" __global__ void __launch_bounds__(1024) pw_k_compact_offsets(PwParams P, int ncat) {
     const PawcsDev& S = P.streams[0];
     const int nb = (S.sd.npx + kPwCompactBlk - 1) / kPwCompactBlk;
     __shared__ uint32_t tot[kPwCats];
     const int lane = threadIdx.x & 31;
-    for (int c = threadIdx.x >> 5; c < kPwCats; c += 32) {
+    for (int i = threadIdx.x; i < kPwCats; i += blockDim.x) tot[i] = 0;
+    __syncthreads();
+    for (int c = threadIdx.x >> 5; c < ncat; c += blockDim.x >> 5) {
         uint32_t run = 0;
         for (int b0 = 0; b0 < nb; b0 += 32) {
             const int b = b0 + lane;
@@ -378,15 +380,13 @@ extern "C" __global__ void __launch_bounds__(1024) pw_k_compact_offsets(PwParams
             if (b < nb) *e = run + inc - v;
             run += __shfl_sync(0xffffffffu, inc, 31);
         }
-        if (lane == 0) {
-            tot[c] = run;
-            S.catInfo[c] = run;
-        }
+        if (lane == 0) tot[c] = run;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t base = 0;
         for (int k = 0; k < kPwCats; ++k) {
+            S.catInfo[k] = tot[k];
             S.catInfo[kPwCatBase + k] = base;
             base += tot[k];
         }
@@ -430,28 +430,22 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_compact_scatter(PwParams 
         __syncthreads();
         if (c >= 0) {
             const uint32_t pos = run[c] + warpCnt[w][c] + rank;
-            if (mode == 0 && D.C == 3) {
-                // three channels: two records per item (pixel, colour|bits, thresholds, descriptors 0-1;
-                // descriptor 2|event flags, fixed position|word)
+            if (mode == 0) {
+                // two records per item (pixel, colour|bits, thresholds, descriptors 0-1; descriptor 2|event
+                // flags, fixed position|word, and the global scan's speculative outcome)
                 const PwRec& R = S.rec[p];
-                const PwThr th = pw3_thresholds(fm[FM_R * D.npx + p], S.unstable[p], S.minColor, S.descOff);
+                const bool c3 = D.C == 3;
+                const PwThr th = c3 ? pw3_thresholds(fm[FM_R * D.npx + p], S.unstable[p], S.minColor, S.descOff)
+                                    : pw_thresholds(fm[FM_R * D.npx + p], S.unstable[p], S.minColor, S.descOff);
                 const uint32_t g = S.gitem[p];
-                const uint16_t* dt = S.descT + (size_t)p * 3;
-                const uint32_t a = pw3_color(D.frame, p) | ((uint32_t)R.bits << 24);
+                const uint16_t* dt = S.descT + (size_t)p * (c3 ? 3 : 1);
+                const uint32_t a = (c3 ? pw3_color(D.frame, p) : (uint32_t)D.frame[p]) | ((uint32_t)R.bits << 24);
                 const uint32_t b = min(th.color, 65535u) | (min(th.desc / 4u, 65535u) << 16);
-                S.itemList[2 * pos] = make_uint4((uint32_t)p, a, b, (uint32_t)dt[0] | ((uint32_t)dt[1] << 16));
-                S.itemList[2 * pos + 1] =
-                    make_uint4((uint32_t)dt[2] | ((uint32_t)(R.flags & (kRfEvent | kRfRepDraw)) << 16),
-                               ((g >> 6) & 63u) | ((g & 63u) << 8), 0u, 0u);
-            } else if (mode == 0) {
-                const PwRec& R = S.rec[p];
-                const PwThr th = pw_thresholds(fm[FM_R * D.npx + p], S.unstable[p], S.minColor, S.descOff);
-                const uint32_t g = S.gitem[p];
-                const uint32_t a = (uint32_t)D.frame[p] | ((uint32_t)R.bits << 8) | (((g >> 6) & 63u) << 16) |
-                                   ((g & 63u) << 24);
-                const uint32_t b = min(th.color, 65535u) | (min(th.desc / 4u, 65535u) << 16);
-                const uint32_t d = (uint32_t)S.descT[p] | ((uint32_t)(R.flags & (kRfEvent | kRfRepDraw)) << 16);
-                S.itemList[pos] = make_uint4((uint32_t)p, a, b, d);
+                const uint32_t d01 = c3 ? (uint32_t)dt[0] | ((uint32_t)dt[1] << 16) : (uint32_t)dt[0];
+                const uint32_t d2 = c3 ? (uint32_t)dt[2] : 0u;
+                S.itemList[2 * pos] = make_uint4((uint32_t)p, a, b, d01);
+                S.itemList[2 * pos + 1] = make_uint4(d2 | ((uint32_t)(R.flags & (kRfEvent | kRfRepDraw)) << 16),
+                                                     ((g >> 6) & 63u) | ((g & 63u) << 8), 0u, 0u);
             } else if (mode == 2) {
                 S.updList[pos] = (uint32_t)p;
             } else {
@@ -461,70 +455,6 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_compact_scatter(PwParams 
         __syncthreads();
         if (threadIdx.x < ncat) run[threadIdx.x] += passTot[threadIdx.x];
         __syncthreads();
-    }
-}
-
-// ordered scan of the items that depend on the replaceable word (one warp per stream): the
-// replaceable word's features change with each replacement (:776-786). Each chunk of 32 items is
-// settled in parallel against the current features up to the first item that replaces the word,
-// which then becomes the features the rest of the chunk is matched against.
-extern "C" __global__ void pw_k_gscan(PwParams P) {
-    const int si = blockIdx.x;
-    if (si >= P.nStreams) return;
-    const PawcsDev& S = P.streams[si];
-    PawcsCtl* pc = S.pc;
-    const int lane = threadIdx.x;
-    const int G = S.G;
-    const int wr = pc->gdict[G - 1];
-    uint32_t wrColor = pc->gw_color[wr], wrDesc = pc->gw_desc[wr], wrBits = pc->gw_bits[wr];
-    uint32_t epoch = 0;
-    const uint32_t n = S.catInfo[0];
-    uint4 nextIt = lane < (int)n ? S.itemList[lane] : make_uint4(0, 0, 0, 0);
-    for (uint32_t base = 0; base < n; base += 32) {
-        const uint4 it = nextIt;
-        if (base + 32 + lane < n) nextIt = S.itemList[base + 32 + lane];  // prefetch the next chunk
-        const int cnt = (int)min(32u, n - base);
-        const bool valid = lane < cnt;
-        const uint32_t col = it.y & 255u, bits = (it.y >> 8) & 255u, fixedPos = (it.y >> 16) & 255u;
-        const uint32_t fixedWord = it.y >> 24, cthr = it.z & 65535u, dq = it.z >> 16;
-        const bool evRep = ((it.w >> 16) & kRfEvent) && ((it.w >> 16) & kRfRepDraw);
-        uint32_t myWord = kPwNone, myEpoch = 0, myRepl = 0;
-        int cursor = 0;
-        while (cursor < cnt) {
-            const bool mWr = pw_absdiff(wrColor, col) <= cthr && pw_absdiff(bits, wrBits) <= dq;
-            const bool repl = valid && !mWr && (int)fixedPos >= G && evRep;
-            const unsigned cand = __ballot_sync(0xffffffffu, repl && lane >= cursor);
-            const int stop = cand ? __ffs(cand) - 1 : cnt;  // the first replacing item, or the chunk end
-            if (lane >= cursor && lane < stop) {
-                myWord = mWr ? (uint32_t)wr : ((int)fixedPos < G ? fixedWord : kPwNone);
-                myEpoch = epoch;
-            }
-            if (stop < cnt) {
-                ++epoch;
-                if (lane == stop) {
-                    myWord = (uint32_t)wr;
-                    myEpoch = epoch;
-                    myRepl = 1;
-                }
-                wrColor = __shfl_sync(0xffffffffu, col, stop);
-                wrDesc = __shfl_sync(0xffffffffu, it.w & 65535u, stop);
-                wrBits = __shfl_sync(0xffffffffu, bits, stop);
-            }
-            cursor = stop + 1;
-        }
-        if (valid) {
-            PwOut& O = S.out[it.x];
-            O.gword = myWord;
-            O.epoch = myEpoch;
-            if (myRepl) O.gflags |= 1;
-        }
-    }
-    if (lane == 0) {
-        pc->wr_color = wrColor;
-        pc->wr_desc = wrDesc;
-        pc->wr_desc2 = 0u;
-        pc->wr_bits = wrBits;
-        pc->n_repl = epoch;
     }
 }
 
