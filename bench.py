@@ -261,13 +261,14 @@ def serving_run(seconds):
     from litiv_gb300 import serving
     r = serving.simulate(duration_s=seconds, warmup_s=3.0, render_threads=8, seed=1)
     keep = ["window_s", "frames", "mpix_per_s", "frames_per_s", "offered_mpix_per_s", "p50_ms", "p90_ms", "p99_ms",
-            "max_ms", "admit_wait_p50_ms", "admit_wait_p99_ms", "pawcs_frames", "pawcs_p50_ms", "pawcs_p99_ms",
+            "max_ms", "admit_wait_p50_ms", "admit_wait_p99_ms", "subsense_p50_ms", "subsense_p99_ms", "pawcs_frames",
+            "pawcs_p50_ms", "pawcs_p99_ms",
             "mean_live", "mean_resident", "mean_tick_streams", "gpu_busy_frac", "ticks", "arrivals", "admitted",
             "rejected", "dropped", "spills", "restores", "late_frames", "peak_live", "peak_device_bytes", "status"]
     out = {k: r[k] for k in keep}
     out["workload"] = ("SuBSENSE/PAWCS mixed: Poisson arrivals 4/s (max 256 live), lives U[10,60] s, 30 fps, "
                        "320x240/640x480/1280x720/1920x1080 at .3/.3/.3/.1, 1/4 single-channel, 2.5 % of the streams "
-                       "(either channel count) on PAWCS, frames of PAWCS streams on 2 PAWCS lanes beside the "
+                       "(either channel count) on PAWCS, frames of PAWCS streams on 1 PAWCS lane (lowest stream priority) beside the "
                        "batched SuBSENSE ticks; stationary start; latency = submit -> mask in pinned host memory")
     return out
 

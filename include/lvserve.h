@@ -44,7 +44,9 @@ typedef struct {
     int max_queue;                  /* queued frames per stream before lvserve_submit answers LVBGS_BUSY; 8 */
     double idle_spill_ms;           /* a stream idle this long may be spilled to make room; 500 */
     int max_inflight;               /* ticks in flight, 1..LVBGS_BATCH_MAX_INFLIGHT; 2 */
-    int pawcs_lanes;                /* host threads running PAWCS frame steps beside the batched ticks; 2 */
+    int pawcs_lanes;                /* host threads running PAWCS frame steps (and creating / destroying
+                                       PAWCS handles) beside the batched ticks, on streams of the lowest
+                                       priority (the ticks: the highest); 1 */
 } lvserve_config;
 
 typedef struct {
@@ -130,6 +132,7 @@ typedef struct {
     double admit_wait_p50_ms, admit_wait_p99_ms; /* open -> admitted */
     double pawcs_p50_ms, pawcs_p99_ms;           /* latency of the PAWCS streams' frames */
     uint64_t pawcs_frames;                       /* PAWCS frames finished in the window */
+    double subsense_p50_ms, subsense_p99_ms;     /* latency of the SuBSENSE streams' frames (batched ticks) */
     double mean_live, mean_resident, mean_tick_streams, gpu_busy_frac;
     uint64_t ticks, arrivals, admitted, rejected, dropped, spills, restores, late_frames;
     int peak_live;

@@ -90,7 +90,7 @@ class SimResult(C.Structure):
                 ("p90_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double),
                 ("admit_wait_p50_ms", C.c_double), ("admit_wait_p99_ms", C.c_double),
                 ("pawcs_p50_ms", C.c_double), ("pawcs_p99_ms", C.c_double), ("pawcs_frames", C.c_uint64),
-                ("mean_live", C.c_double),
+                ("subsense_p50_ms", C.c_double), ("subsense_p99_ms", C.c_double), ("mean_live", C.c_double),
                 ("mean_resident", C.c_double), ("mean_tick_streams", C.c_double), ("gpu_busy_frac", C.c_double),
                 ("ticks", C.c_uint64), ("arrivals", C.c_uint64), ("admitted", C.c_uint64),
                 ("rejected", C.c_uint64), ("dropped", C.c_uint64), ("spills", C.c_uint64),

@@ -44,7 +44,9 @@ struct Req {
     Clock::time_point t0;
 };
 
-enum { S_RESIDENT = 0, S_WAITING = 1, S_SPILLED = 2, S_CLOSED = 3 };
+// S_INIT: a PAWCS stream admitted (its bytes reserved) whose handle a PAWCS lane is creating;
+// reported as S_WAITING
+enum { S_RESIDENT = 0, S_WAITING = 1, S_SPILLED = 2, S_CLOSED = 3, S_INIT = 4 };
 
 struct SStream {
     int id = 0;
@@ -56,6 +58,7 @@ struct SStream {
     lvbgs_handle h = nullptr;
     std::deque<Req> q;
     bool inFlight = false, closing = false, failed = false;
+    bool laneDestroy = false;  // PAWCS: a lane destroys the handle (freeing memory waits for the device)
     size_t bytes = 0;       // accounted device bytes while resident
     size_t stateBytes = 0;  // size of the spill image
     void* spill = nullptr;
@@ -250,7 +253,7 @@ void destroy_stream(lvserve_ctx* s, SStream* x) {
     if (x->h) lvbgs_destroy(x->h);
     x->h = nullptr;
     std::lock_guard<std::mutex> lk(s->mu);
-    if (x->state == S_RESIDENT && x->bytes) s->used -= x->bytes;
+    if ((x->state == S_RESIDENT || x->state == S_INIT) && x->bytes) s->used -= x->bytes;
     if (x->state == S_SPILLED) s->hostSpilled -= x->stateBytes;
     if (x->spill) s->pinnedFree.emplace(x->spillCap, x->spill);
     x->spill = nullptr;
@@ -272,8 +275,14 @@ void housekeeping(lvserve_ctx* s) {
         for (auto& kv : s->streams) {
             SStream* x = kv.second.get();
             if (s->stop && x->state == S_WAITING) fail_queue(s, x, LVBGS_BUSY);  // shutting down: no admission
-            if (x->closing && x->q.empty() && !x->inFlight) closing.push_back(x);
-            else if (x->state == S_SPILLED && !x->q.empty()) restore.push_back(x);
+            if (x->closing && x->q.empty() && !x->inFlight) {
+                // PAWCS handles are destroyed on a PAWCS lane, so that the device-wide wait of freeing
+                // their memory does not hold the ticks back
+                if (x->algo == LVBGS_ALGO_PAWCS && x->h) x->laneDestroy = true;
+                else closing.push_back(x);
+            } else if (x->state == S_SPILLED && !x->q.empty()) {
+                restore.push_back(x);
+            }
         }
         std::sort(restore.begin(), restore.end(),
                   [](const SStream* a, const SStream* b) { return a->q.front().t0 < b->q.front().t0; });
@@ -309,6 +318,17 @@ void housekeeping(lvserve_ctx* s) {
             x = s->admitQ.front();
         }
         if (!make_room(s, x->bytes, x)) break;  // first come, first served
+        if (x->algo == LVBGS_ALGO_PAWCS) {
+            // created and initialized on a PAWCS lane: refreshModel over every pixel (tens of ms for a
+            // 1080p BGR stream) would hold the ticks back
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->admitQ.pop_front();
+            x->state = S_INIT;
+            s->used += x->bytes;
+            s->st.peak_device_bytes = std::max(s->st.peak_device_bytes, s->used);
+            s->cvWork.notify_all();
+            continue;
+        }
         lvbgs_handle h = nullptr;
         lvbgs_status r = lvbgs_create(x->algo, &x->prm, &h);
         if (r == LVBGS_OK)
@@ -416,11 +436,67 @@ bool launch(lvserve_ctx* s, std::vector<lvbgs_handle>& hs, std::vector<lvbgs_fra
 // submission order (one in flight per stream), so its results are those of the stream alone.
 void pawcs_lane(lvserve_ctx* s) {
     cudaSetDevice(s->cfg.device_id);
+    // the lane's frames run on a stream of the lowest priority: when the blocks of a PAWCS kernel
+    // drain, the ticks' pending blocks (highest priority) are scheduled first, so a PAWCS stream
+    // that costs more than the device can give (a 1080p BGR stream at 30 fps) queues its own frames
+    // instead of delaying the batched ones
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    cudaStream_t lst = nullptr;
+    if (cudaStreamCreateWithPriority(&lst, cudaStreamNonBlocking, least) != cudaSuccess) {
+        cudaGetLastError();
+        lst = nullptr;  // the handle's own stream
+    }
     for (;;) {
         SStream* x = nullptr;
         Req r;
         {
             std::unique_lock<std::mutex> lk(s->mu);
+            // handle destruction and creation first (claimed with inFlight)
+            SStream* job = nullptr;
+            for (auto& kv : s->streams) {
+                SStream* y = kv.second.get();
+                if (y->algo != LVBGS_ALGO_PAWCS || y->inFlight) continue;
+                if (y->laneDestroy || (y->state == S_INIT && !y->closing)) {
+                    job = y;
+                    break;
+                }
+            }
+            if (job) {
+                job->inFlight = true;
+                lk.unlock();
+                if (job->laneDestroy) {
+                    destroy_stream(s, job);
+                } else {
+                    lvbgs_handle h = nullptr;
+                    lvbgs_status rc = lvbgs_create(job->algo, &job->prm, &h);
+                    if (rc == LVBGS_OK)
+                        rc = lvbgs_initialize(h, job->init.data(), job->W, job->H, job->C, 0,
+                                              job->roi.empty() ? nullptr : job->roi.data());
+                    std::lock_guard<std::mutex> lk2(s->mu);
+                    job->inFlight = false;
+                    if (rc != LVBGS_OK) {
+                        s->err = lvbgs_last_error(h);
+                        if (h) lvbgs_destroy(h);
+                        s->used -= job->bytes;
+                        job->failed = true;
+                        job->state = S_CLOSED;
+                        fail_queue(s, job, rc);
+                        job->closing = true;
+                    } else {
+                        job->h = h;
+                        job->state = S_RESIDENT;
+                        job->init.clear();
+                        job->init.shrink_to_fit();
+                        job->lastActive = Clock::now();
+                        ++s->st.admitted;
+                        if (s->onAdmit) s->onAdmit(*job, job->lastActive);
+                    }
+                }
+                s->cvDone.notify_all();
+                s->cvWork.notify_all();
+                continue;
+            }
             for (auto& kv : s->streams) {
                 SStream* y = kv.second.get();
                 if (y->algo != LVBGS_ALGO_PAWCS || y->state != S_RESIDENT || y->inFlight || y->q.empty() || y->failed)
@@ -439,7 +515,7 @@ void pawcs_lane(lvserve_ctx* s) {
             if (s->inflightN == 0) s->busySince = Clock::now();
             ++s->inflightN;
         }
-        const lvbgs_status st = lvbgs_apply(x->h, r.img, r.stride, r.mask, r.lr, nullptr);
+        const lvbgs_status st = lvbgs_apply(x->h, r.img, r.stride, r.mask, r.lr, lst);
         const Clock::time_point now = Clock::now();
         {
             std::lock_guard<std::mutex> lk(s->mu);
@@ -463,6 +539,10 @@ void pawcs_lane(lvserve_ctx* s) {
         }
         s->cvDone.notify_all();
         s->cvWork.notify_all();
+    }
+    if (lst) {
+        cudaStreamSynchronize(lst);
+        cudaStreamDestroy(lst);
     }
 }
 
@@ -490,7 +570,7 @@ extern "C" {
 
 lvbgs_status lvserve_default_config(lvserve_config* out) {
     if (!out) return LVBGS_BAD_ARG;
-    *out = lvserve_config{0, 0, 0, 256, 8, 500.0, 2, 2};
+    *out = lvserve_config{0, 0, 0, 256, 8, 500.0, 2, 1};
     return LVBGS_OK;
 }
 
@@ -518,7 +598,10 @@ lvbgs_status lvserve_create(const lvserve_config* cfg, lvserve_handle* out) {
     // with PAWCS lanes, the ticks share the device: the cooperative repair grid takes half of the
     // co-resident blocks so that it can start beside the lanes' kernels
     if (c.pawcs_lanes > 0) lvbgs_batch_set_repair_share(s->batch, 2);
-    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    // the ticks run on a stream of the highest priority (the PAWCS lanes on the lowest)
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (cudaStreamCreateWithPriority(&s->stream, cudaStreamNonBlocking, greatest) != cudaSuccess) {
         lvbgs_batch_destroy(s->batch);
         return LVBGS_DEVICE_ERROR;
     }
@@ -707,7 +790,8 @@ int lvserve_stream_state(lvserve_handle s, int id) {
     if (!s) return S_CLOSED;
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->streams.find(id);
-    return it == s->streams.end() ? S_CLOSED : it->second->state;
+    if (it == s->streams.end()) return S_CLOSED;
+    return it->second->state == S_INIT ? S_WAITING : it->second->state;
 }
 
 const char* lvserve_last_error(lvserve_handle s) {
@@ -866,7 +950,7 @@ lvbgs_status lvserve_simulate(const lvserve_config* cfg, const lvserve_sim_confi
     Slabs slabs;
     const int K = sim.pool_frames;
     // latency records of frames submitted in the measured window (guarded by the server's mutex)
-    std::vector<double> lat, admitWait, pawcsLat;
+    std::vector<double> lat, admitWait, pawcsLat, subLat;
     uint64_t donePx = 0, doneFrames = 0, pawcsFrames = 0;
     int firstErr = 0;
     Clock::time_point T0;
@@ -883,6 +967,7 @@ lvbgs_status lvserve_simulate(const lvserve_config* cfg, const lvserve_sim_confi
         if (in_window(r.t0)) {
             lat.push_back(ms_between(r.t0, now));
             if (x.algo == LVBGS_ALGO_PAWCS) pawcsLat.push_back(ms_between(r.t0, now));
+            else subLat.push_back(ms_between(r.t0, now));
         }
         if (in_window(now)) {
             donePx += x.npx();
@@ -1054,6 +1139,8 @@ lvbgs_status lvserve_simulate(const lvserve_config* cfg, const lvserve_sim_confi
         out->pawcs_p50_ms = quantile(pawcsLat, 0.50);
         out->pawcs_p99_ms = quantile(pawcsLat, 0.99);
         out->pawcs_frames = pawcsFrames;
+        out->subsense_p50_ms = quantile(subLat, 0.50);
+        out->subsense_p99_ms = quantile(subLat, 0.99);
         out->status = firstErr;
     }
     out->offered_mpix_per_s = (double)offeredPx / 1e6 / sim.duration_s;

@@ -19,7 +19,7 @@ GiB = 1 << 30
 
 def test_default_config_and_workload():
     cfg = serving.default_config()
-    assert (cfg.max_live, cfg.max_queue, cfg.max_inflight, cfg.pawcs_lanes) == (256, 8, 2, 2)
+    assert (cfg.max_live, cfg.max_queue, cfg.max_inflight, cfg.pawcs_lanes) == (256, 8, 2, 1)
     assert cfg.idle_spill_ms == 500.0
     sim = serving.default_sim_config()
     # Poisson arrivals at 4 streams/s, lives U[10, 60] s, 30 fps, resolution mix .3/.3/.3/.1
