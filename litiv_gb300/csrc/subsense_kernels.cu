@@ -1130,13 +1130,43 @@ __device__ void phaseF_tile(const TickParams& P, const StreamDev& S, int lt, uin
             }
             ++nw;
         };
+        // the writes targeting q, in raster order of their writers, packed 12 bits each (window slot,
+        // sample index, own write) into a register list, then executed by the warp together: a write
+        // body per list position instead of one per window slot that any lane uses. More than five
+        // writes (rare) take the slot loop.
+        unsigned long long wlist = 0;
+        int nwr = 0;
 #pragma unroll
         for (int k = 0; k < 25; ++k) {
             const int dy = k / 5 - 2, dx = k % 5 - 2;
             const uint32_t w = it[(ly + 2 + dy) * IW + lx + 2 + dx];
-            if (k == 12 && (w & kInValid) && (w & kInOwn)) commit_write(q, (int)in_sown(w));
-            if ((w & kNbMask) == (kInValid | ((uint32_t)(24 - k) << kInCodeShift) | (1u << kInNStShift)))
-                commit_write((y + dy) * W + (x + dx), (int)in_snb(w));
+            if (k == 12 && (w & kInValid) && (w & kInOwn)) {
+                if (nwr < 5) wlist |= (unsigned long long)(2048u | (12u << 6) | in_sown(w)) << (12 * nwr);
+                ++nwr;
+            }
+            if ((w & kNbMask) == (kInValid | ((uint32_t)(24 - k) << kInCodeShift) | (1u << kInNStShift))) {
+                if (nwr < 5) wlist |= (unsigned long long)(((uint32_t)k << 6) | in_snb(w)) << (12 * nwr);
+                ++nwr;
+            }
+        }
+        const int nconv = nwr <= 5 ? nwr : 0;
+        const int iters = __reduce_max_sync(__activemask(), (unsigned)nconv);
+        for (int j = 0; j < iters; ++j) {
+            if (j < nconv) {
+                const uint32_t e = (uint32_t)(wlist >> (12 * j)) & 0xfffu;
+                const int k = (int)((e >> 6) & 31u), sidx = (int)(e & 63u);
+                const int p = (e & 2048u) ? q : (y + k / 5 - 2) * W + (x + k % 5 - 2);
+                commit_write(p, sidx);
+            }
+        }
+        if (nwr > 5) {
+            for (int k = 0; k < 25; ++k) {
+                const int dy = k / 5 - 2, dx = k % 5 - 2;
+                const uint32_t w = it[(ly + 2 + dy) * IW + lx + 2 + dx];
+                if (k == 12 && (w & kInValid) && (w & kInOwn)) commit_write(q, (int)in_sown(w));
+                if ((w & kNbMask) == (kInValid | ((uint32_t)(24 - k) << kInCodeShift) | (1u << kInNStShift)))
+                    commit_write((y + dy) * W + (x + dx), (int)in_snb(w));
+            }
         }
         const uint32_t wq = it[(ly + 2) * IW + lx + 2];
         uint16_t kend = 0;
