@@ -177,10 +177,13 @@ def pawcs_run(n_frames, stream, cpu=True, channels=1):
             rounds.append(b.scalars()["fixed_point_rounds"])
         b.close()
         m = np.array(ms[9:])
+        med = float(np.percentile(m, 50))
         r = {"value": W * H / (m.mean() / 1e3) / 1e6, "unit": "Mpix/s", "frames_per_s": 1e3 / m.mean(),
-             "ms_per_frame": float(m.mean()), "p50_frame_ms": float(np.percentile(m, 50)),
+             "ms_per_frame": float(m.mean()), "p50_frame_ms": med,
              "p99_frame_ms": float(np.percentile(m, 99)), "rounds_mean": float(np.mean(rounds)),
-             "rounds_max": int(np.max(rounds))}
+             "rounds_max": int(np.max(rounds)),
+             # frames (index, ms, fixed-point rounds) that took more than three times the median
+             "slow_frames": [[t + 1, round(v, 2), int(rounds[t])] for t, v in enumerate(ms) if t >= 9 and v > 3 * med]}
         if leg == "device":
             out.update(r)
         else:
