@@ -173,6 +173,7 @@ struct TickWork {
     unsigned long long ts[40];  // %globaltimer after each grid barrier (CTA 0), for the phase profile
     unsigned int nts, anyReset;  // anyReset: some stream refreshes its model this frame
     unsigned int lcount, pad;    // long sample scans deferred by the evaluation (list in rlist[0..1])
+    unsigned int fetchD[2], fetchR[2];  // repair: next item of each phase, by round parity (warp fetches)
 };
 
 // error codes reported in TickWork::err

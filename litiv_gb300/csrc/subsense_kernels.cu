@@ -1771,29 +1771,50 @@ extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_repair(TickParams
             w->rematched += nItems;
             if (iter < 16) w->phase_ctr[iter] = nItems;
         }
-        const unsigned int nth = gridDim.x * blockDim.x;
-        for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < nItems; i += nth) {
-            const unsigned long long item = __ldcg(&P.dlist[par][i]);
-            const int si = (int)(item >> 40), q = (int)(item & 0xffffffffffull);
-            const StreamDev& S = P.streams[si];
-            const uint32_t stampNext = S.ctl->stamp_base + (uint32_t)iter + 2u;
-            const bool counted = S.C == 3 ? rematch_item<3>(P, si, S, q, stampNext, par)
-                                          : rematch_item<1>(P, si, S, q, stampNext, par);
-            // re-match statistics: one atomic per stream among the lanes here
-            const unsigned am = __activemask();
-            const unsigned grp = __match_any_sync(am, counted ? si : -1 - (int)(threadIdx.x & 31));
-            if (counted && (int)(threadIdx.x & 31) == __ffs(grp) - 1)
-                atomicAdd(&S.ctl->st_rematched, (unsigned long long)__popc(grp));
+        // items are fetched 32 at a time by each warp from a counter (not strided): per-item costs
+        // vary widely, and every round waits for its slowest thread at the grid barrier
+        const int lane = threadIdx.x & 31;
+        for (;;) {
+            unsigned int base = 0;
+            if (lane == 0) base = atomicAdd(&w->fetchD[par], 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= nItems) break;
+            const unsigned int i = base + lane;
+            if (i < nItems) {
+                const unsigned long long item = __ldcg(&P.dlist[par][i]);
+                const int si = (int)(item >> 40), q = (int)(item & 0xffffffffffull);
+                const StreamDev& S = P.streams[si];
+                const uint32_t stampNext = S.ctl->stamp_base + (uint32_t)iter + 2u;
+                const bool counted = S.C == 3 ? rematch_item<3>(P, si, S, q, stampNext, par)
+                                              : rematch_item<1>(P, si, S, q, stampNext, par);
+                // re-match statistics: one atomic per stream among the lanes here
+                const unsigned am = __activemask();
+                const unsigned grp = __match_any_sync(am, counted ? si : -1 - (int)(threadIdx.x & 31));
+                if (counted && (int)(threadIdx.x & 31) == __ffs(grp) - 1)
+                    atomicAdd(&S.ctl->st_rematched, (unsigned long long)__popc(grp));
+            }
         }
         if (!grid_sync(w)) return;
         const unsigned int nr0 = ld_volatile(&w->rcount[par]);
         const unsigned int nr = nr0 < P.listCap ? nr0 : P.listCap;
-        if (blockIdx.x == 0 && threadIdx.x == 0) w->dcount[par] = 0u;
-        for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < nr; i += nth) {
-            const unsigned long long item = __ldcg(&P.rlist[par][i]);
-            const int si = (int)(item >> 40), p = (int)(item & 0xffffffffffull);
-            const StreamDev& S = P.streams[si];
-            reresolve_item(P, si, S, p, S.ctl->stamp_base + (uint32_t)iter + 2u, par);
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            w->dcount[par] = 0u;
+            // the next round's counters (last used a round ago; visible after the next barrier)
+            w->fetchD[par ^ 1] = 0u;
+            w->fetchR[par ^ 1] = 0u;
+        }
+        for (;;) {
+            unsigned int base = 0;
+            if (lane == 0) base = atomicAdd(&w->fetchR[par], 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= nr) break;
+            const unsigned int i = base + lane;
+            if (i < nr) {
+                const unsigned long long item = __ldcg(&P.rlist[par][i]);
+                const int si = (int)(item >> 40), p = (int)(item & 0xffffffffffull);
+                const StreamDev& S = P.streams[si];
+                reresolve_item(P, si, S, p, S.ctl->stamp_base + (uint32_t)iter + 2u, par);
+            }
         }
         if (!grid_sync(w)) return;
         ++iter;
