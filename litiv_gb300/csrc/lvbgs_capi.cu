@@ -79,6 +79,7 @@ extern "C" __global__ void pw3_k_items(PwParams P);
 extern "C" __global__ void pw3_k_gscan_seg(PwParams P);
 extern "C" __global__ void pw3_k_gscan_walk(PwParams P);
 extern "C" __global__ void pw3_k_gscan_fix(PwParams P);
+extern "C" __global__ void pw3_k_gscan_fix_walked(PwParams P);
 extern "C" __global__ void pw3_k_dirty(PwParams P);
 extern "C" __global__ void pw3_k_later(PwParams P);
 extern "C" __global__ void pw3_k_commit(PwParams P);
@@ -543,7 +544,7 @@ enum {
     PL_GMAP, PL_DSLT, PL_DSST, PL_DSROI,
     // scratch (not part of the model)
     PL_BITS, PL_HCOUNT, PL_LABEL, PL_INTENT, PL_DESCT, PL_REC, PL_OUT, PL_REPB, PL_REPA, PL_UFINAL, PL_UV,
-    PL_ITEMLIST, PL_CONTRIBLIST, PL_BLKCOUNTS, PL_CATINFO, PL_DSABS, PL_UPDLIST, PL_GITEM, PL_CONTRIB, PL_DSFRAME, PL_FRAME, PL_MASK, PL_ROWSUM, PL_WORK, PL_FLAGS, PL_PDEV, PL_SDEV, PL_DIRTY, PL_COUNT
+    PL_ITEMLIST, PL_CONTRIBLIST, PL_BLKCOUNTS, PL_CATINFO, PL_DSABS, PL_UPDLIST, PL_GITEM, PL_CONTRIB, PL_DSFRAME, PL_FRAME, PL_MASK, PL_ROWSUM, PL_WORK, PL_FLAGS, PL_PDEV, PL_SDEV, PL_DIRTY, PL_GSEG, PL_GCAND, PL_GTRUE, PL_COUNT
 };
 struct PwLayout {
     size_t off[PL_COUNT];
@@ -579,9 +580,7 @@ PwLayout pw_layout(int W, int H, int C, int L, int G) {
     sz[PL_UV] = npx;
     sz[PL_ITEMLIST] = npx * 32;
     sz[PL_CONTRIBLIST] = npx * 4;
-    // ordered-compaction counts; also the three-channel global scan's per-segment scratch (16 words
-    // per 512 items)
-    sz[PL_BLKCOUNTS] = std::max(((npx + kPwCompactBlk - 1) / kPwCompactBlk) * kPwCats * 4, (npx / 512 + 1) * 16 * 4);
+    sz[PL_BLKCOUNTS] = ((npx + kPwCompactBlk - 1) / kPwCompactBlk) * kPwCats * 4;
     sz[PL_CATINFO] = 2 * kPwCatBase * 4;
     sz[PL_DSABS] = std::max<size_t>(nds, 1) * 4;
     sz[PL_UPDLIST] = npx * 4;
@@ -596,6 +595,9 @@ PwLayout pw_layout(int W, int H, int C, int L, int G) {
     sz[PL_PDEV] = sizeof(PawcsDev);
     sz[PL_SDEV] = sizeof(StreamDev);
     sz[PL_DIRTY] = npx;
+    sz[PL_GSEG] = (npx / 512 + 2) * 24 * 4;
+    sz[PL_GCAND] = npx * 4;
+    sz[PL_GTRUE] = npx;
     PwLayout Lo;
     size_t o = 0;
     for (int i = 0; i < PL_COUNT; ++i) {
@@ -700,6 +702,9 @@ void pw_fill(lvbgs_ctx* h, const PwLayout& Lo, int L, int G) {
     D.dsRoi = b + Lo.off[PL_DSROI];
     D.dsFrame = b + Lo.off[PL_DSFRAME];
     D.dirty = b + Lo.off[PL_DIRTY];
+    D.gseg = (uint32_t*)(b + Lo.off[PL_GSEG]);
+    D.gcand = (uint32_t*)(b + Lo.off[PL_GCAND]);
+    D.gtrue = b + Lo.off[PL_GTRUE];
     h->d_rowsum = (double*)(b + Lo.off[PL_ROWSUM]);
     h->d_work = (TickWork*)(b + Lo.off[PL_WORK]);
     h->d_flags = (unsigned int*)(b + Lo.off[PL_FLAGS]);
@@ -881,6 +886,7 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
             pw3_k_gscan_seg<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
             pw3_k_gscan_walk<<<1, 32, 0, st>>>(P);
             pw3_k_gscan_fix<<<(int)((h->npx + 255) / 256), 256, 0, st>>>(P);
+            pw3_k_gscan_fix_walked<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
             pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
             pw_k_nbr<<<tiles, blk, 0, st>>>(P);
             LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 4, st), "flag reset");
@@ -893,6 +899,7 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
             pw3_k_gscan_seg<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
             pw3_k_gscan_walk<<<1, 32, 0, st>>>(P);
             pw3_k_gscan_fix<<<(int)((h->npx + 255) / 256), 256, 0, st>>>(P);
+            pw3_k_gscan_fix_walked<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
             pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
             pw_k_nbr<<<tiles, blk, 0, st>>>(P);
             compact(2);

@@ -386,14 +386,16 @@ extern "C" __global__ void __launch_bounds__(256) pw3_k_items(PwParams P) {
 }
 
 // ------------------------------------------------------------------------------------------
-// ordered scan of the critical items (:776-786 one channel, :1139-1150 three), segment-parallel. The scan's state
-// is only the replaceable word's features (those of its last replacement), and two scans that both see
-// an item replace the word agree from there on. So each segment of kPw3Seg items is scanned by its
+// ordered scan of the critical items (:776-786 one channel, :1139-1150 three), segment-parallel. The
+// scan's state is only the replaceable word's features (those of its last replacement), only
+// candidates (events with the replacement draw and no fixed match) can replace it, and two scans that
+// both see an item replace it agree from there on. So each segment of kPw3Seg items is scanned by its
 // own warp from kPw3Warm items before its start, from a guessed state (the first of those items'
 // features): with replacements frequent, the scan reaches the segment in the true state. One warp
 // then walks the segments in order: a segment whose speculative state at its start equals the true
-// incoming features keeps its speculative outcomes (one comparison); otherwise it is rescanned up to
-// its first item that replaces the word in both scans. A last parallel pass writes the outcomes.
+// incoming features keeps its speculative outcomes (one comparison); otherwise its candidates are
+// visited up to the first one that replaces the word in both scans. Last, the outcomes: one thread per
+// item from the speculative scan, and a warp per walked segment for its walked items.
 // Records: two uint4 per item (pixel, colour|bits, thresholds, descriptors 0-1; descriptor 2|event
 // flags, fixed position|word, speculative word, speculative epoch | replaced << 31).
 // ------------------------------------------------------------------------------------------
@@ -437,34 +439,30 @@ __device__ __forceinline__ void pw3_set_out(const PawcsDev& S, uint32_t p, uint3
     O.epoch = epoch;
     O.gflags = (uint8_t)((O.gflags & ~1u) | repl);
 }
-// per-segment scratch (in blkCounts, free between the ordered compaction and the next round):
-// [0] replacements of the speculative scan in the segment, [1..4] its state at the segment's start,
-// [5..8] its state at the end; from the walk: [9] mode (1 kept, 2 rescanned), [10] epoch base (mode 1)
-// or shift (mode 2), [11] synchronization item (mode 2; kPwNone: none)
-constexpr int kPw3SegWords = 16;
-__device__ __forceinline__ uint32_t* pw3_segw(const PawcsDev& S, int s) { return S.blkCounts + (size_t)s * kPw3SegWords; }
+// per-segment scratch (PawcsDev::gseg, kPw3SegWords words a segment): [0] replacements of the
+// speculative scan in the segment, [1..4] its state at the segment's start, [5..8] its state at the
+// end, [9] candidates of the segment (listed in gcand from the segment's first item on); from the
+// walk: [10] mode (1 kept, 2 walked), [11] true epoch at the segment's start, [12] synchronization
+// item (kPwNone: none), [13] epoch shift after it, [14..17] true incoming features
+constexpr int kPw3SegWords = 24;
+__device__ __forceinline__ uint32_t* pw3_segw(const PawcsDev& S, int s) { return S.gseg + (size_t)s * kPw3SegWords; }
+__device__ __forceinline__ bool pw3_is_cand(const Pw3Item& it, int G) { return (int)it.fixedPos >= G && it.evRep; }
 
-enum { kGsDry = 0, kGsSpec = 1, kGsRescan = 2 };
-// the serial warp scan of items [a, b) from features f and epoch e, 32 items at a time.
-// kGsDry: no outcome written (warm-up); kGsSpec: outcomes into the item records; kGsRescan: outcomes
-// into the pixels, stopping at the first item that replaces the word both here and in the speculative
-// scan (*syncIdx, kPwNone: none), *offset being the epoch shift of the later items.
+// the speculative warp scan of items [a, b) from features f and epoch e, 32 items at a time;
+// spec = false: a warm-up (nothing written), true: outcomes into the item records
 __device__ void pw3_gscan_range(const PawcsDev& S, int G, int wr, uint32_t a, uint32_t b, Pw3GFeat& f, uint32_t& e,
-                                int mode, uint32_t* syncIdx, uint32_t* offset) {
+                                bool spec) {
     const int lane = threadIdx.x & 31;
-    if (syncIdx) *syncIdx = kPwNone;
+    const bool c3 = S.sd.C == 3;
     for (uint32_t base = a; base < b; base += 32) {
         const int cnt = (int)min(32u, b - base);
         const bool valid = lane < cnt;
-        Pw3Item it;
-        if (valid) it = pw3_item(S, base + lane);
-        else it = pw3_item_of(make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0));
+        const Pw3Item it = valid ? pw3_item(S, base + lane) : pw3_item_of(make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0));
         uint32_t myWord = kPwNone, myEpoch = 0, myRepl = 0;
-        int cursor = 0, last = cnt - 1;
-        bool synced = false;
+        int cursor = 0;
         while (cursor < cnt) {
-            const bool mWr = pw3_gmatch(it, f, S.sd.C == 3);
-            const bool repl = valid && !mWr && (int)it.fixedPos >= G && it.evRep;
+            const bool mWr = pw3_gmatch(it, f, c3);
+            const bool repl = valid && !mWr && pw3_is_cand(it, G);
             const unsigned cand = __ballot_sync(0xffffffffu, repl && lane >= cursor);
             const int stop = cand ? __ffs(cand) - 1 : cnt;
             if (lane >= cursor && lane < stop) {
@@ -482,30 +480,19 @@ __device__ void pw3_gscan_range(const PawcsDev& S, int G, int wr, uint32_t a, ui
                 f.d01 = __shfl_sync(0xffffffffu, it.d01, stop);
                 f.d2 = __shfl_sync(0xffffffffu, it.d2, stop);
                 f.bits = __shfl_sync(0xffffffffu, it.bits, stop);
-                if (mode == kGsRescan && (__shfl_sync(0xffffffffu, it.specEpoch, stop) >> 31)) {
-                    *syncIdx = base + (uint32_t)stop;
-                    *offset = e - (__shfl_sync(0xffffffffu, it.specEpoch, stop) & 0x7fffffffu);
-                    last = stop;
-                    synced = true;
-                    break;
-                }
             }
             cursor = stop + 1;
         }
-        if (valid && lane <= last) {
-            if (mode == kGsRescan) {
-                pw3_set_out(S, it.p, myWord, myEpoch, myRepl);
-            } else if (mode == kGsSpec) {
-                uint4& r = S.itemList[2 * (base + lane) + 1];
-                r.z = myWord;
-                r.w = myEpoch | (myRepl << 31);
-            }
+        if (spec && valid) {
+            uint4& r = S.itemList[2 * (base + lane) + 1];
+            r.z = myWord;
+            r.w = myEpoch | (myRepl << 31);
         }
-        if (synced) return;
     }
 }
 
-// phase 1: one warp per segment, from a guessed state kPw3Warm items before the segment
+// phase 1: one warp per segment: its candidates listed, then its speculative scan from a guessed
+// state kPw3Warm items before it
 extern "C" __global__ void __launch_bounds__(128) pw3_k_gscan_seg(PwParams P) {
     const PawcsDev& S = P.streams[0];
     const uint32_t n = S.catInfo[0];
@@ -517,6 +504,13 @@ extern "C" __global__ void __launch_bounds__(128) pw3_k_gscan_seg(PwParams P) {
     const int G = S.G;
     const int wr = pc->gdict[G - 1];
     uint32_t* sw = pw3_segw(S, s);
+    uint32_t nc = 0;
+    for (uint32_t base = a; base < b; base += 32) {
+        const bool cand = base + lane < b && pw3_is_cand(pw3_item(S, base + lane), G);
+        const unsigned m = __ballot_sync(0xffffffffu, cand);
+        if (cand) S.gcand[a + nc + (uint32_t)__popc(m & ((1u << lane) - 1u))] = base + (uint32_t)lane;
+        nc += (uint32_t)__popc(m);
+    }
     Pw3GFeat f;
     uint32_t e = 0;
     if (a == 0) {
@@ -531,7 +525,7 @@ extern "C" __global__ void __launch_bounds__(128) pw3_k_gscan_seg(PwParams P) {
         f.d01 = g.d01;
         f.d2 = g.d2;
         f.bits = g.bits;
-        pw3_gscan_range(S, G, wr, w0 + 1, a, f, e, kGsDry, nullptr, nullptr);
+        pw3_gscan_range(S, G, wr, w0 + 1, a, f, e, false);
         e = 0;
     }
     if (lane == 0) {
@@ -539,8 +533,9 @@ extern "C" __global__ void __launch_bounds__(128) pw3_k_gscan_seg(PwParams P) {
         sw[2] = f.d01;
         sw[3] = f.d2;
         sw[4] = f.bits;
+        sw[9] = nc;
     }
-    pw3_gscan_range(S, G, wr, a, b, f, e, kGsSpec, nullptr, nullptr);
+    pw3_gscan_range(S, G, wr, a, b, f, e, true);
     if (lane == 0) {
         sw[0] = e;
         sw[5] = f.col;
@@ -550,8 +545,10 @@ extern "C" __global__ void __launch_bounds__(128) pw3_k_gscan_seg(PwParams P) {
     }
 }
 
-// phase 2: one warp walks the segments in order with the true incoming features; 32 segments' data
-// are loaded at once, one per lane
+// phase 2: one warp walks the segments in order with the true features. A segment whose speculative
+// state at its start equals them is kept; otherwise only its candidates are visited (no other item
+// changes the state), up to the first one that replaces the word in both scans, their true outcome
+// marked in gtrue
 extern "C" __global__ void pw3_k_gscan_walk(PwParams P) {
     const PawcsDev& S = P.streams[0];
     PawcsCtl* pc = S.pc;
@@ -559,6 +556,7 @@ extern "C" __global__ void pw3_k_gscan_walk(PwParams P) {
     const uint32_t n = S.catInfo[0];
     const int G = S.G;
     const int wr = pc->gdict[G - 1];
+    const bool c3 = S.sd.C == 3;
     Pw3GFeat f;
     f.col = pc->gw_color[wr];
     f.d01 = pc->gw_desc[wr];
@@ -568,42 +566,79 @@ extern "C" __global__ void pw3_k_gscan_walk(PwParams P) {
     const int nseg = (int)((n + kPw3Seg - 1) / kPw3Seg);
     for (int s0 = 0; s0 < nseg; s0 += 32) {
         const int sl = s0 + lane;
-        uint32_t v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        uint32_t v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         if (sl < nseg) {
             const uint32_t* sw = pw3_segw(S, sl);
 #pragma unroll
-            for (int j = 0; j < 9; ++j) v[j] = sw[j];
+            for (int j = 0; j < 10; ++j) v[j] = sw[j];
         }
         const int cnt = min(32, nseg - s0);
         for (int k = 0; k < cnt; ++k) {
             const int s = s0 + k;
-            uint32_t w[9];
+            uint32_t w[10];
 #pragma unroll
-            for (int j = 0; j < 9; ++j) w[j] = __shfl_sync(0xffffffffu, v[j], k);
-            uint32_t mode, val, sync = kPwNone;
+            for (int j = 0; j < 10; ++j) w[j] = __shfl_sync(0xffffffffu, v[j], k);
+            const Pw3GFeat fin = f;
+            const uint32_t ein = e;
+            uint32_t mode, sync = kPwNone, offset = 0;
             if (w[1] == f.col && w[2] == f.d01 && w[3] == f.d2 && w[4] == f.bits) {
                 mode = 1;  // the speculative scan entered the segment in the true state
-                val = e;
                 e += w[0];
-            } else {
-                mode = 2;
-                const uint32_t a = (uint32_t)s * kPw3Seg, b = min(n, a + (uint32_t)kPw3Seg);
-                uint32_t offset = 0;
-                pw3_gscan_range(S, G, wr, a, b, f, e, kGsRescan, &sync, &offset);
-                val = offset;
-                if (sync != kPwNone) e = w[0] + offset;
-            }
-            if (mode == 1 || sync != kPwNone) {
                 f.col = w[5];
                 f.d01 = w[6];
                 f.d2 = w[7];
                 f.bits = w[8];
+            } else {
+                mode = 2;
+                const uint32_t a = (uint32_t)s * kPw3Seg, nc = w[9];
+                for (uint32_t base = 0; base < nc && sync == kPwNone; base += 32) {
+                    const int cn = (int)min(32u, nc - base);
+                    const bool valid = lane < cn;
+                    const uint32_t ci = valid ? S.gcand[a + base + lane] : 0u;
+                    const Pw3Item it = valid ? pw3_item(S, ci) : pw3_item_of(make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0));
+                    uint32_t mine = 0;
+                    int cursor = 0, last = cn - 1;
+                    while (cursor < cn) {
+                        const bool repl = valid && !pw3_gmatch(it, f, c3);
+                        const unsigned cm = __ballot_sync(0xffffffffu, repl && lane >= cursor);
+                        const int stop = cm ? __ffs(cm) - 1 : cn;
+                        if (stop < cn) {
+                            ++e;
+                            if (lane == stop) mine = 1;
+                            f.col = __shfl_sync(0xffffffffu, it.col, stop);
+                            f.d01 = __shfl_sync(0xffffffffu, it.d01, stop);
+                            f.d2 = __shfl_sync(0xffffffffu, it.d2, stop);
+                            f.bits = __shfl_sync(0xffffffffu, it.bits, stop);
+                            const uint32_t se = __shfl_sync(0xffffffffu, it.specEpoch, stop);
+                            if (se >> 31) {
+                                sync = __shfl_sync(0xffffffffu, ci, stop);
+                                offset = e - (se & 0x7fffffffu);
+                                last = stop;
+                                break;
+                            }
+                        }
+                        cursor = stop + 1;
+                    }
+                    if (valid && lane <= last) S.gtrue[ci] = (uint8_t)mine;
+                }
+                if (sync != kPwNone) {
+                    e = w[0] + offset;
+                    f.col = w[5];
+                    f.d01 = w[6];
+                    f.d2 = w[7];
+                    f.bits = w[8];
+                }
             }
             if (lane == 0) {
                 uint32_t* sw = pw3_segw(S, s);
-                sw[9] = mode;
-                sw[10] = val;
-                sw[11] = sync;
+                sw[10] = mode;
+                sw[11] = ein;
+                sw[12] = sync;
+                sw[13] = offset;
+                sw[14] = fin.col;
+                sw[15] = fin.d01;
+                sw[16] = fin.d2;
+                sw[17] = fin.bits;
             }
         }
     }
@@ -616,16 +651,74 @@ extern "C" __global__ void pw3_k_gscan_walk(PwParams P) {
     }
 }
 
-// phase 3: the outcomes of the kept segments, and of the rescanned ones after their synchronization
+// phase 3a: one thread per item: the kept segments and the items after a synchronization, from the
+// speculative scan (epochs shifted); the walked items are left to phase 3b
 extern "C" __global__ void __launch_bounds__(256) pw3_k_gscan_fix(PwParams P) {
     const PawcsDev& S = P.streams[0];
     const uint32_t n = S.catInfo[0];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t* sw = pw3_segw(S, (int)(i / kPw3Seg));
-    if (sw[9] == 2u && (sw[11] == kPwNone || i <= sw[11])) return;
+    const uint32_t mode = sw[10], sync = sw[12];
+    if (mode == 2 && (sync == kPwNone || i <= sync)) return;
+    const uint32_t shift = mode == 1 ? sw[11] : sw[13];
     const Pw3Item it = pw3_item(S, i);
-    pw3_set_out(S, it.p, it.specWord, (it.specEpoch & 0x7fffffffu) + sw[10], it.specEpoch >> 31);
+    pw3_set_out(S, it.p, it.specWord, (it.specEpoch & 0x7fffffffu) + shift, it.specEpoch >> 31);
+}
+
+// phase 3b: one warp per walked segment, its items up to the synchronization (or all): from the true
+// replacers, with warp prefixes of the last replacer and of the replacement count
+extern "C" __global__ void __launch_bounds__(128) pw3_k_gscan_fix_walked(PwParams P) {
+    const PawcsDev& S = P.streams[0];
+    const uint32_t n = S.catInfo[0];
+    const int s = blockIdx.x * 4 + (int)(threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const uint32_t a = (uint32_t)s * kPw3Seg;
+    if (a >= n) return;
+    const uint32_t* sw = pw3_segw(S, s);
+    if (sw[10] != 2u) return;
+    const uint32_t b = min(n, a + (uint32_t)kPw3Seg);
+    const uint32_t end = sw[12] == kPwNone ? b : sw[12] + 1;
+    const int G = S.G;
+    const int wr = S.pc->gdict[G - 1];
+    const bool c3 = S.sd.C == 3;
+    Pw3GFeat f;
+    f.col = sw[14];
+    f.d01 = sw[15];
+    f.d2 = sw[16];
+    f.bits = sw[17];
+    uint32_t e = sw[11];
+    for (uint32_t base = a; base < end; base += 32) {
+        const uint32_t i = base + lane;
+        const bool valid = i < end;
+        const Pw3Item it = valid ? pw3_item(S, i) : pw3_item_of(make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0));
+        const bool rep = valid && pw3_is_cand(it, G) && S.gtrue[i] != 0;
+        const unsigned m = __ballot_sync(0xffffffffu, rep);
+        const unsigned below = m & ((1u << lane) - 1u);
+        Pw3GFeat g = f;
+        const int src = below ? 31 - __clz(below) : 0;
+        const uint32_t gc = __shfl_sync(0xffffffffu, it.col, src), g01 = __shfl_sync(0xffffffffu, it.d01, src);
+        const uint32_t g2 = __shfl_sync(0xffffffffu, it.d2, src), gb = __shfl_sync(0xffffffffu, it.bits, src);
+        if (below) {
+            g.col = gc;
+            g.d01 = g01;
+            g.d2 = g2;
+            g.bits = gb;
+        }
+        if (rep) {
+            pw3_set_out(S, it.p, (uint32_t)wr, e + (uint32_t)__popc(below) + 1u, 1u);
+        } else if (valid) {
+            const uint32_t word = pw3_gmatch(it, g, c3) ? (uint32_t)wr : ((int)it.fixedPos < G ? it.fixedWord : kPwNone);
+            pw3_set_out(S, it.p, word, e + (uint32_t)__popc(below), 0u);
+        }
+        if (m) {
+            const int top = 31 - __clz(m);
+            f.col = __shfl_sync(0xffffffffu, it.col, top);
+            f.d01 = __shfl_sync(0xffffffffu, it.d01, top);
+            f.d2 = __shfl_sync(0xffffffffu, it.d2, top);
+            f.bits = __shfl_sync(0xffffffffu, it.bits, top);
+            e += (uint32_t)__popc(m);
+        }
+    }
 }
 
 // pixels rerun next round: an earlier updater in the 5x5 window whose loop inputs changed this

@@ -125,6 +125,9 @@ struct PawcsDev {
     float* dsAbs;              // |LT - ST| per down-sampled pixel (0 outside the down-sampled ROI)
     uint32_t* updList;         // pixels that update a neighbour this round, raster order
     uint8_t* dirty;            // three channels: pixels whose local pass reruns next round
+    uint32_t* gseg;            // global-word scan: per-segment state (pawcs3_kernels.cu)
+    uint32_t* gcand;           // global-word scan: candidate items, listed per segment
+    uint8_t* gtrue;            // global-word scan: walked candidates that replace the word
 };
 
 constexpr int kPwCompactBlk = 1024;  // pixels per block of the ordered compactions
