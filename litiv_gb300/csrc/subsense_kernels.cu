@@ -661,11 +661,7 @@ __device__ void phaseA_tile(const TickParams& P, int si, const StreamDev& S, int
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = S.ctl->lut[i];
     const long rowBytes = (long)S.W * C;
     const long b0 = (long)(x0 - kBorder) * C - 2;  // frame byte of tile column 0
-#ifdef LV_AB_BYTE_TILE
-    const bool wordPath = false;
-#else
     const bool wordPath = (rowBytes & 3) == 0 && (((uintptr_t)S.frame) & 3) == 0;
-#endif
     for (int i = threadIdx.x; i < NWORDS * RH; i += blockDim.x) {
         const int r = i / NWORDS, wi = i % NWORDS;
         const int gy = y0 - kBorder + r;
