@@ -78,6 +78,18 @@ def test_state_bytes_accounts_for_the_model(product_lib):
     assert product_lib.lvbgs_state_bytes(L.ALGO_SUBSENSE, 0, 240, 3, 50) == 0
 
 
+def test_pawcs_state_bytes_for_one_and_three_channels(product_lib):
+    # 640x480: 25 local words (one channel) or 50 (three), each double-buffered with colour,
+    # descriptor and three 32-bit counters; four-channel frames are not a PAWCS input
+    npx = 640 * 480
+    b1 = product_lib.lvbgs_state_bytes(L.ALGO_PAWCS, 640, 480, 1, 0)
+    b3 = product_lib.lvbgs_state_bytes(L.ALGO_PAWCS, 640, 480, 3, 0)
+    assert b1 >= npx * 2 * 25 * (1 + 2 + 12)
+    assert b3 >= npx * 2 * 50 * (3 + 6 + 12)
+    assert product_lib.lvbgs_device_bytes(L.ALGO_PAWCS, 640, 480, 3, 0) > b3
+    assert product_lib.lvbgs_state_bytes(L.ALGO_PAWCS, 640, 480, 4, 0) == 0
+
+
 def test_synthetic_presets_and_determinism(product_lib):
     from litiv_gb300 import SyntheticStream
     s = SyntheticStream(0, seed=1)
