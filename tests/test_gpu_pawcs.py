@@ -287,3 +287,22 @@ def test_three_channel_moving_camera_mode_switch():
         if t in (499, 500, 999, 1000):
             modes[t] = gpu.scalars()["using_moving_camera"]
     assert modes[499] == 0 and modes[500] == 1, modes
+
+
+def test_three_channel_set_roi_reinitializes_from_background():
+    # setROI re-initializes from the three-channel background image with the new ROI
+    fr = _bgr(14, 58, 96, 72)
+    gpu, ora = BackgroundSubtractorPAWCS(seed=19), pyoracle.OraclePAWCS(seed=19)
+    gpu.initialize(fr[0])
+    ora.initialize(fr[0])
+    for f in fr[1:6]:
+        assert np.array_equal(gpu.apply(f), ora.apply(f, 0.0))
+    yy, xx = np.mgrid[0:72, 0:96]
+    roi = ((((xx - 48) / 40.0) ** 2 + ((yy - 36) / 30.0) ** 2) <= 1.0).astype(np.uint8) * 255
+    gpu.setROI(roi)
+    ora.set_roi(roi)
+    bad = compare_state(gpu, ora)
+    assert not bad, "after setROI: " + "; ".join(bad)
+    for f in fr[6:]:
+        assert np.array_equal(gpu.apply(f), ora.apply(f, 0.0))
+    assert not compare_state(gpu, ora)
