@@ -43,7 +43,6 @@ extern "C" __global__ void lvbgs_lbsp_dense(const uint8_t* img, int W, int H, in
 // PAWCS (pawcs_kernels.cu)
 extern "C" __global__ void pw_k_local(PwParams P);
 extern "C" __global__ void pw_k_illum(PwParams P);
-extern "C" __global__ void pw_k_items(PwParams P);
 extern "C" __global__ void pw_k_cells(PwParams P, int final);
 extern "C" __global__ void pw_k_nbr(PwParams P);
 extern "C" __global__ void pw_k_replace(PwParams P);
@@ -75,7 +74,6 @@ extern "C" __global__ void pw_k_init_last(PawcsDev S, const uint8_t* img);
 extern "C" __global__ void pw_k_background(PawcsDev S, int buf, uint8_t* outCol, uint16_t* outDesc);
 // PAWCS, three channels (pawcs3_kernels.cu)
 extern "C" __global__ void pw3_k_local(PwParams P);
-extern "C" __global__ void pw3_k_items(PwParams P);
 extern "C" __global__ void pw3_k_gscan_seg(PwParams P);
 extern "C" __global__ void pw3_k_gscan_walk(PwParams P);
 extern "C" __global__ void pw3_k_gscan_fix(PwParams P);
@@ -881,7 +879,6 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
             // three channels: the local pass applies the earlier updaters' loops itself
             pw3_k_local<<<tiles, blk, 0, st>>>(P);
             pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
-            pw3_k_items<<<tiles, blk, 0, st>>>(P);
             compact(0);
             pw3_k_gscan_seg<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
             pw3_k_gscan_walk<<<1, 32, 0, st>>>(P);
@@ -894,7 +891,6 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
         } else {
             pw_k_local<<<tiles, blk, 0, st>>>(P);
             pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
-            pw_k_items<<<tiles, blk, 0, st>>>(P);
             compact(0);
             pw3_k_gscan_seg<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
             pw3_k_gscan_walk<<<1, 32, 0, st>>>(P);

@@ -153,6 +153,8 @@ __device__ void pw3_loop(Pw3Word* wd, int L, const Pw3Upd& u, int boot, unsigned
     }
 }
 
+__device__ void pw3_item_pixel(const PawcsDev& S, int p, const PwRec& R, uint32_t col);
+
 #define PW3_PIXEL_PROLOGUE                                                   \
     const int t0 = blockIdx.x;                                              \
     if (t0 >= P.totalTiles) return;                                         \
@@ -343,18 +345,15 @@ extern "C" __global__ void __launch_bounds__(256) pw3_k_local(PwParams P) {
     R.minDesc = (uint16_t)minDesc;
     R.flags = flags;
     R.bits = (uint8_t)bits;
+    pw3_item_pixel(S, q, R, col);
 }
 
 // ------------------------------------------------------------------------------------------
-// global items (:1127-1150): as pw_k_items with the three-channel match (descriptor bits, then the
-// mixed colour distance)
+// global items (:1127-1150): as pw_item_pixel with the three-channel match (descriptor bits, then the
+// mixed colour distance); run at the end of the pixel's local pass
 // ------------------------------------------------------------------------------------------
-extern "C" __global__ void __launch_bounds__(256) pw3_k_items(PwParams P) {
-    PW3_PIXEL_PROLOGUE
-    if (x >= D.W || y >= D.H) return;
-    const int p = y * D.W + x;
-    if (!D.roi[p]) return;
-    const PwRec& R = S.rec[p];
+__device__ void pw3_item_pixel(const PawcsDev& S, int p, const PwRec& R, uint32_t col) {
+    const StreamDev& D = S.sd;
     PwOut& O = S.out[p];
     O.gflags = 0;
     O.epoch = 0;
@@ -365,7 +364,7 @@ extern "C" __global__ void __launch_bounds__(256) pw3_k_items(PwParams P) {
     const int wr = pc->gdict[G - 1];
     const float* fm = D.fm + (size_t)(D.ctl->frame_idx & 1ull) * kNumFloatMaps * D.npx;
     const PwThr th = pw3_thresholds(fm[FM_R * D.npx + p], S.unstable[p], S.minColor, S.descOff);
-    const uint32_t col = pw3_color(D.frame, p), bits = R.bits;
+    const uint32_t bits = R.bits;
     const uint8_t* lut = S.glut + (size_t)p * kPwGlutStride;
     int fixedPos = G, wrPos = G, fixedWord = -1;
     for (int g = 0; g < G; ++g) {

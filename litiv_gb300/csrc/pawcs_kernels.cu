@@ -50,6 +50,8 @@ __device__ __forceinline__ void pw_word(const PwWordSrc& s, int j, uint32_t& c, 
 // dictionary with the last slot replaced by the latest earlier neighbour update, if any. Writes the
 // scanned dictionary (next-frame buffer, illumination updates not yet applied) and the record.
 // ------------------------------------------------------------------------------------------
+__device__ void pw_item_pixel(const PawcsDev& S, int p, const PwRec& R, uint32_t col);
+
 extern "C" __global__ void __launch_bounds__(256) pw_k_local(PwParams P) {
     const int t0 = blockIdx.x;
     if (t0 >= P.totalTiles) return;
@@ -226,6 +228,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_local(PwParams P) {
     R.m1hi = 0;
     R.flags = flags;
     R.bits = (uint8_t)bits;
+    pw_item_pixel(S, p, R, col);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -270,53 +273,40 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_illum(PwParams P) {
 // global items: a BG pixel's dictionary event or an FG pixel's consultation. The first matching
 // word in the pixel's sort table decides; only the replaceable word (last dictionary slot) changes
 // features during a frame, so an item whose first non-replaceable match precedes the replaceable
-// word is settled here, and the others go to the ordered scan.
+// word is settled here, and the others go to the ordered scan. Run at the end of the pixel's local
+// pass: it depends on nothing else that changes during the frame, so a pixel that does not rerun
+// keeps its item.
 // ------------------------------------------------------------------------------------------
-extern "C" __global__ void __launch_bounds__(256) pw_k_items(PwParams P) {
-    const int t0 = blockIdx.x;
-    if (t0 >= P.totalTiles) return;
-    const PawcsDev& S = P.streams[pw_stream_by_tile(P, t0)];
+__device__ void pw_item_pixel(const PawcsDev& S, int p, const PwRec& R, uint32_t col) {
     const StreamDev& D = S.sd;
-    const int lt = t0 - D.tileBase;
-    const int x = (lt % D.tilesX) * kTileW + (int)threadIdx.x % kTileW;
-    const int y = (lt / D.tilesX) * kTileH + (int)threadIdx.x / kTileW;
-    const bool in = x < D.W && y < D.H;
-    const int p = in ? y * D.W + x : 0;
-    int critical = 0;
-    if (in && D.roi[p]) {
-        const PwRec& R = S.rec[p];
-        PwOut& O = S.out[p];
-        O.gflags = 0;
-        O.epoch = 0;
-        O.gword = kPwNone;
-        if (R.flags & kRfItem) {
-            const PawcsCtl* pc = S.pc;
-            const int G = S.G;
-            const int wr = pc->gdict[G - 1];
-            const float* fm = D.fm + (size_t)(D.ctl->frame_idx & 1ull) * kNumFloatMaps * D.npx;
-            const PwThr th = pw_thresholds(fm[FM_R * D.npx + p], S.unstable[p], S.minColor, S.descOff);
-            const uint32_t col = D.frame[p], bits = R.bits;
-            const uint8_t* lut = S.glut + (size_t)p * kPwGlutStride;
-            int fixedPos = G, wrPos = G, fixedWord = -1;
-            for (int g = 0; g < G; ++g) {
-                const int w = lut[g];
-                if (w == wr) {
-                    wrPos = g;
-                    continue;
-                }
-                if (fixedPos == G && pw_absdiff(pc->gw_color[w], col) <= th.color &&
-                    pw_absdiff(bits, pc->gw_bits[w]) <= th.desc / 4u) {
-                    fixedPos = g;
-                    fixedWord = w;
-                }
-            }
-            critical = wrPos < fixedPos;
-            if (!critical) O.gword = (uint32_t)fixedWord;
-            S.gitem[p] = (uint32_t)(fixedWord < 0 ? 63 : fixedWord) | ((uint32_t)fixedPos << 6) | ((uint32_t)critical << 12);
-            if (critical) O.gflags |= 4;
+    PwOut& O = S.out[p];
+    O.gflags = 0;
+    O.epoch = 0;
+    O.gword = kPwNone;
+    if (!(R.flags & kRfItem)) return;
+    const PawcsCtl* pc = S.pc;
+    const int G = S.G;
+    const int wr = pc->gdict[G - 1];
+    const float* fm = D.fm + (size_t)(D.ctl->frame_idx & 1ull) * kNumFloatMaps * D.npx;
+    const PwThr th = pw_thresholds(fm[FM_R * D.npx + p], S.unstable[p], S.minColor, S.descOff);
+    const uint32_t bits = R.bits;
+    const uint8_t* lut = S.glut + (size_t)p * kPwGlutStride;
+    int fixedPos = G, wrPos = G, fixedWord = -1;
+    for (int g = 0; g < G; ++g) {
+        const int w = lut[g];
+        if (w == wr) {
+            wrPos = g;
+            continue;
+        }
+        if (fixedPos == G && pw_absdiff(pc->gw_color[w], col) <= th.color && pw_absdiff(bits, pc->gw_bits[w]) <= th.desc / 4u) {
+            fixedPos = g;
+            fixedWord = w;
         }
     }
-    (void)critical;
+    const int critical = wrPos < fixedPos;
+    if (!critical) O.gword = (uint32_t)fixedWord;
+    S.gitem[p] = (uint32_t)(fixedWord < 0 ? 63 : fixedWord) | ((uint32_t)fixedPos << 6) | ((uint32_t)critical << 12);
+    if (critical) O.gflags |= 4;
 }
 
 // ------------------------------------------------------------------------------------------
