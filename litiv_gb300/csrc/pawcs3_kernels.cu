@@ -83,8 +83,10 @@ struct Pw3Upd {
     uint32_t p;
 };
 
-// the loop inputs of updater p that do not depend on the round, computed from its own frame-start
-// state (the same values its local pass computes)
+// the loop inputs of updater p, computed from its frame-start state (the same values its local pass
+// computes); its weight threshold comes from the previous round's snapshot (PwOut::thrW, written by
+// pw_k_nbr), and its current descriptor from round 0 (a rerun of p in this round rewrites the same
+// descriptor)
 __device__ __forceinline__ Pw3Upd pw3_updater(const PawcsDev& S, int p, int cur, uint32_t t, double lr) {
     const StreamDev& D = S.sd;
     const float* fm = D.fm + (size_t)cur * kNumFloatMaps * D.npx;
