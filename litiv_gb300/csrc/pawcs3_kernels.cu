@@ -171,7 +171,7 @@ __device__ void pw3_item_pixel(const PawcsDev& S, int p, const PwRec& R, uint32_
 // updaters' loops, in raster order), then its word scan. Writes the scanned dictionary (next-frame
 // buffer; illumination updates as marks) and the record.
 // ------------------------------------------------------------------------------------------
-extern "C" __global__ void __launch_bounds__(256) pw3_k_local(PwParams P) {
+extern "C" __global__ void __launch_bounds__(256, 3) pw3_k_local(PwParams P) {
     PW3_PIXEL_PROLOGUE
     if (x >= D.W || y >= D.H) return;
     const int q = y * D.W + x;
