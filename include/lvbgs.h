@@ -88,8 +88,9 @@ lvbgs_status lvbgs_initialize(lvbgs_handle h, const uint8_t* image, int width, i
 lvbgs_status lvbgs_apply(lvbgs_handle h, const uint8_t* image, size_t stride, uint8_t* fgmask,
                          double learning_rate, void* cuda_stream);
 
-/* Batched frame step: one persistent launch processes one frame of each of the n streams
- * (handles on the same device, all initialized). Results are identical to n separate
+/* Batched frame step: one frame of each of the n streams (handles on the same device, all
+ * initialized) in one sequence of phase kernels over a per-stream descriptor table (15 launches
+ * per group; large batches run as up to four concurrent groups, see lvbgs_set_batch_groups). Results are identical to n separate
  * lvbgs_apply calls. Enqueued on cuda_stream; lvbgs_batch_wait() waits and reports device errors.
  * Host buffers referenced by `frames` must stay valid until the wait returns. */
 /* How lvbgs_batch_apply runs large batches (>= 8 streams and >= 4 Mi pixels): G in 2..4 (default 4)
@@ -166,12 +167,16 @@ lvbgs_status lvbgs_lbsp_compute2(const uint8_t* image, int width, int height, in
 /* Same computation as lvbgs_lbsp_compute2, for callers that must not allocate device memory
  * (a real-time thread with a no-allocation rule, a process held to a fixed GPU memory budget).
  * No counterpart in the reference. It allocates nothing: the image and descriptors are staged in
- * one device array reserved when the library is loaded (24 MiB on every GPU that loads it, kept
- * until the process exits), so width*height*channels may not exceed 8,388,608 (LVBGS_BAD_SIZE
- * otherwise). The first call on a device looks the array up on that device; make that first call
- * before any stream capture. All calls share the one array: calls that overlap on the GPU (from
- * several host threads, or on streams that run concurrently) race and must be serialised by the
- * caller. The call returns after its work on cuda_stream (NULL: the default stream) completed. */
+ * one file-scope device array of 24 MiB, so width*height*channels may not exceed 8,388,608
+ * (LVBGS_BAD_SIZE otherwise). The CUDA runtime reserves that array, and loads the LBSP kernel,
+ * when the library's modules are first used on a device (lazy module loading is the default), so
+ * the FIRST call on a device is the one that may allocate: make it during set-up, before any
+ * stream capture, or run with CUDA_MODULE_LOADING=EAGER. The array then stays on every GPU that
+ * used it until the process exits (or the application resets the device). All calls share the one
+ * array: calls that overlap on the GPU (from several host threads, or on streams that run
+ * concurrently) race and must be serialised by the caller. cuda_stream must belong to device_id
+ * (NULL: the default stream); the call returns after its work there completed, and the caller's
+ * current device is left as it was. */
 lvbgs_status lvbgs_lbsp_compute2_noalloc(const uint8_t* image, int width, int height, int channels,
                                          long abs_threshold, float rel_threshold, size_t offset, uint16_t* desc,
                                          int device_id, void* cuda_stream);

@@ -4,12 +4,14 @@
 // allocates per call. Code that runs where cudaMalloc/cudaFree are off limits -- a real-time
 // capture thread with a no-allocation rule, or a host that shares the GPU under a fixed memory
 // budget -- uses lvbgs_lbsp_compute2_noalloc() instead: the staging lives in one file-scope
-// device array, reserved when the library is loaded, so a call allocates nothing.
+// device array, so a call allocates nothing once the array exists on the device. The CUDA runtime
+// loads a module (and reserves its __device__ arrays) when the module is first used on a device
+// (lazy loading, the default unless CUDA_MODULE_LOADING=EAGER), so the first call on a device --
+// or any earlier use of this library there -- is what reserves the 24 MiB and loads the LBSP
+// kernel; a caller under a no-allocation rule makes that first call during its set-up.
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <mutex>
-#include <vector>
 
 #include "../../include/lvbgs.h"
 #include "lvbgs_internal.h"
@@ -31,22 +33,31 @@ constexpr size_t kScratchBytes = kDescOffset + 2 * kMaxElems;
 
 static __device__ __align__(256) unsigned char g_lbsp_scratch[kScratchBytes];
 
-// device address of g_lbsp_scratch per device, fetched once with that device current
-std::mutex g_mu;
-std::vector<unsigned char*> g_addr;
-
-cudaError_t scratch_address(int device, unsigned char** out) {
-    std::lock_guard<std::mutex> lk(g_mu);
-    if ((int)g_addr.size() <= device) g_addr.resize(device + 1, nullptr);
-    if (!g_addr[device]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_lbsp_scratch);
-        if (e != cudaSuccess) return e;
-        g_addr[device] = (unsigned char*)p;
-    }
-    *out = g_addr[device];
+// Device address of g_lbsp_scratch on the current device. In host code the array's name is only
+// a host-side stand-in, so the address is looked up with the device current. It is looked up on
+// every call (a host-side table lookup once the module is loaded; it allocates nothing), so a
+// cudaDeviceReset() by the application, which unloads the module, leaves no stale address behind.
+cudaError_t scratch_address(unsigned char** out) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_lbsp_scratch);
+    if (e != cudaSuccess) return e;
+    *out = (unsigned char*)p;
     return cudaSuccess;
 }
+
+// Makes `device` current for the life of the object and puts the caller's current device back.
+struct DeviceGuard {
+    int prev = -1, dev = -1;
+    bool ok = false;
+    explicit DeviceGuard(int device) : dev(device) {
+        if (cudaGetDevice(&prev) != cudaSuccess) { cudaGetLastError(); prev = -1; }
+        ok = prev == device || cudaSetDevice(device) == cudaSuccess;
+        if (!ok) cudaGetLastError();
+    }
+    ~DeviceGuard() {
+        if (prev >= 0 && prev != dev) cudaSetDevice(prev);
+    }
+};
 
 }  // namespace
 
@@ -62,15 +73,25 @@ extern "C" lvbgs_status lvbgs_lbsp_compute2_noalloc(const uint8_t* image, int W,
         return report_error(LVBGS_BAD_SIZE,
                             "lvbgs_lbsp_compute2_noalloc: width*height*channels exceeds its fixed scratch of 8,388,608 "
                             "elements; use lvbgs_lbsp_compute2");
-    if (cudaSetDevice(device_id) != cudaSuccess) return report_error(LVBGS_DEVICE_ERROR, "cannot select the CUDA device");
+    DeviceGuard guard(device_id);
+    if (!guard.ok) return report_error(LVBGS_DEVICE_ERROR, "cannot select the CUDA device");
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    if (st) {
+        int sdev = -1;
+        if (cudaStreamGetDevice(st, &sdev) != cudaSuccess) {
+            cudaGetLastError();
+            return report_error(LVBGS_BAD_ARG, "lvbgs_lbsp_compute2_noalloc: invalid cuda_stream");
+        }
+        if (sdev != device_id)
+            return report_error(LVBGS_BAD_ARG, "lvbgs_lbsp_compute2_noalloc: cuda_stream belongs to another device");
+    }
     unsigned char* base = nullptr;
-    if (scratch_address(device_id, &base) != cudaSuccess) {
+    if (scratch_address(&base) != cudaSuccess) {
         cudaGetLastError();
         return report_error(LVBGS_DEVICE_ERROR, "cannot look up the no-allocation scratch array on this device");
     }
     uint8_t* dimg = base;
     uint16_t* ddesc = (uint16_t*)(base + kDescOffset);
-    cudaStream_t st = (cudaStream_t)cuda_stream;
     // the descriptors are staged too, so the 2-pixel border keeps the caller's content, as with
     // lvbgs_lbsp_compute2; nothing of the previous call's contents is read
     cudaError_t e = cudaMemcpyAsync(dimg, image, n, cudaMemcpyDefault, st);

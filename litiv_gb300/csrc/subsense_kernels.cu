@@ -1641,8 +1641,9 @@ __device__ void refresh_pixel(const StreamDev& S, int p, uint32_t frame, int sta
 }
 
 // ------------------------------------------------------------------------------------------
-// the frame step: one kernel per phase, launched back to back (and captured in a CUDA graph) over
-// all streams of the batch; the repair loop is a cooperative kernel with grid barriers
+// the frame step: one kernel per phase, launched back to back over all streams of the batch (each
+// kernel indexes the per-stream descriptor table); the repair loop is a cooperative kernel with
+// grid barriers
 // ------------------------------------------------------------------------------------------
 #define LV_TILE_KERNEL_PROLOGUE                                              \
     const int t = blockIdx.x;                                               \

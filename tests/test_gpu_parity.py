@@ -112,7 +112,7 @@ def test_subsense_auto_model_reset_bitexact():
 
 
 def test_batched_streams_match_individual_runs():
-    """Three streams of different sizes / channel counts in one persistent launch per tick."""
+    """Three streams of different sizes / channel counts batched into one set of phase kernels per tick."""
     streams = [SyntheticStream(0, seed=21), SyntheticStream(0, seed=22, channels=1, width=160, height=120),
                SyntheticStream(0, seed=23, width=64, height=48, shape_min=8, shape_max=16)]
     frames = [frames_of(s, 16) for s in streams]
