@@ -1123,7 +1123,8 @@ lvbgs_status lvbgs_initialize(lvbgs_handle h, const uint8_t* img, int W, int H, 
             if (r[i] != 0 && r[i] != 255) return fail(h, LVBGS_BAD_ARG, "provided ROI mat values must be 0 or 255 only");
         std::vector<uint8_t> d;
         host_dilate(r, d, W, H, kBorder);
-        for (size_t i = 0; i < npx; ++i) newroi[i] = (uint8_t)(r[i] | (d[i] / 2));
+        // `Mat / 2` is OpenCV's scaling expression, rounded half to even: 255 -> 128
+        for (size_t i = 0; i < npx; ++i) newroi[i] = (uint8_t)(r[i] | ((d[i] + 1) / 2));
     }
     size_t orig = 0;
     for (size_t i = 0; i < npx; ++i) orig += newroi[i] != 0;

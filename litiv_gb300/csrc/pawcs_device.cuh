@@ -115,10 +115,12 @@ __device__ __forceinline__ PwThr pw3_thresholds(float R, uint32_t unstable, uint
     return t;
 }
 __device__ __forceinline__ uint32_t pw3_ch(uint32_t c, int k) { return (c >> (8 * k)) & 255u; }
-// lv::L1dist of two colours
+// lv::L1dist of two three-byte colours (math.hpp:226-250): the reference accumulates the sum in
+// the type of L1dist(uchar, uchar), unsigned char, so it wraps modulo 256 (every three-channel colour
+// L1 of PAWCS goes through it, directly or through cmixdist)
 __device__ __forceinline__ uint32_t pw3_l1(uint32_t a, uint32_t b) {
-    return pw_absdiff(pw3_ch(a, 0), pw3_ch(b, 0)) + pw_absdiff(pw3_ch(a, 1), pw3_ch(b, 1)) +
-           pw_absdiff(pw3_ch(a, 2), pw3_ch(b, 2));
+    return (pw_absdiff(pw3_ch(a, 0), pw3_ch(b, 0)) + pw_absdiff(pw3_ch(a, 1), pw3_ch(b, 1)) +
+            pw_absdiff(pw3_ch(a, 2), pw3_ch(b, 2))) & 0xffu;
 }
 // lv::cdist<3> of two byte colours (math.hpp:474-496): sqrt of the colour distortion, 0 for a grey
 // pair or identical colours

@@ -437,13 +437,16 @@ __device__ uint32_t eval_tail(const StreamDev& S, const FrameK& F, int x, int y,
     const int nreq = S.nreq, nGood = st.nGood, s = st.s;
     const uint32_t minDesc = st.minDesc, minSum = st.minSum;
 
-    // D_last (:254-255 / :396-397): depends on the pixel alone
+    // D_last (:254-255 / :396-397): depends on the pixel alone. With three channels the reference
+    // takes the colour term from lv::L1dist<3>(const uchar*, const uchar*) (math.hpp:226-232), whose
+    // accumulator type is that of L1dist(uchar, uchar), unsigned char: the sum wraps modulo 256.
     uint32_t l1 = 0, hd = 0;
 #pragma unroll
     for (int c = 0; c < C; ++c) {
         l1 += (uint32_t)abs((int)in.lc[c] - (int)curr[c]);
         hd += __popc(in.ld[c] ^ intra[c]);
     }
+    if (C == 3) l1 &= 0xffu;
     const float* divCol = C == 1 ? g_div_col1 : g_div_col3;    // i / 255 or i / 765
     const float* divDesc = C == 1 ? g_div_desc1 : g_div_desc3;  // i / 16 or i / 48
     const float normLast = (__ldg(&divCol[l1]) + __ldg(&divDesc[hd])) / 2;

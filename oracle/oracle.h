@@ -8,12 +8,14 @@
  * always as the checker.
  *
  * Parity pins: the LBSP descriptor is pinned by the reference's golden vector
- * (modules/features2d/test/data/test_lbsp.bin, see tests/golden/). The rest of
- * the path has no golden vectors in the reference and the reference itself
- * cannot be built here (it needs OpenCV, which is absent), so the SuBSENSE and
- * PAWCS model state, masks and the OpenCV image operations they call are "parity
- * unpinned" against the real reference; each function cites the reference
- * lines it restates and states the OpenCV definition it uses.
+ * (modules/features2d/test/data/test_lbsp.bin, see tests/golden/). The SuBSENSE and PAWCS
+ * restatements are pinned to the reference itself: oracle/refshim/build_ref.py compiles the
+ * reference's own modules/video/src sources (against a project-written OpenCV stand-in, with rand()
+ * routed to the same generator) into oracle/_ref/libref.so, which exposes this same API (rsub_* /
+ * rpawcs_*), and tests/test_oracle_reference.py compares every map bit for bit. The OpenCV image
+ * operations use one set of definitions on both sides (written from OpenCV's documentation); their
+ * parity with a real OpenCV build is unpinned (OpenCV is not installed). Each function cites the
+ * reference lines it restates.
  */
 #ifndef LV_ORACLE_H
 #define LV_ORACLE_H

@@ -143,8 +143,12 @@ static size_t cdist3(const uint8_t* curr, const uint8_t* bg) {
     const float sq = (float)(cs - (mix * mix) / (bs > 1 ? bs : 1));
     return (size_t)sqrtf(sq);
 }
+/* lv::L1dist<3> of two byte arrays (math.hpp:226-250, the overloads taking pointers and std::arrays):
+ * the sum accumulates in its Tout = decltype(L1dist(uchar, uchar)) = unsigned char, so it wraps
+ * modulo 256. Every three-channel colour L1 of the path goes through it (directly, :1006, :1179, or
+ * through cmixdist, :294, :367, :1085, :1122). */
 static size_t l1dist3(const uint8_t* a, const uint8_t* b) {
-    return absdiff(a[0], b[0]) + absdiff(a[1], b[1]) + absdiff(a[2], b[2]);
+    return (uint8_t)(absdiff(a[0], b[0]) + absdiff(a[1], b[1]) + absdiff(a[2], b[2]));
 }
 /* lv::cmixdist, math.hpp:596-605 */
 static size_t cmixdist3(const uint8_t* a, const uint8_t* b) { return l1dist3(a, b) / 2 + cdist3(a, b) * 4; }
@@ -475,7 +479,8 @@ int opawcs_initialize(opawcs_t* o, const uint8_t* img, int W, int H, int C, cons
         uint8_t* d = (uint8_t*)malloc(npx);
         uint8_t* t = (uint8_t*)malloc(npx);
         box_minmax(roi, d, t, W, H, LBSP_BORDER, 1);
-        for (size_t i = 0; i < npx; ++i) newroi[i] = roi[i] | (uint8_t)(d[i] / 2);
+        /* `Mat / 2` rounds half to even: 255 -> 128 (BackgroundSubtractionUtils.cpp:95) */
+        for (size_t i = 0; i < npx; ++i) newroi[i] = roi[i] | (uint8_t)((d[i] + 1) / 2);
         free(d);
         free(t);
     }

@@ -1,4 +1,8 @@
-"""ORACLE (test infrastructure only): ctypes wrapper of oracle/_build/liboracle.so.
+"""ORACLE (test infrastructure only): ctypes wrapper of oracle/_build/liboracle.so (the C
+restatement of the reference, "port") and of oracle/_ref/libref.so (the reference's own SuBSENSE /
+PAWCS sources compiled against the project-written OpenCV stand-in, "reference"; built only where
+the reference sources are present, see oracle/refshim/build_ref.py). Both expose the same C API,
+so OracleSuBSENSE / OraclePAWCS drive either one (``impl=``).
 
 Loaded only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, as the checker.
 """
@@ -58,10 +62,70 @@ class PScalars(C.Structure):
 
 
 _lib = None
+_ref_lib = None
+REF_LIB_PATH = os.path.join(HERE, "_ref", "libref.so")
 
 
 def build():
     subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def build_reference(ref_root=None):
+    """Builds oracle/_ref/libref.so from the reference's sources; returns its path, or None when the
+    reference sources are not present."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("lv_build_ref", os.path.join(HERE, "refshim", "build_ref.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(ref_root) if ref_root else mod.build()
+
+
+def ref_lib():
+    """The reference compiled from its own sources (None when it cannot be built here)."""
+    global _ref_lib
+    if _ref_lib is None:
+        path = build_reference()
+        if path is None and not os.path.exists(REF_LIB_PATH):
+            return None
+        L = C.CDLL(REF_LIB_PATH)
+        for pre, Par, Sc in (("rsub_", OParams, OScalars), ("rpawcs_", PParams, PScalars)):
+            getattr(L, pre + "create").restype = C.c_void_p
+            getattr(L, pre + "create").argtypes = [C.POINTER(Par)]
+            getattr(L, pre + "destroy").argtypes = [C.c_void_p]
+            getattr(L, pre + "initialize").argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
+            getattr(L, pre + "apply").argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
+            getattr(L, pre + "get_background").argtypes = [C.c_void_p, C.c_void_p]
+            getattr(L, pre + "set_roi").argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+            getattr(L, pre + "get_background_descriptors").argtypes = [C.c_void_p, C.c_void_p]
+            getattr(L, pre + "set_automatic_model_reset").argtypes = [C.c_void_p, C.c_int]
+            getattr(L, pre + "get_scalars").argtypes = [C.c_void_p, C.POINTER(Sc)]
+        L.r_last_error.restype = C.c_char_p
+        L.rsub_refresh_model.argtypes = [C.c_void_p, C.c_float, C.c_int]
+        L.rsub_map.restype = C.c_void_p
+        L.rsub_map.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]
+        L.rpawcs_refresh_model.argtypes = [C.c_void_p, C.c_size_t, C.c_float, C.c_int]
+        L.rpawcs_export.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]
+        L.rpawcs_export_bytes.restype = C.c_size_t
+        L.rpawcs_export_bytes.argtypes = [C.c_void_p, C.c_int]
+        _ref_lib = L
+    return _ref_lib
+
+
+class _Api:
+    """Calls `name` of the restatement (prefix o...) or of the reference (prefix r...)."""
+
+    def __init__(self, impl, port_prefix, ref_prefix):
+        if impl == "port":
+            self.L, self.pre = lib(), port_prefix
+        elif impl == "reference":
+            self.L, self.pre = ref_lib(), ref_prefix
+            if self.L is None:
+                raise RuntimeError("the reference cannot be built here (its sources are not present)")
+        else:
+            raise ValueError("impl must be 'port' or 'reference'")
+
+    def __getattr__(self, name):
+        return getattr(self.L, self.pre + name)
 
 
 def lib():
@@ -117,23 +181,26 @@ def lib():
 
 
 class OracleSuBSENSE:
-    """Sequential CPU SuBSENSE (the checker)."""
+    """Sequential CPU SuBSENSE (the checker): the C restatement (impl="port") or the reference's own
+    BackgroundSubtractorSuBSENSE (impl="reference")."""
 
-    def __init__(self, seed=0, **params):
+    def __init__(self, seed=0, impl="port", **params):
         p = OParams()
         lib().osub_default_params(C.byref(p))
         p.seed = seed
         for k, v in params.items():
             setattr(p, k, v)
         self.params = p
-        self._o = lib().osub_create(C.byref(p))
+        self.impl = impl
+        self._a = _Api(impl, "osub_", "rsub_")
+        self._o = self._a.create(C.byref(p))
         if not self._o:
             raise ValueError("invalid oracle parameters")
         self.shape = None
 
     def close(self):
         if self._o:
-            lib().osub_destroy(self._o)
+            self._a.destroy(self._o)
             self._o = None
 
     def __del__(self):
@@ -147,7 +214,7 @@ class OracleSuBSENSE:
         H, W = img.shape[:2]
         Cc = img.shape[2] if img.ndim == 3 else 1
         r = None if roi is None else np.ascontiguousarray(roi, np.uint8)
-        st = lib().osub_initialize(self._o, img.ctypes.data_as(C.c_void_p), W, H, Cc,
+        st = self._a.initialize(self._o, img.ctypes.data_as(C.c_void_p), W, H, Cc,
                                    r.ctypes.data_as(C.c_void_p) if r is not None else None)
         if st != 0:
             raise ValueError("oracle initialize failed (%d)" % st)
@@ -157,37 +224,40 @@ class OracleSuBSENSE:
         img = np.ascontiguousarray(img, np.uint8)
         H, W, _ = self.shape
         mask = np.empty((H, W), np.uint8)
-        st = lib().osub_apply(self._o, img.ctypes.data_as(C.c_void_p), mask.ctypes.data_as(C.c_void_p), float(lr))
+        st = self._a.apply(self._o, img.ctypes.data_as(C.c_void_p), mask.ctypes.data_as(C.c_void_p), float(lr))
         if st != 0:
-            raise ValueError("oracle apply failed (%d)" % st)
+            raise ValueError("oracle apply failed (%d)%s" % (st, self._err()))
         return mask
 
+    def _err(self):
+        return ": " + ref_lib().r_last_error().decode(errors="replace") if self.impl == "reference" else ""
+
     def refresh_model(self, frac, force=False):
-        return lib().osub_refresh_model(self._o, float(frac), 1 if force else 0)
+        return self._a.refresh_model(self._o, float(frac), 1 if force else 0)
 
     def set_automatic_model_reset(self, v):
-        lib().osub_set_automatic_model_reset(self._o, 1 if v else 0)
+        self._a.set_automatic_model_reset(self._o, 1 if v else 0)
 
     def background(self):
         H, W, Cc = self.shape
         out = np.empty((H, W, Cc) if Cc > 1 else (H, W), np.uint8)
-        lib().osub_get_background(self._o, out.ctypes.data_as(C.c_void_p))
+        self._a.get_background(self._o, out.ctypes.data_as(C.c_void_p))
         return out
 
     def set_roi(self, roi):
         r = np.ascontiguousarray(roi, dtype=np.uint8)
-        if lib().osub_set_roi(self._o, r.ctypes.data_as(C.c_void_p), r.shape[1], r.shape[0]) != 0:
+        if self._a.set_roi(self._o, r.ctypes.data_as(C.c_void_p), r.shape[1], r.shape[0]) != 0:
             raise ValueError("oracle setROI failed")
 
     def background_descriptors(self):
         H, W, Cc = self.shape
         out = np.empty((H, W, Cc) if Cc > 1 else (H, W), np.uint16)
-        lib().osub_get_background_descriptors(self._o, out.ctypes.data_as(C.c_void_p))
+        self._a.get_background_descriptors(self._o, out.ctypes.data_as(C.c_void_p))
         return out
 
     def state_map(self, name):
         n = C.c_size_t()
-        ptr = lib().osub_map(self._o, MAP_NAMES.index(name), C.byref(n))
+        ptr = self._a.map(self._o, MAP_NAMES.index(name), C.byref(n))
         raw = np.ctypeslib.as_array((C.c_uint8 * n.value).from_address(ptr)).copy()
         H, W, Cc = self.shape
         from litiv_gb300.bgs import map_view  # layout helper only (pure numpy)
@@ -195,28 +265,31 @@ class OracleSuBSENSE:
 
     def scalars(self):
         s = OScalars()
-        lib().osub_get_scalars(self._o, C.byref(s))
+        self._a.get_scalars(self._o, C.byref(s))
         return {f: getattr(s, f) for f, _ in OScalars._fields_}
 
 
 class OraclePAWCS:
-    """Sequential CPU PAWCS (the checker)."""
+    """Sequential CPU PAWCS (the checker): the C restatement (impl="port") or the reference's own
+    BackgroundSubtractorPAWCS (impl="reference")."""
 
-    def __init__(self, seed=0, **params):
+    def __init__(self, seed=0, impl="port", **params):
         p = PParams()
         lib().opawcs_default_params(C.byref(p))
         p.seed = seed
         for k, v in params.items():
             setattr(p, k, v)
         self.params = p
-        self._o = lib().opawcs_create(C.byref(p))
+        self.impl = impl
+        self._a = _Api(impl, "opawcs_", "rpawcs_")
+        self._o = self._a.create(C.byref(p))
         if not self._o:
             raise ValueError("invalid oracle parameters")
         self.shape = None
 
     def close(self):
         if self._o:
-            lib().opawcs_destroy(self._o)
+            self._a.destroy(self._o)
             self._o = None
 
     def __del__(self):
@@ -230,7 +303,7 @@ class OraclePAWCS:
         H, W = img.shape[:2]
         Cc = img.shape[2] if img.ndim == 3 else 1
         r = None if roi is None else np.ascontiguousarray(roi, np.uint8)
-        st = lib().opawcs_initialize(self._o, img.ctypes.data_as(C.c_void_p), W, H, Cc,
+        st = self._a.initialize(self._o, img.ctypes.data_as(C.c_void_p), W, H, Cc,
                                      r.ctypes.data_as(C.c_void_p) if r is not None else None)
         if st != 0:
             raise ValueError("oracle initialize failed (%d)" % st)
@@ -240,47 +313,47 @@ class OraclePAWCS:
         img = np.ascontiguousarray(img, np.uint8)
         H, W, _ = self.shape
         mask = np.empty((H, W), np.uint8)
-        st = lib().opawcs_apply(self._o, img.ctypes.data_as(C.c_void_p), mask.ctypes.data_as(C.c_void_p), float(lr))
+        st = self._a.apply(self._o, img.ctypes.data_as(C.c_void_p), mask.ctypes.data_as(C.c_void_p), float(lr))
         if st != 0:
             raise ValueError("oracle apply failed (%d)" % st)
         return mask
 
     def refresh_model(self, base_occ, occ_decr_frac, force=False):
-        return lib().opawcs_refresh_model(self._o, int(base_occ), float(occ_decr_frac), 1 if force else 0)
+        return self._a.refresh_model(self._o, int(base_occ), float(occ_decr_frac), 1 if force else 0)
 
     def set_automatic_model_reset(self, v):
-        lib().opawcs_set_automatic_model_reset(self._o, 1 if v else 0)
+        self._a.set_automatic_model_reset(self._o, 1 if v else 0)
 
     def background(self):
         H, W, Cc = self.shape
         out = np.empty((H, W, Cc) if Cc > 1 else (H, W), np.uint8)
-        lib().opawcs_get_background(self._o, out.ctypes.data_as(C.c_void_p))
+        self._a.get_background(self._o, out.ctypes.data_as(C.c_void_p))
         return out
 
     def set_roi(self, roi):
         r = np.ascontiguousarray(roi, dtype=np.uint8)
-        if lib().opawcs_set_roi(self._o, r.ctypes.data_as(C.c_void_p), r.shape[1], r.shape[0]) != 0:
+        if self._a.set_roi(self._o, r.ctypes.data_as(C.c_void_p), r.shape[1], r.shape[0]) != 0:
             raise ValueError("oracle setROI failed")
 
     def background_descriptors(self):
         H, W, Cc = self.shape
         out = np.empty((H, W, Cc) if Cc > 1 else (H, W), np.uint16)
-        lib().opawcs_get_background_descriptors(self._o, out.ctypes.data_as(C.c_void_p))
+        self._a.get_background_descriptors(self._o, out.ctypes.data_as(C.c_void_p))
         return out
 
     def state_map(self, name):
         """Raw bytes of one exported state array (layouts in oracle.h, OPAWCS_MAP_*)."""
         which = PAWCS_MAP_NAMES.index(name)
-        n = lib().opawcs_export_bytes(self._o, which)
+        n = self._a.export_bytes(self._o, which)
         out = np.empty(n, np.uint8)
-        st = lib().opawcs_export(self._o, which, out.ctypes.data_as(C.c_void_p), n)
+        st = self._a.export(self._o, which, out.ctypes.data_as(C.c_void_p), n)
         if st != 0:
             raise ValueError("oracle export failed (%d)" % st)
         return out
 
     def scalars(self):
         s = PScalars()
-        lib().opawcs_get_scalars(self._o, C.byref(s))
+        self._a.get_scalars(self._o, C.byref(s))
         return {f: getattr(s, f) for f, _ in PScalars._fields_}
 
 

@@ -1,0 +1,268 @@
+// ORACLE (test infrastructure only): project-written stand-in for the OpenCV imgproc operations
+// that the reference's SuBSENSE / PAWCS path calls. Each definition is written from OpenCV's
+// documented semantics and is the one the C restatement uses (oracle/common.h, oracle/subsense.c,
+// oracle/pawcs.c); parity with a real OpenCV build is unpinned.
+#pragma once
+
+#include <deque>
+
+#include "opencv2/core.hpp"
+
+namespace cv {
+
+enum MorphShapes { MORPH_RECT = 0, MORPH_CROSS = 1, MORPH_ELLIPSE = 2 };
+enum MorphTypes { MORPH_ERODE = 0, MORPH_DILATE = 1, MORPH_OPEN = 2, MORPH_CLOSE = 3 };
+enum InterpolationFlags { INTER_NEAREST = 0, INTER_LINEAR = 1, INTER_CUBIC = 2, INTER_AREA = 3 };
+
+inline Mat getStructuringElement(int shape, Size ksize, Point anchor = Point(-1, -1)) {
+    if (shape != MORPH_RECT) throw std::runtime_error("getStructuringElement: only MORPH_RECT is supported");
+    (void)anchor;
+    return Mat(ksize, CV_8UC1, Scalar(1));
+}
+
+// half-width of the square window equivalent to `iterations` passes of `kernel` (empty: 3x3)
+inline int morph_radius(InputArray kernel, int iterations) {
+    int k = 3;
+    if (!kernel.empty()) {
+        const Mat m = kernel.getMat();
+        if (m.rows != m.cols || !(m.rows & 1) || countNonZero(m) != m.rows * m.cols)
+            throw std::runtime_error("morphology: only odd square rectangular kernels are supported");
+        k = m.rows;
+    }
+    return (k / 2) * (iterations < 1 ? 1 : iterations);
+}
+
+// max (dilate) or min (erode) over the (2r+1)x(2r+1) window clipped to the image: with the default
+// border value (morphologyDefaultBorderValue) pixels outside the image never win, and n passes of a
+// 3x3 rectangle equal one (2n+1)x(2n+1) rectangle under that rule. 8-bit, single channel.
+inline void morph_minmax(const Mat& src, Mat& dst, int r, bool is_max) {
+    const int W = src.cols, H = src.rows;
+    Mat tmp(H, W, CV_8UC1), out(H, W, CV_8UC1);
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            int v = is_max ? 0 : 255;
+            for (int d = -r; d <= r; ++d) {
+                const int xx = x + d;
+                if (xx < 0 || xx >= W) continue;
+                const int s = src.ptr(y)[xx];
+                v = is_max ? std::max(v, s) : std::min(v, s);
+            }
+            tmp.ptr(y)[x] = (uchar)v;
+        }
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            int v = is_max ? 0 : 255;
+            for (int d = -r; d <= r; ++d) {
+                const int yy = y + d;
+                if (yy < 0 || yy >= H) continue;
+                const int s = tmp.ptr(yy)[x];
+                v = is_max ? std::max(v, s) : std::min(v, s);
+            }
+            out.ptr(y)[x] = (uchar)v;
+        }
+    dst.create(H, W, CV_8UC1);
+    out.copyTo(dst);
+}
+
+inline void dilate(InputArray src, OutputArray dst, InputArray kernel, Point anchor = Point(-1, -1),
+                   int iterations = 1) {
+    (void)anchor;
+    const Mat s = src.getMat();
+    if (s.type() != CV_8UC1) throw std::runtime_error("dilate: 8UC1 only");
+    morph_minmax(s, dst.getMatRef(), morph_radius(kernel, iterations), true);
+}
+inline void erode(InputArray src, OutputArray dst, InputArray kernel, Point anchor = Point(-1, -1),
+                  int iterations = 1) {
+    (void)anchor;
+    const Mat s = src.getMat();
+    if (s.type() != CV_8UC1) throw std::runtime_error("erode: 8UC1 only");
+    morph_minmax(s, dst.getMatRef(), morph_radius(kernel, iterations), false);
+}
+// closing: dilation then erosion with the same kernel
+inline void morphologyEx(InputArray src, OutputArray dst, int op, InputArray kernel, Point anchor = Point(-1, -1),
+                         int iterations = 1) {
+    if (op != MORPH_CLOSE) throw std::runtime_error("morphologyEx: only MORPH_CLOSE is supported");
+    Mat t;
+    dilate(src, t, kernel, anchor, iterations);
+    erode(t, dst, kernel, anchor, iterations);
+}
+
+// 4-connected flood fill with zero tolerances (the default flags and loDiff/upDiff): every pixel
+// 4-connected to the seed through pixels equal to the seed's value takes newVal. 8UC1.
+inline int floodFill(InputOutputArray image, Point seed, Scalar newVal) {
+    Mat& m = image.getMatRef();
+    if (m.type() != CV_8UC1) throw std::runtime_error("floodFill: 8UC1 only");
+    const int W = m.cols, H = m.rows;
+    if (seed.x < 0 || seed.y < 0 || seed.x >= W || seed.y >= H) return 0;
+    const uchar v0 = m.ptr(seed.y)[seed.x];
+    const uchar nv = saturate_cast<uchar>(newVal.val[0]);
+    std::vector<uchar> seen((size_t)W * H, 0);
+    std::deque<int> q;
+    q.push_back(seed.y * W + seed.x);
+    seen[(size_t)seed.y * W + seed.x] = 1;
+    int n = 0;
+    while (!q.empty()) {
+        const int p = q.front();
+        q.pop_front();
+        const int x = p % W, y = p / W;
+        m.ptr(y)[x] = nv;
+        ++n;
+        const int nx[4] = {x - 1, x + 1, x, x}, ny[4] = {y, y, y - 1, y + 1};
+        for (int k = 0; k < 4; ++k) {
+            if (nx[k] < 0 || ny[k] < 0 || nx[k] >= W || ny[k] >= H) continue;
+            const size_t j = (size_t)ny[k] * W + nx[k];
+            if (seen[j] || m.ptr(ny[k])[nx[k]] != v0) continue;
+            seen[j] = 1;
+            q.push_back((int)j);
+        }
+    }
+    return n;
+}
+
+// median of the k x k window with BORDER_REPLICATE (k odd), 8UC1: a 256-bin histogram slid along
+// each row
+inline void medianBlur(InputArray src_, OutputArray dst_, int k) {
+    const Mat src = src_.getMat();
+    if (src.type() != CV_8UC1 || k < 1 || !(k & 1)) throw std::runtime_error("medianBlur: 8UC1, odd k");
+    const int W = src.cols, H = src.rows, r = k / 2, half = k * k / 2;
+    Mat out(H, W, CV_8UC1);
+    auto at = [&](int y, int x) {
+        y = y < 0 ? 0 : y >= H ? H - 1 : y;
+        x = x < 0 ? 0 : x >= W ? W - 1 : x;
+        return src.ptr(y)[x];
+    };
+    for (int y = 0; y < H; ++y) {
+        int hist[256] = {0};
+        for (int dy = -r; dy <= r; ++dy)
+            for (int dx = -r; dx <= r; ++dx) ++hist[at(y + dy, dx)];
+        for (int x = 0; x < W; ++x) {
+            if (x > 0)
+                for (int dy = -r; dy <= r; ++dy) {
+                    --hist[at(y + dy, x - 1 - r)];
+                    ++hist[at(y + dy, x + r)];
+                }
+            int acc = 0, v = 0;
+            for (; v < 256; ++v) {
+                acc += hist[v];
+                if (acc > half) break;
+            }
+            out.ptr(y)[x] = (uchar)v;
+        }
+    }
+    Mat& dst = dst_.getMatRef();
+    dst.create(H, W, CV_8UC1);
+    out.copyTo(dst);
+}
+
+// INTER_AREA when the source size is an integral multiple of the output (OpenCV's "area fast"
+// case): each output element is saturate_cast(block sum * (1.f/area)), the sum in int (8-bit
+// sources) or double (float sources). INTER_NEAREST: source x = floor(dx * (1/(dw/W))), clamped.
+inline void resize(InputArray src_, OutputArray dst_, Size dsize, double fx = 0, double fy = 0,
+                   int interpolation = INTER_LINEAR) {
+    (void)fx;
+    (void)fy;
+    const Mat src = src_.getMat();
+    const int W = src.cols, H = src.rows, cn = src.channels(), dw = dsize.width, dh = dsize.height;
+    Mat out(dh, dw, src.type());
+    if (interpolation == INTER_AREA) {
+        if (dw <= 0 || dh <= 0 || W % dw || H % dh)
+            throw std::runtime_error("resize(INTER_AREA): only integral scales are supported");
+        const int sx = W / dw, sy = H / dh;
+        const float scale = 1.f / (float)(sx * sy);
+        for (int y = 0; y < dh; ++y)
+            for (int x = 0; x < dw; ++x)
+                for (int c = 0; c < cn; ++c) {
+                    if (src.depth() == CV_8U) {
+                        int s = 0;
+                        for (int yy = 0; yy < sy; ++yy)
+                            for (int xx = 0; xx < sx; ++xx) s += src.ptr(y * sy + yy)[(x * sx + xx) * cn + c];
+                        out.ptr(y)[x * cn + c] = saturate_cast<uchar>((float)s * scale);
+                    } else {
+                        double s = 0;
+                        for (int yy = 0; yy < sy; ++yy)
+                            for (int xx = 0; xx < sx; ++xx) s += src.get_d(y * sy + yy, (x * sx + xx) * cn + c);
+                        out.put_d(y, x * cn + c, s * scale);
+                    }
+                }
+    } else if (interpolation == INTER_NEAREST) {
+        const double ifx = 1.0 / ((double)dw / W), ify = 1.0 / ((double)dh / H);
+        const size_t es = src.elemSize();
+        for (int y = 0; y < dh; ++y) {
+            int syy = (int)std::floor(y * ify);
+            syy = syy < H - 1 ? syy : H - 1;
+            for (int x = 0; x < dw; ++x) {
+                int sxx = (int)std::floor(x * ifx);
+                sxx = sxx < W - 1 ? sxx : W - 1;
+                std::memcpy(out.ptr(y) + x * es, src.ptr(syy) + sxx * es, es);
+            }
+        }
+    } else {
+        throw std::runtime_error("resize: only INTER_AREA and INTER_NEAREST are supported");
+    }
+    Mat& dst = dst_.getMatRef();
+    dst.create(dh, dw, src.type());
+    out.copyTo(dst);
+}
+
+// dst = src*a + dst*(1-a), a = (float)alpha, in float, each product rounded separately
+inline void accumulateWeighted(InputArray src_, InputOutputArray dst_, double alpha, InputArray mask = noArray()) {
+    if (!mask.empty()) throw std::runtime_error("accumulateWeighted: masks are not supported");
+    const Mat src = src_.getMat();
+    Mat& dst = dst_.getMatRef();
+    const float a = (float)alpha, b = 1.0f - a;
+    for (int y = 0; y < src.rows; ++y)
+        for (int i = 0; i < src.cols * src.channels(); ++i) {
+            float* d = dst.ptr<float>(y) + i;
+            const float t1 = (float)src.get_d(y, i) * a;
+            const float t2 = *d * b;
+            *d = t1 + t2;
+        }
+}
+
+// dst += src1*src2 where mask != 0, in float
+inline void accumulateProduct(InputArray s1_, InputArray s2_, InputOutputArray dst_, InputArray mask_ = noArray()) {
+    const Mat s1 = s1_.getMat(), s2 = s2_.getMat(), mask = mask_.getMat();
+    Mat& dst = dst_.getMatRef();
+    if (dst.depth() != CV_32F || dst.channels() != 1) throw std::runtime_error("accumulateProduct: 32FC1 only");
+    for (int y = 0; y < dst.rows; ++y)
+        for (int x = 0; x < dst.cols; ++x) {
+            if (!mask.empty() && !mask.ptr(y)[x]) continue;
+            const float prod = (float)s1.get_d(y, x) * (float)s2.get_d(y, x);
+            float* d = dst.ptr<float>(y) + x;
+            *d = *d + prod;
+        }
+}
+
+// normalized 3x3 box filter with BORDER_REPLICATE on 32FC1, sums in double: per row
+// s = v[x-1] + v[x] + v[x+1], per column t = s[y-1] + s[y] + s[y+1], dst = (float)(t * (1.0/9))
+inline void blur(InputArray src_, OutputArray dst_, Size ksize, Point anchor = Point(-1, -1),
+                 int borderType = BORDER_DEFAULT) {
+    (void)anchor;
+    const Mat src = src_.getMat();
+    if (ksize.width != 3 || ksize.height != 3 || borderType != BORDER_REPLICATE || src.type() != CV_32FC1)
+        throw std::runtime_error("blur: 3x3 BORDER_REPLICATE on 32FC1 only");
+    const int w = src.cols, h = src.rows;
+    std::vector<double> row((size_t)w * h);
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) {
+            const int x0 = x > 0 ? x - 1 : 0, x1 = x < w - 1 ? x + 1 : w - 1;
+            const float* p = src.ptr<float>(y);
+            row[(size_t)y * w + x] = ((double)p[x0] + (double)p[x]) + (double)p[x1];
+        }
+    Mat out(h, w, CV_32FC1);
+    for (int y = 0; y < h; ++y) {
+        const int y0 = y > 0 ? y - 1 : 0, y1 = y < h - 1 ? y + 1 : h - 1;
+        for (int x = 0; x < w; ++x) {
+            const double t = (row[(size_t)y0 * w + x] + row[(size_t)y * w + x]) + row[(size_t)y1 * w + x];
+            out.ptr<float>(y)[x] = (float)(t * (1.0 / 9.0));
+        }
+    }
+    Mat& dst = dst_.getMatRef();
+    dst.create(h, w, CV_32FC1);
+    out.copyTo(dst);
+}
+
+// drawing is only called in the reference's debug-display code, which is compiled out here
+void circle(InputOutputArray img, Point center, int radius, const Scalar& color, int thickness = 1);
+
+}  // namespace cv

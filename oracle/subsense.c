@@ -224,11 +224,13 @@ int osub_initialize(osub_t* o, const uint8_t* img, int W, int H, int C, const ui
                 free(newroi);
                 return OSUB_EBADARG;
             }
-        /* dilate by m_nROIBorderSize (=2) iterations, /2, OR: pixels near the ROI edge get 127 */
+        /* dilate by m_nROIBorderSize (=2) iterations, /2, OR (BackgroundSubtractionUtils.cpp:94-95):
+         * `Mat / 2` is OpenCV's scaling expression, saturate_cast(v * 0.5) rounded half to even, so the
+         * pixels near the ROI edge get 128 (255 / 2 = 127.5) */
         uint8_t* d = (uint8_t*)malloc(npx);
         uint8_t* t = (uint8_t*)malloc(npx);
         box_minmax(roi, d, t, W, H, LBSP_BORDER, 1);
-        for (size_t i = 0; i < npx; ++i) newroi[i] = roi[i] | (uint8_t)(d[i] / 2);
+        for (size_t i = 0; i < npx; ++i) newroi[i] = roi[i] | (uint8_t)((d[i] + 1) / 2);
         free(d);
         free(t);
     }
@@ -470,7 +472,9 @@ int osub_apply(osub_t* o, const uint8_t* img, uint8_t* mask, double lr) {
             fail3:
                 s++;
             }
-            const size_t l1 = absdiff(lastCol[0], curr[0]) + absdiff(lastCol[1], curr[1]) + absdiff(lastCol[2], curr[2]);
+            /* lv::L1dist<3>(const uchar*, const uchar*) (math.hpp:226-232) accumulates in its Tout, which is
+             * decltype(L1dist(uchar, uchar)) = unsigned char: the three-channel sum wraps modulo 256 */
+            const size_t l1 = (uint8_t)(absdiff(lastCol[0], curr[0]) + absdiff(lastCol[1], curr[1]) + absdiff(lastCol[2], curr[2]));
             const size_t hd = popc16(lastDesc[0] ^ intra[0]) + popc16(lastDesc[1] ^ intra[1]) + popc16(lastDesc[2] ^ intra[2]);
             normLast = ((float)l1 / (float)colMax3 + (float)hd / (float)descMax3) / 2;
         }

@@ -166,7 +166,7 @@ def test_oracle_roi_excludes_pixels(product_lib):
     o = pyoracle.OracleSuBSENSE(seed=3)
     o.initialize(s.render(0), roi)
     r = o.state_map("ROI")
-    assert r[40, 60] == 255 and r[0, 0] == 0 and r[39, 60] == 127  # 127 near the ROI edge
+    assert r[40, 60] == 255 and r[0, 0] == 0 and r[39, 60] == 128  # 255/2 rounded half to even near the ROI edge
     for t in range(1, 6):
         o.apply(s.render(t))
     raw = o.state_map("LAST_RAW_FG")
@@ -175,7 +175,7 @@ def test_oracle_roi_excludes_pixels(product_lib):
 
 def test_oracle_roi_rules():
     # setROI before initialize keeps the validated ROI as is; initialize() without a ROI of the same size
-    # reuses the last validated ROI; setROI on an initialized model re-initializes (edge pixels 127)
+    # reuses the last validated ROI; setROI on an initialized model re-initializes (edge pixels 128)
     from litiv_gb300 import SyntheticStream
     s = SyntheticStream(0, seed=63, width=96, height=72, shape_min=10, shape_max=24)
     fr = [s.render(t) for t in range(3)]
@@ -194,4 +194,4 @@ def test_oracle_roi_rules():
     o.initialize(fr[2])
     assert np.array_equal(o.state_map("ROI"), v)
     o.set_roi(roi)
-    assert set(np.unique(o.state_map("ROI")).tolist()) == {0, 127, 255}
+    assert set(np.unique(o.state_map("ROI")).tolist()) == {0, 128, 255}
