@@ -296,7 +296,7 @@ def map_view(name, raw, W, H, Cc, N):
 
 
 def batch_apply(subtractors, images, masks=None, learning_rates=None, wait=True):
-    """One frame of each stream in a single persistent launch (lvbgs_batch_apply)."""
+    """One frame of each stream in one batched frame step over all of them (lvbgs_batch_apply)."""
     n = len(subtractors)
     if masks is None:
         masks = [np.empty(s._need_init()[:2], np.uint8) for s in subtractors]

@@ -307,8 +307,6 @@ void fill_geometry(lvbgs_ctx* h) {
     S.nSegs = (h->H + kMedSegRows - 1) / kMedSegRows;
     S.dsW = h->W / 8;
     S.dsH = h->H / 8;
-    S.dsSX = S.dsW > 0 ? h->W / S.dsW : 1;
-    S.dsSY = S.dsH > 0 ? h->H / S.dsH : 1;
     S.N = (int)h->prm.bg_samples;
     S.nreq = (int)h->prm.required_bg_samples;
     S.minColor = (int)h->prm.min_color_dist_threshold;
@@ -756,19 +754,14 @@ lvbgs_status pw_initialize(lvbgs_ctx* h, const uint8_t* img, int W, int H, int C
         return fail(h, LVBGS_UNSUPPORTED, "word counts above the supported maximum");
     if (g.median_k > 13) return fail(h, LVBGS_UNSUPPORTED, "median kernel sizes above 13 are not supported");
     const int dsW = W / 8, dsH = H / 8;
-    if (dsW <= 0 || dsH <= 0 || W % dsW != 0 || H % dsH != 0)
-        return fail(h, LVBGS_UNSUPPORTED,
-                    "frame-level analysis needs an integral 1/8 down-sampling (INTER_AREA fast path): width and height must be multiples of width/8 and height/8");
-    // down-sampled ROI (INTER_AREA of the validated ROI, :445) and its pixel count
-    const int sx = W / dsW, sy = H / dsH;
+    // the reference's cv::resize to (W/8, H/8) (:446) needs a non-empty output
+    if (dsW <= 0 || dsH <= 0) return fail(h, LVBGS_BAD_SIZE, "frames must be at least 8x8 pixels");
+    // down-sampled ROI (INTER_AREA of the validated ROI, :446) and its pixel count
     std::vector<uint8_t> dsRoi((size_t)dsW * dsH);
     size_t dsCount = 0;
     for (int y = 0; y < dsH; ++y)
         for (int x = 0; x < dsW; ++x) {
-            int sum = 0;
-            for (int yy = 0; yy < sy; ++yy)
-                for (int xx = 0; xx < sx; ++xx) sum += newroi[(size_t)(y * sy + yy) * W + x * sx + xx];
-            uint8_t v = sat_round_u8((float)sum * (1.f / (float)(sx * sy)));
+            uint8_t v = area_resample(W, H, dsW, dsH, x, y, [&](int sx, int sy) { return (int)newroi[(size_t)sy * W + sx]; });
             if (g.big) v |= 127;
             dsRoi[(size_t)y * dsW + x] = v;
             dsCount += v != 0;
@@ -1150,10 +1143,6 @@ lvbgs_status lvbgs_initialize(lvbgs_handle h, const uint8_t* img, int W, int H, 
         ctl.median_k = (raw % 2) ? raw : raw - 1;
         ctl.t_lo = 2.0f;
         ctl.t_hi = 256.0f;
-        const int dsW = W / 8, dsH = H / 8;
-        if (dsW <= 0 || dsH <= 0 || W % dsW != 0 || H % dsH != 0)
-            return fail(h, LVBGS_UNSUPPORTED,
-                        "frame-level analysis needs an integral 1/8 down-sampling (INTER_AREA fast path): width and height must be multiples of width/8 and height/8");
     } else {
         ctl.lr_scaling = 0;
         ctl.auto_reset = 0;

@@ -13,6 +13,7 @@
 //   u8 maps: roi, blinks, last raw mask, last final mask, inverted dilated mask, last raw blinks,
 //   plus per-frame scratch (closed mask, combined mask, union-find labels, intents, draw counters).
 #pragma once
+#include <math.h>
 #include <stddef.h>
 #include <stdint.h>
 
@@ -131,7 +132,7 @@ struct StreamDev {
     int tilesX, tilesY, tileBase, nTiles;
     int rowBase, rowWords;  // first row of this stream in the batch's row index space; bit-plane words per row
     int segBase, nSegs;     // first median column segment of this stream in the batch, and its count
-    int dsW, dsH, dsSX, dsSY;
+    int dsW, dsH;  // size of the frame-level down-sampled frame (W/8, H/8)
     int N, nreq, minColor, descOff, stabColorOff, nmv;
     float relThr;
     unsigned int lbspOff;
@@ -200,5 +201,54 @@ __host__ __device__ __forceinline__ uint32_t* bit_plane(const StreamDev& S, int 
     return S.bits + (size_t)i * S.H * S.rowWords;
 }
 inline size_t bit_planes_bytes(int W, int H) { return (size_t)BP_COUNT * H * ((W + 31) / 32) * 4; }
+
+// ---- cv::resize(src, dst, (dW, dH), INTER_AREA) of an 8-bit image, one output element ----
+// When the source size is an integral multiple of the output (OpenCV's "area fast" case, e.g. the
+// 1/8 down-sampling of frames whose sides are multiples of 8) the output is the block mean computed as
+// round(sum * (1.f/area)), as before. Otherwise it is the exact area-weighted mean of the source
+// pixels under the output pixel's footprint: in units of 1/dW (1/dH) a source pixel i spans
+// [i*dW, (i+1)*dW) and output pixel x spans [x*W, (x+1)*W), so every overlap is an integer and the
+// output is round(sum(ox * oy * src) / (W * H)) with ties to even, computed exactly in integers. The
+// definition is written from the mathematics of the area relation (OpenCV documents INTER_AREA as
+// "resampling using pixel area relation" and is not installed here); both the GPU and the oracle use it.
+// get(i, j) returns the source value at column i, row j.
+LV_HD uint8_t area_round_ties_even(unsigned long long num, unsigned long long den) {
+    unsigned long long q = num / den;
+    const unsigned long long r2 = (num % den) * 2ull;
+    if (r2 > den || (r2 == den && (q & 1ull))) ++q;
+    return (uint8_t)(q > 255ull ? 255ull : q);
+}
+template <typename Get>
+LV_HD uint8_t area_resample(int W, int H, int dW, int dH, int x, int y, Get get) {
+    if (W % dW == 0 && H % dH == 0) {
+        const int sx = W / dW, sy = H / dH;
+        int sum = 0;
+        for (int j = 0; j < sy; ++j)
+            for (int i = 0; i < sx; ++i) sum += get(x * sx + i, y * sy + j);
+        const float v = (float)sum * (1.f / (float)(sx * sy));
+#ifdef __CUDA_ARCH__
+        const int r = __float2int_rn(v);
+#else
+        const int r = (int)nearbyintf(v);
+#endif
+        return (uint8_t)(r < 0 ? 0 : r > 255 ? 255 : r);
+    }
+    const long long x0 = (long long)x * W, x1 = x0 + W, y0 = (long long)y * H, y1 = y0 + H;
+    const int i0 = (int)(x0 / dW), i1 = (int)((x1 + dW - 1) / dW);
+    const int j0 = (int)(y0 / dH), j1 = (int)((y1 + dH - 1) / dH);
+    unsigned long long num = 0;
+    for (int j = j0; j < j1; ++j) {
+        const long long a = (long long)j * dH, b = a + dH;
+        const long long oy = (b < y1 ? b : y1) - (a > y0 ? a : y0);
+        unsigned long long row = 0;
+        for (int i = i0; i < i1; ++i) {
+            const long long c = (long long)i * dW, d = c + dW;
+            const long long ox = (d < x1 ? d : x1) - (c > x0 ? c : x0);
+            row += (unsigned long long)ox * (unsigned long long)get(i, j);
+        }
+        num += row * (unsigned long long)oy;
+    }
+    return area_round_ties_even(num, (unsigned long long)W * (unsigned long long)H);
+}
 
 }  // namespace lvbgs

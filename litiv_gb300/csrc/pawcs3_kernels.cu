@@ -837,10 +837,12 @@ extern "C" __global__ void __launch_bounds__(256) pw3_k_commit(PwParams P) {
         const PwOut& O = S.out[p];
         flat = (R.flags & kRfFlat) != 0;
         const uint8_t u = S.uFinal[p];
+        // the neighbours' updates write 1 & ROI (:1025-1026): 0 in the ROI's edge band of 128
+        const int roiBit = D.roi[p] & 1;
         const int uRight = (x + 1 < D.W && D.roi[p + 1]) ? (S.uFinal[p + 1] & 1) : 0;
-        const int mStart = (x > 0 && D.roi[p - 1] && (S.uFinal[p - 1] & 1)) ? 1 : (int)S.illum[p];
+        const int mStart = (x > 0 && D.roi[p - 1] && (S.uFinal[p - 1] & 1)) ? roiBit : (int)S.illum[p];
         int mEnd;
-        if (uRight) mEnd = 1;
+        if (uRight) mEnd = roiBit;
         else if (u & 1) mEnd = 1;
         else mEnd = mStart > 0 ? mStart - 1 : 0;
         S.illum[p] = (uint8_t)mEnd;
@@ -928,15 +930,12 @@ extern "C" __global__ void pw3_k_ds(PwParams P) {
     float fLT, fST;
     pw_factors(t, (int)S.nmv, &fLT, &fST);
     const int bx = i % D.dsW, by = i / D.dsW;
-    const float scale = 1.f / (float)(D.dsSX * D.dsSY);
     float e = 0.0f;
     for (int c = 0; c < 3; ++c) {
-        int sum = 0;
-        for (int yy = 0; yy < D.dsSY; ++yy)
-            for (int xx = 0; xx < D.dsSX; ++xx)
-                sum += D.frame[((size_t)(by * D.dsSY + yy) * D.W + bx * D.dsSX + xx) * 3 + c];
-        const int r = __float2int_rn((float)sum * scale);
-        const uint8_t vb = (uint8_t)(r < 0 ? 0 : r > 255 ? 255 : r);
+        const uint8_t* fr = D.frame;
+        const int W = D.W;
+        const uint8_t vb = area_resample(D.W, D.H, D.dsW, D.dsH, bx, by,
+                                         [&](int sx, int sy) { return (int)fr[((size_t)sy * W + sx) * 3 + c]; });
         const size_t k = (size_t)i * 3 + c;
         const float lt = (float)vb * fLT + D.dsLT[k] * (1.0f - fLT);
         const float st = (float)vb * fST + D.dsST[k] * (1.0f - fST);
@@ -965,28 +964,22 @@ extern "C" __global__ void pw3_k_motion_bg(PwParams P, int buf) {
     const uint32_t t = (uint32_t)(D.ctl->frame_idx + 1ull);
     const unsigned long long off = S.pc->lword_offset;
     const int bx = i % D.dsW, by = i / D.dsW;
-    int sum[3] = {0, 0, 0};
-    for (int yy = 0; yy < D.dsSY; ++yy)
-        for (int xx = 0; xx < D.dsSX; ++xx) {
-            const int p = (by * D.dsSY + yy) * D.W + bx * D.dsSX + xx;
-            if (!D.roi[p]) continue;
-            float tw = 0.0f, tc[3] = {0.0f, 0.0f, 0.0f};
+    float a[3], b[3], e = 0.0f;
+    for (int c = 0; c < 3; ++c) {
+        // channel c of the background image (0 outside the ROI), area-down-sampled
+        b[c] = (float)area_resample(D.W, D.H, D.dsW, D.dsH, bx, by, [&](int sx, int sy) {
+            const int p = sy * D.W + sx;
+            if (!D.roi[p]) return 0;
+            float tw = 0.0f, tc = 0.0f;
             for (int j = 0; j < S.L; ++j) {
                 const size_t a = pw_slot(S, buf, j, p);
                 const float w = pw_weight(S.wOcc[a], S.wFirst[a], S.wLast[a], t, off);
-                for (int c = 0; c < 3; ++c) tc[c] = tc[c] + (float)S.wColor[a * 3 + c] * w;
+                tc = tc + (float)S.wColor[a * 3 + c] * w;
                 tw = tw + w;
             }
-            for (int c = 0; c < 3; ++c) {
-                const int r = __float2int_rn(tc[c] / tw);
-                sum[c] += r < 0 ? 0 : r > 255 ? 255 : r;
-            }
-        }
-    const float scale = 1.f / (float)(D.dsSX * D.dsSY);
-    float a[3], b[3], e = 0.0f;
-    for (int c = 0; c < 3; ++c) {
-        const int r = __float2int_rn((float)sum[c] * scale);
-        b[c] = (float)(r < 0 ? 0 : r > 255 ? 255 : r);
+            const int r = __float2int_rn(tc / tw);
+            return r < 0 ? 0 : r > 255 ? 255 : r;
+        });
         a[c] = D.dsLT[(size_t)i * 3 + c];
         e = e + fabsf(a[c] - b[c]);
     }

@@ -63,10 +63,30 @@ __device__ __forceinline__ float pw_weight(uint32_t occ, uint32_t first, uint32_
 struct PwThr {
     uint32_t color, desc;
 };
+
+// (size_t)(sqrt(R) * m) as the reference evaluates it: an unqualified sqrt of a float there is the
+// C library's double sqrt, and the product is taken in double (:119, :267, :663, :993). For a float R
+// and a small integer m that truncation equals the exact floor(m * sqrt(R)), the largest k with
+// k^2 <= m^2 R (a float R lies at least 2^-24/m^2 in relative terms from any such boundary, far more
+// than the two double roundings move the product). A float candidate is corrected by one with an
+// exact comparison: hi + lo = m^2 R exactly (two-product), k^2 exact in float below 2^24.
+__device__ __forceinline__ uint32_t pw_sqrt_floor(float R, uint32_t m) {
+    uint32_t k = (uint32_t)(__fsqrt_rn(R) * (float)m);
+    const float mm = (float)(m * m);
+    if (m * m >= (1u << 24) || k >= 4095u) return (uint32_t)(__dsqrt_rn((double)R) * (double)m);
+    const float hi = mm * R, lo = __fmaf_rn(mm, R, -hi);
+    const auto le = [&](uint32_t kk) {  // kk^2 <= m^2 R
+        const float k2 = (float)(kk * kk);
+        return k2 < hi || (k2 == hi && lo >= 0.0f);
+    };
+    if (!le(k)) --k;
+    else if (le(k + 1)) ++k;
+    return k;
+}
 // nCurrColorDistThreshold / nCurrDescDistThreshold of one channel (:633-634)
 __device__ __forceinline__ PwThr pw_thresholds(float R, uint32_t unstable, uint32_t minColor, uint32_t descOff) {
     PwThr t;
-    t.color = (uint32_t)(__fsqrt_rn(R) * (float)minColor) / 2u;
+    t.color = pw_sqrt_floor(R, minColor) / 2u;
     const unsigned long long sh = (unsigned long long)floorf(R + 0.5f);
     const unsigned long long d = (sh < 64 ? (1ull << sh) : 0ull) + descOff + (unsigned long long)unstable * descOff;
     t.desc = d > 0xffffffffull ? 0xffffffffu : (uint32_t)d;
@@ -108,7 +128,7 @@ namespace lvbgs {
 // nCurrColorDistThreshold / nCurrDescDistThreshold of three channels (:1011-1012)
 __device__ __forceinline__ PwThr pw3_thresholds(float R, uint32_t unstable, uint32_t minColor, uint32_t descOff) {
     PwThr t;
-    t.color = (uint32_t)(__fsqrt_rn(R) * (float)minColor) * 3u;
+    t.color = pw_sqrt_floor(R, minColor) * 3u;
     const unsigned long long sh = (unsigned long long)floorf(R + 0.5f);
     const unsigned long long d = ((sh < 64 ? (1ull << sh) : 0ull) + descOff + (unsigned long long)unstable * descOff) * 3ull;
     t.desc = d > 0xffffffffull ? 0xffffffffu : (uint32_t)d;

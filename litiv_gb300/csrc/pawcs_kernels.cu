@@ -232,9 +232,10 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_local(PwParams P) {
 }
 
 // ------------------------------------------------------------------------------------------
-// illumination chain: the mask a pixel sees is 1 when its left neighbour made an illumination update
-// this frame, else its frame-start value (:686-688, :893-894). Each pixel's outcome is a function of
-// its left neighbour's (two states), so one warp per row scans the compositions 32 pixels at a time.
+// illumination chain: the mask a pixel sees is 1 & ROI when its left neighbour made an illumination
+// update this frame (the neighbour writes 1 & m_oROI, :689-690: 1 inside the ROI, 0 in its edge band
+// of 128), else its frame-start value (:686-688, :893-894). Each pixel's outcome is a function of its
+// left neighbour's (two states), so one warp per row scans the compositions 32 pixels at a time.
 // ------------------------------------------------------------------------------------------
 extern "C" __global__ void __launch_bounds__(256) pw_k_illum(PwParams P) {
     const int gr = blockIdx.x * 8 + (int)threadIdx.x / 32, lane = threadIdx.x & 31;
@@ -247,12 +248,13 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_illum(PwParams P) {
         const int x = x0 + lane;
         const int p = y * D.W + x;
         const bool in = x < D.W && D.roi[p];
-        uint32_t f = 0, m0 = 0;  // f: bit0 = outcome if the left neighbour made no update, bit1 = if it did
+        uint32_t f = 0, m0 = 0, mL = 0;  // f: bit0 = outcome if the left neighbour made no update, bit1 = if it did
         if (in) {
             const uint32_t uvp = S.uv[p];
             m0 = S.illum[p] != 0;
+            mL = D.roi[p] & 1u;  // the mask after the left neighbour's update
             const uint32_t u0 = uvp & 1u, u1 = (uvp >> 1) & 1u;
-            f = (m0 ? u1 : u0) | (u1 << 1);
+            f = (m0 ? u1 : u0) | ((mL ? u1 : u0) << 1);
         }
         // inclusive scan: F = f_lane o f_lane-1 o ... o f_x0
         uint32_t F = f;
@@ -264,7 +266,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_illum(PwParams P) {
         const uint32_t u = (F >> carry) & 1u;
         uint32_t prevU = __shfl_up_sync(0xffffffffu, u, 1);
         if (lane == 0) prevU = carry;
-        if (x < D.W) S.uFinal[p] = in ? (uint8_t)(u | ((prevU || m0) ? 2u : 0u)) : (uint8_t)0;
+        if (x < D.W) S.uFinal[p] = in ? (uint8_t)(u | ((prevU ? mL : m0) ? 2u : 0u)) : (uint8_t)0;
         carry = __shfl_sync(0xffffffffu, u, 31);
     }
 }
@@ -782,12 +784,14 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_commit(PwParams P) {
             S.wFirst[a] = t;
             S.wLast[a] = t;
         }
-        // illumination mask at the end of the frame (:686-688, :893-894): the right neighbour's
-        // update sets 1; else the own update leaves 2-1 = 1; else the start value minus one
+        // illumination mask at the end of the frame (:686-690, :889-890): the right neighbour's
+        // update sets 1 & ROI; else the own update leaves 2-1 = 1; else the start value (1 & ROI
+        // after the left neighbour's update) minus one
+        const int roiBit = D.roi[p] & 1;
         const int uRight = (x + 1 < D.W && D.roi[p + 1]) ? (S.uFinal[p + 1] & 1) : 0;
-        const int mStart = (x > 0 && D.roi[p - 1] && (S.uFinal[p - 1] & 1)) ? 1 : (int)S.illum[p];
+        const int mStart = (x > 0 && D.roi[p - 1] && (S.uFinal[p - 1] & 1)) ? roiBit : (int)S.illum[p];
         int mEnd;
-        if (uRight) mEnd = 1;
+        if (uRight) mEnd = roiBit;
         else if (u & 1) mEnd = 1;
         else mEnd = mStart > 0 ? mStart - 1 : 0;
         S.illum[p] = (uint8_t)mEnd;
@@ -1112,12 +1116,10 @@ extern "C" __global__ void pw_k_ds(PwParams P) {
     float fLT, fST;
     pw_factors(t, (int)S.nmv, &fLT, &fST);
     const int bx = i % D.dsW, by = i / D.dsW;
-    int sum = 0;
-    for (int yy = 0; yy < D.dsSY; ++yy)
-        for (int xx = 0; xx < D.dsSX; ++xx) sum += D.frame[(size_t)(by * D.dsSY + yy) * D.W + bx * D.dsSX + xx];
-    const float scale = 1.f / (float)(D.dsSX * D.dsSY);
-    const int r = __float2int_rn((float)sum * scale);
-    const uint8_t vb = (uint8_t)(r < 0 ? 0 : r > 255 ? 255 : r);
+    const uint8_t* fr = D.frame;
+    const int W = D.W;
+    const uint8_t vb = area_resample(D.W, D.H, D.dsW, D.dsH, bx, by,
+                                     [&](int sx, int sy) { return (int)fr[(size_t)sy * W + sx]; });
     const float lt = (float)vb * fLT + D.dsLT[i] * (1.0f - fLT);
     const float st = (float)vb * fST + D.dsST[i] * (1.0f - fST);
     D.dsLT[i] = lt;
@@ -1484,24 +1486,20 @@ extern "C" __global__ void pw_k_motion_bg(PwParams P, int buf) {
     const uint32_t t = (uint32_t)(D.ctl->frame_idx + 1ull);
     const unsigned long long off = S.pc->lword_offset;
     const int bx = i % D.dsW, by = i / D.dsW;
-    int sum = 0;
-    for (int yy = 0; yy < D.dsSY; ++yy)
-        for (int xx = 0; xx < D.dsSX; ++xx) {
-            const int p = (by * D.dsSY + yy) * D.W + bx * D.dsSX + xx;
-            if (!D.roi[p]) continue;
-            float tw = 0.0f, tc = 0.0f;
-            for (int j = 0; j < S.L; ++j) {
-                const size_t a = pw_slot(S, buf, j, p);
-                const float w = pw_weight(S.wOcc[a], S.wFirst[a], S.wLast[a], t, off);
-                tc = tc + (float)S.wColor[a] * w;
-                tw = tw + w;
-            }
-            const int r = __float2int_rn(tc / tw);
-            sum += r < 0 ? 0 : r > 255 ? 255 : r;
+    // the background image (0 outside the ROI), area-down-sampled
+    const uint8_t v = area_resample(D.W, D.H, D.dsW, D.dsH, bx, by, [&](int sx, int sy) {
+        const int p = sy * D.W + sx;
+        if (!D.roi[p]) return 0;
+        float tw = 0.0f, tc = 0.0f;
+        for (int j = 0; j < S.L; ++j) {
+            const size_t a = pw_slot(S, buf, j, p);
+            const float w = pw_weight(S.wOcc[a], S.wFirst[a], S.wLast[a], t, off);
+            tc = tc + (float)S.wColor[a] * w;
+            tw = tw + w;
         }
-    const float scale = 1.f / (float)(D.dsSX * D.dsSY);
-    const int r = __float2int_rn((float)sum * scale);
-    const uint8_t v = (uint8_t)(r < 0 ? 0 : r > 255 ? 255 : r);
+        const int r = __float2int_rn(tc / tw);
+        return r < 0 ? 0 : r > 255 ? 255 : r;
+    });
     S.dsAbs[i] = fabsf(D.dsLT[i] - (float)v);
 }
 

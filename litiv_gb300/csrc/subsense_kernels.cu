@@ -860,16 +860,12 @@ __device__ void ds_item(const StreamDev& S, int i) {
     const int C = S.C;
     const int dx = i % S.dsW, dy = i / S.dsW;
     const FrameK F = frame_consts(S);
-    const float scale = 1.f / (float)(S.dsSX * S.dsSY);
     uint32_t dmax = 0;
     for (int c = 0; c < C; ++c) {
-        int sum = 0;
-        for (int yy = 0; yy < S.dsSY; ++yy) {
-            const uint8_t* row = S.frame + ((size_t)(dy * S.dsSY + yy) * S.W + (size_t)dx * S.dsSX) * C + c;
-            for (int xx = 0; xx < S.dsSX; ++xx) sum += __ldg(row + xx * C);
-        }
-        int v = __float2int_rn((float)sum * scale);
-        v = v < 0 ? 0 : v > 255 ? 255 : v;
+        const uint8_t* fr = S.frame;
+        const int W = S.W;
+        const int v = area_resample(S.W, S.H, S.dsW, S.dsH, dx, dy,
+                                    [&](int sx, int sy) { return (int)__ldg(fr + ((size_t)sy * W + sx) * C + c); });
         const size_t k = (size_t)i * C + c;
         // accumulateWeighted: dst = src*a + dst*(1-a)
         const float aL = F.fLT, bL = 1.0f - aL, aS = F.fST, bS = 1.0f - aS;

@@ -172,22 +172,60 @@ OC_UNUSED static void add_weighted_mask(float* a, const uint8_t* m, size_t n, do
     }
 }
 
-/* cv::resize(src, dst, (W/8, H/8), INTER_AREA) when the scale is an exact integer
- * (OpenCV's "area fast" case): each output is the mean of its 8x8 block, computed as
- * cvRound(sum * (1.f/64)) (round half to even). Returns 0 when the scale is not integral. */
-OC_UNUSED static int resize_area_div8(const uint8_t* src, int W, int H, int C, uint8_t* dst, int dw, int dh) {
-    if (dw <= 0 || dh <= 0 || W % dw != 0 || H % dh != 0) return 0;
-    const int sx = W / dw, sy = H / dh;
-    const float scale = 1.f / (float)(sx * sy);
+/* cv::resize(src, dst, (dw, dh), INTER_AREA) of an 8-bit image with C interleaved channels.
+ * When the source size is an integral multiple of the output (OpenCV's "area fast" case) each output
+ * is the block mean computed as cvRound(sum * (1.f/area)) (round half to even). Otherwise it is the
+ * exact area-weighted mean of the source pixels under the output pixel's footprint: in units of 1/dw
+ * (1/dh) source pixel i spans [i*dw, (i+1)*dw) and output x spans [x*W, (x+1)*W), every overlap is an
+ * integer, and the output is round(sum(ox * oy * src) / (W * H)) with ties to even, in integers. The
+ * definition follows the mathematics of the area relation (OpenCV documents INTER_AREA as
+ * "resampling using pixel area relation"; its own arithmetic for this case is unpinned here).
+ * Returns 0 when the output is empty. */
+OC_UNUSED static int resize_area_u8(const uint8_t* src, int W, int H, int C, uint8_t* dst, int dw, int dh) {
+    if (dw <= 0 || dh <= 0) return 0;
+    if (W % dw == 0 && H % dh == 0) {
+        const int sx = W / dw, sy = H / dh;
+        const float scale = 1.f / (float)(sx * sy);
+        for (int y = 0; y < dh; ++y)
+            for (int x = 0; x < dw; ++x)
+                for (int c = 0; c < C; ++c) {
+                    int sum = 0;
+                    for (int yy = 0; yy < sy; ++yy)
+                        for (int xx = 0; xx < sx; ++xx) sum += src[((size_t)(y * sy + yy) * W + (x * sx + xx)) * C + c];
+                    dst[((size_t)y * dw + x) * C + c] = sat_u8f((float)sum * scale);
+                }
+        return 1;
+    }
+    const unsigned long long den = (unsigned long long)W * (unsigned long long)H;
     for (int y = 0; y < dh; ++y)
-        for (int x = 0; x < dw; ++x)
+        for (int x = 0; x < dw; ++x) {
+            const long long x0 = (long long)x * W, x1 = x0 + W, y0 = (long long)y * H, y1 = y0 + H;
+            const int i0 = (int)(x0 / dw), i1 = (int)((x1 + dw - 1) / dw);
+            const int j0 = (int)(y0 / dh), j1 = (int)((y1 + dh - 1) / dh);
             for (int c = 0; c < C; ++c) {
-                int sum = 0;
-                for (int yy = 0; yy < sy; ++yy)
-                    for (int xx = 0; xx < sx; ++xx) sum += src[((size_t)(y * sy + yy) * W + (x * sx + xx)) * C + c];
-                dst[((size_t)y * dw + x) * C + c] = sat_u8f((float)sum * scale);
+                unsigned long long num = 0;
+                for (int j = j0; j < j1; ++j) {
+                    const long long a = (long long)j * dh, b = a + dh;
+                    const long long oy = (b < y1 ? b : y1) - (a > y0 ? a : y0);
+                    unsigned long long row = 0;
+                    for (int i = i0; i < i1; ++i) {
+                        const long long cc = (long long)i * dw, d = cc + dw;
+                        const long long ox = (d < x1 ? d : x1) - (cc > x0 ? cc : x0);
+                        row += (unsigned long long)ox * src[((size_t)j * W + i) * C + c];
+                    }
+                    num += row * (unsigned long long)oy;
+                }
+                unsigned long long q = num / den;
+                const unsigned long long r2 = (num % den) * 2ull;
+                if (r2 > den || (r2 == den && (q & 1ull))) ++q;
+                dst[((size_t)y * dw + x) * C + c] = (uint8_t)(q > 255ull ? 255ull : q);
             }
+        }
     return 1;
+}
+/* the frame-level down-sampling of SuBSENSE (BackgroundSubtractorSuBSENSE.cpp:568) */
+OC_UNUSED static int resize_area_div8(const uint8_t* src, int W, int H, int C, uint8_t* dst, int dw, int dh) {
+    return resize_area_u8(src, W, H, C, dst, dw, dh);
 }
 
 /* cv::accumulateWeighted(src, dst, alpha): dst = src*a + dst*(1-a) with a = (float)alpha,

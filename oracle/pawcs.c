@@ -167,11 +167,13 @@ static void thresholds(const opawcs_t* o, size_t px, size_t* colorThr, size_t* d
     const float R = o->R[px];
     const size_t base = ((size_t)1 << (size_t)floorf(R + 0.5f)) + o->p.desc_dist_threshold_offset +
                         (size_t)o->unstable[px] * o->p.desc_dist_threshold_offset;
+    /* the reference's unqualified sqrt of a float is the C library's double sqrt (only <cmath> is in
+     * scope, whose global namespace has no float overload), and the product is taken in double */
     if (o->C == 1) {
-        *colorThr = (size_t)(sqrtf(R) * (float)o->p.min_color_dist_threshold) / 2;
+        *colorThr = (size_t)(sqrt((double)R) * (double)o->p.min_color_dist_threshold) / 2;
         *descThr = base;
     } else {
-        *colorThr = (size_t)(sqrtf(R) * (float)o->p.min_color_dist_threshold) * 3;
+        *colorThr = (size_t)(sqrt((double)R) * (double)o->p.min_color_dist_threshold) * 3;
         *descThr = base * 3;
     }
 }
@@ -244,21 +246,9 @@ static void pflood_holes(opawcs_t* o, const uint8_t* pre, uint8_t* holes) {
     for (size_t i = 0; i < o->npx; ++i) holes[i] = (pre[i] == 0 && !o->visited[i]) ? 255 : 0;
 }
 
-/* cv::resize(src, dst, (dw, dh), INTER_AREA) of an 8-bit image whose size is an integral
- * multiple of the output (the "area fast" case): cvRound(block sum * (1.f/area)) */
+/* cv::resize(src, dst, (dw, dh), INTER_AREA) of an 8-bit image (resize_area_u8, oracle/common.h) */
 static int resize_area_int(const uint8_t* src, int W, int H, int C, uint8_t* dst, int dw, int dh) {
-    if (dw <= 0 || dh <= 0 || W % dw != 0 || H % dh != 0) return 0;
-    const int sx = W / dw, sy = H / dh;
-    const float scale = 1.f / (float)(sx * sy);
-    for (int y = 0; y < dh; ++y)
-        for (int x = 0; x < dw; ++x)
-            for (int c = 0; c < C; ++c) {
-                int sum = 0;
-                for (int yy = 0; yy < sy; ++yy)
-                    for (int xx = 0; xx < sx; ++xx) sum += src[((size_t)(y * sy + yy) * W + (x * sx + xx)) * C + c];
-                dst[((size_t)y * dw + x) * C + c] = sat_u8f((float)sum * scale);
-            }
-    return 1;
+    return resize_area_u8(src, W, H, C, dst, dw, dh);
 }
 
 /* cv::blur(src, dst, 3x3, BORDER_REPLICATE) on CV_32F: normalized box filter whose sums run in
@@ -546,10 +536,11 @@ int opawcs_initialize(opawcs_t* o, const uint8_t* img, int W, int H, int C, cons
     o->gw_h = H / GWORD_LOOKUP_MAPS_DOWNSAMPLE_RATIO;
     const size_t nds = (size_t)o->ds_w * o->ds_h;
     o->ds_roi = (uint8_t*)calloc(nds ? nds : 1, 1);
-    if (nds && !resize_area_int(newroi, W, H, 1, o->ds_roi, o->ds_w, o->ds_h)) {
+    if (!nds) { /* the reference's cv::resize to an empty size (:446) throws */
         pfree_state(o);
-        return OSUB_EUNSUPPORTED; /* INTER_AREA with a non-integral scale is not restated */
+        return OSUB_EBADARG;
     }
+    resize_area_int(newroi, W, H, 1, o->ds_roi, o->ds_w, o->ds_h);
     o->last_nonflat_ratio = 0.0f;
     o->L = o->p.max_words;
     const size_t maxG = o->p.max_words / 2;

@@ -156,7 +156,9 @@ inline void medianBlur(InputArray src_, OutputArray dst_, int k) {
 
 // INTER_AREA when the source size is an integral multiple of the output (OpenCV's "area fast"
 // case): each output element is saturate_cast(block sum * (1.f/area)), the sum in int (8-bit
-// sources) or double (float sources). INTER_NEAREST: source x = floor(dx * (1/(dw/W))), clamped.
+// sources) or double (float sources); for other scales the exact area-weighted mean, rounded half to
+// even (the same definition as oracle/common.h resize_area_u8). INTER_NEAREST: source x =
+// floor(dx * (1/(dw/W))), clamped.
 inline void resize(InputArray src_, OutputArray dst_, Size dsize, double fx = 0, double fy = 0,
                    int interpolation = INTER_LINEAR) {
     (void)fx;
@@ -164,9 +166,36 @@ inline void resize(InputArray src_, OutputArray dst_, Size dsize, double fx = 0,
     const Mat src = src_.getMat();
     const int W = src.cols, H = src.rows, cn = src.channels(), dw = dsize.width, dh = dsize.height;
     Mat out(dh, dw, src.type());
-    if (interpolation == INTER_AREA) {
-        if (dw <= 0 || dh <= 0 || W % dw || H % dh)
-            throw std::runtime_error("resize(INTER_AREA): only integral scales are supported");
+    if (interpolation == INTER_AREA && (dw <= 0 || dh <= 0)) throw std::runtime_error("resize: empty output size");
+    if (interpolation == INTER_AREA && (W % dw || H % dh)) {
+        // non-integral scale: the exact area-weighted mean of the source pixels under each output
+        // pixel (overlaps are integers in units of 1/dw, 1/dh), rounded half to even; 8-bit only
+        if (src.depth() != CV_8U) throw std::runtime_error("resize(INTER_AREA): non-integral scales of 8-bit images only");
+        const unsigned long long den = (unsigned long long)W * (unsigned long long)H;
+        for (int y = 0; y < dh; ++y)
+            for (int x = 0; x < dw; ++x) {
+                const long long x0 = (long long)x * W, x1 = x0 + W, y0 = (long long)y * H, y1 = y0 + H;
+                const int i0 = (int)(x0 / dw), i1 = (int)((x1 + dw - 1) / dw);
+                const int j0 = (int)(y0 / dh), j1 = (int)((y1 + dh - 1) / dh);
+                for (int c = 0; c < cn; ++c) {
+                    unsigned long long num = 0;
+                    for (int j = j0; j < j1; ++j) {
+                        const long long a = (long long)j * dh, b = a + dh;
+                        const long long oy = std::min(b, y1) - std::max(a, y0);
+                        unsigned long long row = 0;
+                        for (int i = i0; i < i1; ++i) {
+                            const long long cc = (long long)i * dw, d = cc + dw;
+                            row += (unsigned long long)(std::min(d, x1) - std::max(cc, x0)) * src.ptr(j)[i * cn + c];
+                        }
+                        num += row * (unsigned long long)oy;
+                    }
+                    unsigned long long q = num / den;
+                    const unsigned long long r2 = (num % den) * 2ull;
+                    if (r2 > den || (r2 == den && (q & 1ull))) ++q;
+                    out.ptr(y)[x * cn + c] = (uchar)std::min(q, 255ull);
+                }
+            }
+    } else if (interpolation == INTER_AREA) {
         const int sx = W / dw, sy = H / dh;
         const float scale = 1.f / (float)(sx * sy);
         for (int y = 0; y < dh; ++y)

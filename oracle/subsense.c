@@ -588,7 +588,7 @@ int osub_apply(osub_t* o, const uint8_t* img, uint8_t* mask, double lr) {
     o->last_colordiff = 0;
     /* frame-level analysis, :567-611 */
     if (o->lr_scaling) {
-        if (!resize_area_div8(img, W, H, (int)C, o->dsframe, o->ds_w, o->ds_h)) return OSUB_EUNSUPPORTED;
+        if (!resize_area_div8(img, W, H, (int)C, o->dsframe, o->ds_w, o->ds_h)) return OSUB_EBADARG;
         const size_t nds = (size_t)o->ds_w * o->ds_h * C;
         accumulate_weighted(o->dsframe, o->dsLT, nds, (double)fLT);
         accumulate_weighted(o->dsframe, o->dsST, nds, (double)fST);

@@ -276,3 +276,11 @@ def _split_batch_case(groups):
     for b, a in zip(batched, alone):
         for name in ("R", "T", "V", "DMIN_LT", "UNSTABLE", "LAST_FG", "SAMPLE_COLOR", "SAMPLE_DESC"):
             assert np.array_equal(b.state_map(name), a.state_map(name)), name
+
+
+@pytest.mark.parametrize("W,H", [(640, 350), (595, 245)])
+def test_non_integral_down_sampling_bitexact(W, H):
+    """Frame sizes whose 1/8 frame-level down-sampling is not integral (INTER_AREA as the exact
+    area-weighted mean, :568): masks and every map, including the down-sampled means."""
+    s = SyntheticStream(0, seed=42, width=W, height=H)
+    run_pair(frames_of(s, 16), seed=14, check_every=3)

@@ -306,3 +306,11 @@ def test_three_channel_set_roi_reinitializes_from_background():
     for f in fr[6:]:
         assert np.array_equal(gpu.apply(f), ora.apply(f, 0.0))
     assert not compare_state(gpu, ora)
+
+
+@pytest.mark.parametrize("W,H,C", [(595, 245, 1), (640, 350, 3)])
+def test_non_integral_down_sampling(W, H, C):
+    """Sizes whose 1/8 down-sampling is not integral: INTER_AREA of the ROI (:446) and of each frame
+    (:1475) as the exact area-weighted mean."""
+    s = SyntheticStream(0, 0, 43, width=W, height=H, channels=C)
+    run_pair([s.render(t) for t in range(8)], seed=15, check_every=2)

@@ -199,3 +199,15 @@ def test_pawcs_moving_camera_mode_switch():
         if t in (499, 500, 999, 1000):
             modes[t] = ref.scalars()["using_moving_camera"]
     assert modes == {499: 0, 500: 1, 999: 1, 1000: 0}
+
+
+@pytest.mark.parametrize("algo,shape", [("subsense", (350, 640, 3)), ("subsense", (245, 595, 3)),
+                                        ("pawcs", (245, 595, 1)), ("pawcs", (350, 640, 3))])
+def test_non_integral_frame_level_down_sampling(algo, shape):
+    """Frame sizes whose 1/8 down-sampling is not integral (common CDnet sizes): INTER_AREA with a
+    non-integral scale in the frame-level analysis (BackgroundSubtractorSuBSENSE.cpp:568,
+    BackgroundSubtractorPAWCS.cpp:446,1475)."""
+    H, W, C = shape
+    frames = _frames(0, 8, 41, width=W, height=H, channels=C)
+    pair = sub_pair if algo == "subsense" else pawcs_pair
+    pair(frames, seed=13, check_every=2)
