@@ -231,6 +231,20 @@ int lvbgs_debug_tick_profile(lvbgs_handle h, int batched, double* out_ms, int ma
  * written. */
 int lvbgs_debug_repair_phases(lvbgs_handle h, int batched, double* out_us, int max_n);
 
+/* Failure detection (tests): no counterpart in the reference. Makes one of the device-side bounded
+ * waits of h's next frame step (lvbgs_apply, or a batched step h leads) run out, so that the path that
+ * gives up can be tested without a fault: the kernels return and the call reports the status below;
+ * the model state of the streams in that step is then undefined (initialize them again), and the
+ * context and every other handle stay usable. One-shot.
+ *   LVBGS_FAULT_BARRIER_TIMEOUT  the repair kernel's grid barrier waits 2 ms for a CTA that never
+ *                                arrives, then gives up: LVBGS_DEVICE_TIMEOUT
+ *   LVBGS_FAULT_REPAIR_LIMIT     the raster-order repair may run no round: LVBGS_DEVICE_ERROR when the
+ *                                frame needs one
+ *   LVBGS_FAULT_PAWCS_ROUNDS     PAWCS's fixed point may run one round: LVBGS_DEVICE_ERROR when the
+ *                                frame needs more */
+enum { LVBGS_FAULT_NONE = 0, LVBGS_FAULT_BARRIER_TIMEOUT = 1, LVBGS_FAULT_REPAIR_LIMIT = 2, LVBGS_FAULT_PAWCS_ROUNDS = 3 };
+lvbgs_status lvbgs_debug_inject_fault(lvbgs_handle h, int kind);
+
 /* ---- PAWCS (BackgroundSubtractorPAWCS, modules/video/src/BackgroundSubtractorPAWCS.cpp) ----
  * A handle created with LVBGS_ALGO_PAWCS runs PAWCS on single-channel (:608-934) and three-channel
  * (:935-1299) frames. lvbgs_params maps onto the constructor (BackgroundSubtractorPAWCS.hpp:47-51):

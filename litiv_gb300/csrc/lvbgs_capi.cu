@@ -189,6 +189,7 @@ struct lvbgs_ctx {
     unsigned long long pw_frames = 0;
     unsigned long long pw_offset = 1000;
     int pw_rounds_last = 0;
+    int dbg_fault = 0;  // one-shot fault injection of the next frame step (lvbgs_debug_inject_fault)
 };
 
 namespace {
@@ -370,6 +371,12 @@ lvbgs_status launch_tick(lvbgs_handle errh, Workspace& ws, int n, cudaStream_t s
     LV_CUDA(errh, coop_grid(&maxBlocks), "occupancy query");
     if (maxBlocks <= 0) return fail(errh, LVBGS_DEVICE_ERROR, "repair kernel cannot be resident on this device");
     TickParams P;
+    // one-shot fault injection of the lead handle (lvbgs_debug_inject_fault): waits that give up
+    const int fault = errh ? errh->dbg_fault : 0;
+    if (errh) errh->dbg_fault = 0;
+    P.dbgFault = fault;
+    P.barrierNs = fault == LVBGS_FAULT_BARRIER_TIMEOUT ? kDebugBarrierNs : kBarrierNs;
+    P.maxRepairIters = fault == LVBGS_FAULT_REPAIR_LIMIT ? 0 : kRepairIterLimit;
     P.streams = ws.d_streams;
     P.nStreams = n;
     P.totalTiles = totalTiles;
@@ -865,8 +872,11 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
     };
     const bool c3 = h->C == 3;
     int round = 0;
+    const int maxRounds = h->dbg_fault == LVBGS_FAULT_PAWCS_ROUNDS ? 1 : 64;
+    h->dbg_fault = 0;
     for (;; ++round) {
-        if (round >= 64) return fail(h, LVBGS_DEVICE_ERROR, "PAWCS raster-order fixed point did not converge in 64 rounds");
+        if (round >= maxRounds)
+            return fail(h, LVBGS_DEVICE_ERROR, "PAWCS raster-order fixed point did not converge in the round limit");
         P.round = round;
         if (c3) {
             // three channels: the local pass applies the earlier updaters' loops itself
@@ -972,6 +982,13 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
 }
 
 }  // namespace
+
+lvbgs_status lvbgs_debug_inject_fault(lvbgs_handle h, int kind) {
+    if (!h) return fail(nullptr, LVBGS_BAD_ARG, "null handle");
+    if (kind < LVBGS_FAULT_NONE || kind > LVBGS_FAULT_PAWCS_ROUNDS) return fail(h, LVBGS_BAD_ARG, "unknown fault kind");
+    h->dbg_fault = kind;
+    return LVBGS_OK;
+}
 
 lvbgs_status lvbgs_default_params(lvbgs_algo algo, lvbgs_params* out) {
     if (!out) return fail(nullptr, LVBGS_BAD_ARG, "null output");

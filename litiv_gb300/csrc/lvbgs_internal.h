@@ -190,7 +190,13 @@ struct TickParams {
     unsigned long long* rlist[2];
     unsigned int listCap;
     int totalSegs, colBlocks;  // median: column segments of all streams; 256-pixel column blocks of the widest
+    unsigned long long barrierNs;  // limit of one grid-barrier wait of the repair, then ERR_BARRIER_TIMEOUT
+    int maxRepairIters;            // repair rounds before ERR_REPAIR_LIMIT
+    int dbgFault;                  // injected fault (lvbgs_debug_inject_fault), 0: none
 };
+constexpr unsigned long long kBarrierNs = 2000000000ull;  // 2 s
+constexpr unsigned long long kDebugBarrierNs = 2000000ull;  // 2 ms, for the injected barrier timeout
+constexpr int kRepairIterLimit = 4096;
 
 // mask bit planes of a stream (scratch of one frame step; bits beyond the frame width are 0)
 enum { BP_CLOSED = 0, BP_RAW, BP_HOLES, BP_COMB, BP_FG, BP_COUNT };

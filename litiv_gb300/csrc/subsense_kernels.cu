@@ -35,8 +35,6 @@ __constant__ int c_nb5[24][2] = {{-2, 2}, {-1, 2}, {0, 2},   {1, 2},   {2, 2},  
                                  {1, 1},  {2, 1},  {-2, 0},  {-1, 0},  {1, 0},   {2, 0},   {-2, -1}, {-1, -1},
                                  {0, -1}, {1, -1}, {2, -1},  {-2, -2}, {-1, -2}, {0, -2},  {1, -2}, {2, -2}};
 
-constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
-constexpr int kMaxRepairIters = 4096;
 constexpr int kUFLimit = 1 << 22;
 
 // ------------------------------------------------------------------------------------------
@@ -50,8 +48,8 @@ __device__ __forceinline__ unsigned long long gtimer() {
 __device__ __forceinline__ unsigned int ld_volatile(const unsigned int* p) { return *(const volatile unsigned int*)p; }
 
 // Grid-wide barrier for a cooperative launch (all CTAs co-resident). The wait is bounded: after
-// kBarrierTimeoutNs the CTA records ERR_BARRIER_TIMEOUT and every CTA leaves at its next check.
-__device__ bool grid_sync(TickWork* w) {
+// timeoutNs the CTA records ERR_BARRIER_TIMEOUT and every CTA leaves at its next check.
+__device__ bool grid_sync(TickWork* w, unsigned long long timeoutNs) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -71,7 +69,7 @@ __device__ bool grid_sync(TickWork* w) {
                     break;
                 }
                 __nanosleep(40);
-                if (gtimer() - t0 > kBarrierTimeoutNs) {
+                if (gtimer() - t0 > timeoutNs) {
                     atomicOr(&w->err, ERR_BARRIER_TIMEOUT);
                     ok = 0;
                     break;
@@ -1752,12 +1750,18 @@ extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_resolve(TickParam
 extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_repair(TickParams P) {
     TickWork* w = P.work;
     if (blockIdx.x == 0 && threadIdx.x == 0 && w->nts < 40u) w->ts[w->nts++] = gtimer();  // phase profile
+    if (P.dbgFault == LVBGS_FAULT_BARRIER_TIMEOUT) {
+        // injected fault: every CTA but CTA 0 waits at a barrier CTA 0 never reaches; each wait gives
+        // up after P.barrierNs and records ERR_BARRIER_TIMEOUT, and every CTA returns
+        if (blockIdx.x != 0) grid_sync(w, P.barrierNs);
+        return;
+    }
     int iter = 0;
     for (;;) {
         const int par = iter & 1;
         const unsigned int n = ld_volatile(&w->dcount[par]);
         if (n == 0u) break;
-        if (iter >= kMaxRepairIters) {
+        if (iter >= P.maxRepairIters) {
             if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&w->err, ERR_REPAIR_LIMIT);
             return;
         }
@@ -1790,7 +1794,7 @@ extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_repair(TickParams
                     atomicAdd(&S.ctl->st_rematched, (unsigned long long)__popc(grp));
             }
         }
-        if (!grid_sync(w)) return;
+        if (!grid_sync(w, P.barrierNs)) return;
         const unsigned int nr0 = ld_volatile(&w->rcount[par]);
         const unsigned int nr = nr0 < P.listCap ? nr0 : P.listCap;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1812,7 +1816,7 @@ extern "C" __global__ void __launch_bounds__(kThreads) lvbgs_k_repair(TickParams
                 reresolve_item(P, si, S, p, S.ctl->stamp_base + (uint32_t)iter + 2u, par);
             }
         }
-        if (!grid_sync(w)) return;
+        if (!grid_sync(w, P.barrierNs)) return;
         ++iter;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) w->iters = (unsigned)iter;
