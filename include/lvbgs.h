@@ -147,14 +147,15 @@ lvbgs_status lvbgs_get_roi(lvbgs_handle h, uint8_t* out);
 
 /* sizes of an initialized handle */
 lvbgs_status lvbgs_get_size(lvbgs_handle h, int* width, int* height, int* channels);
-/* device bytes of the model state of a width x height x channels SuBSENSE stream (admission control) */
+/* device bytes of the model state of a width x height x channels stream of `algo` (admission control;
+ * the size of a spill buffer) */
 size_t lvbgs_state_bytes(lvbgs_algo algo, int width, int height, int channels, size_t bg_samples);
 /* all device bytes an initialized, resident handle holds (model, scratch and its own workspace) */
 size_t lvbgs_device_bytes(lvbgs_algo algo, int width, int height, int channels, size_t bg_samples);
 
-/* Moves a stream's whole device state to `host_buffer` (lvbgs_state_bytes() bytes, pinned memory
- * recommended) and frees the device model; lvbgs_restore() uploads it again. The model evolves
- * bit-identically across a spill/restore pair. */
+/* Moves a stream's whole device state (SuBSENSE or PAWCS) to `host_buffer` (lvbgs_state_bytes()
+ * bytes, pinned memory recommended) and frees the device model; lvbgs_restore() uploads it again.
+ * The model evolves bit-identically across a spill/restore pair. */
 lvbgs_status lvbgs_spill(lvbgs_handle h, void* host_buffer, size_t bytes);
 lvbgs_status lvbgs_restore(lvbgs_handle h, const void* host_buffer, size_t bytes);
 

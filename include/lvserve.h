@@ -73,8 +73,9 @@ lvbgs_status lvserve_destroy(lvserve_handle s);
 
 /* Opens a stream (BackgroundSubtractorSuBSENSE_ / BackgroundSubtractorPAWCS_ constructor +
  * initialize(img, roi)); the image and roi are copied, and initialize() runs when the stream is
- * admitted. SuBSENSE streams are batched into ticks; PAWCS streams (single-channel) run frame by
- * frame on the PAWCS lanes and are never spilled. LVBGS_BUSY at max_live; LVBGS_BAD_SIZE if the
+ * admitted. SuBSENSE streams are batched into ticks; PAWCS streams (one or three channels) run frame
+ * by frame on the PAWCS lanes. Idle streams of either algorithm spill to pinned host memory when room
+ * is needed. LVBGS_BUSY at max_live; LVBGS_BAD_SIZE if the
  * stream alone can never fit the budget. */
 lvbgs_status lvserve_open(lvserve_handle s, lvbgs_algo algo, const lvbgs_params* params, const uint8_t* init_image,
                           int width, int height, int channels, size_t stride, const uint8_t* roi, int* stream_id);

@@ -255,6 +255,13 @@ class BackgroundSubtractorPAWCS:
     getParallelAlgoType = BackgroundSubtractorSuBSENSE.getParallelAlgoType
     _need_init = BackgroundSubtractorSuBSENSE._need_init
 
+    spill = BackgroundSubtractorSuBSENSE.spill
+    restore = BackgroundSubtractorSuBSENSE.restore
+
+    def state_bytes(self):
+        H, W, Cc = self._need_init()
+        return L.lib().lvbgs_state_bytes(L.ALGO_PAWCS, W, H, Cc, self.params.bg_samples)
+
     def refreshModel(self, nBaseOccCount, fOccDecrFrac, bForceFGUpdate=False):
         _check(L.lib().lvbgs_pawcs_refresh_model(self._h, int(nBaseOccCount), float(fOccDecrFrac),
                                                  1 if bForceFGUpdate else 0), self._h)

@@ -1681,7 +1681,6 @@ size_t lvbgs_device_bytes(lvbgs_algo algo, int W, int H, int C, size_t N) {
 lvbgs_status lvbgs_spill(lvbgs_handle h, void* host, size_t bytes) {
     lvbgs_status s = check_ready(h);
     if (s != LVBGS_OK) return s;
-    if (h->algo != LVBGS_ALGO_SUBSENSE) return fail(h, LVBGS_UNSUPPORTED, "spilling is implemented for SuBSENSE streams");
     if (!host || bytes < h->persistBytes) return fail(h, LVBGS_BAD_ARG, "spill buffer is smaller than lvbgs_state_bytes()");
     LV_CUDA(h, cudaStreamSynchronize(h->stream), "spill");
     LV_CUDA(h, cudaMemcpy(host, h->dmem, h->persistBytes, cudaMemcpyDeviceToHost), "spill copy");
@@ -1698,6 +1697,22 @@ lvbgs_status lvbgs_restore(lvbgs_handle h, const void* host, size_t bytes) {
     if (!h->initialized || !h->spilled) return fail(h, LVBGS_NOT_INITIALIZED, "stream is not spilled");
     if (bytes < h->persistBytes) return fail(h, LVBGS_BAD_ARG, "restore buffer is smaller than lvbgs_state_bytes()");
     cudaSetDevice(h->device);
+    if (h->algo == LVBGS_ALGO_PAWCS) {
+        // PAWCS: the persistent prefix of the layout holds every cross-frame array (control blocks,
+        // word planes, feedback and mask maps, sort tables, spatial word maps); the rest is per-frame
+        // scratch, and the device descriptors are rebuilt from the handle's parameters
+        const int L = h->pd.L, G = h->pd.G;
+        const PwLayout Lo = pw_layout(h->W, h->H, h->C, L, G);
+        LV_CUDA(h, cudaMalloc(&h->dmem, Lo.total), "model allocation");
+        LV_CUDA(h, cudaMemcpy(h->dmem, host, h->persistBytes, cudaMemcpyHostToDevice), "restore copy");
+        LV_CUDA(h, cudaMemset(h->dmem + h->persistBytes, 0, Lo.total - h->persistBytes), "scratch reset");
+        pw_fill(h, Lo, L, G);
+        lvbgs_status s = pw_upload_desc(h, h->stream);
+        if (s != LVBGS_OK) return s;
+        LV_CUDA(h, cudaStreamSynchronize(h->stream), "restore");
+        h->spilled = false;
+        return LVBGS_OK;
+    }
     const Layout L = make_layout(h->W, h->H, h->C, h->prm.bg_samples);
     LV_CUDA(h, cudaMalloc(&h->dmem, L.total), "model allocation");
     LV_CUDA(h, cudaMemcpy(h->dmem, host, h->persistBytes, cudaMemcpyHostToDevice), "restore copy");

@@ -185,16 +185,34 @@ int plan_room(size_t used, size_t budget, size_t need, const size_t* bytes, cons
 }
 
 bool spill_stream(lvserve_ctx* s, SStream* x) {
+    const bool lane = x->algo == LVBGS_ALGO_PAWCS;
+    if (lane) {
+        // PAWCS frames run on the lanes: claim the stream as a lane claims a frame, so that no lane
+        // starts one of its frames while its state is copied out
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (x->state != S_RESIDENT || x->inFlight || !x->q.empty()) return false;
+        x->inFlight = true;
+    }
+    auto release = [&] {
+        if (!lane) return;
+        std::lock_guard<std::mutex> lk(s->mu);
+        x->inFlight = false;
+    };
     size_t cap = 0;
     void* buf = x->spill ? x->spill : take_pinned(s, x->stateBytes, &cap);
-    if (!buf) return false;
+    if (!buf) {
+        release();
+        return false;
+    }
     if (!x->spill) x->spillCap = cap;
     x->spill = buf;
     if (lvbgs_spill(x->h, buf, x->spillCap) != LVBGS_OK) {
         set_err(s, lvbgs_last_error(x->h));
+        release();
         return false;
     }
     std::lock_guard<std::mutex> lk(s->mu);
+    if (lane) x->inFlight = false;
     x->state = S_SPILLED;
     s->used -= x->bytes;
     s->hostSpilled += x->stateBytes;
@@ -216,7 +234,6 @@ bool make_room(lvserve_ctx* s, size_t need, const SStream* except) {
         for (auto& kv : s->streams) {
             SStream* x = kv.second.get();
             if (x == except || x->state != S_RESIDENT || x->inFlight || !x->q.empty()) continue;
-            if (x->algo != LVBGS_ALGO_SUBSENSE) continue;  // spilling is implemented for SuBSENSE streams
             if (s->cfg.host_spill_budget_bytes && s->hostSpilled + x->stateBytes > s->cfg.host_spill_budget_bytes)
                 continue;
             cand.push_back(x);

@@ -25,7 +25,7 @@ FAULT_BARRIER_TIMEOUT, FAULT_REPAIR_LIMIT, FAULT_PAWCS_ROUNDS = 1, 2, 3
 
 
 def _inject(model, kind):
-    assert L.lib().lvbgs_debug_inject_fault(C.c_void_p(model.handle), kind) == L.OK
+    assert L.lib().lvbgs_debug_inject_fault(model.handle, kind) == L.OK
 
 
 def _frames(n, seed, channels=3, **kw):
@@ -132,4 +132,4 @@ def test_inject_fault_argument_checks():
     lib = L.lib()
     assert lib.lvbgs_debug_inject_fault(None, FAULT_BARRIER_TIMEOUT) == L.BAD_ARG
     m = BackgroundSubtractorSuBSENSE(seed=1)
-    assert lib.lvbgs_debug_inject_fault(C.c_void_p(m.handle), 99) == L.BAD_ARG
+    assert lib.lvbgs_debug_inject_fault(m.handle, 99) == L.BAD_ARG

@@ -314,3 +314,25 @@ def test_non_integral_down_sampling(W, H, C):
     (:1475) as the exact area-weighted mean."""
     s = SyntheticStream(0, 0, 43, width=W, height=H, channels=C)
     run_pair([s.render(t) for t in range(8)], seed=15, check_every=2)
+
+
+@pytest.mark.parametrize("channels", [1, 3])
+def test_spill_restore_is_transparent(channels):
+    """lvbgs_spill / lvbgs_restore of a PAWCS stream: the model evolves bit-identically across the pair
+    (every mask and, at the end, every map equal to the oracle's)."""
+    s = SyntheticStream(0, 0, 44, width=128, height=96, channels=channels)
+    frames = [s.render(t) for t in range(14)]
+    a = BackgroundSubtractorPAWCS(seed=3)
+    ora = pyoracle.OraclePAWCS(seed=3)
+    a.initialize(frames[0])
+    ora.initialize(frames[0])
+    for t in range(1, 14):
+        if t in (5, 9):
+            buf = bytearray(a.state_bytes())
+            a.spill(buf)
+            with pytest.raises(LvException):
+                a.apply(frames[t])
+            a.restore(buf)
+        assert np.array_equal(a.apply(frames[t]), ora.apply(frames[t])), "frame %d" % t
+    bad = compare_state(a, ora)
+    assert not bad, "; ".join(bad)

@@ -208,3 +208,43 @@ def test_pawcs_and_subsense_streams_served_together_equal_alone():
         assert diff == 0, "stream %d frame %d: served mask differs from the stream alone at %d px" % (i, t, diff)
     assert st["pawcs_frames"] == 2 * (n_frames - 1)
 
+
+
+@pytest.mark.gpu
+def test_pawcs_streams_spill_and_come_back_equal_alone():
+    # two PAWCS streams under a budget that holds one of them at a time: they take turns, so the
+    # idle one spills to pinned host memory (claimed from the PAWCS lanes first) and is restored when
+    # its next frames arrive; every mask must equal the same stream run alone
+    from litiv_gb300 import BackgroundSubtractorPAWCS
+    lib = L.lib()
+    mix = [(96, 72, 1, 41), (160, 120, 3, 42)]
+    n_frames = 13
+    data = [_frames(W, H, Cn, seed, n_frames) for (W, H, Cn, seed) in mix]
+    alone = []
+    for (_, _, _, seed), fr in zip(mix, data):
+        b = BackgroundSubtractorPAWCS(seed=seed)
+        b.initialize(fr[0])
+        alone.append([b.apply(f) for f in fr[1:]])
+    need = [lib.lvbgs_device_bytes(L.ALGO_PAWCS, W, H, Cn, 50) + 32 * W * H for (W, H, Cn, _) in mix]
+    budget = max(need) + 1024
+    assert sum(need) > budget
+    with serving.StreamServer(hbm_budget_bytes=budget, idle_spill_ms=0.0, max_queue=64, pawcs_lanes=1) as srv:
+        ids = [srv.open(fr[0], params={"seed": seed}, algo=L.ALGO_PAWCS) for fr, (_, _, _, seed) in zip(data, mix)]
+        masks = {}
+        results = []
+        for k, i in enumerate([0, 1, 0, 1]):
+            for t in range(1 + (k // 2) * 6, 7 + (k // 2) * 6):
+                W, H = mix[i][0], mix[i][1]
+                m = np.full((H, W), 77, np.uint8)
+                masks[(i, t)] = m
+                assert srv.submit(ids[i], data[i][t], m, tag=t)
+            srv.drain()
+            results += srv.poll(4096)
+        st = srv.stats()
+    assert all(r[2] == L.OK for r in results), [r for r in results if r[2] != L.OK][:3]
+    assert len(results) == len(masks) == 2 * (n_frames - 1)
+    for (i, t), m in masks.items():
+        diff = int((m != alone[i][t - 1]).sum())
+        assert diff == 0, "stream %d frame %d: served mask differs from the stream alone at %d px" % (i, t, diff)
+    assert st["spills"] > 0 and st["restores"] > 0, st
+    assert st["peak_device_bytes"] <= budget
