@@ -222,14 +222,17 @@ def single_stream_run(config, n_frames, stream, cpu=True, cpu_frames=4):
     s = SyntheticStream(config, 0, 1)
     W, H = s.cfg.width, s.cfg.height
     n = min(n_frames, s.n_frames)
+    from litiv_gb300.metrics import BinClassif
     dev = torch.empty((n,) + s.shape, dtype=torch.uint8, device="cuda")
+    dgt = torch.empty((n, H, W), dtype=torch.uint8, device="cuda")
     for t in range(n):
-        s.render_device(t, dev[t].data_ptr(), cuda_stream=stream.cuda_stream)
+        s.render_device(t, dev[t].data_ptr(), dgt[t].data_ptr(), cuda_stream=stream.cuda_stream)
     dmask = torch.empty((H, W), dtype=torch.uint8, device="cuda")
     torch.cuda.synchronize()
     b = BackgroundSubtractorSuBSENSE(seed=1)
     b.initialize(dev[0])
     ms = []
+    quality = BinClassif()
     for t in range(1, n):
         t0 = time.perf_counter()
         st = lib.lvbgs_apply(b.handle, C.c_void_p(dev[t].data_ptr()), 0, C.c_void_p(dmask.data_ptr()), 0.0,
@@ -239,13 +242,20 @@ def single_stream_run(config, n_frames, stream, cpu=True, cpu_frames=4):
         ms.append((time.perf_counter() - t0) * 1e3)
         if st != L.OK:
             raise RuntimeError("apply failed: %s" % lib.lvbgs_last_error(b.handle))
+        if t > 25:  # scored on the device after the timed call, once the model has learnt the scene
+            quality.accumulate(dmask, dgt[t], cuda_stream=stream.cuda_stream)
     b.close()
+    qm = quality.metrics()
     m = np.array(ms[9:])
     out = {"workload": "SuBSENSE config %d: one %dx%d %s stream, %d frames, default parameters" % (
                config, W, H, "BGR" if s.cfg.channels == 3 else "gray", n),
            "value": W * H / (m.mean() / 1e3) / 1e6, "unit": "Mpix/s", "frames_per_s": 1e3 / m.mean(),
            "ms_per_frame": float(m.mean()), "p50_frame_ms": float(np.percentile(m, 50)),
-           "p99_frame_ms": float(np.percentile(m, 99))}
+           "p99_frame_ms": float(np.percentile(m, 99)),
+           "quality": {"f_measure": qm["dFMeasure"], "recall": qm["dRecall"], "precision": qm["dPrecision"],
+                       "pbc": qm["dPBC"], "frames_scored": max(0, n - 26),
+                       "note": "lv::BinClassif on the device (lvbgs_classif_accumulate) against the synthetic "
+                               "ground truth (union of the shapes), frames 26 and later"}}
     if cpu:
         from oracle import pyoracle
         fr = np.stack([s.render(t) for t in range(cpu_frames + 1)])

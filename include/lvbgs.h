@@ -182,6 +182,19 @@ lvbgs_status lvbgs_lbsp_compute2_noalloc(const uint8_t* image, int width, int he
                                          long abs_threshold, float rel_threshold, size_t offset, uint16_t* desc,
                                          int device_id, void* cuda_stream);
 
+/* Change-detection evaluation on the device (modules/datasets: lv::BinClassif::accumulate,
+ * src/metrics.cpp:21-61). Adds to counts[6] = {TP, TN, FP, FN, shadow errors, don't care} the
+ * classification of a foreground mask (255 = positive) against CDnet-coded ground truth (255
+ * positive, 0 negative, 85 out of scope and 170 unknown = don't care, 50 shadow) and an optional ROI
+ * (0 = don't care). width*height bytes each, host or device memory; gt NULL counts every pixel as
+ * don't care. Runs on cuda_stream (NULL: the default stream) and returns after it. */
+lvbgs_status lvbgs_classif_accumulate(const uint8_t* fgmask, const uint8_t* gt, const uint8_t* roi, int width,
+                                      int height, uint64_t counts[6], int device_id, void* cuda_stream);
+/* lv::BinClassifMetrics (include/litiv/datasets/metrics.hpp:203-256) of counts[6]: out[8] = recall,
+ * specificity, false positive rate, false negative rate, percentage of bad classifications,
+ * precision, F-measure, Matthews correlation coefficient (0 where a denominator is 0). */
+lvbgs_status lvbgs_classif_metrics(const uint64_t counts[6], double out[8]);
+
 /* last error message of a handle (or of the library when h is NULL) */
 const char* lvbgs_last_error(lvbgs_handle h);
 
