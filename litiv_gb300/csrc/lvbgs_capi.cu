@@ -48,6 +48,7 @@ extern "C" __global__ void pw_k_nbr(PwParams P);
 extern "C" __global__ void pw_k_replace(PwParams P);
 extern "C" __global__ void pw_k_nbr_loops(PwParams P);
 extern "C" __global__ void pw_k_dirty(PwParams P);
+extern "C" __global__ void pw_k_round_end(PwParams P);
 extern "C" __global__ void pw_k_commit(PwParams P);
 extern "C" __global__ void pw_k_weights(PwParams P);
 extern "C" __global__ void pw_k_gw_recalc(PwParams P);
@@ -725,6 +726,7 @@ PwParams pw_params(lvbgs_ctx* h, double lr) {
     P.round = 0;
     P.lr = lr;
     P.flags = h->d_flags;
+    P.conv = nullptr;
     return P;
 }
 
@@ -864,54 +866,71 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
     LV_CUDA(h, cudaMemsetAsync(h->d_work, 0, sizeof(TickWork), st), "scratch reset");
     const int cblocks = (int)((h->npx + kPwCompactBlk - 1) / kPwCompactBlk);
     // ordered compaction: mode 0 lists the critical global items, mode 1 the word weight contributions
-    auto compact = [&](int mode) {
-        pw_k_compact_count<<<cblocks, 256, 0, st>>>(P, mode);
+    auto compact = [&](const PwParams& Pc, int mode) {
+        pw_k_compact_count<<<cblocks, 256, 0, st>>>(Pc, mode);
         const int ncat = mode == 1 ? h->pd.G : 1;
-        pw_k_compact_offsets<<<1, 32 * std::min(ncat, 32), 0, st>>>(P, ncat);
-        pw_k_compact_scatter<<<cblocks, 256, 0, st>>>(P, mode);
+        pw_k_compact_offsets<<<1, 32 * std::min(ncat, 32), 0, st>>>(Pc, ncat);
+        pw_k_compact_scatter<<<cblocks, 256, 0, st>>>(Pc, mode);
     };
     const bool c3 = h->C == 3;
-    int round = 0;
+    // The fixed point runs on the device: the rounds are enqueued ahead (as many as the previous frame
+    // needed, then one at a time), each ends with pw_k_round_end, and once a round finds no dirty pixel
+    // every later kernel of the rounds returns at once (PW_ROUND_GUARD), so the host waits once per
+    // batch of rounds instead of once per round.
     const int maxRounds = h->dbg_fault == LVBGS_FAULT_PAWCS_ROUNDS ? 1 : 64;
     h->dbg_fault = 0;
-    for (;; ++round) {
-        if (round >= maxRounds)
-            return fail(h, LVBGS_DEVICE_ERROR, "PAWCS raster-order fixed point did not converge in the round limit");
-        P.round = round;
-        if (c3) {
-            // three channels: the local pass applies the earlier updaters' loops itself
-            pw3_k_local<<<tiles, blk, 0, st>>>(P);
-            pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
-            compact(0);
-            pw3_k_gscan_seg<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
-            pw3_k_gscan_walk<<<1, 32, 0, st>>>(P);
-            pw3_k_gscan_fix<<<(int)((h->npx + 255) / 256), 256, 0, st>>>(P);
-            pw3_k_gscan_fix_walked<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
-            pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
-            pw_k_nbr<<<tiles, blk, 0, st>>>(P);
-            LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 4, st), "flag reset");
-            pw3_k_dirty<<<tiles, blk, 0, st>>>(P);
-        } else {
-            pw_k_local<<<tiles, blk, 0, st>>>(P);
-            pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
-            compact(0);
-            pw3_k_gscan_seg<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
-            pw3_k_gscan_walk<<<1, 32, 0, st>>>(P);
-            pw3_k_gscan_fix<<<(int)((h->npx + 255) / 256), 256, 0, st>>>(P);
-            pw3_k_gscan_fix_walked<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
-            pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
-            pw_k_nbr<<<tiles, blk, 0, st>>>(P);
-            compact(2);
-            pw_k_nbr_loops<<<std::max(1, std::min(cblocks * 4, 1216)), 256, 0, st>>>(P);
-            pw_k_replace<<<tiles, blk, 0, st>>>(P);
-            LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 4, st), "flag reset");
-            pw_k_dirty<<<tiles, blk, 0, st>>>(P);
+    LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 5 * sizeof(unsigned int), st), "flag reset");
+    PwParams PR = P;
+    PR.conv = h->d_flags + 3;
+    int enq = 0, chunk = std::max(1, std::min(h->pw_rounds_last, maxRounds)), rounds = 0;
+    for (;;) {
+        for (int r = 0; r < chunk && enq < maxRounds; ++r, ++enq) {
+            PR.round = enq;
+            const PwParams& P = PR;
+            if (c3) {
+                // three channels: the local pass applies the earlier updaters' loops itself
+                pw3_k_local<<<tiles, blk, 0, st>>>(P);
+                pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
+                compact(P, 0);
+                pw3_k_gscan_seg<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
+                pw3_k_gscan_walk<<<1, 32, 0, st>>>(P);
+                pw3_k_gscan_fix<<<(int)((h->npx + 255) / 256), 256, 0, st>>>(P);
+                pw3_k_gscan_fix_walked<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
+                pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
+                pw_k_nbr<<<tiles, blk, 0, st>>>(P);
+                LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 4, st), "flag reset");
+                pw3_k_dirty<<<tiles, blk, 0, st>>>(P);
+            } else {
+                pw_k_local<<<tiles, blk, 0, st>>>(P);
+                pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
+                compact(P, 0);
+                pw3_k_gscan_seg<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
+                pw3_k_gscan_walk<<<1, 32, 0, st>>>(P);
+                pw3_k_gscan_fix<<<(int)((h->npx + 255) / 256), 256, 0, st>>>(P);
+                pw3_k_gscan_fix_walked<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
+                pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
+                pw_k_nbr<<<tiles, blk, 0, st>>>(P);
+                compact(P, 2);
+                pw_k_nbr_loops<<<std::max(1, std::min(cblocks * 4, 1216)), 256, 0, st>>>(P);
+                pw_k_replace<<<tiles, blk, 0, st>>>(P);
+                LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 4, st), "flag reset");
+                pw_k_dirty<<<tiles, blk, 0, st>>>(P);
+            }
+            pw_k_round_end<<<1, 1, 0, st>>>(P);
         }
         LV_CUDA(h, cudaGetLastError(), "PAWCS round launch");
-        LV_CUDA(h, cudaMemcpyAsync(h->h_flags, h->d_flags, 4, cudaMemcpyDeviceToHost, st), "flag read-back");
-        LV_CUDA(h, cudaStreamSynchronize(st), "PAWCS round");
-        if (h->h_flags[0] == 0) break;
+        LV_CUDA(h, cudaMemcpyAsync(h->h_flags + 3, h->d_flags + 3, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, st),
+                "flag read-back");
+        LV_CUDA(h, cudaStreamSynchronize(st), "PAWCS rounds");
+        if (h->h_flags[3]) {
+            rounds = (int)h->h_flags[4];
+            break;
+        }
+        if (enq >= maxRounds)
+            return fail(h, LVBGS_DEVICE_ERROR, "PAWCS raster-order fixed point did not converge in the round limit");
+        chunk = 1;
     }
+    const int round = rounds - 1;
     h->pw_rounds_last = round + 1;
     if (c3) {
         pw3_k_later<<<tiles, blk, 0, st>>>(P);
@@ -920,7 +939,7 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
         pw_k_commit<<<tiles, blk, 0, st>>>(P);
     }
     pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 1);
-    compact(1);
+    compact(P, 1);
     pw_k_weights<<<kPwMaxGlobal, 256, 0, st>>>(P);
     pw_k_gw_recalc<<<kPwMaxGlobal, 256, 0, st>>>(P);
     pw_k_gw_decay<<<dim3(64, kPwMaxGlobal), 256, 0, st>>>(P, h->d_rowsum);

@@ -94,7 +94,7 @@ extern "C" lvbgs_status lvbgs_classif_accumulate(const uint8_t* fgmask, const ui
     const uint8_t* dptr[3] = {nullptr, nullptr, nullptr};
     uint8_t* tmp = nullptr;
     unsigned long long* dcounts = nullptr;
-    size_t need = 6 * sizeof(unsigned long long);
+    size_t need = 256;  // the counters, then each staged input at a 256-byte boundary
     for (int i = 0; i < 3; ++i)
         if (src[i] && !on_device(src[i])) need += (n + 255) & ~(size_t)255;
     cudaError_t e = cudaMallocAsync((void**)&tmp, need, st);

@@ -172,6 +172,7 @@ __device__ void pw3_item_pixel(const PawcsDev& S, int p, const PwRec& R, uint32_
 // buffer; illumination updates as marks) and the record.
 // ------------------------------------------------------------------------------------------
 extern "C" __global__ void __launch_bounds__(256, 3) pw3_k_local(PwParams P) {
+    PW_ROUND_GUARD(P);
     PW3_PIXEL_PROLOGUE
     if (x >= D.W || y >= D.H) return;
     const int q = y * D.W + x;
@@ -495,6 +496,7 @@ __device__ void pw3_gscan_range(const PawcsDev& S, int G, int wr, uint32_t a, ui
 // phase 1: one warp per segment: its candidates listed, then its speculative scan from a guessed
 // state kPw3Warm items before it
 extern "C" __global__ void __launch_bounds__(128) pw3_k_gscan_seg(PwParams P) {
+    PW_ROUND_GUARD(P);
     const PawcsDev& S = P.streams[0];
     const uint32_t n = S.catInfo[0];
     const int s = blockIdx.x * 4 + (int)(threadIdx.x >> 5), lane = threadIdx.x & 31;
@@ -551,6 +553,7 @@ extern "C" __global__ void __launch_bounds__(128) pw3_k_gscan_seg(PwParams P) {
 // changes the state), up to the first one that replaces the word in both scans, their true outcome
 // marked in gtrue
 extern "C" __global__ void pw3_k_gscan_walk(PwParams P) {
+    PW_ROUND_GUARD(P);
     const PawcsDev& S = P.streams[0];
     PawcsCtl* pc = S.pc;
     const int lane = threadIdx.x & 31;
@@ -655,6 +658,7 @@ extern "C" __global__ void pw3_k_gscan_walk(PwParams P) {
 // phase 3a: one thread per item: the kept segments and the items after a synchronization, from the
 // speculative scan (epochs shifted); the walked items are left to phase 3b
 extern "C" __global__ void __launch_bounds__(256) pw3_k_gscan_fix(PwParams P) {
+    PW_ROUND_GUARD(P);
     const PawcsDev& S = P.streams[0];
     const uint32_t n = S.catInfo[0];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -670,6 +674,7 @@ extern "C" __global__ void __launch_bounds__(256) pw3_k_gscan_fix(PwParams P) {
 // phase 3b: one warp per walked segment, its items up to the synchronization (or all): from the true
 // replacers, with warp prefixes of the last replacer and of the replacement count
 extern "C" __global__ void __launch_bounds__(128) pw3_k_gscan_fix_walked(PwParams P) {
+    PW_ROUND_GUARD(P);
     const PawcsDev& S = P.streams[0];
     const uint32_t n = S.catInfo[0];
     const int s = blockIdx.x * 4 + (int)(threadIdx.x >> 5), lane = threadIdx.x & 31;
@@ -725,6 +730,7 @@ extern "C" __global__ void __launch_bounds__(128) pw3_k_gscan_fix_walked(PwParam
 // pixels rerun next round: an earlier updater in the 5x5 window whose loop inputs changed this
 // round and that targets the pixel now or did before
 extern "C" __global__ void __launch_bounds__(256) pw3_k_dirty(PwParams P) {
+    PW_ROUND_GUARD(P);
     PW3_PIXEL_PROLOGUE
     bool dirty = false;
     if (x < D.W && y < D.H) {

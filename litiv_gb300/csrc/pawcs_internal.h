@@ -144,7 +144,12 @@ struct PwParams {
     int totalCells;
     int round;            // fixed-point round of the local pass (0: every pixel)
     double lr;            // learningRateOverride of the tick (<= 0: internal, inf: never)
-    unsigned int* flags;  // [0] dirty pixels of the round
+    unsigned int* flags;  // [0] dirty pixels of the round, [3] fixed point reached, [4] its round count
+    // set for the launches of a fixed-point round: the rounds of a frame are enqueued ahead, and
+    // every kernel of a round returns at once when an earlier round reached the fixed point
+    const unsigned int* conv;
 };
+#define PW_ROUND_GUARD(P) \
+    if ((P).conv && *(const volatile unsigned int*)(P).conv) return
 
 }  // namespace lvbgs

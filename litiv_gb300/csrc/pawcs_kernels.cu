@@ -53,6 +53,7 @@ __device__ __forceinline__ void pw_word(const PwWordSrc& s, int j, uint32_t& c, 
 __device__ void pw_item_pixel(const PawcsDev& S, int p, const PwRec& R, uint32_t col);
 
 extern "C" __global__ void __launch_bounds__(256) pw_k_local(PwParams P) {
+    PW_ROUND_GUARD(P);
     const int t0 = blockIdx.x;
     if (t0 >= P.totalTiles) return;
     const PawcsDev& S = P.streams[pw_stream_by_tile(P, t0)];
@@ -238,6 +239,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_local(PwParams P) {
 // left neighbour's (two states), so one warp per row scans the compositions 32 pixels at a time.
 // ------------------------------------------------------------------------------------------
 extern "C" __global__ void __launch_bounds__(256) pw_k_illum(PwParams P) {
+    PW_ROUND_GUARD(P);
     const int gr = blockIdx.x * 8 + (int)threadIdx.x / 32, lane = threadIdx.x & 31;
     if (gr >= P.totalRows) return;
     const PawcsDev& S = P.streams[pw_stream_by_row(P, gr)];
@@ -329,6 +331,7 @@ __device__ __forceinline__ int pw_category(const PawcsDev& S, int p, int mode, i
 }
 
 extern "C" __global__ void __launch_bounds__(256) pw_k_compact_count(PwParams P, int mode) {
+    PW_ROUND_GUARD(P);
     const PawcsDev& S = P.streams[0];
     const int nb = (S.sd.npx + kPwCompactBlk - 1) / kPwCompactBlk;
     if ((int)blockIdx.x >= nb) return;
@@ -351,6 +354,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_compact_count(PwParams P,
 // per category (one warp each): exclusive offsets over the blocks (in place), totals and the category
 // bases of the word-major list; the compaction uses categories [0, ncat), the others are left empty
 extern "C" __global__ void __launch_bounds__(1024) pw_k_compact_offsets(PwParams P, int ncat) {
+    PW_ROUND_GUARD(P);
     const PawcsDev& S = P.streams[0];
     const int nb = (S.sd.npx + kPwCompactBlk - 1) / kPwCompactBlk;
     __shared__ uint32_t tot[kPwCats];
@@ -386,6 +390,7 @@ extern "C" __global__ void __launch_bounds__(1024) pw_k_compact_offsets(PwParams
 }
 
 extern "C" __global__ void __launch_bounds__(256) pw_k_compact_scatter(PwParams P, int mode) {
+    PW_ROUND_GUARD(P);
     const PawcsDev& S = P.streams[0];
     const StreamDev& D = S.sd;
     const int nb = (D.npx + kPwCompactBlk - 1) / kPwCompactBlk;
@@ -453,6 +458,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_compact_scatter(PwParams 
 // per 2x2 cell of the spatial maps: the cell's (at most four) items in raster order (:786-791,
 // :805-812); final = 1 also writes the frame's map values and word contributions
 extern "C" __global__ void pw_k_cells(PwParams P, int final) {
+    PW_ROUND_GUARD(P);
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= P.totalCells) return;
     int si = 0;
@@ -532,6 +538,7 @@ extern "C" __global__ void pw_k_cells(PwParams P, int final) {
 
 // neighbour-update gate and target (:839-848): the draws before it depend on the global outcome
 extern "C" __global__ void __launch_bounds__(256) pw_k_nbr(PwParams P) {
+    PW_ROUND_GUARD(P);
     const int t0 = blockIdx.x;
     if (t0 >= P.totalTiles) return;
     const PawcsDev& S = P.streams[pw_stream_by_tile(P, t0)];
@@ -653,6 +660,7 @@ __device__ float pw_nbr_loop(const PawcsDev& S, uint32_t t, int cur, int nxt, in
 // neighbour updates, pass 1: every updater's loop (one thread each, over the compacted list), as if no
 // earlier updater of its target had replaced the target's last word
 extern "C" __global__ void __launch_bounds__(256) pw_k_nbr_loops(PwParams P) {
+    PW_ROUND_GUARD(P);
     const PawcsDev& S = P.streams[0];
     const StreamDev& D = S.sd;
     const uint32_t n = S.catInfo[0];
@@ -676,6 +684,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_nbr_loops(PwParams P) {
 // each group that replaces the last word is the replacement source the next ones see; a later updater
 // whose loop reached that word is redone with it (the earlier words are the same either way)
 extern "C" __global__ void __launch_bounds__(256) pw_k_replace(PwParams P) {
+    PW_ROUND_GUARD(P);
     const int t0 = blockIdx.x;
     if (t0 >= P.totalTiles) return;
     const PawcsDev& S = P.streams[pw_stream_by_tile(P, t0)];
@@ -724,6 +733,7 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_replace(PwParams P) {
 
 // pixels whose replacement source changed since their local pass are redone next round
 extern "C" __global__ void __launch_bounds__(256) pw_k_dirty(PwParams P) {
+    PW_ROUND_GUARD(P);
     const int t0 = blockIdx.x;
     if (t0 >= P.totalTiles) return;
     const PawcsDev& S = P.streams[pw_stream_by_tile(P, t0)];
@@ -738,6 +748,17 @@ extern "C" __global__ void __launch_bounds__(256) pw_k_dirty(PwParams P) {
     }
     const unsigned b = __ballot_sync(0xffffffffu, dirty);
     if ((threadIdx.x & 31) == 0 && b) atomicAdd(&P.flags[0], (unsigned)__popc(b));
+}
+
+// end of a fixed-point round (one thread): no dirty pixel means the fixed point is reached; the
+// round count is recorded and the flag makes the rounds enqueued after this one return at once
+extern "C" __global__ void pw_k_round_end(PwParams P) {
+    PW_ROUND_GUARD(P);
+    if (P.flags[0] == 0u) {
+        P.flags[4] = (unsigned)P.round + 1u;
+        __threadfence();
+        P.flags[3] = 1u;
+    }
 }
 
 // ------------------------------------------------------------------------------------------
