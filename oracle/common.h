@@ -50,7 +50,15 @@ OC_UNUSED static uint16_t sat_u16f(float v) {
     return (uint16_t)(r < 0 ? 0 : r > 65535 ? 65535 : r);
 }
 
-OC_UNUSED static unsigned popc16(unsigned v) { return (unsigned)__builtin_popcount(v & 0xffffu); }
+/* population count of the low 16 bits (bit-parallel sums: no -march flags here, so the builtin would
+ * be a library call) */
+OC_UNUSED static unsigned popc16(unsigned v) {
+    v &= 0xffffu;
+    v = v - ((v >> 1) & 0x5555u);
+    v = (v & 0x3333u) + ((v >> 2) & 0x3333u);
+    v = (v + (v >> 4)) & 0x0f0fu;
+    return (v + (v >> 8)) & 0x1fu;
+}
 
 OC_UNUSED static size_t absdiff(int a, int b) { return (size_t)(a > b ? a - b : b - a); }
 
@@ -99,10 +107,28 @@ OC_UNUSED static void lbsp_lookup(const uint8_t* img, int W, int C, int x, int y
     for (int n = 0; n < 16; ++n) vals[n] = base[(long)row * k_lbsp_dy[n] + (long)C * k_lbsp_dx[n]];
 }
 
-/* LBSP::computeDescriptor_threshold (LBSP.hpp:193-202): bit n = |val_n - ref| > thr */
+/* LBSP::computeDescriptor_threshold (LBSP.hpp:193-202): bit n = |val_n - ref| > thr, written as
+ * the equivalent range test val_n < lo || val_n > hi with lo = max(ref - thr, 0) and
+ * hi = min(ref + thr, 255), on eight taps at a time in 16-bit lanes of a 64-bit word: with a tap in
+ * bits 0-7 of a lane, bit 8 of tap + (256 - lo) is tap >= lo and bit 8 of tap + (255 - hi) is
+ * tap > hi (no carry leaves a lane) */
 OC_UNUSED static uint16_t lbsp_threshold(const uint8_t vals[16], uint8_t ref, uint8_t thr) {
+    const uint64_t lo = ref > thr ? (uint64_t)(ref - thr) : 0u;
+    const uint64_t hi = (unsigned)ref + thr < 255u ? (uint64_t)ref + thr : 255u;
+    const uint64_t lanes = 0x0001000100010001ull, k1 = (256u - lo) * lanes, k2 = (255u - hi) * lanes;
     unsigned d = 0;
-    for (int n = 0; n < 16; ++n) d |= (unsigned)(absdiff(vals[n], ref) > thr) << n;
+    for (int h = 0; h < 2; ++h) {
+        const uint8_t* v = vals + 8 * h;
+        /* taps 0, 2, 4, 6 of this half in the lanes of e; taps 1, 3, 5, 7 in those of o */
+        const uint64_t e = (uint64_t)v[0] | ((uint64_t)v[2] << 16) | ((uint64_t)v[4] << 32) | ((uint64_t)v[6] << 48);
+        const uint64_t o = (uint64_t)v[1] | ((uint64_t)v[3] << 16) | ((uint64_t)v[5] << 32) | ((uint64_t)v[7] << 48);
+        const uint64_t fe = (~(e + k1) | (e + k2)) & 0x0100010001000100ull;
+        const uint64_t fo = (~(o + k1) | (o + k2)) & 0x0100010001000100ull;
+        uint64_t m = (fe | (fo << 1)) >> 8; /* taps 2i, 2i+1 at bits 16i, 16i+1 */
+        m |= m >> 14;                       /* taps 0-3 at bits 0-3, taps 4-7 at bits 32-35 */
+        m |= m >> 28;                       /* taps 4-7 at bits 4-7 */
+        d |= (unsigned)(m & 0xffu) << (8 * h);
+    }
     return (uint16_t)d;
 }
 
