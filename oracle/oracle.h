@@ -1,15 +1,15 @@
 /* ORACLE (test infrastructure only; never linked into the product library).
  *
- * CPU restatement of the reference's SuBSENSE and PAWCS per-pixel background
+ * CPU restatement of the reference's SuBSENSE, PAWCS and LOBSTER per-pixel background
  * subtraction (plstcharles/litiv, modules/video/src/BackgroundSubtractorSuBSENSE.cpp,
- * BackgroundSubtractorPAWCS.cpp) and of the LBSP descriptor
+ * BackgroundSubtractorPAWCS.cpp, BackgroundSubtractorLOBSTER.cpp) and of the LBSP descriptor
  * (modules/features2d/include/litiv/features2d/LBSP.hpp).
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it,
  * always as the checker.
  *
  * Parity pins: the LBSP descriptor is pinned by the reference's golden vector
  * (modules/features2d/test/data/test_lbsp.bin, see tests/golden/). The SuBSENSE and PAWCS
- * restatements are pinned to the reference itself: oracle/refshim/build_ref.py compiles the
+ * (and LOBSTER) restatements are pinned to the reference itself: oracle/refshim/build_ref.py compiles the
  * reference's own modules/video/src sources (against a project-written OpenCV stand-in, with rand()
  * routed to the same generator) into oracle/_ref/libref.so, which exposes this same API (rsub_* /
  * rpawcs_*), and tests/test_oracle_reference.py compares every map bit for bit. The OpenCV image
@@ -154,6 +154,53 @@ void opawcs_set_automatic_model_reset(opawcs_t* o, int enabled);
 int opawcs_export(const opawcs_t* o, int which, void* out, size_t bytes);
 size_t opawcs_export_bytes(const opawcs_t* o, int which);
 void opawcs_get_scalars(const opawcs_t* o, opawcs_scalars* s);
+
+/* ---- LOBSTER (modules/video/src/BackgroundSubtractorLOBSTER.cpp, the non-parallel path) ---- */
+typedef struct olob olob_t;
+
+typedef struct {
+    size_t desc_dist_threshold;          /* BGSLOBSTER_DEFAULT_DESC_DIST_THRESHOLD = 4 */
+    size_t color_dist_threshold;         /* BGSLOBSTER_DEFAULT_COLOR_DIST_THRESHOLD = 30 */
+    size_t bg_samples;                   /* BGSLOBSTER_DEFAULT_NB_BG_SAMPLES = 35 */
+    size_t required_bg_samples;          /* BGSLOBSTER_DEFAULT_REQUIRED_NB_BG_SAMPLES = 2 */
+    float rel_lbsp_threshold;            /* BGSLBSP_DEFAULT_LBSP_REL_SIMILARITY_THRESHOLD = 0.333f */
+    size_t lbsp_threshold_offset;        /* = 0 */
+    int default_median_blur_kernel_size; /* BGSLBSP_DEFAULT_MEDIAN_BLUR_KERNEL_SIZE = 9 */
+    uint64_t seed;
+} olob_params;
+
+typedef struct {
+    uint64_t frames; /* apply() calls since initialize() (the generator's frame) */
+    uint64_t n_relevant_px, orig_roi_px;
+    uint64_t stat_samples_evaluated, stat_sample_writes;
+} olob_scalars;
+
+enum {
+    OLOB_MAP_LAST_FG = 0, OLOB_MAP_ROI,             /* uint8 [H*W] */
+    OLOB_MAP_LAST_COLOR, OLOB_MAP_LAST_DESC,        /* [H*W*C] u8 / u16 */
+    OLOB_MAP_SAMPLE_COLOR, OLOB_MAP_SAMPLE_DESC,    /* [N][H*W*C] u8 / u16 */
+    OLOB_MAP_LUT,                                   /* uint8 [256] */
+    OLOB_MAP_COUNT
+};
+
+void olob_default_params(olob_params* p);
+olob_t* olob_create(const olob_params* p);
+void olob_destroy(olob_t* o);
+/* BackgroundSubtractorLOBSTER::initialize (BackgroundSubtractorLOBSTER.cpp:442-457) */
+int olob_initialize(olob_t* o, const uint8_t* img, int width, int height, int channels, const uint8_t* roi);
+/* BackgroundSubtractorLOBSTER::apply (:459-581); learning_rate > 0 (the reference's default is 16) */
+int olob_apply(olob_t* o, const uint8_t* img, uint8_t* fgmask, double learning_rate);
+/* BackgroundSubtractorLOBSTER::refreshModel (:410-440) */
+int olob_refresh_model(olob_t* o, float frac, int force_fg);
+int olob_get_background(const olob_t* o, uint8_t* out);              /* :583-600 */
+int olob_get_background_descriptors(const olob_t* o, uint16_t* out); /* :602-620 */
+const void* olob_map(const olob_t* o, int which, size_t* nbytes);
+void olob_get_scalars(const olob_t* o, olob_scalars* s);
+
+/* CPU baseline for LOBSTER: as orun_streams (apply phase timed, learning rate 16) */
+double orun_lobster_streams(int n_streams, const uint8_t* const* frames, const int* n_frames,
+                            const int* widths, const int* heights, const int* channels,
+                            const uint64_t* seeds, int n_threads);
 
 /* CPU baseline: runs n independent SuBSENSE instances (one per stream) over their
  * frame sequences on n_threads workers (streams k, k+T, ... on worker k, like the

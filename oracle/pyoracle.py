@@ -1,5 +1,5 @@
 """ORACLE (test infrastructure only): ctypes wrapper of oracle/_build/liboracle.so (the C
-restatement of the reference, "port") and of oracle/_ref/libref.so (the reference's own SuBSENSE /
+restatement of the reference's SuBSENSE, PAWCS and LOBSTER, "port") and of oracle/_ref/libref.so (the reference's own SuBSENSE /
 PAWCS sources compiled against the project-written OpenCV stand-in, "reference"; built only where
 the reference sources are present, see oracle/refshim/build_ref.py). Both expose the same C API,
 so OracleSuBSENSE / OraclePAWCS drive either one (``impl=``).
@@ -66,6 +66,21 @@ _ref_lib = None
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libref.so")
 
 
+class LParams(C.Structure):
+    _fields_ = [("desc_dist_threshold", C.c_size_t), ("color_dist_threshold", C.c_size_t),
+                ("bg_samples", C.c_size_t), ("required_bg_samples", C.c_size_t),
+                ("rel_lbsp_threshold", C.c_float), ("lbsp_threshold_offset", C.c_size_t),
+                ("default_median_blur_kernel_size", C.c_int), ("seed", C.c_uint64)]
+
+
+class LScalars(C.Structure):
+    _fields_ = [("frames", C.c_uint64), ("n_relevant_px", C.c_uint64), ("orig_roi_px", C.c_uint64),
+                ("stat_samples_evaluated", C.c_uint64), ("stat_sample_writes", C.c_uint64)]
+
+
+LOBSTER_MAP_NAMES = ["LAST_FG", "ROI", "LAST_COLOR", "LAST_DESC", "SAMPLE_COLOR", "SAMPLE_DESC", "LUT"]
+
+
 def build():
     subprocess.run(["make", "-s", "-C", HERE], check=True)
 
@@ -88,7 +103,7 @@ def ref_lib():
         if path is None and not os.path.exists(REF_LIB_PATH):
             return None
         L = C.CDLL(REF_LIB_PATH)
-        for pre, Par, Sc in (("rsub_", OParams, OScalars), ("rpawcs_", PParams, PScalars)):
+        for pre, Par, Sc in (("rsub_", OParams, OScalars), ("rpawcs_", PParams, PScalars), ("rlob_", LParams, LScalars)):
             getattr(L, pre + "create").restype = C.c_void_p
             getattr(L, pre + "create").argtypes = [C.POINTER(Par)]
             getattr(L, pre + "destroy").argtypes = [C.c_void_p]
@@ -97,13 +112,17 @@ def ref_lib():
             getattr(L, pre + "get_background").argtypes = [C.c_void_p, C.c_void_p]
             getattr(L, pre + "set_roi").argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
             getattr(L, pre + "get_background_descriptors").argtypes = [C.c_void_p, C.c_void_p]
-            getattr(L, pre + "set_automatic_model_reset").argtypes = [C.c_void_p, C.c_int]
             getattr(L, pre + "get_scalars").argtypes = [C.c_void_p, C.POINTER(Sc)]
+            if pre != "rlob_":
+                getattr(L, pre + "set_automatic_model_reset").argtypes = [C.c_void_p, C.c_int]
         L.r_last_error.restype = C.c_char_p
         L.rsub_refresh_model.argtypes = [C.c_void_p, C.c_float, C.c_int]
         L.rsub_map.restype = C.c_void_p
         L.rsub_map.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]
         L.rpawcs_refresh_model.argtypes = [C.c_void_p, C.c_size_t, C.c_float, C.c_int]
+        L.rlob_refresh_model.argtypes = [C.c_void_p, C.c_float, C.c_int]
+        L.rlob_map.restype = C.c_void_p
+        L.rlob_map.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]
         L.rpawcs_export.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]
         L.rpawcs_export_bytes.restype = C.c_size_t
         L.rpawcs_export_bytes.argtypes = [C.c_void_p, C.c_int]
@@ -176,6 +195,21 @@ def lib():
         L.opawcs_export_bytes.restype = C.c_size_t
         L.opawcs_export_bytes.argtypes = [C.c_void_p, C.c_int]
         L.opawcs_get_scalars.argtypes = [C.c_void_p, C.POINTER(PScalars)]
+        L.olob_default_params.argtypes = [C.POINTER(LParams)]
+        L.olob_create.restype = C.c_void_p
+        L.olob_create.argtypes = [C.POINTER(LParams)]
+        L.olob_destroy.argtypes = [C.c_void_p]
+        L.olob_initialize.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        L.olob_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
+        L.olob_refresh_model.argtypes = [C.c_void_p, C.c_float, C.c_int]
+        L.olob_get_background.argtypes = [C.c_void_p, C.c_void_p]
+        L.olob_get_background_descriptors.argtypes = [C.c_void_p, C.c_void_p]
+        L.olob_map.restype = C.c_void_p
+        L.olob_map.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]
+        L.olob_get_scalars.argtypes = [C.c_void_p, C.POINTER(LScalars)]
+        L.orun_lobster_streams.restype = C.c_double
+        L.orun_lobster_streams.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                           C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_uint64), C.c_int]
         _lib = L
     return _lib
 
@@ -357,6 +391,100 @@ class OraclePAWCS:
         return {f: getattr(s, f) for f, _ in PScalars._fields_}
 
 
+class OracleLOBSTER:
+    """Sequential CPU LOBSTER (the checker): the C restatement (impl="port") or the reference's own
+    BackgroundSubtractorLOBSTER (impl="reference"). apply()'s learning rate defaults to the reference's
+    getDefaultLearningRate() (16)."""
+
+    def __init__(self, seed=0, impl="port", **params):
+        p = LParams()
+        lib().olob_default_params(C.byref(p))
+        p.seed = seed
+        for k, v in params.items():
+            setattr(p, k, v)
+        self.params = p
+        self.impl = impl
+        self._a = _Api(impl, "olob_", "rlob_")
+        self._o = self._a.create(C.byref(p))
+        if not self._o:
+            raise ValueError("invalid oracle parameters")
+        self.shape = None
+
+    def close(self):
+        if self._o:
+            self._a.destroy(self._o)
+            self._o = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _err(self):
+        return ": " + ref_lib().r_last_error().decode(errors="replace") if self.impl == "reference" else ""
+
+    def initialize(self, img, roi=None):
+        img = np.ascontiguousarray(img, np.uint8)
+        H, W = img.shape[:2]
+        Cc = img.shape[2] if img.ndim == 3 else 1
+        r = None if roi is None else np.ascontiguousarray(roi, np.uint8)
+        st = self._a.initialize(self._o, img.ctypes.data_as(C.c_void_p), W, H, Cc,
+                                r.ctypes.data_as(C.c_void_p) if r is not None else None)
+        if st != 0:
+            raise ValueError("oracle initialize failed (%d)%s" % (st, self._err()))
+        self.shape = (H, W, Cc)
+
+    def apply(self, img, lr=16.0):
+        img = np.ascontiguousarray(img, np.uint8)
+        H, W, _ = self.shape
+        mask = np.empty((H, W), np.uint8)
+        st = self._a.apply(self._o, img.ctypes.data_as(C.c_void_p), mask.ctypes.data_as(C.c_void_p), float(lr))
+        if st != 0:
+            raise ValueError("oracle apply failed (%d)%s" % (st, self._err()))
+        return mask
+
+    def refresh_model(self, frac, force=False):
+        return self._a.refresh_model(self._o, float(frac), 1 if force else 0)
+
+    def background(self):
+        H, W, Cc = self.shape
+        out = np.empty((H, W, Cc) if Cc > 1 else (H, W), np.uint8)
+        self._a.get_background(self._o, out.ctypes.data_as(C.c_void_p))
+        return out
+
+    def background_descriptors(self):
+        H, W, Cc = self.shape
+        out = np.empty((H, W, Cc) if Cc > 1 else (H, W), np.uint16)
+        self._a.get_background_descriptors(self._o, out.ctypes.data_as(C.c_void_p))
+        return out
+
+    def state_map(self, name):
+        """LAST_FG / ROI (uint8 [H, W]), LAST_COLOR (uint8 [H, W(, C)]), LAST_DESC (uint16 [H, W(, C)]),
+        SAMPLE_COLOR (uint8 [N, H, W(, C)]), SAMPLE_DESC (uint16 [N, H, W(, C)]), LUT (uint8 [256])"""
+        n = C.c_size_t()
+        ptr = self._a.map(self._o, LOBSTER_MAP_NAMES.index(name), C.byref(n))
+        raw = np.ctypeslib.as_array((C.c_uint8 * n.value).from_address(ptr)).copy()
+        H, W, Cc = self.shape
+        tail = (H, W, Cc) if Cc > 1 else (H, W)
+        if name in ("LAST_FG", "ROI"):
+            return raw.reshape(H, W)
+        if name == "LUT":
+            return raw
+        if name == "LAST_COLOR":
+            return raw.reshape(tail)
+        if name == "LAST_DESC":
+            return raw.view(np.uint16).reshape(tail)
+        if name == "SAMPLE_COLOR":
+            return raw.reshape((-1,) + tail)
+        return raw.view(np.uint16).reshape((-1,) + tail)
+
+    def scalars(self):
+        s = LScalars()
+        self._a.get_scalars(self._o, C.byref(s))
+        return {f: getattr(s, f) for f, _ in LScalars._fields_}
+
+
 def lbsp_compute2(img, abs_threshold=None, rel_threshold=0.333, offset=0, out=None):
     img = np.ascontiguousarray(img, np.uint8)
     H, W = img.shape[:2]
@@ -401,3 +529,17 @@ def run_pawcs_streams(frames_list, seeds, n_threads):
     cs = (C.c_int * n)(*[(a.shape[3] if a.ndim == 4 else 1) for a in arrs])
     sd = (C.c_uint64 * n)(*seeds)
     return lib().orun_pawcs_streams(n, ptrs, nf, ws, hs, cs, sd, int(n_threads))
+
+
+def run_lobster_streams(frames_list, seeds, n_threads):
+    """LOBSTER CPU baseline (learning rate 16): frames_list[i] is uint8 [F, H, W(, C)]; returns wall
+    seconds of the apply phase."""
+    n = len(frames_list)
+    arrs = [np.ascontiguousarray(f) for f in frames_list]
+    ptrs = (C.c_void_p * n)(*[a.ctypes.data for a in arrs])
+    nf = (C.c_int * n)(*[a.shape[0] for a in arrs])
+    ws = (C.c_int * n)(*[a.shape[2] for a in arrs])
+    hs = (C.c_int * n)(*[a.shape[1] for a in arrs])
+    cs = (C.c_int * n)(*[(a.shape[3] if a.ndim == 4 else 1) for a in arrs])
+    sd = (C.c_uint64 * n)(*seeds)
+    return lib().orun_lobster_streams(n, ptrs, nf, ws, hs, cs, sd, int(n_threads))

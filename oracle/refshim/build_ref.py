@@ -1,4 +1,4 @@
-"""ORACLE build recipe (test infrastructure only): compiles the REFERENCE's own SuBSENSE / PAWCS
+"""ORACLE build recipe (test infrastructure only): compiles the REFERENCE's own SuBSENSE / PAWCS / LOBSTER
 sources into oracle/_ref/libref.so, for the CPU tests that pin the C restatement (oracle/*.c) to the
 reference itself.
 
@@ -7,9 +7,9 @@ used here. Instead:
 
 * the reference sources are compiled unmodified, from where they lie:
   modules/video/src/BackgroundSubtractionUtils.cpp, BackgroundSubtractorLBSP.cpp,
-  BackgroundSubtractorSuBSENSE.cpp, BackgroundSubtractorPAWCS.cpp, with the reference's own headers
-  (BackgroundSubtractionUtils.hpp, BackgroundSubtractorLBSP.hpp, BackgroundSubtractorSuBSENSE.hpp,
-  BackgroundSubtractorPAWCS.hpp, features2d LBSP.hpp, utils algo.hpp, math.hpp, cxx.hpp, simd.hpp,
+  BackgroundSubtractorSuBSENSE.cpp, BackgroundSubtractorPAWCS.cpp, BackgroundSubtractorLOBSTER.cpp, with
+  the reference's own headers (BackgroundSubtractionUtils.hpp, BackgroundSubtractorLBSP.hpp,
+  BackgroundSubtractorSuBSENSE.hpp, BackgroundSubtractorPAWCS.hpp, BackgroundSubtractorLOBSTER.hpp, features2d LBSP.hpp, utils algo.hpp, math.hpp, cxx.hpp, simd.hpp,
   platform.hpp, console.hpp);
 * ``litiv/utils/defines.hpp`` is the reference's ``defines.hpp.in`` with its @VARIABLES@ filled in
   (what CMake's configure_file does): no GLSL/CUDA/OpenCL, no SIMD paths (scalar code on every host),
@@ -23,7 +23,7 @@ used here. Instead:
   definitions as the C restatement (oracle/common.h);
 * ``rand()`` is routed to the counter-based generator (oracle/refshim/lvshim_rand.h, force-included);
 * oracle/refshim/ref_bridge.cpp exposes the reference classes through the same C API as the
-  restatement (rsub_* / rpawcs_* beside osub_* / opawcs_*).
+  restatement (rsub_* / rpawcs_* / rlob_* beside osub_* / opawcs_* / olob_*).
 
 Run: python oracle/refshim/build_ref.py [reference root]. Outputs go to oracle/_ref/ only. The
 reference root defaults to /root/reference; without it nothing is built (the GPU parity tests do not
@@ -43,7 +43,8 @@ DEFAULT_REF = "/root/reference"
 SOURCES = ["modules/video/src/BackgroundSubtractionUtils.cpp",
            "modules/video/src/BackgroundSubtractorLBSP.cpp",
            "modules/video/src/BackgroundSubtractorSuBSENSE.cpp",
-           "modules/video/src/BackgroundSubtractorPAWCS.cpp"]
+           "modules/video/src/BackgroundSubtractorPAWCS.cpp",
+           "modules/video/src/BackgroundSubtractorLOBSTER.cpp"]
 INCLUDES = ["modules/video/include", "modules/features2d/include", "modules/utils/include"]
 SHIM_SOURCES = ["ref_bridge.cpp", "lv_support.cpp"]
 

@@ -1,8 +1,9 @@
-// ORACLE (test infrastructure only): C API over the REFERENCE's own BackgroundSubtractorSuBSENSE
-// and BackgroundSubtractorPAWCS classes (compiled from the reference's sources by
+// ORACLE (test infrastructure only): C API over the REFERENCE's own BackgroundSubtractorSuBSENSE,
+// BackgroundSubtractorPAWCS and BackgroundSubtractorLOBSTER classes (compiled from the reference's sources by
 // oracle/refshim/build_ref.py), with the same signatures and state layouts as the C restatement's
 // osub_* / opawcs_* (oracle/oracle.h), so that the tests can run both on the same frames and compare
 // every map bit for bit. Built into oracle/_ref/libref.so, which only the CPU tests load.
+#include "litiv/video/BackgroundSubtractorLOBSTER.hpp"
 #include "litiv/video/BackgroundSubtractorPAWCS.hpp"
 #include "litiv/video/BackgroundSubtractorSuBSENSE.hpp"
 #include "oracle.h"
@@ -140,6 +141,53 @@ struct RefSub : BackgroundSubtractorSuBSENSE {
         s->lr_lower_cap = m_fCurrLearningRateLowerCap;
         s->lr_upper_cap = m_fCurrLearningRateUpperCap;
         s->last_nonzero_desc_ratio = m_fLastNonZeroDescRatio;
+        s->n_relevant_px = m_nTotRelevantPxCount;
+        s->orig_roi_px = m_nOrigROIPxCount;
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// LOBSTER. Its apply() never advances m_nFrameIdx, so the generator's frame is a count of the apply()
+// calls kept here (initialize() and the refreshes before the first apply() are frame 0).
+// ---------------------------------------------------------------------------------------------
+struct RefLob : BackgroundSubtractorLOBSTER {
+    RngCtx rng;
+    size_t frames = 0;
+    std::vector<uint8_t> exported;
+    explicit RefLob(const olob_params& p)
+        : BackgroundSubtractorLOBSTER(p.desc_dist_threshold, p.color_dist_threshold, p.bg_samples,
+                                      p.required_bg_samples, p.lbsp_threshold_offset, p.rel_lbsp_threshold) {
+        rng.seed = p.seed;
+        rng.frame = &frames;
+    }
+    int W() const { return m_oImgSize.width; }
+    int H() const { return m_oImgSize.height; }
+    int C() const { return (int)m_nImgChannels; }
+    bool inited() const { return m_bInitialized; }
+    const void* map(int which, size_t* nbytes) {
+        exported.clear();
+        const cv::Mat* m = nullptr;
+        switch (which) {
+            case OLOB_MAP_LAST_FG: m = &m_oLastFGMask; break;
+            case OLOB_MAP_ROI: m = &m_oROI; break;
+            case OLOB_MAP_LAST_COLOR: m = &m_oLastColorFrame; break;
+            case OLOB_MAP_LAST_DESC: m = &m_oLastDescFrame; break;
+            case OLOB_MAP_SAMPLE_COLOR:
+                for (const cv::Mat& s : m_voBGColorSamples) append_mat<uint8_t>(exported, s);
+                break;
+            case OLOB_MAP_SAMPLE_DESC:
+                for (const cv::Mat& s : m_voBGDescSamples) append_mat<uint8_t>(exported, s);
+                break;
+            case OLOB_MAP_LUT: exported.assign(m_anLBSPThreshold_8bitLUT.begin(), m_anLBSPThreshold_8bitLUT.end()); break;
+            default: *nbytes = 0; return nullptr;
+        }
+        if (m) append_mat<uint8_t>(exported, *m);
+        *nbytes = exported.size();
+        return exported.data();
+    }
+    void scalars(olob_scalars* s) const {
+        std::memset(s, 0, sizeof(*s));
+        s->frames = frames;
         s->n_relevant_px = m_nTotRelevantPxCount;
         s->orig_roi_px = m_nOrigROIPxCount;
     }
@@ -453,5 +501,63 @@ void rpawcs_set_automatic_model_reset(void* h, int enabled) { ((RefPawcs*)h)->se
 int rpawcs_export(void* h, int which, void* out, size_t bytes) { return ((RefPawcs*)h)->export_map(which, out, bytes); }
 size_t rpawcs_export_bytes(void* h, int which) { return ((RefPawcs*)h)->export_bytes(which); }
 void rpawcs_get_scalars(void* h, opawcs_scalars* s) { ((RefPawcs*)h)->scalars(s); }
+
+// ---- LOBSTER: the reference's BackgroundSubtractorLOBSTER (BackgroundSubtractorLOBSTER.cpp) ----
+void* rlob_create(const olob_params* p) {
+    // the reference's constructor fixes the default median size (9)
+    if (p->default_median_blur_kernel_size != 9) return nullptr;
+    try {
+        return new RefLob(*p);
+    } catch (...) {
+        return nullptr;
+    }
+}
+void rlob_destroy(void* h) { delete (RefLob*)h; }
+int rlob_initialize(void* h, const uint8_t* img, int W, int H, int C, const uint8_t* roi) {
+    RefLob* o = (RefLob*)h;
+    o->frames = 0;
+    o->rng.start_frame((size_t)W * H);
+    cv::Mat m(H, W, mat_type(C), (void*)img);
+    const cv::Mat r = roi_mat(roi, W, H);
+    return guarded(o->rng, [&] { o->initialize(m, r); });
+}
+int rlob_apply(void* h, const uint8_t* img, uint8_t* mask, double lr) {
+    RefLob* o = (RefLob*)h;
+    if (!o->inited()) return OSUB_ENOTINIT;
+    ++o->frames;
+    o->rng.start_frame((size_t)o->W() * o->H());
+    cv::Mat m(o->H(), o->W(), mat_type(o->C()), (void*)img);
+    cv::Mat out(o->H(), o->W(), CV_8UC1, (void*)mask);
+    return guarded(o->rng, [&] { o->apply(m, out, lr); });
+}
+int rlob_refresh_model(void* h, float frac, int force) {
+    RefLob* o = (RefLob*)h;
+    if (!o->inited()) return OSUB_ENOTINIT;
+    return guarded(o->rng, [&] { o->refreshModel(frac, force != 0); });
+}
+int rlob_get_background(void* h, uint8_t* out) {
+    RefLob* o = (RefLob*)h;
+    if (!o->inited()) return OSUB_ENOTINIT;
+    cv::Mat bg;
+    const int rc = guarded(o->rng, [&] { o->getBackgroundImage(bg); });
+    if (rc == OSUB_OK) std::memcpy(out, bg.data, bg.total() * bg.elemSize());
+    return rc;
+}
+int rlob_get_background_descriptors(void* h, uint16_t* out) {
+    RefLob* o = (RefLob*)h;
+    if (!o->inited()) return OSUB_ENOTINIT;
+    cv::Mat bg;
+    const int rc = guarded(o->rng, [&] { o->getBackgroundDescriptorsImage(bg); });
+    if (rc == OSUB_OK) std::memcpy(out, bg.data, bg.total() * bg.elemSize());
+    return rc;
+}
+int rlob_set_roi(void* h, const uint8_t* roi, int W, int H) {
+    RefLob* o = (RefLob*)h;
+    cv::Mat r = roi_mat(roi, W, H);
+    o->rng.start_frame((size_t)W * H);
+    return guarded(o->rng, [&] { o->setROI(r); });
+}
+const void* rlob_map(void* h, int which, size_t* nbytes) { return ((RefLob*)h)->map(which, nbytes); }
+void rlob_get_scalars(void* h, olob_scalars* s) { ((RefLob*)h)->scalars(s); }
 
 }  // extern "C"

@@ -1,7 +1,9 @@
-"""CPU tests that pin the C restatement (oracle/subsense.c, oracle/pawcs.c) to the REFERENCE itself.
+"""CPU tests that pin the C restatement (oracle/subsense.c, oracle/pawcs.c, oracle/lobster.c) to the
+REFERENCE itself.
 
-oracle/_ref/libref.so is the reference's own BackgroundSubtractorSuBSENSE / BackgroundSubtractorPAWCS
-/ BackgroundSubtractorLBSP / BackgroundSubtractionUtils sources (modules/video/src), compiled unmodified
+oracle/_ref/libref.so is the reference's own BackgroundSubtractorSuBSENSE / BackgroundSubtractorPAWCS /
+BackgroundSubtractorLOBSTER / BackgroundSubtractorLBSP / BackgroundSubtractionUtils sources
+(modules/video/src), compiled unmodified
 against a project-written OpenCV stand-in with rand() routed to the counter-based generator
 (oracle/refshim/build_ref.py). Both run on the same frames and every model map is compared after
 initialize() and after every frame: masks, every integer map, every FP32 map (tolerance 0 ulp), all
@@ -211,3 +213,49 @@ def test_non_integral_frame_level_down_sampling(algo, shape):
     frames = _frames(0, 8, 41, width=W, height=H, channels=C)
     pair = sub_pair if algo == "subsense" else pawcs_pair
     pair(frames, seed=13, check_every=2)
+
+
+# ---- LOBSTER (BackgroundSubtractorLOBSTER.cpp:410-620) ----
+LOB_NAMES = pyoracle.LOBSTER_MAP_NAMES
+
+
+def _lob_run(frames, seed, lrs=None, roi=None, refreshes=(), **params):
+    """run_both for LOBSTER (its learning rate is an integer-like rate > 0, default 16); refreshes:
+    (frame index, fraction, force) refreshModel calls made after that frame"""
+    port = pyoracle.OracleLOBSTER(seed=seed, impl="port", **params)
+    ref = pyoracle.OracleLOBSTER(seed=seed, impl="reference", **params)
+    port.initialize(frames[0], roi)
+    ref.initialize(frames[0], roi)
+    _compare(port, ref, LOB_NAMES, "after initialize")
+    for t, f in enumerate(frames[1:], start=1):
+        lr = 16.0 if lrs is None else lrs[t]
+        mp, mr = port.apply(f, lr), ref.apply(f, lr)
+        assert np.array_equal(mp, mr), "frame %d: mask differs at %d px" % (t, int((mp != mr).sum()))
+        _compare(port, ref, LOB_NAMES, "frame %d" % t)
+        for (ti, frac, force) in refreshes:
+            if ti == t:
+                assert port.refresh_model(frac, force) == 0 and ref.refresh_model(frac, force) == 0
+                _compare(port, ref, LOB_NAMES, "refresh after frame %d" % t)
+    return port, ref
+
+
+@pytest.mark.parametrize("config", [0, 2])
+def test_lobster_scene(config):
+    # config 0: 320x240 BGR moving shapes; config 2: 640x480 single-channel scene
+    _lob_run(_frames(config, 16, 1), seed=21)
+
+
+def test_lobster_learning_rates_roi_refresh_and_background_images():
+    fr = _frames(0, 14, 3)
+    roi = np.zeros(fr[0].shape[:2], np.uint8)
+    roi[20:200, 30:290] = 255
+    lrs = [16.0, 1.0, 1.0, 2.0, 3.5, 16.0, float("inf"), 1.0, 4.0, 16.0, 1.0, 2.0, 16.0, 1.0]
+    port, ref = _lob_run(fr, seed=4, lrs=lrs, roi=roi, refreshes=((5, 0.4, False), (9, 1.0, True)))
+    assert np.array_equal(port.background(), ref.background())
+    assert np.array_equal(port.background_descriptors(), ref.background_descriptors())
+
+
+def test_lobster_parameters_gray():
+    fr = _frames(0, 10, 5, channels=1)
+    _lob_run(fr, seed=8, bg_samples=20, required_bg_samples=3, desc_dist_threshold=2, color_dist_threshold=40,
+             rel_lbsp_threshold=0.5)
