@@ -20,6 +20,7 @@
 // Post-processing, frame-level statistics and the automatic model reset follow in the same launch.
 #include <cuda_runtime.h>
 
+#include "lbsp_device.cuh"
 #include "lvbgs_internal.h"
 
 namespace lvbgs {
@@ -124,18 +125,6 @@ __device__ __forceinline__ unsigned long long mod_draw(uint32_t a, unsigned long
 __device__ __forceinline__ uint32_t mod_n(uint32_t a, const StreamDev& S) {
     const uint32_t q = (uint32_t)(((unsigned long long)a * S.nMagic) >> 40);
     return a - q * (uint32_t)S.N;
-}
-
-// LBSP::computeDescriptor_threshold (LBSP.hpp:193-202) on 16 packed taps: bit n = |tap_n - ref| > thr
-__device__ __forceinline__ uint32_t lbsp_thr(const uint32_t v[4], uint32_t ref, uint32_t thr) {
-    const uint32_t r4 = ref * 0x01010101u, t4 = thr * 0x01010101u;
-    uint32_t d = 0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const uint32_t m = __vcmpgtu4(__vabsdiffu4(v[j], r4), t4);
-        d |= (((m & 0x80808080u) * 0x00204081u) >> 28) << (4 * j);
-    }
-    return d;
 }
 
 __device__ __forceinline__ void clamp_xy(int& x, int& y, int W, int H) {
@@ -654,9 +643,28 @@ __device__ void phaseA_tile(const TickParams& P, int si, const StreamDev& S, int
     const bool inFrame = x < S.W && y < S.H;
     const int p = y * S.W + x;
     const bool active = inFrame && S.roi[p] != 0;
-    // per-pixel loads first: they overlap the tile load below
-    PixIn<C> in;
-    if (active) load_pix<C>(S, F, p, in);
+    // the scan's inputs first (they overlap the tile load below); the other maps after the scan
+    float tR = 0, tRwLT = 0, tRwST = 0, tFnLT = 0, tFnST = 0;
+    uint32_t tU = 0, c0 = 0, c1 = 0;
+    uint64_t d0 = 0, d1 = 0;
+    if (active) {
+        const int npx = S.npx;
+        const float* fc = S.fm + (size_t)F.cur * kNumFloatMaps * npx;
+        tR = fc[FM_R * npx + p];
+        tRwLT = fc[FM_RAW_LT * npx + p];
+        tRwST = fc[FM_RAW_ST * npx + p];
+        tFnLT = fc[FM_FIN_LT * npx + p];
+        tFnST = fc[FM_FIN_ST * npx + p];
+        tU = S.unst[(size_t)F.cur * npx + p];
+        if (S.N > 0) {
+            d0 = C == 3 ? ((const uint64_t*)S.sD)[p] : (uint64_t)((const uint16_t*)S.sD)[p];
+            c0 = S.sC[p];
+        }
+        if (S.N > 1) {
+            d1 = C == 3 ? ((const uint64_t*)S.sD)[(size_t)npx + p] : (uint64_t)((const uint16_t*)S.sD)[(size_t)npx + p];
+            c1 = S.sC[(size_t)npx + p];
+        }
+    }
     uint8_t* tile = smem;
     uint8_t* lut = smem + RW * RH;
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = S.ctl->lut[i];
@@ -695,11 +703,10 @@ __device__ void phaseA_tile(const TickParams& P, int si, const StreamDev& S, int
                 intra[c] = lbsp_thr(vals[c], curr[c], lut[curr[c]]);
             }
             nz = desc_nonzero<C>(intra);
-            const EvalThr th = eval_thresholds(S, in.R, in.RwLT, in.RwST, in.FnLT, in.FnST, in.uOld);
+            const EvalThr th = eval_thresholds(S, tR, tRwLT, tRwST, tFnLT, tFnST, tU);
             ScanSt st;
             scan_init<C>(st);
-            scan_samples<C, false>(S, lut, p, vals, curr, intra, th, nullptr, 0, 0ull, kScanCap, in.d0, in.c0, in.d1,
-                                   in.c1, st);
+            scan_samples<C, false>(S, lut, p, vals, curr, intra, th, nullptr, 0, 0ull, kScanCap, d0, c0, d1, c1, st);
             if (st.nGood < S.nreq && st.s < S.N) {
                 // a long scan: continued and finished by lvbgs_k_longscan over the compacted list, so
                 // that its warps hold only long scans
@@ -710,6 +717,8 @@ __device__ void phaseA_tile(const TickParams& P, int si, const StreamDev& S, int
                            ((unsigned long long)st.minDesc << 32) | ((unsigned long long)st.minSum << 48);
             } else {
                 if (st.s >= S.N) record_scan(S, F, p, st);  // a foreground scan that ended within the cap
+                PixIn<C> in;
+                load_pix<C>(S, F, p, in);
                 intent = eval_tail<C>(S, F, x, y, p, in, curr, intra, th.uNew, st);
             }
         }
@@ -1649,7 +1658,7 @@ __device__ void refresh_pixel(const StreamDev& S, int p, uint32_t frame, int sta
     const StreamDev& S = P.streams[si];                                     \
     const int lt = t - S.tileBase;
 
-extern "C" __global__ void __launch_bounds__(kThreads, 4) lvbgs_k_eval(TickParams P) {
+extern "C" __global__ void __launch_bounds__(kThreads, 5) lvbgs_k_eval(TickParams P) {
     __shared__ __align__(16) uint8_t smem[((((kTileW + 4) * 3 + 2 + 3) / 4) * 4) * (kTileH + 4) + 256];
     LV_TILE_KERNEL_PROLOGUE
     if (S.C == 3) phaseA_tile<3>(P, si, S, lt, smem);
