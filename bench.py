@@ -267,6 +267,62 @@ def single_stream_run(config, n_frames, stream, cpu=True, cpu_frames=4):
     return out
 
 
+def lobster_run(config, n_frames, stream, cpu=True, cpu_frames=4):
+    """LOBSTER (BackgroundSubtractorLOBSTER's non-parallel path) on the scenes of SuBSENSE configs 0 and 1
+    (one seeded stream: 320x240 BGR; 1920x1080 BGR) at the reference's default learning rate (16): every
+    frame through lvbgs_apply from frames resident on the device, wall clock per frame (the first 10
+    frames are warm-up); the CPU baseline is the oracle's LOBSTER on one core over the first cpu_frames
+    frames."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    from litiv_gb300 import BackgroundSubtractorLOBSTER, SyntheticStream
+    from litiv_gb300 import _lib as L
+    from litiv_gb300.metrics import BinClassif
+    lib = L.lib()
+    s = SyntheticStream(config, 0, 1)
+    W, H = s.cfg.width, s.cfg.height
+    n = min(n_frames, s.n_frames)
+    dev = torch.empty((n,) + s.shape, dtype=torch.uint8, device="cuda")
+    dgt = torch.empty((n, H, W), dtype=torch.uint8, device="cuda")
+    for t in range(n):
+        s.render_device(t, dev[t].data_ptr(), dgt[t].data_ptr(), cuda_stream=stream.cuda_stream)
+    dmask = torch.empty((H, W), dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    b = BackgroundSubtractorLOBSTER(seed=1)
+    b.initialize(dev[0])
+    ms = []
+    quality = BinClassif()
+    for t in range(1, n):
+        t0 = time.perf_counter()
+        st = lib.lvbgs_apply(b.handle, C.c_void_p(dev[t].data_ptr()), 0, C.c_void_p(dmask.data_ptr()), 16.0,
+                             C.c_void_p(stream.cuda_stream))
+        stream.synchronize()
+        ms.append((time.perf_counter() - t0) * 1e3)
+        if st != L.OK:
+            raise RuntimeError("apply failed: %s" % lib.lvbgs_last_error(b.handle))
+        if t > 25:
+            quality.accumulate(dmask, dgt[t], cuda_stream=stream.cuda_stream)
+    b.close()
+    qm = quality.metrics()
+    m = np.array(ms[9:])
+    out = {"workload": "LOBSTER: one %dx%d %s stream (the SuBSENSE config %d scene), %d frames, default "
+                       "parameters, learning rate 16" % (W, H, "BGR" if s.cfg.channels == 3 else "gray", config, n),
+           "value": W * H / (m.mean() / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_frame": float(m.mean()),
+           "p50_frame_ms": float(np.percentile(m, 50)), "p99_frame_ms": float(np.percentile(m, 99)),
+           "quality": {"f_measure": qm["dFMeasure"], "recall": qm["dRecall"], "precision": qm["dPrecision"],
+                       "frames_scored": max(0, n - 26)}}
+    if cpu:
+        from oracle import pyoracle
+        fr = np.stack([s.render(t) for t in range(cpu_frames + 1)])
+        wall = pyoracle.run_lobster_streams([fr], [1], 1)
+        px = W * H * cpu_frames
+        out["cpu_baseline"] = {"value": px / wall / 1e6, "unit": "Mpix/s", "cores": 1, "kind": "port",
+                               "sample": "the first %d applied frames on one core, %.1f Mpix in %.2f s" % (
+                                   cpu_frames, px / 1e6, wall)}
+    return out
+
+
 def serving_run(seconds):
     """The serving workload (Poisson arrivals of 4 streams/s up to 256 live, lives U[10, 60] s, 30 fps,
     320x240/640x480/1280x720/1920x1080 with p = .3/.3/.3/.1, a quarter single-channel), started from its
@@ -328,6 +384,8 @@ def main():
                     help="measured span of the serving workload run (0: skip)")
     ap.add_argument("--single-frames", type=int, default=100,
                     help="frames of the single-stream SuBSENSE configs 0 and 1 (0: skip)")
+    ap.add_argument("--lobster-frames", type=int, default=100,
+                    help="frames of the single-stream LOBSTER legs (0: skip)")
     ap.add_argument("--pawcs-channels", default="both", choices=["1", "3", "both"],
                     help="PAWCS legs: the single-channel scene (config 2), the BGR scene, or both")
     ap.add_argument("--pawcs-only", action="store_true",
@@ -481,36 +539,89 @@ def main():
     rounds = sum(b["stat_repair_rounds"] - a["stat_repair_rounds"] for a, b in zip(sc0[:1], sc1[:1])) / args.steps
     remat = sum(b["stat_repair_rematched"] - a["stat_repair_rematched"] for a, b in zip(sc0, sc1)) / args.steps
 
-    # ---- e2e through the C-ABI: pinned host frames in, host masks out ----
+    # ---- e2e through the C-ABI: host frames in, host masks out ----
+    # Pipelined (the headline): a frame precacher (lvbgs_precacher_*) whose packet is one tick (the 64
+    # frames back to back) copies each tick from host memory into a pinned slot on its worker thread
+    # (as a decoder would write it) and uploads it on its own copy stream while the previous tick
+    # computes; each tick then runs lvbgs_batch_apply on the device copies and waits for its host masks.
+    # Precaching starts inside the timed region with an empty ring, so every timed tick's copies are
+    # timed. Unpipelined (e2e.unpipelined): lvbgs_batch_apply on pinned host frames, uploads on the
+    # compute stream, one wait per tick.
     e2e = None
     if not args.no_e2e:
-        e2e_steps = min(args.steps, 10)
+        e2e_steps = args.steps
+        h2d = sum(int(np.prod(s.shape)) for s in synth)
+        offs, o = [], 0
+        for s in synth:
+            offs.append(o)
+            o += (int(np.prod(s.shape)) + 255) // 256 * 256
+        pkt_bytes = o
+        first = 1 + args.warmup
+        packets = torch.empty((e2e_steps, pkt_bytes), dtype=torch.uint8, pin_memory=True)
+        for k in range(e2e_steps):
+            for i in range(n):
+                nb = int(np.prod(synth[i].shape))
+                packets[k, offs[i]:offs[i] + nb].copy_(dev_frames[i][first + k].reshape(-1))
+        hmasks = [torch.empty((s.cfg.height, s.cfg.width), dtype=torch.uint8, pin_memory=True) for s in synth]
+        hm = [m.data_ptr() for m in hmasks]
+        hp = L.HostPackets(packets.data_ptr(), pkt_bytes, e2e_steps)
+        pc = C.c_void_p()
+        check(lib.lvbgs_precacher_create(C.cast(lib.lvbgs_precache_copy_loader, C.c_void_p),
+                                         C.cast(C.pointer(hp), C.c_void_p), pkt_bytes, local, C.byref(pc)), None)
+        subs_e = make_subtractors(5000)
+        hse = (C.c_void_p * n)(*[b.handle for b in subs_e])
+        fr = (L.LvbgsFrame * n)()
+        for t in range(1, first):  # warm-up ticks from device frames
+            check(lib.lvbgs_batch_apply(hse, frames_struct(subs_e, t, hm), n, sptr), hse[0])
+            check(lib.lvbgs_batch_wait(hse, n, sptr), hse[0])
+        # the ring's pinned slots are allocated by a first start, outside the timed region
+        check(lib.lvbgs_precacher_start(pc, 4 * pkt_bytes), None)
+        check(lib.lvbgs_precacher_stop(pc), None)
+        torch.cuda.synchronize()
+        dp, hpp, sz = C.c_void_p(), C.c_void_p(), C.c_size_t()
+        t0 = time.perf_counter()
+        check(lib.lvbgs_precacher_start(pc, 4 * pkt_bytes), None)
+        for k in range(e2e_steps):
+            check(lib.lvbgs_precacher_get(pc, k, sptr, C.byref(dp), C.byref(hpp), C.byref(sz)), None)
+            for i in range(n):
+                fr[i].image = dp.value + offs[i]
+                fr[i].stride = 0
+                fr[i].fgmask = hm[i]
+                fr[i].learning_rate = 0.0
+            check(lib.lvbgs_batch_apply(hse, fr, n, sptr), hse[0])
+            check(lib.lvbgs_batch_wait(hse, n, sptr), hse[0])  # masks are on the host after the wait
+        el = time.perf_counter() - t0
+        lib.lvbgs_precacher_destroy(pc)
+        for b in subs_e:
+            b.close()
+        # unpipelined: pinned host frames straight into lvbgs_batch_apply
+        subs_u = make_subtractors(5000)
+        hsu = (C.c_void_p * n)(*[b.handle for b in subs_u])
         host = []
         for i in range(n):
             hb = torch.empty(dev_frames[i].shape, dtype=torch.uint8, pin_memory=True)
             hb.copy_(dev_frames[i])
             host.append(hb.numpy())
-        hmasks = [torch.empty((s.cfg.height, s.cfg.width), dtype=torch.uint8, pin_memory=True) for s in synth]
-        hm = [m.data_ptr() for m in hmasks]
-        subs_e = make_subtractors(5000)
-        hse = (C.c_void_p * n)(*[b.handle for b in subs_e])
-        fre = [frames_struct(subs_e, t, hm, host=host) for t in range(ticks)]
-        for t in range(1, 1 + args.warmup):
-            check(lib.lvbgs_batch_apply(hse, fre[t], n, sptr), hse[0])
-        check(lib.lvbgs_batch_wait(hse, n, sptr), hse[0])
+        fru = [frames_struct(subs_u, t, hm, host=host) for t in range(ticks)]
+        for t in range(1, first):
+            check(lib.lvbgs_batch_apply(hsu, fru[t], n, sptr), hsu[0])
+        check(lib.lvbgs_batch_wait(hsu, n, sptr), hsu[0])
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        t1 = time.perf_counter()
         for k in range(e2e_steps):
-            t = 1 + args.warmup + k
-            check(lib.lvbgs_batch_apply(hse, fre[t], n, sptr), hse[0])
-            check(lib.lvbgs_batch_wait(hse, n, sptr), hse[0])  # masks are on the host after the wait
-        el = time.perf_counter() - t0
-        h2d = sum(int(np.prod(s.shape)) for s in synth)
+            check(lib.lvbgs_batch_apply(hsu, fru[first + k], n, sptr), hsu[0])
+            check(lib.lvbgs_batch_wait(hsu, n, sptr), hsu[0])
+        el_u = time.perf_counter() - t1
+        for b in subs_u:
+            b.close()
         e2e = {"value": px_step * e2e_steps / el / 1e6, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": px_step, "ms_per_step": el / e2e_steps * 1e3,
-               "note": "pinned host frames -> lvbgs_batch_apply -> host masks, wall clock incl. the waits"}
-        for b in subs_e:
-            b.close()
+               "note": "host frames -> frame precacher (pinned slots, uploads on a copy stream overlapping the "
+                       "previous tick, started inside the timed region) -> lvbgs_batch_apply -> host masks; "
+                       "wall clock incl. one wait per tick",
+               "unpipelined": {"value": px_step * e2e_steps / el_u / 1e6, "ms_per_step": el_u / e2e_steps * 1e3,
+                               "note": "pinned host frames -> lvbgs_batch_apply (uploads on the compute "
+                                       "stream) -> host masks"}}
 
     # ---- plain form: one stream per launch ----
     plain = None
@@ -554,6 +665,11 @@ def main():
                    "config1": single_stream_run(1, args.single_frames, stream, cpu=not args.no_cpu_baseline,
                                                 cpu_frames=2)}
 
+    lobster = None
+    if rank == 0 and args.lobster_frames > 0:
+        lobster = {"config0": lobster_run(0, args.lobster_frames, stream, cpu=not args.no_cpu_baseline, cpu_frames=10),
+                   "config1": lobster_run(1, args.lobster_frames, stream, cpu=not args.no_cpu_baseline, cpu_frames=2)}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline()
@@ -591,6 +707,7 @@ def main():
             "serving": serve,
             "pawcs": pawcs,
             "single_stream": singles,
+            "lobster": lobster,
             "clocks": clk.summary(),
         }
         print(json.dumps(out))

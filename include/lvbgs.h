@@ -39,7 +39,7 @@ typedef enum {
     LVBGS_BUSY = 9             /* serving: a queue or capacity limit refused the request (retry later) */
 } lvbgs_status;
 
-typedef enum { LVBGS_ALGO_SUBSENSE = 0, LVBGS_ALGO_PAWCS = 1 } lvbgs_algo;
+typedef enum { LVBGS_ALGO_SUBSENSE = 0, LVBGS_ALGO_PAWCS = 1, LVBGS_ALGO_LOBSTER = 2 } lvbgs_algo;
 
 typedef struct lvbgs_ctx* lvbgs_handle;
 
@@ -296,6 +296,64 @@ enum {
 };
 size_t lvbgs_pawcs_debug_export_bytes(lvbgs_handle h, int which);
 lvbgs_status lvbgs_pawcs_debug_export(lvbgs_handle h, int which, void* out, size_t bytes);
+
+/* ---- Frame precaching: lv::DataPrecacher (modules/datasets/include/litiv/datasets/utils.hpp:456-478,
+ * modules/datasets/src/utils.cpp:302-470) for a GPU consumer ----
+ * A loader fills packet `idx` into `dst` (capacity `cap` bytes) and returns its size, 0 at the end of the
+ * stream (an empty packet halts precaching, utils.hpp:458), or a size above `cap` for an error. With
+ * precaching started, a worker thread loads the packets after the last request into a ring of pinned
+ * host slots, each uploaded to its own device slot on a dedicated copy stream, so the uploads of the
+ * next packets overlap the caller's work on the current one. */
+typedef size_t (*lvbgs_packet_loader)(void* user, size_t idx, uint8_t* dst, size_t cap);
+typedef struct lvbgs_precacher_ctx* lvbgs_precacher;
+/* DataPrecacher(lDataLoaderCallback) (utils.cpp:302-308); packets are at most max_packet_bytes */
+lvbgs_status lvbgs_precacher_create(lvbgs_packet_loader loader, void* user, size_t max_packet_bytes, int device_id,
+                                    lvbgs_precacher* out);
+/* ~DataPrecacher(): stops the worker, waits for the device and frees the slots */
+lvbgs_status lvbgs_precacher_destroy(lvbgs_precacher p);
+/* startAsyncPrecaching(nSuggestedBufferSize) (utils.cpp:358-374): an empty ring of
+ * buffer_bytes / max_packet_bytes slots (2 to 64), filled from packet 0 on; a ring of the same size as the
+ * last one is reused (allocating pinned slots is slow); 0 leaves precaching off */
+lvbgs_status lvbgs_precacher_start(lvbgs_precacher p, size_t buffer_bytes);
+/* stopAsyncPrecaching() (utils.cpp:376-386): joins the worker and empties the ring (its slots stay
+ * allocated); reports a loader error the worker met (the reference rethrows it) */
+lvbgs_status lvbgs_precacher_stop(lvbgs_precacher p);
+/* getPacket(idx) (utils.cpp:314-356): *device_packet / *host_packet receive the packet's device and pinned
+ * host copies and *size its size (0 and null pointers past the end of the stream). cuda_stream (a
+ * cudaStream_t, NULL = the legacy default stream) is made to wait for the packet's upload; no host wait
+ * when it is already loaded. The packet stays valid until the next call with another index, which
+ * releases it on that call's stream: work enqueued there before the call may still read it. Requests are
+ * expected in order; another index restarts the sequence there. When the loader fails, the packets
+ * loaded before are still served and the request of the failing one reports the error. Not to be called
+ * concurrently. */
+lvbgs_status lvbgs_precacher_get(lvbgs_precacher p, size_t idx, void* cuda_stream, const uint8_t** device_packet,
+                                 const uint8_t** host_packet, size_t* size);
+/* isActive() and getLastReqIdx() (utils.hpp:468-471); SIZE_MAX before the first request */
+int lvbgs_precacher_is_active(lvbgs_precacher p);
+size_t lvbgs_precacher_last_index(lvbgs_precacher p);
+/* a loader over packets already in host memory: user points to an lvbgs_host_packets; packet idx is the
+ * packet_bytes bytes at base + idx * packet_bytes, for idx < count */
+typedef struct {
+    const uint8_t* base;
+    size_t packet_bytes;
+    size_t count;
+} lvbgs_host_packets;
+size_t lvbgs_precache_copy_loader(void* user, size_t idx, uint8_t* dst, size_t cap);
+
+/* ---- LOBSTER (BackgroundSubtractorLOBSTER, modules/video/src/BackgroundSubtractorLOBSTER.cpp) ----
+ * A handle created with LVBGS_ALGO_LOBSTER runs LOBSTER's non-parallel path (:459-581) on single- and
+ * three-channel frames; the reference's GLSL path is not part of this library. lvbgs_params maps onto
+ * the constructor (BackgroundSubtractorLOBSTER.hpp:50-55): desc_dist_threshold_offset carries
+ * nDescDistThreshold (4), min_color_dist_threshold nColorDistThreshold (30), bg_samples (35, at most 64),
+ * required_bg_samples (2), lbsp_threshold_offset (0), rel_lbsp_threshold (0.333); samples_for_moving_avgs
+ * is unused. lvbgs_apply's learning_rate is LOBSTER's dLearningRate: it must be positive (ceil() gives
+ * the update rate; +inf never updates) and the reference's default is 16 (lvbgs_get_default_learning_rate).
+ * initialize, get_background, get_background_descriptors, refresh_model (refreshModel(frac, force),
+ * :410-440), set_roi, get_roi, get_size, get_scalars (frame_idx counts apply() calls) and the maps
+ * LVBGS_MAP_LAST_FG, _ROI, _LAST_COLOR, _LAST_DESC, _SAMPLE_COLOR, _SAMPLE_DESC and _LUT work as for
+ * SuBSENSE; batched steps and spilling are SuBSENSE/PAWCS-only. LOBSTER keeps no frame counter of its own,
+ * so draw k of pixel p in the i-th apply() is keyed by frame i (initialize() and refreshes before the first
+ * apply() are frame 0). */
 
 #ifdef __cplusplus
 }

@@ -1,9 +1,11 @@
-"""GB300 (sm_103a) SuBSENSE and PAWCS background subtraction with LITIV's interface.
+"""GB300 (sm_103a) SuBSENSE, PAWCS and LOBSTER background subtraction with LITIV's interface.
 
 The compute path is the in-tree CUDA library ``_build/liblvbgs.so`` (C-ABI in include/lvbgs.h);
-this package is its host-side mirror of the reference's BackgroundSubtractorSuBSENSE and
-BackgroundSubtractorPAWCS interfaces.
+this package is its host-side mirror of the reference's BackgroundSubtractorSuBSENSE,
+BackgroundSubtractorPAWCS and BackgroundSubtractorLOBSTER interfaces.
 """
-from .bgs import BackgroundSubtractorPAWCS, BackgroundSubtractorSuBSENSE, LvException, batch_apply, lbsp_compute2  # noqa: F401
+from .bgs import (BackgroundSubtractorLOBSTER, BackgroundSubtractorPAWCS, BackgroundSubtractorSuBSENSE,  # noqa: F401
+                  LvException, batch_apply, lbsp_compute2)
+from .precache import DataPrecacher, DevicePacket  # noqa: F401
 from .synth import SyntheticStream  # noqa: F401
 from . import _lib  # noqa: F401

@@ -16,7 +16,7 @@ LIB_PATH = os.environ.get("LVBGS_LIB") or os.path.join(HERE, "_build", "liblvbgs
 OK, BAD_ARG, BAD_SIZE, BAD_TYPE, NOT_INITIALIZED, OOM, DEVICE_TIMEOUT, DEVICE_ERROR, UNSUPPORTED, BUSY = range(10)
 STATUS_NAMES = ["OK", "BAD_ARG", "BAD_SIZE", "BAD_TYPE", "NOT_INITIALIZED", "OOM", "DEVICE_TIMEOUT",
                 "DEVICE_ERROR", "UNSUPPORTED", "BUSY"]
-ALGO_SUBSENSE, ALGO_PAWCS = 0, 1
+ALGO_SUBSENSE, ALGO_PAWCS, ALGO_LOBSTER = 0, 1, 2
 
 # map ids (LVBGS_MAP_*)
 MAP_NAMES = ["R", "V", "T", "DLAST", "DMIN_LT", "DMIN_ST", "RAW_LT", "RAW_ST", "FIN_LT", "FIN_ST",
@@ -36,6 +36,14 @@ class LvbgsParams(C.Structure):
 class LvbgsFrame(C.Structure):
     _fields_ = [("image", C.c_void_p), ("stride", C.c_size_t), ("fgmask", C.c_void_p),
                 ("learning_rate", C.c_double)]
+
+
+class HostPackets(C.Structure):
+    """lvbgs_host_packets: packets already in host memory, for lvbgs_precache_copy_loader"""
+    _fields_ = [("base", C.c_void_p), ("packet_bytes", C.c_size_t), ("count", C.c_size_t)]
+
+
+PACKET_LOADER = C.CFUNCTYPE(C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(C.c_uint8), C.c_size_t)
 
 
 class LvbgsScalars(C.Structure):
@@ -146,6 +154,15 @@ SIGNATURES = {
     "lvbgs_classif_accumulate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                            C.POINTER(C.c_uint64), C.c_int, C.c_void_p]),
     "lvbgs_classif_metrics": (C.c_int, [C.POINTER(C.c_uint64), C.POINTER(C.c_double)]),
+    "lvbgs_precacher_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int, C.POINTER(C.c_void_p)]),
+    "lvbgs_precacher_destroy": (C.c_int, [C.c_void_p]),
+    "lvbgs_precacher_start": (C.c_int, [C.c_void_p, C.c_size_t]),
+    "lvbgs_precacher_stop": (C.c_int, [C.c_void_p]),
+    "lvbgs_precacher_get": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.POINTER(C.c_void_p),
+                                      C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]),
+    "lvbgs_precacher_is_active": (C.c_int, [C.c_void_p]),
+    "lvbgs_precacher_last_index": (C.c_size_t, [C.c_void_p]),
+    "lvbgs_precache_copy_loader": (C.c_size_t, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t]),
     "lvbgs_set_roi": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
     "lvbgs_batch_set_repair_share": (C.c_int, [C.c_void_p, C.c_int]),
     "lvbgs_set_batch_groups": (C.c_int, [C.c_int]),

@@ -97,7 +97,11 @@ class BackgroundSubtractorSuBSENSE:
         _check(L.lib().lvbgs_initialize(self._h, ip, W, H, Cc, 0, rp), self._h)
         self._shape = (H, W, Cc)
 
-    def apply(self, image, fgmask=None, learningRateOverride=0.0):
+    def apply(self, image, fgmask=None, learningRateOverride=0.0, stream=None):
+        """apply(image, fgmask, learningRateOverride); `stream` (a cudaStream_t as int, or a
+        torch.cuda.Stream) runs the frame step on that stream instead of the handle's own"""
+        if stream is not None and hasattr(stream, "cuda_stream"):
+            stream = stream.cuda_stream
         if self._shape is None:
             raise LvException(L.NOT_INITIALIZED, "algo & model must be initialized first")
         H, W, Cc = _shape(image)
@@ -107,7 +111,8 @@ class BackgroundSubtractorSuBSENSE:
             fgmask = np.empty((H, W), np.uint8)
         ip, keep = _ptr(image)
         mp, mkeep = _ptr(fgmask)
-        _check(L.lib().lvbgs_apply(self._h, ip, 0, mp, float(learningRateOverride), None), self._h)
+        _check(L.lib().lvbgs_apply(self._h, ip, 0, mp, float(learningRateOverride),
+                                   C.c_void_p(stream) if stream else None), self._h)
         if isinstance(fgmask, np.ndarray) and mkeep is not fgmask:
             fgmask[...] = mkeep
         return fgmask
@@ -279,6 +284,68 @@ class BackgroundSubtractorPAWCS:
         s = L.PawcsScalars()
         _check(L.lib().lvbgs_pawcs_get_scalars(self._h, C.byref(s)), self._h)
         return {f: getattr(s, f) for f, _ in L.PawcsScalars._fields_}
+
+
+class BackgroundSubtractorLOBSTER:
+    """LOBSTER on the GPU, single- and three-channel frames (the non-parallel path of
+    BackgroundSubtractorLOBSTER, modules/video/src/BackgroundSubtractorLOBSTER.cpp:410-620);
+    BackgroundSubtractorLOBSTER.hpp:50-55 for the constructor parameters and their defaults. apply()'s
+    learning rate is LOBSTER's dLearningRate (positive; BGSLOBSTER_DEFAULT_LEARNING_RATE = 16)."""
+
+    def __init__(self, nDescDistThreshold=4, nColorDistThreshold=30, nBGSamples=35, nRequiredBGSamples=2,
+                 nLBSPThresholdOffset=0, fRelLBSPThreshold=0.333, seed=0, device_id=0,
+                 nDefaultMedianBlurKernelSize=9):
+        lib = L.lib()
+        p = L.LvbgsParams()
+        _check(lib.lvbgs_default_params(L.ALGO_LOBSTER, C.byref(p)))
+        p.desc_dist_threshold_offset = nDescDistThreshold
+        p.min_color_dist_threshold = nColorDistThreshold
+        p.bg_samples = nBGSamples
+        p.required_bg_samples = nRequiredBGSamples
+        p.rel_lbsp_threshold = fRelLBSPThreshold
+        p.lbsp_threshold_offset = nLBSPThresholdOffset
+        p.default_median_blur_kernel_size = nDefaultMedianBlurKernelSize
+        p.seed = seed
+        p.device_id = device_id
+        self.params = p
+        h = C.c_void_p()
+        _check(lib.lvbgs_create(L.ALGO_LOBSTER, C.byref(p), C.byref(h)))
+        self._h = h
+        self._shape = None
+
+    def close(self):
+        if self._h:
+            L.lib().lvbgs_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    initialize = BackgroundSubtractorSuBSENSE.initialize
+    getBackgroundImage = BackgroundSubtractorSuBSENSE.getBackgroundImage
+    getBackgroundDescriptorsImage = BackgroundSubtractorSuBSENSE.getBackgroundDescriptorsImage
+    refreshModel = BackgroundSubtractorSuBSENSE.refreshModel
+    setAutomaticModelReset = BackgroundSubtractorSuBSENSE.setAutomaticModelReset
+    getDefaultLearningRate = BackgroundSubtractorSuBSENSE.getDefaultLearningRate
+    getROICopy = BackgroundSubtractorSuBSENSE.getROICopy
+    validateROI = BackgroundSubtractorSuBSENSE.validateROI
+    setROI = BackgroundSubtractorSuBSENSE.setROI
+    isParallel = BackgroundSubtractorSuBSENSE.isParallel
+    getParallelAlgoType = BackgroundSubtractorSuBSENSE.getParallelAlgoType
+    state_map = BackgroundSubtractorSuBSENSE.state_map
+    scalars = BackgroundSubtractorSuBSENSE.scalars
+    _need_init = BackgroundSubtractorSuBSENSE._need_init
+
+    def apply(self, image, fgmask=None, learningRate=16.0, stream=None):
+        """BackgroundSubtractorLOBSTER::apply(image, fgmask, dLearningRate=16) (:459-581)"""
+        return BackgroundSubtractorSuBSENSE.apply(self, image, fgmask, learningRate, stream)
 
 
 def map_view(name, raw, W, H, Cc, N):

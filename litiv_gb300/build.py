@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liblvbgs.so")
 SOURCES = ["subsense_kernels.cu", "pawcs_kernels.cu", "pawcs3_kernels.cu", "lvbgs_capi.cu", "synth.cu", "lbsp_noalloc.cu",
-           "serve.cu", "metrics.cu"]
+           "serve.cu", "metrics.cu", "lobster.cu", "precache.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
          "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I" + os.path.join(HERE, "..", "include")]

@@ -1,0 +1,806 @@
+// LOBSTER frame step for sm_103a (BackgroundSubtractorLOBSTER.cpp:459-581, the non-parallel path).
+//
+// The reference scans the ROI pixels in raster order. A pixel reads its own samples, which an earlier
+// pixel's neighbour update may have overwritten in the same frame (:510-512 / :569-574); nothing else
+// it reads changes during the frame. Random draws are keyed by (seed, frame, pixel, draw index), so
+// they do not depend on the scan order. A frame step therefore
+//   1. evaluates every pixel against the frame-start samples (lob_k_eval): decision, samples scanned
+//      e, and the model writes it makes (own sample, neighbour target and sample), in an intent word;
+//   2. marks the pixels whose scan read a sample that an earlier neighbour writes (lob_k_mark);
+//   3. re-evaluates the marked pixels with the samples the raster scan would see (the latest earlier
+//      writer of each sample), and marks the later pixels whose incoming writes changed, round after
+//      round until nothing changes (lob_k_round; the dependencies follow raster order, so this is the
+//      raster-order fixed point). Rounds are enqueued ahead; a converged flag makes the rest return;
+//   4. commits every sample write in raster order, each pixel gathering the writes aimed at it from
+//      its 3x3 neighbourhood (lob_k_commit), then the median blur of the mask (:577-579).
+// The writers of a pixel are within one pixel of it: getNeighborPosition_3x3 moves one step and
+// clamps into the LBSP border, and ROI pixels lie inside that border.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "lbsp_device.cuh"
+#include "lobster_internal.h"
+
+namespace lvbgs {
+
+namespace {
+
+// LBSP 16-bit double-cross pattern (LBSP.hpp:297-298) as compile-time offsets: (offset + 2) in three
+// bits per tap, so that unrolled tap loops fold the offsets into immediates
+constexpr unsigned long long pack3(const int (&a)[16]) {
+    unsigned long long v = 0;
+    for (int i = 0; i < 16; ++i) v |= (unsigned long long)(a[i] + 2) << (3 * i);
+    return v;
+}
+constexpr int kDx[16] = {-2, 2, 0, 0, -2, 2, 2, -2, 0, -1, 0, 1, -1, 1, 1, -1};
+constexpr int kDy[16] = {0, 0, -2, 2, 2, -2, 2, -2, 1, 0, -1, 0, -1, 1, -1, 1};
+constexpr unsigned long long kDx3 = pack3(kDx), kDy3 = pack3(kDy);
+__device__ __forceinline__ constexpr int tap_dx(int n) { return (int)((kDx3 >> (3 * n)) & 7ull) - 2; }
+__device__ __forceinline__ constexpr int tap_dy(int n) { return (int)((kDy3 >> (3 * n)) & 7ull) - 2; }
+
+// 7x7 Gaussian sampling weights (opencv.hpp:915-923) and the 3x3 neighbour table (opencv.hpp:945-953)
+__constant__ int c_lob_pat7[49] = {2,  4,  6,  7,  6,  4,  2,  4,  8,  12, 14, 12, 8,  4,  6, 12, 21,
+                                   25, 21, 12, 6,  7,  14, 25, 28, 25, 14, 7,  6,  12, 21, 25, 21, 12,
+                                   6,  4,  8,  12, 14, 12, 8,  4,  2,  4,  6,  7,  6,  4,  2};
+__constant__ int c_lob_nb3[8][2] = {{-1, 1}, {0, 1}, {1, 1}, {-1, 0}, {1, 0}, {-1, -1}, {0, -1}, {1, -1}};
+
+constexpr int kThreadsL = 256;
+constexpr int kMaxRoundsL = 4096;  // repair rounds of one frame step before LVBGS_DEVICE_ERROR
+
+// ---- intent word ----
+// bit 0 valid (ROI pixel evaluated), bit 1 foreground, bits 2-8 samples scanned, bit 9 own-sample write,
+// bits 10-15 its sample, bit 16 neighbour write, bits 17-20 neighbour code (dy+1)*3+(dx+1), bits 21-26
+// its sample, bits 27-29 draws consumed
+constexpr uint32_t kIValid = 1u, kIFG = 2u, kIOwn = 1u << 9, kINb = 1u << 16;
+__device__ __forceinline__ int i_e(uint32_t w) { return (int)((w >> 2) & 127u); }
+__device__ __forceinline__ int i_sown(uint32_t w) { return (int)((w >> 10) & 63u); }
+__device__ __forceinline__ int i_code(uint32_t w) { return (int)((w >> 17) & 15u); }
+__device__ __forceinline__ int i_snb(uint32_t w) { return (int)((w >> 21) & 63u); }
+__device__ __forceinline__ int i_draws(uint32_t w) { return (int)((w >> 27) & 7u); }
+// the neighbour-write part of an intent (target and sample)
+__device__ __forceinline__ uint32_t i_nbpart(uint32_t w) { return (w & kIValid) ? (w & (kINb | (1023u << 17))) : 0u; }
+__device__ __forceinline__ int nb_target(uint32_t w, int q, int W) {
+    const int c = i_code(w);
+    return q + (c / 3 - 1) * W + (c % 3 - 1);
+}
+
+__device__ __forceinline__ unsigned int ld_vol(const unsigned int* p) { return *(const volatile unsigned int*)p; }
+
+// draw k of pixel p in frame t (the counter-based generator that replaces rand())
+struct Draws {
+    uint32_t blk, v[4];
+};
+__device__ __forceinline__ uint32_t draw(const LobDev& D, uint32_t p, uint32_t k, Draws& ds) {
+    const uint32_t blk = k >> 2;
+    if (blk != ds.blk) {
+        uint32_t c[4] = {blk, p, D.frameKey, 0u};
+        philox4x32_10(c, (uint32_t)D.seed, (uint32_t)(D.seed >> 32));
+        ds.v[0] = c[0];
+        ds.v[1] = c[1];
+        ds.v[2] = c[2];
+        ds.v[3] = c[3];
+        ds.blk = blk;
+    }
+    return ds.v[k & 3u] & 0x7fffffffu;
+}
+// rand() % m for a 31-bit draw and a size_t modulus
+__device__ __forceinline__ unsigned long long mod64(uint32_t a, unsigned long long m) {
+    if (m > 0xffffffffull) return a;
+    const uint32_t m32 = (uint32_t)m;
+    if ((m32 & (m32 - 1u)) == 0u) return a & (m32 - 1u);
+    return a % m32;
+}
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : v > hi ? hi : v; }
+
+// the 16 LBSP taps of channel c at pixel index p of a dense image, packed four to a word
+template <int C>
+__device__ __forceinline__ void taps(const uint8_t* img, int W, int p, int c, uint32_t (&v)[4]) {
+    const uint8_t* base = img + (size_t)p * C + c;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        uint32_t w = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int n = 4 * j + i;
+            w |= (uint32_t)__ldg(base + (tap_dy(n) * W + tap_dx(n)) * C) << (8 * i);
+        }
+        v[j] = w;
+    }
+}
+
+// sample s of pixel p (packed word, colour byte)
+template <int C>
+__device__ __forceinline__ void load_sample(const LobDev& D, int s, int p, unsigned long long& d, uint32_t& c2) {
+    if (C == 3) d = __ldg((const unsigned long long*)D.sD + (size_t)s * D.npx + p);
+    else d = __ldg((const uint16_t*)D.sD + (size_t)s * D.npx + p);
+    c2 = __ldg(D.sC + (size_t)s * D.npx + p);
+}
+
+// one sample against the pixel (:479-494 / :522-541)
+template <int C>
+__device__ __forceinline__ bool match(const LobDev& D, const uint32_t (&vals)[C][4], const uint32_t (&curr)[C],
+                                      unsigned long long d, uint32_t c2) {
+    if (C == 1) {
+        const uint32_t bgc = c2, bgd = (uint32_t)d & 0xffffu;
+        if ((uint32_t)abs((int)curr[0] - (int)bgc) > D.colThr / 2u) return false;
+        return (uint32_t)__popc(lbsp_thr(vals[0], bgc, __ldg(D.lut + bgc)) ^ bgd) <= D.descThr;
+    } else {
+        const uint32_t descThr = D.descThr * 3u, colThr = D.colThr * 3u;
+        const uint32_t scDesc = descThr / 2u, scCol = colThr / 2u;
+        uint32_t totCol = 0, totDesc = 0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const uint32_t bgc = c == 0 ? (uint32_t)(d >> 48) & 0xffu : c == 1 ? (uint32_t)(d >> 56) & 0xffu : c2;
+            const uint32_t bgd = (uint32_t)(d >> (16 * c)) & 0xffffu;
+            const uint32_t colDist = (uint32_t)abs((int)curr[c] - (int)bgc);
+            if (colDist > scCol) return false;
+            const uint32_t descDist = (uint32_t)__popc(lbsp_thr(vals[c], bgc, __ldg(D.lut + bgc)) ^ bgd);
+            if (descDist > scDesc) return false;
+            totCol += colDist;
+            totDesc += descDist;
+        }
+        return totDesc <= descThr && totCol <= colThr;
+    }
+}
+
+// overrides of a re-evaluation: the samples that earlier neighbours write (latest writer last)
+struct LobOvr {
+    int n;
+    int s[4];
+    unsigned long long d[4];
+    uint32_t c[4];
+    unsigned long long mask;
+};
+
+// the evaluation of pixel p (x, y): ordered scan (with overrides), then the decision and the model
+// writes with their draws (:497-513 / :545-575); returns the intent word
+template <int C, bool OVR>
+__device__ uint32_t eval_px(const LobDev& D, int p, int x, int y, const uint32_t (&vals)[C][4],
+                            const uint32_t (&curr)[C], const LobOvr& ov, unsigned long long* scanned) {
+    int nGood = 0, s = 0;
+    unsigned long long dB = 0;
+    uint32_t cB = 0;
+    if (D.N > 0) load_sample<C>(D, 0, p, dB, cB);
+    while (nGood < D.nreq && s < D.N) {
+        unsigned long long d = dB;
+        uint32_t c2 = cB;
+        if (s + 1 < D.N) load_sample<C>(D, s + 1, p, dB, cB);
+        if (OVR && ((ov.mask >> s) & 1ull)) {
+            for (int k = 0; k < ov.n; ++k)
+                if (ov.s[k] == s) {
+                    d = ov.d[k];
+                    c2 = ov.c[k];
+                }
+        }
+        if (match<C>(D, vals, curr, d, c2)) ++nGood;
+        ++s;
+    }
+    *scanned += (unsigned long long)s;
+    uint32_t w = kIValid | ((uint32_t)s << 2);
+    if (nGood < D.nreq) return w | kIFG;
+    Draws ds;
+    ds.blk = 0xffffffffu;
+    uint32_t k = 0;
+    if (mod64(draw(D, (uint32_t)p, k++, ds), D.nLR) == 0ull) {
+        const uint32_t so = draw(D, (uint32_t)p, k++, ds) % (uint32_t)D.N;
+        w |= kIOwn | (so << 10);
+    }
+    if (mod64(draw(D, (uint32_t)p, k++, ds), D.nLR) == 0ull) {
+        const int r = (int)(draw(D, (uint32_t)p, k++, ds) % 8u);
+        const int nx = clampi(x + c_lob_nb3[r][0], kBorder, D.W - kBorder - 1);
+        const int ny = clampi(y + c_lob_nb3[r][1], kBorder, D.H - kBorder - 1);
+        const uint32_t sn = draw(D, (uint32_t)p, k++, ds) % (uint32_t)D.N;
+        const uint32_t code = (uint32_t)((ny - y + 1) * 3 + (nx - x + 1));
+        w |= kINb | (code << 17) | (sn << 21);
+    }
+    return w | (k << 27);
+}
+
+template <int C>
+__device__ __forceinline__ void pixel_inputs(const LobDev& D, int p, uint32_t (&vals)[C][4], uint32_t (&curr)[C]) {
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        taps<C>(D.frame, D.W, p, c, vals[c]);
+        curr[c] = __ldg(D.frame + (size_t)p * C + c);
+    }
+}
+
+// warp-aggregated count of a per-thread value into a 64-bit counter
+__device__ __forceinline__ void warp_add(unsigned long long* ctr, unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(ctr, v);
+}
+
+// list push with per-round dedupe; the lanes that push together share one counter atomic
+__device__ __forceinline__ void push(const LobDev& D, uint32_t* list, unsigned int* count, uint32_t stamp, int t) {
+    if (atomicExch(&D.stamp[t], stamp) == stamp) return;
+    const unsigned am = __activemask();
+    const int lane = threadIdx.x & 31, leader = __ffs(am) - 1;
+    unsigned int base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned int)__popc(am));
+    base = __shfl_sync(am, base, leader);
+    const unsigned int i = base + (unsigned int)__popc(am & ((1u << lane) - 1u));
+    if (i < D.listCap) list[i] = (uint32_t)t;
+    else atomicOr(&D.flags[LOB_F_ERR], 1u);
+}
+
+}  // namespace
+
+// 1. every ROI pixel against the frame-start samples
+template <int C>
+__global__ void __launch_bounds__(kThreadsL) lob_k_eval(LobDev D) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long scanned = 0;
+    if (p < D.npx) {
+        if (!D.roi[p]) {
+            D.intent[p] = 0u;
+        } else {
+            const int x = p % D.W, y = p / D.W;
+            uint32_t vals[C][4], curr[C];
+            pixel_inputs<C>(D, p, vals, curr);
+            // the sample word this pixel writes: its descriptors (:499-500 / :548-550) and colour
+            unsigned long long wd = 0;
+#pragma unroll
+            for (int c = 0; c < C; ++c)
+                wd |= (unsigned long long)lbsp_thr(vals[c], curr[c], __ldg(D.lut + curr[c])) << (16 * c);
+            if (C == 3) wd |= ((unsigned long long)curr[0] << 48) | ((unsigned long long)curr[1] << 56);
+            D.wD[p] = wd;
+            LobOvr none;
+            none.n = 0;
+            none.mask = 0;
+            D.intent[p] = eval_px<C, false>(D, p, x, y, vals, curr, none, &scanned);
+        }
+    }
+    warp_add(&D.stats[0], scanned);
+}
+
+// 2. the pixels whose scan read a sample that an earlier neighbour writes
+__global__ void __launch_bounds__(kThreadsL) lob_k_mark(LobDev D) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= D.npx) return;
+    const uint32_t w = D.intent[p];
+    if (!(w & kIValid)) return;
+    const int x = p % D.W, y = p / D.W, e = i_e(w);
+    bool dirty = false;
+    // earlier pixels within one step: the row above, then the left neighbour
+    const int q4[4] = {p - D.W - 1, p - D.W, p - D.W + 1, p - 1};
+    const bool ok4[4] = {y > 0 && x > 0, y > 0, y > 0 && x + 1 < D.W, x > 0};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (!ok4[i]) continue;
+        const uint32_t wq = D.intent[q4[i]];
+        if ((wq & kIValid) && (wq & kINb) && nb_target(wq, q4[i], D.W) == p && i_snb(wq) < e) dirty = true;
+    }
+    if (dirty) push(D, D.list0, &D.flags[LOB_F_COUNT0], D.stampBase, p);
+}
+
+// 3. one repair round: re-evaluates the pixels of list (round & 1) with the samples their earlier
+// neighbours write now, and lists the later pixels whose incoming writes changed
+template <int C>
+__global__ void __launch_bounds__(kThreadsL) lob_k_round(LobDev D, int round) {
+    if (ld_vol(&D.flags[LOB_F_CONV])) return;
+    const int cur = round & 1;
+    const unsigned int n0 = ld_vol(&D.flags[cur]);
+    const unsigned int n = n0 < D.listCap ? n0 : D.listCap;
+    const uint32_t* in = cur ? D.list1 : D.list0;
+    uint32_t* out = cur ? D.list0 : D.list1;
+    unsigned int* outCount = &D.flags[cur ^ 1];
+    const uint32_t stamp = D.stampBase + (uint32_t)round + 1u;
+    unsigned long long scanned = 0;
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int p = (int)__ldcg(in + i);
+        const int x = p % D.W, y = p / D.W;
+        LobOvr ov;
+        ov.n = 0;
+        ov.mask = 0;
+        const int q4[4] = {p - D.W - 1, p - D.W, p - D.W + 1, p - 1};
+        const bool ok4[4] = {y > 0 && x > 0, y > 0, y > 0 && x + 1 < D.W, x > 0};
+        for (int j = 0; j < 4; ++j) {
+            if (!ok4[j]) continue;
+            const uint32_t wq = ld_vol(&D.intent[q4[j]]);
+            if ((wq & kIValid) && (wq & kINb) && nb_target(wq, q4[j], D.W) == p) {
+                const int s = i_snb(wq);
+                ov.s[ov.n] = s;
+                ov.d[ov.n] = __ldcg(D.wD + q4[j]);
+                ov.c[ov.n] = __ldg(D.frame + (size_t)q4[j] * C + (C == 3 ? 2 : 0));
+                ++ov.n;
+                ov.mask |= 1ull << s;
+            }
+        }
+        uint32_t vals[C][4], curr[C];
+        pixel_inputs<C>(D, p, vals, curr);
+        const uint32_t wNew = eval_px<C, true>(D, p, x, y, vals, curr, ov, &scanned);
+        const uint32_t wOld = ld_vol(&D.intent[p]);
+        if (wNew == wOld) continue;
+        *(volatile uint32_t*)&D.intent[p] = wNew;
+        if (i_nbpart(wNew) == i_nbpart(wOld)) continue;
+        // the targets of the old and the new neighbour write that come later in raster order
+        if (wOld & kINb) {
+            const int t = nb_target(wOld, p, D.W);
+            if (t > p) push(D, out, outCount, stamp, t);
+        }
+        if (wNew & kINb) {
+            const int t = nb_target(wNew, p, D.W);
+            if (t > p) push(D, out, outCount, stamp, t);
+        }
+    }
+    warp_add(&D.stats[0], scanned);
+}
+
+// end of repair round `round`: converged when the round listed nothing; otherwise its input list
+// becomes the next round's output
+__global__ void lob_k_round_end(LobDev D, int round) {
+    if (D.flags[LOB_F_CONV]) return;
+    const int cur = round & 1;
+    const unsigned int next = D.flags[cur ^ 1];
+    D.flags[LOB_F_ROUNDS] = (unsigned int)round + 1u;
+    if (next > D.listCap) {
+        D.flags[LOB_F_ERR] |= 1u;
+        D.flags[LOB_F_CONV] = 1u;
+    } else if (next == 0u) {
+        D.flags[LOB_F_CONV] = 1u;
+    } else {
+        D.flags[cur] = 0u;
+    }
+}
+
+// 4. every pixel gathers the sample writes aimed at it, in raster order of the writers (own update
+// before neighbour update within a writer); the raw mask and the draw counters of the frame
+template <int C>
+__global__ void __launch_bounds__(kThreadsL) lob_k_commit(LobDev D) {
+    if (!ld_vol(&D.flags[LOB_F_CONV])) return;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long writes = 0;
+    if (p < D.npx) {
+        const uint32_t wp = D.intent[p];
+        const bool valid = (wp & kIValid) != 0;
+        D.rawFG[p] = (valid && (wp & kIFG)) ? 255 : 0;
+        D.kctr[p] = (uint16_t)(valid ? i_draws(wp) : 0);
+        if (valid) writes = ((wp & kIOwn) ? 1ull : 0ull) + ((wp & kINb) ? 1ull : 0ull);
+        const int x = p % D.W, y = p / D.W;
+        if (x >= kBorder && y >= kBorder && x < D.W - kBorder && y < D.H - kBorder) {
+            int ns = 0;
+            int ss[10], sq[10];
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const int q = p + dy * D.W + dx;
+                    const uint32_t wq = D.intent[q];
+                    if (!(wq & kIValid)) continue;
+                    int sv[2], nv = 0;
+                    if (q == p && (wq & kIOwn)) sv[nv++] = i_sown(wq);
+                    if ((wq & kINb) && nb_target(wq, q, D.W) == p) sv[nv++] = i_snb(wq);
+                    for (int v = 0; v < nv; ++v) {
+                        int k = 0;
+                        while (k < ns && ss[k] != sv[v]) ++k;
+                        ss[k] = sv[v];
+                        sq[k] = q;
+                        if (k == ns) ++ns;
+                    }
+                }
+            for (int k = 0; k < ns; ++k) {
+                const size_t o = (size_t)ss[k] * D.npx + p;
+                const int q = sq[k];
+                if (C == 3) ((unsigned long long*)D.sD)[o] = D.wD[q];
+                else ((uint16_t*)D.sD)[o] = (uint16_t)D.wD[q];
+                D.sC[o] = __ldg(D.frame + (size_t)q * C + (C == 3 ? 2 : 0));
+            }
+        }
+    }
+    warp_add(&D.stats[1], writes);
+}
+
+// cv::medianBlur(raw mask, k) with replicated borders: 255 where more than half of the k*k window is
+// set (:577), which becomes the last mask and the output (:578); the frame becomes the last colour
+// frame (:580)
+template <int C>
+__global__ void __launch_bounds__(kThreadsL) lob_k_median(LobDev D) {
+    if (!ld_vol(&D.flags[LOB_F_CONV])) return;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= D.npx) return;
+    const int x = p % D.W, y = p / D.W, r = D.medianK / 2;
+    int cnt = 0;
+    for (int dy = -r; dy <= r; ++dy) {
+        const uint8_t* row = D.rawFG + (size_t)clampi(y + dy, 0, D.H - 1) * D.W;
+        for (int dx = -r; dx <= r; ++dx) cnt += __ldg(row + clampi(x + dx, 0, D.W - 1)) != 0;
+    }
+    const uint8_t m = (2 * cnt > D.medianK * D.medianK) ? 255 : 0;
+    D.lastFG[p] = m;
+    D.maskOut[p] = m;
+#pragma unroll
+    for (int c = 0; c < C; ++c) D.lastColor[(size_t)p * C + c] = __ldg(D.frame + (size_t)p * C + c);
+}
+
+// initialize() (:442-457 with BackgroundSubtractionUtils.cpp:70-155, BackgroundSubtractorLBSP.cpp:21-65):
+// last colour frame = the ROI part of the frame, last descriptors of the strict interior ROI pixels
+template <int C>
+__global__ void __launch_bounds__(kThreadsL) lob_k_init(LobDev D, const uint8_t* img) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= D.npx) return;
+    const int x = p % D.W, y = p / D.W;
+    const bool in = D.roi[p] != 0;
+    const bool desc = in && x > kBorder && y > kBorder && x < D.W - kBorder && y < D.H - kBorder;
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        const uint32_t v = __ldg(img + (size_t)p * C + c);
+        D.lastColor[(size_t)p * C + c] = in ? (uint8_t)v : 0;
+        uint16_t d = 0;
+        if (desc) {
+            uint32_t t[4];
+            taps<C>(img, D.W, p, c, t);
+            d = (uint16_t)lbsp_thr(t, v, __ldg(D.lut + v));
+        }
+        D.lastDesc[(size_t)p * C + c] = d;
+    }
+    D.lastFG[p] = 0;
+    D.kctr[p] = 0;
+}
+
+// refreshModel(frac, force) (:410-440): samples [start, start+nref) of every ROI pixel (not in the last
+// foreground unless forced) from a 7x7 Gaussian position of the last colour frame, with its descriptor,
+// which also goes to the last descriptor frame (:427-433); the draws continue the frame's counters
+template <int C>
+__global__ void __launch_bounds__(kThreadsL) lob_k_refresh(LobDev D, int start, int nref, int force) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= D.npx || !D.roi[p]) return;
+    if (!force && D.lastFG[p]) return;
+    const int x0 = p % D.W, y0 = p / D.W;
+    uint32_t k = D.kctr[p];
+    Draws ds;
+    ds.blk = 0xffffffffu;
+    for (int s = start; s < start + nref; ++s) {
+        int r = 1 + (int)(draw(D, (uint32_t)p, k++, ds) % 512u);
+        int sx = 0, sy = 0;
+        for (int i = 0; i < 49; ++i) {
+            r -= c_lob_pat7[i];
+            if (r <= 0) {
+                sy = i / 7;
+                sx = i % 7;
+                break;
+            }
+        }
+        sx = clampi(sx + x0 - 3, kBorder, D.W - kBorder - 1);
+        sy = clampi(sy + y0 - 3, kBorder, D.H - kBorder - 1);
+        const int sp = sy * D.W + sx;
+        if (!force && D.lastFG[sp]) continue;
+        const int rs = s % D.N;
+        unsigned long long wd = 0;
+        uint32_t col[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            col[c] = D.lastColor[(size_t)sp * C + c];
+            uint32_t t[4];
+            taps<C>(D.lastColor, D.W, sp, c, t);
+            const uint16_t d = (uint16_t)lbsp_thr(t, col[c], __ldg(D.lut + col[c]));
+            D.lastDesc[(size_t)sp * C + c] = d;
+            wd |= (unsigned long long)d << (16 * c);
+        }
+        const size_t o = (size_t)rs * D.npx + p;
+        if (C == 3) {
+            ((unsigned long long*)D.sD)[o] = wd | ((unsigned long long)col[0] << 48) | ((unsigned long long)col[1] << 56);
+            D.sC[o] = (uint8_t)col[2];
+        } else {
+            ((uint16_t*)D.sD)[o] = (uint16_t)wd;
+            D.sC[o] = (uint8_t)col[0];
+        }
+    }
+    D.kctr[p] = (uint16_t)k;
+}
+
+// getBackgroundImage / getBackgroundDescriptorsImage (:583-620): per channel the float sum of
+// sample / N in sample order, converted with rounding and saturation
+template <int C>
+__global__ void lob_k_background(LobDev D, void* out, int descriptors) {
+    const size_t n = (size_t)D.npx * C;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int p = (int)(i / C), c = (int)(i % C);
+        float acc = 0.0f;
+        for (int s = 0; s < D.N; ++s) {
+            const size_t o = (size_t)s * D.npx + p;
+            uint32_t v;
+            if (descriptors) {
+                v = C == 3 ? (uint32_t)(((const unsigned long long*)D.sD)[o] >> (16 * c)) & 0xffffu
+                           : ((const uint16_t*)D.sD)[o];
+            } else if (C == 3 && c < 2) {
+                v = (uint32_t)(((const unsigned long long*)D.sD)[o] >> (48 + 8 * c)) & 0xffu;
+            } else {
+                v = D.sC[o];
+            }
+            acc += (float)v / (float)D.N;
+        }
+        const int r = __float2int_rn(acc);
+        if (descriptors) ((uint16_t*)out)[i] = (uint16_t)clampi(r, 0, 65535);
+        else ((uint8_t*)out)[i] = (uint8_t)clampi(r, 0, 255);
+    }
+}
+
+// the sample planes in the reference's layout ([N][H*W*C] colours or descriptors)
+template <int C>
+__global__ void lob_k_export_samples(LobDev D, void* out, int descriptors) {
+    const size_t n = (size_t)D.N * D.npx * C;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t sp = i / C;
+        const int c = (int)(i % C);
+        if (descriptors) {
+            ((uint16_t*)out)[i] = C == 3 ? (uint16_t)(((const unsigned long long*)D.sD)[sp] >> (16 * c))
+                                         : ((const uint16_t*)D.sD)[sp];
+        } else {
+            ((uint8_t*)out)[i] = (C == 3 && c < 2) ? (uint8_t)(((const unsigned long long*)D.sD)[sp] >> (48 + 8 * c))
+                                                   : D.sC[sp];
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------------------------------
+namespace {
+
+inline size_t al(size_t v) { return (v + 255) & ~(size_t)255; }
+
+inline uint8_t sat_round_u8f(float v) {
+    const float r = std::nearbyint(v);
+    return (uint8_t)(r < 0.f ? 0.f : r > 255.f ? 255.f : r);
+}
+
+#define LOB_CUDA(call, what)                                                      \
+    do {                                                                          \
+        const cudaError_t e_ = (call);                                            \
+        if (e_ != cudaSuccess) {                                                  \
+            err = std::string(what) + ": " + cudaGetErrorString(e_);              \
+            return e_ == cudaErrorMemoryAllocation ? LVBGS_OOM : LVBGS_DEVICE_ERROR; \
+        }                                                                         \
+    } while (0)
+
+inline int blocks_for(size_t n) { return (int)((n + kThreadsL - 1) / kThreadsL); }
+
+}  // namespace
+
+void lob_release(LobState& L) {
+    cudaFree(L.mem);
+    L.mem = nullptr;
+    L.bytes = 0;
+    if (L.h_flags) cudaFreeHost(L.h_flags);
+    L.h_flags = nullptr;
+}
+
+lvbgs_status lob_setup(LobState& L, const lvbgs_params& prm, int W, int H, int C, const std::vector<uint8_t>& roi,
+                       size_t orig, size_t fin, cudaStream_t st, std::string& err) {
+    cudaFree(L.mem);
+    L.mem = nullptr;
+    const size_t npx = (size_t)W * H, N = prm.bg_samples;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off += al(bytes);
+        return o;
+    };
+    const size_t oRoi = take(npx), oLastColor = take(npx * C), oLastFG = take(npx), oRawFG = take(npx),
+                 oLut = take(256), oLastDesc = take(npx * C * 2), oKctr = take(npx * 2),
+                 oSD = take(N * npx * (C == 3 ? 8 : 2)), oSC = take(N * npx), oIntent = take(npx * 4),
+                 oWD = take(npx * 8), oList0 = take(npx * 4), oList1 = take(npx * 4), oStamp = take(npx * 4),
+                 oFlags = take(LOB_F_WORDS * 4), oStats = take(16), oFrame = take(npx * C), oMask = take(npx);
+    LOB_CUDA(cudaMalloc(&L.mem, off), "model allocation");
+    if (!L.h_flags) LOB_CUDA(cudaHostAlloc((void**)&L.h_flags, LOB_F_WORDS * 4, cudaHostAllocDefault), "pinned allocation");
+    L.bytes = off;
+    LobDev& D = L.d;
+    D = LobDev{};
+    D.W = W;
+    D.H = H;
+    D.C = C;
+    D.N = (int)N;
+    D.nreq = (int)prm.required_bg_samples;
+    D.npx = (int)npx;
+    D.descThr = (unsigned int)prm.desc_dist_threshold_offset;
+    D.colThr = (unsigned int)prm.min_color_dist_threshold;
+    D.seed = prm.seed;
+    D.medianK = prm.default_median_blur_kernel_size;
+    D.listCap = (unsigned int)npx;
+    D.stampBase = 1;  // nonzero: the stamps start at 0
+    uint8_t* b = L.mem;
+    D.roi = b + oRoi;
+    D.lastColor = b + oLastColor;
+    D.lastFG = b + oLastFG;
+    D.rawFG = b + oRawFG;
+    D.lut = b + oLut;
+    D.lastDesc = (uint16_t*)(b + oLastDesc);
+    D.kctr = (uint16_t*)(b + oKctr);
+    D.sD = b + oSD;
+    D.sC = b + oSC;
+    D.intent = (uint32_t*)(b + oIntent);
+    D.wD = (unsigned long long*)(b + oWD);
+    D.list0 = (uint32_t*)(b + oList0);
+    D.list1 = (uint32_t*)(b + oList1);
+    D.stamp = (uint32_t*)(b + oStamp);
+    D.flags = (unsigned int*)(b + oFlags);
+    D.stats = (unsigned long long*)(b + oStats);
+    L.d_frame = b + oFrame;
+    L.d_mask = b + oMask;
+    L.ksent = 0;
+    L.lastRounds = 1;
+    L.frames = 0;
+    L.n_rel = fin;
+    L.orig_roi = orig;
+    // BackgroundSubtractorLBSP.cpp:30-34 / :47-48: the LBSP threshold LUT (one channel divides by 3)
+    uint8_t lut[256];
+    const float rel = prm.rel_lbsp_threshold;
+    for (int t = 0; t <= 255; ++t)
+        lut[t] = C == 1 ? sat_round_u8f(((float)t * rel + (float)prm.lbsp_threshold_offset) / 3)
+                        : sat_round_u8f((float)t * rel + (float)prm.lbsp_threshold_offset);
+    LOB_CUDA(cudaMemsetAsync(L.mem, 0, off, st), "model reset");
+    LOB_CUDA(cudaMemcpyAsync(D.roi, roi.data(), npx, cudaMemcpyHostToDevice, st), "roi upload");
+    LOB_CUDA(cudaMemcpyAsync(D.lut, lut, 256, cudaMemcpyHostToDevice, st), "lut upload");
+    return LVBGS_OK;
+}
+
+namespace {
+lvbgs_status lob_refresh_launch(LobState& L, float frac, int force, cudaStream_t st, std::string& err) {
+    LobDev& D = L.d;
+    const int N = D.N;
+    const int nref = frac < 1.0f ? (int)(frac * (float)N) : N;
+    int start = 0;
+    if (frac < 1.0f) {
+        // the frame-level draw of the start position (:416)
+        uint32_t c[4] = {L.ksent >> 2, kSentinelPx, D.frameKey, 0u};
+        philox4x32_10(c, (uint32_t)D.seed, (uint32_t)(D.seed >> 32));
+        start = (int)((c[L.ksent & 3u] & 0x7fffffffu) % (uint32_t)N);
+        ++L.ksent;
+    }
+    if (nref > 0) {
+        if (D.C == 3) lob_k_refresh<3><<<blocks_for(D.npx), kThreadsL, 0, st>>>(D, start, nref, force);
+        else lob_k_refresh<1><<<blocks_for(D.npx), kThreadsL, 0, st>>>(D, start, nref, force);
+        LOB_CUDA(cudaGetLastError(), "refresh launch");
+    }
+    return LVBGS_OK;
+}
+}  // namespace
+
+lvbgs_status lob_init_model(LobState& L, const uint8_t* dimg, cudaStream_t st, std::string& err) {
+    LobDev& D = L.d;
+    D.frameKey = 0;
+    L.ksent = 0;
+    if (D.C == 3) lob_k_init<3><<<blocks_for(D.npx), kThreadsL, 0, st>>>(D, dimg);
+    else lob_k_init<1><<<blocks_for(D.npx), kThreadsL, 0, st>>>(D, dimg);
+    LOB_CUDA(cudaGetLastError(), "init launch");
+    // refreshModel(1.0f, true) (:455)
+    lvbgs_status s = lob_refresh_launch(L, 1.0f, 1, st, err);
+    if (s != LVBGS_OK) return s;
+    LOB_CUDA(cudaStreamSynchronize(st), "initialization");
+    return LVBGS_OK;
+}
+
+lvbgs_status lob_refresh(LobState& L, float frac, int force, cudaStream_t st, std::string& err) {
+    lvbgs_status s = lob_refresh_launch(L, frac, force, st, err);
+    if (s != LVBGS_OK) return s;
+    LOB_CUDA(cudaStreamSynchronize(st), "refresh");
+    return LVBGS_OK;
+}
+
+lvbgs_status lob_apply(LobState& L, const uint8_t* dimg, uint8_t* dmask, uint8_t* hostMask, double lr,
+                       cudaStream_t st, std::string& err) {
+    LobDev& D = L.d;
+    D.frame = dimg;
+    D.maskOut = dmask;
+    D.nLR = std::isinf(lr) ? ~0ull : (unsigned long long)std::ceil(lr);  // :470
+    ++L.frames;
+    D.frameKey = (uint32_t)L.frames;
+    L.ksent = 0;
+    const int C = D.C, nb = blocks_for(D.npx);
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int roundBlocks = 2 * (sms > 0 ? sms : 1);
+    LOB_CUDA(cudaMemsetAsync(D.flags, 0, LOB_F_WORDS * 4, st), "flag reset");
+    if (C == 3) lob_k_eval<3><<<nb, kThreadsL, 0, st>>>(D);
+    else lob_k_eval<1><<<nb, kThreadsL, 0, st>>>(D);
+    lob_k_mark<<<nb, kThreadsL, 0, st>>>(D);
+    LOB_CUDA(cudaGetLastError(), "evaluation launch");
+    int round = 0, chunk = L.lastRounds + 1;
+    for (;;) {
+        for (int i = 0; i < chunk; ++i, ++round) {
+            if (C == 3) lob_k_round<3><<<roundBlocks, kThreadsL, 0, st>>>(D, round);
+            else lob_k_round<1><<<roundBlocks, kThreadsL, 0, st>>>(D, round);
+            lob_k_round_end<<<1, 1, 0, st>>>(D, round);
+        }
+        if (C == 3) {
+            lob_k_commit<3><<<nb, kThreadsL, 0, st>>>(D);
+            lob_k_median<3><<<nb, kThreadsL, 0, st>>>(D);
+        } else {
+            lob_k_commit<1><<<nb, kThreadsL, 0, st>>>(D);
+            lob_k_median<1><<<nb, kThreadsL, 0, st>>>(D);
+        }
+        LOB_CUDA(cudaGetLastError(), "repair launch");
+        if (hostMask) LOB_CUDA(cudaMemcpyAsync(hostMask, dmask, (size_t)D.npx, cudaMemcpyDeviceToHost, st), "mask download");
+        LOB_CUDA(cudaMemcpyAsync(L.h_flags, D.flags, LOB_F_WORDS * 4, cudaMemcpyDeviceToHost, st), "flag read-back");
+        LOB_CUDA(cudaStreamSynchronize(st), "frame step");
+        if (L.h_flags[LOB_F_ERR]) {
+            err = "LOBSTER repair list overflow";
+            return LVBGS_DEVICE_ERROR;
+        }
+        if (L.h_flags[LOB_F_CONV]) break;
+        if (round >= kMaxRoundsL) {
+            err = "LOBSTER raster-order repair did not converge";
+            return LVBGS_DEVICE_ERROR;
+        }
+        chunk *= 2;
+    }
+    L.lastRounds = (int)L.h_flags[LOB_F_ROUNDS];
+    D.stampBase += (uint32_t)round + 2u;
+    return LVBGS_OK;
+}
+
+lvbgs_status lob_background(LobState& L, void* hostOut, bool descriptors, cudaStream_t st, std::string& err) {
+    LobDev& D = L.d;
+    const size_t n = (size_t)D.npx * D.C * (descriptors ? 2 : 1);
+    void* tmp = nullptr;
+    LOB_CUDA(cudaMallocAsync(&tmp, n, st), "staging allocation");
+    if (D.C == 3) lob_k_background<3><<<1024, 256, 0, st>>>(D, tmp, descriptors ? 1 : 0);
+    else lob_k_background<1><<<1024, 256, 0, st>>>(D, tmp, descriptors ? 1 : 0);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hostOut, tmp, n, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(tmp, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    LOB_CUDA(e, "background image");
+    return LVBGS_OK;
+}
+
+size_t lob_map_bytes(const LobState& L, int which) {
+    const size_t npx = (size_t)L.d.npx, C = (size_t)L.d.C, N = (size_t)L.d.N;
+    switch (which) {
+        case LVBGS_MAP_LAST_FG:
+        case LVBGS_MAP_ROI: return npx;
+        case LVBGS_MAP_LAST_COLOR: return npx * C;
+        case LVBGS_MAP_LAST_DESC: return npx * C * 2;
+        case LVBGS_MAP_SAMPLE_COLOR: return N * npx * C;
+        case LVBGS_MAP_SAMPLE_DESC: return N * npx * C * 2;
+        case LVBGS_MAP_LUT: return 256;
+        default: return 0;
+    }
+}
+
+lvbgs_status lob_get_map(LobState& L, int which, void* hostOut, size_t bytes, cudaStream_t st, std::string& err) {
+    LobDev& D = L.d;
+    const size_t need = lob_map_bytes(L, which);
+    if (need == 0) {
+        err = "map not kept by LOBSTER";
+        return LVBGS_BAD_ARG;
+    }
+    if (bytes < need) {
+        err = "output buffer too small";
+        return LVBGS_BAD_ARG;
+    }
+    const void* src = nullptr;
+    switch (which) {
+        case LVBGS_MAP_LAST_FG: src = D.lastFG; break;
+        case LVBGS_MAP_ROI: src = D.roi; break;
+        case LVBGS_MAP_LAST_COLOR: src = D.lastColor; break;
+        case LVBGS_MAP_LAST_DESC: src = D.lastDesc; break;
+        case LVBGS_MAP_LUT: src = D.lut; break;
+        default: break;
+    }
+    if (src) {
+        LOB_CUDA(cudaMemcpyAsync(hostOut, src, need, cudaMemcpyDeviceToHost, st), "map download");
+        LOB_CUDA(cudaStreamSynchronize(st), "map download");
+        return LVBGS_OK;
+    }
+    void* tmp = nullptr;
+    LOB_CUDA(cudaMallocAsync(&tmp, need, st), "staging allocation");
+    const int desc = which == LVBGS_MAP_SAMPLE_DESC ? 1 : 0;
+    if (D.C == 3) lob_k_export_samples<3><<<1024, 256, 0, st>>>(D, tmp, desc);
+    else lob_k_export_samples<1><<<1024, 256, 0, st>>>(D, tmp, desc);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hostOut, tmp, need, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(tmp, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    LOB_CUDA(e, "sample export");
+    return LVBGS_OK;
+}
+
+lvbgs_status lob_stats(LobState& L, unsigned long long out[2], cudaStream_t st, std::string& err) {
+    LOB_CUDA(cudaMemcpyAsync(out, L.d.stats, 16, cudaMemcpyDeviceToHost, st), "statistics download");
+    LOB_CUDA(cudaStreamSynchronize(st), "statistics download");
+    return LVBGS_OK;
+}
+
+}  // namespace lvbgs

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/lvbgs.h"
+#include "lobster_internal.h"
 #include "lvbgs_internal.h"
 #include "pawcs_internal.h"
 
@@ -191,6 +192,7 @@ struct lvbgs_ctx {
     unsigned long long pw_offset = 1000;
     int pw_rounds_last = 0;
     int dbg_fault = 0;  // one-shot fault injection of the next frame step (lvbgs_debug_inject_fault)
+    LobState* lob = nullptr;  // LOBSTER (algo == LVBGS_ALGO_LOBSTER): the stream's device state
 };
 
 namespace {
@@ -848,6 +850,36 @@ lvbgs_status pw_initialize(lvbgs_ctx* h, const uint8_t* img, int W, int H, int C
     return LVBGS_OK;
 }
 
+// LOBSTER initialize() (BackgroundSubtractorLOBSTER.cpp:442-457) on the validated ROI
+lvbgs_status lob_initialize(lvbgs_ctx* h, const uint8_t* img, int W, int H, int C, size_t stride,
+                            const std::vector<uint8_t>& newroi, size_t orig, size_t fin) {
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaFree(h->dmem);
+    h->dmem = nullptr;
+    h->initialized = false;
+    h->spilled = false;
+    std::string err;
+    lvbgs_status s = lob_setup(*h->lob, h->prm, W, H, C, newroi, orig, fin, h->stream, err);
+    if (s != LVBGS_OK) return fail(h, s, err);
+    h->W = W;
+    h->H = H;
+    h->C = C;
+    h->npx = (size_t)W * H;
+    h->roi = newroi;
+    h->roiW = W;
+    h->roiH = H;
+    h->n_rel = fin;
+    h->orig_roi = orig;
+    h->d_frame = h->lob->d_frame;
+    h->d_mask = h->lob->d_mask;
+    h->persistBytes = h->totalBytes = h->lob->bytes;
+    const uint8_t* dimg = nullptr;
+    if ((s = stage_frame(h, img, stride, h->stream, &dimg)) != LVBGS_OK) return s;
+    if ((s = lob_init_model(*h->lob, dimg, h->stream, err)) != LVBGS_OK) return fail(h, s, err);
+    h->initialized = true;
+    return LVBGS_OK;
+}
+
 // one PAWCS frame step: local passes to the raster-order fixed point, then commit, global words,
 // post-processing and the frame level
 lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* mask, double lr, cudaStream_t st) {
@@ -1025,6 +1057,21 @@ lvbgs_status lvbgs_default_params(lvbgs_algo algo, lvbgs_params* out) {
         out->device_id = 0;
         return LVBGS_OK;
     }
+    if (algo == LVBGS_ALGO_LOBSTER) {
+        // BackgroundSubtractorLOBSTER.hpp:22-31 (desc_dist_threshold_offset carries nDescDistThreshold,
+        // min_color_dist_threshold nColorDistThreshold), BackgroundSubtractorLBSP.hpp:23-28
+        out->desc_dist_threshold_offset = 4;
+        out->min_color_dist_threshold = 30;
+        out->bg_samples = 35;
+        out->required_bg_samples = 2;
+        out->samples_for_moving_avgs = 100;
+        out->rel_lbsp_threshold = 0.333f;
+        out->lbsp_threshold_offset = 0;
+        out->default_median_blur_kernel_size = 9;
+        out->seed = 0;
+        out->device_id = 0;
+        return LVBGS_OK;
+    }
     if (algo != LVBGS_ALGO_SUBSENSE) return fail(nullptr, LVBGS_BAD_ARG, "unknown algorithm");
     out->desc_dist_threshold_offset = 3;
     out->min_color_dist_threshold = 30;
@@ -1042,7 +1089,8 @@ lvbgs_status lvbgs_default_params(lvbgs_algo algo, lvbgs_params* out) {
 lvbgs_status lvbgs_create(lvbgs_algo algo, const lvbgs_params* p, lvbgs_handle* out) {
     if (!out) return fail(nullptr, LVBGS_BAD_ARG, "null output handle");
     *out = nullptr;
-    if (algo != LVBGS_ALGO_SUBSENSE && algo != LVBGS_ALGO_PAWCS) return fail(nullptr, LVBGS_BAD_ARG, "unknown algorithm");
+    if (algo != LVBGS_ALGO_SUBSENSE && algo != LVBGS_ALGO_PAWCS && algo != LVBGS_ALGO_LOBSTER)
+        return fail(nullptr, LVBGS_BAD_ARG, "unknown algorithm");
     lvbgs_params prm;
     if (p) prm = *p;
     else lvbgs_default_params(algo, &prm);
@@ -1096,6 +1144,7 @@ lvbgs_status lvbgs_create(lvbgs_algo algo, const lvbgs_params* p, lvbgs_handle* 
     }
     lvbgs_ctx* h = new lvbgs_ctx();
     h->algo = algo;
+    if (algo == LVBGS_ALGO_LOBSTER) h->lob = new LobState();
     h->prm = prm;
     h->device = prm.device_id;
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -1123,6 +1172,10 @@ lvbgs_status lvbgs_destroy(lvbgs_handle h) {
     }
     if (h->evFork) cudaEventDestroy(h->evFork);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->lob) {
+        lob_release(*h->lob);
+        delete h->lob;
+    }
     delete h;
     return LVBGS_OK;
 }
@@ -1166,6 +1219,7 @@ lvbgs_status lvbgs_initialize(lvbgs_handle h, const uint8_t* img, int W, int H, 
     if (fin == 0)
         return fail(h, LVBGS_BAD_ARG, "provided ROI mat contains no useful pixels away from borders (descriptors will hit image bounds)");
     if (h->algo == LVBGS_ALGO_PAWCS) return pw_initialize(h, img, W, H, C, stride, newroi, orig, fin);
+    if (h->algo == LVBGS_ALGO_LOBSTER) return lob_initialize(h, img, W, H, C, stride, newroi, orig, fin);
     // resolution-dependent parameters (BackgroundSubtractorSuBSENSE.cpp:112-128)
     StreamCtl ctl;
     std::memset(&ctl, 0, sizeof(ctl));
@@ -1241,6 +1295,16 @@ lvbgs_status lvbgs_apply(lvbgs_handle h, const uint8_t* img, size_t stride, uint
     if (!img) return fail(h, LVBGS_BAD_ARG, "null input image");
     cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : h->stream;
     if (h->algo == LVBGS_ALGO_PAWCS) return pw_apply(h, img, stride, mask, lr, st);
+    if (h->algo == LVBGS_ALGO_LOBSTER) {
+        // BackgroundSubtractorLOBSTER.cpp:463: the rate is reinterpreted as an integer and must be positive
+        if (!(lr > 0)) return fail(h, LVBGS_BAD_ARG, "learning rate must be a positive value; faster learning is achieved with smaller values");
+        const uint8_t* dimg = nullptr;
+        if ((s = stage_frame(h, img, stride, st, &dimg)) != LVBGS_OK) return s;
+        const bool devMask = mask && is_device_ptr(mask);
+        std::string err;
+        s = lob_apply(*h->lob, dimg, devMask ? mask : h->d_mask, (mask && !devMask) ? mask : nullptr, lr, st, err);
+        return s == LVBGS_OK ? s : fail(h, s, err);
+    }
     const uint8_t* dimg = nullptr;
     if ((s = stage_frame(h, img, stride, st, &dimg)) != LVBGS_OK) return s;
     const bool devMask = mask && is_device_ptr(mask);
@@ -1551,6 +1615,11 @@ lvbgs_status lvbgs_get_background(lvbgs_handle h, uint8_t* out) {
     lvbgs_status s = check_ready(h);
     if (s != LVBGS_OK) return s;
     if (!out) return fail(h, LVBGS_BAD_ARG, "null output");
+    if (h->algo == LVBGS_ALGO_LOBSTER) {
+        std::string err;
+        s = lob_background(*h->lob, out, false, h->stream, err);
+        return s == LVBGS_OK ? s : fail(h, s, err);
+    }
     if (h->algo == LVBGS_ALGO_PAWCS) {
         const bool dev = is_device_ptr(out);
         uint8_t* d = dev ? out : h->d_frame;
@@ -1574,6 +1643,11 @@ lvbgs_status lvbgs_get_background_descriptors(lvbgs_handle h, uint16_t* out) {
     lvbgs_status s = check_ready(h);
     if (s != LVBGS_OK) return s;
     if (!out) return fail(h, LVBGS_BAD_ARG, "null output");
+    if (h->algo == LVBGS_ALGO_LOBSTER) {
+        std::string err;
+        s = lob_background(*h->lob, out, true, h->stream, err);
+        return s == LVBGS_OK ? s : fail(h, s, err);
+    }
     uint16_t* d = nullptr;
     LV_CUDA(h, cudaMallocAsync((void**)&d, h->npx * h->C * 2, h->stream), "temporary allocation");
     if (h->algo == LVBGS_ALGO_PAWCS && h->C == 3)
@@ -1595,6 +1669,11 @@ lvbgs_status lvbgs_refresh_model(lvbgs_handle h, float frac, int force) {
     if (h->algo == LVBGS_ALGO_PAWCS)
         return fail(h, LVBGS_BAD_ARG, "PAWCS's refreshModel takes (base occurrences, decrement fraction, force): use lvbgs_pawcs_refresh_model");
     if (!(frac > 0.0f && frac <= 1.0f)) return fail(h, LVBGS_BAD_ARG, "model refresh must be given as a non-null fraction");
+    if (h->algo == LVBGS_ALGO_LOBSTER) {
+        std::string err;
+        s = lob_refresh(*h->lob, frac, force ? 1 : 0, h->stream, err);
+        return s == LVBGS_OK ? s : fail(h, s, err);
+    }
     StreamCtl ctl;
     LV_CUDA(h, cudaMemcpy(&ctl, h->sd.ctl, sizeof(ctl), cudaMemcpyDeviceToHost), "control read");
     const size_t N = h->prm.bg_samples;
@@ -1619,11 +1698,15 @@ lvbgs_status lvbgs_set_automatic_model_reset(lvbgs_handle h, int enabled) {
     lvbgs_status s = check_ready(h);
     if (s != LVBGS_OK) return s;
     const int v = enabled ? 1 : 0;
+    // LOBSTER keeps the flag of its base class but has no automatic model reset
+    if (h->algo == LVBGS_ALGO_LOBSTER) return LVBGS_OK;
     LV_CUDA(h, cudaMemcpy(&h->sd.ctl->auto_reset, &v, sizeof(v), cudaMemcpyHostToDevice), "control write");
     return LVBGS_OK;
 }
 
-double lvbgs_get_default_learning_rate(lvbgs_handle) { return 0.0; }
+// getDefaultLearningRate(): LOBSTER's BGSLOBSTER_DEFAULT_LEARNING_RATE (BackgroundSubtractorLOBSTER.hpp:31,57);
+// 0 (the internal T(x)) for the others
+double lvbgs_get_default_learning_rate(lvbgs_handle h) { return h && h->algo == LVBGS_ALGO_LOBSTER ? 16.0 : 0.0; }
 
 lvbgs_status lvbgs_set_roi(lvbgs_handle h, const uint8_t* roi, int width, int height) {
     if (!h || !roi || width <= 0 || height <= 0) return fail(h, LVBGS_BAD_ARG, "null or empty ROI");
@@ -1700,6 +1783,7 @@ size_t lvbgs_device_bytes(lvbgs_algo algo, int W, int H, int C, size_t N) {
 lvbgs_status lvbgs_spill(lvbgs_handle h, void* host, size_t bytes) {
     lvbgs_status s = check_ready(h);
     if (s != LVBGS_OK) return s;
+    if (h->algo == LVBGS_ALGO_LOBSTER) return fail(h, LVBGS_UNSUPPORTED, "spilling is implemented for SuBSENSE and PAWCS streams");
     if (!host || bytes < h->persistBytes) return fail(h, LVBGS_BAD_ARG, "spill buffer is smaller than lvbgs_state_bytes()");
     LV_CUDA(h, cudaStreamSynchronize(h->stream), "spill");
     LV_CUDA(h, cudaMemcpy(host, h->dmem, h->persistBytes, cudaMemcpyDeviceToHost), "spill copy");
@@ -1781,6 +1865,10 @@ const char* lvbgs_last_error(lvbgs_handle h) {
 lvbgs_status lvbgs_debug_map_bytes(lvbgs_handle h, int which, size_t* bytes) {
     if (!h || !bytes) return fail(h, LVBGS_BAD_ARG, "null argument");
     if (!h->initialized) return fail(h, LVBGS_NOT_INITIALIZED, "algo must be initialized first");
+    if (h->algo == LVBGS_ALGO_LOBSTER) {
+        *bytes = lob_map_bytes(*h->lob, which);
+        return *bytes ? LVBGS_OK : fail(h, LVBGS_BAD_ARG, "map not kept by LOBSTER");
+    }
     const size_t npx = h->npx, C = (size_t)h->C, N = h->prm.bg_samples;
     const size_t nds = (size_t)h->sd.dsW * h->sd.dsH * C;
     if (which >= LVBGS_MAP_R && which <= LVBGS_MAP_FIN_ST) *bytes = npx * 4;
@@ -1801,6 +1889,11 @@ lvbgs_status lvbgs_debug_get_map(lvbgs_handle h, int which, void* out, size_t by
     size_t need = 0;
     if ((s = lvbgs_debug_map_bytes(h, which, &need)) != LVBGS_OK) return s;
     if (!out || bytes < need) return fail(h, LVBGS_BAD_ARG, "output buffer too small");
+    if (h->algo == LVBGS_ALGO_LOBSTER) {
+        std::string err;
+        s = lob_get_map(*h->lob, which, out, bytes, h->stream, err);
+        return s == LVBGS_OK ? s : fail(h, s, err);
+    }
     LV_CUDA(h, cudaStreamSynchronize(h->stream), "sync");
     StreamCtl ctl;
     LV_CUDA(h, cudaMemcpy(&ctl, h->sd.ctl, sizeof(ctl), cudaMemcpyDeviceToHost), "control read");
@@ -1902,6 +1995,21 @@ lvbgs_status lvbgs_get_scalars(lvbgs_handle h, lvbgs_scalars* out) {
     lvbgs_status s = check_ready(h);
     if (s != LVBGS_OK) return s;
     if (!out) return fail(h, LVBGS_BAD_ARG, "null output");
+    if (h->algo == LVBGS_ALGO_LOBSTER) {
+        // LOBSTER keeps no frame-level state; frame_idx counts its apply() calls
+        std::memset(out, 0, sizeof(*out));
+        unsigned long long st[2] = {0, 0};
+        std::string err;
+        s = lob_stats(*h->lob, st, h->stream, err);
+        if (s != LVBGS_OK) return fail(h, s, err);
+        out->frame_idx = h->lob->frames;
+        out->median_blur_kernel_size = h->prm.default_median_blur_kernel_size;
+        out->n_relevant_px = h->lob->n_rel;
+        out->orig_roi_px = h->lob->orig_roi;
+        out->stat_samples_evaluated = st[0];
+        out->stat_sample_writes = st[1];
+        return LVBGS_OK;
+    }
     LV_CUDA(h, cudaStreamSynchronize(h->stream), "sync");
     StreamCtl c;
     LV_CUDA(h, cudaMemcpy(&c, h->sd.ctl, sizeof(c), cudaMemcpyDeviceToHost), "control read");

@@ -554,6 +554,8 @@ int rlob_get_background_descriptors(void* h, uint16_t* out) {
 int rlob_set_roi(void* h, const uint8_t* roi, int W, int H) {
     RefLob* o = (RefLob*)h;
     cv::Mat r = roi_mat(roi, W, H);
+    // setROI re-initializes from the background image when initialized: frame 0 again
+    o->frames = 0;
     o->rng.start_frame((size_t)W * H);
     return guarded(o->rng, [&] { o->setROI(r); });
 }

@@ -42,6 +42,11 @@ def test_default_params_match_reference(product_lib):
     assert product_lib.lvbgs_default_params(L.ALGO_PAWCS, C.byref(p)) == L.OK
     assert (p.desc_dist_threshold_offset, p.min_color_dist_threshold, p.bg_samples, p.samples_for_moving_avgs,
             p.default_median_blur_kernel_size) == (2, 20, 50, 100, 9)
+    # BackgroundSubtractorLOBSTER.hpp:22-31: descriptor 4, colour 30, 35 samples, 2 required
+    assert product_lib.lvbgs_default_params(L.ALGO_LOBSTER, C.byref(p)) == L.OK
+    assert (p.desc_dist_threshold_offset, p.min_color_dist_threshold, p.bg_samples, p.required_bg_samples,
+            p.lbsp_threshold_offset, p.default_median_blur_kernel_size) == (4, 30, 35, 2, 0, 9)
+    assert abs(p.rel_lbsp_threshold - 0.333) < 1e-7
     assert product_lib.lvbgs_default_params(7, C.byref(p)) == L.BAD_ARG
 
 
