@@ -390,6 +390,8 @@ def main():
                     help="PAWCS legs: the single-channel scene (config 2), the BGR scene, or both")
     ap.add_argument("--pawcs-only", action="store_true",
                     help="run the PAWCS workload alone and print its object (profiling)")
+    ap.add_argument("--lobster-only", action="store_true",
+                    help="run the LOBSTER legs alone and print their object (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -404,6 +406,17 @@ def main():
         if args.pawcs_channels != "1":
             out["bgr"] = pawcs_run(min(args.pawcs_frames, 100), stream, cpu=not args.no_cpu_baseline, channels=3)
         print(json.dumps(out))
+        return
+
+    if args.lobster_only:
+        import torch
+        torch.cuda.set_device(0)
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        print(json.dumps({"config0": lobster_run(0, args.lobster_frames, stream, cpu=not args.no_cpu_baseline,
+                                                 cpu_frames=10),
+                          "config1": lobster_run(1, args.lobster_frames, stream, cpu=not args.no_cpu_baseline,
+                                                 cpu_frames=2)}))
         return
 
     import numpy as np

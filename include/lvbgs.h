@@ -39,7 +39,7 @@ typedef enum {
     LVBGS_BUSY = 9             /* serving: a queue or capacity limit refused the request (retry later) */
 } lvbgs_status;
 
-typedef enum { LVBGS_ALGO_SUBSENSE = 0, LVBGS_ALGO_PAWCS = 1, LVBGS_ALGO_LOBSTER = 2 } lvbgs_algo;
+typedef enum { LVBGS_ALGO_SUBSENSE = 0, LVBGS_ALGO_PAWCS = 1, LVBGS_ALGO_LOBSTER = 2, LVBGS_ALGO_VIBE = 3 } lvbgs_algo;
 
 typedef struct lvbgs_ctx* lvbgs_handle;
 
@@ -354,6 +354,18 @@ size_t lvbgs_precache_copy_loader(void* user, size_t idx, uint8_t* dst, size_t c
  * SuBSENSE; batched steps and spilling are SuBSENSE/PAWCS-only. LOBSTER keeps no frame counter of its own,
  * so draw k of pixel p in the i-th apply() is keyed by frame i (initialize() and refreshes before the first
  * apply() are frame 0). */
+
+/* ---- ViBe (BackgroundSubtractorViBe, modules/video/src/BackgroundSubtractorViBe.cpp) ----
+ * A handle created with LVBGS_ALGO_VIBE runs BackgroundSubtractorViBe_1ch on single-channel frames
+ * (:57-103) and BackgroundSubtractorViBe_3ch on three-channel frames (:112-191), with the header's
+ * configuration (L2 colour distance, no single-channel validation, BackgroundSubtractorViBe.hpp:47-52).
+ * lvbgs_params: min_color_dist_threshold carries nColorDistThreshold (20), bg_samples (20, at most 64),
+ * required_bg_samples (2); the others are unused. lvbgs_initialize takes no ROI (ViBe has none; a
+ * non-null roi is LVBGS_UNSUPPORTED); lvbgs_apply's learning_rate must be positive (default 16);
+ * get_background, get_size, get_scalars and the maps LVBGS_MAP_SAMPLE_COLOR and _ROI work as above;
+ * refresh_model, set_roi, background descriptors, batched steps and spilling are LVBGS_UNSUPPORTED.
+ * Draws are keyed like LOBSTER's (frame i = the i-th apply(); initialize() draws sample s of pixel p
+ * as draw s of p in frame 0). */
 
 #ifdef __cplusplus
 }

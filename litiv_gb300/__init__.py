@@ -1,11 +1,11 @@
-"""GB300 (sm_103a) SuBSENSE, PAWCS and LOBSTER background subtraction with LITIV's interface.
+"""GB300 (sm_103a) SuBSENSE, PAWCS, LOBSTER and ViBe background subtraction with LITIV's interface.
 
 The compute path is the in-tree CUDA library ``_build/liblvbgs.so`` (C-ABI in include/lvbgs.h);
 this package is its host-side mirror of the reference's BackgroundSubtractorSuBSENSE,
-BackgroundSubtractorPAWCS and BackgroundSubtractorLOBSTER interfaces.
+BackgroundSubtractorPAWCS, BackgroundSubtractorLOBSTER and BackgroundSubtractorViBe interfaces.
 """
 from .bgs import (BackgroundSubtractorLOBSTER, BackgroundSubtractorPAWCS, BackgroundSubtractorSuBSENSE,  # noqa: F401
-                  LvException, batch_apply, lbsp_compute2)
+                  BackgroundSubtractorViBe, LvException, batch_apply, lbsp_compute2)
 from .precache import DataPrecacher, DevicePacket  # noqa: F401
 from .synth import SyntheticStream  # noqa: F401
 from . import _lib  # noqa: F401

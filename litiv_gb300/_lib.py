@@ -16,7 +16,7 @@ LIB_PATH = os.environ.get("LVBGS_LIB") or os.path.join(HERE, "_build", "liblvbgs
 OK, BAD_ARG, BAD_SIZE, BAD_TYPE, NOT_INITIALIZED, OOM, DEVICE_TIMEOUT, DEVICE_ERROR, UNSUPPORTED, BUSY = range(10)
 STATUS_NAMES = ["OK", "BAD_ARG", "BAD_SIZE", "BAD_TYPE", "NOT_INITIALIZED", "OOM", "DEVICE_TIMEOUT",
                 "DEVICE_ERROR", "UNSUPPORTED", "BUSY"]
-ALGO_SUBSENSE, ALGO_PAWCS, ALGO_LOBSTER = 0, 1, 2
+ALGO_SUBSENSE, ALGO_PAWCS, ALGO_LOBSTER, ALGO_VIBE = 0, 1, 2, 3
 
 # map ids (LVBGS_MAP_*)
 MAP_NAMES = ["R", "V", "T", "DLAST", "DMIN_LT", "DMIN_ST", "RAW_LT", "RAW_ST", "FIN_LT", "FIN_ST",

@@ -348,6 +348,56 @@ class BackgroundSubtractorLOBSTER:
         return BackgroundSubtractorSuBSENSE.apply(self, image, fgmask, learningRate, stream)
 
 
+class BackgroundSubtractorViBe:
+    """ViBe on the GPU: BackgroundSubtractorViBe_1ch on single-channel frames and _3ch on three-channel
+    frames (modules/video/src/BackgroundSubtractorViBe.cpp, BackgroundSubtractorViBe.hpp:54-112 for the
+    interface and defaults). initialize() takes no ROI; apply()'s learning rate must be positive."""
+
+    def __init__(self, nColorDistThreshold=20, nBGSamples=20, nRequiredBGSamples=2, seed=0, device_id=0):
+        lib = L.lib()
+        p = L.LvbgsParams()
+        _check(lib.lvbgs_default_params(L.ALGO_VIBE, C.byref(p)))
+        p.min_color_dist_threshold = nColorDistThreshold
+        p.bg_samples = nBGSamples
+        p.required_bg_samples = nRequiredBGSamples
+        p.seed = seed
+        p.device_id = device_id
+        self.params = p
+        h = C.c_void_p()
+        _check(lib.lvbgs_create(L.ALGO_VIBE, C.byref(p), C.byref(h)))
+        self._h = h
+        self._shape = None
+
+    def close(self):
+        if self._h:
+            L.lib().lvbgs_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    getBackgroundImage = BackgroundSubtractorSuBSENSE.getBackgroundImage
+    getDefaultLearningRate = BackgroundSubtractorSuBSENSE.getDefaultLearningRate
+    state_map = BackgroundSubtractorSuBSENSE.state_map
+    scalars = BackgroundSubtractorSuBSENSE.scalars
+    _need_init = BackgroundSubtractorSuBSENSE._need_init
+
+    def initialize(self, oInitImg):
+        """initialize(oInitImg) (BackgroundSubtractorViBe.cpp:57-75 / :112-134)"""
+        BackgroundSubtractorSuBSENSE.initialize(self, oInitImg, None)
+
+    def apply(self, image, fgmask=None, learningRate=16.0, stream=None):
+        """apply(image, fgmask, learningRate=16) (:77-103 / :136-191)"""
+        return BackgroundSubtractorSuBSENSE.apply(self, image, fgmask, learningRate, stream)
+
+
 def map_view(name, raw, W, H, Cc, N):
     """Interprets raw map bytes (reference layout) as a typed numpy array."""
     if name in ("R", "V", "T", "DLAST", "DMIN_LT", "DMIN_ST", "RAW_LT", "RAW_ST", "FIN_LT", "FIN_ST"):

@@ -1,4 +1,8 @@
-// LOBSTER frame step for sm_103a (BackgroundSubtractorLOBSTER.cpp:459-581, the non-parallel path).
+// LOBSTER and ViBe frame steps for sm_103a (BackgroundSubtractorLOBSTER.cpp:459-581, the non-parallel
+// path; BackgroundSubtractorViBe.cpp:77-191). The kernels are written for LOBSTER and take the algorithm
+// as a template parameter: ViBe evaluates every pixel (no ROI), matches colours only, keeps plain colour
+// samples and outputs its raw mask, and its neighbour positions are clamped to the frame instead of the
+// LBSP border; the scheme below is the same.
 //
 // The reference scans the ROI pixels in raster order. A pixel reads its own samples, which an earlier
 // pixel's neighbour update may have overwritten in the same frame (:510-512 / :569-574); nothing else
@@ -110,18 +114,42 @@ __device__ __forceinline__ void taps(const uint8_t* img, int W, int p, int c, ui
     }
 }
 
-// sample s of pixel p (packed word, colour byte)
-template <int C>
+// sample s of pixel p: LOBSTER, the packed word and the colour byte; ViBe, the colour bytes packed into d
+template <int C, int ALG>
 __device__ __forceinline__ void load_sample(const LobDev& D, int s, int p, unsigned long long& d, uint32_t& c2) {
+    if (ALG == ALG_VIBE) {
+        const uint8_t* b = D.sC + ((size_t)s * D.npx + p) * C;
+        d = C == 3 ? ((unsigned long long)__ldg(b) | ((unsigned long long)__ldg(b + 1) << 8) |
+                      ((unsigned long long)__ldg(b + 2) << 16))
+                   : (unsigned long long)__ldg(b);
+        c2 = 0;
+        return;
+    }
     if (C == 3) d = __ldg((const unsigned long long*)D.sD + (size_t)s * D.npx + p);
     else d = __ldg((const uint16_t*)D.sD + (size_t)s * D.npx + p);
     c2 = __ldg(D.sC + (size_t)s * D.npx + p);
 }
 
-// one sample against the pixel (:479-494 / :522-541)
-template <int C>
+// one sample against the pixel: LOBSTER (:479-494 / :522-541); ViBe (BackgroundSubtractorViBe.cpp:87 /
+// :165-170): |in - bg| < R on one channel; on three, lv::L2dist<3>(uchar*, uchar*) < 3R, whose squared
+// differences add up in uint16_t (utils/math.hpp:391-396), so the sum s wraps modulo 65536 before the
+// square root. For integers s < 65536 and T = 3R, (float)sqrt(s) < (float)T is exactly s < T*T when
+// T < 256 (sqrt(T*T - 1) < T - 1/(2T), and 1/(2T) is far above the float spacing near T), and always true
+// when T >= 256
+template <int C, int ALG>
 __device__ __forceinline__ bool match(const LobDev& D, const uint32_t (&vals)[C][4], const uint32_t (&curr)[C],
                                       unsigned long long d, uint32_t c2) {
+    if (ALG == ALG_VIBE) {
+        if (C == 1) return (uint32_t)abs((int)curr[0] - (int)(d & 0xffu)) < D.colThr;
+        uint32_t acc = 0;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const int dv = (int)curr[c] - (int)((d >> (8 * c)) & 0xffu);
+            acc += (uint32_t)(dv * dv);
+        }
+        const unsigned long long T = 3ull * D.colThr;
+        return T >= 256ull || (unsigned long long)(acc & 0xffffu) < T * T;
+    }
     if (C == 1) {
         const uint32_t bgc = c2, bgd = (uint32_t)d & 0xffffu;
         if ((uint32_t)abs((int)curr[0] - (int)bgc) > D.colThr / 2u) return false;
@@ -156,17 +184,17 @@ struct LobOvr {
 
 // the evaluation of pixel p (x, y): ordered scan (with overrides), then the decision and the model
 // writes with their draws (:497-513 / :545-575); returns the intent word
-template <int C, bool OVR>
+template <int C, int ALG, bool OVR>
 __device__ uint32_t eval_px(const LobDev& D, int p, int x, int y, const uint32_t (&vals)[C][4],
                             const uint32_t (&curr)[C], const LobOvr& ov, unsigned long long* scanned) {
     int nGood = 0, s = 0;
     unsigned long long dB = 0;
     uint32_t cB = 0;
-    if (D.N > 0) load_sample<C>(D, 0, p, dB, cB);
+    if (D.N > 0) load_sample<C, ALG>(D, 0, p, dB, cB);
     while (nGood < D.nreq && s < D.N) {
         unsigned long long d = dB;
         uint32_t c2 = cB;
-        if (s + 1 < D.N) load_sample<C>(D, s + 1, p, dB, cB);
+        if (s + 1 < D.N) load_sample<C, ALG>(D, s + 1, p, dB, cB);
         if (OVR && ((ov.mask >> s) & 1ull)) {
             for (int k = 0; k < ov.n; ++k)
                 if (ov.s[k] == s) {
@@ -174,7 +202,7 @@ __device__ uint32_t eval_px(const LobDev& D, int p, int x, int y, const uint32_t
                     c2 = ov.c[k];
                 }
         }
-        if (match<C>(D, vals, curr, d, c2)) ++nGood;
+        if (match<C, ALG>(D, vals, curr, d, c2)) ++nGood;
         ++s;
     }
     *scanned += (unsigned long long)s;
@@ -188,9 +216,11 @@ __device__ uint32_t eval_px(const LobDev& D, int p, int x, int y, const uint32_t
         w |= kIOwn | (so << 10);
     }
     if (mod64(draw(D, (uint32_t)p, k++, ds), D.nLR) == 0ull) {
+        // getNeighborPosition_3x3 (opencv.hpp:945-953), clamped into the LBSP border (LOBSTER) or the frame (ViBe)
+        constexpr int bord = ALG == ALG_VIBE ? 0 : kBorder;
         const int r = (int)(draw(D, (uint32_t)p, k++, ds) % 8u);
-        const int nx = clampi(x + c_lob_nb3[r][0], kBorder, D.W - kBorder - 1);
-        const int ny = clampi(y + c_lob_nb3[r][1], kBorder, D.H - kBorder - 1);
+        const int nx = clampi(x + c_lob_nb3[r][0], bord, D.W - bord - 1);
+        const int ny = clampi(y + c_lob_nb3[r][1], bord, D.H - bord - 1);
         const uint32_t sn = draw(D, (uint32_t)p, k++, ds) % (uint32_t)D.N;
         const uint32_t code = (uint32_t)((ny - y + 1) * 3 + (nx - x + 1));
         w |= kINb | (code << 17) | (sn << 21);
@@ -198,11 +228,12 @@ __device__ uint32_t eval_px(const LobDev& D, int p, int x, int y, const uint32_t
     return w | (k << 27);
 }
 
-template <int C>
+// the pixel's colour and (LOBSTER) its LBSP taps
+template <int C, int ALG>
 __device__ __forceinline__ void pixel_inputs(const LobDev& D, int p, uint32_t (&vals)[C][4], uint32_t (&curr)[C]) {
 #pragma unroll
     for (int c = 0; c < C; ++c) {
-        taps<C>(D.frame, D.W, p, c, vals[c]);
+        if (ALG == ALG_LOBSTER) taps<C>(D.frame, D.W, p, c, vals[c]);
         curr[c] = __ldg(D.frame + (size_t)p * C + c);
     }
 }
@@ -228,29 +259,35 @@ __device__ __forceinline__ void push(const LobDev& D, uint32_t* list, unsigned i
 
 }  // namespace
 
-// 1. every ROI pixel against the frame-start samples
-template <int C>
+// 1. every ROI pixel (ViBe: every pixel) against the frame-start samples
+template <int C, int ALG>
 __global__ void __launch_bounds__(kThreadsL) lob_k_eval(LobDev D) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long scanned = 0;
     if (p < D.npx) {
-        if (!D.roi[p]) {
+        if (ALG == ALG_LOBSTER && !D.roi[p]) {
             D.intent[p] = 0u;
         } else {
             const int x = p % D.W, y = p / D.W;
             uint32_t vals[C][4], curr[C];
-            pixel_inputs<C>(D, p, vals, curr);
-            // the sample word this pixel writes: its descriptors (:499-500 / :548-550) and colour
+            pixel_inputs<C, ALG>(D, p, vals, curr);
+            // the sample word this pixel writes: LOBSTER, its descriptors (:499-500 / :548-550) and colour;
+            // ViBe, its colour
             unsigned long long wd = 0;
+            if (ALG == ALG_VIBE) {
 #pragma unroll
-            for (int c = 0; c < C; ++c)
-                wd |= (unsigned long long)lbsp_thr(vals[c], curr[c], __ldg(D.lut + curr[c])) << (16 * c);
-            if (C == 3) wd |= ((unsigned long long)curr[0] << 48) | ((unsigned long long)curr[1] << 56);
+                for (int c = 0; c < C; ++c) wd |= (unsigned long long)curr[c] << (8 * c);
+            } else {
+#pragma unroll
+                for (int c = 0; c < C; ++c)
+                    wd |= (unsigned long long)lbsp_thr(vals[c], curr[c], __ldg(D.lut + curr[c])) << (16 * c);
+                if (C == 3) wd |= ((unsigned long long)curr[0] << 48) | ((unsigned long long)curr[1] << 56);
+            }
             D.wD[p] = wd;
             LobOvr none;
             none.n = 0;
             none.mask = 0;
-            D.intent[p] = eval_px<C, false>(D, p, x, y, vals, curr, none, &scanned);
+            D.intent[p] = eval_px<C, ALG, false>(D, p, x, y, vals, curr, none, &scanned);
         }
     }
     warp_add(&D.stats[0], scanned);
@@ -278,7 +315,7 @@ __global__ void __launch_bounds__(kThreadsL) lob_k_mark(LobDev D) {
 
 // 3. one repair round: re-evaluates the pixels of list (round & 1) with the samples their earlier
 // neighbours write now, and lists the later pixels whose incoming writes changed
-template <int C>
+template <int C, int ALG>
 __global__ void __launch_bounds__(kThreadsL) lob_k_round(LobDev D, int round) {
     if (ld_vol(&D.flags[LOB_F_CONV])) return;
     const int cur = round & 1;
@@ -304,14 +341,14 @@ __global__ void __launch_bounds__(kThreadsL) lob_k_round(LobDev D, int round) {
                 const int s = i_snb(wq);
                 ov.s[ov.n] = s;
                 ov.d[ov.n] = __ldcg(D.wD + q4[j]);
-                ov.c[ov.n] = __ldg(D.frame + (size_t)q4[j] * C + (C == 3 ? 2 : 0));
+                ov.c[ov.n] = ALG == ALG_VIBE ? 0u : __ldg(D.frame + (size_t)q4[j] * C + (C == 3 ? 2 : 0));
                 ++ov.n;
                 ov.mask |= 1ull << s;
             }
         }
         uint32_t vals[C][4], curr[C];
-        pixel_inputs<C>(D, p, vals, curr);
-        const uint32_t wNew = eval_px<C, true>(D, p, x, y, vals, curr, ov, &scanned);
+        pixel_inputs<C, ALG>(D, p, vals, curr);
+        const uint32_t wNew = eval_px<C, ALG, true>(D, p, x, y, vals, curr, ov, &scanned);
         const uint32_t wOld = ld_vol(&D.intent[p]);
         if (wNew == wOld) continue;
         *(volatile uint32_t*)&D.intent[p] = wNew;
@@ -347,8 +384,9 @@ __global__ void lob_k_round_end(LobDev D, int round) {
 }
 
 // 4. every pixel gathers the sample writes aimed at it, in raster order of the writers (own update
-// before neighbour update within a writer); the raw mask and the draw counters of the frame
-template <int C>
+// before neighbour update within a writer); the raw mask (ViBe: the output, :84 / :176) and the draw
+// counters of the frame
+template <int C, int ALG>
 __global__ void __launch_bounds__(kThreadsL) lob_k_commit(LobDev D) {
     if (!ld_vol(&D.flags[LOB_F_CONV])) return;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -356,15 +394,20 @@ __global__ void __launch_bounds__(kThreadsL) lob_k_commit(LobDev D) {
     if (p < D.npx) {
         const uint32_t wp = D.intent[p];
         const bool valid = (wp & kIValid) != 0;
-        D.rawFG[p] = (valid && (wp & kIFG)) ? 255 : 0;
+        const uint8_t raw = (valid && (wp & kIFG)) ? 255 : 0;
+        if (ALG == ALG_VIBE) D.maskOut[p] = raw;
+        else D.rawFG[p] = raw;
         D.kctr[p] = (uint16_t)(valid ? i_draws(wp) : 0);
         if (valid) writes = ((wp & kIOwn) ? 1ull : 0ull) + ((wp & kINb) ? 1ull : 0ull);
         const int x = p % D.W, y = p / D.W;
-        if (x >= kBorder && y >= kBorder && x < D.W - kBorder && y < D.H - kBorder) {
+        // the pixels a write can reach: inside the LBSP border (LOBSTER), the whole frame (ViBe)
+        constexpr int bord = ALG == ALG_VIBE ? 0 : kBorder;
+        if (x >= bord && y >= bord && x < D.W - bord && y < D.H - bord) {
             int ns = 0;
             int ss[10], sq[10];
             for (int dy = -1; dy <= 1; ++dy)
                 for (int dx = -1; dx <= 1; ++dx) {
+                    if (y + dy < 0 || y + dy >= D.H || x + dx < 0 || x + dx >= D.W) continue;
                     const int q = p + dy * D.W + dx;
                     const uint32_t wq = D.intent[q];
                     if (!(wq & kIValid)) continue;
@@ -382,9 +425,15 @@ __global__ void __launch_bounds__(kThreadsL) lob_k_commit(LobDev D) {
             for (int k = 0; k < ns; ++k) {
                 const size_t o = (size_t)ss[k] * D.npx + p;
                 const int q = sq[k];
-                if (C == 3) ((unsigned long long*)D.sD)[o] = D.wD[q];
-                else ((uint16_t*)D.sD)[o] = (uint16_t)D.wD[q];
-                D.sC[o] = __ldg(D.frame + (size_t)q * C + (C == 3 ? 2 : 0));
+                if (ALG == ALG_VIBE) {
+                    const unsigned long long wq = D.wD[q];
+#pragma unroll
+                    for (int c = 0; c < C; ++c) D.sC[o * C + c] = (uint8_t)(wq >> (8 * c));
+                } else {
+                    if (C == 3) ((unsigned long long*)D.sD)[o] = D.wD[q];
+                    else ((uint16_t*)D.sD)[o] = (uint16_t)D.wD[q];
+                    D.sC[o] = __ldg(D.frame + (size_t)q * C + (C == 3 ? 2 : 0));
+                }
             }
         }
     }
@@ -435,6 +484,35 @@ __global__ void __launch_bounds__(kThreadsL) lob_k_init(LobDev D, const uint8_t*
     }
     D.lastFG[p] = 0;
     D.kctr[p] = 0;
+}
+
+// ViBe's initialize() (BackgroundSubtractorViBe.cpp:57-75 / :112-134): sample s of every pixel from a
+// 7x7 Gaussian position of the frame clamped to the frame (draw s of the pixel in frame 0)
+template <int C>
+__global__ void __launch_bounds__(kThreadsL) lob_k_vibe_init(LobDev D, const uint8_t* img) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= D.npx) return;
+    const int x0 = p % D.W, y0 = p / D.W;
+    Draws ds;
+    ds.blk = 0xffffffffu;
+    for (int s = 0; s < D.N; ++s) {
+        int r = 1 + (int)(draw(D, (uint32_t)p, (uint32_t)s, ds) % 512u);
+        int sx = 0, sy = 0;
+        for (int i = 0; i < 49; ++i) {
+            r -= c_lob_pat7[i];
+            if (r <= 0) {
+                sy = i / 7;
+                sx = i % 7;
+                break;
+            }
+        }
+        sx = clampi(sx + x0 - 3, 0, D.W - 1);
+        sy = clampi(sy + y0 - 3, 0, D.H - 1);
+        const uint8_t* src = img + ((size_t)sy * D.W + sx) * C;
+        uint8_t* dst = D.sC + ((size_t)s * D.npx + p) * C;
+#pragma unroll
+        for (int c = 0; c < C; ++c) dst[c] = __ldg(src + c);
+    }
 }
 
 // refreshModel(frac, force) (:410-440): samples [start, start+nref) of every ROI pixel (not in the last
@@ -499,7 +577,9 @@ __global__ void lob_k_background(LobDev D, void* out, int descriptors) {
         for (int s = 0; s < D.N; ++s) {
             const size_t o = (size_t)s * D.npx + p;
             uint32_t v;
-            if (descriptors) {
+            if (D.alg == ALG_VIBE) {
+                v = D.sC[o * C + c];
+            } else if (descriptors) {
                 v = C == 3 ? (uint32_t)(((const unsigned long long*)D.sD)[o] >> (16 * c)) & 0xffffu
                            : ((const uint16_t*)D.sD)[o];
             } else if (C == 3 && c < 2) {
@@ -565,20 +645,24 @@ void lob_release(LobState& L) {
     L.h_flags = nullptr;
 }
 
-lvbgs_status lob_setup(LobState& L, const lvbgs_params& prm, int W, int H, int C, const std::vector<uint8_t>& roi,
-                       size_t orig, size_t fin, cudaStream_t st, std::string& err) {
+lvbgs_status lob_setup(LobState& L, int alg, const lvbgs_params& prm, int W, int H, int C,
+                       const std::vector<uint8_t>& roi, size_t orig, size_t fin, cudaStream_t st, std::string& err) {
     cudaFree(L.mem);
     L.mem = nullptr;
     const size_t npx = (size_t)W * H, N = prm.bg_samples;
+    // ViBe keeps only colour samples ([N][npx*C] bytes); LOBSTER the packed descriptor plane and a colour byte
+    const bool vibe = alg == ALG_VIBE;
+    const size_t lob = vibe ? 0 : 1;
     size_t off = 0;
     auto take = [&](size_t bytes) {
         const size_t o = off;
         off += al(bytes);
         return o;
     };
-    const size_t oRoi = take(npx), oLastColor = take(npx * C), oLastFG = take(npx), oRawFG = take(npx),
-                 oLut = take(256), oLastDesc = take(npx * C * 2), oKctr = take(npx * 2),
-                 oSD = take(N * npx * (C == 3 ? 8 : 2)), oSC = take(N * npx), oIntent = take(npx * 4),
+    const size_t oRoi = take(npx), oLastColor = take(lob * npx * C), oLastFG = take(lob * npx),
+                 oRawFG = take(lob * npx), oLut = take(256), oLastDesc = take(lob * npx * C * 2), oKctr = take(npx * 2),
+                 oSD = take(lob * N * npx * (C == 3 ? 8 : 2)), oSC = take(vibe ? N * npx * C : N * npx),
+                 oIntent = take(npx * 4),
                  oWD = take(npx * 8), oList0 = take(npx * 4), oList1 = take(npx * 4), oStamp = take(npx * 4),
                  oFlags = take(LOB_F_WORDS * 4), oStats = take(16), oFrame = take(npx * C), oMask = take(npx);
     LOB_CUDA(cudaMalloc(&L.mem, off), "model allocation");
@@ -586,6 +670,7 @@ lvbgs_status lob_setup(LobState& L, const lvbgs_params& prm, int W, int H, int C
     L.bytes = off;
     LobDev& D = L.d;
     D = LobDev{};
+    D.alg = alg;
     D.W = W;
     D.H = H;
     D.C = C;
@@ -635,6 +720,30 @@ lvbgs_status lob_setup(LobState& L, const lvbgs_params& prm, int W, int H, int C
 }
 
 namespace {
+// one kernel of the frame step for the stream's (channels, algorithm)
+template <template <int, int> class K, typename... A>
+void launch(const LobDev& D, int blocks, cudaStream_t st, A... args) {
+    if (D.alg == ALG_VIBE) {
+        if (D.C == 3) K<3, ALG_VIBE>::run(blocks, st, D, args...);
+        else K<1, ALG_VIBE>::run(blocks, st, D, args...);
+    } else {
+        if (D.C == 3) K<3, ALG_LOBSTER>::run(blocks, st, D, args...);
+        else K<1, ALG_LOBSTER>::run(blocks, st, D, args...);
+    }
+}
+template <int C, int ALG>
+struct Eval {
+    static void run(int b, cudaStream_t st, const LobDev& D) { lob_k_eval<C, ALG><<<b, kThreadsL, 0, st>>>(D); }
+};
+template <int C, int ALG>
+struct Round {
+    static void run(int b, cudaStream_t st, const LobDev& D, int r) { lob_k_round<C, ALG><<<b, kThreadsL, 0, st>>>(D, r); }
+};
+template <int C, int ALG>
+struct Commit {
+    static void run(int b, cudaStream_t st, const LobDev& D) { lob_k_commit<C, ALG><<<b, kThreadsL, 0, st>>>(D); }
+};
+
 lvbgs_status lob_refresh_launch(LobState& L, float frac, int force, cudaStream_t st, std::string& err) {
     LobDev& D = L.d;
     const int N = D.N;
@@ -660,6 +769,13 @@ lvbgs_status lob_init_model(LobState& L, const uint8_t* dimg, cudaStream_t st, s
     LobDev& D = L.d;
     D.frameKey = 0;
     L.ksent = 0;
+    if (D.alg == ALG_VIBE) {
+        if (D.C == 3) lob_k_vibe_init<3><<<blocks_for(D.npx), kThreadsL, 0, st>>>(D, dimg);
+        else lob_k_vibe_init<1><<<blocks_for(D.npx), kThreadsL, 0, st>>>(D, dimg);
+        LOB_CUDA(cudaGetLastError(), "init launch");
+        LOB_CUDA(cudaStreamSynchronize(st), "initialization");
+        return LVBGS_OK;
+    }
     if (D.C == 3) lob_k_init<3><<<blocks_for(D.npx), kThreadsL, 0, st>>>(D, dimg);
     else lob_k_init<1><<<blocks_for(D.npx), kThreadsL, 0, st>>>(D, dimg);
     LOB_CUDA(cudaGetLastError(), "init launch");
@@ -692,23 +808,20 @@ lvbgs_status lob_apply(LobState& L, const uint8_t* dimg, uint8_t* dmask, uint8_t
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int roundBlocks = 2 * (sms > 0 ? sms : 1);
     LOB_CUDA(cudaMemsetAsync(D.flags, 0, LOB_F_WORDS * 4, st), "flag reset");
-    if (C == 3) lob_k_eval<3><<<nb, kThreadsL, 0, st>>>(D);
-    else lob_k_eval<1><<<nb, kThreadsL, 0, st>>>(D);
+    launch<Eval>(D, nb, st);
     lob_k_mark<<<nb, kThreadsL, 0, st>>>(D);
     LOB_CUDA(cudaGetLastError(), "evaluation launch");
     int round = 0, chunk = L.lastRounds + 1;
     for (;;) {
         for (int i = 0; i < chunk; ++i, ++round) {
-            if (C == 3) lob_k_round<3><<<roundBlocks, kThreadsL, 0, st>>>(D, round);
-            else lob_k_round<1><<<roundBlocks, kThreadsL, 0, st>>>(D, round);
+            launch<Round>(D, roundBlocks, st, round);
             lob_k_round_end<<<1, 1, 0, st>>>(D, round);
         }
-        if (C == 3) {
-            lob_k_commit<3><<<nb, kThreadsL, 0, st>>>(D);
-            lob_k_median<3><<<nb, kThreadsL, 0, st>>>(D);
-        } else {
-            lob_k_commit<1><<<nb, kThreadsL, 0, st>>>(D);
-            lob_k_median<1><<<nb, kThreadsL, 0, st>>>(D);
+        launch<Commit>(D, nb, st);
+        // LOBSTER's median blur, last mask and last colour frame (ViBe outputs its raw mask)
+        if (D.alg == ALG_LOBSTER) {
+            if (C == 3) lob_k_median<3><<<nb, kThreadsL, 0, st>>>(D);
+            else lob_k_median<1><<<nb, kThreadsL, 0, st>>>(D);
         }
         LOB_CUDA(cudaGetLastError(), "repair launch");
         if (hostMask) LOB_CUDA(cudaMemcpyAsync(hostMask, dmask, (size_t)D.npx, cudaMemcpyDeviceToHost, st), "mask download");
@@ -747,6 +860,7 @@ lvbgs_status lob_background(LobState& L, void* hostOut, bool descriptors, cudaSt
 
 size_t lob_map_bytes(const LobState& L, int which) {
     const size_t npx = (size_t)L.d.npx, C = (size_t)L.d.C, N = (size_t)L.d.N;
+    if (L.d.alg == ALG_VIBE) return which == LVBGS_MAP_SAMPLE_COLOR ? N * npx * C : which == LVBGS_MAP_ROI ? npx : 0;
     switch (which) {
         case LVBGS_MAP_LAST_FG:
         case LVBGS_MAP_ROI: return npx;
@@ -771,7 +885,8 @@ lvbgs_status lob_get_map(LobState& L, int which, void* hostOut, size_t bytes, cu
         return LVBGS_BAD_ARG;
     }
     const void* src = nullptr;
-    switch (which) {
+    if (D.alg == ALG_VIBE) src = which == LVBGS_MAP_ROI ? (const void*)D.roi : (const void*)D.sC;
+    else switch (which) {
         case LVBGS_MAP_LAST_FG: src = D.lastFG; break;
         case LVBGS_MAP_ROI: src = D.roi; break;
         case LVBGS_MAP_LAST_COLOR: src = D.lastColor; break;

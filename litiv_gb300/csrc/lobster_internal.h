@@ -1,10 +1,13 @@
-// LOBSTER on the device: state of one stream and the host functions that run its frame steps
-// (lobster.cu), called by the C-ABI layer for handles created with LVBGS_ALGO_LOBSTER.
+// LOBSTER and ViBe on the device: state of one stream and the host functions that run its frame steps
+// (lobster.cu), called by the C-ABI layer for handles created with LVBGS_ALGO_LOBSTER / LVBGS_ALGO_VIBE.
+// Both are sample-consensus models whose in-frame dependency is the same (a pixel's scan reads its own
+// samples, which earlier pixels' neighbour updates may overwrite), so they share the frame step.
 //
 // Device layout (one allocation per stream, each array 256-byte aligned):
 //   roi[npx], lastColor[npx*C], lastFG[npx], lastDesc[npx*C] (u16), kctr[npx] (u16, draws of the last
 //   frame), samples sD[N][npx] / sC[N][npx] (the SuBSENSE packing: for C=3 one u64 = desc0 | desc1<<16 |
 //   desc2<<32 | B<<48 | G<<56 and the R byte, for C=1 one u16 descriptor and the intensity),
+//   ViBe keeps only its samples, sC[N][npx*C] (the reference's layout: C colour bytes per sample);
 //   scratch of a frame step: intent[npx] (u32), wD[npx] (the sample word a pixel writes), rawFG[npx],
 //   two repair lists and their dedupe stamps, flags and counters, the staged frame and mask.
 #pragma once
@@ -17,13 +20,17 @@
 
 namespace lvbgs {
 
+// the algorithm of a stream
+enum { ALG_LOBSTER = 0, ALG_VIBE = 1 };
+
 // flags of one frame step (device words)
 enum { LOB_F_COUNT0 = 0, LOB_F_COUNT1, LOB_F_CONV, LOB_F_ROUNDS, LOB_F_ERR, LOB_F_WORDS = 8 };
 
 // kernel parameters (by value)
 struct LobDev {
+    int alg;  // ALG_LOBSTER or ALG_VIBE
     int W, H, C, N, nreq, npx;
-    unsigned int descThr, colThr;  // m_nDescDistThreshold, m_nColorDistThreshold
+    unsigned int descThr, colThr;  // m_nDescDistThreshold (LOBSTER), m_nColorDistThreshold (both)
     unsigned long long seed;
     unsigned long long nLR;  // ceil(learning rate), ~0 for an infinite rate
     uint32_t frameKey;       // apply() calls since initialize(): the generator's frame
@@ -56,12 +63,13 @@ struct LobState {
     size_t n_rel = 0, orig_roi = 0;
 };
 
-// allocates the stream's device state for a W x H x C frame and uploads the validated ROI and the LBSP
-// threshold LUT; the model itself is built by lob_init_model
-lvbgs_status lob_setup(LobState& L, const lvbgs_params& prm, int W, int H, int C, const std::vector<uint8_t>& roi,
-                       size_t orig, size_t fin, cudaStream_t st, std::string& err);
-// initialize() after lob_setup: last colour/descriptor frames from dimg (a device frame), zero samples,
-// then refreshModel(1.0, true); waits for the device
+// allocates the stream's device state for a W x H x C frame and uploads the validated ROI (ViBe: every
+// pixel) and the LBSP threshold LUT; the model itself is built by lob_init_model
+lvbgs_status lob_setup(LobState& L, int alg, const lvbgs_params& prm, int W, int H, int C,
+                       const std::vector<uint8_t>& roi, size_t orig, size_t fin, cudaStream_t st, std::string& err);
+// initialize() after lob_setup, from dimg (a device frame); waits for the device. LOBSTER: last
+// colour/descriptor frames, zero samples, then refreshModel(1.0, true); ViBe: every sample of every pixel
+// from a 7x7 position of the frame
 lvbgs_status lob_init_model(LobState& L, const uint8_t* dimg, cudaStream_t st, std::string& err);
 // apply(): one frame step on dimg (device); the mask goes to dmask (device) and, when hostMask is not
 // null, to host memory; waits for the device
@@ -71,8 +79,8 @@ lvbgs_status lob_apply(LobState& L, const uint8_t* dimg, uint8_t* dmask, uint8_t
 lvbgs_status lob_refresh(LobState& L, float frac, int force, cudaStream_t st, std::string& err);
 // getBackgroundImage (u8 [H*W*C]) or getBackgroundDescriptorsImage (u16 [H*W*C]) into host memory
 lvbgs_status lob_background(LobState& L, void* hostOut, bool descriptors, cudaStream_t st, std::string& err);
-// model maps in the reference's layout (LVBGS_MAP_LAST_FG, _ROI, _LAST_COLOR, _LAST_DESC, _SAMPLE_COLOR,
-// _SAMPLE_DESC, _LUT); 0 bytes for the others
+// model maps in the reference's layout (LOBSTER: LVBGS_MAP_LAST_FG, _ROI, _LAST_COLOR, _LAST_DESC,
+// _SAMPLE_COLOR, _SAMPLE_DESC, _LUT; ViBe: _SAMPLE_COLOR, _ROI); 0 bytes for the others
 size_t lob_map_bytes(const LobState& L, int which);
 lvbgs_status lob_get_map(LobState& L, int which, void* hostOut, size_t bytes, cudaStream_t st, std::string& err);
 // samples evaluated and sample writes since initialize()

@@ -1,15 +1,16 @@
 /* ORACLE (test infrastructure only; never linked into the product library).
  *
- * CPU restatement of the reference's SuBSENSE, PAWCS and LOBSTER per-pixel background
+ * CPU restatement of the reference's SuBSENSE, PAWCS, LOBSTER and ViBe per-pixel background
  * subtraction (plstcharles/litiv, modules/video/src/BackgroundSubtractorSuBSENSE.cpp,
- * BackgroundSubtractorPAWCS.cpp, BackgroundSubtractorLOBSTER.cpp) and of the LBSP descriptor
+ * BackgroundSubtractorPAWCS.cpp, BackgroundSubtractorLOBSTER.cpp, BackgroundSubtractorViBe.cpp) and of
+ * the LBSP descriptor
  * (modules/features2d/include/litiv/features2d/LBSP.hpp).
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it,
  * always as the checker.
  *
  * Parity pins: the LBSP descriptor is pinned by the reference's golden vector
  * (modules/features2d/test/data/test_lbsp.bin, see tests/golden/). The SuBSENSE and PAWCS
- * (and LOBSTER) restatements are pinned to the reference itself: oracle/refshim/build_ref.py compiles the
+ * (and LOBSTER, ViBe) restatements are pinned to the reference itself: oracle/refshim/build_ref.py compiles the
  * reference's own modules/video/src sources (against a project-written OpenCV stand-in, with rand()
  * routed to the same generator) into oracle/_ref/libref.so, which exposes this same API (rsub_* /
  * rpawcs_*), and tests/test_oracle_reference.py compares every map bit for bit. The OpenCV image
@@ -196,6 +197,27 @@ int olob_get_background(const olob_t* o, uint8_t* out);              /* :583-600
 int olob_get_background_descriptors(const olob_t* o, uint16_t* out); /* :602-620 */
 const void* olob_map(const olob_t* o, int which, size_t* nbytes);
 void olob_get_scalars(const olob_t* o, olob_scalars* s);
+
+/* ---- ViBe (modules/video/src/BackgroundSubtractorViBe.cpp: _1ch for one channel, _3ch for three) ---- */
+typedef struct ovibe ovibe_t;
+typedef struct {
+    size_t color_dist_threshold; /* BGSVIBE_DEFAULT_COLOR_DIST_THRESHOLD = 20 */
+    size_t bg_samples;           /* BGSVIBE_DEFAULT_NB_BG_SAMPLES = 20 */
+    size_t required_bg_samples;  /* BGSVIBE_DEFAULT_REQUIRED_NB_BG_SAMPLES = 2 */
+    uint64_t seed;
+} ovibe_params;
+void ovibe_default_params(ovibe_params* p);
+ovibe_t* ovibe_create(const ovibe_params* p);
+void ovibe_destroy(ovibe_t* o);
+/* initialize (BackgroundSubtractorViBe.cpp:57-75 / :112-134) */
+int ovibe_initialize(ovibe_t* o, const uint8_t* img, int width, int height, int channels);
+/* apply (:77-103 / :136-191); learning_rate > 0 (the reference's default is 16) */
+int ovibe_apply(ovibe_t* o, const uint8_t* img, uint8_t* fgmask, double learning_rate);
+int ovibe_get_background(const ovibe_t* o, uint8_t* out); /* :33-48 */
+/* the samples, [N][H*W*C] */
+const void* ovibe_samples(const ovibe_t* o, size_t* nbytes);
+/* apply() calls, samples evaluated, sample writes */
+void ovibe_get_stats(const ovibe_t* o, uint64_t out[3]);
 
 /* CPU baseline for LOBSTER: as orun_streams (apply phase timed, learning rate 16) */
 double orun_lobster_streams(int n_streams, const uint8_t* const* frames, const int* n_frames,

@@ -1,5 +1,5 @@
 """ORACLE (test infrastructure only): ctypes wrapper of oracle/_build/liboracle.so (the C
-restatement of the reference's SuBSENSE, PAWCS and LOBSTER, "port") and of oracle/_ref/libref.so (the reference's own SuBSENSE /
+restatement of the reference's SuBSENSE, PAWCS, LOBSTER and ViBe, "port") and of oracle/_ref/libref.so (the reference's own SuBSENSE /
 PAWCS sources compiled against the project-written OpenCV stand-in, "reference"; built only where
 the reference sources are present, see oracle/refshim/build_ref.py). Both expose the same C API,
 so OracleSuBSENSE / OraclePAWCS drive either one (``impl=``).
@@ -81,6 +81,11 @@ class LScalars(C.Structure):
 LOBSTER_MAP_NAMES = ["LAST_FG", "ROI", "LAST_COLOR", "LAST_DESC", "SAMPLE_COLOR", "SAMPLE_DESC", "LUT"]
 
 
+class VParams(C.Structure):
+    _fields_ = [("color_dist_threshold", C.c_size_t), ("bg_samples", C.c_size_t),
+                ("required_bg_samples", C.c_size_t), ("seed", C.c_uint64)]
+
+
 def build():
     subprocess.run(["make", "-s", "-C", HERE], check=True)
 
@@ -121,6 +126,14 @@ def ref_lib():
         L.rsub_map.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]
         L.rpawcs_refresh_model.argtypes = [C.c_void_p, C.c_size_t, C.c_float, C.c_int]
         L.rlob_refresh_model.argtypes = [C.c_void_p, C.c_float, C.c_int]
+        L.rvibe_create.restype = C.c_void_p
+        L.rvibe_create.argtypes = [C.POINTER(VParams)]
+        L.rvibe_destroy.argtypes = [C.c_void_p]
+        L.rvibe_initialize.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int]
+        L.rvibe_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
+        L.rvibe_get_background.argtypes = [C.c_void_p, C.c_void_p]
+        L.rvibe_samples.restype = C.c_void_p
+        L.rvibe_samples.argtypes = [C.c_void_p, C.POINTER(C.c_size_t)]
         L.rlob_map.restype = C.c_void_p
         L.rlob_map.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]
         L.rpawcs_export.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]
@@ -207,6 +220,16 @@ def lib():
         L.olob_map.restype = C.c_void_p
         L.olob_map.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]
         L.olob_get_scalars.argtypes = [C.c_void_p, C.POINTER(LScalars)]
+        L.ovibe_default_params.argtypes = [C.POINTER(VParams)]
+        L.ovibe_create.restype = C.c_void_p
+        L.ovibe_create.argtypes = [C.POINTER(VParams)]
+        L.ovibe_destroy.argtypes = [C.c_void_p]
+        L.ovibe_initialize.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int]
+        L.ovibe_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
+        L.ovibe_get_background.argtypes = [C.c_void_p, C.c_void_p]
+        L.ovibe_samples.restype = C.c_void_p
+        L.ovibe_samples.argtypes = [C.c_void_p, C.POINTER(C.c_size_t)]
+        L.ovibe_get_stats.argtypes = [C.c_void_p, C.POINTER(C.c_uint64)]
         L.orun_lobster_streams.restype = C.c_double
         L.orun_lobster_streams.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                            C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_uint64), C.c_int]
@@ -483,6 +506,73 @@ class OracleLOBSTER:
         s = LScalars()
         self._a.get_scalars(self._o, C.byref(s))
         return {f: getattr(s, f) for f, _ in LScalars._fields_}
+
+
+class OracleViBe:
+    """Sequential CPU ViBe (the checker): the C restatement (impl="port") or the reference's own
+    BackgroundSubtractorViBe_1ch / _3ch (impl="reference"), chosen by the frame's channel count.
+    apply()'s learning rate defaults to BGSVIBE_DEFAULT_LEARNING_RATE (16)."""
+
+    def __init__(self, seed=0, impl="port", **params):
+        p = VParams()
+        lib().ovibe_default_params(C.byref(p))
+        p.seed = seed
+        for k, v in params.items():
+            setattr(p, k, v)
+        self.params = p
+        self.impl = impl
+        self._a = _Api(impl, "ovibe_", "rvibe_")
+        self._o = self._a.create(C.byref(p))
+        if not self._o:
+            raise ValueError("invalid oracle parameters")
+        self.shape = None
+
+    def close(self):
+        if self._o:
+            self._a.destroy(self._o)
+            self._o = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def initialize(self, img):
+        img = np.ascontiguousarray(img, np.uint8)
+        H, W = img.shape[:2]
+        Cc = img.shape[2] if img.ndim == 3 else 1
+        if self._a.initialize(self._o, img.ctypes.data_as(C.c_void_p), W, H, Cc) != 0:
+            raise ValueError("oracle initialize failed")
+        self.shape = (H, W, Cc)
+
+    def apply(self, img, lr=16.0):
+        img = np.ascontiguousarray(img, np.uint8)
+        H, W, _ = self.shape
+        mask = np.empty((H, W), np.uint8)
+        if self._a.apply(self._o, img.ctypes.data_as(C.c_void_p), mask.ctypes.data_as(C.c_void_p), float(lr)) != 0:
+            raise ValueError("oracle apply failed")
+        return mask
+
+    def background(self):
+        H, W, Cc = self.shape
+        out = np.empty((H, W, Cc) if Cc > 1 else (H, W), np.uint8)
+        self._a.get_background(self._o, out.ctypes.data_as(C.c_void_p))
+        return out
+
+    def samples(self):
+        """uint8 [N, H, W(, C)]"""
+        n = C.c_size_t()
+        ptr = self._a.samples(self._o, C.byref(n))
+        raw = np.ctypeslib.as_array((C.c_uint8 * n.value).from_address(ptr)).copy()
+        H, W, Cc = self.shape
+        return raw.reshape((-1, H, W, Cc) if Cc > 1 else (-1, H, W))
+
+    def stats(self):
+        """apply() calls, samples evaluated, sample writes (the port only)"""
+        out = (C.c_uint64 * 3)()
+        lib().ovibe_get_stats(self._o, out)
+        return list(out)
 
 
 def lbsp_compute2(img, abs_threshold=None, rel_threshold=0.333, offset=0, out=None):

@@ -1,5 +1,5 @@
-"""ORACLE build recipe (test infrastructure only): compiles the REFERENCE's own SuBSENSE / PAWCS / LOBSTER
-sources into oracle/_ref/libref.so, for the CPU tests that pin the C restatement (oracle/*.c) to the
+"""ORACLE build recipe (test infrastructure only): compiles the REFERENCE's own SuBSENSE / PAWCS / LOBSTER /
+ViBe sources into oracle/_ref/libref.so, for the CPU tests that pin the C restatement (oracle/*.c) to the
 reference itself.
 
 The reference is a CMake project that needs OpenCV; neither CMake's configure step nor OpenCV is
@@ -7,7 +7,8 @@ used here. Instead:
 
 * the reference sources are compiled unmodified, from where they lie:
   modules/video/src/BackgroundSubtractionUtils.cpp, BackgroundSubtractorLBSP.cpp,
-  BackgroundSubtractorSuBSENSE.cpp, BackgroundSubtractorPAWCS.cpp, BackgroundSubtractorLOBSTER.cpp, with
+  BackgroundSubtractorSuBSENSE.cpp, BackgroundSubtractorPAWCS.cpp, BackgroundSubtractorLOBSTER.cpp,
+  BackgroundSubtractorViBe.cpp, with
   the reference's own headers (BackgroundSubtractionUtils.hpp, BackgroundSubtractorLBSP.hpp,
   BackgroundSubtractorSuBSENSE.hpp, BackgroundSubtractorPAWCS.hpp, BackgroundSubtractorLOBSTER.hpp, features2d LBSP.hpp, utils algo.hpp, math.hpp, cxx.hpp, simd.hpp,
   platform.hpp, console.hpp);
@@ -21,9 +22,10 @@ used here. Instead:
 * ``opencv2/*`` are project-written stand-ins (oracle/refshim/opencv2/) holding the cv types and the
   image operations the path calls, written from OpenCV's documented semantics with the same
   definitions as the C restatement (oracle/common.h);
-* ``rand()`` is routed to the counter-based generator (oracle/refshim/lvshim_rand.h, force-included);
+* ``rand()`` is routed to the counter-based generator (oracle/refshim/lvshim_rand.h, force-included;
+  for ViBe also oracle/refshim/lvshim_rand_xy.h, which attributes its draws to the loop's pixel);
 * oracle/refshim/ref_bridge.cpp exposes the reference classes through the same C API as the
-  restatement (rsub_* / rpawcs_* / rlob_* beside osub_* / opawcs_* / olob_*).
+  restatement (rsub_* / rpawcs_* / rlob_* / rvibe_* beside osub_* / opawcs_* / olob_* / ovibe_*).
 
 Run: python oracle/refshim/build_ref.py [reference root]. Outputs go to oracle/_ref/ only. The
 reference root defaults to /root/reference; without it nothing is built (the GPU parity tests do not
@@ -45,6 +47,8 @@ SOURCES = ["modules/video/src/BackgroundSubtractionUtils.cpp",
            "modules/video/src/BackgroundSubtractorSuBSENSE.cpp",
            "modules/video/src/BackgroundSubtractorPAWCS.cpp",
            "modules/video/src/BackgroundSubtractorLOBSTER.cpp"]
+# compiled on its own with lvshim_rand_xy.h as well (its pixel loops name the pixel (x, y) / (x_orig, y_orig))
+XY_SOURCES = ["modules/video/src/BackgroundSubtractorViBe.cpp"]
 INCLUDES = ["modules/video/include", "modules/features2d/include", "modules/utils/include"]
 SHIM_SOURCES = ["ref_bridge.cpp", "lv_support.cpp"]
 
@@ -94,16 +98,26 @@ def build(ref=DEFAULT_REF, verbose=False):
     configure_defines(ref, gen)
     extract_sampling_helpers(ref, gen)
     srcs = [os.path.join(ref, s) for s in SOURCES] + [os.path.join(HERE, s) for s in SHIM_SOURCES]
-    deps = srcs + [os.path.join(dp, f) for dp, _, fs in os.walk(HERE) for f in fs if f.endswith((".h", ".hpp"))]
+    xy_srcs = [os.path.join(ref, s) for s in XY_SOURCES]
+    deps = srcs + xy_srcs + [os.path.join(dp, f) for dp, _, fs in os.walk(HERE) for f in fs if f.endswith((".h", ".hpp"))]
     deps += [os.path.join(gen, "lv_sampling_helpers.inc"), os.path.join(gen, "litiv/utils/defines.hpp"),
              os.path.join(ORACLE, "philox.h"), __file__]
     if os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
         return LIB
     # shim headers first, so that they replace opencv2/* and litiv/utils/opencv.hpp; the configured
     # defines.hpp next; then the reference's include directories
-    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-w",
-           "-I" + HERE, "-I" + gen, "-I" + ORACLE] + ["-I" + os.path.join(ref, d) for d in INCLUDES]
-    cmd += ["-include", os.path.join(HERE, "lvshim_rand.h"), "-o", LIB] + srcs + ["-lpthread"]
+    base = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-w",
+            "-I" + HERE, "-I" + gen, "-I" + ORACLE] + ["-I" + os.path.join(ref, d) for d in INCLUDES]
+    base += ["-include", os.path.join(HERE, "lvshim_rand.h")]
+    objs = []
+    for src in xy_srcs:
+        obj = os.path.join(OUT, os.path.splitext(os.path.basename(src))[0] + ".o")
+        cmd = base + ["-include", os.path.join(HERE, "lvshim_rand_xy.h"), "-c", src, "-o", obj]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        subprocess.run(cmd, check=True)
+        objs.append(obj)
+    cmd = base + ["-shared", "-o", LIB] + srcs + objs + ["-lpthread"]
     if verbose:
         print(" ".join(cmd), flush=True)
     subprocess.run(cmd, check=True)

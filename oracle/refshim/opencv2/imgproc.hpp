@@ -13,6 +13,7 @@ namespace cv {
 enum MorphShapes { MORPH_RECT = 0, MORPH_CROSS = 1, MORPH_ELLIPSE = 2 };
 enum MorphTypes { MORPH_ERODE = 0, MORPH_DILATE = 1, MORPH_OPEN = 2, MORPH_CLOSE = 3 };
 enum InterpolationFlags { INTER_NEAREST = 0, INTER_LINEAR = 1, INTER_CUBIC = 2, INTER_AREA = 3 };
+enum ColorConversionCodes { COLOR_GRAY2BGR = 8 };
 
 inline Mat getStructuringElement(int shape, Size ksize, Point anchor = Point(-1, -1)) {
     if (shape != MORPH_RECT) throw std::runtime_error("getStructuringElement: only MORPH_RECT is supported");
@@ -117,6 +118,19 @@ inline int floodFill(InputOutputArray image, Point seed, Scalar newVal) {
         }
     }
     return n;
+}
+
+// cv::cvtColor for COLOR_GRAY2BGR only: the single channel repeated into three (8UC1 -> 8UC3)
+inline void cvtColor(InputArray src_, OutputArray dst_, int code) {
+    const Mat src = src_.getMat();
+    if (code != COLOR_GRAY2BGR || src.type() != CV_8UC1) throw std::runtime_error("cvtColor: GRAY2BGR of 8UC1 only");
+    Mat out(src.rows, src.cols, CV_8UC3);
+    for (int y = 0; y < src.rows; ++y)
+        for (int x = 0; x < src.cols; ++x)
+            for (int c = 0; c < 3; ++c) out.ptr(y)[3 * x + c] = src.ptr(y)[x];
+    Mat& dst = dst_.getMatRef();
+    dst.create(src.rows, src.cols, CV_8UC3);
+    out.copyTo(dst);
 }
 
 // median of the k x k window with BORDER_REPLICATE (k odd), 8UC1: a 256-bin histogram slid along

@@ -1,11 +1,12 @@
 // ORACLE (test infrastructure only): C API over the REFERENCE's own BackgroundSubtractorSuBSENSE,
-// BackgroundSubtractorPAWCS and BackgroundSubtractorLOBSTER classes (compiled from the reference's sources by
+// BackgroundSubtractorPAWCS, BackgroundSubtractorLOBSTER and BackgroundSubtractorViBe classes (compiled from the reference's sources by
 // oracle/refshim/build_ref.py), with the same signatures and state layouts as the C restatement's
 // osub_* / opawcs_* (oracle/oracle.h), so that the tests can run both on the same frames and compare
 // every map bit for bit. Built into oracle/_ref/libref.so, which only the CPU tests load.
 #include "litiv/video/BackgroundSubtractorLOBSTER.hpp"
 #include "litiv/video/BackgroundSubtractorPAWCS.hpp"
 #include "litiv/video/BackgroundSubtractorSuBSENSE.hpp"
+#include "litiv/video/BackgroundSubtractorViBe.hpp"
 #include "oracle.h"
 #include "philox.h"
 
@@ -44,6 +45,14 @@ int lvshim_rand(size_t px) {
     uint32_t out[4];
     ophilox4x32_10(ctr, key, out);
     return (int)(out[kk & 3u] & 0x7fffffffu);
+}
+
+// the draws of BackgroundSubtractorViBe.cpp (lvshim_rand_xy.h): the loop's pixel (x, y) in apply(),
+// (x_orig, y_orig) in initialize(); the sentinels (-1) elsewhere
+int lvshim_rand_xy(int px, int py, int pxo, int pyo, int width) {
+    if (px >= 0 && py >= 0) return lvshim_rand((size_t)py * (size_t)width + (size_t)px);
+    if (pxo >= 0 && pyo >= 0) return lvshim_rand((size_t)pyo * (size_t)width + (size_t)pxo);
+    return lvshim_rand(SIZE_MAX);
 }
 
 namespace {
@@ -190,6 +199,33 @@ struct RefLob : BackgroundSubtractorLOBSTER {
         s->frames = frames;
         s->n_relevant_px = m_nTotRelevantPxCount;
         s->orig_roi_px = m_nOrigROIPxCount;
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// ViBe: BackgroundSubtractorViBe_1ch for single-channel frames, _3ch for three-channel frames (the
+// instance is made at initialize()); no frame counter either, so the generator's frame counts apply()
+// calls here too
+// ---------------------------------------------------------------------------------------------
+template <typename B>
+struct RefVibeT : B {
+    using B::B;
+    const std::vector<cv::Mat>& samples() const { return this->m_voBGImg; }
+};
+struct RefVibe {
+    ovibe_params p;
+    RngCtx rng;
+    size_t frames = 0;
+    int W = 0, H = 0, C = 0;
+    std::unique_ptr<BackgroundSubtractorViBe> algo;
+    std::vector<uint8_t> exported;
+    explicit RefVibe(const ovibe_params& q) : p(q) {
+        rng.seed = q.seed;
+        rng.frame = &frames;
+    }
+    const std::vector<cv::Mat>& samples() const {
+        return C == 1 ? static_cast<const RefVibeT<BackgroundSubtractorViBe_1ch>*>(algo.get())->samples()
+                      : static_cast<const RefVibeT<BackgroundSubtractorViBe_3ch>*>(algo.get())->samples();
     }
 };
 
@@ -561,5 +597,58 @@ int rlob_set_roi(void* h, const uint8_t* roi, int W, int H) {
 }
 const void* rlob_map(void* h, int which, size_t* nbytes) { return ((RefLob*)h)->map(which, nbytes); }
 void rlob_get_scalars(void* h, olob_scalars* s) { ((RefLob*)h)->scalars(s); }
+
+// ---- ViBe: the reference's BackgroundSubtractorViBe_1ch / _3ch (BackgroundSubtractorViBe.cpp) ----
+void* rvibe_create(const ovibe_params* p) {
+    if (!p || p->bg_samples == 0 || p->required_bg_samples > p->bg_samples) return nullptr;
+    return new RefVibe(*p);
+}
+void rvibe_destroy(void* h) { delete (RefVibe*)h; }
+int rvibe_initialize(void* h, const uint8_t* img, int W, int H, int C) {
+    RefVibe* o = (RefVibe*)h;
+    if (C != 1 && C != 3) return OSUB_EUNSUPPORTED;
+    o->frames = 0;
+    o->rng.start_frame((size_t)W * H);
+    return guarded(o->rng, [&] {
+        if (C == 1)
+            o->algo.reset(new RefVibeT<BackgroundSubtractorViBe_1ch>(o->p.color_dist_threshold, o->p.bg_samples,
+                                                                     o->p.required_bg_samples));
+        else
+            o->algo.reset(new RefVibeT<BackgroundSubtractorViBe_3ch>(o->p.color_dist_threshold, o->p.bg_samples,
+                                                                     o->p.required_bg_samples));
+        o->W = W;
+        o->H = H;
+        o->C = C;
+        o->algo->initialize(cv::Mat(H, W, mat_type(C), (void*)img));
+    });
+}
+int rvibe_apply(void* h, const uint8_t* img, uint8_t* mask, double lr) {
+    RefVibe* o = (RefVibe*)h;
+    if (!o->algo) return OSUB_ENOTINIT;
+    ++o->frames;
+    o->rng.start_frame((size_t)o->W * o->H);
+    cv::Mat m(o->H, o->W, mat_type(o->C), (void*)img);
+    cv::Mat out(o->H, o->W, CV_8UC1, (void*)mask);
+    return guarded(o->rng, [&] { o->algo->apply(m, out, lr); });
+}
+int rvibe_get_background(void* h, uint8_t* out) {
+    RefVibe* o = (RefVibe*)h;
+    if (!o->algo) return OSUB_ENOTINIT;
+    cv::Mat bg;
+    const int rc = guarded(o->rng, [&] { o->algo->getBackgroundImage(bg); });
+    if (rc == OSUB_OK) std::memcpy(out, bg.data, bg.total() * bg.elemSize());
+    return rc;
+}
+const void* rvibe_samples(void* h, size_t* nbytes) {
+    RefVibe* o = (RefVibe*)h;
+    o->exported.clear();
+    if (!o->algo) {
+        *nbytes = 0;
+        return nullptr;
+    }
+    for (const cv::Mat& s : o->samples()) append_mat<uint8_t>(o->exported, s);
+    *nbytes = o->exported.size();
+    return o->exported.data();
+}
 
 }  // extern "C"

@@ -259,3 +259,22 @@ def test_lobster_parameters_gray():
     fr = _frames(0, 10, 5, channels=1)
     _lob_run(fr, seed=8, bg_samples=20, required_bg_samples=3, desc_dist_threshold=2, color_dist_threshold=40,
              rel_lbsp_threshold=0.5)
+
+
+# ---- ViBe (BackgroundSubtractorViBe.cpp: _1ch / _3ch) ----
+@pytest.mark.parametrize("config,channels", [(0, 3), (0, 1), (2, 1)])
+def test_vibe(config, channels):
+    kw = {"channels": channels} if config == 0 else {}
+    fr = _frames(config, 12, 2, **kw)
+    params = {} if config == 0 else {"color_dist_threshold": 12, "bg_samples": 25, "required_bg_samples": 3}
+    port = pyoracle.OracleViBe(seed=31, impl="port", **params)
+    ref = pyoracle.OracleViBe(seed=31, impl="reference", **params)
+    port.initialize(fr[0])
+    ref.initialize(fr[0])
+    assert np.array_equal(port.samples(), ref.samples()), "after initialize"
+    for t, f in enumerate(fr[1:], start=1):
+        lr = [16.0, 1.0, 2.0, float(3 + t)][t % 4]
+        mp, mr = port.apply(f, lr), ref.apply(f, lr)
+        assert np.array_equal(mp, mr), "frame %d: mask differs at %d px" % (t, int((mp != mr).sum()))
+        assert np.array_equal(port.samples(), ref.samples()), "frame %d: samples differ" % t
+    assert np.array_equal(port.background(), ref.background())
