@@ -137,6 +137,16 @@ def cpu_baseline(n_frames=6, threads=None):
                 len(frames), n_frames - 1, px / 1e6, wall)}
 
 
+def _runqueue_wait_ms():
+    """Time the calling thread has spent waiting on a run queue (descheduled while runnable), from
+    /proc/self/task/<tid>/schedstat; 0 where that is not available."""
+    try:
+        with open("/proc/self/task/%d/schedstat" % threading.get_native_id()) as f:
+            return int(f.read().split()[1]) / 1e6
+    except (OSError, ValueError, IndexError):
+        return 0.0
+
+
 def pawcs_run(n_frames, stream, cpu=True, channels=1):
     """PAWCS on the thermal-like 640x480 single-channel scene (channels=3: a 640x480 BGR scene of moving
     shapes on a smoothed texture): every frame through lvbgs_apply, from frames resident on the device
@@ -166,24 +176,36 @@ def pawcs_run(n_frames, stream, cpu=True, channels=1):
     for leg, frames, mask in (("device", dev, dmask), ("host", host, hmask)):
         b = BackgroundSubtractorPAWCS(seed=1)
         b.initialize(frames[0].cpu().numpy())
-        ms, rounds = [], []
+        ms, rounds, gpu_ev, waits = [], [], [], []
         for t in range(1, n):
+            # per frame: CUDA events around the frame step (its GPU time) and the calling thread's run-queue
+            # wait (time spent descheduled), to tell a slow GPU step from a descheduled host thread
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            w0 = _runqueue_wait_ms()
             t0 = time.perf_counter()
+            e0.record(stream)
             st = lib.lvbgs_apply(b.handle, C.c_void_p(frames[t].data_ptr()), 0, C.c_void_p(mask.data_ptr()), 0.0,
                                  C.c_void_p(stream.cuda_stream))
+            e1.record(stream)
             ms.append((time.perf_counter() - t0) * 1e3)
+            waits.append(_runqueue_wait_ms() - w0)
+            gpu_ev.append((e0, e1))
             if st != L.OK:
                 raise RuntimeError("PAWCS apply failed: %s" % lib.lvbgs_last_error(b.handle))
             rounds.append(b.scalars()["fixed_point_rounds"])
         b.close()
+        torch.cuda.synchronize()
+        gms = [a.elapsed_time(z) for a, z in gpu_ev]
         m = np.array(ms[9:])
         med = float(np.percentile(m, 50))
         r = {"value": W * H / (m.mean() / 1e3) / 1e6, "unit": "Mpix/s", "frames_per_s": 1e3 / m.mean(),
              "ms_per_frame": float(m.mean()), "p50_frame_ms": med,
              "p99_frame_ms": float(np.percentile(m, 99)), "rounds_mean": float(np.mean(rounds)),
              "rounds_max": int(np.max(rounds)),
-             # frames (index, ms, fixed-point rounds) that took more than three times the median
-             "slow_frames": [[t + 1, round(v, 2), int(rounds[t])] for t, v in enumerate(ms) if t >= 9 and v > 3 * med]}
+             # frames that took more than three times the median: index, wall ms, fixed-point rounds, GPU ms
+             # between CUDA events around the step, ms the calling thread waited on the run queue
+             "slow_frames": [[t + 1, round(v, 2), int(rounds[t]), round(gms[t], 2), round(waits[t], 2)]
+                             for t, v in enumerate(ms) if t >= 9 and v > 3 * med]}
         if leg == "device":
             out.update(r)
         else:
@@ -553,10 +575,10 @@ def main():
     remat = sum(b["stat_repair_rematched"] - a["stat_repair_rematched"] for a, b in zip(sc0, sc1)) / args.steps
 
     # ---- e2e through the C-ABI: host frames in, host masks out ----
-    # Pipelined (the headline): a frame precacher (lvbgs_precacher_*) whose packet is one tick (the 64
-    # frames back to back) copies each tick from host memory into a pinned slot on its worker thread
-    # (as a decoder would write it) and uploads it on its own copy stream while the previous tick
-    # computes; each tick then runs lvbgs_batch_apply on the device copies and waits for its host masks.
+    # Pipelined (the headline): a frame precacher over the pinned host ticks (lvbgs_precacher_create_host;
+    # a packet is one tick, the 64 frames back to back) uploads each tick from pinned host memory on its
+    # own copy stream while the previous tick computes; each tick then runs lvbgs_batch_apply on the
+    # device copies and waits for its host masks.
     # Precaching starts inside the timed region with an empty ring, so every timed tick's copies are
     # timed. Unpipelined (e2e.unpipelined): lvbgs_batch_apply on pinned host frames, uploads on the
     # compute stream, one wait per tick.
@@ -577,10 +599,9 @@ def main():
                 packets[k, offs[i]:offs[i] + nb].copy_(dev_frames[i][first + k].reshape(-1))
         hmasks = [torch.empty((s.cfg.height, s.cfg.width), dtype=torch.uint8, pin_memory=True) for s in synth]
         hm = [m.data_ptr() for m in hmasks]
-        hp = L.HostPackets(packets.data_ptr(), pkt_bytes, e2e_steps)
         pc = C.c_void_p()
-        check(lib.lvbgs_precacher_create(C.cast(lib.lvbgs_precache_copy_loader, C.c_void_p),
-                                         C.cast(C.pointer(hp), C.c_void_p), pkt_bytes, local, C.byref(pc)), None)
+        check(lib.lvbgs_precacher_create_host(C.c_void_p(packets.data_ptr()), pkt_bytes, e2e_steps, local,
+                                              C.byref(pc)), None)
         subs_e = make_subtractors(5000)
         hse = (C.c_void_p * n)(*[b.handle for b in subs_e])
         fr = (L.LvbgsFrame * n)()
@@ -629,9 +650,9 @@ def main():
             b.close()
         e2e = {"value": px_step * e2e_steps / el / 1e6, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": px_step, "ms_per_step": el / e2e_steps * 1e3,
-               "note": "host frames -> frame precacher (pinned slots, uploads on a copy stream overlapping the "
-                       "previous tick, started inside the timed region) -> lvbgs_batch_apply -> host masks; "
-                       "wall clock incl. one wait per tick",
+               "note": "pinned host frames -> frame precacher (uploads on a copy stream overlapping the previous "
+                       "tick, started inside the timed region) -> lvbgs_batch_apply -> host masks; wall clock "
+                       "incl. one wait per tick",
                "unpipelined": {"value": px_step * e2e_steps / el_u / 1e6, "ms_per_step": el_u / e2e_steps * 1e3,
                                "note": "pinned host frames -> lvbgs_batch_apply (uploads on the compute "
                                        "stream) -> host masks"}}

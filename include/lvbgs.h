@@ -309,6 +309,11 @@ typedef struct lvbgs_precacher_ctx* lvbgs_precacher;
 /* DataPrecacher(lDataLoaderCallback) (utils.cpp:302-308); packets are at most max_packet_bytes */
 lvbgs_status lvbgs_precacher_create(lvbgs_packet_loader loader, void* user, size_t max_packet_bytes, int device_id,
                                     lvbgs_precacher* out);
+/* a precacher over packets already in the caller's host memory: packet idx < count is the packet_bytes
+ * bytes at packets + idx * packet_bytes, uploaded from there (no loader, no copy into the ring; pinned
+ * memory for asynchronous uploads); the memory must stay valid while the precacher lives */
+lvbgs_status lvbgs_precacher_create_host(const uint8_t* packets, size_t packet_bytes, size_t count, int device_id,
+                                         lvbgs_precacher* out);
 /* ~DataPrecacher(): stops the worker, waits for the device and frees the slots */
 lvbgs_status lvbgs_precacher_destroy(lvbgs_precacher p);
 /* startAsyncPrecaching(nSuggestedBufferSize) (utils.cpp:358-374): an empty ring of

@@ -155,6 +155,7 @@ SIGNATURES = {
                                            C.POINTER(C.c_uint64), C.c_int, C.c_void_p]),
     "lvbgs_classif_metrics": (C.c_int, [C.POINTER(C.c_uint64), C.POINTER(C.c_double)]),
     "lvbgs_precacher_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int, C.POINTER(C.c_void_p)]),
+    "lvbgs_precacher_create_host": (C.c_int, [C.c_void_p, C.c_size_t, C.c_size_t, C.c_int, C.POINTER(C.c_void_p)]),
     "lvbgs_precacher_destroy": (C.c_int, [C.c_void_p]),
     "lvbgs_precacher_start": (C.c_int, [C.c_void_p, C.c_size_t]),
     "lvbgs_precacher_stop": (C.c_int, [C.c_void_p]),

@@ -34,6 +34,7 @@ struct Slot {
     uint8_t* host = nullptr;
     uint8_t* dev = nullptr;
     size_t idx = SIZE_MAX, size = 0;
+    const uint8_t* src = nullptr;  // the host copy of the packet (the slot's buffer or the caller's memory)
     enum State { FREE, LOADING, READY, HANDED } state = FREE;
     cudaEvent_t ready = nullptr, release = nullptr;
     bool released = false;  // `release` holds the last consumer use of the device buffer
@@ -44,6 +45,10 @@ struct Slot {
 struct lvbgs_precacher_ctx {
     lvbgs_packet_loader loader = nullptr;
     void* user = nullptr;
+    // packets already in the caller's host memory (lvbgs_precacher_create_host): uploaded from there,
+    // with no loader and no host slots
+    const uint8_t* direct = nullptr;
+    size_t directCount = 0;
     size_t cap = 0;
     int device = 0;
     std::vector<Slot> slots;
@@ -89,7 +94,7 @@ void free_slots(lvbgs_precacher p) {
 lvbgs_status alloc_slots(lvbgs_precacher p, int n) {
     p->slots.resize((size_t)n);
     for (Slot& s : p->slots) {
-        if (cudaHostAlloc((void**)&s.host, p->cap, cudaHostAllocDefault) != cudaSuccess ||
+        if ((!p->direct && cudaHostAlloc((void**)&s.host, p->cap, cudaHostAllocDefault) != cudaSuccess) ||
             cudaMalloc(&s.dev, p->cap) != cudaSuccess ||
             cudaEventCreateWithFlags(&s.ready, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&s.release, cudaEventDisableTiming) != cudaSuccess) {
@@ -140,13 +145,21 @@ void lvbgs_precacher_ctx::run() {
         s.state = Slot::LOADING;
         s.idx = idx;
         lk.unlock();
-        // the host buffer's previous upload has finished long before a slot is free again; wait for it anyway
-        cudaEventSynchronize(s.ready);
-        const size_t size = loader(user, idx, s.host, cap);
+        size_t size;
+        const uint8_t* src;
+        if (direct) {
+            size = idx < directCount ? cap : 0;
+            src = direct + idx * cap;
+        } else {
+            // the host buffer's previous upload has finished long before a slot is free again; wait for it anyway
+            cudaEventSynchronize(s.ready);
+            size = loader(user, idx, s.host, cap);
+            src = s.host;
+        }
         cudaError_t e = cudaSuccess;
         if (size != 0 && size <= cap) {
             if (s.released) e = cudaStreamWaitEvent(copy, s.release, 0);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(s.dev, s.host, size, cudaMemcpyHostToDevice, copy);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(s.dev, src, size, cudaMemcpyHostToDevice, copy);
             if (e == cudaSuccess) e = cudaEventRecord(s.ready, copy);
         }
         lk.lock();
@@ -164,6 +177,7 @@ void lvbgs_precacher_ctx::run() {
             break;
         } else {
             s.size = size;
+            s.src = src;
             s.state = Slot::READY;
         }
         cvReady.notify_all();
@@ -202,6 +216,35 @@ lvbgs_status lvbgs_precacher_create(lvbgs_packet_loader loader, void* user, size
         return pfail(nullptr, LVBGS_DEVICE_ERROR, "stream creation failed");
     }
     // one slot for requests made while precaching is off
+    lvbgs_status s = alloc_slots(p, 1);
+    if (s != LVBGS_OK) {
+        cudaStreamDestroy(p->copy);
+        delete p;
+        return s;
+    }
+    *out = p;
+    return LVBGS_OK;
+}
+
+lvbgs_status lvbgs_precacher_create_host(const uint8_t* packets, size_t packet_bytes, size_t count, int device_id,
+                                         lvbgs_precacher* out) {
+    if (!out) return pfail(nullptr, LVBGS_BAD_ARG, "null output");
+    *out = nullptr;
+    if (!packets || packet_bytes == 0) return pfail(nullptr, LVBGS_BAD_ARG, "packets and a positive packet size are required");
+    if (cudaSetDevice(device_id) != cudaSuccess) {
+        cudaGetLastError();
+        return pfail(nullptr, LVBGS_DEVICE_ERROR, "cannot select the CUDA device");
+    }
+    lvbgs_precacher p = new lvbgs_precacher_ctx();
+    p->direct = packets;
+    p->directCount = count;
+    p->cap = packet_bytes;
+    p->device = device_id;
+    if (cudaStreamCreateWithFlags(&p->copy, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete p;
+        return pfail(nullptr, LVBGS_DEVICE_ERROR, "stream creation failed");
+    }
     lvbgs_status s = alloc_slots(p, 1);
     if (s != LVBGS_OK) {
         cudaStreamDestroy(p->copy);
@@ -309,7 +352,7 @@ lvbgs_status lvbgs_precacher_get(lvbgs_precacher p, size_t idx, void* cuda_strea
             return pfail(p, LVBGS_DEVICE_ERROR, "cannot order the caller's stream after the packet upload");
         }
         if (device_packet) *device_packet = s.dev;
-        if (host_packet) *host_packet = s.host;
+        if (host_packet) *host_packet = s.src;
         *size = s.size;
         p->lastReq = idx;
         return LVBGS_OK;
@@ -329,8 +372,15 @@ lvbgs_status lvbgs_precacher_get(lvbgs_precacher p, size_t idx, void* cuda_strea
         // no precaching (utils.cpp:320-325): load into the single slot, synchronously
         Slot& s = p->slots[0];
         lk.unlock();
-        cudaEventSynchronize(s.ready);  // the host buffer's last upload
-        const size_t n = p->loader(p->user, idx, s.host, p->cap);
+        size_t n;
+        if (p->direct) {
+            n = idx < p->directCount ? p->cap : 0;
+            s.src = p->direct + idx * p->cap;
+        } else {
+            cudaEventSynchronize(s.ready);  // the host buffer's last upload
+            n = p->loader(p->user, idx, s.host, p->cap);
+            s.src = s.host;
+        }
         lk.lock();
         if (n > p->cap) return pfail(p, LVBGS_BAD_ARG, "the loader returned a packet larger than the precacher's packet capacity");
         s.size = n;
@@ -343,7 +393,7 @@ lvbgs_status lvbgs_precacher_get(lvbgs_precacher p, size_t idx, void* cuda_strea
             return LVBGS_OK;
         }
         if ((s.released && cudaStreamWaitEvent(p->copy, s.release, 0) != cudaSuccess) ||
-            cudaMemcpyAsync(s.dev, s.host, n, cudaMemcpyHostToDevice, p->copy) != cudaSuccess ||
+            cudaMemcpyAsync(s.dev, s.src, n, cudaMemcpyHostToDevice, p->copy) != cudaSuccess ||
             cudaEventRecord(s.ready, p->copy) != cudaSuccess) {
             cudaGetLastError();
             return pfail(p, LVBGS_DEVICE_ERROR, "packet upload failed");

@@ -109,3 +109,33 @@ def test_argument_checks():
     arr = packets(3, 1000)
     with pytest.raises(LvException):
         DataPrecacher(arr, max_packet_bytes=10).getPacket(0)  # the packets do not fit the capacity
+
+
+def test_packets_in_pinned_host_memory_are_uploaded_in_place():
+    import torch
+    arr = packets(30, 123_456, seed=3)
+    pinned = torch.from_numpy(arr).pin_memory()
+    h = C.c_void_p()
+    assert L.lib().lvbgs_precacher_create_host(C.c_void_p(pinned.data_ptr()), arr.shape[1], arr.shape[0], 0,
+                                               C.byref(h)) == L.OK
+    dp, hp, sz = C.c_void_p(), C.c_void_p(), C.c_size_t()
+
+    class Pkt:
+        def __init__(self):
+            self.nbytes = sz.value
+
+        def data_ptr(self):
+            return dp.value
+
+    for start in (False, True):
+        if start:
+            assert L.lib().lvbgs_precacher_start(h, 3 * arr.shape[1]) == L.OK
+        for i in list(range(12)) + [20, 21, 5, 29]:
+            assert L.lib().lvbgs_precacher_get(h, i, None, C.byref(dp), C.byref(hp), C.byref(sz)) == L.OK
+            assert sz.value == arr.shape[1]
+            # the host copy is the caller's own memory
+            assert hp.value == pinned.data_ptr() + i * arr.shape[1]
+            assert np.array_equal(device_bytes(Pkt()), arr[i]), (start, i)
+        assert L.lib().lvbgs_precacher_get(h, 30, None, C.byref(dp), C.byref(hp), C.byref(sz)) == L.OK
+        assert sz.value == 0
+    assert L.lib().lvbgs_precacher_destroy(h) == L.OK
