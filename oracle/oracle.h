@@ -1,8 +1,9 @@
 /* ORACLE (test infrastructure only; never linked into the product library).
  *
- * CPU restatement of the reference's SuBSENSE, PAWCS, LOBSTER and ViBe per-pixel background
+ * CPU restatement of the reference's SuBSENSE, PAWCS, LOBSTER, ViBe and PBAS per-pixel background
  * subtraction (plstcharles/litiv, modules/video/src/BackgroundSubtractorSuBSENSE.cpp,
- * BackgroundSubtractorPAWCS.cpp, BackgroundSubtractorLOBSTER.cpp, BackgroundSubtractorViBe.cpp) and of
+ * BackgroundSubtractorPAWCS.cpp, BackgroundSubtractorLOBSTER.cpp, BackgroundSubtractorViBe.cpp,
+ * BackgroundSubtractorPBAS.cpp) and of
  * the LBSP descriptor
  * (modules/features2d/include/litiv/features2d/LBSP.hpp).
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it,
@@ -10,7 +11,7 @@
  *
  * Parity pins: the LBSP descriptor is pinned by the reference's golden vector
  * (modules/features2d/test/data/test_lbsp.bin, see tests/golden/). The SuBSENSE and PAWCS
- * (and LOBSTER, ViBe) restatements are pinned to the reference itself: oracle/refshim/build_ref.py compiles the
+ * (and LOBSTER, ViBe, PBAS) restatements are pinned to the reference itself: oracle/refshim/build_ref.py compiles the
  * reference's own modules/video/src sources (against a project-written OpenCV stand-in, with rand()
  * routed to the same generator) into oracle/_ref/libref.so, which exposes this same API (rsub_* /
  * rpawcs_*), and tests/test_oracle_reference.py compares every map bit for bit. The OpenCV image
@@ -218,6 +219,33 @@ int ovibe_get_background(const ovibe_t* o, uint8_t* out); /* :33-48 */
 const void* ovibe_samples(const ovibe_t* o, size_t* nbytes);
 /* apply() calls, samples evaluated, sample writes */
 void ovibe_get_stats(const ovibe_t* o, uint64_t out[3]);
+
+/* ---- PBAS (modules/video/src/BackgroundSubtractorPBAS.cpp: _1ch for one channel, _3ch for three) ---- */
+typedef struct opbas opbas_t;
+typedef struct {
+    size_t color_dist_threshold; /* BGSPBAS_DEFAULT_COLOR_DIST_THRESHOLD = 30 */
+    float update_rate;           /* BGSPBAS_DEFAULT_LEARNING_RATE = 16 */
+    size_t bg_samples;           /* BGSPBAS_DEFAULT_NB_BG_SAMPLES = 35 */
+    size_t required_bg_samples;  /* BGSPBAS_DEFAULT_REQUIRED_NB_BG_SAMPLES = 2 */
+    uint64_t seed;
+} opbas_params;
+enum { OPBAS_MAP_SAMPLE_COLOR = 0, OPBAS_MAP_SAMPLE_GRAD, /* uint8 [N][H*W*C] */
+       OPBAS_MAP_R, OPBAS_MAP_T, OPBAS_MAP_D,            /* float [H*W] */
+       OPBAS_MAP_GRAD,                                   /* uint8 [H*W*C]: the last frame's gradient image */
+       OPBAS_MAP_COUNT };
+void opbas_default_params(opbas_params* p);
+opbas_t* opbas_create(const opbas_params* p);
+void opbas_destroy(opbas_t* o);
+/* initialize (BackgroundSubtractorPBAS.cpp:61-109 / :287-324) */
+int opbas_initialize(opbas_t* o, const uint8_t* img, int width, int height, int channels);
+/* apply (:111-281 / :326-496); learning_rate_override <= 0 uses T(x) (the reference's default is -1) */
+int opbas_apply(opbas_t* o, const uint8_t* img, uint8_t* fgmask, double learning_rate_override);
+int opbas_get_background(const opbas_t* o, uint8_t* out); /* :36-51 */
+const void* opbas_map(const opbas_t* o, int which, size_t* nbytes);
+/* m_fFormerMeanGradDist */
+float opbas_mean_grad(const opbas_t* o);
+/* the gradient image of a frame (GaussianBlur 3x3, Scharr, convertScaleAbs, addWeighted) */
+void opbas_gradient(const uint8_t* img, int width, int height, int channels, uint8_t* out);
 
 /* CPU baseline for LOBSTER: as orun_streams (apply phase timed, learning rate 16) */
 double orun_lobster_streams(int n_streams, const uint8_t* const* frames, const int* n_frames,

@@ -1,5 +1,5 @@
 """ORACLE (test infrastructure only): ctypes wrapper of oracle/_build/liboracle.so (the C
-restatement of the reference's SuBSENSE, PAWCS, LOBSTER and ViBe, "port") and of oracle/_ref/libref.so (the reference's own SuBSENSE /
+restatement of the reference's SuBSENSE, PAWCS, LOBSTER, ViBe and PBAS, "port") and of oracle/_ref/libref.so (the reference's own SuBSENSE /
 PAWCS sources compiled against the project-written OpenCV stand-in, "reference"; built only where
 the reference sources are present, see oracle/refshim/build_ref.py). Both expose the same C API,
 so OracleSuBSENSE / OraclePAWCS drive either one (``impl=``).
@@ -81,6 +81,14 @@ class LScalars(C.Structure):
 LOBSTER_MAP_NAMES = ["LAST_FG", "ROI", "LAST_COLOR", "LAST_DESC", "SAMPLE_COLOR", "SAMPLE_DESC", "LUT"]
 
 
+class BParams(C.Structure):
+    _fields_ = [("color_dist_threshold", C.c_size_t), ("update_rate", C.c_float), ("bg_samples", C.c_size_t),
+                ("required_bg_samples", C.c_size_t), ("seed", C.c_uint64)]
+
+
+PBAS_MAP_NAMES = ["SAMPLE_COLOR", "SAMPLE_GRAD", "R", "T", "D", "GRAD"]
+
+
 class VParams(C.Structure):
     _fields_ = [("color_dist_threshold", C.c_size_t), ("bg_samples", C.c_size_t),
                 ("required_bg_samples", C.c_size_t), ("seed", C.c_uint64)]
@@ -126,6 +134,16 @@ def ref_lib():
         L.rsub_map.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]
         L.rpawcs_refresh_model.argtypes = [C.c_void_p, C.c_size_t, C.c_float, C.c_int]
         L.rlob_refresh_model.argtypes = [C.c_void_p, C.c_float, C.c_int]
+        L.rpbas_create.restype = C.c_void_p
+        L.rpbas_create.argtypes = [C.POINTER(BParams)]
+        L.rpbas_destroy.argtypes = [C.c_void_p]
+        L.rpbas_initialize.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int]
+        L.rpbas_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
+        L.rpbas_get_background.argtypes = [C.c_void_p, C.c_void_p]
+        L.rpbas_map.restype = C.c_void_p
+        L.rpbas_map.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]
+        L.rpbas_mean_grad.restype = C.c_float
+        L.rpbas_mean_grad.argtypes = [C.c_void_p]
         L.rvibe_create.restype = C.c_void_p
         L.rvibe_create.argtypes = [C.POINTER(VParams)]
         L.rvibe_destroy.argtypes = [C.c_void_p]
@@ -230,6 +248,18 @@ def lib():
         L.ovibe_samples.restype = C.c_void_p
         L.ovibe_samples.argtypes = [C.c_void_p, C.POINTER(C.c_size_t)]
         L.ovibe_get_stats.argtypes = [C.c_void_p, C.POINTER(C.c_uint64)]
+        L.opbas_default_params.argtypes = [C.POINTER(BParams)]
+        L.opbas_create.restype = C.c_void_p
+        L.opbas_create.argtypes = [C.POINTER(BParams)]
+        L.opbas_destroy.argtypes = [C.c_void_p]
+        L.opbas_initialize.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int]
+        L.opbas_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
+        L.opbas_get_background.argtypes = [C.c_void_p, C.c_void_p]
+        L.opbas_map.restype = C.c_void_p
+        L.opbas_map.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]
+        L.opbas_mean_grad.restype = C.c_float
+        L.opbas_mean_grad.argtypes = [C.c_void_p]
+        L.opbas_gradient.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
         L.orun_lobster_streams.restype = C.c_double
         L.orun_lobster_streams.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                            C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_uint64), C.c_int]
@@ -573,6 +603,86 @@ class OracleViBe:
         out = (C.c_uint64 * 3)()
         lib().ovibe_get_stats(self._o, out)
         return list(out)
+
+
+class OraclePBAS:
+    """Sequential CPU PBAS (the checker): the C restatement (impl="port") or the reference's own
+    BackgroundSubtractorPBAS_1ch / _3ch (impl="reference"), chosen by the frame's channel count.
+    apply()'s learning rate override defaults to BGSPBAS_DEFAULT_LEARNING_RATE_OVERRIDE (-1: T(x))."""
+
+    def __init__(self, seed=0, impl="port", **params):
+        p = BParams()
+        lib().opbas_default_params(C.byref(p))
+        p.seed = seed
+        for k, v in params.items():
+            setattr(p, k, v)
+        self.params = p
+        self.impl = impl
+        self._a = _Api(impl, "opbas_", "rpbas_")
+        self._o = self._a.create(C.byref(p))
+        if not self._o:
+            raise ValueError("invalid oracle parameters")
+        self.shape = None
+
+    def close(self):
+        if self._o:
+            self._a.destroy(self._o)
+            self._o = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def initialize(self, img):
+        img = np.ascontiguousarray(img, np.uint8)
+        H, W = img.shape[:2]
+        Cc = img.shape[2] if img.ndim == 3 else 1
+        if self._a.initialize(self._o, img.ctypes.data_as(C.c_void_p), W, H, Cc) != 0:
+            raise ValueError("oracle initialize failed")
+        self.shape = (H, W, Cc)
+
+    def apply(self, img, lr=-1.0):
+        img = np.ascontiguousarray(img, np.uint8)
+        H, W, _ = self.shape
+        mask = np.empty((H, W), np.uint8)
+        if self._a.apply(self._o, img.ctypes.data_as(C.c_void_p), mask.ctypes.data_as(C.c_void_p), float(lr)) != 0:
+            raise ValueError("oracle apply failed")
+        return mask
+
+    def background(self):
+        H, W, Cc = self.shape
+        out = np.empty((H, W, Cc) if Cc > 1 else (H, W), np.uint8)
+        self._a.get_background(self._o, out.ctypes.data_as(C.c_void_p))
+        return out
+
+    def state_map(self, name):
+        """SAMPLE_COLOR / SAMPLE_GRAD (uint8 [N, H, W(, C)]), R / T / D (float32 [H, W]); GRAD (the
+        port only: the last frame's gradient image)"""
+        n = C.c_size_t()
+        ptr = self._a.map(self._o, PBAS_MAP_NAMES.index(name), C.byref(n))
+        raw = np.ctypeslib.as_array((C.c_uint8 * n.value).from_address(ptr)).copy()
+        H, W, Cc = self.shape
+        tail = (H, W, Cc) if Cc > 1 else (H, W)
+        if name in ("R", "T", "D"):
+            return raw.view(np.float32).reshape(H, W)
+        if name == "GRAD":
+            return raw.reshape(tail)
+        return raw.reshape((-1,) + tail)
+
+    def mean_grad(self):
+        return self._a.mean_grad(self._o)
+
+
+def pbas_gradient(img):
+    """The port's gradient image of a frame (GaussianBlur 3x3, Scharr, convertScaleAbs, addWeighted)"""
+    img = np.ascontiguousarray(img, np.uint8)
+    H, W = img.shape[:2]
+    Cc = img.shape[2] if img.ndim == 3 else 1
+    out = np.empty(img.shape, np.uint8)
+    lib().opbas_gradient(img.ctypes.data_as(C.c_void_p), W, H, Cc, out.ctypes.data_as(C.c_void_p))
+    return out
 
 
 def lbsp_compute2(img, abs_threshold=None, rel_threshold=0.333, offset=0, out=None):

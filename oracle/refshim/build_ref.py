@@ -1,5 +1,5 @@
 """ORACLE build recipe (test infrastructure only): compiles the REFERENCE's own SuBSENSE / PAWCS / LOBSTER /
-ViBe sources into oracle/_ref/libref.so, for the CPU tests that pin the C restatement (oracle/*.c) to the
+ViBe / PBAS sources into oracle/_ref/libref.so, for the CPU tests that pin the C restatement (oracle/*.c) to the
 reference itself.
 
 The reference is a CMake project that needs OpenCV; neither CMake's configure step nor OpenCV is
@@ -8,7 +8,7 @@ used here. Instead:
 * the reference sources are compiled unmodified, from where they lie:
   modules/video/src/BackgroundSubtractionUtils.cpp, BackgroundSubtractorLBSP.cpp,
   BackgroundSubtractorSuBSENSE.cpp, BackgroundSubtractorPAWCS.cpp, BackgroundSubtractorLOBSTER.cpp,
-  BackgroundSubtractorViBe.cpp, with
+  BackgroundSubtractorViBe.cpp, BackgroundSubtractorPBAS.cpp, with
   the reference's own headers (BackgroundSubtractionUtils.hpp, BackgroundSubtractorLBSP.hpp,
   BackgroundSubtractorSuBSENSE.hpp, BackgroundSubtractorPAWCS.hpp, BackgroundSubtractorLOBSTER.hpp, features2d LBSP.hpp, utils algo.hpp, math.hpp, cxx.hpp, simd.hpp,
   platform.hpp, console.hpp);
@@ -23,9 +23,10 @@ used here. Instead:
   image operations the path calls, written from OpenCV's documented semantics with the same
   definitions as the C restatement (oracle/common.h);
 * ``rand()`` is routed to the counter-based generator (oracle/refshim/lvshim_rand.h, force-included;
-  for ViBe also oracle/refshim/lvshim_rand_xy.h, which attributes its draws to the loop's pixel);
+  for ViBe and PBAS also oracle/refshim/lvshim_rand_xy.h, which attributes their draws to the loop's pixel);
 * oracle/refshim/ref_bridge.cpp exposes the reference classes through the same C API as the
-  restatement (rsub_* / rpawcs_* / rlob_* / rvibe_* beside osub_* / opawcs_* / olob_* / ovibe_*).
+  restatement (rsub_* / rpawcs_* / rlob_* / rvibe_* / rpbas_* beside osub_* / opawcs_* / olob_* / ovibe_* /
+  opbas_*).
 
 Run: python oracle/refshim/build_ref.py [reference root]. Outputs go to oracle/_ref/ only. The
 reference root defaults to /root/reference; without it nothing is built (the GPU parity tests do not
@@ -48,7 +49,7 @@ SOURCES = ["modules/video/src/BackgroundSubtractionUtils.cpp",
            "modules/video/src/BackgroundSubtractorPAWCS.cpp",
            "modules/video/src/BackgroundSubtractorLOBSTER.cpp"]
 # compiled on its own with lvshim_rand_xy.h as well (its pixel loops name the pixel (x, y) / (x_orig, y_orig))
-XY_SOURCES = ["modules/video/src/BackgroundSubtractorViBe.cpp"]
+XY_SOURCES = ["modules/video/src/BackgroundSubtractorViBe.cpp", "modules/video/src/BackgroundSubtractorPBAS.cpp"]
 INCLUDES = ["modules/video/include", "modules/features2d/include", "modules/utils/include"]
 SHIM_SOURCES = ["ref_bridge.cpp", "lv_support.cpp"]
 

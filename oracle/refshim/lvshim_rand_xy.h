@@ -1,6 +1,6 @@
 /* ORACLE (test infrastructure only): force-included after lvshim_rand.h for
- * modules/video/src/BackgroundSubtractorViBe.cpp alone. Its pixel loops declare no nPxIter: they name
- * the pixel (x, y) in apply() and (x_orig, y_orig) in initialize(). The namespace-scope sentinels below
+ * modules/video/src/BackgroundSubtractorViBe.cpp and BackgroundSubtractorPBAS.cpp alone. Their pixel loops
+ * declare no nPxIter: they name the pixel (x, y) (ViBe's initialize(): (x_orig, y_orig)). The namespace-scope sentinels below
  * carry those names, so inside a loop the loop variables shadow them and rand() is attributed to the
  * loop's pixel (the same keying as the other algorithms: draw k of pixel p in frame t). */
 #ifndef LV_ORACLE_SHIM_RAND_XY_H

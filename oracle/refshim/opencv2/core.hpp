@@ -46,6 +46,7 @@ typedef unsigned short ushort;
 #define CV_16UC1 CV_16UC(1)
 #define CV_16UC3 CV_16UC(3)
 #define CV_16UC4 CV_16UC(4)
+#define CV_16SC(n) CV_MAKETYPE(CV_16S, (n))
 #define CV_32SC(n) CV_MAKETYPE(CV_32S, (n))
 #define CV_32SC1 CV_32SC(1)
 #define CV_32FC(n) CV_MAKETYPE(CV_32F, (n))
@@ -522,9 +523,25 @@ inline void bitwise_not(InputArray a_, OutputArray d_) {
 // dst = src1*alpha + src2*beta + gamma. The restated case is src1 CV_32F, src2 CV_8U, dtype CV_32F:
 // src2 is converted to float and the sum is taken in float with float weights, each product
 // rounded separately (no fused multiply-add), as oracle/common.h add_weighted_mask.
+// Two CV_8U sources with an 8-bit output: saturate(src1*alpha + src2*beta + gamma) in float, rounded
+// half to even (the pairs PBAS adds, weights 0.5 and 0.5, give exact halves).
 inline void addWeighted(InputArray s1_, double alpha, InputArray s2_, double beta, double gamma, OutputArray d_,
                         int dtype = -1) {
     const Mat s1 = s1_.getMat(), s2 = s2_.getMat();
+    if (s1.depth() == CV_8U && s2.depth() == CV_8U && (dtype < 0 || CV_MAT_DEPTH(dtype) == CV_8U)) {
+        const float fa = (float)alpha, fb = (float)beta, fg = (float)gamma;
+        Mat out(s1.rows, s1.cols, s1.type());
+        for (int y = 0; y < s1.rows; ++y)
+            for (int i = 0; i < s1.cols * s1.channels(); ++i) {
+                const float v = ((float)s1.ptr(y)[i] * fa + (float)s2.ptr(y)[i] * fb) + fg;
+                const float r = std::nearbyint(v);
+                out.ptr(y)[i] = (uchar)(r < 0.f ? 0.f : r > 255.f ? 255.f : r);
+            }
+        Mat& d = d_.getMatRef();
+        d.create(s1.rows, s1.cols, s1.type());
+        out.copyTo(d);
+        return;
+    }
     if (s1.depth() != CV_32F || (dtype >= 0 && CV_MAT_DEPTH(dtype) != CV_32F))
         throw std::runtime_error("addWeighted: only CV_32F outputs are supported");
     const float fa = (float)alpha, fb = (float)beta, fg = (float)gamma;

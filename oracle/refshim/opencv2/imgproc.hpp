@@ -120,6 +120,87 @@ inline int floodFill(InputOutputArray image, Point seed, Scalar newVal) {
     return n;
 }
 
+// BORDER_REFLECT_101 index (OpenCV's BORDER_DEFAULT): -1 -> 1, n -> n-2
+inline int border_reflect101(int i, int n) {
+    if (n == 1) return 0;
+    while (i < 0 || i >= n) i = i < 0 ? -i : 2 * n - 2 - i;
+    return i;
+}
+
+// cv::GaussianBlur of 8-bit images, 3x3 kernel, sigma 0, BORDER_DEFAULT: the kernel [1 2 1]/4 in both
+// directions, whose 8-bit result is the exact weighted sum rounded half up: (sum(w*p) + 8) >> 4
+inline void GaussianBlur(InputArray src_, OutputArray dst_, Size ksize, double sigmaX, double sigmaY = 0,
+                         int borderType = BORDER_DEFAULT) {
+    const Mat src = src_.getMat();
+    if (src.depth() != CV_8U || ksize.width != 3 || ksize.height != 3 || sigmaX != 0 || sigmaY != 0 ||
+        borderType != BORDER_DEFAULT)
+        throw std::runtime_error("GaussianBlur: 8-bit, 3x3, sigma 0, BORDER_DEFAULT only");
+    const int W = src.cols, H = src.rows, C = src.channels();
+    static const int w[3] = {1, 2, 1};
+    Mat out(H, W, src.type());
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x)
+            for (int c = 0; c < C; ++c) {
+                int acc = 0;
+                for (int j = -1; j <= 1; ++j)
+                    for (int i = -1; i <= 1; ++i)
+                        acc += w[j + 1] * w[i + 1] * src.ptr(border_reflect101(y + j, H))[border_reflect101(x + i, W) * C + c];
+                out.ptr(y)[x * C + c] = (uchar)((acc + 8) >> 4);
+            }
+    Mat& dst = dst_.getMatRef();
+    dst.create(H, W, src.type());
+    out.copyTo(dst);
+}
+
+// cv::Scharr of an 8-bit image into CV_16S (dx = 1, dy = 0: [-3 0 3; -10 0 10; -3 0 3]; dx = 0, dy = 1:
+// its transpose), scale 1, delta 0, BORDER_DEFAULT
+inline void Scharr(InputArray src_, OutputArray dst_, int ddepth, int dx, int dy, double scale = 1, double delta = 0,
+                   int borderType = BORDER_DEFAULT) {
+    const Mat src = src_.getMat();
+    if (src.depth() != CV_8U || ddepth != CV_16S || dx + dy != 1 || scale != 1 || delta != 0 ||
+        borderType != BORDER_DEFAULT)
+        throw std::runtime_error("Scharr: 8-bit into CV_16S, first derivative, scale 1, BORDER_DEFAULT only");
+    const int W = src.cols, H = src.rows, C = src.channels();
+    static const int ws[3] = {3, 10, 3};
+    Mat out(H, W, CV_16SC(C));
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x)
+            for (int c = 0; c < C; ++c) {
+                int g = 0;
+                for (int k = -1; k <= 1; ++k) {
+                    if (dx) {
+                        const uchar* row = src.ptr(border_reflect101(y + k, H));
+                        g += ws[k + 1] * ((int)row[border_reflect101(x + 1, W) * C + c] -
+                                          (int)row[border_reflect101(x - 1, W) * C + c]);
+                    } else {
+                        const int xx = border_reflect101(x + k, W) * C + c;
+                        g += ws[k + 1] * ((int)src.ptr(border_reflect101(y + 1, H))[xx] -
+                                          (int)src.ptr(border_reflect101(y - 1, H))[xx]);
+                    }
+                }
+                out.ptr<short>(y)[x * C + c] = (short)g;
+            }
+    Mat& dst = dst_.getMatRef();
+    dst.create(H, W, CV_16SC(C));
+    out.copyTo(dst);
+}
+
+// cv::convertScaleAbs of a CV_16S image (alpha 1, beta 0): |v| saturated to 255
+inline void convertScaleAbs(InputArray src_, OutputArray dst_, double alpha = 1, double beta = 0) {
+    const Mat src = src_.getMat();
+    if (src.depth() != CV_16S || alpha != 1 || beta != 0) throw std::runtime_error("convertScaleAbs: CV_16S, alpha 1, beta 0 only");
+    const int C = src.channels();
+    Mat out(src.rows, src.cols, CV_8UC(C));
+    for (int y = 0; y < src.rows; ++y)
+        for (int i = 0; i < src.cols * C; ++i) {
+            const int v = std::abs((int)src.ptr<short>(y)[i]);
+            out.ptr(y)[i] = (uchar)(v > 255 ? 255 : v);
+        }
+    Mat& dst = dst_.getMatRef();
+    dst.create(src.rows, src.cols, CV_8UC(C));
+    out.copyTo(dst);
+}
+
 // cv::cvtColor for COLOR_GRAY2BGR only: the single channel repeated into three (8UC1 -> 8UC3)
 inline void cvtColor(InputArray src_, OutputArray dst_, int code) {
     const Mat src = src_.getMat();

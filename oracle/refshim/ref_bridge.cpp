@@ -1,10 +1,12 @@
 // ORACLE (test infrastructure only): C API over the REFERENCE's own BackgroundSubtractorSuBSENSE,
-// BackgroundSubtractorPAWCS, BackgroundSubtractorLOBSTER and BackgroundSubtractorViBe classes (compiled from the reference's sources by
+// BackgroundSubtractorPAWCS, BackgroundSubtractorLOBSTER, BackgroundSubtractorViBe and BackgroundSubtractorPBAS
+// classes (compiled from the reference's sources by
 // oracle/refshim/build_ref.py), with the same signatures and state layouts as the C restatement's
 // osub_* / opawcs_* (oracle/oracle.h), so that the tests can run both on the same frames and compare
 // every map bit for bit. Built into oracle/_ref/libref.so, which only the CPU tests load.
 #include "litiv/video/BackgroundSubtractorLOBSTER.hpp"
 #include "litiv/video/BackgroundSubtractorPAWCS.hpp"
+#include "litiv/video/BackgroundSubtractorPBAS.hpp"
 #include "litiv/video/BackgroundSubtractorSuBSENSE.hpp"
 #include "litiv/video/BackgroundSubtractorViBe.hpp"
 #include "oracle.h"
@@ -226,6 +228,38 @@ struct RefVibe {
     const std::vector<cv::Mat>& samples() const {
         return C == 1 ? static_cast<const RefVibeT<BackgroundSubtractorViBe_1ch>*>(algo.get())->samples()
                       : static_cast<const RefVibeT<BackgroundSubtractorViBe_3ch>*>(algo.get())->samples();
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// PBAS: BackgroundSubtractorPBAS_1ch / _3ch, made at initialize() like ViBe's
+// ---------------------------------------------------------------------------------------------
+template <typename B>
+struct RefPbasT : B {
+    using B::B;
+    const std::vector<cv::Mat>& colours() const { return this->m_voBGImg; }
+    const std::vector<cv::Mat>& grads() const { return this->m_voBGGrad; }
+    const cv::Mat& map(int which) const {
+        return which == OPBAS_MAP_R ? this->m_oDistThresholdFrame
+                                    : which == OPBAS_MAP_T ? this->m_oUpdateRateFrame : this->m_oMeanMinDistFrame;
+    }
+    float meanGrad() const { return this->m_fFormerMeanGradDist; }
+};
+struct RefPbas {
+    opbas_params p;
+    RngCtx rng;
+    size_t frames = 0;
+    int W = 0, H = 0, C = 0;
+    std::unique_ptr<BackgroundSubtractorPBAS> algo;
+    std::vector<uint8_t> exported;
+    explicit RefPbas(const opbas_params& q) : p(q) {
+        rng.seed = q.seed;
+        rng.frame = &frames;
+    }
+    template <typename F>
+    auto with(F&& f) const {
+        return C == 1 ? f(static_cast<const RefPbasT<BackgroundSubtractorPBAS_1ch>*>(algo.get()))
+                      : f(static_cast<const RefPbasT<BackgroundSubtractorPBAS_3ch>*>(algo.get()));
     }
 };
 
@@ -649,6 +683,71 @@ const void* rvibe_samples(void* h, size_t* nbytes) {
     for (const cv::Mat& s : o->samples()) append_mat<uint8_t>(o->exported, s);
     *nbytes = o->exported.size();
     return o->exported.data();
+}
+
+// ---- PBAS: the reference's BackgroundSubtractorPBAS_1ch / _3ch (BackgroundSubtractorPBAS.cpp) ----
+void* rpbas_create(const opbas_params* p) {
+    if (!p || p->bg_samples == 0 || p->required_bg_samples > p->bg_samples) return nullptr;
+    return new RefPbas(*p);
+}
+void rpbas_destroy(void* h) { delete (RefPbas*)h; }
+int rpbas_initialize(void* h, const uint8_t* img, int W, int H, int C) {
+    RefPbas* o = (RefPbas*)h;
+    if (C != 1 && C != 3) return OSUB_EUNSUPPORTED;
+    o->frames = 0;
+    o->rng.start_frame((size_t)W * H);
+    return guarded(o->rng, [&] {
+        if (C == 1)
+            o->algo.reset(new RefPbasT<BackgroundSubtractorPBAS_1ch>(o->p.color_dist_threshold, o->p.update_rate,
+                                                                     o->p.bg_samples, o->p.required_bg_samples));
+        else
+            o->algo.reset(new RefPbasT<BackgroundSubtractorPBAS_3ch>(o->p.color_dist_threshold, o->p.update_rate,
+                                                                     o->p.bg_samples, o->p.required_bg_samples));
+        o->W = W;
+        o->H = H;
+        o->C = C;
+        o->algo->initialize(cv::Mat(H, W, mat_type(C), (void*)img));
+    });
+}
+int rpbas_apply(void* h, const uint8_t* img, uint8_t* mask, double lr) {
+    RefPbas* o = (RefPbas*)h;
+    if (!o->algo) return OSUB_ENOTINIT;
+    ++o->frames;
+    o->rng.start_frame((size_t)o->W * o->H);
+    cv::Mat m(o->H, o->W, mat_type(o->C), (void*)img);
+    cv::Mat out(o->H, o->W, CV_8UC1, (void*)mask);
+    return guarded(o->rng, [&] { o->algo->apply(m, out, lr); });
+}
+int rpbas_get_background(void* h, uint8_t* out) {
+    RefPbas* o = (RefPbas*)h;
+    if (!o->algo) return OSUB_ENOTINIT;
+    cv::Mat bg;
+    const int rc = guarded(o->rng, [&] { o->algo->getBackgroundImage(bg); });
+    if (rc == OSUB_OK) std::memcpy(out, bg.data, bg.total() * bg.elemSize());
+    return rc;
+}
+const void* rpbas_map(void* h, int which, size_t* nbytes) {
+    RefPbas* o = (RefPbas*)h;
+    o->exported.clear();
+    if (!o->algo || which == OPBAS_MAP_GRAD) {
+        *nbytes = 0;
+        return nullptr;
+    }
+    o->with([&](auto* a) {
+        if (which == OPBAS_MAP_SAMPLE_COLOR)
+            for (const cv::Mat& s : a->colours()) append_mat<uint8_t>(o->exported, s);
+        else if (which == OPBAS_MAP_SAMPLE_GRAD)
+            for (const cv::Mat& s : a->grads()) append_mat<uint8_t>(o->exported, s);
+        else
+            append_mat<uint8_t>(o->exported, a->map(which));
+        return 0;
+    });
+    *nbytes = o->exported.size();
+    return o->exported.data();
+}
+float rpbas_mean_grad(void* h) {
+    RefPbas* o = (RefPbas*)h;
+    return o->algo ? o->with([](auto* a) { return a->meanGrad(); }) : 0.0f;
 }
 
 }  // extern "C"

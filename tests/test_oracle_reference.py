@@ -278,3 +278,27 @@ def test_vibe(config, channels):
         assert np.array_equal(mp, mr), "frame %d: mask differs at %d px" % (t, int((mp != mr).sum()))
         assert np.array_equal(port.samples(), ref.samples()), "frame %d: samples differ" % t
     assert np.array_equal(port.background(), ref.background())
+
+
+# ---- PBAS (BackgroundSubtractorPBAS.cpp: _1ch / _3ch) ----
+@pytest.mark.parametrize("config,channels", [(0, 3), (0, 1), (2, 1)])
+def test_pbas(config, channels):
+    kw = {"channels": channels} if config == 0 else {}
+    fr = _frames(config, 12, 3, **kw)
+    params = {} if config == 0 else {"color_dist_threshold": 20, "update_rate": 8.0, "bg_samples": 25,
+                                     "required_bg_samples": 3}
+    port = pyoracle.OraclePBAS(seed=37, impl="port", **params)
+    ref = pyoracle.OraclePBAS(seed=37, impl="reference", **params)
+    port.initialize(fr[0])
+    ref.initialize(fr[0])
+    names = ("SAMPLE_COLOR", "SAMPLE_GRAD", "R", "T", "D")
+    for n in names:
+        assert np.array_equal(port.state_map(n), ref.state_map(n)), "after initialize: %s" % n
+    for t, f in enumerate(fr[1:], start=1):
+        lr = [-1.0, 1.0, -1.0, 3.5][t % 4]  # <= 0: T(x); > 0: the override
+        mp, mr = port.apply(f, lr), ref.apply(f, lr)
+        assert np.array_equal(mp, mr), "frame %d: mask differs at %d px" % (t, int((mp != mr).sum()))
+        for n in names:
+            assert np.array_equal(port.state_map(n), ref.state_map(n)), "frame %d: %s differs" % (t, n)
+        assert port.mean_grad() == ref.mean_grad(), "frame %d: mean gradient distance" % t
+    assert np.array_equal(port.background(), ref.background())
