@@ -345,12 +345,12 @@ def lobster_run(config, n_frames, stream, cpu=True, cpu_frames=4):
     return out
 
 
-def serving_run(seconds):
+def serving_run(seconds, pawcs_lanes=1):
     """The serving workload (Poisson arrivals of 4 streams/s up to 256 live, lives U[10, 60] s, 30 fps,
     320x240/640x480/1280x720/1920x1080 with p = .3/.3/.3/.1, a quarter single-channel), started from its
     stationary population, through the native serving loop with pinned host frames and masks."""
     from litiv_gb300 import serving
-    r = serving.simulate(duration_s=seconds, warmup_s=3.0, render_threads=8, seed=1)
+    r = serving.simulate(server={"pawcs_lanes": pawcs_lanes}, duration_s=seconds, warmup_s=3.0, render_threads=8, seed=1)
     keep = ["window_s", "frames", "mpix_per_s", "frames_per_s", "offered_mpix_per_s", "p50_ms", "p90_ms", "p99_ms",
             "max_ms", "admit_wait_p50_ms", "admit_wait_p99_ms", "subsense_p50_ms", "subsense_p99_ms", "pawcs_frames",
             "pawcs_p50_ms", "pawcs_p99_ms",
@@ -358,9 +358,10 @@ def serving_run(seconds):
             "rejected", "dropped", "spills", "restores", "late_frames", "peak_live", "peak_device_bytes", "status"]
     out = {k: r[k] for k in keep}
     out["workload"] = ("SuBSENSE/PAWCS mixed: Poisson arrivals 4/s (max 256 live), lives U[10,60] s, 30 fps, "
-                       "320x240/640x480/1280x720/1920x1080 at .3/.3/.3/.1, 1/4 single-channel, 2.5 % of the streams "
-                       "(either channel count) on PAWCS, frames of PAWCS streams on 1 PAWCS lane (lowest stream priority) beside the "
-                       "batched SuBSENSE ticks; stationary start; latency = submit -> mask in pinned host memory")
+                       "320x240/640x480/1280x720/1920x1080 at .3/.3/.3/.1, 1/4 single-channel, 2.5 %% of the streams "
+                       "(either channel count) on PAWCS, frames of PAWCS streams on %d PAWCS lane(s) (lowest stream priority) "
+                       "beside the batched SuBSENSE ticks; stationary start; latency = submit -> mask in pinned host "
+                       "memory" % pawcs_lanes)
     return out
 
 
@@ -404,6 +405,10 @@ def main():
                     help="frames of the PAWCS workload (640x480 thermal-like scene; 0: skip)")
     ap.add_argument("--serving-seconds", type=float, default=20.0,
                     help="measured span of the serving workload run (0: skip)")
+    ap.add_argument("--pawcs-lanes", type=int, default=1,
+                    help="host lanes running the PAWCS streams' frames in the serving run (lvserve_config.pawcs_lanes)")
+    ap.add_argument("--serving-only", action="store_true",
+                    help="run the serving workload alone and print its object (profiling)")
     ap.add_argument("--single-frames", type=int, default=100,
                     help="frames of the single-stream SuBSENSE configs 0 and 1 (0: skip)")
     ap.add_argument("--lobster-frames", type=int, default=100,
@@ -428,6 +433,12 @@ def main():
         if args.pawcs_channels != "1":
             out["bgr"] = pawcs_run(min(args.pawcs_frames, 100), stream, cpu=not args.no_cpu_baseline, channels=3)
         print(json.dumps(out))
+        return
+
+    if args.serving_only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(serving_run(args.serving_seconds, args.pawcs_lanes)))
         return
 
     if args.lobster_only:
@@ -687,7 +698,7 @@ def main():
 
     serve = None
     if rank == 0 and args.serving_seconds > 0:
-        serve = serving_run(args.serving_seconds)
+        serve = serving_run(args.serving_seconds, args.pawcs_lanes)
     pawcs = None
     if rank == 0 and args.pawcs_frames > 0:
         pawcs = pawcs_run(args.pawcs_frames, stream, cpu=not args.no_cpu_baseline)

@@ -39,7 +39,13 @@ typedef enum {
     LVBGS_BUSY = 9             /* serving: a queue or capacity limit refused the request (retry later) */
 } lvbgs_status;
 
-typedef enum { LVBGS_ALGO_SUBSENSE = 0, LVBGS_ALGO_PAWCS = 1, LVBGS_ALGO_LOBSTER = 2, LVBGS_ALGO_VIBE = 3 } lvbgs_algo;
+typedef enum {
+    LVBGS_ALGO_SUBSENSE = 0,
+    LVBGS_ALGO_PAWCS = 1,
+    LVBGS_ALGO_LOBSTER = 2,
+    LVBGS_ALGO_VIBE = 3,
+    LVBGS_ALGO_PBAS = 4
+} lvbgs_algo;
 
 typedef struct lvbgs_ctx* lvbgs_handle;
 
@@ -57,6 +63,7 @@ typedef struct {
     int default_median_blur_kernel_size; /* 9 */
     uint64_t seed;                       /* generator key; streams with different seeds draw independently */
     int device_id;                       /* CUDA device (IParallelAlgo_<CUDA>(bInitUseCUDA, nDeviceID), algo.hpp:82-129) */
+    float update_rate;                   /* PBAS: fInitUpdateRate (16), in (0, 255]; unused by the others */
 } lvbgs_params;
 
 /* one stream's frame in a batched call */
@@ -212,6 +219,9 @@ enum {
     LVBGS_MAP_SAMPLE_DESC,                                                   /* uint16 [N][H*W*C] */
     LVBGS_MAP_DS_LT, LVBGS_MAP_DS_ST,                                        /* float [H/8*W/8*C] */
     LVBGS_MAP_LUT,                                                           /* uint8 [256] */
+    LVBGS_MAP_SAMPLE_GRAD,                                                   /* PBAS: uint8 [N][H*W*C] */
+    LVBGS_MAP_GRAD,                                                          /* PBAS: uint8 [H*W*C] */
+    LVBGS_MAP_MEAN_GRAD,                                                     /* PBAS: float [1] */
     LVBGS_MAP_COUNT
 };
 lvbgs_status lvbgs_debug_map_bytes(lvbgs_handle h, int which, size_t* bytes);

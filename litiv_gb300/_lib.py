@@ -16,12 +16,13 @@ LIB_PATH = os.environ.get("LVBGS_LIB") or os.path.join(HERE, "_build", "liblvbgs
 OK, BAD_ARG, BAD_SIZE, BAD_TYPE, NOT_INITIALIZED, OOM, DEVICE_TIMEOUT, DEVICE_ERROR, UNSUPPORTED, BUSY = range(10)
 STATUS_NAMES = ["OK", "BAD_ARG", "BAD_SIZE", "BAD_TYPE", "NOT_INITIALIZED", "OOM", "DEVICE_TIMEOUT",
                 "DEVICE_ERROR", "UNSUPPORTED", "BUSY"]
-ALGO_SUBSENSE, ALGO_PAWCS, ALGO_LOBSTER, ALGO_VIBE = 0, 1, 2, 3
+ALGO_SUBSENSE, ALGO_PAWCS, ALGO_LOBSTER, ALGO_VIBE, ALGO_PBAS = 0, 1, 2, 3, 4
 
 # map ids (LVBGS_MAP_*)
 MAP_NAMES = ["R", "V", "T", "DLAST", "DMIN_LT", "DMIN_ST", "RAW_LT", "RAW_ST", "FIN_LT", "FIN_ST",
              "UNSTABLE", "BLINKS", "LAST_RAW_FG", "LAST_FG", "LAST_FG_DIL_INV", "LAST_RAW_BLINK", "ROI",
-             "LAST_COLOR", "LAST_DESC", "SAMPLE_COLOR", "SAMPLE_DESC", "DS_LT", "DS_ST", "LUT"]
+             "LAST_COLOR", "LAST_DESC", "SAMPLE_COLOR", "SAMPLE_DESC", "DS_LT", "DS_ST", "LUT",
+             "SAMPLE_GRAD", "GRAD", "MEAN_GRAD"]
 MAP_IDS = {n: i for i, n in enumerate(MAP_NAMES)}
 
 
@@ -30,7 +31,7 @@ class LvbgsParams(C.Structure):
                 ("bg_samples", C.c_size_t), ("required_bg_samples", C.c_size_t),
                 ("samples_for_moving_avgs", C.c_size_t), ("rel_lbsp_threshold", C.c_float),
                 ("lbsp_threshold_offset", C.c_size_t), ("default_median_blur_kernel_size", C.c_int),
-                ("seed", C.c_uint64), ("device_id", C.c_int)]
+                ("seed", C.c_uint64), ("device_id", C.c_int), ("update_rate", C.c_float)]
 
 
 class LvbgsFrame(C.Structure):

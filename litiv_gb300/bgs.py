@@ -398,6 +398,48 @@ class BackgroundSubtractorViBe:
         return BackgroundSubtractorSuBSENSE.apply(self, image, fgmask, learningRate, stream)
 
 
+class BackgroundSubtractorPBAS:
+    """PBAS on the GPU: BackgroundSubtractorPBAS_1ch on single-channel frames and _3ch on three-channel
+    frames (modules/video/src/BackgroundSubtractorPBAS.cpp, BackgroundSubtractorPBAS.hpp:48-57 and :81-93
+    for the interface and defaults). initialize() takes no ROI; apply()'s learningRateOverride replaces
+    the per-pixel update rate T(x) when positive (default -1: no override). Maps: SAMPLE_COLOR,
+    SAMPLE_GRAD, R, T, DMIN_LT (the D map), GRAD (the last frame's gradient image), MEAN_GRAD."""
+
+    def __init__(self, nInitColorDistThreshold=30, fInitUpdateRate=16.0, nBGSamples=35, nRequiredBGSamples=2,
+                 seed=0, device_id=0):
+        lib = L.lib()
+        p = L.LvbgsParams()
+        _check(lib.lvbgs_default_params(L.ALGO_PBAS, C.byref(p)))
+        p.min_color_dist_threshold = nInitColorDistThreshold
+        p.update_rate = fInitUpdateRate
+        p.bg_samples = nBGSamples
+        p.required_bg_samples = nRequiredBGSamples
+        p.seed = seed
+        p.device_id = device_id
+        self.params = p
+        h = C.c_void_p()
+        _check(lib.lvbgs_create(L.ALGO_PBAS, C.byref(p), C.byref(h)))
+        self._h = h
+        self._shape = None
+
+    close = BackgroundSubtractorViBe.close
+    __del__ = BackgroundSubtractorViBe.__del__
+    handle = BackgroundSubtractorViBe.handle
+    getBackgroundImage = BackgroundSubtractorSuBSENSE.getBackgroundImage
+    getDefaultLearningRate = BackgroundSubtractorSuBSENSE.getDefaultLearningRate
+    state_map = BackgroundSubtractorSuBSENSE.state_map
+    scalars = BackgroundSubtractorSuBSENSE.scalars
+    _need_init = BackgroundSubtractorSuBSENSE._need_init
+
+    def initialize(self, oInitImg):
+        """initialize(oInitImg) (BackgroundSubtractorPBAS.cpp:61-109 / :287-324)"""
+        BackgroundSubtractorSuBSENSE.initialize(self, oInitImg, None)
+
+    def apply(self, image, fgmask=None, learningRateOverride=-1.0, stream=None):
+        """apply(image, fgmask, learningRateOverride=-1) (:111-281 / :326-496)"""
+        return BackgroundSubtractorSuBSENSE.apply(self, image, fgmask, learningRateOverride, stream)
+
+
 def map_view(name, raw, W, H, Cc, N):
     """Interprets raw map bytes (reference layout) as a typed numpy array."""
     if name in ("R", "V", "T", "DLAST", "DMIN_LT", "DMIN_ST", "RAW_LT", "RAW_ST", "FIN_LT", "FIN_ST"):
@@ -408,8 +450,12 @@ def map_view(name, raw, W, H, Cc, N):
         return raw.reshape(H, W, Cc)
     if name == "LAST_DESC":
         return raw.view(np.uint16).reshape(H, W, Cc)
-    if name == "SAMPLE_COLOR":
+    if name in ("SAMPLE_COLOR", "SAMPLE_GRAD"):
         return raw.reshape(N, H, W, Cc)
+    if name == "GRAD":
+        return raw.reshape(H, W, Cc)
+    if name == "MEAN_GRAD":
+        return raw.view(np.float32).reshape(1)
     if name == "SAMPLE_DESC":
         return raw.view(np.uint16).reshape(N, H, W, Cc)
     if name in ("DS_LT", "DS_ST"):

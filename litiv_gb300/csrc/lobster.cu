@@ -1,8 +1,10 @@
-// LOBSTER and ViBe frame steps for sm_103a (BackgroundSubtractorLOBSTER.cpp:459-581, the non-parallel
-// path; BackgroundSubtractorViBe.cpp:77-191). The kernels are written for LOBSTER and take the algorithm
-// as a template parameter: ViBe evaluates every pixel (no ROI), matches colours only, keeps plain colour
-// samples and outputs its raw mask, and its neighbour positions are clamped to the frame instead of the
-// LBSP border; the scheme below is the same.
+// LOBSTER, ViBe and PBAS frame steps for sm_103a (BackgroundSubtractorLOBSTER.cpp:459-581, the
+// non-parallel path; BackgroundSubtractorViBe.cpp:77-191; BackgroundSubtractorPBAS.cpp:111-496). The
+// kernels are written for LOBSTER and take the algorithm as a template parameter: ViBe evaluates every
+// pixel (no ROI), matches colours only, keeps plain colour samples and outputs its raw mask, and its
+// neighbour positions are clamped to the frame instead of the LBSP border; PBAS adds a gradient image,
+// gradient samples, per-pixel R/T/D maps and a frame-level mean gradient distance, and its neighbour
+// update writes the target's own values (self diffusion). The scheme below is the same for all three.
 //
 // The reference scans the ROI pixels in raster order. A pixel reads its own samples, which an earlier
 // pixel's neighbour update may have overwritten in the same frame (:510-512 / :569-574); nothing else
@@ -117,11 +119,15 @@ __device__ __forceinline__ void taps(const uint8_t* img, int W, int p, int c, ui
 // sample s of pixel p: LOBSTER, the packed word and the colour byte; ViBe, the colour bytes packed into d
 template <int C, int ALG>
 __device__ __forceinline__ void load_sample(const LobDev& D, int s, int p, unsigned long long& d, uint32_t& c2) {
-    if (ALG == ALG_VIBE) {
-        const uint8_t* b = D.sC + ((size_t)s * D.npx + p) * C;
-        d = C == 3 ? ((unsigned long long)__ldg(b) | ((unsigned long long)__ldg(b + 1) << 8) |
-                      ((unsigned long long)__ldg(b + 2) << 16))
-                   : (unsigned long long)__ldg(b);
+    if (ALG == ALG_VIBE || ALG == ALG_PBAS) {
+        // colour c at bits 8c; PBAS: gradient c at bits 24 + 8c
+        const size_t o = ((size_t)s * D.npx + p) * C;
+        d = 0;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            d |= (unsigned long long)__ldg(D.sC + o + c) << (8 * c);
+            if (ALG == ALG_PBAS) d |= (unsigned long long)__ldg(D.sG + o + c) << (24 + 8 * c);
+        }
         c2 = 0;
         return;
     }
@@ -228,6 +234,102 @@ __device__ uint32_t eval_px(const LobDev& D, int p, int x, int y, const uint32_t
     return w | (k << 27);
 }
 
+// PBAS's evaluation of pixel p (:146-231 / :365-458): the ordered scan with the colour + weighted
+// gradient distance against the threshold R(x) * R0, the bad samples' gradient distances for the frame
+// level, then the D(x), T(x) and R(x) updates (written to the maps of the next parity) and the model
+// updates with their draws. g holds the pixel's gradient. Three-channel distances: (float)sqrt((double)s)
+// of the uint16 sum s equals sqrtf((float)s), since double rounding through double is innocuous for the
+// square root (53 >= 2 * 24 + 2 bits).
+template <int C, bool OVR>
+__device__ uint32_t pbas_eval_px(const LobDev& D, int p, int x, int y, const uint32_t (&curr)[C], const uint32_t (&g)[C],
+                                 const LobOvr& ov, unsigned long long* scanned) {
+    const size_t npx = (size_t)D.npx;
+    const float* fc = D.fm + (size_t)D.cur * 3 * npx;
+    float* fn = D.fm + (size_t)(D.cur ^ 1) * 3 * npx;
+    const float R = fc[p], T = fc[npx + p], Dm = fc[2 * npx + p];
+    const float thr = R * D.R0;
+    const float gw = 10.0f / *D.meanGrad;  // BGSPBAS_GRAD_WEIGHT_ALPHA / m_fFormerMeanGradDist
+    float fMin = 255.0f;
+    int nGood = 0, s = 0, nb = 0;
+    uint32_t badSum = 0;
+    unsigned long long dB = 0;
+    uint32_t cB = 0;
+    if (D.N > 0) load_sample<C, ALG_PBAS>(D, 0, p, dB, cB);
+    while (nGood < D.nreq && s < D.N) {
+        unsigned long long d = dB;
+        if (s + 1 < D.N) load_sample<C, ALG_PBAS>(D, s + 1, p, dB, cB);
+        if (OVR && ((ov.mask >> s) & 1ull)) d = ov.d[0];  // self diffusion: the pixel's own values
+        float fSum, fGrad = 0.0f;
+        uint32_t nGrad = 0;
+        if (C == 1) {
+            const uint32_t nCol = (uint32_t)abs((int)curr[0] - (int)(d & 0xffu));
+            nGrad = (uint32_t)abs((int)g[0] - (int)((d >> 24) & 0xffu));
+            fSum = gw * (float)nGrad + (float)nCol;
+        } else {
+            uint32_t aC = 0, aG = 0;
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                const int dc = (int)curr[c] - (int)((d >> (8 * c)) & 0xffu);
+                const int dg = (int)g[c] - (int)((d >> (24 + 8 * c)) & 0xffu);
+                aC += (uint32_t)(dc * dc);
+                aG += (uint32_t)(dg * dg);
+            }
+            fGrad = __fsqrt_rn((float)(aG & 0xffffu));
+            fSum = gw * fGrad + __fsqrt_rn((float)(aC & 0xffffu));
+        }
+        if (fSum > 255.0f) fSum = 255.0f;
+        if (fSum <= thr) {
+            if (fMin > fSum) fMin = fSum;
+            ++nGood;
+        } else {
+            if (C == 1) badSum += nGrad;
+            else D.badVals[(size_t)p * D.N + nb] = fGrad;
+            ++nb;
+        }
+        ++s;
+    }
+    *scanned += (unsigned long long)s;
+    const float Nf = (float)D.N;
+    const float Dn = (Dm * (Nf - 1.0f) + fMin / 255.0f) / Nf;
+    uint32_t w = kIValid | ((uint32_t)s << 2);
+    float Tn;
+    uint32_t k = 0;
+    if (nGood < D.nreq) {
+        w |= kIFG;
+        Tn = T + 1.0000f / (Dn * 255.00f + 1.0000f);
+        if (Tn > 200.00f) Tn = 200.00f;
+    } else {
+        const unsigned long long nLR = D.lrOverride ? D.nLR : (unsigned long long)__float2uint_rz(ceilf(T));
+        Draws ds;
+        ds.blk = 0xffffffffu;
+        if (mod64(draw(D, (uint32_t)p, k++, ds), nLR) == 0ull) {
+            const uint32_t so = draw(D, (uint32_t)p, k++, ds) % (uint32_t)D.N;
+            w |= kIOwn | (so << 10);
+        }
+        if (mod64(draw(D, (uint32_t)p, k++, ds), nLR) == 0ull) {
+            const int r = (int)(draw(D, (uint32_t)p, k++, ds) % 8u);
+            const int nx = clampi(x + c_lob_nb3[r][0], 0, D.W - 1);
+            const int ny = clampi(y + c_lob_nb3[r][1], 0, D.H - 1);
+            const uint32_t sn = draw(D, (uint32_t)p, k++, ds) % (uint32_t)D.N;
+            w |= kINb | ((uint32_t)((ny - y + 1) * 3 + (nx - x + 1)) << 17) | (sn << 21);
+        }
+        Tn = T - 0.0500f / (Dn * 255.00f + 1.0000f);
+        if (Tn < 2.0000f) Tn = 2.0000f;
+    }
+    float Rn = R;
+    if (R < 0.6000f + Dn * 5.0000f + 0.0000f) {
+        if (R < 99.0000f) Rn = R * 1.0500f;
+    } else if (R > 0.6000f) {
+        Rn = R * 0.9500f;
+    }
+    fn[p] = Rn;
+    fn[npx + p] = Tn;
+    fn[2 * npx + p] = Dn;
+    D.badSum[p] = badSum;
+    D.badCnt[p] = (uint8_t)nb;
+    return w | (k << 27);
+}
+
 // the pixel's colour and (LOBSTER) its LBSP taps
 template <int C, int ALG>
 __device__ __forceinline__ void pixel_inputs(const LobDev& D, int p, uint32_t (&vals)[C][4], uint32_t (&curr)[C]) {
@@ -272,8 +374,23 @@ __global__ void __launch_bounds__(kThreadsL) lob_k_eval(LobDev D) {
             uint32_t vals[C][4], curr[C];
             pixel_inputs<C, ALG>(D, p, vals, curr);
             // the sample word this pixel writes: LOBSTER, its descriptors (:499-500 / :548-550) and colour;
-            // ViBe, its colour
+            // ViBe, its colour; PBAS, its colour and gradient (also what a neighbour update writes into it)
             unsigned long long wd = 0;
+            if (ALG == ALG_PBAS) {
+                uint32_t g[C];
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    g[c] = __ldg(D.grad + (size_t)p * C + c);
+                    wd |= ((unsigned long long)curr[c] << (8 * c)) | ((unsigned long long)g[c] << (24 + 8 * c));
+                }
+                D.wD[p] = wd;
+                LobOvr none;
+                none.n = 0;
+                none.mask = 0;
+                D.intent[p] = pbas_eval_px<C, false>(D, p, x, y, curr, g, none, &scanned);
+                warp_add(&D.stats[0], scanned);
+                return;
+            }
             if (ALG == ALG_VIBE) {
 #pragma unroll
                 for (int c = 0; c < C; ++c) wd |= (unsigned long long)curr[c] << (8 * c);
@@ -341,14 +458,24 @@ __global__ void __launch_bounds__(kThreadsL) lob_k_round(LobDev D, int round) {
                 const int s = i_snb(wq);
                 ov.s[ov.n] = s;
                 ov.d[ov.n] = __ldcg(D.wD + q4[j]);
-                ov.c[ov.n] = ALG == ALG_VIBE ? 0u : __ldg(D.frame + (size_t)q4[j] * C + (C == 3 ? 2 : 0));
+                ov.c[ov.n] = ALG != ALG_LOBSTER ? 0u : __ldg(D.frame + (size_t)q4[j] * C + (C == 3 ? 2 : 0));
                 ++ov.n;
                 ov.mask |= 1ull << s;
             }
         }
         uint32_t vals[C][4], curr[C];
         pixel_inputs<C, ALG>(D, p, vals, curr);
-        const uint32_t wNew = eval_px<C, ALG, true>(D, p, x, y, vals, curr, ov, &scanned);
+        uint32_t wNew;
+        if (ALG == ALG_PBAS) {
+            // self diffusion: a sample that an earlier neighbour writes holds the pixel's own values
+            uint32_t g[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c) g[c] = __ldg(D.grad + (size_t)p * C + c);
+            ov.d[0] = __ldcg(D.wD + p);
+            wNew = pbas_eval_px<C, true>(D, p, x, y, curr, g, ov, &scanned);
+        } else {
+            wNew = eval_px<C, ALG, true>(D, p, x, y, vals, curr, ov, &scanned);
+        }
         const uint32_t wOld = ld_vol(&D.intent[p]);
         if (wNew == wOld) continue;
         *(volatile uint32_t*)&D.intent[p] = wNew;
@@ -397,11 +524,13 @@ __global__ void __launch_bounds__(kThreadsL) lob_k_commit(LobDev D) {
         const uint8_t raw = (valid && (wp & kIFG)) ? 255 : 0;
         if (ALG == ALG_VIBE) D.maskOut[p] = raw;
         else D.rawFG[p] = raw;
+        // PBAS: every write into pixel p holds p's own colour and gradient
+        const unsigned long long wOwn = ALG == ALG_PBAS ? D.wD[p] : 0ull;
         D.kctr[p] = (uint16_t)(valid ? i_draws(wp) : 0);
         if (valid) writes = ((wp & kIOwn) ? 1ull : 0ull) + ((wp & kINb) ? 1ull : 0ull);
         const int x = p % D.W, y = p / D.W;
-        // the pixels a write can reach: inside the LBSP border (LOBSTER), the whole frame (ViBe)
-        constexpr int bord = ALG == ALG_VIBE ? 0 : kBorder;
+        // the pixels a write can reach: inside the LBSP border (LOBSTER), the whole frame (ViBe, PBAS)
+        constexpr int bord = ALG == ALG_LOBSTER ? kBorder : 0;
         if (x >= bord && y >= bord && x < D.W - bord && y < D.H - bord) {
             int ns = 0;
             int ss[10], sq[10];
@@ -425,7 +554,13 @@ __global__ void __launch_bounds__(kThreadsL) lob_k_commit(LobDev D) {
             for (int k = 0; k < ns; ++k) {
                 const size_t o = (size_t)ss[k] * D.npx + p;
                 const int q = sq[k];
-                if (ALG == ALG_VIBE) {
+                if (ALG == ALG_PBAS) {
+#pragma unroll
+                    for (int c = 0; c < C; ++c) {
+                        D.sC[o * C + c] = (uint8_t)(wOwn >> (8 * c));
+                        D.sG[o * C + c] = (uint8_t)(wOwn >> (24 + 8 * c));
+                    }
+                } else if (ALG == ALG_VIBE) {
                     const unsigned long long wq = D.wD[q];
 #pragma unroll
                     for (int c = 0; c < C; ++c) D.sC[o * C + c] = (uint8_t)(wq >> (8 * c));
@@ -443,7 +578,7 @@ __global__ void __launch_bounds__(kThreadsL) lob_k_commit(LobDev D) {
 // cv::medianBlur(raw mask, k) with replicated borders: 255 where more than half of the k*k window is
 // set (:577), which becomes the last mask and the output (:578); the frame becomes the last colour
 // frame (:580)
-template <int C>
+template <int C, bool KEEP>
 __global__ void __launch_bounds__(kThreadsL) lob_k_median(LobDev D) {
     if (!ld_vol(&D.flags[LOB_F_CONV])) return;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -455,8 +590,9 @@ __global__ void __launch_bounds__(kThreadsL) lob_k_median(LobDev D) {
         for (int dx = -r; dx <= r; ++dx) cnt += __ldg(row + clampi(x + dx, 0, D.W - 1)) != 0;
     }
     const uint8_t m = (2 * cnt > D.medianK * D.medianK) ? 255 : 0;
-    D.lastFG[p] = m;
     D.maskOut[p] = m;
+    if (!KEEP) return;  // PBAS keeps neither
+    D.lastFG[p] = m;
 #pragma unroll
     for (int c = 0; c < C; ++c) D.lastColor[(size_t)p * C + c] = __ldg(D.frame + (size_t)p * C + c);
 }
@@ -512,6 +648,160 @@ __global__ void __launch_bounds__(kThreadsL) lob_k_vibe_init(LobDev D, const uin
         uint8_t* dst = D.sC + ((size_t)s * D.npx + p) * C;
 #pragma unroll
         for (int c = 0; c < C; ++c) dst[c] = __ldg(src + c);
+    }
+}
+
+// ---- PBAS (BackgroundSubtractorPBAS.cpp) ----
+
+__device__ __forceinline__ int reflect101(int i, int n) {
+    if (n == 1) return 0;
+    while (i < 0 || i >= n) i = i < 0 ? -i : 2 * n - 2 - i;
+    return i;
+}
+
+// the gradient image of a frame (:127-135 / :338-346), first pass: GaussianBlur 3x3 (sigma 0), the
+// separable [1 2 1] / 4 kernel in 8-bit fixed point, (sum + 8) >> 4, with BORDER_REFLECT_101
+template <int C>
+__global__ void __launch_bounds__(kThreadsL) pbas_k_blur(LobDev D, const uint8_t* img) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= D.npx * C) return;
+    const int p = i / C, c = i % C, x = p % D.W, y = p / D.W;
+    const int xs[3] = {reflect101(x - 1, D.W), x, reflect101(x + 1, D.W)};
+    const int ys[3] = {reflect101(y - 1, D.H), y, reflect101(y + 1, D.H)};
+    int acc = 0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const uint8_t* row = img + (size_t)ys[j] * D.W * C + c;
+        const int r = __ldg(row + xs[0] * C) + 2 * __ldg(row + xs[1] * C) + __ldg(row + xs[2] * C);
+        acc += (j == 1 ? 2 : 1) * r;
+    }
+    D.blur[i] = (uint8_t)((acc + 8) >> 4);
+}
+
+// second pass: the Scharr derivatives ([-3 0 3; -10 0 10; -3 0 3] and its transpose, int16, no
+// overflow at these magnitudes), convertScaleAbs (|v| saturated to 255) and addWeighted(0.5, 0.5)
+// ((a + b) * 0.5 rounded half to even), BORDER_REFLECT_101
+template <int C>
+__global__ void __launch_bounds__(kThreadsL) pbas_k_grad(LobDev D) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= D.npx * C) return;
+    const int p = i / C, c = i % C, x = p % D.W, y = p / D.W;
+    const int xs[3] = {reflect101(x - 1, D.W), x, reflect101(x + 1, D.W)};
+    const int ys[3] = {reflect101(y - 1, D.H), y, reflect101(y + 1, D.H)};
+    int v[3][3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) v[j][k] = __ldg(D.blur + ((size_t)ys[j] * D.W + xs[k]) * C + c);
+    const int gx = 3 * (v[0][2] - v[0][0]) + 10 * (v[1][2] - v[1][0]) + 3 * (v[2][2] - v[2][0]);
+    const int gy = 3 * (v[2][0] - v[0][0]) + 10 * (v[2][1] - v[0][1]) + 3 * (v[2][2] - v[0][2]);
+    const int ax = min(abs(gx), 255), ay = min(abs(gy), 255);
+    const int sum = ax + ay;
+    D.grad[i] = (uint8_t)((sum >> 1) + ((sum & 1) & ((sum >> 1) & 1)));
+}
+
+// PBAS's initialize() (:61-109 / :287-324): R = 1, T = the default update rate, D = 0 in the maps of
+// parity 0, the mean gradient distance mean0 (20, or the last one), and sample s of every pixel (colour and gradient) from a 7x7
+// Gaussian position of the frame clamped to the frame (draw s of the pixel in frame 0)
+template <int C>
+__global__ void __launch_bounds__(kThreadsL) pbas_k_init(LobDev D, const uint8_t* img, float mean0) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= D.npx) return;
+    const size_t npx = (size_t)D.npx;
+    D.fm[p] = 1.0f;
+    D.fm[npx + p] = D.updateRate;
+    D.fm[2 * npx + p] = 0.0f;
+    if (p == 0) *D.meanGrad = mean0;
+    const int x0 = p % D.W, y0 = p / D.W;
+    Draws ds;
+    ds.blk = 0xffffffffu;
+    for (int s = 0; s < D.N; ++s) {
+        int r = 1 + (int)(draw(D, (uint32_t)p, (uint32_t)s, ds) % 512u);
+        int sx = 0, sy = 0;
+        for (int i = 0; i < 49; ++i) {
+            r -= c_lob_pat7[i];
+            if (r <= 0) {
+                sy = i / 7;
+                sx = i % 7;
+                break;
+            }
+        }
+        sx = clampi(sx + x0 - 3, 0, D.W - 1);
+        sy = clampi(sy + y0 - 3, 0, D.H - 1);
+        const size_t src = ((size_t)sy * D.W + sx) * C, dst = ((size_t)s * npx + p) * C;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            D.sC[dst + c] = __ldg(img + src + c);
+            D.sG[dst + c] = D.grad[src + c];
+        }
+    }
+}
+
+// the frame-level mean gradient distance of the bad samples, single channel (:232): the size_t sum
+// of their gradient distances and their count (which starts at 1), per block into two counters
+__global__ void __launch_bounds__(kThreadsL) pbas_k_mean1(LobDev D) {
+    if (!ld_vol(&D.flags[LOB_F_CONV])) return;
+    unsigned long long sum = 0, cnt = 0;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < D.npx; p += gridDim.x * blockDim.x) {
+        sum += D.badSum[p];
+        cnt += D.badCnt[p];
+    }
+    warp_add(&D.stats[2], sum);
+    warp_add(&D.stats[3], cnt);
+}
+__global__ void pbas_k_mean1_end(LobDev D) {
+    if (!ld_vol(&D.flags[LOB_F_CONV])) return;
+    const float mean = (float)D.stats[2] / (float)(D.stats[3] + 1ull);
+    *D.meanGrad = mean > 20.0f ? mean : 20.0f;
+}
+
+// three channels (:460): the float sum of the bad samples' gradient distances in raster order (pixel,
+// then scan order), which one thread adds up; the block stages the values of kMeanChunk pixels at a
+// time, compacted in order, in shared memory
+constexpr int kMeanThreads = 512, kMeanChunk = kMeanThreads;
+__global__ void __launch_bounds__(kMeanThreads) pbas_k_mean3(LobDev D) {
+    if (!ld_vol(&D.flags[LOB_F_CONV])) return;
+    extern __shared__ float sm_vals[];  // kMeanChunk * N values
+    __shared__ int sm_warp[kMeanThreads / 32 + 1];
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    float total = 0.0f;
+    unsigned long long nBad = 1;
+    for (int base = 0; base < D.npx; base += kMeanChunk) {
+        const int p = base + t;
+        const int n = p < D.npx ? (int)D.badCnt[p] : 0;
+        // exclusive scan of the counts over the block
+        int inc = n;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += v;
+        }
+        if (lane == 31) sm_warp[wid] = inc;
+        __syncthreads();
+        if (wid == 0) {
+            int w = lane < kMeanThreads / 32 ? sm_warp[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += v;
+            }
+            if (lane < kMeanThreads / 32) sm_warp[lane] = w;  // inclusive totals of the warps
+            if (lane == 31) sm_warp[kMeanThreads / 32] = w;
+        }
+        __syncthreads();
+        const int off = inc - n + (wid > 0 ? sm_warp[wid - 1] : 0);
+        for (int k = 0; k < n; ++k) sm_vals[off + k] = D.badVals[(size_t)p * D.N + k];
+        const int m = sm_warp[kMeanThreads / 32];
+        __syncthreads();
+        if (t == 0) {
+            float acc = total;
+            for (int k = 0; k < m; ++k) acc += sm_vals[k];
+            total = acc;
+            nBad += (unsigned long long)m;
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        const float mean = total / (float)nBad;
+        *D.meanGrad = mean > 20.0f ? mean : 20.0f;
     }
 }
 
@@ -577,7 +867,7 @@ __global__ void lob_k_background(LobDev D, void* out, int descriptors) {
         for (int s = 0; s < D.N; ++s) {
             const size_t o = (size_t)s * D.npx + p;
             uint32_t v;
-            if (D.alg == ALG_VIBE) {
+            if (D.alg != ALG_LOBSTER) {
                 v = D.sC[o * C + c];
             } else if (descriptors) {
                 v = C == 3 ? (uint32_t)(((const unsigned long long*)D.sD)[o] >> (16 * c)) & 0xffffu
@@ -638,6 +928,10 @@ inline int blocks_for(size_t n) { return (int)((n + kThreadsL - 1) / kThreadsL);
 }  // namespace
 
 void lob_release(LobState& L) {
+    if (L.meanDone) cudaEventSynchronize(L.meanDone);
+    if (L.done) cudaEventDestroy(L.done);
+    if (L.meanDone) cudaEventDestroy(L.meanDone);
+    L.done = L.meanDone = nullptr;
     cudaFree(L.mem);
     L.mem = nullptr;
     L.bytes = 0;
@@ -647,12 +941,19 @@ void lob_release(LobState& L) {
 
 lvbgs_status lob_setup(LobState& L, int alg, const lvbgs_params& prm, int W, int H, int C,
                        const std::vector<uint8_t>& roi, size_t orig, size_t fin, cudaStream_t st, std::string& err) {
+    // PBAS keeps its former mean gradient distance when initialized again (it is set by the
+    // constructor only, BackgroundSubtractorPBAS.cpp:29)
+    if (L.mem && L.d.alg == ALG_PBAS && L.d.meanGrad) {
+        LOB_CUDA(cudaEventSynchronize(L.meanDone), "frame step");
+        LOB_CUDA(cudaMemcpy(&L.pbasMean, L.d.meanGrad, sizeof(float), cudaMemcpyDeviceToHost), "state read-back");
+    }
     cudaFree(L.mem);
     L.mem = nullptr;
     const size_t npx = (size_t)W * H, N = prm.bg_samples;
-    // ViBe keeps only colour samples ([N][npx*C] bytes); LOBSTER the packed descriptor plane and a colour byte
-    const bool vibe = alg == ALG_VIBE;
-    const size_t lob = vibe ? 0 : 1;
+    // ViBe keeps only colour samples ([N][npx*C] bytes); PBAS colour and gradient samples and its maps;
+    // LOBSTER the packed descriptor plane and a colour byte
+    const bool vibe = alg != ALG_LOBSTER, pbas = alg == ALG_PBAS;
+    const size_t lob = vibe ? 0 : 1, pb = pbas ? 1 : 0;
     size_t off = 0;
     auto take = [&](size_t bytes) {
         const size_t o = off;
@@ -664,9 +965,15 @@ lvbgs_status lob_setup(LobState& L, int alg, const lvbgs_params& prm, int W, int
                  oSD = take(lob * N * npx * (C == 3 ? 8 : 2)), oSC = take(vibe ? N * npx * C : N * npx),
                  oIntent = take(npx * 4),
                  oWD = take(npx * 8), oList0 = take(npx * 4), oList1 = take(npx * 4), oStamp = take(npx * 4),
-                 oFlags = take(LOB_F_WORDS * 4), oStats = take(16), oFrame = take(npx * C), oMask = take(npx);
+                 oFlags = take(LOB_F_WORDS * 4), oStats = take(32), oFrame = take(npx * C), oMask = take(npx),
+                 oSG = take(pb * N * npx * C), oGrad = take(pb * npx * C), oBlur = take(pb * npx * C),
+                 oFm = take(pb * 6 * npx * 4), oMean = take(pb * 4), oBadSum = take(pb * (C == 1 ? npx * 4 : 0)),
+                 oBadCnt = take(pb * npx), oBadVals = take(pb * (C == 3 ? npx * N * 4 : 0)),
+                 oRawPb = take(pb * npx);
     LOB_CUDA(cudaMalloc(&L.mem, off), "model allocation");
     if (!L.h_flags) LOB_CUDA(cudaHostAlloc((void**)&L.h_flags, LOB_F_WORDS * 4, cudaHostAllocDefault), "pinned allocation");
+    if (!L.done) LOB_CUDA(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming), "event creation");
+    if (!L.meanDone) LOB_CUDA(cudaEventCreateWithFlags(&L.meanDone, cudaEventDisableTiming), "event creation");
     L.bytes = off;
     LobDev& D = L.d;
     D = LobDev{};
@@ -702,6 +1009,22 @@ lvbgs_status lob_setup(LobState& L, int alg, const lvbgs_params& prm, int W, int
     D.stats = (unsigned long long*)(b + oStats);
     L.d_frame = b + oFrame;
     L.d_mask = b + oMask;
+    if (pbas) {
+        D.sG = b + oSG;
+        D.grad = b + oGrad;
+        D.blur = b + oBlur;
+        D.fm = (float*)(b + oFm);
+        D.meanGrad = (float*)(b + oMean);
+        D.badSum = (uint32_t*)(b + oBadSum);
+        D.badCnt = b + oBadCnt;
+        D.badVals = (float*)(b + oBadVals);
+        D.rawFG = b + oRawPb;
+        // the constructor's arguments (BackgroundSubtractorPBAS.cpp:21-32) and medianBlur(.., 9) (:266 / :494)
+        D.R0 = (float)prm.min_color_dist_threshold;
+        D.updateRate = prm.update_rate;
+        D.medianK = 9;
+        D.cur = 0;
+    }
     L.ksent = 0;
     L.lastRounds = 1;
     L.frames = 0;
@@ -726,6 +1049,9 @@ void launch(const LobDev& D, int blocks, cudaStream_t st, A... args) {
     if (D.alg == ALG_VIBE) {
         if (D.C == 3) K<3, ALG_VIBE>::run(blocks, st, D, args...);
         else K<1, ALG_VIBE>::run(blocks, st, D, args...);
+    } else if (D.alg == ALG_PBAS) {
+        if (D.C == 3) K<3, ALG_PBAS>::run(blocks, st, D, args...);
+        else K<1, ALG_PBAS>::run(blocks, st, D, args...);
     } else {
         if (D.C == 3) K<3, ALG_LOBSTER>::run(blocks, st, D, args...);
         else K<1, ALG_LOBSTER>::run(blocks, st, D, args...);
@@ -743,6 +1069,32 @@ template <int C, int ALG>
 struct Commit {
     static void run(int b, cudaStream_t st, const LobDev& D) { lob_k_commit<C, ALG><<<b, kThreadsL, 0, st>>>(D); }
 };
+
+// PBAS's gradient image of a device frame into D.grad
+void pbas_gradient(const LobDev& D, const uint8_t* img, cudaStream_t st) {
+    const int nb = blocks_for((size_t)D.npx * D.C);
+    if (D.C == 3) {
+        pbas_k_blur<3><<<nb, kThreadsL, 0, st>>>(D, img);
+        pbas_k_grad<3><<<nb, kThreadsL, 0, st>>>(D);
+    } else {
+        pbas_k_blur<1><<<nb, kThreadsL, 0, st>>>(D, img);
+        pbas_k_grad<1><<<nb, kThreadsL, 0, st>>>(D);
+    }
+}
+
+// PBAS's frame-level mean gradient distance, after the commit
+lvbgs_status pbas_mean_launch(const LobDev& D, int sms, cudaStream_t st, std::string& err) {
+    if (D.C == 1) {
+        pbas_k_mean1<<<2 * sms, kThreadsL, 0, st>>>(D);
+        pbas_k_mean1_end<<<1, 1, 0, st>>>(D);
+    } else {
+        const size_t smem = (size_t)kMeanChunk * D.N * sizeof(float);
+        LOB_CUDA(cudaFuncSetAttribute(pbas_k_mean3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                 "mean kernel attribute");
+        pbas_k_mean3<<<1, kMeanThreads, smem, st>>>(D);
+    }
+    return LVBGS_OK;
+}
 
 lvbgs_status lob_refresh_launch(LobState& L, float frac, int force, cudaStream_t st, std::string& err) {
     LobDev& D = L.d;
@@ -769,6 +1121,15 @@ lvbgs_status lob_init_model(LobState& L, const uint8_t* dimg, cudaStream_t st, s
     LobDev& D = L.d;
     D.frameKey = 0;
     L.ksent = 0;
+    if (D.alg == ALG_PBAS) {
+        D.cur = 0;
+        pbas_gradient(D, dimg, st);
+        if (D.C == 3) pbas_k_init<3><<<blocks_for(D.npx), kThreadsL, 0, st>>>(D, dimg, L.pbasMean);
+        else pbas_k_init<1><<<blocks_for(D.npx), kThreadsL, 0, st>>>(D, dimg, L.pbasMean);
+        LOB_CUDA(cudaGetLastError(), "init launch");
+        LOB_CUDA(cudaStreamSynchronize(st), "initialization");
+        return LVBGS_OK;
+    }
     if (D.alg == ALG_VIBE) {
         if (D.C == 3) lob_k_vibe_init<3><<<blocks_for(D.npx), kThreadsL, 0, st>>>(D, dimg);
         else lob_k_vibe_init<1><<<blocks_for(D.npx), kThreadsL, 0, st>>>(D, dimg);
@@ -799,6 +1160,11 @@ lvbgs_status lob_apply(LobState& L, const uint8_t* dimg, uint8_t* dmask, uint8_t
     D.frame = dimg;
     D.maskOut = dmask;
     D.nLR = std::isinf(lr) ? ~0ull : (unsigned long long)std::ceil(lr);  // :470
+    if (D.alg == ALG_PBAS) {
+        // learningRateOverride > 0 replaces ceil(T(x)) (:174 / :402)
+        D.lrOverride = lr > 0 ? 1 : 0;
+        if (!(lr > 0)) D.nLR = 0;
+    }
     ++L.frames;
     D.frameKey = (uint32_t)L.frames;
     L.ksent = 0;
@@ -808,6 +1174,10 @@ lvbgs_status lob_apply(LobState& L, const uint8_t* dimg, uint8_t* dmask, uint8_t
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int roundBlocks = 2 * (sms > 0 ? sms : 1);
     LOB_CUDA(cudaMemsetAsync(D.flags, 0, LOB_F_WORDS * 4, st), "flag reset");
+    if (D.alg == ALG_PBAS) {
+        LOB_CUDA(cudaMemsetAsync(D.stats + 2, 0, 16, st), "counter reset");
+        pbas_gradient(D, dimg, st);
+    }
     launch<Eval>(D, nb, st);
     lob_k_mark<<<nb, kThreadsL, 0, st>>>(D);
     LOB_CUDA(cudaGetLastError(), "evaluation launch");
@@ -818,15 +1188,29 @@ lvbgs_status lob_apply(LobState& L, const uint8_t* dimg, uint8_t* dmask, uint8_t
             lob_k_round_end<<<1, 1, 0, st>>>(D, round);
         }
         launch<Commit>(D, nb, st);
-        // LOBSTER's median blur, last mask and last colour frame (ViBe outputs its raw mask)
+        // LOBSTER's median blur, last mask and last colour frame; PBAS's median blur (ViBe outputs its
+        // raw mask)
         if (D.alg == ALG_LOBSTER) {
-            if (C == 3) lob_k_median<3><<<nb, kThreadsL, 0, st>>>(D);
-            else lob_k_median<1><<<nb, kThreadsL, 0, st>>>(D);
+            if (C == 3) lob_k_median<3, true><<<nb, kThreadsL, 0, st>>>(D);
+            else lob_k_median<1, true><<<nb, kThreadsL, 0, st>>>(D);
+        } else if (D.alg == ALG_PBAS) {
+            lob_k_median<1, false><<<nb, kThreadsL, 0, st>>>(D);
         }
         LOB_CUDA(cudaGetLastError(), "repair launch");
         if (hostMask) LOB_CUDA(cudaMemcpyAsync(hostMask, dmask, (size_t)D.npx, cudaMemcpyDeviceToHost, st), "mask download");
         LOB_CUDA(cudaMemcpyAsync(L.h_flags, D.flags, LOB_F_WORDS * 4, cudaMemcpyDeviceToHost, st), "flag read-back");
-        LOB_CUDA(cudaStreamSynchronize(st), "frame step");
+        // PBAS's frame-level mean gradient distance is only needed by the next frame step: the host does
+        // not wait for it
+        if (D.alg == ALG_PBAS) {
+            LOB_CUDA(cudaEventRecord(L.done, st), "event record");
+            lvbgs_status ms = pbas_mean_launch(D, sms, st, err);
+            if (ms != LVBGS_OK) return ms;
+            LOB_CUDA(cudaGetLastError(), "mean launch");
+            LOB_CUDA(cudaEventRecord(L.meanDone, st), "event record");
+            LOB_CUDA(cudaEventSynchronize(L.done), "frame step");
+        } else {
+            LOB_CUDA(cudaStreamSynchronize(st), "frame step");
+        }
         if (L.h_flags[LOB_F_ERR]) {
             err = "LOBSTER repair list overflow";
             return LVBGS_DEVICE_ERROR;
@@ -840,11 +1224,13 @@ lvbgs_status lob_apply(LobState& L, const uint8_t* dimg, uint8_t* dmask, uint8_t
     }
     L.lastRounds = (int)L.h_flags[LOB_F_ROUNDS];
     D.stampBase += (uint32_t)round + 2u;
+    if (D.alg == ALG_PBAS) D.cur ^= 1;  // the maps this frame step wrote are the next one's start
     return LVBGS_OK;
 }
 
 lvbgs_status lob_background(LobState& L, void* hostOut, bool descriptors, cudaStream_t st, std::string& err) {
     LobDev& D = L.d;
+    LOB_CUDA(cudaEventSynchronize(L.meanDone), "frame step");  // the last frame step may run on another stream
     const size_t n = (size_t)D.npx * D.C * (descriptors ? 2 : 1);
     void* tmp = nullptr;
     LOB_CUDA(cudaMallocAsync(&tmp, n, st), "staging allocation");
@@ -861,6 +1247,17 @@ lvbgs_status lob_background(LobState& L, void* hostOut, bool descriptors, cudaSt
 size_t lob_map_bytes(const LobState& L, int which) {
     const size_t npx = (size_t)L.d.npx, C = (size_t)L.d.C, N = (size_t)L.d.N;
     if (L.d.alg == ALG_VIBE) return which == LVBGS_MAP_SAMPLE_COLOR ? N * npx * C : which == LVBGS_MAP_ROI ? npx : 0;
+    if (L.d.alg == ALG_PBAS) switch (which) {
+            case LVBGS_MAP_SAMPLE_COLOR:
+            case LVBGS_MAP_SAMPLE_GRAD: return N * npx * C;
+            case LVBGS_MAP_R:
+            case LVBGS_MAP_T:
+            case LVBGS_MAP_DMIN_LT: return npx * 4;
+            case LVBGS_MAP_GRAD: return npx * C;
+            case LVBGS_MAP_MEAN_GRAD: return 4;
+            case LVBGS_MAP_ROI: return npx;
+            default: return 0;
+        }
     switch (which) {
         case LVBGS_MAP_LAST_FG:
         case LVBGS_MAP_ROI: return npx;
@@ -875,6 +1272,7 @@ size_t lob_map_bytes(const LobState& L, int which) {
 
 lvbgs_status lob_get_map(LobState& L, int which, void* hostOut, size_t bytes, cudaStream_t st, std::string& err) {
     LobDev& D = L.d;
+    LOB_CUDA(cudaEventSynchronize(L.meanDone), "frame step");
     const size_t need = lob_map_bytes(L, which);
     if (need == 0) {
         err = "map not kept by LOBSTER";
@@ -885,7 +1283,18 @@ lvbgs_status lob_get_map(LobState& L, int which, void* hostOut, size_t bytes, cu
         return LVBGS_BAD_ARG;
     }
     const void* src = nullptr;
+    const float* fm = D.fm ? D.fm + (size_t)D.cur * 3 * D.npx : nullptr;
     if (D.alg == ALG_VIBE) src = which == LVBGS_MAP_ROI ? (const void*)D.roi : (const void*)D.sC;
+    else if (D.alg == ALG_PBAS) switch (which) {
+            case LVBGS_MAP_SAMPLE_COLOR: src = D.sC; break;
+            case LVBGS_MAP_SAMPLE_GRAD: src = D.sG; break;
+            case LVBGS_MAP_R: src = fm; break;
+            case LVBGS_MAP_T: src = fm + D.npx; break;
+            case LVBGS_MAP_DMIN_LT: src = fm + 2 * (size_t)D.npx; break;
+            case LVBGS_MAP_GRAD: src = D.grad; break;
+            case LVBGS_MAP_MEAN_GRAD: src = D.meanGrad; break;
+            default: src = D.roi; break;
+        }
     else switch (which) {
         case LVBGS_MAP_LAST_FG: src = D.lastFG; break;
         case LVBGS_MAP_ROI: src = D.roi; break;
@@ -913,6 +1322,7 @@ lvbgs_status lob_get_map(LobState& L, int which, void* hostOut, size_t bytes, cu
 }
 
 lvbgs_status lob_stats(LobState& L, unsigned long long out[2], cudaStream_t st, std::string& err) {
+    LOB_CUDA(cudaEventSynchronize(L.meanDone), "frame step");
     LOB_CUDA(cudaMemcpyAsync(out, L.d.stats, 16, cudaMemcpyDeviceToHost, st), "statistics download");
     LOB_CUDA(cudaStreamSynchronize(st), "statistics download");
     return LVBGS_OK;

@@ -851,7 +851,8 @@ lvbgs_status pw_initialize(lvbgs_ctx* h, const uint8_t* img, int W, int H, int C
 }
 
 // LOBSTER initialize() (BackgroundSubtractorLOBSTER.cpp:442-457) on the validated ROI, or ViBe's
-// (BackgroundSubtractorViBe.cpp:57-75 / :112-134) on every pixel
+// (BackgroundSubtractorViBe.cpp:57-75 / :112-134) or PBAS's (BackgroundSubtractorPBAS.cpp:61-109 /
+// :287-324) on every pixel
 lvbgs_status lob_initialize(lvbgs_ctx* h, const uint8_t* img, int W, int H, int C, size_t stride,
                             const std::vector<uint8_t>& newroi, size_t orig, size_t fin) {
     if (h->stream) cudaStreamSynchronize(h->stream);
@@ -860,8 +861,8 @@ lvbgs_status lob_initialize(lvbgs_ctx* h, const uint8_t* img, int W, int H, int 
     h->initialized = false;
     h->spilled = false;
     std::string err;
-    lvbgs_status s = lob_setup(*h->lob, h->algo == LVBGS_ALGO_VIBE ? ALG_VIBE : ALG_LOBSTER, h->prm, W, H, C, newroi,
-                               orig, fin, h->stream, err);
+    const int alg = h->algo == LVBGS_ALGO_VIBE ? ALG_VIBE : h->algo == LVBGS_ALGO_PBAS ? ALG_PBAS : ALG_LOBSTER;
+    lvbgs_status s = lob_setup(*h->lob, alg, h->prm, W, H, C, newroi, orig, fin, h->stream, err);
     if (s != LVBGS_OK) return fail(h, s, err);
     h->W = W;
     h->H = H;
@@ -1045,6 +1046,21 @@ lvbgs_status lvbgs_debug_inject_fault(lvbgs_handle h, int kind) {
 
 lvbgs_status lvbgs_default_params(lvbgs_algo algo, lvbgs_params* out) {
     if (!out) return fail(nullptr, LVBGS_BAD_ARG, "null output");
+    out->update_rate = 16.0f;  // PBAS's BGSPBAS_DEFAULT_LEARNING_RATE (BackgroundSubtractorPBAS.hpp:55)
+    if (algo == LVBGS_ALGO_PBAS) {
+        // BackgroundSubtractorPBAS.hpp:48-55 (min_color_dist_threshold carries nInitColorDistThreshold)
+        out->desc_dist_threshold_offset = 0;
+        out->min_color_dist_threshold = 30;
+        out->bg_samples = 35;
+        out->required_bg_samples = 2;
+        out->samples_for_moving_avgs = 100;
+        out->rel_lbsp_threshold = 0.333f;
+        out->lbsp_threshold_offset = 0;
+        out->default_median_blur_kernel_size = 9;
+        out->seed = 0;
+        out->device_id = 0;
+        return LVBGS_OK;
+    }
     if (algo == LVBGS_ALGO_PAWCS) {
         // BackgroundSubtractorPAWCS.hpp:22-29 (bg_samples carries nMaxNbWords), BackgroundSubtractorLBSP.hpp:23-28
         out->desc_dist_threshold_offset = 2;
@@ -1105,7 +1121,8 @@ lvbgs_status lvbgs_default_params(lvbgs_algo algo, lvbgs_params* out) {
 lvbgs_status lvbgs_create(lvbgs_algo algo, const lvbgs_params* p, lvbgs_handle* out) {
     if (!out) return fail(nullptr, LVBGS_BAD_ARG, "null output handle");
     *out = nullptr;
-    if (algo != LVBGS_ALGO_SUBSENSE && algo != LVBGS_ALGO_PAWCS && algo != LVBGS_ALGO_LOBSTER && algo != LVBGS_ALGO_VIBE)
+    if (algo != LVBGS_ALGO_SUBSENSE && algo != LVBGS_ALGO_PAWCS && algo != LVBGS_ALGO_LOBSTER && algo != LVBGS_ALGO_VIBE &&
+        algo != LVBGS_ALGO_PBAS)
         return fail(nullptr, LVBGS_BAD_ARG, "unknown algorithm");
     lvbgs_params prm;
     if (p) prm = *p;
@@ -1120,8 +1137,12 @@ lvbgs_status lvbgs_create(lvbgs_algo algo, const lvbgs_params* p, lvbgs_handle* 
     // BackgroundSubtractorSuBSENSE.cpp:76-77, BackgroundSubtractorLBSP.hpp:53
     if (prm.bg_samples == 0 || prm.required_bg_samples > prm.bg_samples)
         return fail(nullptr, LVBGS_BAD_ARG, "algo cannot require more sample matches than sample count in model");
-    // ViBe's constructor checks the sample counts only (BackgroundSubtractorViBe.cpp:28)
-    if (algo != LVBGS_ALGO_VIBE && prm.min_color_dist_threshold == 0 && prm.desc_dist_threshold_offset == 0)
+    // ViBe's constructor checks the sample counts only (BackgroundSubtractorViBe.cpp:28); PBAS's also the
+    // update rate (BackgroundSubtractorPBAS.cpp:31-32)
+    if (algo == LVBGS_ALGO_PBAS && !(prm.update_rate > 0 && prm.update_rate <= 255))
+        return fail(nullptr, LVBGS_BAD_ARG, "update rate must be in (0, 255]");
+    if (algo != LVBGS_ALGO_VIBE && algo != LVBGS_ALGO_PBAS && prm.min_color_dist_threshold == 0 &&
+        prm.desc_dist_threshold_offset == 0)
         return fail(nullptr, LVBGS_BAD_ARG, "distance thresholds must be positive values");
     if (!(prm.rel_lbsp_threshold >= 0)) return fail(nullptr, LVBGS_BAD_ARG, "relative threshold for LBSP features must be non-negative");
     if (prm.bg_samples > (size_t)kMaxSamples)
@@ -1161,7 +1182,7 @@ lvbgs_status lvbgs_create(lvbgs_algo algo, const lvbgs_params* p, lvbgs_handle* 
     }
     lvbgs_ctx* h = new lvbgs_ctx();
     h->algo = algo;
-    if (algo == LVBGS_ALGO_LOBSTER || algo == LVBGS_ALGO_VIBE) h->lob = new LobState();
+    if (algo == LVBGS_ALGO_LOBSTER || algo == LVBGS_ALGO_VIBE || algo == LVBGS_ALGO_PBAS) h->lob = new LobState();
     h->prm = prm;
     h->device = prm.device_id;
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -1208,9 +1229,10 @@ lvbgs_status lvbgs_initialize(lvbgs_handle h, const uint8_t* img, int W, int H, 
     const size_t row = (size_t)W * C;
     if (stride == 0) stride = row;
     if (stride < row) return fail(h, LVBGS_BAD_ARG, "image stride is smaller than width*channels");
-    if (h->algo == LVBGS_ALGO_VIBE) {
-        // ViBe's initialize(img) takes no ROI and uses every pixel (BackgroundSubtractorViBe.cpp:57-75)
-        if (roi) return fail(h, LVBGS_UNSUPPORTED, "ViBe has no region of interest");
+    if (h->algo == LVBGS_ALGO_VIBE || h->algo == LVBGS_ALGO_PBAS) {
+        // ViBe's and PBAS's initialize(img) take no ROI and use every pixel (BackgroundSubtractorViBe.cpp:57-75,
+        // BackgroundSubtractorPBAS.cpp:61-109)
+        if (roi) return fail(h, LVBGS_UNSUPPORTED, "ViBe and PBAS have no region of interest");
         return lob_initialize(h, img, W, H, C, stride, std::vector<uint8_t>(npx, 255), npx, npx);
     }
     // ROI handling (BackgroundSubtractionUtils.cpp:83-101, validateROI :28-36)
@@ -1317,10 +1339,11 @@ lvbgs_status lvbgs_apply(lvbgs_handle h, const uint8_t* img, size_t stride, uint
     if (!img) return fail(h, LVBGS_BAD_ARG, "null input image");
     cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : h->stream;
     if (h->algo == LVBGS_ALGO_PAWCS) return pw_apply(h, img, stride, mask, lr, st);
-    if (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE) {
+    if (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE || h->algo == LVBGS_ALGO_PBAS) {
         // BackgroundSubtractorLOBSTER.cpp:463, BackgroundSubtractorViBe.cpp:79: the rate is reinterpreted as an
-        // integer and must be positive
-        if (!(lr > 0)) return fail(h, LVBGS_BAD_ARG, "learning rate must be a positive value; faster learning is achieved with smaller values");
+        // integer and must be positive; PBAS's learningRateOverride replaces T(x) when positive (:174 / :402)
+        if (h->algo != LVBGS_ALGO_PBAS && !(lr > 0))
+            return fail(h, LVBGS_BAD_ARG, "learning rate must be a positive value; faster learning is achieved with smaller values");
         const uint8_t* dimg = nullptr;
         if ((s = stage_frame(h, img, stride, st, &dimg)) != LVBGS_OK) return s;
         const bool devMask = mask && is_device_ptr(mask);
@@ -1638,7 +1661,7 @@ lvbgs_status lvbgs_get_background(lvbgs_handle h, uint8_t* out) {
     lvbgs_status s = check_ready(h);
     if (s != LVBGS_OK) return s;
     if (!out) return fail(h, LVBGS_BAD_ARG, "null output");
-    if (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE) {
+    if (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE || h->algo == LVBGS_ALGO_PBAS) {
         std::string err;
         s = lob_background(*h->lob, out, false, h->stream, err);
         return s == LVBGS_OK ? s : fail(h, s, err);
@@ -1666,7 +1689,8 @@ lvbgs_status lvbgs_get_background_descriptors(lvbgs_handle h, uint16_t* out) {
     lvbgs_status s = check_ready(h);
     if (s != LVBGS_OK) return s;
     if (!out) return fail(h, LVBGS_BAD_ARG, "null output");
-    if (h->algo == LVBGS_ALGO_VIBE) return fail(h, LVBGS_UNSUPPORTED, "ViBe keeps no descriptors");
+    if (h->algo == LVBGS_ALGO_VIBE || h->algo == LVBGS_ALGO_PBAS)
+        return fail(h, LVBGS_UNSUPPORTED, "ViBe and PBAS keep no descriptors");
     if (h->algo == LVBGS_ALGO_LOBSTER) {
         std::string err;
         s = lob_background(*h->lob, out, true, h->stream, err);
@@ -1692,7 +1716,8 @@ lvbgs_status lvbgs_refresh_model(lvbgs_handle h, float frac, int force) {
     if (s != LVBGS_OK) return s;
     if (h->algo == LVBGS_ALGO_PAWCS)
         return fail(h, LVBGS_BAD_ARG, "PAWCS's refreshModel takes (base occurrences, decrement fraction, force): use lvbgs_pawcs_refresh_model");
-    if (h->algo == LVBGS_ALGO_VIBE) return fail(h, LVBGS_UNSUPPORTED, "ViBe has no refreshModel");
+    if (h->algo == LVBGS_ALGO_VIBE || h->algo == LVBGS_ALGO_PBAS)
+        return fail(h, LVBGS_UNSUPPORTED, "ViBe and PBAS have no refreshModel");
     if (!(frac > 0.0f && frac <= 1.0f)) return fail(h, LVBGS_BAD_ARG, "model refresh must be given as a non-null fraction");
     if (h->algo == LVBGS_ALGO_LOBSTER) {
         std::string err;
@@ -1723,8 +1748,8 @@ lvbgs_status lvbgs_set_automatic_model_reset(lvbgs_handle h, int enabled) {
     lvbgs_status s = check_ready(h);
     if (s != LVBGS_OK) return s;
     const int v = enabled ? 1 : 0;
-    // LOBSTER keeps the flag of its base class but has no automatic model reset; ViBe has neither
-    if (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE) return LVBGS_OK;
+    // LOBSTER keeps the flag of its base class but has no automatic model reset; ViBe and PBAS have neither
+    if (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE || h->algo == LVBGS_ALGO_PBAS) return LVBGS_OK;
     LV_CUDA(h, cudaMemcpy(&h->sd.ctl->auto_reset, &v, sizeof(v), cudaMemcpyHostToDevice), "control write");
     return LVBGS_OK;
 }
@@ -1732,13 +1757,18 @@ lvbgs_status lvbgs_set_automatic_model_reset(lvbgs_handle h, int enabled) {
 // getDefaultLearningRate(): LOBSTER's BGSLOBSTER_DEFAULT_LEARNING_RATE (BackgroundSubtractorLOBSTER.hpp:31,57);
 // 0 (the internal T(x)) for the others
 double lvbgs_get_default_learning_rate(lvbgs_handle h) {
+    if (!h) return 0.0;
     // BGSLOBSTER_DEFAULT_LEARNING_RATE and BGSVIBE_DEFAULT_LEARNING_RATE (BackgroundSubtractorViBe.hpp:46)
-    return h && (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE) ? 16.0 : 0.0;
+    if (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE) return 16.0;
+    // BGSPBAS_DEFAULT_LEARNING_RATE_OVERRIDE (BackgroundSubtractorPBAS.hpp:57): no override
+    if (h->algo == LVBGS_ALGO_PBAS) return -1.0;
+    return 0.0;
 }
 
 lvbgs_status lvbgs_set_roi(lvbgs_handle h, const uint8_t* roi, int width, int height) {
     if (!h || !roi || width <= 0 || height <= 0) return fail(h, LVBGS_BAD_ARG, "null or empty ROI");
-    if (h->algo == LVBGS_ALGO_VIBE) return fail(h, LVBGS_UNSUPPORTED, "ViBe has no region of interest");
+    if (h->algo == LVBGS_ALGO_VIBE || h->algo == LVBGS_ALGO_PBAS)
+        return fail(h, LVBGS_UNSUPPORTED, "ViBe and PBAS have no region of interest");
     const size_t npx = (size_t)width * height;
     std::vector<uint8_t> r(npx);
     if (is_device_ptr(roi)) LV_CUDA(h, cudaMemcpy(r.data(), roi, npx, cudaMemcpyDeviceToHost), "roi download");
@@ -1812,7 +1842,7 @@ size_t lvbgs_device_bytes(lvbgs_algo algo, int W, int H, int C, size_t N) {
 lvbgs_status lvbgs_spill(lvbgs_handle h, void* host, size_t bytes) {
     lvbgs_status s = check_ready(h);
     if (s != LVBGS_OK) return s;
-    if (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE)
+    if (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE || h->algo == LVBGS_ALGO_PBAS)
         return fail(h, LVBGS_UNSUPPORTED, "spilling is implemented for SuBSENSE and PAWCS streams");
     if (!host || bytes < h->persistBytes) return fail(h, LVBGS_BAD_ARG, "spill buffer is smaller than lvbgs_state_bytes()");
     LV_CUDA(h, cudaStreamSynchronize(h->stream), "spill");
@@ -1895,7 +1925,7 @@ const char* lvbgs_last_error(lvbgs_handle h) {
 lvbgs_status lvbgs_debug_map_bytes(lvbgs_handle h, int which, size_t* bytes) {
     if (!h || !bytes) return fail(h, LVBGS_BAD_ARG, "null argument");
     if (!h->initialized) return fail(h, LVBGS_NOT_INITIALIZED, "algo must be initialized first");
-    if (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE) {
+    if (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE || h->algo == LVBGS_ALGO_PBAS) {
         *bytes = lob_map_bytes(*h->lob, which);
         return *bytes ? LVBGS_OK : fail(h, LVBGS_BAD_ARG, "map not kept by this algorithm");
     }
@@ -1919,7 +1949,7 @@ lvbgs_status lvbgs_debug_get_map(lvbgs_handle h, int which, void* out, size_t by
     size_t need = 0;
     if ((s = lvbgs_debug_map_bytes(h, which, &need)) != LVBGS_OK) return s;
     if (!out || bytes < need) return fail(h, LVBGS_BAD_ARG, "output buffer too small");
-    if (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE) {
+    if (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE || h->algo == LVBGS_ALGO_PBAS) {
         std::string err;
         s = lob_get_map(*h->lob, which, out, bytes, h->stream, err);
         return s == LVBGS_OK ? s : fail(h, s, err);
@@ -2025,8 +2055,8 @@ lvbgs_status lvbgs_get_scalars(lvbgs_handle h, lvbgs_scalars* out) {
     lvbgs_status s = check_ready(h);
     if (s != LVBGS_OK) return s;
     if (!out) return fail(h, LVBGS_BAD_ARG, "null output");
-    if (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE) {
-        // LOBSTER and ViBe keep no frame-level state; frame_idx counts their apply() calls
+    if (h->algo == LVBGS_ALGO_LOBSTER || h->algo == LVBGS_ALGO_VIBE || h->algo == LVBGS_ALGO_PBAS) {
+        // LOBSTER, ViBe and PBAS keep no frame counter; frame_idx counts their apply() calls
         std::memset(out, 0, sizeof(*out));
         unsigned long long st[2] = {0, 0};
         std::string err;

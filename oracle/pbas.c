@@ -81,6 +81,7 @@ opbas_t* opbas_create(const opbas_params* p) {
     if (!(p->update_rate > 0 && p->update_rate <= 255)) return NULL;
     opbas_t* o = (opbas_t*)calloc(1, sizeof(opbas_t));
     o->p = *p;
+    o->meanGrad = 20.0f; /* m_fFormerMeanGradDist(20) (:29); initialize() keeps it */
     return o;
 }
 
@@ -88,8 +89,10 @@ static void pbas_free(opbas_t* o) {
     void* ptrs[] = {o->scol, o->sgrad, o->R, o->T, o->D, o->grad, o->rawFG, o->colcnt, o->kctr};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
     opbas_params p = o->p;
+    const float mean = o->meanGrad;
     memset(o, 0, sizeof(*o));
     o->p = p;
+    o->meanGrad = mean;
 }
 
 void opbas_destroy(opbas_t* o) {
@@ -150,7 +153,8 @@ static float pbas_l2(const uint8_t* a, const uint8_t* b) {
 }
 
 /* initialize (:61-109 / :287-324): maps at their starting values, every sample of every pixel (colour
- * and gradient) from a 7x7 Gaussian position of the frame */
+ * and gradient) from a 7x7 Gaussian position of the frame; the frame-level mean gradient distance is
+ * the constructor's (20) or the last frame's */
 int opbas_initialize(opbas_t* o, const uint8_t* img, int W, int H, int C) {
     if (!img || W <= 0 || H <= 0) return OSUB_EBADARG;
     if (C != 1 && C != 3) return OSUB_EUNSUPPORTED;
@@ -173,7 +177,6 @@ int opbas_initialize(opbas_t* o, const uint8_t* img, int W, int H, int C) {
         o->R[i] = 1.0f;
         o->T[i] = o->p.update_rate;
     }
-    o->meanGrad = 20.0f;
     o->frames = 0;
     opbas_gradient(img, W, H, C, o->grad);
     for (size_t s = 0; s < N; ++s)
@@ -249,7 +252,9 @@ int opbas_apply(opbas_t* o, const uint8_t* img, uint8_t* mask, double lr_overrid
                 *Tp += PBAS_T_INCR / ((*Dp) * PBAS_T_SCALE + PBAS_T_OFFST);
                 if (*Tp > PBAS_T_UPPER) *Tp = PBAS_T_UPPER;
             } else {
-                const size_t nLR = lr_override > 0 ? (size_t)ceil(lr_override) : (size_t)ceil((double)*Tp);
+                /* +inf (undefined behaviour in the conversion) is taken as SIZE_MAX, as LOBSTER does */
+                const size_t nLR = lr_override > 0 ? (isinf(lr_override) ? (size_t)-1 : (size_t)ceil(lr_override))
+                                                   : (size_t)ceil((double)*Tp);
                 if (((size_t)pdraw(o, px) % nLR) == 0) {
                     const size_t rs = (size_t)pdraw(o, px) % N;
                     memcpy(o->scol + rs * npx * C + px * C, in, (size_t)C);

@@ -697,12 +697,16 @@ int rpbas_initialize(void* h, const uint8_t* img, int W, int H, int C) {
     o->frames = 0;
     o->rng.start_frame((size_t)W * H);
     return guarded(o->rng, [&] {
-        if (C == 1)
+        // one instance per channel count, initialized again like a user's (which keeps its former mean
+        // gradient distance)
+        if (o->algo && o->C == C) {
+        } else if (C == 1) {
             o->algo.reset(new RefPbasT<BackgroundSubtractorPBAS_1ch>(o->p.color_dist_threshold, o->p.update_rate,
                                                                      o->p.bg_samples, o->p.required_bg_samples));
-        else
+        } else {
             o->algo.reset(new RefPbasT<BackgroundSubtractorPBAS_3ch>(o->p.color_dist_threshold, o->p.update_rate,
                                                                      o->p.bg_samples, o->p.required_bg_samples));
+        }
         o->W = W;
         o->H = H;
         o->C = C;

@@ -116,7 +116,8 @@ int ovibe_apply(ovibe_t* o, const uint8_t* img, uint8_t* mask, double lr) {
     if (!img || !mask || !(lr > 0)) return OSUB_EBADARG;
     const int W = o->W, H = o->H, C = o->C;
     const size_t N = o->p.bg_samples, npx = o->npx, nreq = o->p.required_bg_samples, R = o->p.color_dist_threshold;
-    const size_t nLR = (size_t)ceil(lr);
+    /* (size_t)ceil(lr); +inf (undefined behaviour in the conversion) is taken as SIZE_MAX, as LOBSTER does */
+    const size_t nLR = isinf(lr) ? (size_t)-1 : (size_t)ceil(lr);
     ++o->frames;
     memset(o->kctr, 0, npx * sizeof(uint32_t));
     memset(mask, 0, npx);

@@ -47,6 +47,12 @@ def test_default_params_match_reference(product_lib):
     assert (p.desc_dist_threshold_offset, p.min_color_dist_threshold, p.bg_samples, p.required_bg_samples,
             p.lbsp_threshold_offset, p.default_median_blur_kernel_size) == (4, 30, 35, 2, 0, 9)
     assert abs(p.rel_lbsp_threshold - 0.333) < 1e-7
+    # BackgroundSubtractorViBe.hpp:39-46: colour 20, 20 samples, 2 required
+    assert product_lib.lvbgs_default_params(L.ALGO_VIBE, C.byref(p)) == L.OK
+    assert (p.min_color_dist_threshold, p.bg_samples, p.required_bg_samples) == (20, 20, 2)
+    # BackgroundSubtractorPBAS.hpp:48-55: colour 30, update rate 16, 35 samples, 2 required
+    assert product_lib.lvbgs_default_params(L.ALGO_PBAS, C.byref(p)) == L.OK
+    assert (p.min_color_dist_threshold, p.update_rate, p.bg_samples, p.required_bg_samples) == (30, 16.0, 35, 2)
     assert product_lib.lvbgs_default_params(7, C.byref(p)) == L.BAD_ARG
 
 
@@ -64,6 +70,11 @@ def test_create_rejects_bad_parameters(product_lib):
     product_lib.lvbgs_default_params(L.ALGO_SUBSENSE, C.byref(p))
     p.bg_samples = 65
     assert product_lib.lvbgs_create(L.ALGO_SUBSENSE, C.byref(p), C.byref(h)) == L.UNSUPPORTED
+    # PBAS's update rate must be in (0, 255] (BackgroundSubtractorPBAS.cpp:32)
+    for rate in (0.0, -1.0, 256.0, float("nan")):
+        product_lib.lvbgs_default_params(L.ALGO_PBAS, C.byref(p))
+        p.update_rate = rate
+        assert product_lib.lvbgs_create(L.ALGO_PBAS, C.byref(p), C.byref(h)) == L.BAD_ARG
 
 
 def test_null_handle_calls_fail_cleanly(product_lib):

@@ -302,3 +302,12 @@ def test_pbas(config, channels):
             assert np.array_equal(port.state_map(n), ref.state_map(n)), "frame %d: %s differs" % (t, n)
         assert port.mean_grad() == ref.mean_grad(), "frame %d: mean gradient distance" % t
     assert np.array_equal(port.background(), ref.background())
+    # initialize() again: new samples and maps, the former mean gradient distance kept
+    port.initialize(fr[5])
+    ref.initialize(fr[5])
+    assert port.mean_grad() == ref.mean_grad() != 20.0
+    for t, f in enumerate(fr[6:9], start=1):
+        mp, mr = port.apply(f, -1.0), ref.apply(f, -1.0)
+        assert np.array_equal(mp, mr), "again, frame %d: mask differs" % t
+        for n in names:
+            assert np.array_equal(port.state_map(n), ref.state_map(n)), "again, frame %d: %s differs" % (t, n)
