@@ -325,7 +325,7 @@ __device__ uint32_t pbas_eval_px(const LobDev& D, int p, int x, int y, const uin
     fn[p] = Rn;
     fn[npx + p] = Tn;
     fn[2 * npx + p] = Dn;
-    D.badSum[p] = badSum;
+    if (C == 1) D.badSum[p] = badSum;  // three channels keep the values themselves (badVals)
     D.badCnt[p] = (uint8_t)nb;
     return w | (k << 27);
 }
@@ -376,6 +376,9 @@ __global__ void __launch_bounds__(kThreadsL) lob_k_eval(LobDev D) {
             // the sample word this pixel writes: LOBSTER, its descriptors (:499-500 / :548-550) and colour;
             // ViBe, its colour; PBAS, its colour and gradient (also what a neighbour update writes into it)
             unsigned long long wd = 0;
+            LobOvr none;
+            none.n = 0;
+            none.mask = 0;
             if (ALG == ALG_PBAS) {
                 uint32_t g[C];
 #pragma unroll
@@ -384,27 +387,20 @@ __global__ void __launch_bounds__(kThreadsL) lob_k_eval(LobDev D) {
                     wd |= ((unsigned long long)curr[c] << (8 * c)) | ((unsigned long long)g[c] << (24 + 8 * c));
                 }
                 D.wD[p] = wd;
-                LobOvr none;
-                none.n = 0;
-                none.mask = 0;
                 D.intent[p] = pbas_eval_px<C, false>(D, p, x, y, curr, g, none, &scanned);
-                warp_add(&D.stats[0], scanned);
-                return;
-            }
-            if (ALG == ALG_VIBE) {
-#pragma unroll
-                for (int c = 0; c < C; ++c) wd |= (unsigned long long)curr[c] << (8 * c);
             } else {
+                if (ALG == ALG_VIBE) {
 #pragma unroll
-                for (int c = 0; c < C; ++c)
-                    wd |= (unsigned long long)lbsp_thr(vals[c], curr[c], __ldg(D.lut + curr[c])) << (16 * c);
-                if (C == 3) wd |= ((unsigned long long)curr[0] << 48) | ((unsigned long long)curr[1] << 56);
+                    for (int c = 0; c < C; ++c) wd |= (unsigned long long)curr[c] << (8 * c);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < C; ++c)
+                        wd |= (unsigned long long)lbsp_thr(vals[c], curr[c], __ldg(D.lut + curr[c])) << (16 * c);
+                    if (C == 3) wd |= ((unsigned long long)curr[0] << 48) | ((unsigned long long)curr[1] << 56);
+                }
+                D.wD[p] = wd;
+                D.intent[p] = eval_px<C, ALG, false>(D, p, x, y, vals, curr, none, &scanned);
             }
-            D.wD[p] = wd;
-            LobOvr none;
-            none.n = 0;
-            none.mask = 0;
-            D.intent[p] = eval_px<C, ALG, false>(D, p, x, y, vals, curr, none, &scanned);
         }
     }
     warp_add(&D.stats[0], scanned);
