@@ -289,18 +289,27 @@ def single_stream_run(config, n_frames, stream, cpu=True, cpu_frames=4):
     return out
 
 
-def lobster_run(config, n_frames, stream, cpu=True, cpu_frames=4):
-    """LOBSTER (BackgroundSubtractorLOBSTER's non-parallel path) on the scenes of SuBSENSE configs 0 and 1
-    (one seeded stream: 320x240 BGR; 1920x1080 BGR) at the reference's default learning rate (16): every
-    frame through lvbgs_apply from frames resident on the device, wall clock per frame (the first 10
-    frames are warm-up); the CPU baseline is the oracle's LOBSTER on one core over the first cpu_frames
-    frames."""
+SAMPLE_MODELS = {
+    # name: (Python class, learning-rate argument of apply, the reference's default rate, description)
+    "lobster": ("BackgroundSubtractorLOBSTER", 16.0, "LOBSTER (BackgroundSubtractorLOBSTER's non-parallel path)"),
+    "vibe": ("BackgroundSubtractorViBe", 16.0, "ViBe (BackgroundSubtractorViBe_3ch)"),
+    "pbas": ("BackgroundSubtractorPBAS", -1.0, "PBAS (BackgroundSubtractorPBAS_3ch, per-pixel update rates T(x))"),
+}
+
+
+def sample_model_run(algo, config, n_frames, stream, cpu=True, cpu_frames=4):
+    """LOBSTER, ViBe or PBAS on the scenes of SuBSENSE configs 0 and 1 (one seeded stream: 320x240 BGR;
+    1920x1080 BGR) at the reference's default learning rate: every frame through lvbgs_apply from frames
+    resident on the device, wall clock per frame (the first 10 frames are warm-up); the CPU baseline is
+    the oracle's restatement on one core over the first cpu_frames frames."""
     import ctypes as C
     import numpy as np
     import torch
-    from litiv_gb300 import BackgroundSubtractorLOBSTER, SyntheticStream
+    import litiv_gb300
+    from litiv_gb300 import SyntheticStream
     from litiv_gb300 import _lib as L
     from litiv_gb300.metrics import BinClassif
+    cls_name, lr, what = SAMPLE_MODELS[algo]
     lib = L.lib()
     s = SyntheticStream(config, 0, 1)
     W, H = s.cfg.width, s.cfg.height
@@ -311,13 +320,13 @@ def lobster_run(config, n_frames, stream, cpu=True, cpu_frames=4):
         s.render_device(t, dev[t].data_ptr(), dgt[t].data_ptr(), cuda_stream=stream.cuda_stream)
     dmask = torch.empty((H, W), dtype=torch.uint8, device="cuda")
     torch.cuda.synchronize()
-    b = BackgroundSubtractorLOBSTER(seed=1)
+    b = getattr(litiv_gb300, cls_name)(seed=1)
     b.initialize(dev[0])
     ms = []
     quality = BinClassif()
     for t in range(1, n):
         t0 = time.perf_counter()
-        st = lib.lvbgs_apply(b.handle, C.c_void_p(dev[t].data_ptr()), 0, C.c_void_p(dmask.data_ptr()), 16.0,
+        st = lib.lvbgs_apply(b.handle, C.c_void_p(dev[t].data_ptr()), 0, C.c_void_p(dmask.data_ptr()), lr,
                              C.c_void_p(stream.cuda_stream))
         stream.synchronize()
         ms.append((time.perf_counter() - t0) * 1e3)
@@ -328,8 +337,8 @@ def lobster_run(config, n_frames, stream, cpu=True, cpu_frames=4):
     b.close()
     qm = quality.metrics()
     m = np.array(ms[9:])
-    out = {"workload": "LOBSTER: one %dx%d %s stream (the SuBSENSE config %d scene), %d frames, default "
-                       "parameters, learning rate 16" % (W, H, "BGR" if s.cfg.channels == 3 else "gray", config, n),
+    out = {"workload": "%s: one %dx%d %s stream (the SuBSENSE config %d scene), %d frames, default parameters, "
+                       "learning rate %g" % (what, W, H, "BGR" if s.cfg.channels == 3 else "gray", config, n, lr),
            "value": W * H / (m.mean() / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_frame": float(m.mean()),
            "p50_frame_ms": float(np.percentile(m, 50)), "p99_frame_ms": float(np.percentile(m, 99)),
            "quality": {"f_measure": qm["dFMeasure"], "recall": qm["dRecall"], "precision": qm["dPrecision"],
@@ -337,12 +346,27 @@ def lobster_run(config, n_frames, stream, cpu=True, cpu_frames=4):
     if cpu:
         from oracle import pyoracle
         fr = np.stack([s.render(t) for t in range(cpu_frames + 1)])
-        wall = pyoracle.run_lobster_streams([fr], [1], 1)
+        if algo == "lobster":
+            wall = pyoracle.run_lobster_streams([fr], [1], 1)
+        else:
+            o = (pyoracle.OracleViBe if algo == "vibe" else pyoracle.OraclePBAS)(seed=1)
+            o.initialize(fr[0])
+            t0 = time.perf_counter()
+            for t in range(1, cpu_frames + 1):
+                o.apply(fr[t], lr)
+            wall = time.perf_counter() - t0
         px = W * H * cpu_frames
         out["cpu_baseline"] = {"value": px / wall / 1e6, "unit": "Mpix/s", "cores": 1, "kind": "port",
                                "sample": "the first %d applied frames on one core, %.1f Mpix in %.2f s" % (
                                    cpu_frames, px / 1e6, wall)}
     return out
+
+
+def sample_models_run(n_frames, stream, cpu=True):
+    """the LOBSTER, ViBe and PBAS legs, each on the 320x240 and 1920x1080 scenes"""
+    return {algo: {"config0": sample_model_run(algo, 0, n_frames, stream, cpu=cpu, cpu_frames=10),
+                   "config1": sample_model_run(algo, 1, n_frames, stream, cpu=cpu, cpu_frames=2)}
+            for algo in SAMPLE_MODELS}
 
 
 def serving_run(seconds, pawcs_lanes=1):
@@ -412,13 +436,13 @@ def main():
     ap.add_argument("--single-frames", type=int, default=100,
                     help="frames of the single-stream SuBSENSE configs 0 and 1 (0: skip)")
     ap.add_argument("--lobster-frames", type=int, default=100,
-                    help="frames of the single-stream LOBSTER legs (0: skip)")
+                    help="frames of the single-stream LOBSTER, ViBe and PBAS legs (0: skip)")
     ap.add_argument("--pawcs-channels", default="both", choices=["1", "3", "both"],
                     help="PAWCS legs: the single-channel scene (config 2), the BGR scene, or both")
     ap.add_argument("--pawcs-only", action="store_true",
                     help="run the PAWCS workload alone and print its object (profiling)")
     ap.add_argument("--lobster-only", action="store_true",
-                    help="run the LOBSTER legs alone and print their object (profiling)")
+                    help="run the LOBSTER, ViBe and PBAS legs alone and print their object (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -446,10 +470,7 @@ def main():
         torch.cuda.set_device(0)
         stream = torch.cuda.Stream()
         torch.cuda.set_stream(stream)
-        print(json.dumps({"config0": lobster_run(0, args.lobster_frames, stream, cpu=not args.no_cpu_baseline,
-                                                 cpu_frames=10),
-                          "config1": lobster_run(1, args.lobster_frames, stream, cpu=not args.no_cpu_baseline,
-                                                 cpu_frames=2)}))
+        print(json.dumps(sample_models_run(args.lobster_frames, stream, cpu=not args.no_cpu_baseline)))
         return
 
     import numpy as np
@@ -710,10 +731,9 @@ def main():
                    "config1": single_stream_run(1, args.single_frames, stream, cpu=not args.no_cpu_baseline,
                                                 cpu_frames=2)}
 
-    lobster = None
+    models = {}
     if rank == 0 and args.lobster_frames > 0:
-        lobster = {"config0": lobster_run(0, args.lobster_frames, stream, cpu=not args.no_cpu_baseline, cpu_frames=10),
-                   "config1": lobster_run(1, args.lobster_frames, stream, cpu=not args.no_cpu_baseline, cpu_frames=2)}
+        models = sample_models_run(args.lobster_frames, stream, cpu=not args.no_cpu_baseline)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -752,7 +772,9 @@ def main():
             "serving": serve,
             "pawcs": pawcs,
             "single_stream": singles,
-            "lobster": lobster,
+            "lobster": models.get("lobster"),
+            "vibe": models.get("vibe"),
+            "pbas": models.get("pbas"),
             "clocks": clk.summary(),
         }
         print(json.dumps(out))
