@@ -752,51 +752,194 @@ __global__ void pbas_k_mean1_end(LobDev D) {
 }
 
 // three channels (:460): the float sum of the bad samples' gradient distances in raster order (pixel,
-// then scan order), which one thread adds up; the block stages the values of kMeanChunk pixels at a
-// time, compacted in order, in shared memory
-constexpr int kMeanThreads = 512, kMeanChunk = kMeanThreads;
-__global__ void __launch_bounds__(kMeanThreads) pbas_k_mean3(LobDev D) {
+// then scan order), s <- RN(s + v) value after value. The values are non-negative, so s only grows, and
+// while s stays in one binade [2^e, 2^(e+1)) with ulp u = 2^(e-23), RN(s + v) = s + u * q where q is
+// v / u rounded to an integer: up when the fraction is above 1/2, down when below, and on an exact 1/2
+// to the even quotient, which depends on the parity of s / u. The sum over a chunk of values is
+// therefore a function of that parity only: a transfer (d0, d1), the increment in ulps for an even or
+// odd start, composed value by value (d'_p = d_p + d2_{(p + d_p) & 1}).
+//   pbas_k_sum_chunks: the count of bad samples, and each chunk's total in double precision;
+//   pbas_k_sum_scan: their exclusive prefix, which predicts the binade of s at each chunk's start;
+//   pbas_k_sum_tr: each chunk's transfers for the predicted binade and the two beside it;
+//   pbas_k_sum_walk: from s = 0, chunk after chunk, applies the chunk's transfer when s is at least 1024,
+//     its binade is one of the chunk's three and the chunk cannot leave it (s / u + increment + 1 < 2^24:
+//     no value of the chunk reaches the next binade), and otherwise adds the chunk's values one by one.
+// The result is the sequential sum bit for bit; only the first chunks, those where s crosses a power of
+// two and those whose binade was mispredicted are summed value by value.
+constexpr int kSumChunk = 256, kSumNB = 3, kSumEMin = 10, kSumScan = 1024;
+struct Tr {
+    unsigned long long d0, d1;
+};
+__device__ __forceinline__ Tr tr_then(Tr a, Tr b) {
+    Tr r;
+    r.d0 = a.d0 + ((a.d0 & 1ull) ? b.d1 : b.d0);
+    r.d1 = a.d1 + ((a.d1 & 1ull) ? b.d0 : b.d1);
+    return r;
+}
+// one value v >= 0 in binade e: its increment in ulps for an even / odd s / u
+__device__ __forceinline__ Tr tr_value(float v, int e) {
+    const float x = v * __int_as_float((127 + 23 - e) << 23);  // v / u, exact (a power of two)
+    const float a = floorf(x), r = x - a;
+    const unsigned long long ai = (unsigned long long)a;
+    Tr t;
+    if (r > 0.5f) t.d0 = t.d1 = ai + 1ull;
+    else if (r < 0.5f) t.d0 = t.d1 = ai;
+    else {
+        t.d0 = ai + (ai & 1ull);  // even s/u: s/u + a is even when a is
+        t.d1 = ai + ((ai + 1ull) & 1ull);
+    }
+    return t;
+}
+__device__ __forceinline__ Tr tr_shfl_down(Tr t, int o) {
+    Tr r;
+    r.d0 = __shfl_down_sync(0xffffffffu, t.d0, o);
+    r.d1 = __shfl_down_sync(0xffffffffu, t.d1, o);
+    return r;
+}
+// binade of a positive float
+__device__ __forceinline__ int binade(float s) { return (int)((__float_as_uint(s) >> 23) & 0xffu) - 127; }
+
+struct SumWork {
+    double* chunkSum;  // [nChunks], then their exclusive prefix
+    Tr* tr;            // [nChunks][kSumNB]
+    int* eb;           // [nChunks]: the first of the chunk's binades
+};
+
+__global__ void __launch_bounds__(kSumChunk) pbas_k_sum_chunks(LobDev D, SumWork W) {
     if (!ld_vol(&D.flags[LOB_F_CONV])) return;
-    extern __shared__ float sm_vals[];  // kMeanChunk * N values
-    __shared__ int sm_warp[kMeanThreads / 32 + 1];
-    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-    float total = 0.0f;
-    unsigned long long nBad = 1;
-    for (int base = 0; base < D.npx; base += kMeanChunk) {
-        const int p = base + t;
-        const int n = p < D.npx ? (int)D.badCnt[p] : 0;
-        // exclusive scan of the counts over the block
-        int inc = n;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += v;
-        }
-        if (lane == 31) sm_warp[wid] = inc;
+    __shared__ double sm[kSumChunk / 32];
+    const int t = threadIdx.x, p = blockIdx.x * kSumChunk + t;
+    const int n = p < D.npx ? (int)D.badCnt[p] : 0;
+    double acc = 0.0;
+    for (int k = 0; k < n; ++k) acc += (double)__ldg(D.badVals + (size_t)p * D.N + k);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((t & 31) == 0) sm[t >> 5] = acc;
+    __syncthreads();
+    if (t == 0) {
+        double c = 0.0;
+        for (int w = 0; w < kSumChunk / 32; ++w) c += sm[w];
+        W.chunkSum[blockIdx.x] = c;
+    }
+    warp_add(&D.stats[3], (unsigned long long)n);
+}
+
+__global__ void __launch_bounds__(kSumScan) pbas_k_sum_scan(LobDev D, SumWork W, int nChunks) {
+    if (!ld_vol(&D.flags[LOB_F_CONV])) return;
+    __shared__ double sm[kSumScan];
+    const int t = threadIdx.x, per = (nChunks + kSumScan - 1) / kSumScan;
+    const int c0 = min(t * per, nChunks), c1 = min(c0 + per, nChunks);
+    double own = 0.0;
+    for (int c = c0; c < c1; ++c) own += W.chunkSum[c];
+    sm[t] = own;
+    __syncthreads();
+    for (int o = 1; o < kSumScan; o <<= 1) {
+        const double v = t >= o ? sm[t - o] : 0.0;
         __syncthreads();
-        if (wid == 0) {
-            int w = lane < kMeanThreads / 32 ? sm_warp[lane] : 0;
-            for (int o = 1; o < 32; o <<= 1) {
-                const int v = __shfl_up_sync(0xffffffffu, w, o);
-                if (lane >= o) w += v;
-            }
-            if (lane < kMeanThreads / 32) sm_warp[lane] = w;  // inclusive totals of the warps
-            if (lane == 31) sm_warp[kMeanThreads / 32] = w;
-        }
-        __syncthreads();
-        const int off = inc - n + (wid > 0 ? sm_warp[wid - 1] : 0);
-        for (int k = 0; k < n; ++k) sm_vals[off + k] = D.badVals[(size_t)p * D.N + k];
-        const int m = sm_warp[kMeanThreads / 32];
-        __syncthreads();
-        if (t == 0) {
-            float acc = total;
-            for (int k = 0; k < m; ++k) acc += sm_vals[k];
-            total = acc;
-            nBad += (unsigned long long)m;
-        }
+        sm[t] += v;
         __syncthreads();
     }
-    if (t == 0) {
-        const float mean = total / (float)nBad;
+    double run = sm[t] - own;
+    for (int c = c0; c < c1; ++c) {
+        const double v = W.chunkSum[c];
+        W.chunkSum[c] = run;
+        run += v;
+    }
+}
+
+__global__ void __launch_bounds__(kSumChunk) pbas_k_sum_tr(LobDev D, SumWork W) {
+    if (!ld_vol(&D.flags[LOB_F_CONV])) return;
+    __shared__ Tr sm[kSumChunk / 32][kSumNB];
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    const int p = blockIdx.x * kSumChunk + t;
+    const int n = p < D.npx ? (int)D.badCnt[p] : 0;
+    const float* v = D.badVals + (size_t)(p < D.npx ? p : 0) * D.N;
+    const float pre = (float)W.chunkSum[blockIdx.x];
+    const int e0 = max(pre >= 1.0f ? binade(pre) - 1 : kSumEMin, kSumEMin);
+    Tr acc[kSumNB];
+#pragma unroll
+    for (int j = 0; j < kSumNB; ++j) acc[j].d0 = acc[j].d1 = 0ull;
+    for (int k = 0; k < n; ++k) {
+        const float x = __ldg(v + k);
+#pragma unroll
+        for (int j = 0; j < kSumNB; ++j) acc[j] = tr_then(acc[j], tr_value(x, e0 + j));
+    }
+    // ordered reduction: lane 0 of each warp, then the warps in order
+#pragma unroll
+    for (int j = 0; j < kSumNB; ++j) {
+        for (int o = 1; o < 32; o <<= 1) {
+            const Tr y = tr_shfl_down(acc[j], o);
+            if ((lane & (2 * o - 1)) == 0) acc[j] = tr_then(acc[j], y);
+        }
+        if (lane == 0) sm[wid][j] = acc[j];
+    }
+    __syncthreads();
+    if (t < kSumNB) {
+        Tr r = sm[0][t];
+        for (int w = 1; w < kSumChunk / 32; ++w) r = tr_then(r, sm[w][t]);
+        W.tr[(size_t)blockIdx.x * kSumNB + t] = r;
+        if (t == 0) W.eb[blockIdx.x] = e0;
+    }
+}
+
+// the walk over the chunks (one warp; every lane holds the same sum), then the mean and its floor of 20
+__global__ void __launch_bounds__(32) pbas_k_sum_walk(LobDev D, SumWork W, int nChunks) {
+    if (!ld_vol(&D.flags[LOB_F_CONV])) return;
+    __shared__ float vals[32 * 64];
+    const int lane = threadIdx.x;
+    float s = 0.0f;
+    for (int c0 = 0; c0 < nChunks; c0 += 32) {
+        // the window's transfers, one chunk per lane
+        Tr tw[kSumNB];
+        int ew = 0;
+        if (c0 + lane < nChunks) {
+#pragma unroll
+            for (int j = 0; j < kSumNB; ++j) tw[j] = W.tr[(size_t)(c0 + lane) * kSumNB + j];
+            ew = W.eb[c0 + lane];
+        }
+        for (int j = 0; j < 32 && c0 + j < nChunks; ++j) {
+            const int c = c0 + j;
+            const unsigned int bits = __float_as_uint(s);
+            const int k = binade(s) - __shfl_sync(0xffffffffu, ew, j);
+            Tr tc;
+            tc.d0 = tc.d1 = 0ull;
+#pragma unroll
+            for (int i = 0; i < kSumNB; ++i) {
+                const unsigned long long a = __shfl_sync(0xffffffffu, tw[i].d0, j);
+                const unsigned long long b = __shfl_sync(0xffffffffu, tw[i].d1, j);
+                if (k == i) {
+                    tc.d0 = a;
+                    tc.d1 = b;
+                }
+            }
+            if (s >= 1024.0f && k >= 0 && k < kSumNB) {
+                const unsigned long long m = (unsigned long long)((bits & 0x7fffffu) | 0x800000u);
+                const unsigned long long m2 = m + ((m & 1ull) ? tc.d1 : tc.d0);
+                if (m2 + 1ull < (1ull << 24)) {
+                    s = __uint_as_float((bits & 0xff800000u) | ((unsigned int)m2 & 0x7fffffu));
+                    continue;
+                }
+            }
+            // value by value, 32 pixels at a time staged in shared memory, every lane adding them in order
+            const int pEnd = min((c + 1) * kSumChunk, D.npx);
+            for (int pg = c * kSumChunk; pg < pEnd; pg += 32) {
+                const int p = pg + lane;
+                const int n = p < pEnd ? (int)D.badCnt[p] : 0;
+                int off = n;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, off, o);
+                    if (lane >= o) off += y;
+                }
+                const int total = __shfl_sync(0xffffffffu, off, 31);
+                off -= n;
+                for (int q = 0; q < n; ++q) vals[off + q] = D.badVals[(size_t)p * D.N + q];
+                __syncwarp();
+                for (int q = 0; q < total; ++q) s += vals[q];
+                __syncwarp();
+            }
+        }
+    }
+    if (lane == 0) {
+        const float mean = s / (float)(D.stats[3] + 1ull);
         *D.meanGrad = mean > 20.0f ? mean : 20.0f;
     }
 }
@@ -965,6 +1108,8 @@ lvbgs_status lob_setup(LobState& L, int alg, const lvbgs_params& prm, int W, int
                  oSG = take(pb * N * npx * C), oGrad = take(pb * npx * C), oBlur = take(pb * npx * C),
                  oFm = take(pb * 6 * npx * 4), oMean = take(pb * 4), oBadSum = take(pb * (C == 1 ? npx * 4 : 0)),
                  oBadCnt = take(pb * npx), oBadVals = take(pb * (C == 3 ? npx * N * 4 : 0)),
+                 oSumTr = take(pb * (C == 3 ? (npx + kSumChunk - 1) / kSumChunk *
+                                                  (sizeof(double) + kSumNB * sizeof(Tr) + sizeof(int)) : 0)),
                  oRawPb = take(pb * npx);
     LOB_CUDA(cudaMalloc(&L.mem, off), "model allocation");
     if (!L.h_flags) LOB_CUDA(cudaHostAlloc((void**)&L.h_flags, LOB_F_WORDS * 4, cudaHostAllocDefault), "pinned allocation");
@@ -1014,6 +1159,7 @@ lvbgs_status lob_setup(LobState& L, int alg, const lvbgs_params& prm, int W, int
         D.badSum = (uint32_t*)(b + oBadSum);
         D.badCnt = b + oBadCnt;
         D.badVals = (float*)(b + oBadVals);
+        D.sumTr = b + oSumTr;
         D.rawFG = b + oRawPb;
         // the constructor's arguments (BackgroundSubtractorPBAS.cpp:21-32) and medianBlur(.., 9) (:266 / :494)
         D.R0 = (float)prm.min_color_dist_threshold;
@@ -1084,10 +1230,15 @@ lvbgs_status pbas_mean_launch(const LobDev& D, int sms, cudaStream_t st, std::st
         pbas_k_mean1<<<2 * sms, kThreadsL, 0, st>>>(D);
         pbas_k_mean1_end<<<1, 1, 0, st>>>(D);
     } else {
-        const size_t smem = (size_t)kMeanChunk * D.N * sizeof(float);
-        LOB_CUDA(cudaFuncSetAttribute(pbas_k_mean3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                 "mean kernel attribute");
-        pbas_k_mean3<<<1, kMeanThreads, smem, st>>>(D);
+        const int nChunks = (D.npx + kSumChunk - 1) / kSumChunk;
+        SumWork W;
+        W.chunkSum = (double*)D.sumTr;
+        W.tr = (Tr*)(W.chunkSum + nChunks);
+        W.eb = (int*)(W.tr + (size_t)nChunks * kSumNB);
+        pbas_k_sum_chunks<<<nChunks, kSumChunk, 0, st>>>(D, W);
+        pbas_k_sum_scan<<<1, kSumScan, 0, st>>>(D, W, nChunks);
+        pbas_k_sum_tr<<<nChunks, kSumChunk, 0, st>>>(D, W);
+        pbas_k_sum_walk<<<1, 32, 0, st>>>(D, W, nChunks);
     }
     return LVBGS_OK;
 }

@@ -58,6 +58,7 @@ struct LobDev {
     float *fm, *meanGrad, *badVals;
     uint32_t* badSum;
     uint8_t* badCnt;
+    void* sumTr;  // three channels: the per-chunk transfers of the mean's exact float sum
 };
 
 struct LobState {
