@@ -802,8 +802,10 @@ __device__ __forceinline__ int binade(float s) { return (int)((__float_as_uint(s
 struct SumWork {
     double* chunkSum;  // [nChunks], then their exclusive prefix
     Tr* tr;            // [nChunks][kSumNB]
+    Tr* trw;           // [nChunks][kSumChunk / 32][kSumNB]: the transfers of each chunk's 32-pixel granules
     int* eb;           // [nChunks]: the first of the chunk's binades
 };
+constexpr int kSumGran = kSumChunk / 32;
 
 __global__ void __launch_bounds__(kSumChunk) pbas_k_sum_chunks(LobDev D, SumWork W) {
     if (!ld_vol(&D.flags[LOB_F_CONV])) return;
@@ -870,7 +872,10 @@ __global__ void __launch_bounds__(kSumChunk) pbas_k_sum_tr(LobDev D, SumWork W) 
             const Tr y = tr_shfl_down(acc[j], o);
             if ((lane & (2 * o - 1)) == 0) acc[j] = tr_then(acc[j], y);
         }
-        if (lane == 0) sm[wid][j] = acc[j];
+        if (lane == 0) {
+            sm[wid][j] = acc[j];
+            W.trw[((size_t)blockIdx.x * kSumGran + wid) * kSumNB + j] = acc[j];
+        }
     }
     __syncthreads();
     if (t < kSumNB) {
@@ -881,7 +886,20 @@ __global__ void __launch_bounds__(kSumChunk) pbas_k_sum_tr(LobDev D, SumWork W) 
     }
 }
 
-// the walk over the chunks (one warp; every lane holds the same sum), then the mean and its floor of 20
+// s advanced by a transfer when s >= 1024 and the transfer keeps s in its binade; false otherwise
+__device__ __forceinline__ bool tr_apply(float& s, Tr t) {
+    if (s < 1024.0f) return false;
+    const unsigned int bits = __float_as_uint(s);
+    const unsigned long long m = (unsigned long long)((bits & 0x7fffffu) | 0x800000u);
+    const unsigned long long m2 = m + ((m & 1ull) ? t.d1 : t.d0);
+    if (m2 + 1ull >= (1ull << 24)) return false;
+    s = __uint_as_float((bits & 0xff800000u) | ((unsigned int)m2 & 0x7fffffu));
+    return true;
+}
+
+// the walk over the chunks (one warp; every lane holds the same sum), then the mean and its floor of 20:
+// 32 chunks at once when all of them have transfers for the binade of s (their ordered composition),
+// else chunk by chunk, else 32-pixel granule by granule, else value by value
 __global__ void __launch_bounds__(32) pbas_k_sum_walk(LobDev D, SumWork W, int nChunks) {
     if (!ld_vol(&D.flags[LOB_F_CONV])) return;
     __shared__ float vals[32 * 64];
@@ -891,15 +909,36 @@ __global__ void __launch_bounds__(32) pbas_k_sum_walk(LobDev D, SumWork W, int n
         // the window's transfers, one chunk per lane
         Tr tw[kSumNB];
         int ew = 0;
-        if (c0 + lane < nChunks) {
+        const bool in = c0 + lane < nChunks;
 #pragma unroll
-            for (int j = 0; j < kSumNB; ++j) tw[j] = W.tr[(size_t)(c0 + lane) * kSumNB + j];
+        for (int i = 0; i < kSumNB; ++i) tw[i].d0 = tw[i].d1 = 0ull;
+        if (in) {
+#pragma unroll
+            for (int i = 0; i < kSumNB; ++i) tw[i] = W.tr[(size_t)(c0 + lane) * kSumNB + i];
             ew = W.eb[c0 + lane];
+        }
+        {
+            const int k = binade(s) - ew;
+            Tr t;
+            t.d0 = t.d1 = 0ull;
+#pragma unroll
+            for (int i = 0; i < kSumNB; ++i)
+                if (k == i) t = tw[i];
+            if (__all_sync(0xffffffffu, !in || (k >= 0 && k < kSumNB))) {
+                for (int o = 1; o < 32; o <<= 1) {
+                    const Tr y = tr_shfl_down(t, o);
+                    if ((lane & (2 * o - 1)) == 0) t = tr_then(t, y);
+                }
+                Tr tot;
+                tot.d0 = __shfl_sync(0xffffffffu, t.d0, 0);
+                tot.d1 = __shfl_sync(0xffffffffu, t.d1, 0);
+                if (tr_apply(s, tot)) continue;
+            }
         }
         for (int j = 0; j < 32 && c0 + j < nChunks; ++j) {
             const int c = c0 + j;
-            const unsigned int bits = __float_as_uint(s);
-            const int k = binade(s) - __shfl_sync(0xffffffffu, ew, j);
+            const int eb = __shfl_sync(0xffffffffu, ew, j);
+            int k = binade(s) - eb;
             Tr tc;
             tc.d0 = tc.d1 = 0ull;
 #pragma unroll
@@ -911,17 +950,14 @@ __global__ void __launch_bounds__(32) pbas_k_sum_walk(LobDev D, SumWork W, int n
                     tc.d1 = b;
                 }
             }
-            if (s >= 1024.0f && k >= 0 && k < kSumNB) {
-                const unsigned long long m = (unsigned long long)((bits & 0x7fffffu) | 0x800000u);
-                const unsigned long long m2 = m + ((m & 1ull) ? tc.d1 : tc.d0);
-                if (m2 + 1ull < (1ull << 24)) {
-                    s = __uint_as_float((bits & 0xff800000u) | ((unsigned int)m2 & 0x7fffffu));
-                    continue;
-                }
-            }
-            // value by value, 32 pixels at a time staged in shared memory, every lane adding them in order
+            if (k >= 0 && k < kSumNB && tr_apply(s, tc)) continue;
             const int pEnd = min((c + 1) * kSumChunk, D.npx);
-            for (int pg = c * kSumChunk; pg < pEnd; pg += 32) {
+            for (int g = 0; g < kSumGran; ++g) {
+                const int pg = c * kSumChunk + g * 32;
+                if (pg >= pEnd) break;
+                k = binade(s) - eb;
+                if (k >= 0 && k < kSumNB && tr_apply(s, W.trw[((size_t)c * kSumGran + g) * kSumNB + k])) continue;
+                // value by value, the granule's values staged in shared memory, every lane adding them in order
                 const int p = pg + lane;
                 const int n = p < pEnd ? (int)D.badCnt[p] : 0;
                 int off = n;
@@ -1109,7 +1145,8 @@ lvbgs_status lob_setup(LobState& L, int alg, const lvbgs_params& prm, int W, int
                  oFm = take(pb * 6 * npx * 4), oMean = take(pb * 4), oBadSum = take(pb * (C == 1 ? npx * 4 : 0)),
                  oBadCnt = take(pb * npx), oBadVals = take(pb * (C == 3 ? npx * N * 4 : 0)),
                  oSumTr = take(pb * (C == 3 ? (npx + kSumChunk - 1) / kSumChunk *
-                                                  (sizeof(double) + kSumNB * sizeof(Tr) + sizeof(int)) : 0)),
+                                                  (sizeof(double) + (1 + kSumGran) * kSumNB * sizeof(Tr) + sizeof(int))
+                                            : 0)),
                  oRawPb = take(pb * npx);
     LOB_CUDA(cudaMalloc(&L.mem, off), "model allocation");
     if (!L.h_flags) LOB_CUDA(cudaHostAlloc((void**)&L.h_flags, LOB_F_WORDS * 4, cudaHostAllocDefault), "pinned allocation");
@@ -1234,7 +1271,8 @@ lvbgs_status pbas_mean_launch(const LobDev& D, int sms, cudaStream_t st, std::st
         SumWork W;
         W.chunkSum = (double*)D.sumTr;
         W.tr = (Tr*)(W.chunkSum + nChunks);
-        W.eb = (int*)(W.tr + (size_t)nChunks * kSumNB);
+        W.trw = W.tr + (size_t)nChunks * kSumNB;
+        W.eb = (int*)(W.trw + (size_t)nChunks * kSumGran * kSumNB);
         pbas_k_sum_chunks<<<nChunks, kSumChunk, 0, st>>>(D, W);
         pbas_k_sum_scan<<<1, kSumScan, 0, st>>>(D, W, nChunks);
         pbas_k_sum_tr<<<nChunks, kSumChunk, 0, st>>>(D, W);
