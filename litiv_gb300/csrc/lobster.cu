@@ -573,24 +573,43 @@ __global__ void __launch_bounds__(kThreadsL) lob_k_commit(LobDev D) {
 
 // cv::medianBlur(raw mask, k) with replicated borders: 255 where more than half of the k*k window is
 // set (:577), which becomes the last mask and the output (:578); the frame becomes the last colour
-// frame (:580)
+// frame (:580). One block per kMedTile x kMedTile tile: the raw mask with its clamped halo in shared
+// memory, the row-window counts, then the column sums of those.
+constexpr int kMedTile = 32, kMedMaxR = 15, kMedS = kMedTile + 2 * kMedMaxR;
 template <int C, bool KEEP>
 __global__ void __launch_bounds__(kThreadsL) lob_k_median(LobDev D) {
     if (!ld_vol(&D.flags[LOB_F_CONV])) return;
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= D.npx) return;
-    const int x = p % D.W, y = p / D.W, r = D.medianK / 2;
-    int cnt = 0;
-    for (int dy = -r; dy <= r; ++dy) {
-        const uint8_t* row = D.rawFG + (size_t)clampi(y + dy, 0, D.H - 1) * D.W;
-        for (int dx = -r; dx <= r; ++dx) cnt += __ldg(row + clampi(x + dx, 0, D.W - 1)) != 0;
+    __shared__ uint8_t raw[kMedS][kMedS];
+    __shared__ uint8_t rows[kMedS][kMedTile];
+    const int r = D.medianK / 2, span = kMedTile + 2 * r;
+    const int x0 = blockIdx.x * kMedTile, y0 = blockIdx.y * kMedTile, t = threadIdx.x;
+    for (int i = t; i < span * span; i += blockDim.x) {
+        const int ty = i / span, tx = i % span;
+        const int gy = clampi(y0 - r + ty, 0, D.H - 1), gx = clampi(x0 - r + tx, 0, D.W - 1);
+        raw[ty][tx] = D.rawFG[(size_t)gy * D.W + gx] != 0;
     }
-    const uint8_t m = (2 * cnt > D.medianK * D.medianK) ? 255 : 0;
-    D.maskOut[p] = m;
-    if (!KEEP) return;  // PBAS keeps neither
-    D.lastFG[p] = m;
+    __syncthreads();
+    for (int i = t; i < span * kMedTile; i += blockDim.x) {
+        const int ty = i / kMedTile, tx = i % kMedTile;
+        int c = 0;
+        for (int d = 0; d <= 2 * r; ++d) c += raw[ty][tx + d];
+        rows[ty][tx] = (uint8_t)c;
+    }
+    __syncthreads();
+    for (int i = t; i < kMedTile * kMedTile; i += blockDim.x) {
+        const int ty = i / kMedTile, tx = i % kMedTile;
+        const int x = x0 + tx, y = y0 + ty;
+        if (x >= D.W || y >= D.H) continue;
+        int cnt = 0;
+        for (int d = 0; d <= 2 * r; ++d) cnt += rows[ty + d][tx];
+        const size_t p = (size_t)y * D.W + x;
+        const uint8_t m = (2 * cnt > D.medianK * D.medianK) ? 255 : 0;
+        D.maskOut[p] = m;
+        if (!KEEP) continue;  // PBAS keeps neither
+        D.lastFG[p] = m;
 #pragma unroll
-    for (int c = 0; c < C; ++c) D.lastColor[(size_t)p * C + c] = __ldg(D.frame + (size_t)p * C + c);
+        for (int c = 0; c < C; ++c) D.lastColor[p * C + c] = __ldg(D.frame + p * C + c);
+    }
 }
 
 // initialize() (:442-457 with BackgroundSubtractionUtils.cpp:70-155, BackgroundSubtractorLBSP.cpp:21-65):
@@ -1375,11 +1394,12 @@ lvbgs_status lob_apply(LobState& L, const uint8_t* dimg, uint8_t* dmask, uint8_t
         launch<Commit>(D, nb, st);
         // LOBSTER's median blur, last mask and last colour frame; PBAS's median blur (ViBe outputs its
         // raw mask)
+        const dim3 mg((D.W + kMedTile - 1) / kMedTile, (D.H + kMedTile - 1) / kMedTile);
         if (D.alg == ALG_LOBSTER) {
-            if (C == 3) lob_k_median<3, true><<<nb, kThreadsL, 0, st>>>(D);
-            else lob_k_median<1, true><<<nb, kThreadsL, 0, st>>>(D);
+            if (C == 3) lob_k_median<3, true><<<mg, kThreadsL, 0, st>>>(D);
+            else lob_k_median<1, true><<<mg, kThreadsL, 0, st>>>(D);
         } else if (D.alg == ALG_PBAS) {
-            lob_k_median<1, false><<<nb, kThreadsL, 0, st>>>(D);
+            lob_k_median<1, false><<<mg, kThreadsL, 0, st>>>(D);
         }
         LOB_CUDA(cudaGetLastError(), "repair launch");
         if (hostMask) LOB_CUDA(cudaMemcpyAsync(hostMask, dmask, (size_t)D.npx, cudaMemcpyDeviceToHost, st), "mask download");
