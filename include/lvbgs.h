@@ -370,6 +370,21 @@ size_t lvbgs_precache_copy_loader(void* user, size_t idx, uint8_t* dst, size_t c
  * so draw k of pixel p in the i-th apply() is keyed by frame i (initialize() and refreshes before the first
  * apply() are frame 0). */
 
+/* ---- PBAS (BackgroundSubtractorPBAS, modules/video/src/BackgroundSubtractorPBAS.cpp) ----
+ * A handle created with LVBGS_ALGO_PBAS runs BackgroundSubtractorPBAS_1ch on single-channel frames
+ * (:61-273) and BackgroundSubtractorPBAS_3ch on three-channel frames (:287-496), with the header's
+ * configuration (self diffusion, no R2 acceleration, no advanced morphology; BackgroundSubtractorPBAS.hpp:41-46).
+ * lvbgs_params: min_color_dist_threshold carries nInitColorDistThreshold (30), update_rate
+ * fInitUpdateRate (16, in (0, 255]), bg_samples (35, at most 64), required_bg_samples (2); the others are
+ * unused (the median blur is 9x9 as in the reference). lvbgs_initialize takes no ROI (a non-null roi is
+ * LVBGS_UNSUPPORTED); lvbgs_apply's learning_rate is learningRateOverride: when positive it replaces
+ * ceil(T(x)), otherwise each pixel uses its own update rate (lvbgs_get_default_learning_rate returns the
+ * reference's default, -1). The frame-level mean gradient distance (20 at creation) is kept across
+ * initialize() calls, as the reference keeps m_fFormerMeanGradDist. get_background, get_size, get_scalars and
+ * the maps LVBGS_MAP_SAMPLE_COLOR, _SAMPLE_GRAD, _R (R(x)), _T (T(x)), _DMIN_LT (D(x)), _GRAD (the last
+ * frame's gradient image), _MEAN_GRAD and _ROI work as above; refresh_model, set_roi, background
+ * descriptors, batched steps and spilling are LVBGS_UNSUPPORTED. Draws are keyed like ViBe's. */
+
 /* ---- ViBe (BackgroundSubtractorViBe, modules/video/src/BackgroundSubtractorViBe.cpp) ----
  * A handle created with LVBGS_ALGO_VIBE runs BackgroundSubtractorViBe_1ch on single-channel frames
  * (:57-103) and BackgroundSubtractorViBe_3ch on three-channel frames (:112-191), with the header's
