@@ -1,13 +1,14 @@
-// SuBSENSE frame step for sm_103a: one cooperative persistent kernel per tick processes one
-// frame of every stream in the batch (a per-stream descriptor table, tiles drawn from a device
-// work queue), separated into phases by a bounded grid barrier.
+// SuBSENSE frame step for sm_103a: one tick processes one frame of every stream in the batch as a
+// sequence of ordinary launches over a per-stream descriptor table (a tile, row or segment index is
+// mapped to its stream by binary search); only the repair rounds run as one cooperative kernel whose
+// rounds are separated by a bounded grid barrier.
 //
 // Exactness of the reference's sequential raster scan (BackgroundSubtractorSuBSENSE.cpp:201-481):
 // a pixel p reads two things another pixel writes during the same frame -- its own samples, which
 // an earlier pixel's neighbour update may have overwritten (:296-299/:442-448), and the D_last /
 // raw-segmentation-ST values of its randomly chosen neighbour q, which are this frame's values when
 // q precedes p (:292-293/:438-439). Random draws are keyed by (stream, frame, pixel, draw index),
-// so they do not depend on the scan order. The kernel therefore
+// so they do not depend on the scan order. The tick therefore
 //   A  evaluates every pixel against the frame-start model and records an "intent" (decision,
 //      samples evaluated, own/neighbour sample writes, neighbour-update state),
 //   B  resolves the ghost test of each neighbour update against the values the scan would see,
@@ -17,7 +18,8 @@
 //      writes changed, until nothing changes (the dependencies follow raster order, so this is a
 //      fixed point reached in at most the length of the longest dependency chain),
 //   F  commits every sample write in raster order (last writer wins) and starts post-processing.
-// Post-processing, frame-level statistics and the automatic model reset follow in the same launch.
+// Post-processing, frame-level statistics and the automatic model reset follow in later launches of
+// the same tick.
 #include <cuda_runtime.h>
 
 #include "lbsp_device.cuh"
@@ -228,9 +230,11 @@ __device__ __forceinline__ void load_pix(const StreamDev& S, const FrameK& F, in
 }
 
 // thresholds of one evaluation from R(x) and the previous unstable flag, and the new unstable flag
+// descThr is clamped to 255: a descriptor distance is at most 16 per channel (48 summed), so every
+// comparison against the clamped value (or three times it) has the result of the unclamped one
 struct EvalThr {
     uint32_t colThr;
-    unsigned long long descThr;
+    uint32_t descThr;
     uint32_t uNew;
 };
 __device__ __forceinline__ EvalThr eval_thresholds(const StreamDev& S, float R, float RwLT, float RwST, float FnLT,
@@ -238,8 +242,9 @@ __device__ __forceinline__ EvalThr eval_thresholds(const StreamDev& S, float R, 
     EvalThr t;
     t.colThr =
         (uint32_t)__float2ull_rz(R * (float)S.minColor - (float)((uint32_t)(uOld == 0u) * (uint32_t)S.stabColorOff));
-    t.descThr = (1ull << (unsigned)__float2ull_rz(floorf(R + 0.5f))) + (unsigned long long)S.descOff +
-                (unsigned long long)uOld * S.descOff;
+    const unsigned long long descThr = (1ull << (unsigned)__float2ull_rz(floorf(R + 0.5f))) +
+                                       (unsigned long long)S.descOff + (unsigned long long)uOld * S.descOff;
+    t.descThr = descThr < 255ull ? (uint32_t)descThr : 255u;
     t.uNew = (R > 3.000f || (RwLT - FnLT) > 0.100f || (RwST - FnST) > 0.100f) ? 1u : 0u;
     return t;
 }
@@ -253,7 +258,9 @@ struct ScanSt {
 };
 
 // one sample against the pixel (the body of the sample loops, :226-250 / :357-393): whether it is a
-// good match, and its descriptor and summed distances
+// good match, and its descriptor and summed distances. The reference rejects a sample at the first
+// failed check; the verdict is the conjunction of all checks, so the three-channel form tests the
+// three colour distances first (one branch), then evaluates the three channels without branches.
 template <int C>
 __device__ __forceinline__ bool sample_match(const uint8_t* __restrict__ lut, const uint32_t (&vals)[C][4],
                                              const uint32_t (&curr)[C], const uint32_t (&intra)[C],
@@ -261,13 +268,13 @@ __device__ __forceinline__ bool sample_match(const uint8_t* __restrict__ lut, co
                                              uint32_t& sd) {
     if (C == 1) {
         const uint32_t cthr = th.colThr / 2u;
-        const uint32_t bgc = c2, bgd = (uint32_t)d;
+        const uint32_t bgc = c2, bgd = (uint32_t)d & 0xffffu;
         const uint32_t colDist = (uint32_t)abs((int)curr[0] - (int)bgc);
         if (colDist > cthr) return false;
         const uint32_t intraD = __popc(intra[0] ^ bgd);
-        const uint32_t interD = __popc(lbsp_thr(vals[0], bgc, lut[bgc]) ^ bgd);
+        const uint32_t interD = __popc((lbsp_thr_raw(vals[0], bgc, lut[bgc]) ^ bgd) & 0xffffu);
         const uint32_t descDist = (intraD + interD) / 2u;
-        if ((unsigned long long)descDist > th.descThr) return false;
+        if (descDist > th.descThr) return false;
         uint32_t sumDist = (descDist / 4u) * 15u + colDist;
         if (sumDist > 255u) sumDist = 255u;
         if (sumDist > cthr) return false;
@@ -276,24 +283,29 @@ __device__ __forceinline__ bool sample_match(const uint8_t* __restrict__ lut, co
         return true;
     } else {
         const uint32_t totColThr = th.colThr * 3u, scThr = totColThr / 2u;
-        const unsigned long long totDescThr = th.descThr * 3ull;
+        const uint32_t hiw = (uint32_t)(d >> 32), low = (uint32_t)d;
+        // bytes 0-2: the sample's colours (d bits 48-55, 56-63, c2); byte 3 repeats byte 2
+        const uint32_t bgW = __byte_perm(hiw, c2, 0x4432);
+        const uint32_t currW = curr[0] | (curr[1] << 8) | (curr[2] * 0x01010000u);
+        const uint32_t cd = __vabsdiffu4(currW, bgW);
+        const uint32_t col0 = cd & 0xffu, col1 = (cd >> 8) & 0xffu, col2 = (cd >> 16) & 0xffu;
+        if (max(max(col0, col1), col2) > scThr) return false;
+        const uint32_t col[3] = {col0, col1, col2};
+        const uint32_t bgc[3] = {bgW & 0xffu, (bgW >> 8) & 0xffu, (bgW >> 16) & 0xffu};
+        const uint32_t bgd[3] = {low & 0xffffu, low >> 16, hiw & 0xffffu};
         uint32_t totDesc = 0, totSum = 0;
+        bool bad = false;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const uint32_t bgc = c == 0 ? (uint32_t)(d >> 48) & 0xffu : c == 1 ? (uint32_t)(d >> 56) & 0xffu : c2;
-            const uint32_t bgd = (uint32_t)(d >> (16 * c)) & 0xffffu;
-            const uint32_t colDist = (uint32_t)abs((int)curr[c] - (int)bgc);
-            if (colDist > scThr) return false;
-            const uint32_t intraD = __popc(intra[c] ^ bgd);
-            const uint32_t interD = __popc(lbsp_thr(vals[c], bgc, lut[bgc]) ^ bgd);
+            const uint32_t intraD = __popc(intra[c] ^ bgd[c]);
+            const uint32_t interD = __popc((lbsp_thr_raw(vals[c], bgc[c], lut[bgc[c]]) ^ bgd[c]) & 0xffffu);
             const uint32_t descDist = (intraD + interD) / 2u;
-            uint32_t sumDist = (descDist / 2u) * 15u + colDist;
-            if (sumDist > 255u) sumDist = 255u;
-            if (sumDist > scThr) return false;
+            const uint32_t sumDist = min((descDist / 2u) * 15u + col[c], 255u);
+            bad |= sumDist > scThr;
             totDesc += descDist;
             totSum += sumDist;
         }
-        if ((unsigned long long)totDesc > totDescThr || totSum > totColThr) return false;
+        if (bad || totDesc > th.descThr * 3u || totSum > totColThr) return false;
         dd = totDesc;
         sd = totSum;
         return true;
@@ -345,7 +357,7 @@ __device__ __forceinline__ void scan_samples(const StreamDev& S, const uint8_t* 
         uint32_t c2 = cA;
         dA = dB;
         cA = cB;
-        if (s + 2 < N) {
+        if (s + 2 < sMax) {
             dB = C == 3 ? ((const uint64_t*)S.sD)[(size_t)(s + 2) * npx + p]
                         : (uint64_t)((const uint16_t*)S.sD)[(size_t)(s + 2) * npx + p];
             cB = S.sC[(size_t)(s + 2) * npx + p];
