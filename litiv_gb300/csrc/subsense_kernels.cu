@@ -336,7 +336,7 @@ __device__ __forceinline__ void scan_init(ScanSt& st) {
     st.minDesc = C == 1 ? 16u : 48u;
     st.minSum = C == 1 ? 255u : 765u;
 }
-template <int C, bool OVR>
+template <int C, bool OVR, bool REC = true>
 __device__ __forceinline__ void scan_samples(const StreamDev& S, const uint8_t* __restrict__ lut, int p,
                                              const uint32_t (&vals)[C][4], const uint32_t (&curr)[C],
                                              const uint32_t (&intra)[C], const EvalThr& th, const Ovr* ov, int nov,
@@ -380,9 +380,11 @@ __device__ __forceinline__ void scan_samples(const StreamDev& S, const uint8_t* 
             if (minSum > sd) minSum = sd;
             if (g0 < 0) {
                 g0 = s;
-                g0d = dd;
-                g0s = sd;
-            } else if (g1 < 0) {
+                if (REC) {
+                    g0d = dd;
+                    g0s = sd;
+                }
+            } else if (REC && g1 < 0) {
                 g1 = s;
                 g1d = dd;
                 g1s = sd;
@@ -718,17 +720,20 @@ __device__ void phaseA_tile(const TickParams& P, int si, const StreamDev& S, int
             const EvalThr th = eval_thresholds(S, tR, tRwLT, tRwST, tFnLT, tFnST, tU);
             ScanSt st;
             scan_init<C>(st);
-            scan_samples<C, false>(S, lut, p, vals, curr, intra, th, nullptr, 0, 0ull, kScanCap, d0, c0, d1, c1, st);
-            if (st.nGood < S.nreq && st.s < S.N) {
-                // a long scan: continued and finished by lvbgs_k_longscan over the compacted list, so
-                // that its warps hold only long scans
+            // the first good sample's index is tracked (the long-scan record keeps it), not the distances
+            // of the first two good samples (only a scan that ends unsettled records them)
+            scan_samples<C, false, false>(S, lut, p, vals, curr, intra, th, nullptr, 0, 0ull, kScanCap, d0, c0, d1,
+                                          c1, st);
+            if (st.nGood < S.nreq) {
+                // a long scan, or a scan that ended unsettled within the cap (N <= kScanCap): continued,
+                // recorded and finished by lvbgs_k_longscan over the compacted list, so that its warps
+                // hold only long scans
                 defer = true;
                 // s | nGood | first good index (255: none) | minDesc | minSum
                 scanWord = (unsigned long long)st.s | ((unsigned long long)st.nGood << 8) |
                            ((unsigned long long)(st.g0 < 0 ? 255 : st.g0) << 16) |
                            ((unsigned long long)st.minDesc << 32) | ((unsigned long long)st.minSum << 48);
             } else {
-                if (st.s >= S.N) record_scan(S, F, p, st);  // a foreground scan that ended within the cap
                 PixIn<C> in;
                 load_pix<C>(S, F, p, in);
                 intent = eval_tail<C>(S, F, x, y, p, in, curr, intra, th.uNew, st);
