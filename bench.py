@@ -25,10 +25,10 @@ sys.path.insert(0, ROOT)
 METRIC = "SuBSENSE Mpix/s: batched 64-stream vs plain 1-stream on GB300; p99 frame ms"
 # DRAM bytes (read + write) of the evaluation per pixel (lvbgs_k_eval + lvbgs_k_longscan), from an
 # ncu capture of dram__bytes_read.sum + dram__bytes_write.sum on six streams of the mix (indices
-# 52-57: four 1280x720, one of them gray, and two 1920x1080; 7,833,600 px): eval 903,555,328 +
-# 341,958,912 bytes, long scans 437,656,576 + 46,936,064 bytes. roofline.traffic scales it to a tick
+# 52-57: four 1280x720, one of them gray, and two 1920x1080; 7,833,600 px): eval 878,392,064 +
+# 393,505,536 bytes, long scans 435,291,392 + 44,822,016 bytes. roofline.traffic scales it to a tick
 # by pixels.
-EVAL_DRAM_BYTES_PER_PX = (903555328 + 341958912 + 437656576 + 46936064) / 7833600
+EVAL_DRAM_BYTES_PER_PX = (878392064 + 393505536 + 435291392 + 44822016) / 7833600
 WORKLOAD = ("subsense-mix64: 16x320x240 + 24x640x480 + 16x1280x720 + 8x1920x1080, 48 BGR + 16 gray, "
             "default parameters, synthetic seeded scenes")
 # CPU sample: 4 streams of each resolution class
@@ -92,8 +92,9 @@ class ClockSampler:
                     reasons.add(n)
         if not sm:
             return None
-        sm.sort()
-        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        srt = sorted(sm)
+        return {"sm_mhz": srt[len(srt) // 2], "sm_min_mhz": srt[0], "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(srt)}
 
 
 KERNELS = ["eval", "longscan", "resolve", "repair", "commit", "runs", "vunion", "holes", "combine",
@@ -176,7 +177,7 @@ def pawcs_run(n_frames, stream, cpu=True, channels=1):
     for leg, frames, mask in (("device", dev, dmask), ("host", host, hmask)):
         b = BackgroundSubtractorPAWCS(seed=1)
         b.initialize(frames[0].cpu().numpy())
-        ms, rounds, gpu_ev, waits = [], [], [], []
+        ms, rounds, gpu_ev, waits, parts = [], [], [], [], []
         for t in range(1, n):
             # per frame: CUDA events around the frame step (its GPU time) and the calling thread's run-queue
             # wait (time spent descheduled), to tell a slow GPU step from a descheduled host thread
@@ -192,6 +193,9 @@ def pawcs_run(n_frames, stream, cpu=True, channels=1):
             gpu_ev.append((e0, e1))
             if st != L.OK:
                 raise RuntimeError("PAWCS apply failed: %s" % lib.lvbgs_last_error(b.handle))
+            hparts = (C.c_double * 5)()
+            lib.lvbgs_debug_pawcs_host_timing(b.handle, hparts)
+            parts.append([round(v, 2) for v in hparts])
             rounds.append(b.scalars()["fixed_point_rounds"])
         b.close()
         torch.cuda.synchronize()
@@ -200,12 +204,19 @@ def pawcs_run(n_frames, stream, cpu=True, channels=1):
         med = float(np.percentile(m, 50))
         r = {"value": W * H / (m.mean() / 1e3) / 1e6, "unit": "Mpix/s", "frames_per_s": 1e3 / m.mean(),
              "ms_per_frame": float(m.mean()), "p50_frame_ms": med,
+             # the same at the median frame time: the slow frames seen in some runs are pauses of 50-150 ms
+             # inside single CUDA calls of the step (a launch, a wait or a copy; see slow_frames' parts),
+             # with no throttle reason and the calling thread not descheduled
+             "value_at_median_frame": W * H / (med / 1e3) / 1e6,
              "p99_frame_ms": float(np.percentile(m, 99)), "rounds_mean": float(np.mean(rounds)),
              "rounds_max": int(np.max(rounds)),
              # frames that took more than three times the median: index, wall ms, fixed-point rounds, GPU ms
-             # between CUDA events around the step, ms the calling thread waited on the run queue
-             "slow_frames": [[t + 1, round(v, 2), int(rounds[t]), round(gms[t], 2), round(waits[t], 2)]
-                             for t, v in enumerate(ms) if t >= 9 and v > 3 * med]}
+             # between CUDA events around the step, ms the calling thread waited on the run queue, and the
+             # host ms of the step's parts (lvbgs_debug_pawcs_host_timing: enqueue rounds, round waits,
+             # enqueue the rest, final wait, status read)
+             "slow_frames": [[t + 1, round(v, 2), int(rounds[t]), round(gms[t], 2), round(waits[t], 2), parts[t]]
+                             for t, v in enumerate(ms) if t >= 9 and v > 3 * med],
+             "median_frame_parts_ms": [round(float(np.median([q[i] for q in parts[9:]])), 3) for i in range(5)]}
         if leg == "device":
             out.update(r)
         else:
@@ -610,7 +621,8 @@ def main():
     # Pipelined (the headline): a frame precacher over the pinned host ticks (lvbgs_precacher_create_host;
     # a packet is one tick, the 64 frames back to back) uploads each tick from pinned host memory on its
     # own copy stream while the previous tick computes; each tick then runs lvbgs_batch_apply on the
-    # device copies and waits for its host masks.
+    # device copies, and the host waits for a tick's masks (two pinned mask sets, alternating) once the
+    # next tick is enqueued, so that the mask download of one tick overlaps the next tick's kernels.
     # Precaching starts inside the timed region with an empty ring, so every timed tick's copies are
     # timed. Unpipelined (e2e.unpipelined): lvbgs_batch_apply on pinned host frames, uploads on the
     # compute stream, one wait per tick.
@@ -629,8 +641,10 @@ def main():
             for i in range(n):
                 nb = int(np.prod(synth[i].shape))
                 packets[k, offs[i]:offs[i] + nb].copy_(dev_frames[i][first + k].reshape(-1))
-        hmasks = [torch.empty((s.cfg.height, s.cfg.width), dtype=torch.uint8, pin_memory=True) for s in synth]
-        hm = [m.data_ptr() for m in hmasks]
+        hmasks = [[torch.empty((s.cfg.height, s.cfg.width), dtype=torch.uint8, pin_memory=True) for s in synth]
+                  for _ in range(2)]
+        hm2 = [[m.data_ptr() for m in ms] for ms in hmasks]
+        hm = hm2[0]
         pc = C.c_void_p()
         check(lib.lvbgs_precacher_create_host(C.c_void_p(packets.data_ptr()), pkt_bytes, e2e_steps, local,
                                               C.byref(pc)), None)
@@ -645,6 +659,7 @@ def main():
         check(lib.lvbgs_precacher_stop(pc), None)
         torch.cuda.synchronize()
         dp, hpp, sz = C.c_void_p(), C.c_void_p(), C.c_size_t()
+        done = [torch.cuda.Event() for _ in range(e2e_steps)]
         t0 = time.perf_counter()
         check(lib.lvbgs_precacher_start(pc, 4 * pkt_bytes), None)
         for k in range(e2e_steps):
@@ -652,10 +667,13 @@ def main():
             for i in range(n):
                 fr[i].image = dp.value + offs[i]
                 fr[i].stride = 0
-                fr[i].fgmask = hm[i]
+                fr[i].fgmask = hm2[k % 2][i]
                 fr[i].learning_rate = 0.0
             check(lib.lvbgs_batch_apply(hse, fr, n, sptr), hse[0])
-            check(lib.lvbgs_batch_wait(hse, n, sptr), hse[0])  # masks are on the host after the wait
+            done[k].record(stream)
+            if k > 0:
+                done[k - 1].synchronize()  # the previous tick's masks are on the host
+        check(lib.lvbgs_batch_wait(hse, n, sptr), hse[0])  # the last tick's masks, and the device status
         el = time.perf_counter() - t0
         lib.lvbgs_precacher_destroy(pc)
         for b in subs_e:
@@ -683,8 +701,8 @@ def main():
         e2e = {"value": px_step * e2e_steps / el / 1e6, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": px_step, "ms_per_step": el / e2e_steps * 1e3,
                "note": "pinned host frames -> frame precacher (uploads on a copy stream overlapping the previous "
-                       "tick, started inside the timed region) -> lvbgs_batch_apply -> host masks; wall clock "
-                       "incl. one wait per tick",
+                       "tick, started inside the timed region) -> lvbgs_batch_apply -> host masks (two pinned sets; "
+                       "the host waits for each tick's masks after enqueueing the next tick); wall clock",
                "unpipelined": {"value": px_step * e2e_steps / el_u / 1e6, "ms_per_step": el_u / e2e_steps * 1e3,
                                "note": "pinned host frames -> lvbgs_batch_apply (uploads on the compute "
                                        "stream) -> host masks"}}
@@ -717,13 +735,14 @@ def main():
         for b in subs_p:
             b.close()
 
-    serve = None
-    if rank == 0 and args.serving_seconds > 0:
-        serve = serving_run(args.serving_seconds, args.pawcs_lanes)
     pawcs = None
     if rank == 0 and args.pawcs_frames > 0:
-        pawcs = pawcs_run(args.pawcs_frames, stream, cpu=not args.no_cpu_baseline)
-        pawcs["bgr"] = pawcs_run(min(args.pawcs_frames, 100), stream, cpu=not args.no_cpu_baseline, channels=3)
+        with ClockSampler(local) as pclk:
+            pawcs = pawcs_run(args.pawcs_frames, stream, cpu=not args.no_cpu_baseline)
+        pawcs["clocks"] = pclk.summary()
+        with ClockSampler(local) as pclk3:
+            pawcs["bgr"] = pawcs_run(min(args.pawcs_frames, 100), stream, cpu=not args.no_cpu_baseline, channels=3)
+        pawcs["bgr"]["clocks"] = pclk3.summary()
     singles = None
     if rank == 0 and args.single_frames > 0:
         singles = {"config0": single_stream_run(0, args.single_frames, stream, cpu=not args.no_cpu_baseline,
@@ -734,6 +753,15 @@ def main():
     models = {}
     if rank == 0 and args.lobster_frames > 0:
         models = sample_models_run(args.lobster_frames, stream, cpu=not args.no_cpu_baseline)
+
+    # the serving workload runs last: it creates and frees hundreds of streams (tens of GB of device
+    # memory), and legs run right after it showed pauses of 50-150 ms inside single CUDA calls
+    serve = None
+    if rank == 0 and args.serving_seconds > 0:
+        with ClockSampler(local) as sclk:
+            serve = serving_run(args.serving_seconds, args.pawcs_lanes)
+        if serve is not None:
+            serve["clocks"] = sclk.summary()
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

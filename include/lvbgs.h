@@ -96,10 +96,16 @@ lvbgs_status lvbgs_apply(lvbgs_handle h, const uint8_t* image, size_t stride, ui
                          double learning_rate, void* cuda_stream);
 
 /* Batched frame step: one frame of each of the n streams (handles on the same device, all
- * initialized) in one sequence of phase kernels over a per-stream descriptor table (15 launches
- * per group; large batches run as up to four concurrent groups, see lvbgs_set_batch_groups). Results are identical to n separate
- * lvbgs_apply calls. Enqueued on cuda_stream; lvbgs_batch_wait() waits and reports device errors.
- * Host buffers referenced by `frames` must stay valid until the wait returns. */
+ * initialized). The SuBSENSE streams run in one sequence of phase kernels over a per-stream
+ * descriptor table (15 launches per group; large batches run as up to four concurrent groups, see
+ * lvbgs_set_batch_groups), enqueued on cuda_stream. The PAWCS streams' frame steps run on their
+ * handles' own CUDA streams, forked from cuda_stream and joined back into it, all in flight together;
+ * a PAWCS step waits on the host for its fixed-point rounds, so the call returns once every PAWCS
+ * step is enqueued to its end (their device errors are returned by this call). Other algorithms are
+ * rejected (LVBGS_UNSUPPORTED). Results are identical to n separate lvbgs_apply calls.
+ * lvbgs_batch_wait() waits and reports the SuBSENSE part's device errors. Host buffers referenced
+ * by `frames` must stay valid until the wait returns. No reference counterpart (the reference runs
+ * one subtractor per sequence). */
 /* How lvbgs_batch_apply runs large batches (>= 8 streams and >= 4 Mi pixels): G in 2..4 (default 4)
  * splits them into up to G groups of about equal pixels (at least 4 streams each), run on the
  * caller's stream and on further streams of the first handle (forked and joined with events), so
@@ -268,6 +274,11 @@ int lvbgs_debug_repair_phases(lvbgs_handle h, int batched, double* out_us, int m
  *                                frame needs more */
 enum { LVBGS_FAULT_NONE = 0, LVBGS_FAULT_BARRIER_TIMEOUT = 1, LVBGS_FAULT_REPAIR_LIMIT = 2, LVBGS_FAULT_PAWCS_ROUNDS = 3 };
 lvbgs_status lvbgs_debug_inject_fault(lvbgs_handle h, int kind);
+/* Host time (ms) of the last PAWCS frame step's parts (inspection; no reference counterpart):
+ * [0] enqueueing the fixed-point rounds (the first batch and any further ones), [1] the waits for
+ * the rounds, [2] enqueueing the rest of the frame step (with the camera-motion decision's wait every
+ * 8 or 16 frames), [3] the final wait, [4] the status read-back. */
+lvbgs_status lvbgs_debug_pawcs_host_timing(lvbgs_handle h, double* out_ms);
 
 /* ---- PAWCS (BackgroundSubtractorPAWCS, modules/video/src/BackgroundSubtractorPAWCS.cpp) ----
  * A handle created with LVBGS_ALGO_PAWCS runs PAWCS on single-channel (:608-934) and three-channel

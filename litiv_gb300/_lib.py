@@ -152,6 +152,7 @@ SIGNATURES = {
     "lvbgs_debug_tick_profile": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int]),
     "lvbgs_debug_repair_phases": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_int]),
     "lvbgs_debug_inject_fault": (C.c_int, [C.c_void_p, C.c_int]),
+    "lvbgs_debug_pawcs_host_timing": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "lvbgs_classif_accumulate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                            C.POINTER(C.c_uint64), C.c_int, C.c_void_p]),
     "lvbgs_classif_metrics": (C.c_int, [C.POINTER(C.c_uint64), C.POINTER(C.c_double)]),

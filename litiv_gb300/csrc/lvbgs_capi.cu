@@ -3,6 +3,8 @@
 // host/device frames, and the cooperative launch of the tick kernel for one or many streams.
 #include <cuda_runtime.h>
 
+#include <chrono>
+
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -157,6 +159,16 @@ struct Workspace {
 
 }  // namespace
 
+// a PAWCS frame step in flight: its stream, launch parameters and the stage of its host waits (0: the
+// fixed-point rounds, 1: the camera-motion decision, 2: the end of the frame)
+struct PwStep {
+    cudaStream_t st = nullptr;
+    PwParams P{}, PR{};
+    int enq = 0, maxRounds = 64, stage = 0;
+    uint8_t* mask = nullptr;
+    bool devMask = false, active = false;
+};
+
 struct lvbgs_ctx {
     lvbgs_algo algo;
     lvbgs_params prm;
@@ -191,6 +203,9 @@ struct lvbgs_ctx {
     unsigned long long pw_frames = 0;
     unsigned long long pw_offset = 1000;
     int pw_rounds_last = 0;
+    double pw_host_ms[5] = {0, 0, 0, 0, 0};  // last PAWCS frame: lvbgs_debug_pawcs_host_timing
+    PwStep pws;  // the PAWCS frame step in flight (pw_begin / pw_advance)
+    cudaEvent_t evPw = nullptr;  // fork / join of the handle's PAWCS step in a batch
     int dbg_fault = 0;  // one-shot fault injection of the next frame step (lvbgs_debug_inject_fault)
     LobState* lob = nullptr;  // LOBSTER and ViBe (LVBGS_ALGO_LOBSTER / _VIBE): the stream's device state
 };
@@ -883,90 +898,115 @@ lvbgs_status lob_initialize(lvbgs_ctx* h, const uint8_t* img, int W, int H, int 
     return LVBGS_OK;
 }
 
-// one PAWCS frame step: local passes to the raster-order fixed point, then commit, global words,
-// post-processing and the frame level
-lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* mask, double lr, cudaStream_t st) {
+// PAWCS frame steps are resumable: pw_begin enqueues a frame's first batch of fixed-point rounds and
+// returns; pw_advance waits for the step's latest read-back and enqueues what follows (more rounds, the
+// camera-motion decision, the rest of the frame), until the step is done. lvbgs_apply runs one step to
+// the end; a batch keeps the steps of several PAWCS streams in flight on their own CUDA streams.
+double pw_ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// ordered compaction: mode 0 lists the critical global items, mode 1 the word weight contributions,
+// mode 2 the neighbour-update loops
+void pw_compact(lvbgs_ctx* h, const PwParams& Pc, int mode, cudaStream_t st) {
+    const int cblocks = (int)((h->npx + kPwCompactBlk - 1) / kPwCompactBlk);
+    pw_k_compact_count<<<cblocks, 256, 0, st>>>(Pc, mode);
+    const int ncat = mode == 1 ? h->pd.G : 1;
+    pw_k_compact_offsets<<<1, 32 * std::min(ncat, 32), 0, st>>>(Pc, ncat);
+    pw_k_compact_scatter<<<cblocks, 256, 0, st>>>(Pc, mode);
+}
+
+// enqueues fixed-point rounds enq .. enq+n-1 (each ends with pw_k_round_end; once a round finds no dirty
+// pixel every later kernel of the rounds returns at once, PW_ROUND_GUARD) and the read-back of the
+// converged flag and round count
+lvbgs_status pw_enqueue_rounds(lvbgs_ctx* h, int n) {
+    PwStep& w = h->pws;
+    const cudaStream_t st = w.st;
+    const dim3 blk(kThreads);
+    const int tiles = h->sd.nTiles;
+    const int cblocks = (int)((h->npx + kPwCompactBlk - 1) / kPwCompactBlk);
+    for (int r = 0; r < n && w.enq < w.maxRounds; ++r, ++w.enq) {
+        w.PR.round = w.enq;
+        const PwParams& P = w.PR;
+        if (h->C == 3) {
+            // three channels: the local pass applies the earlier updaters' loops itself
+            pw3_k_local<<<tiles, blk, 0, st>>>(P);
+            pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
+            pw_compact(h, P, 0, st);
+            pw3_k_gscan_seg<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
+            pw3_k_gscan_walk<<<1, 32, 0, st>>>(P);
+            pw3_k_gscan_fix<<<(int)((h->npx + 255) / 256), 256, 0, st>>>(P);
+            pw3_k_gscan_fix_walked<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
+            pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
+            pw_k_nbr<<<tiles, blk, 0, st>>>(P);
+            LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 4, st), "flag reset");
+            pw3_k_dirty<<<tiles, blk, 0, st>>>(P);
+        } else {
+            pw_k_local<<<tiles, blk, 0, st>>>(P);
+            pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
+            pw_compact(h, P, 0, st);
+            pw3_k_gscan_seg<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
+            pw3_k_gscan_walk<<<1, 32, 0, st>>>(P);
+            pw3_k_gscan_fix<<<(int)((h->npx + 255) / 256), 256, 0, st>>>(P);
+            pw3_k_gscan_fix_walked<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
+            pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
+            pw_k_nbr<<<tiles, blk, 0, st>>>(P);
+            pw_compact(h, P, 2, st);
+            pw_k_nbr_loops<<<std::max(1, std::min(cblocks * 4, 1216)), 256, 0, st>>>(P);
+            pw_k_replace<<<tiles, blk, 0, st>>>(P);
+            LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 4, st), "flag reset");
+            pw_k_dirty<<<tiles, blk, 0, st>>>(P);
+        }
+        pw_k_round_end<<<1, 1, 0, st>>>(P);
+    }
+    LV_CUDA(h, cudaGetLastError(), "PAWCS round launch");
+    LV_CUDA(h, cudaMemcpyAsync(h->h_flags + 3, h->d_flags + 3, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, st),
+            "flag read-back");
+    return LVBGS_OK;
+}
+
+// one PAWCS frame step: local passes to the raster-order fixed point (enqueued ahead, as many rounds as
+// the previous frame needed, then one at a time), then commit, global words, post-processing and the
+// frame level. Host time of the parts goes to pw_host_ms (lvbgs_debug_pawcs_host_timing).
+lvbgs_status pw_begin(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* mask, double lr, cudaStream_t st) {
+    const std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    for (double& v : h->pw_host_ms) v = 0.0;
+    PwStep& w = h->pws;
+    w = PwStep();
+    w.st = st;
     const uint8_t* dimg = nullptr;
     lvbgs_status s = stage_frame(h, img, stride, st, &dimg);
     if (s != LVBGS_OK) return s;
-    const bool devMask = mask && is_device_ptr(mask);
+    w.mask = mask;
+    w.devMask = mask && is_device_ptr(mask);
     h->sd.frame = dimg;
-    h->sd.maskOut = devMask ? mask : h->d_mask;
+    h->sd.maskOut = w.devMask ? mask : h->d_mask;
     if ((s = pw_upload_desc(h, st)) != LVBGS_OK) return s;
-    PwParams P = pw_params(h, lr);
-    const dim3 blk(kThreads);
-    const int tiles = h->sd.nTiles;
-    const int cur = (int)(h->pw_frames & 1ull), nxt = cur ^ 1;
+    w.P = pw_params(h, lr);
     LV_CUDA(h, cudaMemsetAsync(h->pd.repBefore, 0xff, h->npx * 4, st), "scratch reset");
     LV_CUDA(h, cudaMemsetAsync(h->d_work, 0, sizeof(TickWork), st), "scratch reset");
-    const int cblocks = (int)((h->npx + kPwCompactBlk - 1) / kPwCompactBlk);
-    // ordered compaction: mode 0 lists the critical global items, mode 1 the word weight contributions
-    auto compact = [&](const PwParams& Pc, int mode) {
-        pw_k_compact_count<<<cblocks, 256, 0, st>>>(Pc, mode);
-        const int ncat = mode == 1 ? h->pd.G : 1;
-        pw_k_compact_offsets<<<1, 32 * std::min(ncat, 32), 0, st>>>(Pc, ncat);
-        pw_k_compact_scatter<<<cblocks, 256, 0, st>>>(Pc, mode);
-    };
-    const bool c3 = h->C == 3;
-    // The fixed point runs on the device: the rounds are enqueued ahead (as many as the previous frame
-    // needed, then one at a time), each ends with pw_k_round_end, and once a round finds no dirty pixel
-    // every later kernel of the rounds returns at once (PW_ROUND_GUARD), so the host waits once per
-    // batch of rounds instead of once per round.
-    const int maxRounds = h->dbg_fault == LVBGS_FAULT_PAWCS_ROUNDS ? 1 : 64;
+    w.maxRounds = h->dbg_fault == LVBGS_FAULT_PAWCS_ROUNDS ? 1 : 64;
     h->dbg_fault = 0;
     LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 5 * sizeof(unsigned int), st), "flag reset");
-    PwParams PR = P;
-    PR.conv = h->d_flags + 3;
-    int enq = 0, chunk = std::max(1, std::min(h->pw_rounds_last, maxRounds)), rounds = 0;
-    for (;;) {
-        for (int r = 0; r < chunk && enq < maxRounds; ++r, ++enq) {
-            PR.round = enq;
-            const PwParams& P = PR;
-            if (c3) {
-                // three channels: the local pass applies the earlier updaters' loops itself
-                pw3_k_local<<<tiles, blk, 0, st>>>(P);
-                pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
-                compact(P, 0);
-                pw3_k_gscan_seg<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
-                pw3_k_gscan_walk<<<1, 32, 0, st>>>(P);
-                pw3_k_gscan_fix<<<(int)((h->npx + 255) / 256), 256, 0, st>>>(P);
-                pw3_k_gscan_fix_walked<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
-                pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
-                pw_k_nbr<<<tiles, blk, 0, st>>>(P);
-                LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 4, st), "flag reset");
-                pw3_k_dirty<<<tiles, blk, 0, st>>>(P);
-            } else {
-                pw_k_local<<<tiles, blk, 0, st>>>(P);
-                pw_k_illum<<<(h->H + 7) / 8, 256, 0, st>>>(P);
-                compact(P, 0);
-                pw3_k_gscan_seg<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
-                pw3_k_gscan_walk<<<1, 32, 0, st>>>(P);
-                pw3_k_gscan_fix<<<(int)((h->npx + 255) / 256), 256, 0, st>>>(P);
-                pw3_k_gscan_fix_walked<<<(int)((h->npx + 4 * 512 - 1) / (4 * 512)), 128, 0, st>>>(P);
-                pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 0);
-                pw_k_nbr<<<tiles, blk, 0, st>>>(P);
-                compact(P, 2);
-                pw_k_nbr_loops<<<std::max(1, std::min(cblocks * 4, 1216)), 256, 0, st>>>(P);
-                pw_k_replace<<<tiles, blk, 0, st>>>(P);
-                LV_CUDA(h, cudaMemsetAsync(h->d_flags, 0, 4, st), "flag reset");
-                pw_k_dirty<<<tiles, blk, 0, st>>>(P);
-            }
-            pw_k_round_end<<<1, 1, 0, st>>>(P);
-        }
-        LV_CUDA(h, cudaGetLastError(), "PAWCS round launch");
-        LV_CUDA(h, cudaMemcpyAsync(h->h_flags + 3, h->d_flags + 3, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, st),
-                "flag read-back");
-        LV_CUDA(h, cudaStreamSynchronize(st), "PAWCS rounds");
-        if (h->h_flags[3]) {
-            rounds = (int)h->h_flags[4];
-            break;
-        }
-        if (enq >= maxRounds)
-            return fail(h, LVBGS_DEVICE_ERROR, "PAWCS raster-order fixed point did not converge in the round limit");
-        chunk = 1;
-    }
-    const int round = rounds - 1;
-    h->pw_rounds_last = round + 1;
+    w.PR = w.P;
+    w.PR.conv = h->d_flags + 3;
+    w.enq = 0;
+    s = pw_enqueue_rounds(h, std::max(1, std::min(h->pw_rounds_last, w.maxRounds)));
+    w.stage = 0;
+    w.active = s == LVBGS_OK;
+    h->pw_host_ms[0] += pw_ms_since(t0);
+    return s;
+}
+
+// the rest of the frame after the fixed point, up to the camera-motion decision (enqueued with its
+// read-back on frames that take it: returns true) or to the end (returns false)
+lvbgs_status pw_enqueue_tail_a(lvbgs_ctx* h, bool& motion) {
+    PwStep& w = h->pws;
+    const cudaStream_t st = w.st;
+    const PwParams& P = w.P;
+    const dim3 blk(kThreads);
+    const int tiles = h->sd.nTiles;
+    const bool c3 = h->C == 3;
     if (c3) {
         pw3_k_later<<<tiles, blk, 0, st>>>(P);
         pw3_k_commit<<<tiles, blk, 0, st>>>(P);
@@ -974,7 +1014,7 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
         pw_k_commit<<<tiles, blk, 0, st>>>(P);
     }
     pw_k_cells<<<(P.totalCells + 255) / 256, 256, 0, st>>>(P, 1);
-    compact(P, 1);
+    pw_compact(h, P, 1, st);
     pw_k_weights<<<kPwMaxGlobal, 256, 0, st>>>(P);
     pw_k_gw_recalc<<<kPwMaxGlobal, 256, 0, st>>>(P);
     pw_k_gw_decay<<<dim3(64, kPwMaxGlobal), 256, 0, st>>>(P, h->d_rowsum);
@@ -1006,36 +1046,119 @@ lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
     }
     pw_k_epilogue<<<1, 256, 0, st>>>(P);
     const uint32_t t = (uint32_t)(h->pw_frames + 1);
-    if (nds > 0 && t % kPwBootWin == 0) {
+    motion = nds > 0 && t % kPwBootWin == 0;
+    if (motion) {
         // camera-motion comparison (:1480-1501): the host waits for the decision, which may switch the
         // local word weight offset and run refreshModel(1, 1, true)
+        const int nxt = (int)((h->pw_frames & 1ull) ^ 1ull);
         if (c3) pw3_k_motion_bg<<<(nds + 255) / 256, 256, 0, st>>>(P, nxt);
         else pw_k_motion_bg<<<(nds + 255) / 256, 256, 0, st>>>(P, nxt);
         pw_k_motion_decide<<<1, 32, 0, st>>>(P);
         LV_CUDA(h, cudaGetLastError(), "PAWCS camera-motion launch");
         LV_CUDA(h, cudaMemcpyAsync(h->h_flags + 1, h->d_flags + 1, 8, cudaMemcpyDeviceToHost, st), "flag read-back");
-        LV_CUDA(h, cudaStreamSynchronize(st), "PAWCS camera-motion decision");
-        if (h->h_flags[1]) {
-            h->pw_offset = h->h_flags[2];
-            if ((s = pw_refresh(h, t, nxt, 1, 1.0f, 1, 0, 1, st)) != LVBGS_OK) return s;
-        }
     }
+    return LVBGS_OK;
+}
+
+// the end of the frame: the automatic model reset and the mask download
+lvbgs_status pw_enqueue_tail_b(lvbgs_ctx* h) {
+    PwStep& w = h->pws;
+    const cudaStream_t st = w.st;
+    const PwParams& P = w.P;
+    const uint32_t t = (uint32_t)(h->pw_frames + 1);
+    const int nxt = (int)((h->pw_frames & 1ull) ^ 1ull);
     pw_k_reset_decide<<<1, 32, 0, st>>>(P);
     // automatic model reset (:1503-1508): refreshModel(offset/8, 0, true) and T(x) := 1
-    if ((s = pw_refresh(h, t, nxt, (int)(h->pw_offset / 8), 0.0f, 1, 1, 1, st)) != LVBGS_OK) return s;
+    lvbgs_status s = pw_refresh(h, t, nxt, (int)(h->pw_offset / 8), 0.0f, 1, 1, 1, st);
+    if (s != LVBGS_OK) return s;
     pw_k_reset_T<<<256, 256, 0, st>>>(h->pd, nxt);
     pw_k_close<<<1, 32, 0, st>>>(P);
     LV_CUDA(h, cudaGetLastError(), "PAWCS frame step launch");
-    if (mask && !devMask) LV_CUDA(h, cudaMemcpyAsync(mask, h->d_mask, h->npx, cudaMemcpyDeviceToHost, st), "mask download");
-    LV_CUDA(h, cudaStreamSynchronize(st), "PAWCS frame step");
-    (void)cur;
+    if (w.mask && !w.devMask)
+        LV_CUDA(h, cudaMemcpyAsync(w.mask, h->d_mask, h->npx, cudaMemcpyDeviceToHost, st), "mask download");
+    return LVBGS_OK;
+}
+
+// waits for the step's latest read-back and enqueues what follows; done is set when the step is over
+lvbgs_status pw_advance(lvbgs_ctx* h, bool& done) {
+    PwStep& w = h->pws;
+    done = false;
+    if (!w.active) {
+        done = true;
+        return fail(h, LVBGS_BAD_ARG, "no PAWCS frame step in flight");
+    }
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    auto finish = [&](lvbgs_status s) {
+        w.active = false;
+        done = true;
+        return s;
+    };
+    cudaError_t e = cudaStreamSynchronize(w.st);
+    h->pw_host_ms[w.stage == 0 ? 1 : w.stage == 1 ? 2 : 3] += pw_ms_since(t0);
+    if (e != cudaSuccess) return finish(cuda_fail(h, e, w.stage == 0 ? "PAWCS rounds" : "PAWCS frame step"));
+    t0 = std::chrono::steady_clock::now();
+    lvbgs_status s = LVBGS_OK;
+    if (w.stage == 0) {
+        if (!h->h_flags[3]) {
+            if (w.enq >= w.maxRounds)
+                return finish(fail(h, LVBGS_DEVICE_ERROR, "PAWCS raster-order fixed point did not converge in the round limit"));
+            s = pw_enqueue_rounds(h, 1);
+            h->pw_host_ms[0] += pw_ms_since(t0);
+            return s == LVBGS_OK ? s : finish(s);
+        }
+        h->pw_rounds_last = (int)h->h_flags[4];
+        bool motion = false;
+        if ((s = pw_enqueue_tail_a(h, motion)) != LVBGS_OK) return finish(s);
+        if (motion) {
+            w.stage = 1;
+            h->pw_host_ms[2] += pw_ms_since(t0);
+            return LVBGS_OK;
+        }
+        s = pw_enqueue_tail_b(h);
+        w.stage = 2;
+        h->pw_host_ms[2] += pw_ms_since(t0);
+        return s == LVBGS_OK ? s : finish(s);
+    }
+    if (w.stage == 1) {
+        if (h->h_flags[1]) {
+            h->pw_offset = h->h_flags[2];
+            const uint32_t t = (uint32_t)(h->pw_frames + 1);
+            const int nxt = (int)((h->pw_frames & 1ull) ^ 1ull);
+            if ((s = pw_refresh(h, t, nxt, 1, 1.0f, 1, 0, 1, w.st)) != LVBGS_OK) return finish(s);
+        }
+        s = pw_enqueue_tail_b(h);
+        w.stage = 2;
+        h->pw_host_ms[2] += pw_ms_since(t0);
+        return s == LVBGS_OK ? s : finish(s);
+    }
+    // stage 2: the frame step is over
     h->pw_frames += 1;
-    TickWork w;
-    LV_CUDA(h, cudaMemcpy(&w, h->d_work, sizeof(TickWork), cudaMemcpyDeviceToHost), "status read-back");
-    return status_from_work(h, w);
+    TickWork tw;
+    e = cudaMemcpy(&tw, h->d_work, sizeof(TickWork), cudaMemcpyDeviceToHost);
+    h->pw_host_ms[4] += pw_ms_since(t0);
+    if (e != cudaSuccess) return finish(cuda_fail(h, e, "status read-back"));
+    return finish(status_from_work(h, tw));
+}
+
+lvbgs_status pw_apply(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* mask, double lr, cudaStream_t st) {
+    lvbgs_status s = pw_begin(h, img, stride, mask, lr, st);
+    if (s != LVBGS_OK) {
+        h->pws.active = false;
+        return s;
+    }
+    bool done = false;
+    while (!done) s = pw_advance(h, done);
+    return s;
 }
 
 }  // namespace
+
+lvbgs_status lvbgs_debug_pawcs_host_timing(lvbgs_handle h, double* out_ms) {
+    if (!h || !out_ms) return fail(nullptr, LVBGS_BAD_ARG, "null argument");
+    if (h->algo != LVBGS_ALGO_PAWCS) return fail(h, LVBGS_BAD_ARG, "not a PAWCS handle");
+    for (int i = 0; i < 5; ++i) out_ms[i] = h->pw_host_ms[i];
+    return LVBGS_OK;
+}
 
 lvbgs_status lvbgs_debug_inject_fault(lvbgs_handle h, int kind) {
     if (!h) return fail(nullptr, LVBGS_BAD_ARG, "null handle");
@@ -1209,6 +1332,7 @@ lvbgs_status lvbgs_destroy(lvbgs_handle h) {
         if (h->evJoin[g]) cudaEventDestroy(h->evJoin[g]);
     }
     if (h->evFork) cudaEventDestroy(h->evFork);
+    if (h->evPw) cudaEventDestroy(h->evPw);
     if (h->stream) cudaStreamDestroy(h->stream);
     if (h->lob) {
         lob_release(*h->lob);
@@ -1367,7 +1491,7 @@ lvbgs_status lvbgs_apply(lvbgs_handle h, const uint8_t* img, size_t stride, uint
 
 namespace {
 // checks a batch (initialized handles on one device, each at most once)
-lvbgs_status check_batch(const lvbgs_handle* hs, const lvbgs_frame* frames, int n) {
+lvbgs_status check_batch(const lvbgs_handle* hs, const lvbgs_frame* frames, int n, bool allowPawcs) {
     if (!hs || !frames || n <= 0) return fail(nullptr, LVBGS_BAD_ARG, "empty batch");
     lvbgs_handle lead = hs[0];
     for (int i = 0; i < n; ++i) {
@@ -1375,8 +1499,10 @@ lvbgs_status check_batch(const lvbgs_handle* hs, const lvbgs_frame* frames, int 
         if (s != LVBGS_OK) return s;
         if (hs[i]->device != lead->device) return fail(lead, LVBGS_BAD_ARG, "batched handles must share one device");
         if (!frames[i].image) return fail(hs[i], LVBGS_BAD_ARG, "null input image");
-        if (hs[i]->algo != LVBGS_ALGO_SUBSENSE)
-            return fail(hs[i], LVBGS_UNSUPPORTED, "batched frame steps are implemented for SuBSENSE streams");
+        if (hs[i]->algo != LVBGS_ALGO_SUBSENSE && !(allowPawcs && hs[i]->algo == LVBGS_ALGO_PAWCS))
+            return fail(hs[i], LVBGS_UNSUPPORTED,
+                        allowPawcs ? "batched frame steps are implemented for SuBSENSE and PAWCS streams"
+                                   : "batch contexts run SuBSENSE streams");
         for (int j = 0; j < i; ++j)
             if (hs[j] == hs[i]) return fail(lead, LVBGS_BAD_ARG, "a handle appears twice in the batch");
     }
@@ -1458,9 +1584,11 @@ lvbgs_status lvbgs_set_batch_groups(int groups) {
     return LVBGS_OK;
 }
 
-lvbgs_status lvbgs_batch_apply(const lvbgs_handle* hs, const lvbgs_frame* frames, int n, void* cuda_stream) {
-    lvbgs_status s = check_batch(hs, frames, n);
-    if (s != LVBGS_OK) return s;
+namespace {
+// the SuBSENSE part of a batch: one sequence of phase kernels over its streams (split into concurrent
+// groups when large)
+lvbgs_status batch_apply_subsense(const lvbgs_handle* hs, const lvbgs_frame* frames, int n, void* cuda_stream) {
+    lvbgs_status s = LVBGS_OK;
     lvbgs_handle lead = hs[0];
     cudaSetDevice(lead->device);
     cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : lead->stream;
@@ -1496,12 +1624,84 @@ lvbgs_status lvbgs_batch_apply(const lvbgs_handle* hs, const lvbgs_frame* frames
     return LVBGS_OK;
 }
 
-lvbgs_status lvbgs_batch_wait(const lvbgs_handle* hs, int n, void* cuda_stream) {
-    if (!hs || n <= 0) return fail(nullptr, LVBGS_BAD_ARG, "empty batch");
+}  // namespace
+
+// A batch may mix SuBSENSE and PAWCS streams. The SuBSENSE streams run as one batched frame step on the
+// caller's stream; each PAWCS stream's frame step runs on the handle's own stream (forked from the
+// caller's and joined back into it), all of them in flight together: the host waits for their
+// fixed-point rounds in turn, so the call returns once every PAWCS step is enqueued to its end.
+lvbgs_status lvbgs_batch_apply(const lvbgs_handle* hs, const lvbgs_frame* frames, int n, void* cuda_stream) {
+    lvbgs_status s = check_batch(hs, frames, n, true);
+    if (s != LVBGS_OK) return s;
+    std::vector<lvbgs_handle> sub, pw;
+    std::vector<lvbgs_frame> fsub, fpw;
+    for (int i = 0; i < n; ++i) {
+        if (hs[i]->algo == LVBGS_ALGO_PAWCS) {
+            pw.push_back(hs[i]);
+            fpw.push_back(frames[i]);
+        } else {
+            sub.push_back(hs[i]);
+            fsub.push_back(frames[i]);
+        }
+    }
+    if (pw.empty()) return batch_apply_subsense(hs, frames, n, cuda_stream);
     lvbgs_handle lead = hs[0];
     cudaSetDevice(lead->device);
     cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : lead->stream;
-    LV_CUDA(lead, cudaStreamSynchronize(st), "batched frame step");
+    for (lvbgs_handle h : pw)
+        if (!h->evPw) LV_CUDA(h, cudaEventCreateWithFlags(&h->evPw, cudaEventDisableTiming), "event creation");
+    // fork: every PAWCS step starts after the work the caller enqueued on st
+    LV_CUDA(lead, cudaEventRecord(pw[0]->evPw, st), "fork");
+    for (lvbgs_handle h : pw) LV_CUDA(h, cudaStreamWaitEvent(h->stream, pw[0]->evPw, 0), "fork");
+    std::vector<char> live(pw.size(), 0);
+    lvbgs_status first = LVBGS_OK;
+    for (size_t i = 0; i < pw.size(); ++i) {
+        s = pw_begin(pw[i], fpw[i].image, fpw[i].stride, fpw[i].fgmask, fpw[i].learning_rate, pw[i]->stream);
+        if (s == LVBGS_OK) live[i] = 1;
+        else {
+            pw[i]->pws.active = false;
+            if (first == LVBGS_OK) first = s;
+        }
+    }
+    if (!sub.empty() && first == LVBGS_OK) first = batch_apply_subsense(sub.data(), fsub.data(), (int)sub.size(), st);
+    // the PAWCS steps advance in turn until each is over (every step in flight is run to its end, also
+    // after an error, so that no handle is left with a step in flight)
+    for (bool any = true; any;) {
+        any = false;
+        for (size_t i = 0; i < pw.size(); ++i) {
+            if (!live[i]) continue;
+            bool done = false;
+            s = pw_advance(pw[i], done);
+            if (done) {
+                live[i] = 0;
+                if (s != LVBGS_OK && first == LVBGS_OK) first = s;
+            } else {
+                any = true;
+            }
+        }
+    }
+    // join: the caller's stream waits for every PAWCS step (they are over; this orders later work)
+    for (lvbgs_handle h : pw) {
+        LV_CUDA(h, cudaEventRecord(h->evPw, h->stream), "join");
+        LV_CUDA(lead, cudaStreamWaitEvent(st, h->evPw, 0), "join");
+    }
+    return first;
+}
+
+lvbgs_status lvbgs_batch_wait(const lvbgs_handle* handles, int n_all, void* cuda_stream) {
+    if (!handles || n_all <= 0) return fail(nullptr, LVBGS_BAD_ARG, "empty batch");
+    lvbgs_handle lead0 = handles[0];
+    cudaSetDevice(lead0->device);
+    cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : lead0->stream;
+    LV_CUDA(lead0, cudaStreamSynchronize(st), "batched frame step");
+    // the device status of the SuBSENSE part (the PAWCS steps reported theirs in lvbgs_batch_apply)
+    std::vector<lvbgs_handle> sub;
+    for (int i = 0; i < n_all; ++i)
+        if (handles[i] && handles[i]->algo != LVBGS_ALGO_PAWCS) sub.push_back(handles[i]);
+    if (sub.empty()) return LVBGS_OK;
+    const lvbgs_handle* hs = sub.data();
+    const int n = (int)sub.size();
+    lvbgs_handle lead = hs[0];
     std::vector<std::vector<int>> groups;
     const int G = split_batch(hs, n, groups);
     if (G == 1) return read_work_status(lead, lead->batchWs);
@@ -1605,7 +1805,7 @@ lvbgs_status lvbgs_batch_set_repair_share(lvbgs_batch b, int divisor) {
 lvbgs_status lvbgs_batch_submit(lvbgs_batch b, const lvbgs_handle* hs, const lvbgs_frame* frames, int n,
                                 void* cuda_stream, uint64_t* ticket) {
     if (!b || !ticket) return fail(nullptr, LVBGS_BAD_ARG, "null argument");
-    lvbgs_status s = check_batch(hs, frames, n);
+    lvbgs_status s = check_batch(hs, frames, n, false);
     if (s != LVBGS_OK) return s;
     lvbgs_handle lead = hs[0];
     if (lead->device != b->device) return fail(lead, LVBGS_BAD_ARG, "batch context and handles are on different devices");

@@ -8,7 +8,7 @@ operation order without fused multiply-adds. Every compared frame checks the who
 import numpy as np
 import pytest
 
-from litiv_gb300 import BackgroundSubtractorPAWCS, LvException, SyntheticStream
+from litiv_gb300 import BackgroundSubtractorPAWCS, BackgroundSubtractorSuBSENSE, LvException, SyntheticStream, batch_apply
 from oracle import pyoracle
 
 pytestmark = pytest.mark.gpu
@@ -336,3 +336,41 @@ def test_spill_restore_is_transparent(channels):
         assert np.array_equal(a.apply(frames[t]), ora.apply(frames[t])), "frame %d" % t
     bad = compare_state(a, ora)
     assert not bad, "; ".join(bad)
+
+
+@pytest.mark.parametrize("with_subsense", [False, True])
+def test_batched_pawcs_streams_equal_streams_alone(with_subsense):
+    """lvbgs_batch_apply with PAWCS streams (one BGR, one gray), alone or beside a SuBSENSE stream: the
+    PAWCS steps run in flight together on their handles' own streams and the SuBSENSE one as a batched
+    step; every mask equals the oracle's stream run alone, also across a spill / restore of a PAWCS
+    stream between two batches, and the PAWCS models end identical to the oracle's."""
+    sp = [SyntheticStream(0, 0, 51, width=128, height=96, channels=3), SyntheticStream(0, 0, 52, width=96, height=64,
+                                                                                       channels=1)]
+    fp = [[s.render(t) for t in range(12)] for s in sp]
+    pw = [BackgroundSubtractorPAWCS(seed=7), BackgroundSubtractorPAWCS(seed=8)]
+    opw = [pyoracle.OraclePAWCS(seed=7), pyoracle.OraclePAWCS(seed=8)]
+    for g, o, f in zip(pw, opw, fp):
+        g.initialize(f[0])
+        o.initialize(f[0])
+    subs, osub, fs = [], [], []
+    if with_subsense:
+        ss = SyntheticStream(0, 0, 53, width=160, height=120, channels=3)
+        fs = [ss.render(t) for t in range(12)]
+        subs = [BackgroundSubtractorSuBSENSE(seed=9)]
+        osub = [pyoracle.OracleSuBSENSE(seed=9)]
+        subs[0].initialize(fs[0])
+        osub[0].initialize(fs[0])
+    for t in range(1, 12):
+        if t == 6:
+            buf = bytearray(pw[0].state_bytes())
+            pw[0].spill(buf)
+            pw[0].restore(buf)
+        handles = [pw[0]] + subs + [pw[1]]
+        images = [fp[0][t]] + [f[t] for f in ([fs] if subs else [])] + [fp[1][t]]
+        masks = batch_apply(handles, images)
+        want = [opw[0].apply(fp[0][t])] + [o.apply(fs[t]) for o in osub] + [opw[1].apply(fp[1][t])]
+        for i, (m, w) in enumerate(zip(masks, want)):
+            assert np.array_equal(m, w), "frame %d, batch entry %d: mask differs at %d px" % (t, i, int((m != w).sum()))
+    for g, o in zip(pw, opw):
+        bad = compare_state(g, o)
+        assert not bad, "; ".join(bad)
