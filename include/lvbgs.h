@@ -91,7 +91,10 @@ lvbgs_status lvbgs_initialize(lvbgs_handle h, const uint8_t* image, int width, i
 
 /* IIBackgroundSubtractor::apply(img, fgmask, learningRateOverride) (BackgroundSubtractorSuBSENSE.cpp:188-612).
  * Enqueues the frame step on `cuda_stream` (a cudaStream_t, NULL = the per-handle stream) and
- * waits for it; fgmask receives the post-processed foreground mask. */
+ * waits for it; fgmask receives the post-processed foreground mask. image and fgmask may be device
+ * or host memory. A SuBSENSE or PAWCS mask in page-locked host memory (cudaHostAlloc /
+ * cudaHostRegister, mapped at the same address) is written by the post-processing kernel itself
+ * over the host link; a mask in pageable host memory is copied from a device staging buffer. */
 lvbgs_status lvbgs_apply(lvbgs_handle h, const uint8_t* image, size_t stride, uint8_t* fgmask,
                          double learning_rate, void* cuda_stream);
 

@@ -237,6 +237,20 @@ bool is_device_ptr(const void* p) {
     }
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
+// a mask destination the kernels can write themselves: device or managed memory, or page-locked host
+// memory registered with CUDA and mapped at the same address (unified addressing), which the
+// post-processing kernel then writes over the host link while it runs, with no copy after the frame
+// step; pageable host memory is written by a copy from a device staging buffer
+bool mask_writable_by_device(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeHost && a.devicePointer == p;
+}
 
 // layout of one stream's device block
 struct Layout {
@@ -978,7 +992,7 @@ lvbgs_status pw_begin(lvbgs_ctx* h, const uint8_t* img, size_t stride, uint8_t* 
     lvbgs_status s = stage_frame(h, img, stride, st, &dimg);
     if (s != LVBGS_OK) return s;
     w.mask = mask;
-    w.devMask = mask && is_device_ptr(mask);
+    w.devMask = mask_writable_by_device(mask);
     h->sd.frame = dimg;
     h->sd.maskOut = w.devMask ? mask : h->d_mask;
     if ((s = pw_upload_desc(h, st)) != LVBGS_OK) return s;
@@ -1477,7 +1491,7 @@ lvbgs_status lvbgs_apply(lvbgs_handle h, const uint8_t* img, size_t stride, uint
     }
     const uint8_t* dimg = nullptr;
     if ((s = stage_frame(h, img, stride, st, &dimg)) != LVBGS_OK) return s;
-    const bool devMask = mask && is_device_ptr(mask);
+    const bool devMask = mask_writable_by_device(mask);
     h->ws.h_streams.assign(1, h->sd);
     StreamDev& S = h->ws.h_streams[0];
     S.frame = dimg;
@@ -1518,7 +1532,7 @@ lvbgs_status prepare_batch(const lvbgs_handle* hs, const lvbgs_frame* frames, in
         out[i] = h->sd;
         StreamDev& S = out[i];
         S.frame = dimg;
-        const bool devMask = frames[i].fgmask && is_device_ptr(frames[i].fgmask);
+        const bool devMask = mask_writable_by_device(frames[i].fgmask);
         S.maskOut = devMask ? frames[i].fgmask : h->d_mask;
         set_lr(S, frames[i].learning_rate);
     }
@@ -1527,7 +1541,7 @@ lvbgs_status prepare_batch(const lvbgs_handle* hs, const lvbgs_frame* frames, in
 // enqueues the copies of the masks that go to host memory
 lvbgs_status download_masks(const lvbgs_handle* hs, const lvbgs_frame* frames, int n, cudaStream_t st) {
     for (int i = 0; i < n; ++i)
-        if (frames[i].fgmask && !is_device_ptr(frames[i].fgmask))
+        if (frames[i].fgmask && !mask_writable_by_device(frames[i].fgmask))
             LV_CUDA(hs[0], cudaMemcpyAsync(frames[i].fgmask, hs[i]->d_mask, hs[i]->npx, cudaMemcpyDeviceToHost, st),
                     "mask download");
     return LVBGS_OK;

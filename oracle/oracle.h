@@ -257,10 +257,11 @@ double orun_lobster_streams(int n_streams, const uint8_t* const* frames, const i
  * per-sequence lv::WorkerPool of apps/changedet/src/main.cpp:148-154).
  * frames[i] holds n_frames[i] frames of widths[i]*heights[i]*channels[i] bytes;
  * the first frame initializes, the others are applied. Returns the wall time in
- * seconds of the apply phase (after every instance is initialized); masks may be NULL. */
+ * seconds of the apply phase after the first warm_frames applied frames of every
+ * instance (untimed); masks may be NULL. */
 double orun_streams(int n_streams, const uint8_t* const* frames, const int* n_frames,
                     const int* widths, const int* heights, const int* channels,
-                    const uint64_t* seeds, int n_threads, uint8_t* const* last_masks);
+                    const uint64_t* seeds, int n_threads, uint8_t* const* last_masks, int warm_frames);
 
 /* CPU baseline for PAWCS: as orun_streams, timing the apply phase only (after every instance is
  * initialized) */

@@ -210,7 +210,7 @@ def lib():
         L.orun_streams.restype = C.c_double
         L.orun_streams.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                    C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_uint64), C.c_int,
-                                   C.POINTER(C.c_void_p)]
+                                   C.POINTER(C.c_void_p), C.c_int]
         L.opawcs_default_params.argtypes = [C.POINTER(PParams)]
         L.opawcs_create.restype = C.c_void_p
         L.opawcs_create.argtypes = [C.POINTER(PParams)]
@@ -705,8 +705,9 @@ def philox(ctr, key):
     return list(o)
 
 
-def run_streams(frames_list, seeds, n_threads):
-    """CPU baseline: frames_list[i] is a uint8 array [F, H, W(, C)]; returns wall seconds."""
+def run_streams(frames_list, seeds, n_threads, warm_frames=0):
+    """CPU baseline: frames_list[i] is a uint8 array [F, H, W(, C)]; returns the wall seconds of the
+    applied frames after the first warm_frames (applied untimed)."""
     n = len(frames_list)
     arrs = [np.ascontiguousarray(f) for f in frames_list]
     ptrs = (C.c_void_p * n)(*[a.ctypes.data for a in arrs])
@@ -715,7 +716,7 @@ def run_streams(frames_list, seeds, n_threads):
     hs = (C.c_int * n)(*[a.shape[1] for a in arrs])
     cs = (C.c_int * n)(*[(a.shape[3] if a.ndim == 4 else 1) for a in arrs])
     sd = (C.c_uint64 * n)(*seeds)
-    return lib().orun_streams(n, ptrs, nf, ws, hs, cs, sd, int(n_threads), None)
+    return lib().orun_streams(n, ptrs, nf, ws, hs, cs, sd, int(n_threads), None, int(warm_frames))
 
 
 def run_pawcs_streams(frames_list, seeds, n_threads):

@@ -17,12 +17,14 @@ typedef struct {
     const int *nf, *w, *h, *c;
     const uint64_t* seeds;
     uint8_t* const* last_masks;
+    int warm;  /* applied frames per stream before the timed ones (SuBSENSE runner) */
     int next;
     pthread_mutex_t mu;
 } job_t;
 
-/* Thread k initializes streams k, k+T, ... then, after a barrier, applies their frames; the returned
- * time covers the apply phase only (the per-frame throughput, without the model initialization). */
+/* Thread k initializes streams k, k+T, ... and applies their first `warm` frames, then, after a
+ * barrier, applies the rest; the returned time covers those frames only (the per-frame throughput of
+ * the model after its first frames, without the initialization). */
 typedef struct {
     job_t* j;
     int tid, nth;
@@ -42,13 +44,17 @@ static void* sworker(void* arg) {
         p.seed = j->seeds[i];
         os[m] = osub_create(&p);
         osub_initialize(os[m], j->frames[i], j->w[i], j->h[i], j->c[i], NULL);
+        const size_t fb = (size_t)j->w[i] * j->h[i] * j->c[i];
+        uint8_t* mask = (uint8_t*)malloc((size_t)j->w[i] * j->h[i]);
+        for (int f = 1; f <= j->warm && f < j->nf[i]; ++f) osub_apply(os[m], j->frames[i] + (size_t)f * fb, mask, 0.0);
+        free(mask);
     }
     pthread_barrier_wait(pj->bar);
     m = 0;
     for (int i = pj->tid; i < j->n; i += pj->nth, ++m) {
         const size_t fb = (size_t)j->w[i] * j->h[i] * j->c[i];
         uint8_t* mask = (uint8_t*)malloc((size_t)j->w[i] * j->h[i]);
-        for (int f = 1; f < j->nf[i]; ++f) osub_apply(os[m], j->frames[i] + (size_t)f * fb, mask, 0.0);
+        for (int f = 1 + j->warm; f < j->nf[i]; ++f) osub_apply(os[m], j->frames[i] + (size_t)f * fb, mask, 0.0);
         if (j->last_masks && j->last_masks[i])
             for (size_t k = 0; k < (size_t)j->w[i] * j->h[i]; ++k) j->last_masks[i][k] = mask[k];
         free(mask);
@@ -61,8 +67,8 @@ static void* sworker(void* arg) {
 
 double orun_streams(int n_streams, const uint8_t* const* frames, const int* n_frames, const int* widths,
                     const int* heights, const int* channels, const uint64_t* seeds, int n_threads,
-                    uint8_t* const* last_masks) {
-    job_t j = {n_streams, frames, n_frames, widths, heights, channels, seeds, last_masks, 0,
+                    uint8_t* const* last_masks, int warm_frames) {
+    job_t j = {n_streams, frames, n_frames, widths, heights, channels, seeds, last_masks, warm_frames < 0 ? 0 : warm_frames, 0,
                PTHREAD_MUTEX_INITIALIZER};
     if (n_threads < 1) n_threads = 1;
     pthread_barrier_t bar;
@@ -118,7 +124,7 @@ static void* pworker(void* arg) {
 
 double orun_pawcs_streams(int n_streams, const uint8_t* const* frames, const int* n_frames, const int* widths,
                           const int* heights, const int* channels, const uint64_t* seeds, int n_threads) {
-    job_t j = {n_streams, frames, n_frames, widths, heights, channels, seeds, NULL, 0, PTHREAD_MUTEX_INITIALIZER};
+    job_t j = {n_streams, frames, n_frames, widths, heights, channels, seeds, NULL, 0, 0, PTHREAD_MUTEX_INITIALIZER};
     if (n_threads < 1) n_threads = 1;
     pthread_barrier_t bar;
     pthread_barrier_init(&bar, NULL, (unsigned)n_threads + 1);
@@ -172,7 +178,7 @@ static void* lworker(void* arg) {
 
 double orun_lobster_streams(int n_streams, const uint8_t* const* frames, const int* n_frames, const int* widths,
                             const int* heights, const int* channels, const uint64_t* seeds, int n_threads) {
-    job_t j = {n_streams, frames, n_frames, widths, heights, channels, seeds, NULL, 0, PTHREAD_MUTEX_INITIALIZER};
+    job_t j = {n_streams, frames, n_frames, widths, heights, channels, seeds, NULL, 0, 0, PTHREAD_MUTEX_INITIALIZER};
     if (n_threads < 1) n_threads = 1;
     pthread_barrier_t bar;
     pthread_barrier_init(&bar, NULL, (unsigned)n_threads + 1);

@@ -284,3 +284,39 @@ def test_non_integral_down_sampling_bitexact(W, H):
     area-weighted mean, :568): masks and every map, including the down-sampled means."""
     s = SyntheticStream(0, seed=42, width=W, height=H)
     run_pair(frames_of(s, 16), seed=14, check_every=3)
+
+
+def test_page_locked_host_masks_are_written_by_the_kernels():
+    """Masks into page-locked host memory (written by the post-processing kernel itself over the host
+    link, no copy after the step) equal the masks written into pageable memory (device staging buffer
+    and a copy), for a batch of streams, a single SuBSENSE stream and a PAWCS stream."""
+    torch = pytest.importorskip("torch")
+    from litiv_gb300 import BackgroundSubtractorPAWCS
+    streams = [SyntheticStream(0, seed=61), SyntheticStream(0, seed=62, channels=1, width=160, height=120)]
+    frames = [frames_of(s, 8) for s in streams]
+    runs = []
+    for pinned in (False, True):
+        subs = [BackgroundSubtractorSuBSENSE(seed=70 + i) for i in range(2)]
+        single = BackgroundSubtractorSuBSENSE(seed=80)
+        pw = BackgroundSubtractorPAWCS(seed=81)
+        for g, f in zip(subs, frames):
+            g.initialize(f[0])
+        single.initialize(frames[0][0])
+        pw.initialize(frames[1][0])
+
+        def buf(shape):
+            if pinned:
+                return torch.empty(shape, dtype=torch.uint8).pin_memory().numpy()
+            return np.empty(shape, np.uint8)
+
+        out = []
+        for t in range(1, 8):
+            masks = batch_apply(subs, [f[t] for f in frames], masks=[buf(f[t].shape[:2]) for f in frames])
+            m1 = single.apply(frames[0][t], fgmask=buf(frames[0][t].shape[:2]))
+            m2 = pw.apply(frames[1][t], fgmask=buf(frames[1][t].shape[:2]))
+            out.append([m.copy() for m in masks] + [m1.copy(), m2.copy()])
+        runs.append(out)
+    for t, (a, b) in enumerate(zip(*runs), start=1):
+        for i, (ma, mb) in enumerate(zip(a, b)):
+            assert np.array_equal(ma, mb), "frame %d, output %d differs between pageable and page-locked masks" % (t, i)
+    assert any(m.any() for o in runs[1] for m in o), "no foreground at all: the comparison says nothing"
