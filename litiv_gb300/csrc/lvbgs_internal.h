@@ -52,14 +52,10 @@ LV_HD void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
             k0 += kWeyl0;
             k1 += kWeyl1;
         }
-#if defined(__CUDA_ARCH__)
-        const uint32_t hi0 = __umulhi(kPhilox0, x0), lo0 = kPhilox0 * x0;
-        const uint32_t hi1 = __umulhi(kPhilox1, x2), lo1 = kPhilox1 * x2;
-#else
+        // one 32x32 -> 64-bit multiply each (a single wide multiply-add on the device)
         const uint64_t p0 = (uint64_t)kPhilox0 * x0, p1 = (uint64_t)kPhilox1 * x2;
         const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
         const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
-#endif
         const uint32_t n0 = hi1 ^ x1 ^ k0, n2 = hi0 ^ x3 ^ k1;
         x0 = n0;
         x1 = lo1;

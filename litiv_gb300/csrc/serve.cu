@@ -295,8 +295,9 @@ void housekeeping(lvserve_ctx* s) {
             if (x->closing && x->q.empty() && !x->inFlight) {
                 // PAWCS handles are destroyed on a PAWCS lane, so that the device-wide wait of freeing
                 // their memory does not hold the ticks back
+                // (a PAWCS stream still waiting for its handle, S_INIT, is left to the lanes)
                 if (x->algo == LVBGS_ALGO_PAWCS && x->h) x->laneDestroy = true;
-                else closing.push_back(x);
+                else if (!(x->algo == LVBGS_ALGO_PAWCS && x->state == S_INIT)) closing.push_back(x);
             } else if (x->state == S_SPILLED && !x->q.empty()) {
                 restore.push_back(x);
             }
@@ -474,15 +475,18 @@ void pawcs_lane(lvserve_ctx* s) {
             for (auto& kv : s->streams) {
                 SStream* y = kv.second.get();
                 if (y->algo != LVBGS_ALGO_PAWCS || y->inFlight) continue;
-                if (y->laneDestroy || (y->state == S_INIT && !y->closing)) {
+                // an admitted stream waiting for its handle is set up also when it was closed meanwhile
+                // (its queued frames still run; with none queued it just goes)
+                if (y->laneDestroy || y->state == S_INIT) {
                     job = y;
                     break;
                 }
             }
             if (job) {
                 job->inFlight = true;
+                const bool drop = job->laneDestroy || (job->closing && job->q.empty());
                 lk.unlock();
-                if (job->laneDestroy) {
+                if (drop) {
                     destroy_stream(s, job);
                 } else {
                     lvbgs_handle h = nullptr;

@@ -638,6 +638,16 @@ __device__ __forceinline__ void gather_taps(const uint8_t* base, int rowStride, 
     }
 }
 
+// the evaluation's shared-memory frame tile: byte 0 of a tile row buffer is kTileDelta<C> bytes before
+// the frame byte (x0-2)*C - 2 of the tile's leftmost tap, which puts it on a 16-byte boundary of the
+// frame row (x0 = 32 * tile column: (96k - 8) - 8 for C = 3, (32k - 4) - 12 for C = 1); kTileRW<C> is
+// the row stride, a multiple of 16 that covers the (kTileW + 4) * C + 2 bytes of taps after the delta
+template <int C>
+constexpr int kTileDelta = C == 3 ? 8 : 12;
+template <int C>
+constexpr int kTileRW = (kTileDelta<C> + (kTileW + 2 * kBorder) * C + 2 + 15) / 16 * 16;
+static_assert(kTileW == 32 && kBorder == 2, "the tile deltas assume 32-pixel tile columns and a 2-pixel border");
+
 // ------------------------------------------------------------------------------------------
 // phase A: evaluate every pixel of a tile against the frame-start model
 // ------------------------------------------------------------------------------------------
@@ -645,11 +655,12 @@ template <int C>
 __device__ void phaseA_tile(const TickParams& P, int si, const StreamDev& S, int lt, uint8_t* smem) {
     const int tx = lt % S.tilesX, ty = lt / S.tilesX;
     const int x0 = tx * kTileW, y0 = ty * kTileH;
-    // The tile holds rows y0-2 .. y0+9 of the frame; row r of the tile starts at frame byte
-    // (x0-2)*C - 2, which is 4-byte aligned for C in {1,3} and x0 a multiple of 32, so it is filled
-    // with aligned 32-bit loads when the frame rows are 4-byte aligned.
-    constexpr int NWORDS = ((kTileW + 2 * kBorder) * C + 2 + 3) / 4;  // words per tile row
-    constexpr int RW = NWORDS * 4;                                     // tile row stride (bytes)
+    // The tile holds rows y0-2 .. y0+9 of the frame. The taps of the tile's pixels span frame bytes
+    // b0 = (x0-2)*C - 2 .. b0 + (kTileW+4)*C + 1 of a row; a tile row buffer starts kTileDelta<C> bytes
+    // before b0, at a 16-byte boundary of the row (x0 is a multiple of 32), so it is filled with
+    // aligned 128-bit loads when the frame rows are 16-byte aligned (else 32-bit words, or bytes).
+    constexpr int RW = kTileRW<C>;  // tile row stride (bytes)
+    constexpr int NCH = RW / 16;    // 16-byte chunks per tile row
     constexpr int RH = kTileH + 2 * kBorder;
     const FrameK F = frame_consts(S);
     const int lx = threadIdx.x % kTileW, ly = threadIdx.x / kTileW;
@@ -683,23 +694,35 @@ __device__ void phaseA_tile(const TickParams& P, int si, const StreamDev& S, int
     uint8_t* lut = smem + RW * RH;
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = S.ctl->lut[i];
     const long rowBytes = (long)S.W * C;
-    const long b0 = (long)(x0 - kBorder) * C - 2;  // frame byte of tile column 0
+    const long ws = (long)(x0 - kBorder) * C - 2 - kTileDelta<C>;  // frame byte of a tile row buffer's byte 0
+    const bool vecPath = (rowBytes & 15) == 0 && (((uintptr_t)S.frame) & 15) == 0;
     const bool wordPath = (rowBytes & 3) == 0 && (((uintptr_t)S.frame) & 3) == 0;
-    for (int i = threadIdx.x; i < NWORDS * RH; i += blockDim.x) {
-        const int r = i / NWORDS, wi = i % NWORDS;
+    for (int i = threadIdx.x; i < NCH * RH; i += blockDim.x) {
+        const int r = i / NCH, ci = i % NCH;
         const int gy = y0 - kBorder + r;
-        const long b = b0 + 4 * wi;
-        uint32_t v = 0;
+        const long b = ws + 16 * ci;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
         if (gy >= 0 && gy < S.H) {
             const uint8_t* row = S.frame + (size_t)gy * rowBytes;
-            if (wordPath && b >= 0 && b + 4 <= rowBytes) {
-                v = __ldg((const uint32_t*)(row + b));
+            if (vecPath && b >= 0 && b + 16 <= rowBytes) {
+                v = __ldg((const uint4*)(row + b));
             } else {
-                for (int k = 0; k < 4; ++k)
-                    if (b + k >= 0 && b + k < rowBytes) v |= (uint32_t)__ldg(row + b + k) << (8 * k);
+                uint32_t w[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const long bw = b + 4 * j;
+                    w[j] = 0;
+                    if (wordPath && bw >= 0 && bw + 4 <= rowBytes) {
+                        w[j] = __ldg((const uint32_t*)(row + bw));
+                    } else {
+                        for (int k = 0; k < 4; ++k)
+                            if (bw + k >= 0 && bw + k < rowBytes) w[j] |= (uint32_t)__ldg(row + bw + k) << (8 * k);
+                    }
+                }
+                v = make_uint4(w[0], w[1], w[2], w[3]);
             }
         }
-        *(uint32_t*)(tile + r * RW + 4 * wi) = v;
+        *(uint4*)(tile + r * RW + 16 * ci) = v;
     }
     __syncthreads();
     int nz = 0;
@@ -708,7 +731,7 @@ __device__ void phaseA_tile(const TickParams& P, int si, const StreamDev& S, int
     if (inFrame) {
         uint32_t intent = 0;
         if (active) {
-            const uint8_t* base = tile + (ly + kBorder) * RW + (lx + kBorder) * C + 2;
+            const uint8_t* base = tile + (ly + kBorder) * RW + kTileDelta<C> + (lx + kBorder) * C + 2;
             uint32_t vals[C][4], curr[C], intra[C];
 #pragma unroll
             for (int c = 0; c < C; ++c) {
@@ -1676,7 +1699,7 @@ __device__ void refresh_pixel(const StreamDev& S, int p, uint32_t frame, int sta
     const int lt = t - S.tileBase;
 
 extern "C" __global__ void __launch_bounds__(kThreads, 5) lvbgs_k_eval(TickParams P) {
-    __shared__ __align__(16) uint8_t smem[((((kTileW + 4) * 3 + 2 + 3) / 4) * 4) * (kTileH + 4) + 256];
+    __shared__ __align__(16) uint8_t smem[kTileRW<3> * (kTileH + 2 * kBorder) + 256];
     LV_TILE_KERNEL_PROLOGUE
     if (S.C == 3) phaseA_tile<3>(P, si, S, lt, smem);
     else phaseA_tile<1>(P, si, S, lt, smem);
