@@ -390,6 +390,24 @@ def sample_models_run(n_frames, stream, cpu=True):
             for algo in SAMPLE_MODELS}
 
 
+def serving_subprocess(seconds, pawcs_lanes=1):
+    """serving_run in a fresh child process (bench.py --serving-only); its JSON object, or a note of the
+    failure."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--serving-only", "--serving-seconds", str(seconds),
+           "--pawcs-lanes", str(pawcs_lanes)]
+    try:
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True,
+                           timeout=max(120.0, 6.0 * seconds + 60.0))
+    except subprocess.TimeoutExpired:
+        return {"status": -1, "note": "the serving run did not finish in time"}
+    lines = [ln for ln in r.stdout.strip().splitlines() if ln.startswith("{")]
+    if r.returncode != 0 or not lines:
+        return {"status": -1, "note": "the serving run failed (exit %d): %s" % (r.returncode, r.stderr.strip()[-300:])}
+    out = json.loads(lines[-1])
+    out["process"] = "child process of its own"
+    return out
+
+
 def serving_run(seconds, pawcs_lanes=1):
     """The serving workload (Poisson arrivals of 4 streams/s up to 256 live, lives U[10, 60] s, 30 fps,
     320x240/640x480/1280x720/1920x1080 with p = .3/.3/.3/.1, a quarter single-channel), started from its
@@ -745,6 +763,16 @@ def main():
         for b in subs_p:
             b.close()
 
+    # the serving workload runs in a child process of its own: it creates and frees hundreds of streams
+    # (tens of GB of device memory and GBs of pinned host frames), and it is sensitive to the host
+    # state the other legs leave (pinned buffers, caches); legs run right after it in the same process
+    # showed pauses of 50-150 ms inside single CUDA calls
+    serve = None
+    if rank == 0 and args.serving_seconds > 0:
+        with ClockSampler(local) as sclk:
+            serve = serving_subprocess(args.serving_seconds, args.pawcs_lanes)
+        if serve is not None:
+            serve["clocks"] = sclk.summary()
     pawcs = None
     if rank == 0 and args.pawcs_frames > 0:
         with ClockSampler(local) as pclk:
@@ -763,15 +791,6 @@ def main():
     models = {}
     if rank == 0 and args.lobster_frames > 0:
         models = sample_models_run(args.lobster_frames, stream, cpu=not args.no_cpu_baseline)
-
-    # the serving workload runs last: it creates and frees hundreds of streams (tens of GB of device
-    # memory), and legs run right after it showed pauses of 50-150 ms inside single CUDA calls
-    serve = None
-    if rank == 0 and args.serving_seconds > 0:
-        with ClockSampler(local) as sclk:
-            serve = serving_run(args.serving_seconds, args.pawcs_lanes)
-        if serve is not None:
-            serve["clocks"] = sclk.summary()
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
