@@ -1161,13 +1161,15 @@ __device__ void phaseF_tile(const TickParams& P, const StreamDev& S, int lt, uin
         auto commit_write = [&](int p, int s) {
             const uint16_t* ldn = S.lastDesc + (size_t)F.nxt * npx * C + (size_t)p * C;
             if (C == 3) {
-                const uint64_t d = (uint64_t)__ldcg(&ldn[0]) | ((uint64_t)__ldcg(&ldn[1]) << 16) |
-                                   ((uint64_t)__ldcg(&ldn[2]) << 32) | ((uint64_t)__ldg(S.frame + (size_t)p * 3) << 48) |
+                // the writers' descriptors were written by earlier kernels of the tick and are not
+                // written by this one, so they are read through L1 (neighbouring writers share lines)
+                const uint64_t d = (uint64_t)__ldg(&ldn[0]) | ((uint64_t)__ldg(&ldn[1]) << 16) |
+                                   ((uint64_t)__ldg(&ldn[2]) << 32) | ((uint64_t)__ldg(S.frame + (size_t)p * 3) << 48) |
                                    ((uint64_t)__ldg(S.frame + (size_t)p * 3 + 1) << 56);
                 ((uint64_t*)S.sD)[(size_t)s * npx + q] = d;
                 S.sC[(size_t)s * npx + q] = __ldg(S.frame + (size_t)p * 3 + 2);
             } else {
-                ((uint16_t*)S.sD)[(size_t)s * npx + q] = __ldcg(&ldn[0]);
+                ((uint16_t*)S.sD)[(size_t)s * npx + q] = __ldg(&ldn[0]);
                 S.sC[(size_t)s * npx + q] = __ldg(S.frame + p);
             }
             ++nw;
