@@ -466,7 +466,8 @@ def map_view(name, raw, W, H, Cc, N):
 
 
 def batch_apply(subtractors, images, masks=None, learning_rates=None, wait=True):
-    """One frame of each stream in one batched frame step over all of them (lvbgs_batch_apply)."""
+    """One frame of each stream in one call (lvbgs_batch_apply): the SuBSENSE streams in one batched
+    frame step, the PAWCS streams' frame steps in flight together on their own CUDA streams."""
     n = len(subtractors)
     if masks is None:
         masks = [np.empty(s._need_init()[:2], np.uint8) for s in subtractors]
